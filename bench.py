@@ -1,0 +1,341 @@
+"""Benchmark of the path-tracing-with-MIS hot path on one GB300.
+
+Workload: the 1M-triangle procedural scene -- 200 seeded FBM-displaced
+icospheres (5,120 triangles each) in a 20^3 box over a ground plane, each
+with one of the 7 materials, constant environment 0.5 plus 4 emissive
+spheres -- rendered at 1920x1080, 64 samples per pixel, max depth 8, NEE +
+MIS, FP32, PCG32 streams.  One step = one full 64-spp frame (132.7 M samples).
+
+  value      Msamples/s, device-timed with CUDA events around each step's
+             pt_render call (scene and BVH resident in HBM; L2 flushed with a
+             256 MiB write between steps, outside the timed events)
+  e2e        the same metric through the C-ABI with host buffers: per step
+             the camera + launch parameters go in from pinned host memory and
+             the accumulated frame comes back to pinned host memory
+  roofline   closest-hit traversal kernel: algorithmic bytes (wide nodes +
+             primitive records fetched + 32 B ray + 16 B hit, from the
+             traversal counters of an identical untimed render) / its
+             CUDA-event-timed duration, against the measured HBM bandwidth
+  cpu_baseline  the CPU oracle (C++ restatement of the reference integrator)
+             on all host cores, on a bounded pixel subset of the same frame
+
+`--impl reference` times the reference's CPU implementation of the path
+(the oracle port; the reference's OptiX/DX12 build cannot run here) on the
+same workload and metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOAD = "1M-triangle displaced-icosphere field (200 x 5120 tris + 8192 ground tris + 4 sphere lights), " \
+           "1920x1080, 64 spp, max depth 8, NEE+MIS, 7 materials"
+METRIC = "Msamples/s at 1080p depth 8 (1 GB300)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--width", type=int, default=1920)
+    ap.add_argument("--height", type=int, default=1080)
+    ap.add_argument("--spp", type=int, default=64)
+    ap.add_argument("--depth", type=int, default=8)
+    ap.add_argument("--instances", type=int, default=200)
+    ap.add_argument("--bvh-width", type=int, default=4)
+    ap.add_argument("--max-leaf", type=int, default=4)
+    ap.add_argument("--smem-nodes", type=int, default=0)
+    ap.add_argument("--block-size", type=int, default=0)
+    ap.add_argument("--wave-spp", type=int, default=0)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def committed_traffic():
+    """DRAM bytes per launch of the closest-hit kernel from the committed ncu summary."""
+    p = ROOT / "profiles" / "extend_traffic.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except Exception:
+            return None
+    return None
+
+
+class ClockSampler:
+    FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown," \
+             "clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.tmp = None
+
+    def start(self):
+        try:
+            self.tmp = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.device), "-lms", "200"], stdout=self.tmp,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.tmp.flush()
+        rows = [l.split(",") for l in Path(self.tmp.name).read_text().strip().splitlines() if l.strip()]
+        os.unlink(self.tmp.name)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(scene, spp_seed0: int, seconds: float, depth: int):
+    """The oracle on all host cores over growing pixel subsets until about
+    `seconds` of work have been timed; Msamples/s."""
+    import numpy as np
+
+    import oracle
+    from pupiloptixlab_gb300 import abi
+    o = oracle.OracleScene(scene, bvh=True)
+    npix = scene.width * scene.height
+    threads = os.cpu_count() or 1
+    p = abi.RenderParams(spp=1, max_depth=depth, seed=spp_seed0, sample_cnt=0, accumulate=1, rng=abi.RNG_PCG32)
+    stride = 257
+    done, t_total = 0, 0.0
+    offset = 0
+    while t_total < seconds and offset < stride:
+        px = np.arange(offset, npix, stride, dtype=np.uint32)
+        t0 = time.perf_counter()
+        o.render(p, pixels=px, threads=threads)
+        t_total += time.perf_counter() - t0
+        done += px.shape[0]
+        offset += 1
+    return {"value": done / t_total / 1e6, "unit": "Msamples/s", "cores": threads, "kind": "port",
+            "sample": f"{done} samples (1 spp on {offset} strided 1/{stride} pixel subsets of the 1920x1080 frame, "
+                      f"depth {depth}) in {t_total:.1f} s"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    import numpy as np
+
+    import oracle
+    from pupiloptixlab_gb300 import abi, scenes
+    sc = scenes.icosphere_field(args.width, args.height, args.depth, args.instances)
+    o = oracle.OracleScene(sc, bvh=True)
+    threads = os.cpu_count() or 1
+    npix = sc.width * sc.height
+    stride = 64
+    times, samples = [], []
+    for step in range(args.warmup + args.steps):
+        px = np.arange(step % stride, npix, stride, dtype=np.uint32)
+        p = abi.RenderParams(spp=1, max_depth=args.depth, seed=step, sample_cnt=0, accumulate=1, rng=abi.RNG_PCG32)
+        t0 = time.perf_counter()
+        o.render(p, pixels=px, threads=threads)
+        dt = time.perf_counter() - t0
+        if step >= args.warmup:
+            times.append(dt)
+            samples.append(px.shape[0])
+    total_t = sum(times)
+    value = sum(samples) / total_t / 1e6
+    sample = (f"each step: 1 spp on a strided 1/{stride} pixel subset ({samples[0]} samples) of the "
+              f"{args.width}x{args.height} frame, depth {args.depth}")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Msamples/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_t / len(times) * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "implementation": "CPU restatement of the reference integrator "
+                       "(oracle/pt_oracle.cpp: reference BSDF/emitter/RNG math, host binned-SAH BVH2); the "
+                       "reference's OptiX 7.5 / DX12 build is unavailable on this box"},
+            "cpu_baseline": {"value": value, "unit": "Msamples/s", "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "Msamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    ws, rank, local = dist_env()
+    import numpy as np
+    import torch
+
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from pupiloptixlab_gb300 import abi, scenes
+    from pupiloptixlab_gb300.api import Context, GpuScene
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    sc = scenes.icosphere_field(args.width, args.height, args.depth, args.instances)
+    ctx = Context(local)
+    g = GpuScene(ctx, sc, bvh_width=args.bvh_width, max_leaf=args.max_leaf, smem_nodes=args.smem_nodes)
+    bst = g.bvh_stats()
+    buffers = g.alloc_buffers()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    kw = dict(rng=abi.RNG_PCG32, block_size=args.block_size, wave_spp=args.wave_spp, buffers=buffers)
+
+    for w in range(args.warmup):
+        g.render(args.spp, seed=1000 + w * args.spp, **kw)
+    torch.cuda.synchronize()
+    # identical untimed render with traversal counters (same seeds as step 0)
+    g.render(args.spp, seed=0, flags=abi.RENDER_COUNTERS, **kw)
+    torch.cuda.synchronize()
+    cst = g.render_stats()
+
+    clocks = ClockSampler(local)
+    stream = torch.cuda.current_stream()
+    step_ms, ext_ms, ext_launches, sh_ms, shade_ms, launches = [], 0.0, 0, 0.0, 0.0, 0
+    barrier()
+    clocks.start()
+    for step in range(args.steps):
+        flush.fill_(float(step))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        g.render(args.spp, seed=step * args.spp, flags=abi.RENDER_KERNEL_TIMING, **kw)
+        e1.record(stream)
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+        rs = g.render_stats()
+        ext_ms += rs.extend_ms
+        ext_launches += rs.extend_launches
+        sh_ms += rs.shadow_ms
+        shade_ms += rs.shade_ms
+        launches += rs.kernel_launches
+    barrier()
+    clk = clocks.stop()
+    t_max = sum(step_ms)
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([t_max], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+    samples_per_step = args.width * args.height * args.spp
+    value = ws * samples_per_step * args.steps / (t_max / 1e3) / 1e6
+
+    e2e = None
+    if not args.no_e2e:
+        import ctypes as C
+        host_frame = torch.empty(args.width * args.height, 4, dtype=torch.float32, pin_memory=True)
+        host_cam = torch.empty(32, dtype=torch.float32, pin_memory=True)
+        host_cam.numpy()[:] = np.frombuffer(bytes(sc.camera), dtype=np.float32)
+        barrier()
+        t0 = time.perf_counter()
+        for step in range(args.steps):
+            cam = abi.CameraDesc.from_buffer_copy(host_cam.numpy().tobytes())  # camera from pinned host memory
+            g.set_camera(cam)
+            g.render(args.spp, seed=step * args.spp, **kw)
+            host_frame.copy_(buffers["accum"], non_blocking=True)
+            torch.cuda.synchronize()
+        barrier()
+        t_e2e = time.perf_counter() - t0
+        e2e = {"value": ws * samples_per_step * args.steps / t_e2e / 1e6, "unit": "Msamples/s",
+               "h2d_bytes_per_step": C.sizeof(abi.CameraDesc) + C.sizeof(abi.RenderParams),
+               "d2h_bytes_per_step": host_frame.numel() * 4}
+
+    if rank != 0:
+        return
+    # algorithmic bytes of the closest-hit kernel (per-ray counters of the identical counting render)
+    node_bytes = 32 * args.bvh_width
+    ext_bytes = cst.nodes_visited * node_bytes + cst.prims_tested * 48 + cst.extension_rays * (32 + 16)
+    achieved = ext_bytes / (ext_ms / ext_launches * 1e-3) / 1e9 / (ext_launches / args.steps) if ext_ms > 0 else None
+    # per launch: ext_bytes spread over the launches of one step
+    per_launch_bytes = ext_bytes / max(1, ext_launches // args.steps)
+    avg_launch_s = ext_ms / max(1, ext_launches) * 1e-3
+    achieved = per_launch_bytes / avg_launch_s / 1e9 if ext_ms > 0 else None
+    peak, peak_kind = measured_peaks()
+    traffic = committed_traffic()
+    cpu = None
+    if not args.no_cpu_baseline:
+        cpu = cpu_baseline(sc, 0, args.cpu_seconds, args.depth)
+    line = {
+        "metric": METRIC, "value": value, "unit": "Msamples/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+        "config": {"workload": WORKLOAD, "width": args.width, "height": args.height, "spp": args.spp,
+                   "max_depth": args.depth, "rng": "pcg32", "bvh_width": args.bvh_width, "max_leaf": args.max_leaf,
+                   "smem_nodes": args.smem_nodes, "triangles": int(bst.num_prims),
+                   "l2": "flushed between steps (256 MiB write, outside the timed events)",
+                   "parallelism": "replicas only" if ws > 1 else "single GPU"},
+        "e2e": e2e,
+        "gpu_launches": launches,
+        "clocks": clk,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None,
+                     "traffic": traffic.get("dram_bytes_per_launch") if traffic else None,
+                     "kernel": "k_trace_queue closest hit (extend)",
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else
+                     "fallback 6.8 TB/s",
+                     "algorithmic_bytes_per_ray": ext_bytes / max(1, cst.extension_rays),
+                     "nodes_per_ray": cst.nodes_visited / max(1, cst.extension_rays),
+                     "prims_per_ray": cst.prims_tested / max(1, cst.extension_rays),
+                     "extend_ms_per_step": ext_ms / args.steps, "shadow_ms_per_step": sh_ms / args.steps,
+                     "shade_ms_per_step": shade_ms / args.steps},
+        "rays_per_step": {"extension": cst.extension_rays, "shadow": cst.shadow_rays},
+        "bvh": {"nodes": int(bst.num_nodes), "sah_cost": float(bst.sah_cost), "build_ms": float(bst.build_ms),
+                "depth": int(bst.max_depth)},
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

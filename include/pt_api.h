@@ -1,0 +1,326 @@
+/*
+ * pt_api.h -- C-ABI of the GB300 wavefront path tracer.
+ *
+ * This is the thin layer that the C++ host side (the Pass/System mirror and
+ * the scene loader) calls into.  Every entry point is `extern "C"`, takes
+ * plain pointers and sizes, returns a pt_status and never throws, asserts or
+ * traps.  The last error message of the calling thread is available through
+ * pt_last_error().  Device waits inside kernels are bounded; a wait that runs
+ * out reports PT_ERR_TIMEOUT.
+ *
+ * Reference interfaces replaced (paths relative to the PupilOptixLab tree):
+ *   pt_context_*      cuda::Context::Init         framework/cuda/context.cpp:9-49
+ *                     optix::Context::Init        framework/optix/context.cpp:38-50
+ *   pt_scene_upload   world::World::LoadScene     framework/world/world.cpp:108-146
+ *                     (RenderObject, emitter tables, camera upload:
+ *                      framework/world/render_object.cpp:10-65,
+ *                      framework/world/emitter.cpp:169-243,321-390,
+ *                      framework/world/camera.cpp:72-92)
+ *   pt_bvh_build      GAS::Create / IAS::Create   framework/world/gas_manager.cpp:69-245,
+ *                                                 framework/world/ias_manager.cpp:29-113
+ *   pt_bvh_refit      IAS::Update (OPERATION_UPDATE) framework/world/ias_manager.cpp:116-151
+ *   pt_render         PTPass::OnRun + optixLaunch  example/path_tracer/pt_pass.cpp:39-57,
+ *                     framework/optix/pass.h:71-89, example/path_tracer/main.cu:38-246
+ *   pt_trace_rays     optixTrace (closest hit, main.cu:80-85) and
+ *                     Emitter::TraceShadowRay (any hit, framework/render/emitter.h:91-100)
+ *   pt_bsdf_*_batch   LocalBsdf::Sample / Eval     framework/render/material/optix_material.h:70-91
+ *   pt_camera_make    util::Camera::GetSampleToCameraMatrix / GetToWorldMatrix
+ *                     framework/util/camera.cpp:7-47
+ */
+#ifndef PT_API_H_
+#define PT_API_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PT_API_VERSION 1
+
+typedef enum pt_status {
+    PT_OK = 0,
+    PT_ERR_INVALID = 1,     /* bad argument, size or descriptor */
+    PT_ERR_CUDA = 2,        /* a CUDA runtime call failed */
+    PT_ERR_OOM = 3,         /* device allocation failed */
+    PT_ERR_TIMEOUT = 4,     /* a bounded device wait ran out */
+    PT_ERR_NAN = 5,         /* NaN/Inf detected in a checked build */
+    PT_ERR_UNSUPPORTED = 6, /* feature not available (e.g. no GPU) */
+    PT_ERR_OOB = 7,         /* index out of range in the scene data */
+    PT_ERR_STATE = 8        /* call made in the wrong order (e.g. render before BVH build) */
+} pt_status;
+
+/* Material types: numerically equal to Pupil::EMatType
+ * (framework/render/material/predefine.h:15-22, framework/decl/material_decl.inl:4-10). */
+typedef enum pt_material_type {
+    PT_MAT_UNKNOWN = 0,
+    PT_MAT_DIFFUSE = 1,
+    PT_MAT_DIELECTRIC = 2,
+    PT_MAT_ROUGH_DIELECTRIC = 3,
+    PT_MAT_CONDUCTOR = 4,
+    PT_MAT_ROUGH_CONDUCTOR = 5,
+    PT_MAT_PLASTIC = 6,
+    PT_MAT_ROUGH_PLASTIC = 7
+} pt_material_type;
+
+/* BSDF lobe flags: equal to optix::EBsdfLobeType (framework/render/material/bsdf/bsdf.h:7-24). */
+typedef enum pt_lobe {
+    PT_LOBE_UNKNOWN = 0,
+    PT_LOBE_NULL = 1,
+    PT_LOBE_DIFFUSE_REFLECTION = 1 << 1,
+    PT_LOBE_DIFFUSE_TRANSMISSION = 1 << 2,
+    PT_LOBE_GLOSSY_REFLECTION = 1 << 3,
+    PT_LOBE_GLOSSY_TRANSMISSION = 1 << 4,
+    PT_LOBE_DELTA_REFLECTION = 1 << 5,
+    PT_LOBE_DELTA_TRANSMISSION = 1 << 6,
+    PT_LOBE_DELTA = (1 << 5) | (1 << 6)
+} pt_lobe;
+
+/* Texture kinds: equal to util::ETextureType for RGB and Checkerboard
+ * (framework/util/texture.h). Bitmap textures are not supported yet. */
+typedef enum pt_texture_type { PT_TEX_RGB = 0, PT_TEX_BITMAP = 1, PT_TEX_CHECKERBOARD = 2 } pt_texture_type;
+
+/* Random streams.  PT_RNG_REF_LCG is the reference's cuda::Random (TEA-4
+ * seeding + LCG, framework/cuda/random.h:14-40); PT_RNG_PCG32 is PCG32
+ * (O'Neill, pcg_basic) seeded with initstate = pixel index, initseq = frame
+ * seed, 24-bit float output.  Both are drawn in the reference's order. */
+typedef enum pt_rng_mode { PT_RNG_REF_LCG = 0, PT_RNG_PCG32 = 1 } pt_rng_mode;
+
+/* One texture: cuda::Texture (framework/cuda/texture.h:10-57).  color0 is the
+ * RGB value or checkerboard patch1, color1 is patch2.  uv_transform holds
+ * the first two rows of the 4x4 texture-coordinate transform (row-major). */
+typedef struct pt_texture_desc {
+    uint32_t type;
+    float color0[3];
+    float color1[3];
+    float uv_transform[8];
+} pt_texture_desc;
+
+/* Texture slots per material type (tex[i]):
+ *   DIFFUSE          0 reflectance
+ *   DIELECTRIC       0 specular_reflectance, 1 specular_transmittance
+ *   ROUGH_DIELECTRIC 0 specular_reflectance, 1 specular_transmittance, 2 alpha (.x)
+ *   CONDUCTOR        0 specular_reflectance, 1 eta, 2 k
+ *   ROUGH_CONDUCTOR  0 specular_reflectance, 1 eta, 2 k, 3 alpha (.x)
+ *   PLASTIC          0 diffuse_reflectance, 1 specular_reflectance
+ *   ROUGH_PLASTIC    0 diffuse_reflectance, 1 specular_reflectance, 2 alpha (.x)
+ * Mirrors resource::Material (framework/resource/material.h:16-80). */
+typedef struct pt_material_desc {
+    uint32_t type;      /* pt_material_type */
+    uint32_t twosided;  /* flip the shading normal toward the ray (geometry.h:176-180) */
+    uint32_t nonlinear; /* plastic / rough plastic */
+    float int_ior;
+    float ext_ior;
+    pt_texture_desc tex[4];
+} pt_material_desc;
+
+/* Triangle mesh in object space (resource::Shape mesh, framework/resource/shape.h). */
+typedef struct pt_mesh_desc {
+    const float *positions; /* num_vertices * 3 */
+    const float *normals;   /* num_vertices * 3, or NULL: geometric normal cross(p1-p0,p2-p0) */
+    const float *texcoords; /* num_vertices * 2, or NULL: uv = 0 */
+    const uint32_t *indices; /* num_triangles * 3 */
+    uint32_t num_vertices;
+    uint32_t num_triangles;
+} pt_mesh_desc;
+
+typedef struct pt_sphere_desc {
+    float center[3];
+    float radius;
+} pt_sphere_desc;
+
+enum { PT_SHAPE_MESH = 0, PT_SHAPE_SPHERE = 1 };
+enum { PT_INST_FLIP_NORMALS = 1, PT_INST_FLIP_TEXCOORDS = 2 };
+
+/* One shape instance (resource::ShapeInstance; world::RenderObject,
+ * framework/world/render_object.h:11-38).  to_world is a row-major 4x4 with
+ * the translation in the last column (util::Transform).  Spheres accept
+ * similarity transforms only (rotation, uniform scale, translation). */
+typedef struct pt_instance_desc {
+    uint32_t shape_type;  /* PT_SHAPE_* */
+    uint32_t shape_index; /* into meshes[] or spheres[] */
+    uint32_t material;    /* into materials[] */
+    uint32_t flags;       /* PT_INST_* */
+    float to_world[16];
+    uint32_t is_emitter;  /* area emitter with constant RGB radiance */
+    float radiance[3];
+} pt_instance_desc;
+
+/* optix::Camera (framework/render/camera.h:7-10): two row-major 4x4 matrices. */
+typedef struct pt_camera_desc {
+    float sample_to_camera[16];
+    float camera_to_world[16];
+} pt_camera_desc;
+
+enum { PT_ENV_NONE = 0, PT_ENV_CONST = 1 };
+typedef struct pt_env_desc {
+    uint32_t type;      /* PT_ENV_* (ConstEnvEmitter, framework/render/emitter/env.h:67-86) */
+    float radiance[3];
+} pt_env_desc;
+
+typedef struct pt_scene_desc {
+    const pt_mesh_desc *meshes;
+    uint32_t num_meshes;
+    const pt_sphere_desc *spheres;
+    uint32_t num_spheres;
+    const pt_material_desc *materials;
+    uint32_t num_materials;
+    const pt_instance_desc *instances;
+    uint32_t num_instances;
+    pt_env_desc env;
+    pt_camera_desc camera;
+    uint32_t width;     /* film size (resource::Film) */
+    uint32_t height;
+    uint32_t max_depth; /* integrator max_depth (resource::Integrator) */
+} pt_scene_desc;
+
+typedef struct pt_context pt_context;
+typedef struct pt_scene pt_scene;
+
+typedef struct pt_device_opts {
+    int device;      /* CUDA ordinal */
+    uint32_t flags;  /* reserved, 0 */
+} pt_device_opts;
+
+/* BVH options.  width: 2, 4 or 8 children per node (wide nodes collapsed from a
+ * Morton-code LBVH with an SAH cost model).  max_leaf_size: primitives per leaf
+ * (1..15).  smem_nodes: number of top nodes staged in shared memory by the
+ * traversal kernels (0 = none). */
+typedef struct pt_bvh_opts {
+    uint32_t width;
+    uint32_t max_leaf_size;
+    uint32_t smem_nodes;
+    uint32_t flags;
+} pt_bvh_opts;
+
+typedef struct pt_bvh_stats {
+    uint32_t width;
+    uint32_t num_nodes;
+    uint32_t num_leaves;
+    uint32_t num_prims;
+    uint32_t max_depth;
+    float sah_cost;        /* SAH cost of the wide tree (node cost 1, primitive cost 1) */
+    float build_ms;        /* device time of the last build or refit */
+    uint64_t node_bytes;
+    uint64_t prim_bytes;
+} pt_bvh_stats;
+
+/* Render parameters: PTPass launch params (example/path_tracer/type.h:9-33).
+ * A call renders `spp` frames; frame f uses random seed `seed + f` and
+ * sample count `sample_cnt + f`, exactly as spp consecutive PTPass::OnRun
+ * calls (pt_pass.cpp:39-57) would. */
+typedef struct pt_render_params {
+    uint32_t spp;
+    uint32_t max_depth;   /* 0 = scene value */
+    uint32_t seed;        /* random_seed of the first frame */
+    uint32_t sample_cnt;  /* sample_cnt of the first frame */
+    uint32_t accumulate;  /* accumulated_flag */
+    uint32_t rng;         /* pt_rng_mode */
+    uint32_t wave_spp;    /* frames per wavefront wave (0 = auto) */
+    uint32_t block_size;  /* threads per block of the wavefront kernels (0 = auto) */
+    uint32_t flags;       /* PT_RENDER_* */
+} pt_render_params;
+
+enum {
+    PT_RENDER_MATERIAL_SORT = 1, /* bin hit paths by material before shading */
+    PT_RENDER_COUNTERS = 2,      /* count node visits and primitive tests */
+    PT_RENDER_NO_GRAPH = 4,      /* launch the bounce kernels one by one instead of a CUDA graph */
+    PT_RENDER_KERNEL_TIMING = 8  /* time each traversal / shading launch with CUDA events */
+};
+
+/* Caller-owned DEVICE buffers (BufferManager buffers, framework/system/buffer.h:26-63):
+ * accum and frame are float4 per pixel, albedo and normal float3, test float.
+ * Any pointer except accum may be NULL. */
+typedef struct pt_frame_buffers {
+    float *accum;
+    float *frame;
+    float *albedo;
+    float *normal;
+    float *test;
+} pt_frame_buffers;
+
+/* Traversal / shading counters collected with PT_RENDER_COUNTERS. */
+typedef struct pt_render_stats {
+    uint64_t samples;
+    uint64_t extension_rays;
+    uint64_t shadow_rays;
+    uint64_t nodes_visited;       /* wide nodes fetched, closest + any hit */
+    uint64_t prims_tested;        /* primitive records fetched */
+    uint64_t shadow_nodes_visited;
+    uint64_t shadow_prims_tested;
+    float render_ms;              /* device time of the last pt_render */
+    float extend_ms;              /* closest-hit launches (PT_RENDER_KERNEL_TIMING) */
+    float shadow_ms;              /* any-hit launches (PT_RENDER_KERNEL_TIMING) */
+    float shade_ms;               /* shading launches (PT_RENDER_KERNEL_TIMING) */
+    uint32_t extend_launches;
+    uint32_t shadow_launches;
+    uint32_t shade_launches;
+    uint32_t kernel_launches;     /* all kernels launched by the last pt_render */
+    uint32_t waves;
+    uint32_t overflow;            /* traversal stack overflows (must be 0) */
+} pt_render_stats;
+
+/* Flat local BSDF record used by the BSDF batch entry points (16 floats):
+ *  [0] type  [1] alpha  [2] eta  [3] int_fdr  [4] specular_sampling_weight
+ *  [5] nonlinear  [6..8] colour A  [9..11] colour B  [12..14] colour C  [15] unused
+ * colour A = diffuse reflectance (diffuse, plastics) or specular_reflectance;
+ * colour B = specular_transmittance (dielectrics), eta (conductors) or
+ *            specular_reflectance (plastics);
+ * colour C = k (conductors). */
+#define PT_LOCAL_BSDF_FLOATS 16
+
+/* ---- context ---------------------------------------------------------- */
+int pt_context_create(const pt_device_opts *opts, pt_context **out);
+int pt_context_destroy(pt_context *ctx);
+/* Copies the calling thread's last error message into buf (always NUL-terminated). */
+int pt_last_error(char *buf, size_t buf_size);
+int pt_api_version(void);
+
+/* ---- scene ------------------------------------------------------------ */
+/* The library copies everything it needs; the descriptor can be freed after. */
+int pt_scene_upload(pt_context *ctx, const pt_scene_desc *desc, pt_scene **out);
+int pt_scene_destroy(pt_scene *scene);
+int pt_scene_set_camera(pt_scene *scene, const pt_camera_desc *camera);
+/* Replace the object-space positions of one mesh (all instances of it are
+ * re-transformed).  positions: num_vertices*3 host floats.  The BVH must be
+ * refit or rebuilt afterwards. */
+int pt_scene_update_vertices(pt_scene *scene, uint32_t mesh, const float *positions, uint32_t num_vertices);
+/* Number of primitives (triangles then spheres) in world order. */
+int pt_scene_num_prims(const pt_scene *scene, uint32_t *num_triangles, uint32_t *num_spheres);
+
+/* ---- acceleration structure ------------------------------------------ */
+int pt_bvh_build(pt_scene *scene, const pt_bvh_opts *opts, void *stream);
+int pt_bvh_refit(pt_scene *scene, void *stream);
+int pt_bvh_get_stats(const pt_scene *scene, pt_bvh_stats *out);
+
+/* ---- rendering -------------------------------------------------------- */
+int pt_render(pt_scene *scene, const pt_render_params *params, const pt_frame_buffers *fb, void *stream);
+int pt_render_get_stats(const pt_scene *scene, pt_render_stats *out);
+
+/* ---- query entry points used by the parity tests ---------------------- */
+/* rays: n * 8 floats (ox,oy,oz,tmin, dx,dy,dz,tmax), hits: n * 4 floats
+ * (t, prim id as float bits (-1 = miss), u, v) for closest hit; for any hit
+ * hits[4i] is 1.0 (occluded) or 0.0.  Both are DEVICE pointers. */
+int pt_trace_rays(pt_scene *scene, const float *rays, float *hits, uint32_t n, int anyhit, void *stream);
+/* DEVICE pointers.  bsdf: n * 16 floats; wo, wi: n * 3; out_f: n * 3; out_pdf: n. */
+int pt_bsdf_eval_batch(const float *bsdf, const float *wo, const float *wi,
+                       float *out_f, float *out_pdf, uint32_t n, void *stream);
+/* rng_state: n uint32 reference-LCG seeds, updated in place; out_wi, out_f: n*3;
+ * out_pdf: n; out_type: n lobe flags. */
+int pt_bsdf_sample_batch(const float *bsdf, const float *wo, uint32_t *rng_state,
+                         float *out_wi, float *out_f, float *out_pdf, uint32_t *out_type,
+                         uint32_t n, void *stream);
+
+/* ---- host helpers (no GPU needed) ------------------------------------- */
+/* Camera matrices from a mitsuba-style sensor: fov_y in degrees,
+ * to_world row-major 4x4 in Pupil's convention (+Z points away from the view).
+ * Restates util::Camera (framework/util/camera.cpp:7-47). */
+int pt_camera_make(float fov_y_deg, float aspect, float near_clip, float far_clip,
+                   const float to_world[16], pt_camera_desc *out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PT_API_H_ */

@@ -1,0 +1,14 @@
+"""GB300-native wavefront path tracer: a drop-in for PupilOptixLab's
+"path tracing with MIS" pass.
+
+Layers:
+  include/pt_api.h         C-ABI (the drop-in boundary)
+  csrc/                    CUDA kernels (sm_103a) and the host side of the ABI
+  abi.py                   ctypes mirror of the ABI and the library loader
+  scenes.py                scene builder, materials, procedural scenes
+  api.py                   Python host wrapper (device buffers via torch)
+  passes.py                Pass / System mirror of the reference's pass API
+"""
+from . import abi  # noqa: F401
+
+__all__ = ["abi"]

@@ -1,0 +1,101 @@
+"""Build recipe for the native parts of the package.
+
+``build_library()`` compiles ``csrc/`` into ``_build/libpt_gb300.so``: the CUDA
+translation units with nvcc for sm_103a only, the host translation unit with
+g++, in parallel, then links them with nvcc.  ``build_oracle()`` runs
+``make`` in ``oracle/`` (the CPU checker used by the tests) and, when the
+PupilOptixLab source tree is present, its ``ref`` target.
+
+Host code is built with ``-ffp-contract=off``: the scene flattening must
+produce the same bits on x86-64 and aarch64 hosts.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+ROOT = PKG.parent
+CSRC = PKG / "csrc"
+BUILD = PKG / "_build"
+LIB = BUILD / "libpt_gb300.so"
+ORACLE = ROOT / "oracle"
+REFERENCE_TREE = Path("/root/reference")
+
+GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_COMMON = GENCODE + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
+                         "-I", str(ROOT / "include")]
+# Per-file extra flags.  The shading code is compiled without FMA contraction
+# so that its arithmetic follows the reference's operation order exactly.
+CU_SOURCES = {
+    "pt_bvh.cu": [],
+    "pt_render.cu": ["-fmad=false"],
+}
+CPP_SOURCES = ["pt_scene.cpp"]
+
+
+def _nvcc() -> str:
+    for cand in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and Path(cand).exists():
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _cuda_include() -> str:
+    return str(Path(_nvcc()).resolve().parent.parent / "include")
+
+
+def _run(cmd: list[str]) -> None:
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"command failed ({r.returncode}): {' '.join(cmd)}\n{r.stdout}")
+
+
+def _stale(target: Path, deps: list[Path]) -> bool:
+    if not target.exists():
+        return True
+    t = target.stat().st_mtime
+    return any(d.stat().st_mtime > t for d in deps)
+
+
+def build_library(force: bool = False, verbose: bool = False) -> Path:
+    BUILD.mkdir(exist_ok=True)
+    nvcc = _nvcc()
+    headers = sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh")) + [ROOT / "include" / "pt_api.h"]
+    jobs = []
+    objs = []
+    for src, extra in CU_SOURCES.items():
+        obj = BUILD / (src + ".o")
+        objs.append(obj)
+        if force or _stale(obj, [CSRC / src] + headers):
+            jobs.append([nvcc] + NVCC_COMMON + extra + ["-c", str(CSRC / src), "-o", str(obj)])
+    for src in CPP_SOURCES:
+        obj = BUILD / (src + ".o")
+        objs.append(obj)
+        if force or _stale(obj, [CSRC / src] + headers):
+            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall",
+                         "-I", _cuda_include(), "-I", str(ROOT / "include"), "-c", str(CSRC / src), "-o", str(obj)])
+    with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 1))) as ex:
+        for cmd in jobs:
+            if verbose:
+                print(" ".join(cmd), file=sys.stderr)
+        list(ex.map(_run, jobs))
+    if force or jobs or _stale(LIB, objs):
+        _run([nvcc] + GENCODE + ["-shared", "-o", str(LIB)] + [str(o) for o in objs])
+    return LIB
+
+
+def build_oracle(verbose: bool = False) -> None:
+    _run(["make", "-C", str(ORACLE), "-s", "all"])
+    if (REFERENCE_TREE / "framework").is_dir():
+        _run(["make", "-C", str(ORACLE), "-s", "ref", f"REF_DIR={REFERENCE_TREE}", f"CUDA_INC={_cuda_include()}"])
+
+
+if __name__ == "__main__":
+    build_library(force="--force" in sys.argv, verbose=True)
+    build_oracle(verbose=True)
+    print(LIB)

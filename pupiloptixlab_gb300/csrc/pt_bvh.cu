@@ -1,0 +1,716 @@
+// pt_bvh.cu -- GPU acceleration-structure build and refit.
+//
+// Replaces the closed OptiX builds GAS::Create / IAS::Create / IAS::Update
+// (framework/world/gas_manager.cpp:69-245, framework/world/ias_manager.cpp:
+// 29-151).  Pipeline (all on the device, one GPU):
+//   1. primitive boxes and centroid bounds (block reduction + ordered atomics)
+//   2. 63-bit Morton codes (21 bits per axis)
+//   3. stable LSD radix sort of (code, primitive) pairs, 8 passes of 8 bits:
+//      tile histogram -> one-block exclusive scan -> warp-multisplit scatter
+//      (__match_any_sync ranks, per-warp digit counts in shared memory)
+//   4. Karras (HPG 2012) binary radix tree, equal codes split by index
+//   5. bottom-up boxes with an SAH cost per node (leaf vs split decision,
+//      leaves of at most max_leaf_size primitives)
+//   6. top-down, level-synchronous collapse into 2/4/8-wide nodes: each wide
+//      node repeatedly opens its child with the largest surface area until it
+//      has `width` children (SAH-driven collapse); children that the cost model
+//      made leaves become leaf slots.  Nodes come out in breadth-first order.
+//   7. primitive records gathered into leaf order
+// Child boxes are padded outward (relative to the box and scene magnitude) so
+// that the conservative slab test never rejects a primitive the exact test
+// would hit.
+
+#include "pt_internal.h"
+
+#include <algorithm>
+#include <cfloat>
+
+namespace {
+
+using ptd::f3;
+
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 16;
+constexpr int kSortTile = kSortThreads * kSortItems;
+constexpr float kCostNode = 1.2f;
+constexpr float kCostPrim = 1.0f;
+
+__device__ __forceinline__ uint32_t f2ord(float f) {
+    uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord2f(uint32_t u) {
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+__device__ __forceinline__ void prim_box(const float4 *prims, uint32_t p, float3 &lo, float3 &hi) {
+    float4 a = prims[3 * (size_t)p], b = prims[3 * (size_t)p + 1];
+    if (__float_as_int(a.w) >= 0) {
+        float4 c = prims[3 * (size_t)p + 2];
+        lo = f3(fminf(a.x, fminf(b.x, c.x)), fminf(a.y, fminf(b.y, c.y)), fminf(a.z, fminf(b.z, c.z)));
+        hi = f3(fmaxf(a.x, fmaxf(b.x, c.x)), fmaxf(a.y, fmaxf(b.y, c.y)), fmaxf(a.z, fmaxf(b.z, c.z)));
+    } else {
+        float r = b.x;
+        lo = f3(a.x - r, a.y - r, a.z - r);
+        hi = f3(a.x + r, a.y + r, a.z + r);
+    }
+}
+
+// 1. per-primitive boxes (SoA float4) + centroid bounds into 6 ordered uints.
+__global__ void k_prim_bounds(const float4 *prims, uint32_t n, float4 *plo, float4 *phi, uint32_t *cb) {
+    __shared__ float red[6][32];
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    float v[6] = {FLT_MAX, FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX, -FLT_MAX};
+    if (i < n) {
+        float3 lo, hi;
+        prim_box(prims, i, lo, hi);
+        plo[i] = make_float4(lo.x, lo.y, lo.z, 0.f);
+        phi[i] = make_float4(hi.x, hi.y, hi.z, 0.f);
+        float cx = 0.5f * (lo.x + hi.x), cy = 0.5f * (lo.y + hi.y), cz = 0.5f * (lo.z + hi.z);
+        v[0] = cx; v[1] = cy; v[2] = cz; v[3] = cx; v[4] = cy; v[5] = cz;
+    }
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        float x = v[k];
+        for (int o = 16; o > 0; o >>= 1) {
+            float y = __shfl_xor_sync(0xffffffffu, x, o);
+            x = k < 3 ? fminf(x, y) : fmaxf(x, y);
+        }
+        if (lane == 0) red[k][warp] = x;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        int nw = blockDim.x >> 5;
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            float x = lane < nw ? red[k][lane] : (k < 3 ? FLT_MAX : -FLT_MAX);
+            for (int o = 16; o > 0; o >>= 1) {
+                float y = __shfl_xor_sync(0xffffffffu, x, o);
+                x = k < 3 ? fminf(x, y) : fmaxf(x, y);
+            }
+            if (lane == 0) {
+                if (k < 3) atomicMin(&cb[k], f2ord(x));
+                else atomicMax(&cb[k], f2ord(x));
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ uint64_t split3(uint32_t a) {
+    uint64_t x = a & 0x1fffffu;
+    x = (x | x << 32) & 0x1f00000000ffffULL;
+    x = (x | x << 16) & 0x1f0000ff0000ffULL;
+    x = (x | x << 8) & 0x100f00f00f00f00fULL;
+    x = (x | x << 4) & 0x10c30c30c30c30c3ULL;
+    x = (x | x << 2) & 0x1249249249249249ULL;
+    return x;
+}
+
+// 2. Morton codes of the box centroids.
+__global__ void k_morton(const float4 *plo, const float4 *phi, uint32_t n, const uint32_t *cb, uint64_t *keys, uint32_t *vals) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float mn[3] = {ord2f(cb[0]), ord2f(cb[1]), ord2f(cb[2])};
+    float mx[3] = {ord2f(cb[3]), ord2f(cb[4]), ord2f(cb[5])};
+    float4 lo = plo[i], hi = phi[i];
+    float c[3] = {0.5f * (lo.x + hi.x), 0.5f * (lo.y + hi.y), 0.5f * (lo.z + hi.z)};
+    uint32_t q[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        float ext = mx[k] - mn[k];
+        float t = ext > 0.f ? (c[k] - mn[k]) / ext : 0.f;
+        float s = t * 2097152.0f;
+        q[k] = (uint32_t)fminf(fmaxf(s, 0.f), 2097151.f);
+    }
+    keys[i] = (split3(q[0]) << 2) | (split3(q[1]) << 1) | split3(q[2]);
+    vals[i] = i;
+}
+
+// 3a. per-tile digit histogram, stored digit-major: hist[d * tiles + tile].
+__global__ void k_radix_hist(const uint64_t *keys, uint32_t n, int shift, uint32_t *hist, uint32_t tiles) {
+    __shared__ uint32_t h[256];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    size_t base = (size_t)blockIdx.x * kSortTile;
+#pragma unroll 4
+    for (int k = 0; k < kSortItems; k++) {
+        size_t idx = base + (size_t)k * kSortThreads + threadIdx.x;
+        if (idx < n) atomicAdd(&h[(keys[idx] >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    hist[(size_t)threadIdx.x * tiles + blockIdx.x] = h[threadIdx.x];
+}
+
+// 3b. in-place exclusive scan of m values with one block of 1024 threads.
+__global__ void k_scan_excl(uint32_t *data, uint32_t m) {
+    __shared__ uint32_t part[1024];
+    uint32_t per = (m + 1023) / 1024;
+    uint32_t b = threadIdx.x * per, e = min(m, b + per);
+    uint32_t sum = 0;
+    for (uint32_t i = b; i < e; i++) sum += data[i];
+    part[threadIdx.x] = sum;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        uint32_t v = threadIdx.x >= (uint32_t)o ? part[threadIdx.x - o] : 0;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    uint32_t run = part[threadIdx.x] - sum;
+    for (uint32_t i = b; i < e; i++) {
+        uint32_t v = data[i];
+        data[i] = run;
+        run += v;
+    }
+}
+
+// 3c. stable scatter: ranks within a tile come from warp multisplit.
+__global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const uint64_t *kin, const uint32_t *vin, uint64_t *kout,
+                                                                uint32_t *vout, uint32_t n, int shift,
+                                                                const uint32_t *hist, uint32_t tiles) {
+    __shared__ uint32_t base_off[256];
+    __shared__ uint32_t wcnt[kSortThreads / 32][256];
+    __shared__ uint32_t tot[256];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    base_off[tid] = hist[(size_t)tid * tiles + blockIdx.x];
+    const uint32_t lt = (1u << lane) - 1u;
+    size_t base = (size_t)blockIdx.x * kSortTile;
+    for (int k = 0; k < kSortItems; k++) {
+#pragma unroll
+        for (int w = 0; w < kSortThreads / 32; w++) wcnt[w][tid] = 0;
+        __syncthreads();
+        size_t idx = base + (size_t)k * kSortThreads + tid;
+        bool valid = idx < n;
+        uint64_t key = valid ? kin[idx] : 0;
+        uint32_t val = valid ? vin[idx] : 0;
+        uint32_t digit = valid ? (uint32_t)((key >> shift) & 255u) : 256u;
+        uint32_t peers = __match_any_sync(0xffffffffu, digit);
+        uint32_t lrank = __popc(peers & lt);
+        if (valid && lrank == 0) wcnt[warp][digit] = __popc(peers);
+        __syncthreads();
+        {
+            uint32_t run = 0;
+#pragma unroll
+            for (int w = 0; w < kSortThreads / 32; w++) {
+                uint32_t c = wcnt[w][tid];
+                wcnt[w][tid] = run;
+                run += c;
+            }
+            tot[tid] = run;
+        }
+        __syncthreads();
+        if (valid) {
+            uint32_t pos = base_off[digit] + wcnt[warp][digit] + lrank;
+            kout[pos] = key;
+            vout[pos] = val;
+        }
+        __syncthreads();
+        base_off[tid] += tot[tid];
+    }
+}
+
+__device__ __forceinline__ int delta(const uint64_t *keys, int n, int i, int j) {
+    if (j < 0 || j >= n) return -1;
+    uint64_t a = keys[i], b = keys[j];
+    if (a == b) return 64 + __clz((uint32_t)(i ^ j));
+    return __clzll(a ^ b);
+}
+
+// 4. Karras binary radix tree.  Internal nodes 0..n-2, leaf k is node n-1+k.
+__global__ void k_karras(const uint64_t *keys, int n, int *left, int *right, int *parent, int *rfirst) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    int d = (delta(keys, n, i, i + 1) - delta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
+    int dmin = delta(keys, n, i, i - d);
+    int lmax = 2;
+    while (delta(keys, n, i, i + lmax * d) > dmin) lmax <<= 1;
+    int l = 0;
+    for (int t = lmax >> 1; t >= 1; t >>= 1)
+        if (delta(keys, n, i, i + (l + t) * d) > dmin) l += t;
+    int j = i + l * d;
+    int dnode = delta(keys, n, i, j);
+    int s = 0;
+    int div = 2, t;
+    do {
+        t = (l + div - 1) / div;
+        if (delta(keys, n, i, i + (s + t) * d) > dnode) s += t;
+        div <<= 1;
+    } while (t > 1);
+    int gamma = i + s * d + min(d, 0);
+    int first = min(i, j), last = max(i, j);
+    int lc = (first == gamma) ? (n - 1 + gamma) : gamma;
+    int rc = (last == gamma + 1) ? (n - 1 + gamma + 1) : gamma + 1;
+    left[i] = lc;
+    right[i] = rc;
+    parent[lc] = i;
+    parent[rc] = i;
+    rfirst[i] = first;
+}
+
+__device__ __forceinline__ float half_area(float4 lo, float4 hi) {
+    float ex = hi.x - lo.x, ey = hi.y - lo.y, ez = hi.z - lo.z;
+    return ex * ey + ey * ez + ez * ex;
+}
+
+// 5. bottom-up boxes, counts and SAH costs (second arrival processes a node).
+__global__ void k_bottom_up(int n, const int *left, const int *right, const int *parent, const uint32_t *order,
+                            const float4 *plo, const float4 *phi, float4 *nlo, float4 *nhi, int *ncount, float *ncost,
+                            int *nleaf, int *flags, int max_leaf) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    int leaf = n - 1 + k;
+    uint32_t p = order[k];
+    float4 lo = plo[p], hi = phi[p];
+    nlo[leaf] = lo;
+    nhi[leaf] = hi;
+    ncount[leaf] = 1;
+    ncost[leaf] = kCostPrim * half_area(lo, hi);
+    nleaf[leaf] = 1;
+    int cur = parent[leaf];
+    while (cur >= 0) {
+        __threadfence();
+        if (atomicAdd(&flags[cur], 1) == 0) return;
+        __threadfence();
+        int l = left[cur], r = right[cur];
+        float4 llo = __ldcg(&nlo[l]), lhi = __ldcg(&nhi[l]), rlo = __ldcg(&nlo[r]), rhi = __ldcg(&nhi[r]);
+        float4 blo = make_float4(fminf(llo.x, rlo.x), fminf(llo.y, rlo.y), fminf(llo.z, rlo.z), 0.f);
+        float4 bhi = make_float4(fmaxf(lhi.x, rhi.x), fmaxf(lhi.y, rhi.y), fmaxf(lhi.z, rhi.z), 0.f);
+        int cnt = __ldcg(&ncount[l]) + __ldcg(&ncount[r]);
+        float a = half_area(blo, bhi);
+        float c_split = kCostNode * a + __ldcg(&ncost[l]) + __ldcg(&ncost[r]);
+        float c_leaf = cnt <= max_leaf ? kCostPrim * a * (float)cnt : FLT_MAX;
+        bool mk_leaf = c_leaf <= c_split;
+        nlo[cur] = blo;
+        nhi[cur] = bhi;
+        ncount[cur] = cnt;
+        ncost[cur] = mk_leaf ? c_leaf : c_split;
+        nleaf[cur] = mk_leaf ? 1 : 0;
+        cur = parent[cur];
+    }
+}
+
+__device__ __forceinline__ void padded(float4 lo, float4 hi, float scene_mag, float3 &plo, float3 &phi) {
+    float mag = fmaxf(fmaxf(fmaxf(fabsf(lo.x), fabsf(lo.y)), fmaxf(fabsf(lo.z), fabsf(hi.x))), fmaxf(fabsf(hi.y), fabsf(hi.z)));
+    float ext = fmaxf(fmaxf(hi.x - lo.x, hi.y - lo.y), hi.z - lo.z);
+    float pad = 4e-7f * (mag + scene_mag) + 1e-6f * ext;
+    plo = f3(lo.x - pad, lo.y - pad, lo.z - pad);
+    phi = f3(hi.x + pad, hi.y + pad, hi.z + pad);
+}
+
+template <int K>
+__device__ __forceinline__ void write_slot(float *node, int c, float3 lo, float3 hi, int child, int count) {
+    node[c] = lo.x;
+    node[K + c] = hi.x;
+    node[2 * K + c] = lo.y;
+    node[3 * K + c] = hi.y;
+    node[4 * K + c] = lo.z;
+    node[5 * K + c] = hi.z;
+    node[6 * K + c] = __int_as_float(child);
+    node[7 * K + c] = __int_as_float(count);
+}
+template <int K>
+__device__ __forceinline__ void write_empty(float *node, int c) {
+    write_slot<K>(node, c, f3(1e30f, 1e30f, 1e30f), f3(1e30f, 1e30f, 1e30f), -1, 0);
+}
+
+// 6. one level of the wide collapse.  item = (wide node index, binary node).
+template <int K>
+__global__ void k_collapse(int n, const int2 *items_in, const uint32_t *n_in_ptr, int2 *items_out, uint32_t *n_out,
+                           uint32_t *n_wide, float *nodes, const int *left, const int *right, const int *rfirst,
+                           const float4 *nlo, const float4 *nhi, const int *ncount, const int *nleaf, float scene_mag) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *n_in_ptr) return;
+    int2 it = items_in[i];
+    int ch[K];
+    int cnt = 2;
+    ch[0] = left[it.y];
+    ch[1] = right[it.y];
+    for (int c = 2; c < K; c++) ch[c] = -1;
+    while (cnt < K) {
+        int best = -1;
+        float best_a = -1.f;
+        for (int c = 0; c < cnt; c++) {
+            int b = ch[c];
+            if (b >= n - 1 || nleaf[b]) continue;  // binary leaf or leaf by cost
+            float a = half_area(nlo[b], nhi[b]);
+            if (a > best_a) {
+                best_a = a;
+                best = c;
+            }
+        }
+        if (best < 0) break;
+        int b = ch[best];
+        ch[best] = left[b];
+        ch[cnt++] = right[b];
+    }
+    float *node = nodes + (size_t)it.x * 8 * K;
+    for (int c = 0; c < K; c++) {
+        if (c >= cnt) {
+            write_empty<K>(node, c);
+            continue;
+        }
+        int b = ch[c];
+        float3 lo, hi;
+        padded(nlo[b], nhi[b], scene_mag, lo, hi);
+        if (b >= n - 1) {
+            write_slot<K>(node, c, lo, hi, b - (n - 1), 1);
+        } else if (nleaf[b]) {
+            write_slot<K>(node, c, lo, hi, rfirst[b], ncount[b]);
+        } else {
+            uint32_t w = atomicAdd(n_wide, 1u);
+            uint32_t q = atomicAdd(n_out, 1u);
+            items_out[q] = make_int2((int)w, b);
+            write_slot<K>(node, c, lo, hi, (int)w, 0);
+        }
+    }
+}
+
+// Root that is a single leaf (tiny scenes): one wide node, slot 0 = all primitives.
+template <int K>
+__global__ void k_leaf_root(float *nodes, int n, const float4 *nlo, const float4 *nhi, int root, float scene_mag) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    for (int c = 0; c < K; c++) write_empty<K>(nodes, c);
+    if (n > 0) {
+        float3 lo, hi;
+        padded(nlo[root], nhi[root], scene_mag, lo, hi);
+        write_slot<K>(nodes, 0, lo, hi, 0, n);
+    }
+}
+
+// 7. primitive records into leaf order.
+__global__ void k_gather_prims(const float4 *src, const uint32_t *order, uint32_t n, float4 *dst) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t p = order[i];
+    dst[3 * (size_t)i] = src[3 * (size_t)p];
+    dst[3 * (size_t)i + 1] = src[3 * (size_t)p + 1];
+    dst[3 * (size_t)i + 2] = src[3 * (size_t)p + 2];
+}
+
+// SAH cost of the wide tree: sum over slots of area * (node or primitive cost).
+template <int K>
+__global__ void k_sah(const float *nodes, uint32_t num_nodes, double *acc) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    double v = 0.0;
+    if (i < num_nodes) {
+        const float *nd = nodes + (size_t)i * 8 * K;
+        for (int c = 0; c < K; c++) {
+            int ch = __float_as_int(nd[6 * K + c]);
+            if (ch < 0) continue;
+            float ex = nd[K + c] - nd[c], ey = nd[3 * K + c] - nd[2 * K + c], ez = nd[5 * K + c] - nd[4 * K + c];
+            float a = ex * ey + ey * ez + ez * ex;
+            int cnt = __float_as_int(nd[7 * K + c]);
+            v += (double)a * (cnt > 0 ? (double)kCostPrim * cnt : (double)kCostNode);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(acc, v);
+}
+
+// Refit of one level: leaf slots from the primitives, inner slots from the
+// union of the child node's slots (deeper levels are refit first).
+template <int K>
+__global__ void k_refit_level(float *nodes, uint32_t first, uint32_t last, const float4 *prims_bvh, float scene_mag) {
+    uint32_t i = first + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= last) return;
+    float *nd = nodes + (size_t)i * 8 * K;
+    for (int c = 0; c < K; c++) {
+        int ch = __float_as_int(nd[6 * K + c]);
+        if (ch < 0) continue;
+        int cnt = __float_as_int(nd[7 * K + c]);
+        float4 lo = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0.f), hi = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0.f);
+        if (cnt > 0) {
+            for (int j = 0; j < cnt; j++) {
+                float3 a, b;
+                prim_box(prims_bvh, (uint32_t)(ch + j), a, b);
+                lo = make_float4(fminf(lo.x, a.x), fminf(lo.y, a.y), fminf(lo.z, a.z), 0.f);
+                hi = make_float4(fmaxf(hi.x, b.x), fmaxf(hi.y, b.y), fmaxf(hi.z, b.z), 0.f);
+            }
+        } else {
+            const float *cn = nodes + (size_t)ch * 8 * K;
+            for (int g = 0; g < K; g++) {
+                if (__float_as_int(cn[6 * K + g]) < 0) continue;
+                lo = make_float4(fminf(lo.x, cn[g]), fminf(lo.y, cn[2 * K + g]), fminf(lo.z, cn[4 * K + g]), 0.f);
+                hi = make_float4(fmaxf(hi.x, cn[K + g]), fmaxf(hi.y, cn[3 * K + g]), fmaxf(hi.z, cn[5 * K + g]), 0.f);
+            }
+        }
+        float3 plo, phi;
+        padded(lo, hi, scene_mag, plo, phi);
+        write_slot<K>(nd, c, plo, phi, ch, cnt);
+    }
+}
+
+// World-space re-transform of one mesh instance's vertices (same arithmetic
+// order as the host flattening: x' = m0*x + m1*y + m2*z + m3, unfused).
+__global__ void k_transform_vertices(const float *obj, uint32_t nv, float4 m0, float4 m1, float4 m2, float4 *vpos) {
+    uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nv) return;
+    float x = obj[3 * v], y = obj[3 * v + 1], z = obj[3 * v + 2];
+    float wx = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(m0.x, x), __fmul_rn(m0.y, y)), __fmul_rn(m0.z, z)), m0.w);
+    float wy = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(m1.x, x), __fmul_rn(m1.y, y)), __fmul_rn(m1.z, z)), m1.w);
+    float wz = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(m2.x, x), __fmul_rn(m2.y, y)), __fmul_rn(m2.z, z)), m2.w);
+    vpos[v] = make_float4(wx, wy, wz, 0.f);
+}
+__global__ void k_rebuild_tri_records(const uint32_t *tri_vidx, const float4 *vpos, uint32_t first, uint32_t count,
+                                      float4 *prims) {
+    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    uint32_t p = first + t;
+    float4 a = vpos[tri_vidx[3 * p]], b = vpos[tri_vidx[3 * p + 1]], c = vpos[tri_vidx[3 * p + 2]];
+    float4 *r = prims + 3 * (size_t)p;
+    float w = r[0].w;  // keep the id
+    r[0] = make_float4(a.x, a.y, a.z, w);
+    r[1] = make_float4(b.x, b.y, b.z, 0.f);
+    r[2] = make_float4(c.x, c.y, c.z, 0.f);
+}
+
+inline uint32_t blocks(size_t n, int b) { return (uint32_t)((n + b - 1) / b); }
+
+struct Scratch {
+    uint64_t *keys[2];
+    uint32_t *vals[2];
+    uint32_t *hist;
+    float4 *plo, *phi;
+    int *left, *right, *parent, *rfirst, *ncount, *nleaf, *flags;
+    float4 *nlo, *nhi;
+    float *ncost;
+    int2 *items[2];
+    uint32_t *counters;  // [0..5] centroid bounds, [6] n_wide, [7] n_out0, [8] n_out1
+    double *sah;
+};
+
+template <class T>
+T *carve(char *&p, size_t count) {
+    T *r = reinterpret_cast<T *>(p);
+    size_t bytes = (count * sizeof(T) + 255) & ~size_t(255);
+    p += bytes;
+    return r;
+}
+size_t carve_size(size_t n, uint32_t tiles) {
+    size_t t = 0;
+    auto add = [&](size_t bytes) { t += (bytes + 255) & ~size_t(255); };
+    add(8 * n); add(8 * n); add(4 * n); add(4 * n);
+    add(4 * (size_t)256 * tiles);
+    add(16 * n); add(16 * n);
+    add(4 * n); add(4 * n); add(4 * 2 * n); add(4 * n); add(4 * 2 * n); add(4 * 2 * n); add(4 * n);
+    add(16 * 2 * n); add(16 * 2 * n);
+    add(4 * 2 * n);
+    add(8 * n); add(8 * n);
+    add(64); add(64);
+    return t;
+}
+
+template <int K>
+int build_wide(pt_scene *s, const Scratch &sc, uint32_t n, cudaStream_t st) {
+    s->level_start.clear();
+    size_t node_bytes = (size_t)std::max<uint32_t>(1, n > 1 ? n - 1 : 1) * 32 * K;
+    int e = s->nodes.ensure(node_bytes);
+    if (e != PT_OK) return e;
+    float *nodes = s->nodes.as<float>();
+    const int tb = 256;
+    // root
+    int root_leaf = 0;
+    if (n > 1) PT_CUDA_TRY(cudaMemcpyAsync(&root_leaf, sc.nleaf, sizeof(int), cudaMemcpyDeviceToHost, st));
+    PT_CUDA_TRY(cudaStreamSynchronize(st));
+    if (n <= 1 || root_leaf) {
+        int root = n > 1 ? 0 : 0;  // internal node 0, or the single leaf (node 0 when n == 1)
+        k_leaf_root<K><<<1, 32, 0, st>>>(nodes, (int)n, sc.nlo, sc.nhi, root, s->scene_mag);
+        s->level_start = {0, 1};
+        return PT_OK;
+    }
+    uint32_t h_init[3] = {1, 1, 0};  // n_wide = 1 (root), n_out0 = 1 (root item), n_out1 = 0
+    PT_CUDA_TRY(cudaMemcpyAsync(sc.counters + 6, h_init, sizeof(h_init), cudaMemcpyHostToDevice, st));
+    int2 root_item = make_int2(0, 0);
+    PT_CUDA_TRY(cudaMemcpyAsync(sc.items[0], &root_item, sizeof(int2), cudaMemcpyHostToDevice, st));
+    uint32_t level_count = 1, start = 0;
+    int cur = 0;
+    while (level_count > 0) {
+        s->level_start.push_back(start);
+        uint32_t *n_in = sc.counters + 7 + cur, *n_out = sc.counters + 7 + (cur ^ 1);
+        PT_CUDA_TRY(cudaMemsetAsync(n_out, 0, sizeof(uint32_t), st));
+        k_collapse<K><<<blocks(level_count, tb), tb, 0, st>>>((int)n, sc.items[cur], n_in, sc.items[cur ^ 1], n_out,
+                                                             sc.counters + 6, nodes, sc.left, sc.right, sc.rfirst,
+                                                             sc.nlo, sc.nhi, sc.ncount, sc.nleaf, s->scene_mag);
+        PT_CUDA_TRY(cudaGetLastError());
+        uint32_t nxt = 0;
+        PT_CUDA_TRY(cudaMemcpyAsync(&nxt, n_out, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        PT_CUDA_TRY(cudaStreamSynchronize(st));
+        start += level_count;
+        level_count = nxt;
+        cur ^= 1;
+    }
+    s->level_start.push_back(start);
+    return PT_OK;
+}
+
+template <int K>
+void refit_levels(pt_scene *s, cudaStream_t st) {
+    float *nodes = s->nodes.as<float>();
+    for (int L = (int)s->level_start.size() - 2; L >= 0; L--) {
+        uint32_t a = s->level_start[L], b = s->level_start[L + 1];
+        if (b > a) k_refit_level<K><<<blocks(b - a, 128), 128, 0, st>>>(nodes, a, b, s->prims_bvh.as<float4>(), s->scene_mag);
+    }
+}
+
+template <int K>
+void sah_launch(pt_scene *s, double *acc, cudaStream_t st) {
+    uint32_t nn = s->level_start.back();
+    k_sah<K><<<blocks(nn, 256), 256, 0, st>>>(s->nodes.as<float>(), nn, acc);
+}
+
+}  // namespace
+
+int pt_bvh_build_impl(pt_scene *s, const pt_bvh_opts *o, cudaStream_t st) {
+    const uint32_t n = s->num_prims;
+    const uint32_t tiles = std::max<uint32_t>(1, (n + kSortTile - 1) / kSortTile);
+    const int K = (int)o->width;
+    PT_CUDA_TRY(cudaEventRecord(s->ev0, st));
+    int e = s->bvh_scratch.ensure(carve_size(std::max<uint32_t>(n, 2), tiles));
+    if (e != PT_OK) return e;
+    Scratch sc;
+    char *p = static_cast<char *>(s->bvh_scratch.ptr);
+    size_t nn = std::max<uint32_t>(n, 2);
+    sc.keys[0] = carve<uint64_t>(p, nn);
+    sc.keys[1] = carve<uint64_t>(p, nn);
+    sc.vals[0] = carve<uint32_t>(p, nn);
+    sc.vals[1] = carve<uint32_t>(p, nn);
+    sc.hist = carve<uint32_t>(p, (size_t)256 * tiles);
+    sc.plo = carve<float4>(p, nn);
+    sc.phi = carve<float4>(p, nn);
+    sc.left = carve<int>(p, nn);
+    sc.right = carve<int>(p, nn);
+    sc.parent = carve<int>(p, 2 * nn);
+    sc.rfirst = carve<int>(p, nn);
+    sc.ncount = carve<int>(p, 2 * nn);
+    sc.nleaf = carve<int>(p, 2 * nn);
+    sc.flags = carve<int>(p, nn);
+    sc.nlo = carve<float4>(p, 2 * nn);
+    sc.nhi = carve<float4>(p, 2 * nn);
+    sc.ncost = carve<float>(p, 2 * nn);
+    sc.items[0] = carve<int2>(p, nn);
+    sc.items[1] = carve<int2>(p, nn);
+    sc.counters = carve<uint32_t>(p, 16);
+    sc.sah = carve<double>(p, 8);
+    if ((e = s->bvh_order.ensure(std::max<size_t>(4 * (size_t)n, 16))) != PT_OK) return e;
+    if ((e = s->prims_bvh.ensure(std::max<size_t>(48 * (size_t)n, 48))) != PT_OK) return e;
+
+    const int tb = 256;
+    uint32_t cb_init[6] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0u, 0u, 0u};
+    PT_CUDA_TRY(cudaMemcpyAsync(sc.counters, cb_init, sizeof(cb_init), cudaMemcpyHostToDevice, st));
+    if (n > 0) {
+        const float4 *prims = s->prims_world.as<float4>();
+        k_prim_bounds<<<blocks(n, tb), tb, 0, st>>>(prims, n, sc.plo, sc.phi, sc.counters);
+        k_morton<<<blocks(n, tb), tb, 0, st>>>(sc.plo, sc.phi, n, sc.counters, sc.keys[0], sc.vals[0]);
+        int cur = 0;
+        for (int pass = 0; pass < 8; pass++) {
+            int shift = pass * 8;
+            k_radix_hist<<<tiles, kSortThreads, 0, st>>>(sc.keys[cur], n, shift, sc.hist, tiles);
+            k_scan_excl<<<1, 1024, 0, st>>>(sc.hist, 256 * tiles);
+            k_radix_scatter<<<tiles, kSortThreads, 0, st>>>(sc.keys[cur], sc.vals[cur], sc.keys[cur ^ 1], sc.vals[cur ^ 1],
+                                                             n, shift, sc.hist, tiles);
+            cur ^= 1;
+        }
+        PT_CUDA_TRY(cudaGetLastError());
+        // after 8 passes the sorted pairs are back in buffer 0
+        PT_CUDA_TRY(cudaMemcpyAsync(s->bvh_order.ptr, sc.vals[cur], 4 * (size_t)n, cudaMemcpyDeviceToDevice, st));
+        PT_CUDA_TRY(cudaMemsetAsync(sc.parent, 0xff, 4 * (2 * (size_t)n - 1), st));
+        PT_CUDA_TRY(cudaMemsetAsync(sc.flags, 0, 4 * (size_t)n, st));
+        if (n > 1) k_karras<<<blocks(n - 1, tb), tb, 0, st>>>(sc.keys[cur], (int)n, sc.left, sc.right, sc.parent, sc.rfirst);
+        k_bottom_up<<<blocks(n, tb), tb, 0, st>>>((int)n, sc.left, sc.right, sc.parent, s->bvh_order.as<uint32_t>(), sc.plo,
+                                                  sc.phi, sc.nlo, sc.nhi, sc.ncount, sc.ncost, sc.nleaf, sc.flags,
+                                                  (int)o->max_leaf_size);
+        k_gather_prims<<<blocks(n, tb), tb, 0, st>>>(prims, s->bvh_order.as<uint32_t>(), n, s->prims_bvh.as<float4>());
+        PT_CUDA_TRY(cudaGetLastError());
+    }
+    switch (K) {
+        case 2: e = build_wide<2>(s, sc, n, st); break;
+        case 4: e = build_wide<4>(s, sc, n, st); break;
+        default: e = build_wide<8>(s, sc, n, st); break;
+    }
+    if (e != PT_OK) return e;
+    PT_CUDA_TRY(cudaEventRecord(s->ev1, st));
+    PT_CUDA_TRY(cudaMemsetAsync(sc.sah, 0, sizeof(double), st));
+    switch (K) {
+        case 2: sah_launch<2>(s, sc.sah, st); break;
+        case 4: sah_launch<4>(s, sc.sah, st); break;
+        default: sah_launch<8>(s, sc.sah, st); break;
+    }
+    double sah = 0.0;
+    float4 rlo = make_float4(0, 0, 0, 0), rhi = rlo;
+    PT_CUDA_TRY(cudaMemcpyAsync(&sah, sc.sah, sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (n > 0) {
+        uint32_t root = n > 1 ? 0 : 0;
+        PT_CUDA_TRY(cudaMemcpyAsync(&rlo, sc.nlo + root, sizeof(float4), cudaMemcpyDeviceToHost, st));
+        PT_CUDA_TRY(cudaMemcpyAsync(&rhi, sc.nhi + root, sizeof(float4), cudaMemcpyDeviceToHost, st));
+    }
+    PT_CUDA_TRY(cudaStreamSynchronize(st));
+    float ms = 0.f;
+    PT_CUDA_TRY(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+    float ex = rhi.x - rlo.x, ey = rhi.y - rlo.y, ez = rhi.z - rlo.z;
+    double root_area = (double)ex * ey + (double)ey * ez + (double)ez * ex;
+
+    s->bvh_opts = *o;
+    pt_bvh_stats &bs = s->bvh_stats;
+    bs.width = o->width;
+    bs.num_nodes = s->level_start.back();
+    bs.num_prims = n;
+    bs.max_depth = (uint32_t)s->level_start.size() - 1;
+    bs.sah_cost = root_area > 0 ? (float)((kCostNode * root_area + sah) / root_area) : 0.f;
+    bs.build_ms = ms;
+    bs.node_bytes = (uint64_t)bs.num_nodes * 32 * K;
+    bs.prim_bytes = (uint64_t)n * 48;
+    bs.num_leaves = 0;
+
+    ptd::DevScene &d = s->dev;
+    d.nodes = s->nodes.as<float4>();
+    d.prims = s->prims_bvh.as<float4>();
+    d.width = o->width;
+    d.num_nodes = bs.num_nodes;
+    uint32_t max_smem = (uint32_t)std::max(0, s->ctx->max_smem_per_block - 64 * 1024) / (32 * K);
+    d.smem_nodes = std::min<uint32_t>(std::min(o->smem_nodes, bs.num_nodes), max_smem);
+    s->bvh_built = true;
+    return PT_OK;
+}
+
+int pt_bvh_refit_impl(pt_scene *s, cudaStream_t st) {
+    const uint32_t n = s->num_prims;
+    PT_CUDA_TRY(cudaEventRecord(s->ev0, st));
+    if (n > 0)
+        k_gather_prims<<<blocks(n, 256), 256, 0, st>>>(s->prims_world.as<float4>(), s->bvh_order.as<uint32_t>(), n,
+                                                        s->prims_bvh.as<float4>());
+    switch (s->bvh_opts.width) {
+        case 2: refit_levels<2>(s, st); break;
+        case 4: refit_levels<4>(s, st); break;
+        default: refit_levels<8>(s, st); break;
+    }
+    PT_CUDA_TRY(cudaGetLastError());
+    PT_CUDA_TRY(cudaEventRecord(s->ev1, st));
+    PT_CUDA_TRY(cudaEventSynchronize(s->ev1));
+    float ms = 0.f;
+    PT_CUDA_TRY(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+    s->bvh_stats.build_ms = ms;
+    return PT_OK;
+}
+
+int pt_update_world_vertices(pt_scene *s, uint32_t mesh, const float *d_obj_pos, uint32_t nv, cudaStream_t st) {
+    for (const MeshInstanceRef &r : s->mesh_instances) {
+        if (r.mesh != mesh) continue;
+        const float *m = r.to_world;
+        float4 m0 = make_float4(m[0], m[1], m[2], m[3]), m1 = make_float4(m[4], m[5], m[6], m[7]),
+               m2 = make_float4(m[8], m[9], m[10], m[11]);
+        if (nv) k_transform_vertices<<<blocks(nv, 256), 256, 0, st>>>(d_obj_pos, nv, m0, m1, m2, s->vpos.as<float4>() + r.vertex_offset);
+        uint32_t first = r.prim_offset;
+        uint32_t count = 0;
+        // triangles of this instance: up to the next mesh instance's first primitive
+        uint32_t next = s->num_tris;
+        for (const MeshInstanceRef &q : s->mesh_instances)
+            if (q.prim_offset > first && q.prim_offset < next) next = q.prim_offset;
+        count = next - first;
+        if (count) k_rebuild_tri_records<<<blocks(count, 256), 256, 0, st>>>(s->tri_vidx.as<uint32_t>(), s->vpos.as<float4>(),
+                                                                             first, count, s->prims_world.as<float4>());
+    }
+    PT_CUDA_TRY(cudaGetLastError());
+    PT_CUDA_TRY(cudaStreamSynchronize(st));
+    return PT_OK;
+}

@@ -1,0 +1,100 @@
+// pt_internal.h -- host-side state shared by the translation units of
+// libpt_gb300.so.  Not part of the public C-ABI (include/pt_api.h).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/pt_api.h"
+#include "pt_device.cuh"
+
+// Thread-local last error (pt_last_error).
+void pt_set_error(const char *fmt, ...);
+#define PT_CUDA_TRY(expr)                                                                           \
+    do {                                                                                            \
+        cudaError_t e_ = (expr);                                                                    \
+        if (e_ != cudaSuccess) {                                                                    \
+            pt_set_error("%s failed: %s (%s:%d)", #expr, cudaGetErrorString(e_), __FILE__, __LINE__); \
+            return e_ == cudaErrorMemoryAllocation ? PT_ERR_OOM : PT_ERR_CUDA;                      \
+        }                                                                                           \
+    } while (0)
+
+// Device allocation owned by the scene; freed with cudaFree.
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    int ensure(size_t n);  // grow (no copy) to at least n bytes
+    void release();
+    template <class T> T *as() const { return static_cast<T *>(ptr); }
+};
+
+struct pt_context {
+    int device = 0;
+    int num_sms = 0;
+    int max_smem_per_block = 0;
+};
+
+struct MeshInstanceRef {  // where the world vertices of one mesh instance live
+    uint32_t instance;
+    uint32_t mesh;
+    uint32_t vertex_offset;
+    uint32_t prim_offset;
+    float to_world[16];
+};
+
+struct RenderWorkspace {
+    size_t capacity = 0;  // path slots
+    DevBuf ray_o, ray_d, hit, thr, rad, rng, meta, q0, q1, sh_o, sh_d, sh_c, mat_key, counters, sort_tmp;
+};
+
+struct pt_scene {
+    pt_context *ctx = nullptr;
+    pt_scene_desc desc_shallow{};  // sizes only (pointers are not kept)
+    uint32_t num_tris = 0, num_spheres = 0, num_prims = 0;
+    uint32_t num_vertices = 0;
+    std::vector<MeshInstanceRef> mesh_instances;
+    std::vector<uint32_t> mesh_num_vertices;
+    float scene_mag = 1.f;  // max |coordinate| of the scene bounds and the camera
+
+    // host copies used by refit / updates
+    std::vector<float4> h_prims_world;  // 3 per primitive, world order
+
+    // device data
+    DevBuf prims_world;  // 3 float4 per prim (world order)
+    DevBuf prims_bvh;    // 3 float4 per prim (leaf order)
+    DevBuf nodes;
+    DevBuf tri_vidx, vpos, vnrm, vuv, prim_inst, inst, mats, emitters, emitter_cdf;
+    DevBuf mesh_obj_pos;  // scratch for pt_scene_update_vertices
+    // BVH build scratch and results
+    DevBuf bvh_scratch;
+    DevBuf bvh_order;  // primitive id of each leaf slot (sorted Morton order)
+    std::vector<uint32_t> level_start;  // first wide node of each level; back() = num_nodes
+    pt_bvh_opts bvh_opts{};
+    pt_bvh_stats bvh_stats{};
+    bool bvh_built = false;
+
+    ptd::DevScene dev{};
+    RenderWorkspace ws;
+    pt_render_stats render_stats{};
+
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    ~pt_scene();
+};
+
+// pt_bvh.cu
+int pt_bvh_build_impl(pt_scene *s, const pt_bvh_opts *opts, cudaStream_t stream);
+int pt_bvh_refit_impl(pt_scene *s, cudaStream_t stream);
+// pt_render.cu
+int pt_render_impl(pt_scene *s, const pt_render_params *p, const pt_frame_buffers *fb, cudaStream_t stream);
+int pt_trace_rays_impl(pt_scene *s, const float *rays, float *hits, uint32_t n, int anyhit, cudaStream_t stream);
+int pt_bsdf_eval_impl(const float *bsdf, const float *wo, const float *wi, float *f, float *pdf, uint32_t n,
+                      cudaStream_t stream);
+int pt_bsdf_sample_impl(const float *bsdf, const float *wo, uint32_t *rng, float *wi, float *f, float *pdf,
+                        uint32_t *type, uint32_t n, cudaStream_t stream);
+// Re-transforms the world vertices / primitive records of mesh instances on the device.
+int pt_update_world_vertices(pt_scene *s, uint32_t mesh, const float *d_obj_pos, uint32_t num_vertices,
+                             cudaStream_t stream);

@@ -1,0 +1,715 @@
+// pt_render.cu -- wavefront path tracer with NEE and MIS on GB300.
+//
+// Replaces PTPass::OnRun + optixLaunch (example/path_tracer/pt_pass.cpp:
+// 39-57, framework/optix/pass.h:71-89) and the OptiX megakernel
+// __raygen__main / __miss__* / __closesthit__* (example/path_tracer/main.cu:
+// 38-246).  The megakernel's per-path loop is split into kernels over
+// device-resident SoA path state:
+//
+//   raygen      camera rays for every (frame, pixel) slot of a wave
+//   per bounce: extend   closest-hit traversal of the active queue
+//               shade    hit/miss handling, emitter-hit MIS, Russian
+//                        roulette, NEE sample + BSDF eval (shadow queue),
+//                        BSDF sample (next active queue)
+//               shadow   any-hit traversal; unoccluded NEE adds its radiance
+//   accumulate  per pixel, frames in order: the reference's progressive
+//               lerp (main.cu:190-196)
+//
+// Random numbers are drawn per path in exactly the reference's order (2
+// jitter, 1 `test`, then per bounce RR 1, emitter select 1, SampleDirect 2,
+// BSDF Sample 0-3), so a path consumes the same stream as in the megakernel.
+// Queues are compacted with warp ballots and one atomic per block.
+
+#include "pt_internal.h"
+#include "pt_bsdf.cuh"
+#include "pt_traverse.cuh"
+
+#include <algorithm>
+
+namespace {
+using namespace ptd;
+
+enum Counter : int {
+    kNIn = 0,
+    kNOut = 1,
+    kNShadow = 2,
+    kWorkExtend = 3,
+    kWorkShadow = 4,
+    kOverflow = 5,
+    kStatBase = 8,  // uint64 stats at counters + 8 (as uint64 pairs)
+};
+enum Stat : int { kStatExtNodes = 0, kStatExtPrims, kStatShNodes, kStatShPrims, kStatExtRays, kStatShRays, kNumStats };
+
+struct Wave {
+    uint32_t npix;
+    uint32_t frames;       // frames in this wave
+    uint32_t frame0;       // first frame of the wave (relative to the call)
+    uint32_t seed0;        // random seed of the call's first frame
+    uint32_t cnt0;         // sample_cnt of the call's first frame
+    uint32_t last_frame;   // spp - 1: only that frame writes the AOV / test buffers
+    uint32_t max_depth;
+    uint32_t rng_mode;
+    uint32_t accumulate;
+};
+
+struct State {
+    float4 *ray_o, *ray_d, *hit, *thr, *rad;
+    uint2 *rng;
+    uint32_t *meta;
+    uint32_t *q_in, *q_out;
+    float4 *sh_o, *sh_d, *sh_c;
+    uint32_t *counters;
+    unsigned long long *stats;
+};
+
+struct Outputs {
+    float4 *accum, *frame;
+    float *albedo, *normal, *test;
+};
+
+PT_DI void save_rng(uint2 *dst, const Sampler &s) {
+    *dst = make_uint2((uint32_t)s.state, (uint32_t)(s.state >> 32));
+}
+PT_DI Sampler load_rng(const uint2 *src, uint32_t mode, uint32_t frame_seed) {
+    Sampler s;
+    uint2 v = *src;
+    s.mode = mode;
+    s.state = (uint64_t)v.x | ((uint64_t)v.y << 32);
+    s.inc = (static_cast<uint64_t>(frame_seed) << 1u) | 1u;
+    return s;
+}
+
+// Block-aggregated append to two queues: warp ballots give the lane offsets,
+// thread 0 does one atomicAdd per queue for the whole block.  sh: 66 words of
+// shared memory.  Every thread of the block must call it.
+PT_DI void block_push2(bool p0, bool p1, uint32_t *c0, uint32_t *c1, uint32_t &pos0, uint32_t &pos1, uint32_t *sh) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    uint32_t b0 = __ballot_sync(0xffffffffu, p0), b1 = __ballot_sync(0xffffffffu, p1);
+    uint32_t *wc0 = sh, *wc1 = sh + 32, *base = sh + 64;
+    if (lane == 0) {
+        wc0[warp] = __popc(b0);
+        wc1[warp] = __popc(b1);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t s0 = 0, s1 = 0;
+        for (int w = 0; w < nw; w++) {
+            uint32_t a = wc0[w], b = wc1[w];
+            wc0[w] = s0;
+            wc1[w] = s1;
+            s0 += a;
+            s1 += b;
+        }
+        base[0] = s0 ? atomicAdd(c0, s0) : 0;
+        base[1] = s1 ? atomicAdd(c1, s1) : 0;
+    }
+    __syncthreads();
+    uint32_t lt = (1u << lane) - 1u;
+    pos0 = base[0] + wc0[warp] + __popc(b0 & lt);
+    pos1 = base[1] + wc1[warp] + __popc(b1 & lt);
+    __syncthreads();
+}
+
+// Camera ray, example/path_tracer/main.cu:58-78.
+PT_DI void camera_ray(const DevScene &s, uint32_t x, uint32_t y, Sampler &rng, float3 &o, float3 &d) {
+    float jx = rng.next();
+    float jy = rng.next();
+    float u = (static_cast<float>(x) + jx) / static_cast<float>(s.width_px);
+    float v = (static_cast<float>(y) + jy) / static_cast<float>(s.height_px);
+    float4 pf = make_float4(u, v, 0.f, 1.f);
+    float4 dd = make_float4(dot4(s.s2c[0], pf), dot4(s.s2c[1], pf), dot4(s.s2c[2], pf), dot4(s.s2c[3], pf));
+    float inv = 1.0f / dd.w;
+    dd = make_float4(dd.x * inv, dd.y * inv, dd.z * inv, dd.w * inv);
+    dd.w = 0.f;
+    dd = normalize4(dd);
+    float3 dw = f3(dot4(s.c2w[0], dd), dot4(s.c2w[1], dd), dot4(s.c2w[2], dd));
+    d = normalize(dw);
+    o = f3(s.c2w[0].w, s.c2w[1].w, s.c2w[2].w);
+}
+
+__global__ void k_raygen(DevScene s, State st, Wave w) {
+    const uint32_t total = w.frames * w.npix;
+    for (uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x; slot < total; slot += gridDim.x * blockDim.x) {
+        uint32_t fl = slot / w.npix, p = slot - fl * w.npix;
+        Sampler rng;
+        rng.init(w.rng_mode, p, w.seed0 + w.frame0 + fl);
+        float3 o, d;
+        camera_ray(s, p % s.width_px, p / s.width_px, rng, o, d);
+        st.ray_o[slot] = make_float4(o.x, o.y, o.z, 0.001f);
+        st.ray_d[slot] = make_float4(d.x, d.y, d.z, 1e16f);
+        st.thr[slot] = make_float4(1.f, 1.f, 1.f, 0.f);
+        st.rad[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
+        save_rng(st.rng + slot, rng);
+        st.meta[slot] = 0;
+        st.q_in[slot] = slot;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        st.counters[kNIn] = total;
+        st.counters[kNOut] = 0;
+        st.counters[kNShadow] = 0;
+        st.counters[kWorkExtend] = 0;
+        st.counters[kWorkShadow] = 0;
+    }
+}
+
+// Queue hand-over between bounces: the next active queue becomes the input.
+__global__ void k_advance(uint32_t *counters) {
+    counters[kNIn] = counters[kNOut];
+    counters[kNOut] = 0;
+    counters[kNShadow] = 0;
+    counters[kWorkExtend] = 0;
+    counters[kWorkShadow] = 0;
+}
+
+template <int K>
+PT_DI size_t smem_node_bytes(const DevScene &s) {
+    return (size_t)s.smem_nodes * 32 * K;
+}
+
+// Persistent traversal over a queue: warps take 32 entries at a time.
+// ANY = false: closest hit of the extension rays (q_in entries are path slots).
+// ANY = true: shadow rays (entries are shadow-queue positions).
+template <int K, bool ANY, bool COUNT>
+__global__ void k_trace_queue(DevScene s, State st) {
+    extern __shared__ float4 smem[];
+    float4 *snodes = smem;
+    int2 *sstack = reinterpret_cast<int2 *>(smem + s.smem_nodes * 2 * K);
+    for (uint32_t i = threadIdx.x; i < s.smem_nodes * 2 * K; i += blockDim.x) snodes[i] = __ldg(s.nodes + i);
+    __syncthreads();
+    const uint32_t n = ANY ? st.counters[kNShadow] : st.counters[kNIn];
+    uint32_t *work = st.counters + (ANY ? kWorkShadow : kWorkExtend);
+    const int lane = threadIdx.x & 31;
+    uint32_t nodes = 0, prims = 0, ovf = 0, rays = 0;
+    for (;;) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(work, 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
+        uint32_t i = base + lane;
+        if (i < n) {
+            float4 o4, d4;
+            uint32_t slot = 0;
+            if (ANY) {
+                o4 = st.sh_o[i];
+                d4 = st.sh_d[i];
+            } else {
+                slot = st.q_in[i];
+                o4 = st.ray_o[slot];
+                d4 = st.ray_d[slot];
+            }
+            TraceResult r = traverse<K, ANY, COUNT>(s, snodes, sstack + threadIdx.x, xyz(o4), xyz(d4), o4.w, d4.w, nodes,
+                                                    prims, ovf);
+            if (COUNT) rays++;
+            if (ANY) {
+                if (r.prim < 0) {  // unoccluded: add the NEE contribution
+                    float4 c = st.sh_c[i];
+                    uint32_t ps = __float_as_uint(c.w);
+                    float4 rr = st.rad[ps];
+                    st.rad[ps] = make_float4(rr.x + c.x, rr.y + c.y, rr.z + c.z, rr.w);
+                }
+            } else {
+                st.hit[slot] = make_float4(r.t, __int_as_float(r.prim), r.u, r.v);
+            }
+        }
+    }
+    if (ovf) atomicOr(st.counters + kOverflow, 1u);
+    if (COUNT) {
+        for (int o = 16; o > 0; o >>= 1) {
+            nodes += __shfl_xor_sync(0xffffffffu, nodes, o);
+            prims += __shfl_xor_sync(0xffffffffu, prims, o);
+            rays += __shfl_xor_sync(0xffffffffu, rays, o);
+        }
+        if (lane == 0) {
+            atomicAdd(st.stats + (ANY ? kStatShNodes : kStatExtNodes), (unsigned long long)nodes);
+            atomicAdd(st.stats + (ANY ? kStatShPrims : kStatExtPrims), (unsigned long long)prims);
+            atomicAdd(st.stats + (ANY ? kStatShRays : kStatExtRays), (unsigned long long)rays);
+        }
+    }
+}
+
+struct HitGeo {
+    float3 pos, nrm;
+    float2 uv;
+};
+
+// Geometry::GetHitLocalGeometry (framework/render/geometry.h:60-100,176-180)
+// on world-space data.
+PT_DI void hit_geometry(const DevScene &s, float4 h, float3 o, float3 d, const DevInstance &in, bool twosided, HitGeo &g) {
+    int prim = __float_as_int(h.y);
+    if (!(in.flags & kInstSphere)) {
+        uint32_t i0 = s.tri_vidx[3 * prim], i1 = s.tri_vidx[3 * prim + 1], i2 = s.tri_vidx[3 * prim + 2];
+        float3 p0 = xyz(s.vpos[i0]), p1 = xyz(s.vpos[i1]), p2 = xyz(s.vpos[i2]);
+        float u = h.z, v = h.w;
+        float w0 = 1.f - u - v;
+        g.pos = w0 * p0 + u * p1 + v * p2;
+        float3 n;
+        if (in.flags & kInstHasNormals) n = w0 * xyz(s.vnrm[i0]) + u * xyz(s.vnrm[i1]) + v * xyz(s.vnrm[i2]);
+        else n = cross(p1 - p0, p2 - p0);
+        g.nrm = normalize(n);
+        if (in.flags & PT_INST_FLIP_NORMALS) g.nrm = g.nrm * -1.f;
+        if (in.flags & kInstHasUvs) {
+            g.uv = s.vuv[i0] * w0 + s.vuv[i1] * u + s.vuv[i2] * v;
+            if (in.flags & PT_INST_FLIP_TEXCOORDS) g.uv.y = 1.f - g.uv.y;
+        } else {
+            g.uv = make_float2(0.f, 0.f);
+        }
+    } else {
+        g.pos = o + h.x * d;
+        float3 local = f3(dot4(in.inv0, make_float4(g.pos.x, g.pos.y, g.pos.z, 1.f)),
+                          dot4(in.inv1, make_float4(g.pos.x, g.pos.y, g.pos.z, 1.f)),
+                          dot4(in.inv2, make_float4(g.pos.x, g.pos.y, g.pos.z, 1.f)));
+        g.nrm = normalize(g.pos - xyz(in.sphere));
+        g.uv = sphere_texcoord(normalize(local - xyz(in.obj_center)));
+        if (in.flags & PT_INST_FLIP_NORMALS) g.nrm = g.nrm * -1.f;
+    }
+    if (dot(-d, g.nrm) < 0.f && twosided) g.nrm = -g.nrm;
+}
+
+// One bounce of shading for every entry of the active queue.
+__global__ void __launch_bounds__(256) k_shade(DevScene s, State st, Wave w, Outputs out) {
+    __shared__ uint32_t push_smem[72];
+    const uint32_t n = st.counters[kNIn];
+    const float env_pdf = 0.25f * kInvPi;  // ConstEnvEmitter::Eval (env.h:82-85)
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        uint32_t i = base + threadIdx.x;
+        bool valid = i < n;
+        bool push_ext = false, push_sh = false;
+        uint32_t slot = 0;
+        float3 hit_pos = f3s(0.f), new_d = f3s(0.f), sh_d = f3s(0.f), sh_c = f3s(0.f);
+        float sh_tmax = 0.f;
+        if (valid) {
+            slot = st.q_in[i];
+            uint32_t meta = st.meta[slot];
+            uint32_t depth = meta & 0xffffu;
+            bool prev_delta = (meta >> 16) & 1u;
+            uint32_t fl = slot / w.npix, p = slot - fl * w.npix;
+            uint32_t frame = w.frame0 + fl;
+            bool last = frame == w.last_frame;
+            float4 h = st.hit[slot];
+            float3 ro = xyz(st.ray_o[slot]), rd = xyz(st.ray_d[slot]);
+            float4 t4 = st.thr[slot];
+            float3 thr = xyz(t4);
+            float prev_pdf = t4.w;
+            float4 r4 = st.rad[slot];
+            float3 rad = xyz(r4);
+            Sampler rng = load_rng(st.rng + slot, w.rng_mode, w.seed0 + frame);
+            int prim = __float_as_int(h.y);
+            bool alive = prim >= 0;
+            HitGeo g;
+            LocalBsdf bsdf;
+            if (!alive) {  // __miss__default (main.cu:199-215)
+                if (s.has_env) {
+                    float3 le = xyz(s.env.rad);
+                    if (depth == 0) rad = rad + le;
+                    else rad = rad + le * (thr * mis_weight(prev_pdf, env_pdf));
+                }
+                if (depth == 0 && last) {
+                    if (out.albedo) { out.albedo[3 * p] = 0.f; out.albedo[3 * p + 1] = 0.f; out.albedo[3 * p + 2] = 0.f; }
+                    if (out.normal) { out.normal[3 * p] = 0.f; out.normal[3 * p + 1] = 0.f; out.normal[3 * p + 2] = 0.f; }
+                }
+            } else {  // ClosestHit (main.cu:220-234)
+                const DevInstance &in = s.inst[s.prim_inst[prim]];
+                const DevMaterial &m = s.mats[in.material];
+                hit_geometry(s, h, ro, rd, in, m.twosided != 0, g);
+                bsdf = material_local(m, g.uv);
+                int ei = in.emitter_offset >= 0 ? in.emitter_offset + (prim - (int)in.prim_offset) : -1;
+                if (depth == 0) {  // main.cu:90-98
+                    if (ei >= 0) rad = rad + xyz(s.emitters[ei].rad);
+                    if (last) {
+                        float3 al = bsdf.albedo();
+                        if (out.albedo) { out.albedo[3 * p] = al.x; out.albedo[3 * p + 1] = al.y; out.albedo[3 * p + 2] = al.z; }
+                        if (out.normal) { out.normal[3 * p] = g.nrm.x; out.normal[3 * p + 1] = g.nrm.y; out.normal[3 * p + 2] = g.nrm.z; }
+                    }
+                } else if (ei >= 0) {  // emitter hit with MIS (main.cu:175-185)
+                    const DevEmitter &e = s.emitters[ei];
+                    float epdf = emitter_eval_pdf(e, g.pos, g.nrm, ro);
+                    if (!is_zero(epdf)) {
+                        float mis = prev_delta ? 1.f : mis_weight(prev_pdf, epdf * e.a.y);
+                        rad = rad + thr * xyz(e.rad) * mis;
+                    }
+                }
+            }
+            if (depth == 0) {  // main.cu:104
+                float tv = rng.next();
+                if (last && out.test) out.test[p] = tv;
+            }
+            if (alive) {  // main.cu:107-109
+                depth++;
+                if (depth >= w.max_depth) alive = false;
+            }
+            if (alive) {  // Russian roulette, main.cu:111-114
+                float rr = depth > 2 ? 0.95f : 1.0f;
+                if (rng.next() > rr) alive = false;
+                else thr = thr / rr;
+            }
+            if (alive) {  // next-event estimation, main.cu:117-144
+                float sel = rng.next();
+                float2 xi = rng.next2();
+                int ei = select_emitter(s, sel);
+                if (ei != -2) {
+                    const DevEmitter &e = ei >= 0 ? s.emitters[ei] : s.env;
+                    EmitterSample es;
+                    emitter_sample_direct(e, g.pos, g.nrm, xi, es);
+                    if (es.pdf != 0.f) {
+                        BsdfRecord er;
+                        er.wi = to_local(es.wi, g.nrm);
+                        er.wo = to_local(-rd, g.nrm);
+                        er.f = f3s(0.f);
+                        er.pdf = 0.f;
+                        er.type = 0;
+                        bsdf.eval(er);
+                        if (!is_zero(er.f * es.pdf)) {
+                            float NoL = dot(g.nrm, es.wi);
+                            if (NoL > 0.f) {
+                                float mis = mis_weight(es.pdf, er.pdf);
+                                float pdf = es.pdf * e.a.y;
+                                sh_c = thr * es.radiance * er.f * NoL * mis / pdf;
+                                sh_d = es.wi;
+                                sh_tmax = es.distance - 0.0001f;
+                                push_sh = true;
+                            }
+                        }
+                    }
+                }
+            }
+            if (alive) {  // BSDF sampling, main.cu:146-166
+                BsdfRecord br;
+                br.wo = to_local(-rd, g.nrm);
+                br.wi = f3s(0.f);
+                br.f = f3s(0.f);
+                br.pdf = 0.f;
+                br.type = 0;
+                bsdf.sample(br, rng);
+                if (is_zero(br.f * fabsf(br.wi.z)) || is_zero(br.pdf)) {
+                    alive = false;
+                } else {
+                    thr = thr * (br.f * fabsf(br.wi.z) / br.pdf);
+                    new_d = to_world(br.wi, g.nrm);
+                    prev_pdf = br.pdf;
+                    prev_delta = (br.type & kDelta) != 0;
+                    push_ext = true;
+                }
+            }
+            if (prim >= 0) hit_pos = g.pos;
+            st.rad[slot] = make_float4(rad.x, rad.y, rad.z, r4.w);
+            if (alive) {
+                st.thr[slot] = make_float4(thr.x, thr.y, thr.z, prev_pdf);
+                st.meta[slot] = depth | (prev_delta ? (1u << 16) : 0u);
+                save_rng(st.rng + slot, rng);
+                st.ray_o[slot] = make_float4(hit_pos.x, hit_pos.y, hit_pos.z, 0.001f);
+                st.ray_d[slot] = make_float4(new_d.x, new_d.y, new_d.z, 1e16f);
+            }
+        }
+        uint32_t pos_ext, pos_sh;
+        block_push2(push_ext, push_sh, st.counters + kNOut, st.counters + kNShadow, pos_ext, pos_sh, push_smem);
+        if (push_ext) st.q_out[pos_ext] = slot;
+        if (push_sh) {  // shadow ray from the hit point, tmin 1e-4, tmax distance - 1e-4 (main.cu:122-126)
+            st.sh_o[pos_sh] = make_float4(hit_pos.x, hit_pos.y, hit_pos.z, 0.0001f);
+            st.sh_d[pos_sh] = make_float4(sh_d.x, sh_d.y, sh_d.z, sh_tmax);
+            st.sh_c[pos_sh] = make_float4(sh_c.x, sh_c.y, sh_c.z, __uint_as_float(slot));
+        }
+    }
+}
+
+
+// Accumulation, main.cu:188-196: frames of the wave in order, per pixel.
+__global__ void k_accumulate(State st, Wave w, Outputs out) {
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < w.npix; p += gridDim.x * blockDim.x) {
+        float4 acc = out.accum[p];
+        float3 a = xyz(acc);
+        for (uint32_t fl = 0; fl < w.frames; fl++) {
+            float3 L = xyz(st.rad[(size_t)fl * w.npix + p]);
+            uint32_t cnt = w.cnt0 + w.frame0 + fl;
+            if (w.accumulate && cnt > 0) {
+                const float t = 1.f / (cnt + 1.f);
+                L = lerp(a, L, t);
+            }
+            a = L;
+        }
+        out.accum[p] = make_float4(a.x, a.y, a.z, 1.f);
+        if (out.frame) out.frame[p] = make_float4(a.x, a.y, a.z, 1.f);
+    }
+}
+
+// pt_trace_rays: rays (ox,oy,oz,tmin, dx,dy,dz,tmax) -> hits.
+template <int K, bool ANY>
+__global__ void k_trace_rays(DevScene s, const float4 *rays, float4 *hits, uint32_t n, uint32_t *work, uint32_t *ovf_flag) {
+    extern __shared__ float4 smem[];
+    float4 *snodes = smem;
+    int2 *sstack = reinterpret_cast<int2 *>(smem + s.smem_nodes * 2 * K);
+    for (uint32_t i = threadIdx.x; i < s.smem_nodes * 2 * K; i += blockDim.x) snodes[i] = __ldg(s.nodes + i);
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    uint32_t nn = 0, np = 0, ovf = 0;
+    for (;;) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(work, 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
+        uint32_t i = base + lane;
+        if (i < n) {
+            float4 o4 = rays[2 * (size_t)i], d4 = rays[2 * (size_t)i + 1];
+            TraceResult r = traverse<K, ANY, false>(s, snodes, sstack + threadIdx.x, xyz(o4), xyz(d4), o4.w, d4.w, nn, np, ovf);
+            if (ANY) hits[i] = make_float4(r.prim >= 0 ? 1.f : 0.f, 0.f, 0.f, 0.f);
+            else hits[i] = make_float4(r.prim >= 0 ? r.t : d4.w, __int_as_float(r.prim), r.prim >= 0 ? r.u : 0.f, r.prim >= 0 ? r.v : 0.f);
+        }
+    }
+    if (ovf) atomicOr(ovf_flag, 1u);
+}
+
+__global__ void k_bsdf_eval(const float *bsdf, const float *wo, const float *wi, float *f, float *pdf, uint32_t n) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    LocalBsdf l = LocalBsdf::from_flat(bsdf + 16 * (size_t)i);
+    BsdfRecord r;
+    r.wo = f3(wo[3 * i], wo[3 * i + 1], wo[3 * i + 2]);
+    r.wi = f3(wi[3 * i], wi[3 * i + 1], wi[3 * i + 2]);
+    r.f = f3s(0.f);
+    r.pdf = 0.f;
+    r.type = 0;
+    l.eval(r);
+    f[3 * i] = r.f.x;
+    f[3 * i + 1] = r.f.y;
+    f[3 * i + 2] = r.f.z;
+    pdf[i] = r.pdf;
+}
+
+__global__ void k_bsdf_sample(const float *bsdf, const float *wo, uint32_t *rng, float *wi, float *f, float *pdf,
+                              uint32_t *type, uint32_t n) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    LocalBsdf l = LocalBsdf::from_flat(bsdf + 16 * (size_t)i);
+    Sampler smp;
+    smp.mode = PT_RNG_REF_LCG;
+    smp.inc = 0;
+    smp.state = rng[i];
+    BsdfRecord r;
+    r.wo = f3(wo[3 * i], wo[3 * i + 1], wo[3 * i + 2]);
+    r.wi = f3s(0.f);
+    r.f = f3s(0.f);
+    r.pdf = 0.f;
+    r.type = 0;
+    l.sample(r, smp);
+    rng[i] = (uint32_t)smp.state;
+    wi[3 * i] = r.wi.x;
+    wi[3 * i + 1] = r.wi.y;
+    wi[3 * i + 2] = r.wi.z;
+    f[3 * i] = r.f.x;
+    f[3 * i + 1] = r.f.y;
+    f[3 * i + 2] = r.f.z;
+    pdf[i] = r.pdf;
+    type[i] = r.type;
+}
+
+inline uint32_t nblocks(size_t n, int b) { return (uint32_t)std::max<size_t>(1, (n + b - 1) / b); }
+
+template <class F>
+int set_smem(F kernel, size_t bytes) {
+    if (bytes > 48 * 1024) PT_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    return PT_OK;
+}
+
+// Events for per-kernel timing (PT_RENDER_KERNEL_TIMING).
+struct Timer {
+    std::vector<cudaEvent_t> ev;
+    std::vector<int> kind;
+    size_t used = 0;
+    ~Timer() {
+        for (auto e : ev) cudaEventDestroy(e);
+    }
+    void mark(int k, cudaStream_t st) {  // call twice per interval (start, end)
+        if (used >= ev.size()) {
+            cudaEvent_t e;
+            cudaEventCreate(&e);
+            ev.push_back(e);
+            kind.push_back(0);
+        }
+        kind[used] = k;
+        cudaEventRecord(ev[used++], st);
+    }
+};
+
+template <int K>
+struct Launcher {
+    static int run(pt_scene *s, const pt_render_params *p, const pt_frame_buffers *fb, cudaStream_t st) {
+        const DevScene &d = s->dev;
+        RenderWorkspace &ws = s->ws;
+        const uint32_t npix = d.width_px * d.height_px;
+        const uint32_t max_depth = p->max_depth ? p->max_depth : s->desc_shallow.max_depth;
+        const bool count = (p->flags & PT_RENDER_COUNTERS) != 0;
+        const bool timing = (p->flags & PT_RENDER_KERNEL_TIMING) != 0;
+        uint32_t frames_per_wave = p->wave_spp;
+        if (frames_per_wave == 0) frames_per_wave = std::max<uint32_t>(1, (uint32_t)(16u * 1024u * 1024u / std::max<uint32_t>(npix, 1)));
+        frames_per_wave = std::max<uint32_t>(1, std::min(frames_per_wave, std::max<uint32_t>(p->spp, 1)));
+        const size_t cap = (size_t)frames_per_wave * npix;
+        if (ws.capacity < cap) {
+            int e;
+            if ((e = ws.ray_o.ensure(16 * cap)) || (e = ws.ray_d.ensure(16 * cap)) || (e = ws.hit.ensure(16 * cap)) ||
+                (e = ws.thr.ensure(16 * cap)) || (e = ws.rad.ensure(16 * cap)) || (e = ws.rng.ensure(8 * cap)) ||
+                (e = ws.meta.ensure(4 * cap)) || (e = ws.q0.ensure(4 * cap)) || (e = ws.q1.ensure(4 * cap)) ||
+                (e = ws.sh_o.ensure(16 * cap)) || (e = ws.sh_d.ensure(16 * cap)) || (e = ws.sh_c.ensure(16 * cap)))
+                return e;
+            ws.capacity = cap;
+        }
+        int e = ws.counters.ensure(256);
+        if (e != PT_OK) return e;
+        State stt;
+        stt.ray_o = ws.ray_o.as<float4>();
+        stt.ray_d = ws.ray_d.as<float4>();
+        stt.hit = ws.hit.as<float4>();
+        stt.thr = ws.thr.as<float4>();
+        stt.rad = ws.rad.as<float4>();
+        stt.rng = ws.rng.as<uint2>();
+        stt.meta = ws.meta.as<uint32_t>();
+        stt.sh_o = ws.sh_o.as<float4>();
+        stt.sh_d = ws.sh_d.as<float4>();
+        stt.sh_c = ws.sh_c.as<float4>();
+        stt.counters = ws.counters.as<uint32_t>();
+        stt.stats = reinterpret_cast<unsigned long long *>(ws.counters.as<uint32_t>() + kStatBase * 2);
+        Outputs out;
+        out.accum = reinterpret_cast<float4 *>(fb->accum);
+        out.frame = reinterpret_cast<float4 *>(fb->frame);
+        out.albedo = fb->albedo;
+        out.normal = fb->normal;
+        out.test = fb->test;
+
+        const int tb = p->block_size ? (int)p->block_size : 128;
+        const size_t smem = (size_t)d.smem_nodes * 32 * K + (size_t)kShortStack * 8 * tb;
+        auto k_ext = count ? k_trace_queue<K, false, true> : k_trace_queue<K, false, false>;
+        auto k_sh = count ? k_trace_queue<K, true, true> : k_trace_queue<K, true, false>;
+        if ((e = set_smem(k_ext, smem)) != PT_OK || (e = set_smem(k_sh, smem)) != PT_OK) return e;
+        int occ_t = 0, occ_s = 0;
+        PT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_t, k_ext, tb, smem));
+        PT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, k_shade, 256, 0));
+        const uint32_t grid_trace = (uint32_t)std::max(1, occ_t) * s->ctx->num_sms;
+        const uint32_t grid_shade = (uint32_t)std::max(1, occ_s) * s->ctx->num_sms;
+
+        PT_CUDA_TRY(cudaMemsetAsync(ws.counters.ptr, 0, 256, st));
+        Timer tm;
+        uint32_t launches = 1;
+        PT_CUDA_TRY(cudaEventRecord(s->ev0, st));
+        uint32_t waves = 0;
+        for (uint32_t f0 = 0; f0 < p->spp; f0 += frames_per_wave) {
+            Wave w;
+            w.npix = npix;
+            w.frames = std::min(frames_per_wave, p->spp - f0);
+            w.frame0 = f0;
+            w.seed0 = p->seed;
+            w.cnt0 = p->sample_cnt;
+            w.last_frame = p->spp - 1;
+            w.max_depth = max_depth;
+            w.rng_mode = p->rng;
+            w.accumulate = p->accumulate;
+            stt.q_in = ws.q0.as<uint32_t>();
+            stt.q_out = ws.q1.as<uint32_t>();
+            const size_t slots = (size_t)w.frames * npix;
+            k_raygen<<<nblocks(slots, 256), 256, 0, st>>>(d, stt, w);
+            launches++;
+            for (uint32_t b = 0; b < max_depth; b++) {
+                if (timing) tm.mark(0, st);
+                k_ext<<<grid_trace, tb, smem, st>>>(d, stt);
+                if (timing) { tm.mark(0, st); tm.mark(2, st); }
+                k_shade<<<grid_shade, 256, 0, st>>>(d, stt, w, out);
+                if (timing) { tm.mark(2, st); tm.mark(1, st); }
+                k_sh<<<grid_trace, tb, smem, st>>>(d, stt);
+                if (timing) tm.mark(1, st);
+                k_advance<<<1, 1, 0, st>>>(stt.counters);
+                launches += 4;
+                std::swap(stt.q_in, stt.q_out);
+            }
+            k_accumulate<<<nblocks(npix, 256), 256, 0, st>>>(stt, w, out);
+            launches++;
+            waves++;
+        }
+        PT_CUDA_TRY(cudaGetLastError());
+        PT_CUDA_TRY(cudaEventRecord(s->ev1, st));
+        PT_CUDA_TRY(cudaEventSynchronize(s->ev1));
+        pt_render_stats &rs = s->render_stats;
+        rs = pt_render_stats{};
+        PT_CUDA_TRY(cudaEventElapsedTime(&rs.render_ms, s->ev0, s->ev1));
+        for (size_t i = 0; i + 1 < tm.used; i += 2) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, tm.ev[i], tm.ev[i + 1]);
+            if (tm.kind[i] == 0) { rs.extend_ms += ms; rs.extend_launches++; }
+            else if (tm.kind[i] == 1) { rs.shadow_ms += ms; rs.shadow_launches++; }
+            else { rs.shade_ms += ms; rs.shade_launches++; }
+        }
+        uint32_t hc[8 + 2 * kNumStats] = {};
+        PT_CUDA_TRY(cudaMemcpy(hc, ws.counters.ptr, sizeof(hc), cudaMemcpyDeviceToHost));
+        const unsigned long long *hs = reinterpret_cast<const unsigned long long *>(hc + kStatBase);
+        rs.samples = (uint64_t)npix * p->spp;
+        rs.nodes_visited = hs[kStatExtNodes];
+        rs.prims_tested = hs[kStatExtPrims];
+        rs.shadow_nodes_visited = hs[kStatShNodes];
+        rs.shadow_prims_tested = hs[kStatShPrims];
+        rs.extension_rays = hs[kStatExtRays];
+        rs.shadow_rays = hs[kStatShRays];
+        rs.kernel_launches = launches;
+        rs.waves = waves;
+        rs.overflow = hc[kOverflow];
+        if (rs.overflow) {
+            pt_set_error("traversal stack overflow");
+            return PT_ERR_OOB;
+        }
+        return PT_OK;
+    }
+
+    static int trace(pt_scene *s, const float *rays, float *hits, uint32_t n, int anyhit, cudaStream_t st) {
+        const DevScene &d = s->dev;
+        int e = s->ws.counters.ensure(256);
+        if (e != PT_OK) return e;
+        const int tb = 128;
+        const size_t smem = (size_t)d.smem_nodes * 32 * K + (size_t)kShortStack * 8 * tb;
+        auto kern = anyhit ? k_trace_rays<K, true> : k_trace_rays<K, false>;
+        if ((e = set_smem(kern, smem)) != PT_OK) return e;
+        int occ = 0;
+        PT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, tb, smem));
+        uint32_t *c = s->ws.counters.as<uint32_t>();
+        PT_CUDA_TRY(cudaMemsetAsync(c, 0, 256, st));
+        if (n) kern<<<(uint32_t)std::max(1, occ) * s->ctx->num_sms, tb, smem, st>>>(
+            d, reinterpret_cast<const float4 *>(rays), reinterpret_cast<float4 *>(hits), n, c + kWorkExtend, c + kOverflow);
+        PT_CUDA_TRY(cudaGetLastError());
+        uint32_t ovf = 0;
+        PT_CUDA_TRY(cudaMemcpyAsync(&ovf, c + kOverflow, 4, cudaMemcpyDeviceToHost, st));
+        PT_CUDA_TRY(cudaStreamSynchronize(st));
+        if (ovf) {
+            pt_set_error("traversal stack overflow");
+            return PT_ERR_OOB;
+        }
+        return PT_OK;
+    }
+};
+
+}  // namespace
+
+int pt_render_impl(pt_scene *s, const pt_render_params *p, const pt_frame_buffers *fb, cudaStream_t st) {
+    if (p->spp == 0) return PT_OK;
+    switch (s->dev.width) {
+        case 2: return Launcher<2>::run(s, p, fb, st);
+        case 4: return Launcher<4>::run(s, p, fb, st);
+        default: return Launcher<8>::run(s, p, fb, st);
+    }
+}
+
+int pt_trace_rays_impl(pt_scene *s, const float *rays, float *hits, uint32_t n, int anyhit, cudaStream_t st) {
+    switch (s->dev.width) {
+        case 2: return Launcher<2>::trace(s, rays, hits, n, anyhit, st);
+        case 4: return Launcher<4>::trace(s, rays, hits, n, anyhit, st);
+        default: return Launcher<8>::trace(s, rays, hits, n, anyhit, st);
+    }
+}
+
+int pt_bsdf_eval_impl(const float *bsdf, const float *wo, const float *wi, float *f, float *pdf, uint32_t n, cudaStream_t st) {
+    if (n) k_bsdf_eval<<<nblocks(n, 128), 128, 0, st>>>(bsdf, wo, wi, f, pdf, n);
+    PT_CUDA_TRY(cudaGetLastError());
+    PT_CUDA_TRY(cudaStreamSynchronize(st));
+    return PT_OK;
+}
+
+int pt_bsdf_sample_impl(const float *bsdf, const float *wo, uint32_t *rng, float *wi, float *f, float *pdf, uint32_t *type,
+                        uint32_t n, cudaStream_t st) {
+    if (n) k_bsdf_sample<<<nblocks(n, 128), 128, 0, st>>>(bsdf, wo, rng, wi, f, pdf, type, n);
+    PT_CUDA_TRY(cudaGetLastError());
+    PT_CUDA_TRY(cudaStreamSynchronize(st));
+    return PT_OK;
+}

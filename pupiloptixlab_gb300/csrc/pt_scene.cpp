@@ -1,0 +1,639 @@
+// pt_scene.cpp -- C-ABI glue, context, scene flattening and upload.
+//
+// Scene set-up replaces world::World::LoadScene (framework/world/world.cpp:
+// 108-146), RenderObject (framework/world/render_object.cpp:10-65), the
+// emitter table builder (framework/world/emitter.cpp:169-243,321-390) and the
+// camera upload (framework/world/camera.cpp:72-92).  Instances are flattened
+// to world space here, on the host, with contraction disabled, so that the
+// world-space triangles are bit-identical to the CPU oracle's.
+
+#include "pt_internal.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+
+namespace {
+thread_local std::string g_last_error;
+
+using ptd::DevEmitter;
+using ptd::DevInstance;
+using ptd::DevMaterial;
+using ptd::DevTexture;
+
+struct H3 {
+    float x, y, z;
+};
+inline H3 h3(float x, float y, float z) { return {x, y, z}; }
+inline H3 sub(H3 a, H3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline float hdot(H3 a, H3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline H3 hcross(H3 a, H3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+inline float hlen(H3 v) { return sqrtf(hdot(v, v)); }
+
+// util::Transform::TransformPoint (framework/util/transform.cpp:100-107) for affine matrices.
+inline H3 xform_point(const float m[16], H3 p) {
+    return {m[0] * p.x + m[1] * p.y + m[2] * p.z + m[3], m[4] * p.x + m[5] * p.y + m[6] * p.z + m[7],
+            m[8] * p.x + m[9] * p.y + m[10] * p.z + m[11]};
+}
+inline H3 xform_vec(const float n[9], H3 v) {
+    return {n[0] * v.x + n[1] * v.y + n[2] * v.z, n[3] * v.x + n[4] * v.y + n[5] * v.z, n[6] * v.x + n[7] * v.y + n[8] * v.z};
+}
+
+void inverse4(const double *a, double out[16]) {  // cofactor inverse in double
+    double inv[16];
+    inv[0] = a[5] * a[10] * a[15] - a[5] * a[11] * a[14] - a[9] * a[6] * a[15] + a[9] * a[7] * a[14] + a[13] * a[6] * a[11] - a[13] * a[7] * a[10];
+    inv[4] = -a[4] * a[10] * a[15] + a[4] * a[11] * a[14] + a[8] * a[6] * a[15] - a[8] * a[7] * a[14] - a[12] * a[6] * a[11] + a[12] * a[7] * a[10];
+    inv[8] = a[4] * a[9] * a[15] - a[4] * a[11] * a[13] - a[8] * a[5] * a[15] + a[8] * a[7] * a[13] + a[12] * a[5] * a[11] - a[12] * a[7] * a[9];
+    inv[12] = -a[4] * a[9] * a[14] + a[4] * a[10] * a[13] + a[8] * a[5] * a[14] - a[8] * a[6] * a[13] - a[12] * a[5] * a[10] + a[12] * a[6] * a[9];
+    inv[1] = -a[1] * a[10] * a[15] + a[1] * a[11] * a[14] + a[9] * a[2] * a[15] - a[9] * a[3] * a[14] - a[13] * a[2] * a[11] + a[13] * a[3] * a[10];
+    inv[5] = a[0] * a[10] * a[15] - a[0] * a[11] * a[14] - a[8] * a[2] * a[15] + a[8] * a[3] * a[14] + a[12] * a[2] * a[11] - a[12] * a[3] * a[10];
+    inv[9] = -a[0] * a[9] * a[15] + a[0] * a[11] * a[13] + a[8] * a[1] * a[15] - a[8] * a[3] * a[13] - a[12] * a[1] * a[11] + a[12] * a[3] * a[9];
+    inv[13] = a[0] * a[9] * a[14] - a[0] * a[10] * a[13] - a[8] * a[1] * a[14] + a[8] * a[2] * a[13] + a[12] * a[1] * a[10] - a[12] * a[2] * a[9];
+    inv[2] = a[1] * a[6] * a[15] - a[1] * a[7] * a[14] - a[5] * a[2] * a[15] + a[5] * a[3] * a[14] + a[13] * a[2] * a[7] - a[13] * a[3] * a[6];
+    inv[6] = -a[0] * a[6] * a[15] + a[0] * a[7] * a[14] + a[4] * a[2] * a[15] - a[4] * a[3] * a[14] - a[12] * a[2] * a[7] + a[12] * a[3] * a[6];
+    inv[10] = a[0] * a[5] * a[15] - a[0] * a[7] * a[13] - a[4] * a[1] * a[15] + a[4] * a[3] * a[13] + a[12] * a[1] * a[7] - a[12] * a[3] * a[5];
+    inv[14] = -a[0] * a[5] * a[14] + a[0] * a[6] * a[13] + a[4] * a[1] * a[14] - a[4] * a[2] * a[13] - a[12] * a[1] * a[6] + a[12] * a[2] * a[5];
+    inv[3] = -a[1] * a[6] * a[11] + a[1] * a[7] * a[10] + a[5] * a[2] * a[11] - a[5] * a[3] * a[10] - a[9] * a[2] * a[7] + a[9] * a[3] * a[6];
+    inv[7] = a[0] * a[6] * a[11] - a[0] * a[7] * a[10] - a[4] * a[2] * a[11] + a[4] * a[3] * a[10] + a[8] * a[2] * a[7] - a[8] * a[3] * a[6];
+    inv[11] = -a[0] * a[5] * a[11] + a[0] * a[7] * a[9] + a[4] * a[1] * a[11] - a[4] * a[3] * a[9] - a[8] * a[1] * a[7] + a[8] * a[3] * a[5];
+    inv[15] = a[0] * a[5] * a[10] - a[0] * a[6] * a[9] - a[4] * a[1] * a[10] + a[4] * a[2] * a[9] + a[8] * a[1] * a[6] - a[8] * a[2] * a[5];
+    double det = a[0] * inv[0] + a[1] * inv[4] + a[2] * inv[8] + a[3] * inv[12];
+    double rdet = det != 0.0 ? 1.0 / det : 0.0;
+    for (int i = 0; i < 16; i++) out[i] = inv[i] * rdet;
+}
+void inverse4f(const float *m, double out[16]) {
+    double a[16];
+    for (int i = 0; i < 16; i++) a[i] = m[i];
+    inverse4(a, out);
+}
+// Inverse transpose of the upper 3x3, rounded to float (normal matrix).
+void normal_matrix(const double inv[16], float nm[9]) {
+    const int idx[9] = {0, 4, 8, 1, 5, 9, 2, 6, 10};
+    for (int k = 0; k < 9; k++) nm[k] = (float)inv[idx[k]];
+}
+
+float luminance(H3 c) { return 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z; }  // optix/util.h:161-163
+// fresnel::DiffuseReflectance (framework/render/material/fresnel.h:58-85): published
+// fits of Egan & Hilgeman (eta < 1) and d'Eon & Irving (eta >= 1).
+float diffuse_reflectance(float eta) {
+    if (eta < 1) return -1.4399f * (eta * eta) + 0.7099f * eta + 0.6681f + 0.0636f / eta;
+    float i1 = 1.0f / eta, i2 = i1 * i1, i3 = i2 * i1, i4 = i3 * i1, i5 = i4 * i1;
+    return 0.919317f - 3.4793f * i1 + 6.75335f * i2 - 7.80989f * i3 + 4.98554f * i4 - 1.36881f * i5;
+}
+H3 tex_average(const pt_texture_desc &t) {  // GetPixelAverage (optix_material.cpp:8-35)
+    if (t.type == PT_TEX_CHECKERBOARD)
+        return {(t.color0[0] + t.color1[0]) * 0.5f, (t.color0[1] + t.color1[1]) * 0.5f, (t.color0[2] + t.color1[2]) * 0.5f};
+    return {t.color0[0], t.color0[1], t.color0[2]};
+}
+
+DevTexture to_dev(const pt_texture_desc &t) {
+    DevTexture d{};
+    d.type = t.type;
+    for (int i = 0; i < 3; i++) {
+        d.c0[i] = t.color0[i];
+        d.c1[i] = t.color1[i];
+    }
+    d.r0 = make_float4(t.uv_transform[0], t.uv_transform[1], t.uv_transform[2], t.uv_transform[3]);
+    d.r1 = make_float4(t.uv_transform[4], t.uv_transform[5], t.uv_transform[6], t.uv_transform[7]);
+    return d;
+}
+
+bool affine(const float *m) { return m[12] == 0.f && m[13] == 0.f && m[14] == 0.f && m[15] == 1.f; }
+
+template <class T>
+int upload(DevBuf &b, const std::vector<T> &v) {
+    size_t bytes = std::max<size_t>(v.size() * sizeof(T), 16);
+    int st = b.ensure(bytes);
+    if (st != PT_OK) return st;
+    if (!v.empty()) PT_CUDA_TRY(cudaMemcpy(b.ptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return PT_OK;
+}
+
+int validate(const pt_scene_desc *d) {
+    if (!d) { pt_set_error("scene descriptor is NULL"); return PT_ERR_INVALID; }
+    if ((d->num_meshes && !d->meshes) || (d->num_spheres && !d->spheres) || (d->num_materials && !d->materials) ||
+        (d->num_instances && !d->instances)) {
+        pt_set_error("scene descriptor has a non-zero count with a NULL array");
+        return PT_ERR_INVALID;
+    }
+    if (d->width == 0 || d->height == 0) { pt_set_error("film size must be non-zero"); return PT_ERR_INVALID; }
+    for (uint32_t i = 0; i < d->num_materials; i++) {
+        const pt_material_desc &m = d->materials[i];
+        if (m.type < PT_MAT_DIFFUSE || m.type > PT_MAT_ROUGH_PLASTIC) {
+            pt_set_error("material %u has unknown type %u", i, m.type);
+            return PT_ERR_INVALID;
+        }
+        for (int k = 0; k < 4; k++)
+            if (m.tex[k].type != PT_TEX_RGB && m.tex[k].type != PT_TEX_CHECKERBOARD) {
+                pt_set_error("material %u texture %d: only RGB and checkerboard textures are supported", i, k);
+                return PT_ERR_UNSUPPORTED;
+            }
+    }
+    for (uint32_t i = 0; i < d->num_meshes; i++) {
+        const pt_mesh_desc &m = d->meshes[i];
+        if ((m.num_vertices && !m.positions) || (m.num_triangles && !m.indices)) {
+            pt_set_error("mesh %u has NULL positions or indices", i);
+            return PT_ERR_INVALID;
+        }
+        for (uint64_t t = 0; t < 3ull * m.num_triangles; t++)
+            if (m.indices[t] >= m.num_vertices) {
+                pt_set_error("mesh %u index %llu out of range (%u >= %u)", i, (unsigned long long)t, m.indices[t], m.num_vertices);
+                return PT_ERR_OOB;
+            }
+        for (uint64_t v = 0; v < 3ull * m.num_vertices; v++)
+            if (!std::isfinite(m.positions[v])) {
+                pt_set_error("mesh %u has a non-finite vertex coordinate", i);
+                return PT_ERR_INVALID;
+            }
+    }
+    for (uint32_t i = 0; i < d->num_instances; i++) {
+        const pt_instance_desc &in = d->instances[i];
+        if (in.material >= d->num_materials) { pt_set_error("instance %u: material out of range", i); return PT_ERR_OOB; }
+        if (in.shape_type == PT_SHAPE_MESH) {
+            if (in.shape_index >= d->num_meshes) { pt_set_error("instance %u: mesh out of range", i); return PT_ERR_OOB; }
+        } else if (in.shape_type == PT_SHAPE_SPHERE) {
+            if (in.shape_index >= d->num_spheres) { pt_set_error("instance %u: sphere out of range", i); return PT_ERR_OOB; }
+            if (!(d->spheres[in.shape_index].radius > 0.f)) { pt_set_error("instance %u: sphere radius must be > 0", i); return PT_ERR_INVALID; }
+        } else {
+            pt_set_error("instance %u: unknown shape type %u", i, in.shape_type);
+            return PT_ERR_INVALID;
+        }
+        if (!affine(in.to_world)) { pt_set_error("instance %u: to_world must be affine", i); return PT_ERR_INVALID; }
+        for (int k = 0; k < 16; k++)
+            if (!std::isfinite(in.to_world[k])) { pt_set_error("instance %u: non-finite transform", i); return PT_ERR_INVALID; }
+    }
+    if (d->env.type != PT_ENV_NONE && d->env.type != PT_ENV_CONST) {
+        pt_set_error("environment type %u not supported", d->env.type);
+        return PT_ERR_UNSUPPORTED;
+    }
+    return PT_OK;
+}
+
+void set_camera(pt_scene *s, const pt_camera_desc &c) {
+    for (int r = 0; r < 4; r++) {
+        s->dev.s2c[r] = make_float4(c.sample_to_camera[4 * r], c.sample_to_camera[4 * r + 1], c.sample_to_camera[4 * r + 2],
+                                    c.sample_to_camera[4 * r + 3]);
+        s->dev.c2w[r] = make_float4(c.camera_to_world[4 * r], c.camera_to_world[4 * r + 1], c.camera_to_world[4 * r + 2],
+                                    c.camera_to_world[4 * r + 3]);
+    }
+    float cm = std::max({fabsf(c.camera_to_world[3]), fabsf(c.camera_to_world[7]), fabsf(c.camera_to_world[11])});
+    s->scene_mag = std::max(s->scene_mag, cm);
+}
+
+int build_scene(pt_scene *s, const pt_scene_desc *d) {
+    int st = validate(d);
+    if (st != PT_OK) return st;
+    s->desc_shallow = *d;
+    s->desc_shallow.meshes = nullptr;
+    s->desc_shallow.spheres = nullptr;
+    s->desc_shallow.materials = nullptr;
+    s->desc_shallow.instances = nullptr;
+
+    std::vector<float4> vpos, vnrm, prims;
+    std::vector<float2> vuv;
+    std::vector<uint32_t> tri_vidx, prim_inst;
+    std::vector<DevInstance> insts(d->num_instances);
+    s->mesh_num_vertices.resize(d->num_meshes);
+    for (uint32_t i = 0; i < d->num_meshes; i++) s->mesh_num_vertices[i] = d->meshes[i].num_vertices;
+
+    float mag = 0.f;
+    uint32_t ntri = 0;
+    // triangles first, in instance order
+    for (uint32_t ii = 0; ii < d->num_instances; ii++) {
+        const pt_instance_desc &id = d->instances[ii];
+        DevInstance &in = insts[ii];
+        memset(&in, 0, sizeof(in));
+        in.material = id.material;
+        in.flags = id.flags & (PT_INST_FLIP_NORMALS | PT_INST_FLIP_TEXCOORDS);
+        in.emitter_offset = -1;
+        double inv[16];
+        inverse4f(id.to_world, inv);
+        in.inv0 = make_float4((float)inv[0], (float)inv[1], (float)inv[2], (float)inv[3]);
+        in.inv1 = make_float4((float)inv[4], (float)inv[5], (float)inv[6], (float)inv[7]);
+        in.inv2 = make_float4((float)inv[8], (float)inv[9], (float)inv[10], (float)inv[11]);
+        if (id.shape_type != PT_SHAPE_MESH) continue;
+        const pt_mesh_desc &m = d->meshes[id.shape_index];
+        if (m.normals) in.flags |= ptd::kInstHasNormals;
+        if (m.texcoords) in.flags |= ptd::kInstHasUvs;
+        uint32_t voff = (uint32_t)vpos.size();
+        in.prim_offset = ntri;
+        MeshInstanceRef ref{ii, id.shape_index, voff, ntri, {}};
+        memcpy(ref.to_world, id.to_world, sizeof(ref.to_world));
+        s->mesh_instances.push_back(ref);
+        float nm[9];
+        normal_matrix(inv, nm);
+        for (uint32_t v = 0; v < m.num_vertices; v++) {
+            H3 p = xform_point(id.to_world, h3(m.positions[3 * v], m.positions[3 * v + 1], m.positions[3 * v + 2]));
+            vpos.push_back(make_float4(p.x, p.y, p.z, 0.f));
+            mag = std::max({mag, fabsf(p.x), fabsf(p.y), fabsf(p.z)});
+            if (m.normals) {
+                H3 n = xform_vec(nm, h3(m.normals[3 * v], m.normals[3 * v + 1], m.normals[3 * v + 2]));
+                vnrm.push_back(make_float4(n.x, n.y, n.z, 0.f));
+            } else {
+                vnrm.push_back(make_float4(0.f, 0.f, 0.f, 0.f));
+            }
+            vuv.push_back(m.texcoords ? make_float2(m.texcoords[2 * v], m.texcoords[2 * v + 1]) : make_float2(0.f, 0.f));
+        }
+        for (uint32_t t = 0; t < m.num_triangles; t++) {
+            uint32_t pid = ntri + t;
+            uint32_t a = voff + m.indices[3 * t], b = voff + m.indices[3 * t + 1], c = voff + m.indices[3 * t + 2];
+            tri_vidx.push_back(a);
+            tri_vidx.push_back(b);
+            tri_vidx.push_back(c);
+            prim_inst.push_back(ii);
+            float4 pa = vpos[a], pb = vpos[b], pc = vpos[c];
+            int32_t ip = (int32_t)pid;
+            float idf;
+            memcpy(&idf, &ip, 4);
+            prims.push_back(make_float4(pa.x, pa.y, pa.z, idf));
+            prims.push_back(make_float4(pb.x, pb.y, pb.z, 0.f));
+            prims.push_back(make_float4(pc.x, pc.y, pc.z, 0.f));
+        }
+        ntri += m.num_triangles;
+    }
+    // spheres after all triangles
+    uint32_t nsph = 0;
+    for (uint32_t ii = 0; ii < d->num_instances; ii++) {
+        const pt_instance_desc &id = d->instances[ii];
+        if (id.shape_type != PT_SHAPE_SPHERE) continue;
+        DevInstance &in = insts[ii];
+        const pt_sphere_desc &sp = d->spheres[id.shape_index];
+        H3 c = h3(sp.center[0], sp.center[1], sp.center[2]);
+        H3 cw = xform_point(id.to_world, c);
+        H3 pw = xform_point(id.to_world, h3(c.x + sp.radius, c.y, c.z));
+        float r = hlen(sub(cw, pw));  // world/emitter.cpp:231-237
+        uint32_t pid = ntri + nsph;
+        in.flags |= ptd::kInstSphere;
+        in.prim_offset = pid;
+        in.sphere = make_float4(cw.x, cw.y, cw.z, r);
+        in.obj_center = make_float4(c.x, c.y, c.z, 0.f);
+        prim_inst.push_back(ii);
+        uint32_t bits = pid | 0x80000000u;
+        float idf;
+        memcpy(&idf, &bits, 4);
+        prims.push_back(make_float4(cw.x, cw.y, cw.z, idf));
+        prims.push_back(make_float4(r, 0.f, 0.f, 0.f));
+        prims.push_back(make_float4(0.f, 0.f, 0.f, 0.f));
+        mag = std::max({mag, fabsf(cw.x) + r, fabsf(cw.y) + r, fabsf(cw.z) + r});
+        nsph++;
+    }
+    s->num_tris = ntri;
+    s->num_spheres = nsph;
+    s->num_prims = ntri + nsph;
+    s->num_vertices = (uint32_t)vpos.size();
+    s->scene_mag = std::max(mag, 1e-6f);
+
+    // materials with the host precompute (optix_material.cpp:87-132)
+    std::vector<DevMaterial> mats(d->num_materials);
+    for (uint32_t i = 0; i < d->num_materials; i++) {
+        const pt_material_desc &m = d->materials[i];
+        DevMaterial &dm = mats[i];
+        memset(&dm, 0, sizeof(dm));
+        dm.type = m.type;
+        dm.twosided = m.twosided ? 1 : 0;
+        dm.nonlinear = m.nonlinear ? 1 : 0;
+        dm.eta = m.int_ior / m.ext_ior;
+        if (m.type == PT_MAT_PLASTIC || m.type == PT_MAT_ROUGH_PLASTIC) {
+            float dl = luminance(tex_average(m.tex[0]));
+            float sl = luminance(tex_average(m.tex[1]));
+            dm.spec_weight = sl / (sl + dl);
+            dm.int_fdr = diffuse_reflectance(1.f / dm.eta);
+        }
+        for (int k = 0; k < 4; k++) dm.tex[k] = to_dev(m.tex[k]);
+    }
+
+    // area emitters in instance order (world/emitter.cpp:169-263)
+    std::vector<DevEmitter> ems;
+    std::vector<float> weights;  // Emitter::weight = GetWeight(radiance) * area
+    for (uint32_t ii = 0; ii < d->num_instances; ii++) {
+        const pt_instance_desc &id = d->instances[ii];
+        if (!id.is_emitter) continue;
+        DevInstance &in = insts[ii];
+        in.emitter_offset = (int32_t)ems.size();
+        H3 rad = h3(id.radiance[0], id.radiance[1], id.radiance[2]);
+        float w = std::max(std::max(rad.x, rad.y), rad.z);  // GetWeight (emitter.cpp:77-101)
+        if (id.shape_type == PT_SHAPE_MESH) {
+            const pt_mesh_desc &m = d->meshes[id.shape_index];
+            double inv[16];
+            inverse4f(id.to_world, inv);
+            float nm[9];
+            normal_matrix(inv, nm);
+            uint32_t voff = 0;
+            for (auto &r : s->mesh_instances)
+                if (r.instance == ii) voff = r.vertex_offset;
+            for (uint32_t t = 0; t < m.num_triangles; t++) {
+                DevEmitter e{};
+                H3 P[3], N[3];
+                for (int k = 0; k < 3; k++) {
+                    uint32_t vi = m.indices[3 * t + k];
+                    float4 p = vpos[voff + vi];
+                    P[k] = h3(p.x, p.y, p.z);
+                }
+                for (int k = 0; k < 3; k++) {
+                    uint32_t vi = m.indices[3 * t + k];
+                    H3 nw = m.normals ? xform_vec(nm, h3(m.normals[3 * vi], m.normals[3 * vi + 1], m.normals[3 * vi + 2]))
+                                      : hcross(sub(P[1], P[0]), sub(P[2], P[0]));
+                    float len = sqrtf(nw.x * nw.x + nw.y * nw.y + nw.z * nw.z);  // TransformNormal normalises
+                    N[k] = h3(nw.x / len, nw.y / len, nw.z / len);
+                }
+                float area = hlen(hcross(sub(P[1], P[0]), sub(P[2], P[0]))) * 0.5f;
+                uint32_t type = ptd::kEmitTri;
+                float tf;
+                memcpy(&tf, &type, 4);
+                e.a = make_float4(tf, 0.f, area, 0.f);  // type, select probability, area, radius
+                weights.push_back(w * area);
+                e.rad = make_float4(rad.x, rad.y, rad.z, 0.f);
+                e.p0 = make_float4(P[0].x, P[0].y, P[0].z, 0.f);
+                e.p1 = make_float4(P[1].x, P[1].y, P[1].z, 0.f);
+                e.p2 = make_float4(P[2].x, P[2].y, P[2].z, 0.f);
+                e.n0 = make_float4(N[0].x, N[0].y, N[0].z, 0.f);
+                e.n1 = make_float4(N[1].x, N[1].y, N[1].z, 0.f);
+                e.n2 = make_float4(N[2].x, N[2].y, N[2].z, 0.f);
+                ems.push_back(e);
+            }
+        } else {
+            DevEmitter e{};
+            float r = in.sphere.w;
+            float area = 4 * 3.14159265358979323846f * r * r;
+            uint32_t type = ptd::kEmitSphere;
+            float tf;
+            memcpy(&tf, &type, 4);
+            e.a = make_float4(tf, 0.f, area, r);
+            weights.push_back(w * area);
+            e.rad = make_float4(rad.x, rad.y, rad.z, 0.f);
+            e.p0 = make_float4(in.sphere.x, in.sphere.y, in.sphere.z, 0.f);
+            ems.push_back(e);
+        }
+    }
+    // EmitterHelper::ComputeProbability (world/emitter.cpp:321-337)
+    bool has_env = d->env.type == PT_ENV_CONST;
+    float wsum = 0.f;
+    for (float w : weights) wsum += w;
+    size_t n_emit = (has_env ? 1 : 0) + ems.size();
+    std::vector<float> cdf;
+    float acc = 0.f;
+    for (size_t i = 0; i < ems.size(); i++) {
+        float p = weights[i] / wsum * (float)ems.size();
+        p = p / (float)n_emit;
+        ems[i].a.y = p;
+        cdf.push_back(acc + p);  // the running sums SelectOneEmiiter compares against
+        acc += p;
+    }
+    DevEmitter env{};
+    if (has_env) {
+        uint32_t type = ptd::kEmitConstEnv;
+        float tf;
+        memcpy(&tf, &type, 4);
+        env.a = make_float4(tf, 1.f / (float)n_emit, 0.f, 0.f);
+        env.rad = make_float4(d->env.radiance[0], d->env.radiance[1], d->env.radiance[2], 0.f);
+    }
+
+    int e;
+    if ((e = upload(s->prims_world, prims)) != PT_OK) return e;
+    if ((e = upload(s->tri_vidx, tri_vidx)) != PT_OK) return e;
+    if ((e = upload(s->vpos, vpos)) != PT_OK) return e;
+    if ((e = upload(s->vnrm, vnrm)) != PT_OK) return e;
+    if ((e = upload(s->vuv, vuv)) != PT_OK) return e;
+    if ((e = upload(s->prim_inst, prim_inst)) != PT_OK) return e;
+    if ((e = upload(s->inst, insts)) != PT_OK) return e;
+    if ((e = upload(s->mats, mats)) != PT_OK) return e;
+    if ((e = upload(s->emitters, ems)) != PT_OK) return e;
+    if ((e = upload(s->emitter_cdf, cdf)) != PT_OK) return e;
+    s->h_prims_world = std::move(prims);
+
+    ptd::DevScene &dv = s->dev;
+    dv.tri_vidx = s->tri_vidx.as<uint32_t>();
+    dv.vpos = s->vpos.as<float4>();
+    dv.vnrm = s->vnrm.as<float4>();
+    dv.vuv = s->vuv.as<float2>();
+    dv.prim_inst = s->prim_inst.as<uint32_t>();
+    dv.inst = s->inst.as<DevInstance>();
+    dv.mats = s->mats.as<DevMaterial>();
+    dv.emitters = s->emitters.as<DevEmitter>();
+    dv.emitter_cdf = s->emitter_cdf.as<float>();
+    dv.num_emitters = (uint32_t)ems.size();
+    dv.num_tris = ntri;
+    dv.has_env = has_env ? 1 : 0;
+    dv.env = env;
+    dv.width_px = d->width;
+    dv.height_px = d->height;
+    set_camera(s, d->camera);
+    return PT_OK;
+}
+
+}  // namespace
+
+void pt_set_error(const char *fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+}
+
+int DevBuf::ensure(size_t n) {
+    if (n <= bytes && ptr) return PT_OK;
+    release();
+    cudaError_t e = cudaMalloc(&ptr, n);
+    if (e != cudaSuccess) {
+        ptr = nullptr;
+        pt_set_error("cudaMalloc(%zu) failed: %s", n, cudaGetErrorString(e));
+        return e == cudaErrorMemoryAllocation ? PT_ERR_OOM : PT_ERR_CUDA;
+    }
+    bytes = n;
+    return PT_OK;
+}
+void DevBuf::release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+}
+
+pt_scene::~pt_scene() {
+    DevBuf *all[] = {&prims_world, &prims_bvh, &nodes, &tri_vidx, &vpos, &vnrm, &vuv, &prim_inst, &inst, &mats,
+                     &emitters, &emitter_cdf, &mesh_obj_pos, &bvh_scratch, &bvh_order, &ws.ray_o, &ws.ray_d, &ws.hit, &ws.thr,
+                     &ws.rad, &ws.rng, &ws.meta, &ws.q0, &ws.q1, &ws.sh_o, &ws.sh_d, &ws.sh_c, &ws.mat_key,
+                     &ws.counters, &ws.sort_tmp};
+    for (DevBuf *b : all) b->release();
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+}
+
+extern "C" {
+
+int pt_api_version(void) { return PT_API_VERSION; }
+
+int pt_last_error(char *buf, size_t n) {
+    if (!buf || n == 0) return PT_ERR_INVALID;
+    size_t k = std::min(n - 1, g_last_error.size());
+    memcpy(buf, g_last_error.data(), k);
+    buf[k] = 0;
+    return PT_OK;
+}
+
+int pt_context_create(const pt_device_opts *opts, pt_context **out) {
+    if (!out) { pt_set_error("out is NULL"); return PT_ERR_INVALID; }
+    *out = nullptr;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) {
+        pt_set_error("no CUDA device available (%s)", cudaGetErrorString(e));
+        return PT_ERR_UNSUPPORTED;
+    }
+    int dev = opts ? opts->device : 0;
+    if (dev < 0 || dev >= count) { pt_set_error("device %d out of range", dev); return PT_ERR_INVALID; }
+    PT_CUDA_TRY(cudaSetDevice(dev));
+    auto c = std::make_unique<pt_context>();
+    c->device = dev;
+    PT_CUDA_TRY(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, dev));
+    PT_CUDA_TRY(cudaDeviceGetAttribute(&c->max_smem_per_block, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    *out = c.release();
+    return PT_OK;
+}
+
+int pt_context_destroy(pt_context *ctx) {
+    delete ctx;
+    return PT_OK;
+}
+
+int pt_scene_upload(pt_context *ctx, const pt_scene_desc *desc, pt_scene **out) {
+    if (!ctx || !out) { pt_set_error("context or out is NULL"); return PT_ERR_INVALID; }
+    *out = nullptr;
+    PT_CUDA_TRY(cudaSetDevice(ctx->device));
+    auto s = std::make_unique<pt_scene>();
+    s->ctx = ctx;
+    int st = build_scene(s.get(), desc);
+    if (st != PT_OK) return st;
+    PT_CUDA_TRY(cudaEventCreate(&s->ev0));
+    PT_CUDA_TRY(cudaEventCreate(&s->ev1));
+    *out = s.release();
+    return PT_OK;
+}
+
+int pt_scene_destroy(pt_scene *scene) {
+    if (scene) cudaSetDevice(scene->ctx->device);
+    delete scene;
+    return PT_OK;
+}
+
+int pt_scene_set_camera(pt_scene *scene, const pt_camera_desc *camera) {
+    if (!scene || !camera) { pt_set_error("scene or camera is NULL"); return PT_ERR_INVALID; }
+    set_camera(scene, *camera);
+    return PT_OK;
+}
+
+int pt_scene_num_prims(const pt_scene *scene, uint32_t *nt, uint32_t *ns) {
+    if (!scene) { pt_set_error("scene is NULL"); return PT_ERR_INVALID; }
+    if (nt) *nt = scene->num_tris;
+    if (ns) *ns = scene->num_spheres;
+    return PT_OK;
+}
+
+int pt_scene_update_vertices(pt_scene *scene, uint32_t mesh, const float *positions, uint32_t num_vertices) {
+    if (!scene || !positions) { pt_set_error("scene or positions is NULL"); return PT_ERR_INVALID; }
+    if (mesh >= scene->mesh_num_vertices.size() || num_vertices != scene->mesh_num_vertices[mesh]) {
+        pt_set_error("mesh %u: expected %u vertices", mesh, mesh < scene->mesh_num_vertices.size() ? scene->mesh_num_vertices[mesh] : 0);
+        return PT_ERR_INVALID;
+    }
+    for (uint64_t v = 0; v < 3ull * num_vertices; v++)
+        if (!std::isfinite(positions[v])) { pt_set_error("non-finite vertex coordinate"); return PT_ERR_INVALID; }
+    PT_CUDA_TRY(cudaSetDevice(scene->ctx->device));
+    int st = scene->mesh_obj_pos.ensure(std::max<size_t>(12ull * num_vertices, 16));
+    if (st != PT_OK) return st;
+    PT_CUDA_TRY(cudaMemcpy(scene->mesh_obj_pos.ptr, positions, 12ull * num_vertices, cudaMemcpyHostToDevice));
+    return pt_update_world_vertices(scene, mesh, scene->mesh_obj_pos.as<float>(), num_vertices, 0);
+}
+
+int pt_bvh_build(pt_scene *scene, const pt_bvh_opts *opts, void *stream) {
+    if (!scene) { pt_set_error("scene is NULL"); return PT_ERR_INVALID; }
+    pt_bvh_opts o{4, 4, 0, 0};
+    if (opts) o = *opts;
+    if (o.width != 2 && o.width != 4 && o.width != 8) { pt_set_error("BVH width must be 2, 4 or 8"); return PT_ERR_INVALID; }
+    if (o.max_leaf_size < 1 || o.max_leaf_size > 15) { pt_set_error("max_leaf_size must be in 1..15"); return PT_ERR_INVALID; }
+    PT_CUDA_TRY(cudaSetDevice(scene->ctx->device));
+    return pt_bvh_build_impl(scene, &o, static_cast<cudaStream_t>(stream));
+}
+
+int pt_bvh_refit(pt_scene *scene, void *stream) {
+    if (!scene) { pt_set_error("scene is NULL"); return PT_ERR_INVALID; }
+    if (!scene->bvh_built) { pt_set_error("pt_bvh_refit before pt_bvh_build"); return PT_ERR_STATE; }
+    PT_CUDA_TRY(cudaSetDevice(scene->ctx->device));
+    return pt_bvh_refit_impl(scene, static_cast<cudaStream_t>(stream));
+}
+
+int pt_bvh_get_stats(const pt_scene *scene, pt_bvh_stats *out) {
+    if (!scene || !out) { pt_set_error("scene or out is NULL"); return PT_ERR_INVALID; }
+    *out = scene->bvh_stats;
+    return PT_OK;
+}
+
+int pt_render(pt_scene *scene, const pt_render_params *params, const pt_frame_buffers *fb, void *stream) {
+    if (!scene || !params || !fb || !fb->accum) { pt_set_error("scene, params, buffers or accum is NULL"); return PT_ERR_INVALID; }
+    if (!scene->bvh_built) { pt_set_error("pt_render before pt_bvh_build"); return PT_ERR_STATE; }
+    if (params->rng != PT_RNG_REF_LCG && params->rng != PT_RNG_PCG32) { pt_set_error("unknown rng mode"); return PT_ERR_INVALID; }
+    PT_CUDA_TRY(cudaSetDevice(scene->ctx->device));
+    return pt_render_impl(scene, params, fb, static_cast<cudaStream_t>(stream));
+}
+
+int pt_render_get_stats(const pt_scene *scene, pt_render_stats *out) {
+    if (!scene || !out) { pt_set_error("scene or out is NULL"); return PT_ERR_INVALID; }
+    *out = scene->render_stats;
+    return PT_OK;
+}
+
+int pt_trace_rays(pt_scene *scene, const float *rays, float *hits, uint32_t n, int anyhit, void *stream) {
+    if (!scene || (n && (!rays || !hits))) { pt_set_error("scene, rays or hits is NULL"); return PT_ERR_INVALID; }
+    if (!scene->bvh_built) { pt_set_error("pt_trace_rays before pt_bvh_build"); return PT_ERR_STATE; }
+    PT_CUDA_TRY(cudaSetDevice(scene->ctx->device));
+    return pt_trace_rays_impl(scene, rays, hits, n, anyhit, static_cast<cudaStream_t>(stream));
+}
+
+int pt_bsdf_eval_batch(const float *bsdf, const float *wo, const float *wi, float *f, float *pdf, uint32_t n, void *stream) {
+    if (n && (!bsdf || !wo || !wi || !f || !pdf)) { pt_set_error("NULL buffer"); return PT_ERR_INVALID; }
+    return pt_bsdf_eval_impl(bsdf, wo, wi, f, pdf, n, static_cast<cudaStream_t>(stream));
+}
+
+int pt_bsdf_sample_batch(const float *bsdf, const float *wo, uint32_t *rng, float *wi, float *f, float *pdf,
+                         uint32_t *type, uint32_t n, void *stream) {
+    if (n && (!bsdf || !wo || !rng || !wi || !f || !pdf || !type)) { pt_set_error("NULL buffer"); return PT_ERR_INVALID; }
+    return pt_bsdf_sample_impl(bsdf, wo, rng, wi, f, pdf, type, n, static_cast<cudaStream_t>(stream));
+}
+
+// util::Camera::GetSampleToCameraMatrix (framework/util/camera.cpp:7-20):
+// sample_to_camera = transpose(inverse(P * T(1,1,0) * S(0.5,0.5,1))) where P is
+// DirectXMath's row-vector XMMatrixPerspectiveFovRH; computed in double here.
+int pt_camera_make(float fov_y_deg, float aspect, float near_clip, float far_clip, const float to_world[16],
+                   pt_camera_desc *out) {
+    if (!out || !to_world || !(aspect > 0.f) || !(fov_y_deg > 0.f) || near_clip == far_clip) {
+        pt_set_error("invalid camera parameters");
+        return PT_ERR_INVALID;
+    }
+    double fov = (double)(fov_y_deg / 180.f * 3.14159265358979323846f);
+    double h = cos(0.5 * fov) / sin(0.5 * fov);
+    double w = h / aspect;
+    double range = (double)far_clip / ((double)near_clip - (double)far_clip);
+    double P[16] = {w, 0, 0, 0, 0, h, 0, 0, 0, 0, range, -1, 0, 0, range * near_clip, 0};
+    double T[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 1, 1, 0, 1};
+    double S[16] = {0.5, 0, 0, 0, 0, 0.5, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+    auto mul = [](const double *a, const double *b, double *c) {
+        for (int i = 0; i < 4; i++)
+            for (int j = 0; j < 4; j++) {
+                double acc = 0;
+                for (int k = 0; k < 4; k++) acc += a[4 * i + k] * b[4 * k + j];
+                c[4 * i + j] = acc;
+            }
+    };
+    double PT_[16], A[16], Ainv[16];
+    mul(P, T, PT_);
+    mul(PT_, S, A);
+    inverse4(A, Ainv);
+    for (int r = 0; r < 4; r++)
+        for (int c = 0; c < 4; c++) out->sample_to_camera[4 * r + c] = (float)Ainv[4 * c + r];
+    memcpy(out->camera_to_world, to_world, 16 * sizeof(float));
+    return PT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,292 @@
+// pt_traverse.cuh -- short-stack closest-hit and any-hit traversal of the
+// wide BVH (2, 4 or 8 children per node) on FP32 SIMT cores.
+//
+// Replaces optixTrace (example/path_tracer/main.cu:80-85,161-166; closest hit,
+// tmin 0.001, tmax 1e16) and Emitter::TraceShadowRay (framework/render/
+// emitter.h:91-100; terminate on first hit).  Result semantics (shared with
+// the CPU oracle): a primitive is hit at tmin < t < tmax; the closest hit is
+// the smallest t, ties broken by the smaller primitive id, so the answer does
+// not depend on traversal order.  The triangle test is the watertight test of
+// Woop, Benthin and Wald (JCGT 2013) evaluated with explicitly rounded
+// operations (no FMA contraction), which makes hit ids and distances bit-equal
+// to the host restatement.
+//
+// Memory layout (HBM):
+//   node  = 8*K floats: lo_x[K] hi_x[K] lo_y[K] hi_y[K] lo_z[K] hi_z[K]
+//           child[K] count[K]; count > 0: leaf over primitive slots
+//           [child, child + count); count == 0 and child >= 0: inner node;
+//           child < 0: empty slot.  Loaded as 2*K float4 (128-bit) loads.
+//   prim  = 3 float4 per slot: triangle (v0, id) (v1, 0) (v2, 0);
+//           sphere (centre, id | 1<<31) (radius, 0, 0, 0) (0).
+// Nodes are in breadth-first order, so the first smem_nodes nodes are the
+// top levels; those are staged in shared memory once per (persistent) block.
+#pragma once
+
+#include "pt_device.cuh"
+
+namespace ptd {
+
+constexpr int kShortStack = 16;  // shared-memory entries per thread
+constexpr int kSpillStack = 48;  // local-memory overflow entries per thread
+constexpr float kSlabScale = 1.0000004f;  // 1 + 2*gamma(3): robust slab far bound (Ize 2013)
+
+struct TraceResult {
+    float t;
+    int prim;
+    float u, v;
+};
+
+struct RayWT {  // per-ray constants of the watertight test
+    int kx, ky, kz;
+    float sx, sy, sz;
+};
+
+PT_DI float sel3(float3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+
+PT_DI RayWT ray_wt(float3 d) {
+    RayWT r;
+    float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    r.kz = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
+    r.kx = r.kz + 1 == 3 ? 0 : r.kz + 1;
+    r.ky = r.kx + 1 == 3 ? 0 : r.kx + 1;
+    float dz = sel3(d, r.kz);
+    if (dz < 0.f) {
+        int t = r.kx;
+        r.kx = r.ky;
+        r.ky = t;
+    }
+    r.sx = __fdiv_rn(sel3(d, r.kx), dz);
+    r.sy = __fdiv_rn(sel3(d, r.ky), dz);
+    r.sz = __frcp_rn(dz);
+    return r;
+}
+
+// Watertight ray/triangle test with explicitly rounded operations.
+PT_DI bool intersect_triangle(float3 o, const RayWT &w, float3 p0, float3 p1, float3 p2, float tmin, float tmax,
+                              float &t_out, float &u_out, float &v_out) {
+    float3 A = f3(__fsub_rn(p0.x, o.x), __fsub_rn(p0.y, o.y), __fsub_rn(p0.z, o.z));
+    float3 B = f3(__fsub_rn(p1.x, o.x), __fsub_rn(p1.y, o.y), __fsub_rn(p1.z, o.z));
+    float3 C = f3(__fsub_rn(p2.x, o.x), __fsub_rn(p2.y, o.y), __fsub_rn(p2.z, o.z));
+    float Akz = sel3(A, w.kz), Bkz = sel3(B, w.kz), Ckz = sel3(C, w.kz);
+    float Ax = __fsub_rn(sel3(A, w.kx), __fmul_rn(w.sx, Akz));
+    float Ay = __fsub_rn(sel3(A, w.ky), __fmul_rn(w.sy, Akz));
+    float Bx = __fsub_rn(sel3(B, w.kx), __fmul_rn(w.sx, Bkz));
+    float By = __fsub_rn(sel3(B, w.ky), __fmul_rn(w.sy, Bkz));
+    float Cx = __fsub_rn(sel3(C, w.kx), __fmul_rn(w.sx, Ckz));
+    float Cy = __fsub_rn(sel3(C, w.ky), __fmul_rn(w.sy, Ckz));
+    float U = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
+    float V = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
+    float W = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
+    if (U == 0.f || V == 0.f || W == 0.f) {  // double-precision fallback on edges
+        U = __double2float_rn(__dsub_rn(__dmul_rn((double)Cx, (double)By), __dmul_rn((double)Cy, (double)Bx)));
+        V = __double2float_rn(__dsub_rn(__dmul_rn((double)Ax, (double)Cy), __dmul_rn((double)Ay, (double)Cx)));
+        W = __double2float_rn(__dsub_rn(__dmul_rn((double)Bx, (double)Ay), __dmul_rn((double)By, (double)Ax)));
+    }
+    if ((U < 0.f || V < 0.f || W < 0.f) && (U > 0.f || V > 0.f || W > 0.f)) return false;
+    float det = __fadd_rn(__fadd_rn(U, V), W);
+    if (det == 0.f) return false;
+    float Az = __fmul_rn(w.sz, Akz), Bz = __fmul_rn(w.sz, Bkz), Cz = __fmul_rn(w.sz, Ckz);
+    float T = __fadd_rn(__fadd_rn(__fmul_rn(U, Az), __fmul_rn(V, Bz)), __fmul_rn(W, Cz));
+    float rcp = __frcp_rn(det);
+    float t = __fmul_rn(T, rcp);
+    if (!(t > tmin && t < tmax)) return false;
+    t_out = t;
+    u_out = __fmul_rn(V, rcp);
+    v_out = __fmul_rn(W, rcp);
+    return true;
+}
+
+PT_DI bool intersect_sphere(float3 o, float3 d, float3 c, float r, float tmin, float tmax, float &t_out) {
+    float3 oc = f3(__fsub_rn(o.x, c.x), __fsub_rn(o.y, c.y), __fsub_rn(o.z, c.z));
+    float a = __fadd_rn(__fadd_rn(__fmul_rn(d.x, d.x), __fmul_rn(d.y, d.y)), __fmul_rn(d.z, d.z));
+    float b = __fadd_rn(__fadd_rn(__fmul_rn(oc.x, d.x), __fmul_rn(oc.y, d.y)), __fmul_rn(oc.z, d.z));
+    float cc = __fsub_rn(__fadd_rn(__fadd_rn(__fmul_rn(oc.x, oc.x), __fmul_rn(oc.y, oc.y)), __fmul_rn(oc.z, oc.z)),
+                         __fmul_rn(r, r));
+    float disc = __fsub_rn(__fmul_rn(b, b), __fmul_rn(a, cc));
+    if (!(disc >= 0.f)) return false;
+    float sq = __fsqrt_rn(disc);
+    float t0 = __fdiv_rn(__fsub_rn(-b, sq), a);
+    float t1 = __fdiv_rn(__fadd_rn(-b, sq), a);
+    if (t0 > tmin && t0 < tmax) {
+        t_out = t0;
+        return true;
+    }
+    if (t1 > tmin && t1 < tmax) {
+        t_out = t1;
+        return true;
+    }
+    return false;
+}
+
+PT_DI float3 safe_inv(float3 d) {
+    return f3(d.x != 0.f ? __frcp_rn(d.x) : copysignf(1e30f, d.x), d.y != 0.f ? __frcp_rn(d.y) : copysignf(1e30f, d.y),
+              d.z != 0.f ? __frcp_rn(d.z) : copysignf(1e30f, d.z));
+}
+
+template <int K>
+struct WideNode {
+    float f[8 * K];
+    PT_DI float lox(int c) const { return f[c]; }
+    PT_DI float hix(int c) const { return f[K + c]; }
+    PT_DI float loy(int c) const { return f[2 * K + c]; }
+    PT_DI float hiy(int c) const { return f[3 * K + c]; }
+    PT_DI float loz(int c) const { return f[4 * K + c]; }
+    PT_DI float hiz(int c) const { return f[5 * K + c]; }
+    PT_DI int child(int c) const { return __float_as_int(f[6 * K + c]); }
+    PT_DI int count(int c) const { return __float_as_int(f[7 * K + c]); }
+};
+
+template <int K>
+PT_DI void load_node(const float4 *__restrict__ p, WideNode<K> &n) {
+#pragma unroll
+    for (int i = 0; i < 2 * K; i++) {
+        float4 v = __ldg(p + i);
+        n.f[4 * i + 0] = v.x;
+        n.f[4 * i + 1] = v.y;
+        n.f[4 * i + 2] = v.z;
+        n.f[4 * i + 3] = v.w;
+    }
+}
+template <int K>
+PT_DI void load_node_smem(const float4 *p, WideNode<K> &n) {
+#pragma unroll
+    for (int i = 0; i < 2 * K; i++) {
+        float4 v = p[i];
+        n.f[4 * i + 0] = v.x;
+        n.f[4 * i + 1] = v.y;
+        n.f[4 * i + 2] = v.z;
+        n.f[4 * i + 3] = v.w;
+    }
+}
+
+// Per-thread traversal stack: kShortStack entries in shared memory (strided by
+// the block size to avoid bank conflicts), the rest in local memory.
+struct ShortStack {
+    int2 *smem;  // base + threadIdx.x
+    int stride;
+    int2 spill[kSpillStack];
+    int sp;
+    PT_DI void push(int node, float t, uint32_t &overflow) {
+        int2 e = make_int2(node, __float_as_int(t));
+        if (sp < kShortStack) smem[sp * stride] = e;
+        else if (sp < kShortStack + kSpillStack) spill[sp - kShortStack] = e;
+        else {  // cannot happen for trees of depth <= 16 (width 4); counted, entry dropped
+            overflow = 1;
+            return;
+        }
+        sp++;
+    }
+    PT_DI int2 pop() {
+        sp--;
+        return sp < kShortStack ? smem[sp * stride] : spill[sp - kShortStack];
+    }
+};
+
+template <int K, bool ANY, bool COUNT>
+PT_DI TraceResult traverse(const DevScene &s, const float4 *smem_nodes, int2 *smem_stack, float3 o, float3 d,
+                           float tmin, float tmax, uint32_t &n_nodes, uint32_t &n_prims, uint32_t &overflow) {
+    TraceResult best;
+    best.t = tmax;
+    best.prim = -1;
+    best.u = best.v = 0.f;
+    const RayWT w = ray_wt(d);
+    const float3 inv = safe_inv(d);
+    ShortStack st;
+    st.smem = smem_stack;
+    st.stride = blockDim.x;
+    st.sp = 0;
+    int cur = 0;
+    for (;;) {
+        WideNode<K> n;
+        if (cur < static_cast<int>(s.smem_nodes)) load_node_smem<K>(smem_nodes + (size_t)cur * 2 * K, n);
+        else load_node<K>(s.nodes + (size_t)cur * 2 * K, n);
+        if (COUNT) n_nodes++;
+        int ic[K];
+        float it[K];
+#pragma unroll
+        for (int c = 0; c < K; c++) {
+            ic[c] = -1;
+            it[c] = __int_as_float(0x7f800000);
+            int ch = n.child(c);
+            if (ch < 0) continue;
+            float tx0 = (n.lox(c) - o.x) * inv.x, tx1 = (n.hix(c) - o.x) * inv.x;
+            float ty0 = (n.loy(c) - o.y) * inv.y, ty1 = (n.hiy(c) - o.y) * inv.y;
+            float tz0 = (n.loz(c) - o.z) * inv.z, tz1 = (n.hiz(c) - o.z) * inv.z;
+            float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
+            float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
+            tf = fminf(tf * kSlabScale, best.t * kSlabScale);
+            if (!(tn <= tf)) continue;
+            int cnt = n.count(c);
+            if (cnt > 0) {
+                for (int j = 0; j < cnt; j++) {
+                    const float4 *pr = s.prims + (size_t)(ch + j) * 3;
+                    float4 a = __ldg(pr);
+                    float4 b = __ldg(pr + 1);
+                    if (COUNT) n_prims++;
+                    int pid = __float_as_int(a.w);
+                    float t, u = 0.f, v = 0.f;
+                    float tlim = best.prim < 0 ? tmax : __int_as_float(__float_as_int(best.t) + 1);
+                    bool hit;
+                    if (pid >= 0) {
+                        float4 cc = __ldg(pr + 2);
+                        hit = intersect_triangle(o, w, xyz(a), xyz(b), xyz(cc), tmin, tlim, t, u, v);
+                    } else {
+                        pid &= 0x7fffffff;
+                        hit = intersect_sphere(o, d, xyz(a), b.x, tmin, tlim, t);
+                    }
+                    if (!hit) continue;
+                    if (ANY) {
+                        best.t = t;
+                        best.prim = pid;
+                        return best;
+                    }
+                    if (t < best.t || pid < best.prim) {
+                        best.t = t;
+                        best.prim = pid;
+                        best.u = u;
+                        best.v = v;
+                    }
+                }
+            } else {
+                ic[c] = ch;
+                it[c] = tn;
+            }
+        }
+        // order the inner children by entry distance (sorting network on K slots)
+#pragma unroll
+        for (int i = 1; i < K; i++) {
+#pragma unroll
+            for (int j = i; j > 0; j--) {
+                if (it[j] < it[j - 1]) {
+                    float tt = it[j];
+                    it[j] = it[j - 1];
+                    it[j - 1] = tt;
+                    int ti = ic[j];
+                    ic[j] = ic[j - 1];
+                    ic[j - 1] = ti;
+                }
+            }
+        }
+        // push the farther ones, descend into the nearest
+#pragma unroll
+        for (int i = K - 1; i >= 1; i--)
+            if (ic[i] >= 0 && it[i] <= best.t * kSlabScale) st.push(ic[i], it[i], overflow);
+        if (ic[0] >= 0 && it[0] <= best.t * kSlabScale) {
+            cur = ic[0];
+            continue;
+        }
+        bool found = false;
+        while (st.sp > 0) {
+            int2 e = st.pop();
+            if (__int_as_float(e.y) <= best.t * kSlabScale) {
+                cur = e.x;
+                found = true;
+                break;
+            }
+        }
+        if (!found) break;
+    }
+    return best;
+}
+
+}  // namespace ptd
