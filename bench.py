@@ -296,9 +296,9 @@ def main():
     # algorithmic bytes of the closest-hit kernel (per-ray counters of the identical counting render)
     node_bytes = 32 * args.bvh_width
     ext_bytes = cst.nodes_visited * node_bytes + cst.prims_tested * 48 + cst.extension_rays * (32 + 16)
-    achieved = ext_bytes / (ext_ms / ext_launches * 1e-3) / 1e9 / (ext_launches / args.steps) if ext_ms > 0 else None
-    # per launch: ext_bytes spread over the launches of one step
-    per_launch_bytes = ext_bytes / max(1, ext_launches // args.steps)
+    # per launch: one step's algorithmic bytes over that step's closest-hit launches
+    launches_per_step = max(1, ext_launches // args.steps)
+    per_launch_bytes = ext_bytes / launches_per_step
     avg_launch_s = ext_ms / max(1, ext_launches) * 1e-3
     achieved = per_launch_bytes / avg_launch_s / 1e9 if ext_ms > 0 else None
     peak, peak_kind = measured_peaks()

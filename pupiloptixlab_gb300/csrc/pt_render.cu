@@ -36,7 +36,7 @@ enum Counter : int {
     kWorkExtend = 3,
     kWorkShadow = 4,
     kOverflow = 5,
-    kStatBase = 8,  // uint64 stats at counters + 8 (as uint64 pairs)
+    kStatBase = 8,  // uint64 statistics start at counters + 8 (32-byte offset)
 };
 enum Stat : int { kStatExtNodes = 0, kStatExtPrims, kStatShNodes, kStatShPrims, kStatExtRays, kStatShRays, kNumStats };
 
@@ -565,7 +565,7 @@ struct Launcher {
         stt.sh_d = ws.sh_d.as<float4>();
         stt.sh_c = ws.sh_c.as<float4>();
         stt.counters = ws.counters.as<uint32_t>();
-        stt.stats = reinterpret_cast<unsigned long long *>(ws.counters.as<uint32_t>() + kStatBase * 2);
+        stt.stats = reinterpret_cast<unsigned long long *>(ws.counters.as<uint32_t>() + kStatBase);
         Outputs out;
         out.accum = reinterpret_cast<float4 *>(fb->accum);
         out.frame = reinterpret_cast<float4 *>(fb->frame);

@@ -51,6 +51,11 @@ def test_sample_matches_reference(cuda_ctx, golden):
     # sampled non-delta lobes: value and pdf are the reference's evaluation at the
     # direction the GPU drew (which may differ from the host's by an ulp of sin/cos)
     smooth = same_path & ((typ & 0x60) == 0) & (typ != 0)
+    # early returns after the lobe was chosen (e.g. a refraction that stays on
+    # the same side, rough_dielectric.h:149-150) leave f = pdf = 0 on both sides
+    rejected = smooth & (golden["sample_pdf"] == 0)
+    assert np.all(pdf[rejected] == 0) and np.all(f[rejected] == 0)
+    smooth &= golden["sample_pdf"] != 0
     ref_f, ref_pdf = oracle.bsdf_eval(golden["sample_bsdf"][smooth], golden["sample_wo"][smooth], wi[smooth])
     assert close(f[smooth], ref_f)
     assert close(pdf[smooth], ref_pdf)
