@@ -36,6 +36,12 @@ CU_SOURCES = {
     "pt_render.cu": ["-fmad=false"],
 }
 CPP_SOURCES = ["pt_scene.cpp"]
+# C++ host layer above the C-ABI (Pass / System / scene loader): its own
+# library, linked against libpt_gb300.so, plus the pupil_pt command-line tool.
+HOST = PKG / "host"
+HOST_SOURCES = ["xml.cpp", "scene.cpp", "pass.cpp", "host_capi.cpp"]
+HOST_LIB = BUILD / "libpupil_host.so"
+HOST_CLI = BUILD / "pupil_pt"
 
 
 def _nvcc() -> str:
@@ -89,6 +95,32 @@ def build_library(force: bool = False, verbose: bool = False) -> Path:
     return LIB
 
 
+def _cuda_lib_dir() -> str:
+    root = Path(_nvcc()).resolve().parent.parent
+    for cand in (root / "lib64", root / "lib", root / "targets" / "sbsa-linux" / "lib",
+                 root / "targets" / "x86_64-linux" / "lib"):
+        if (cand / "libcudart.so").exists():
+            return str(cand)
+    return str(root / "lib64")
+
+
+def build_host(force: bool = False) -> Path:
+    """libpupil_host.so and pupil_pt (g++ only; they see nothing but pt_api.h)."""
+    BUILD.mkdir(exist_ok=True)
+    srcs = [HOST / f for f in HOST_SOURCES]
+    deps = srcs + sorted(HOST.glob("*.h")) + [ROOT / "include" / "pt_api.h", LIB]
+    common = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-I", str(ROOT / "include"),
+              "-I", str(HOST), "-I", _cuda_include()]
+    links = ["-L", str(BUILD), "-lpt_gb300", "-L", _cuda_lib_dir(), "-lcudart", "-Wl,-rpath,$ORIGIN",
+             "-Wl,-rpath," + _cuda_lib_dir()]
+    if force or _stale(HOST_LIB, deps):
+        _run(["g++"] + common + ["-shared", "-o", str(HOST_LIB)] + [str(x) for x in srcs] + links)
+    if force or _stale(HOST_CLI, [HOST / "pt_main.cpp", HOST_LIB]):
+        _run(["g++"] + common + ["-o", str(HOST_CLI), str(HOST / "pt_main.cpp"), "-L", str(BUILD), "-lpupil_host"]
+             + links)
+    return HOST_LIB
+
+
 def build_oracle(verbose: bool = False) -> None:
     _run(["make", "-C", str(ORACLE), "-s", "all"])
     if (REFERENCE_TREE / "framework").is_dir():
@@ -97,5 +129,6 @@ def build_oracle(verbose: bool = False) -> None:
 
 if __name__ == "__main__":
     build_library(force="--force" in sys.argv, verbose=True)
+    build_host(force="--force" in sys.argv)
     build_oracle(verbose=True)
     print(LIB)

@@ -1,0 +1,203 @@
+// pass.cpp -- headless Pass / System / WavefrontPTPass (see pass.h).
+#include "pass.h"
+
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cstring>
+
+namespace Pupil {
+
+namespace {
+std::string pt_error() {
+    char buf[1024];
+    pt_last_error(buf, sizeof(buf));
+    return buf;
+}
+}  // namespace
+
+Pass::Pass(std::string_view n, EPassTag t) noexcept : name(n), tag(t) {}
+
+void Pass::Run() noexcept {
+    auto t0 = std::chrono::steady_clock::now();
+    OnRun();
+    last_exec_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+BufferManager::Buffer *BufferManager::AllocBuffer(const std::string &name, size_t bytes) {
+    auto &slot = m_buffers[name];
+    if (slot && slot->bytes >= bytes) {
+        cudaMemset(slot->device, 0, slot->bytes);
+        return slot.get();
+    }
+    if (slot && slot->device) cudaFree(slot->device);
+    slot = std::make_unique<Buffer>();
+    slot->name = name;
+    if (cudaMalloc(&slot->device, bytes) != cudaSuccess) {
+        slot.reset();
+        m_buffers.erase(name);
+        return nullptr;
+    }
+    slot->bytes = bytes;
+    cudaMemset(slot->device, 0, bytes);
+    return slot.get();
+}
+
+BufferManager::Buffer *BufferManager::GetBuffer(const std::string &name) {
+    auto it = m_buffers.find(name);
+    return it == m_buffers.end() ? nullptr : it->second.get();
+}
+
+void BufferManager::Destroy() {
+    for (auto &kv : m_buffers)
+        if (kv.second && kv.second->device) cudaFree(kv.second->device);
+    m_buffers.clear();
+}
+
+System *System::Instance() {
+    static System s;
+    return &s;
+}
+
+bool System::Init(int device) {
+    if (m_ctx) return true;
+    pt_device_opts o{device, 0};
+    if (pt_context_create(&o, &m_ctx) != PT_OK) {
+        m_error = pt_error();
+        return false;
+    }
+    return true;
+}
+
+void System::AddPass(Pass *pass) {
+    if (static_cast<unsigned>(pass->tag) & static_cast<unsigned>(EPassTag::Pre)) m_pre_passes.push_back(pass);
+    else m_passes.push_back(pass);
+}
+
+bool System::SetScene(const std::string &xml_path) {
+    auto s = std::make_unique<resource::Scene>();
+    if (!s->LoadFromXML(xml_path)) {
+        m_error = s->error();
+        return false;
+    }
+    return SetScene(std::move(s));
+}
+
+// System::SetScene (framework/system/system.cpp:136-173): allocate the
+// "final result" buffer, then the SceneLoad event reaches every pass.
+bool System::SetScene(std::unique_ptr<resource::Scene> scene) {
+    if (!m_ctx && !Init()) return false;
+    m_scene = std::move(scene);
+    size_t px = (size_t)m_scene->sensor.width * m_scene->sensor.height;
+    if (!m_buffers.AllocBuffer("final result", px * 16)) {
+        m_error = "cannot allocate the final result buffer";
+        return false;
+    }
+    for (Pass *p : m_pre_passes) p->Run();
+    for (Pass *p : m_passes) {
+        if (auto *pt = dynamic_cast<pt::WavefrontPTPass *>(p)) {
+            if (!pt->SetScene(m_scene.get(), m_ctx, m_buffers)) {
+                m_error = pt->last_error();
+                return false;
+            }
+        }
+    }
+    return true;
+}
+
+void System::Run(uint32_t frames) {
+    for (uint32_t f = 0; f < frames; f++)
+        for (Pass *p : m_passes) p->Run();
+}
+
+void System::Destroy() {
+    m_passes.clear();
+    m_pre_passes.clear();
+    m_buffers.Destroy();
+    m_scene.reset();
+    if (m_ctx) pt_context_destroy(m_ctx);
+    m_ctx = nullptr;
+}
+
+namespace pt {
+
+WavefrontPTPass::WavefrontPTPass(std::string_view n) noexcept : Pass(n) {
+    m_params.spp = 1;
+    m_params.accumulate = 1;
+    m_params.rng = PT_RNG_REF_LCG;
+}
+
+WavefrontPTPass::~WavefrontPTPass() noexcept {
+    if (m_scene) pt_scene_destroy(m_scene);
+}
+
+bool WavefrontPTPass::SetScene(resource::Scene *scene, pt_context *ctx, BufferManager &buffers) noexcept {
+    if (m_scene) pt_scene_destroy(m_scene);
+    m_scene = nullptr;
+    const pt_scene_desc &d = scene->Desc();
+    if ((m_status = pt_scene_upload(ctx, &d, &m_scene)) != PT_OK ||
+        (m_status = pt_bvh_build(m_scene, &m_bvh, nullptr)) != PT_OK) {
+        m_error = pt_error();
+        return false;
+    }
+    size_t px = (size_t)d.width * d.height;
+    auto *accum = buffers.AllocBuffer("pt accum buffer", px * 16);
+    auto *albedo = buffers.AllocBuffer("albedo", px * 12);
+    auto *normal = buffers.AllocBuffer("normal", px * 12);
+    auto *test = buffers.AllocBuffer("test", px * 4);
+    auto *final_result = buffers.GetBuffer("final result");
+    if (!accum || !albedo || !normal || !test || !final_result) {
+        m_status = PT_ERR_OOM;
+        m_error = "cannot allocate the pass buffers";
+        return false;
+    }
+    m_fb.accum = static_cast<float *>(accum->device);
+    m_fb.frame = static_cast<float *>(final_result->device);
+    m_fb.albedo = static_cast<float *>(albedo->device);
+    m_fb.normal = static_cast<float *>(normal->device);
+    m_fb.test = static_cast<float *>(test->device);
+    m_params.max_depth = d.max_depth;
+    m_camera = d.camera;
+    m_dirty = true;
+    return true;
+}
+
+void WavefrontPTPass::SetCamera(const pt_camera_desc &camera) noexcept {
+    m_camera = camera;
+    m_dirty = true;
+}
+void WavefrontPTPass::SetMaxDepth(uint32_t depth) noexcept {
+    m_params.max_depth = depth;
+    m_dirty = true;
+}
+void WavefrontPTPass::SetAccumulate(bool on) noexcept {
+    m_accumulate = on;
+    m_dirty = true;
+}
+
+// PTPass::OnRun (example/path_tracer/pt_pass.cpp:39-57)
+void WavefrontPTPass::OnRun() noexcept {
+    if (!m_scene) return;
+    if (m_dirty) {
+        pt_scene_set_camera(m_scene, &m_camera);
+        m_params.accumulate = m_accumulate ? 1 : 0;
+        m_params.sample_cnt = 0;
+        m_params.seed = 0;
+        m_dirty = false;
+    }
+    m_status = pt_render(m_scene, &m_params, &m_fb, nullptr);
+    if (m_status != PT_OK) {
+        m_error = pt_error();
+        return;
+    }
+    m_params.sample_cnt += m_params.accumulate;
+    ++m_params.seed;
+}
+
+void WavefrontPTPass::Inspector() noexcept {
+    // The reference draws max depth / accumulate controls with ImGui
+    // (pt_pass.cpp:256-268); headless, they are SetMaxDepth / SetAccumulate.
+}
+
+}  // namespace pt
+}  // namespace Pupil

@@ -1,0 +1,115 @@
+// pass.h -- headless mirror of PupilOptixLab's pass / system API over the
+// tracer's C-ABI (include/pt_api.h).
+//
+//   Pupil::Pass              framework/system/pass.h:22-43 (name, OnRun, Inspector, timed Run)
+//   Pupil::BufferManager     framework/system/buffer.h:44-63 (named device buffers)
+//   Pupil::System            framework/system/system.h:22-41 (Init, AddPass, SetScene, Run, Destroy)
+//   Pupil::pt::WavefrontPTPass  the drop-in for pt::PTPass (example/path_tracer/pt_pass.h:21-41):
+//                            one frame (1 spp) per OnRun, sample count and seed advanced per
+//                            frame, accumulation restarted when the camera or scene changes.
+// There is no GUI thread: System::Run(frames) runs the passes on the calling thread.
+#pragma once
+
+#include <atomic>
+#include <map>
+#include <memory>
+#include <string>
+#include <string_view>
+#include <vector>
+
+#include "pt_api.h"
+#include "scene.h"
+
+namespace Pupil {
+
+enum class EPassTag : unsigned { None = 0, Pre = 1 << 0, Post = 1 << 1 };
+
+class Pass {
+public:
+    Pass(std::string_view name, EPassTag tag = EPassTag::None) noexcept;
+    virtual ~Pass() noexcept = default;
+    virtual void OnRun() noexcept = 0;
+    virtual void Inspector() noexcept {}
+    void Run() noexcept;  // OnRun, timed (pass.cpp:6-13)
+
+    const std::string name;
+    const EPassTag tag;
+    double last_exec_ms = 0.0;
+};
+
+class BufferManager {
+public:
+    struct Buffer {
+        std::string name;
+        void *device = nullptr;
+        size_t bytes = 0;
+    };
+    Buffer *AllocBuffer(const std::string &name, size_t bytes);  // zero-filled; reused if big enough
+    Buffer *GetBuffer(const std::string &name);
+    void Destroy();
+    ~BufferManager() { Destroy(); }
+
+private:
+    std::map<std::string, std::unique_ptr<Buffer>> m_buffers;
+};
+
+class System {
+public:
+    static System *Instance();
+    bool Init(int device = 0);
+    void AddPass(Pass *pass);
+    bool SetScene(const std::string &xml_path);
+    bool SetScene(std::unique_ptr<resource::Scene> scene);
+    void Run(uint32_t frames);
+    void Destroy();
+
+    pt_context *context() const { return m_ctx; }
+    resource::Scene *scene() const { return m_scene.get(); }
+    BufferManager &buffers() { return m_buffers; }
+    const std::string &error() const { return m_error; }
+
+private:
+    pt_context *m_ctx = nullptr;
+    std::unique_ptr<resource::Scene> m_scene;
+    std::vector<Pass *> m_passes, m_pre_passes;
+    BufferManager m_buffers;
+    std::string m_error;
+};
+
+namespace pt {
+
+class WavefrontPTPass : public Pass {
+public:
+    explicit WavefrontPTPass(std::string_view name = "Path Tracing") noexcept;
+    ~WavefrontPTPass() noexcept override;
+    void OnRun() noexcept override;
+    void Inspector() noexcept override;
+
+    // SceneLoad event: upload the scene, build the BVH, allocate the pass buffers.
+    bool SetScene(resource::Scene *scene, pt_context *ctx, BufferManager &buffers) noexcept;
+    // CameraChange event: restart accumulation with the new camera.
+    void SetCamera(const pt_camera_desc &camera) noexcept;
+    void SetMaxDepth(uint32_t depth) noexcept;
+    void SetAccumulate(bool on) noexcept;
+    void SetRng(uint32_t mode) noexcept { m_params.rng = mode; }
+    void SetBvhOptions(const pt_bvh_opts &opts) noexcept { m_bvh = opts; }
+
+    int last_status() const { return m_status; }
+    const std::string &last_error() const { return m_error; }
+    uint32_t sample_count() const { return m_params.sample_cnt; }
+    pt_scene *handle() const { return m_scene; }
+
+private:
+    pt_scene *m_scene = nullptr;
+    pt_render_params m_params{};
+    pt_frame_buffers m_fb{};
+    pt_bvh_opts m_bvh{4, 4, 0, 0};
+    pt_camera_desc m_camera{};
+    std::atomic_bool m_dirty{true};
+    bool m_accumulate = true;
+    int m_status = PT_OK;
+    std::string m_error;
+};
+
+}  // namespace pt
+}  // namespace Pupil

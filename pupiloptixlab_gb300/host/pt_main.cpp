@@ -1,0 +1,46 @@
+// pt_main.cpp -- headless counterpart of example/path_tracer/main.cpp: load a
+// mitsuba-style scene, run the WavefrontPTPass for N frames, write a PFM.
+//   pupil_pt <scene.xml> <out.pfm> [frames=64] [rng: lcg|pcg32]
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "pass.h"
+
+extern "C" int pupil_write_pfm(const char *path, const float *rgba, uint32_t w, uint32_t h);
+
+int main(int argc, char **argv) {
+    if (argc < 3) {
+        fprintf(stderr, "usage: %s <scene.xml> <out.pfm> [frames] [lcg|pcg32]\n", argv[0]);
+        return 2;
+    }
+    uint32_t frames = argc > 3 ? (uint32_t)std::stoul(argv[3]) : 64;
+    uint32_t rng = (argc > 4 && std::string(argv[4]) == "pcg32") ? PT_RNG_PCG32 : PT_RNG_REF_LCG;
+    Pupil::System *sys = Pupil::System::Instance();
+    if (!sys->Init(0)) {
+        fprintf(stderr, "%s\n", sys->error().c_str());
+        return 1;
+    }
+    Pupil::pt::WavefrontPTPass pass;
+    pass.SetRng(rng);
+    sys->AddPass(&pass);
+    if (!sys->SetScene(std::string(argv[1]))) {
+        fprintf(stderr, "%s\n", sys->error().c_str());
+        return 1;
+    }
+    sys->Run(frames);
+    if (pass.last_status() != PT_OK) {
+        fprintf(stderr, "render failed: %s\n", pass.last_error().c_str());
+        return 1;
+    }
+    uint32_t w = sys->scene()->sensor.width, h = sys->scene()->sensor.height;
+    std::vector<float> img((size_t)w * h * 4);
+    cudaMemcpy(img.data(), sys->buffers().GetBuffer("final result")->device, img.size() * 4, cudaMemcpyDeviceToHost);
+    pupil_write_pfm(argv[2], img.data(), w, h);
+    printf("%s: %ux%u, %u frames, last frame %.2f ms\n", argv[2], w, h, frames, pass.last_exec_ms);
+    sys->Destroy();
+    return 0;
+}

@@ -1,0 +1,77 @@
+// scene.h -- mitsuba3-style scene loading into the tracer's scene descriptor.
+//
+// The host-side counterpart of resource::Scene (framework/resource/scene.h:
+// 39-57): integrator, perspective sensor + film, shapes (obj, rectangle,
+// cube, sphere) with to_world transforms, the seven BSDFs plus `twosided`,
+// area emitters on shapes and the constant environment.  `$name` values are
+// substituted from <default> entries and <ref id=...> resolves named BSDFs,
+// as in framework/resource/xml/visitor.h.  Bitmap textures and environment
+// maps are reported as unsupported.
+#pragma once
+
+#include <map>
+#include <string>
+#include <vector>
+
+#include "pt_api.h"
+
+namespace Pupil::resource {
+
+struct Mesh {
+    std::vector<float> positions, normals, texcoords;
+    std::vector<uint32_t> indices;
+};
+
+struct ShapeInstance {
+    std::string id;
+    uint32_t shape_type = PT_SHAPE_MESH;
+    uint32_t shape_index = 0;
+    uint32_t material = 0;
+    uint32_t flags = 0;
+    float to_world[16];
+    bool is_emitter = false;
+    float radiance[3] = {0, 0, 0};
+};
+
+struct Sensor {
+    float fov = 90.f;  // vertical, degrees (after the fov_axis conversion)
+    float near_clip = 0.01f;
+    float far_clip = 10000.f;
+    float to_world[16];  // Pupil convention: +X right, +Y up, +Z away from the view
+    uint32_t width = 768, height = 576;
+};
+
+class Scene {
+public:
+    uint32_t max_depth = 1;
+    Sensor sensor;
+    std::vector<Mesh> meshes;
+    std::vector<pt_sphere_desc> spheres;
+    std::vector<pt_material_desc> materials;
+    std::vector<ShapeInstance> shape_instances;
+    bool has_env = false;
+    float env_radiance[3] = {0, 0, 0};
+
+    bool LoadFromXML(const std::string &path);
+    bool LoadFromString(const std::string &text, const std::string &root_dir);
+    const std::string &error() const { return m_error; }
+
+    // Descriptor pointing into this object (valid until the scene changes).
+    const pt_scene_desc &Desc();
+    pt_camera_desc Camera() const;
+
+private:
+    std::string m_error;
+    std::string m_root;
+    std::map<std::string, std::string> m_defaults;
+    std::map<std::string, uint32_t> m_named_bsdf;
+    std::vector<pt_mesh_desc> m_mesh_descs;
+    std::vector<pt_instance_desc> m_inst_descs;
+    pt_scene_desc m_desc{};
+    friend struct Loader;
+};
+
+// Wavefront OBJ (v / vt / vn / f, polygons fan-triangulated).
+bool LoadObj(const std::string &path, Mesh &out, std::string &error);
+
+}  // namespace Pupil::resource

@@ -1,0 +1,76 @@
+"""ctypes access to the C++ host layer (libpupil_host.so): the mitsuba-style
+scene loader and the headless System + WavefrontPTPass."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+from .build import HOST_LIB
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        abi.load()  # libpt_gb300.so first (libpupil_host.so links it)
+        if not HOST_LIB.exists():
+            raise RuntimeError(f"{HOST_LIB} is missing: run __graft_entry__.build()")
+        lib = C.CDLL(str(HOST_LIB))
+        lib.pupil_host_last_error.argtypes = [C.c_char_p, C.c_size_t]
+        lib.pupil_scene_load.argtypes = [C.c_char_p, C.c_int, C.POINTER(C.c_void_p)]
+        lib.pupil_scene_desc.argtypes = [C.c_void_p]
+        lib.pupil_scene_desc.restype = C.POINTER(abi.SceneDesc)
+        lib.pupil_scene_free.argtypes = [C.c_void_p]
+        lib.pupil_scene_free.restype = None
+        lib.pupil_run_scene.argtypes = [C.c_char_p, C.c_int, C.c_uint32, C.c_uint32, C.c_void_p,
+                                        C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
+        lib.pupil_write_pfm.argtypes = [C.c_char_p, C.c_void_p, C.c_uint32, C.c_uint32]
+        _lib = lib
+    return _lib
+
+
+def last_error() -> str:
+    buf = C.create_string_buffer(1024)
+    load().pupil_host_last_error(buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
+class XmlScene:
+    """A scene loaded by the C++ loader; usable wherever a scenes.Scene is
+    (GpuScene, the oracle): .desc(), .width, .height, .max_depth."""
+
+    def __init__(self, path_or_text: str, is_text: bool = False):
+        self.lib = load()
+        h = C.c_void_p()
+        st = self.lib.pupil_scene_load(path_or_text.encode(), 1 if is_text else 0, C.byref(h))
+        if st != 0:
+            raise abi.PtError(st, "pupil_scene_load", last_error())
+        self.handle = h
+        d = self.desc()
+        self.width, self.height, self.max_depth = d.width, d.height, d.max_depth
+
+    def desc(self) -> abi.SceneDesc:
+        return self.lib.pupil_scene_desc(self.handle).contents
+
+    def __del__(self):
+        if getattr(self, "handle", None):
+            self.lib.pupil_scene_free(self.handle)
+            self.handle = None
+
+
+def run_scene(path_or_text: str, frames: int, rng: int = abi.RNG_REF_LCG, is_text: bool = False) -> np.ndarray:
+    """System + WavefrontPTPass for `frames` frames; returns the final frame (h*w, 4)."""
+    lib = load()
+    w, h = C.c_uint32(), C.c_uint32()
+    st = lib.pupil_run_scene(path_or_text.encode(), 1 if is_text else 0, frames, rng, None, C.byref(w), C.byref(h))
+    if st != 0:
+        raise abi.PtError(st, "pupil_run_scene", last_error())
+    out = np.zeros((w.value * h.value, 4), np.float32)
+    st = lib.pupil_run_scene(path_or_text.encode(), 1 if is_text else 0, frames, rng,
+                             out.ctypes.data_as(C.c_void_p), C.byref(w), C.byref(h))
+    if st != 0:
+        raise abi.PtError(st, "pupil_run_scene", last_error())
+    return out
