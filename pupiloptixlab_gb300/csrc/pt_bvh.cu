@@ -667,7 +667,7 @@ int pt_bvh_build_impl(pt_scene *s, const pt_bvh_opts *o, cudaStream_t st) {
     d.prims = s->prims_bvh.as<float4>();
     d.width = o->width;
     d.num_nodes = bs.num_nodes;
-    uint32_t max_smem = (uint32_t)std::max(0, s->ctx->max_smem_per_block - 64 * 1024) / (32 * K);
+    uint32_t max_smem = (uint32_t)std::max(0, s->max_smem_per_block - 64 * 1024) / (32 * K);
     d.smem_nodes = std::min<uint32_t>(std::min(o->smem_nodes, bs.num_nodes), max_smem);
     s->bvh_built = true;
     return PT_OK;

@@ -52,7 +52,10 @@ struct RenderWorkspace {
 };
 
 struct pt_scene {
-    pt_context *ctx = nullptr;
+    pt_context *ctx = nullptr;  // creating context (may be destroyed before the scene)
+    int device = 0;             // copies of the context's device facts
+    int num_sms = 0;
+    int max_smem_per_block = 0;
     pt_scene_desc desc_shallow{};  // sizes only (pointers are not kept)
     uint32_t num_tris = 0, num_spheres = 0, num_prims = 0;
     uint32_t num_vertices = 0;

@@ -581,8 +581,8 @@ struct Launcher {
         int occ_t = 0, occ_s = 0;
         PT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_t, k_ext, tb, smem));
         PT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, k_shade, 256, 0));
-        const uint32_t grid_trace = (uint32_t)std::max(1, occ_t) * s->ctx->num_sms;
-        const uint32_t grid_shade = (uint32_t)std::max(1, occ_s) * s->ctx->num_sms;
+        const uint32_t grid_trace = (uint32_t)std::max(1, occ_t) * s->num_sms;
+        const uint32_t grid_shade = (uint32_t)std::max(1, occ_s) * s->num_sms;
 
         PT_CUDA_TRY(cudaMemsetAsync(ws.counters.ptr, 0, 256, st));
         Timer tm;
@@ -666,7 +666,7 @@ struct Launcher {
         PT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, tb, smem));
         uint32_t *c = s->ws.counters.as<uint32_t>();
         PT_CUDA_TRY(cudaMemsetAsync(c, 0, 256, st));
-        if (n) kern<<<(uint32_t)std::max(1, occ) * s->ctx->num_sms, tb, smem, st>>>(
+        if (n) kern<<<(uint32_t)std::max(1, occ) * s->num_sms, tb, smem, st>>>(
             d, reinterpret_cast<const float4 *>(rays), reinterpret_cast<float4 *>(hits), n, c + kWorkExtend, c + kOverflow);
         PT_CUDA_TRY(cudaGetLastError());
         uint32_t ovf = 0;

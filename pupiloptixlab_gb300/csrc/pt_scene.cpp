@@ -425,6 +425,10 @@ int build_scene(pt_scene *s, const pt_scene_desc *d) {
 
 }  // namespace
 
+// Entry points start by clearing the runtime's last-error state, so that an
+// error left behind by some other call in the process is not reported here.
+static inline void clear_stale_cuda_error() { (void)cudaGetLastError(); }
+
 void pt_set_error(const char *fmt, ...) {
     char buf[1024];
     va_list ap;
@@ -475,6 +479,7 @@ int pt_last_error(char *buf, size_t n) {
 }
 
 int pt_context_create(const pt_device_opts *opts, pt_context **out) {
+    clear_stale_cuda_error();
     if (!out) { pt_set_error("out is NULL"); return PT_ERR_INVALID; }
     *out = nullptr;
     int count = 0;
@@ -500,11 +505,15 @@ int pt_context_destroy(pt_context *ctx) {
 }
 
 int pt_scene_upload(pt_context *ctx, const pt_scene_desc *desc, pt_scene **out) {
+    clear_stale_cuda_error();
     if (!ctx || !out) { pt_set_error("context or out is NULL"); return PT_ERR_INVALID; }
     *out = nullptr;
     PT_CUDA_TRY(cudaSetDevice(ctx->device));
     auto s = std::make_unique<pt_scene>();
     s->ctx = ctx;
+    s->device = ctx->device;
+    s->num_sms = ctx->num_sms;
+    s->max_smem_per_block = ctx->max_smem_per_block;
     int st = build_scene(s.get(), desc);
     if (st != PT_OK) return st;
     PT_CUDA_TRY(cudaEventCreate(&s->ev0));
@@ -514,8 +523,11 @@ int pt_scene_upload(pt_context *ctx, const pt_scene_desc *desc, pt_scene **out) 
 }
 
 int pt_scene_destroy(pt_scene *scene) {
-    if (scene) cudaSetDevice(scene->ctx->device);
-    delete scene;
+    if (scene) {
+        cudaSetDevice(scene->device);
+        delete scene;
+        clear_stale_cuda_error();
+    }
     return PT_OK;
 }
 
@@ -533,6 +545,7 @@ int pt_scene_num_prims(const pt_scene *scene, uint32_t *nt, uint32_t *ns) {
 }
 
 int pt_scene_update_vertices(pt_scene *scene, uint32_t mesh, const float *positions, uint32_t num_vertices) {
+    clear_stale_cuda_error();
     if (!scene || !positions) { pt_set_error("scene or positions is NULL"); return PT_ERR_INVALID; }
     if (mesh >= scene->mesh_num_vertices.size() || num_vertices != scene->mesh_num_vertices[mesh]) {
         pt_set_error("mesh %u: expected %u vertices", mesh, mesh < scene->mesh_num_vertices.size() ? scene->mesh_num_vertices[mesh] : 0);
@@ -540,7 +553,7 @@ int pt_scene_update_vertices(pt_scene *scene, uint32_t mesh, const float *positi
     }
     for (uint64_t v = 0; v < 3ull * num_vertices; v++)
         if (!std::isfinite(positions[v])) { pt_set_error("non-finite vertex coordinate"); return PT_ERR_INVALID; }
-    PT_CUDA_TRY(cudaSetDevice(scene->ctx->device));
+    PT_CUDA_TRY(cudaSetDevice(scene->device));
     int st = scene->mesh_obj_pos.ensure(std::max<size_t>(12ull * num_vertices, 16));
     if (st != PT_OK) return st;
     PT_CUDA_TRY(cudaMemcpy(scene->mesh_obj_pos.ptr, positions, 12ull * num_vertices, cudaMemcpyHostToDevice));
@@ -548,19 +561,21 @@ int pt_scene_update_vertices(pt_scene *scene, uint32_t mesh, const float *positi
 }
 
 int pt_bvh_build(pt_scene *scene, const pt_bvh_opts *opts, void *stream) {
+    clear_stale_cuda_error();
     if (!scene) { pt_set_error("scene is NULL"); return PT_ERR_INVALID; }
     pt_bvh_opts o{4, 4, 0, 0};
     if (opts) o = *opts;
     if (o.width != 2 && o.width != 4 && o.width != 8) { pt_set_error("BVH width must be 2, 4 or 8"); return PT_ERR_INVALID; }
     if (o.max_leaf_size < 1 || o.max_leaf_size > 15) { pt_set_error("max_leaf_size must be in 1..15"); return PT_ERR_INVALID; }
-    PT_CUDA_TRY(cudaSetDevice(scene->ctx->device));
+    PT_CUDA_TRY(cudaSetDevice(scene->device));
     return pt_bvh_build_impl(scene, &o, static_cast<cudaStream_t>(stream));
 }
 
 int pt_bvh_refit(pt_scene *scene, void *stream) {
+    clear_stale_cuda_error();
     if (!scene) { pt_set_error("scene is NULL"); return PT_ERR_INVALID; }
     if (!scene->bvh_built) { pt_set_error("pt_bvh_refit before pt_bvh_build"); return PT_ERR_STATE; }
-    PT_CUDA_TRY(cudaSetDevice(scene->ctx->device));
+    PT_CUDA_TRY(cudaSetDevice(scene->device));
     return pt_bvh_refit_impl(scene, static_cast<cudaStream_t>(stream));
 }
 
@@ -571,10 +586,11 @@ int pt_bvh_get_stats(const pt_scene *scene, pt_bvh_stats *out) {
 }
 
 int pt_render(pt_scene *scene, const pt_render_params *params, const pt_frame_buffers *fb, void *stream) {
+    clear_stale_cuda_error();
     if (!scene || !params || !fb || !fb->accum) { pt_set_error("scene, params, buffers or accum is NULL"); return PT_ERR_INVALID; }
     if (!scene->bvh_built) { pt_set_error("pt_render before pt_bvh_build"); return PT_ERR_STATE; }
     if (params->rng != PT_RNG_REF_LCG && params->rng != PT_RNG_PCG32) { pt_set_error("unknown rng mode"); return PT_ERR_INVALID; }
-    PT_CUDA_TRY(cudaSetDevice(scene->ctx->device));
+    PT_CUDA_TRY(cudaSetDevice(scene->device));
     return pt_render_impl(scene, params, fb, static_cast<cudaStream_t>(stream));
 }
 
@@ -585,19 +601,22 @@ int pt_render_get_stats(const pt_scene *scene, pt_render_stats *out) {
 }
 
 int pt_trace_rays(pt_scene *scene, const float *rays, float *hits, uint32_t n, int anyhit, void *stream) {
+    clear_stale_cuda_error();
     if (!scene || (n && (!rays || !hits))) { pt_set_error("scene, rays or hits is NULL"); return PT_ERR_INVALID; }
     if (!scene->bvh_built) { pt_set_error("pt_trace_rays before pt_bvh_build"); return PT_ERR_STATE; }
-    PT_CUDA_TRY(cudaSetDevice(scene->ctx->device));
+    PT_CUDA_TRY(cudaSetDevice(scene->device));
     return pt_trace_rays_impl(scene, rays, hits, n, anyhit, static_cast<cudaStream_t>(stream));
 }
 
 int pt_bsdf_eval_batch(const float *bsdf, const float *wo, const float *wi, float *f, float *pdf, uint32_t n, void *stream) {
+    clear_stale_cuda_error();
     if (n && (!bsdf || !wo || !wi || !f || !pdf)) { pt_set_error("NULL buffer"); return PT_ERR_INVALID; }
     return pt_bsdf_eval_impl(bsdf, wo, wi, f, pdf, n, static_cast<cudaStream_t>(stream));
 }
 
 int pt_bsdf_sample_batch(const float *bsdf, const float *wo, uint32_t *rng, float *wi, float *f, float *pdf,
                          uint32_t *type, uint32_t n, void *stream) {
+    clear_stale_cuda_error();
     if (n && (!bsdf || !wo || !rng || !wi || !f || !pdf || !type)) { pt_set_error("NULL buffer"); return PT_ERR_INVALID; }
     return pt_bsdf_sample_impl(bsdf, wo, rng, wi, f, pdf, type, n, static_cast<cudaStream_t>(stream));
 }

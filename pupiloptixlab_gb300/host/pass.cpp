@@ -111,6 +111,8 @@ void System::Run(uint32_t frames) {
 }
 
 void System::Destroy() {
+    for (Pass *p : m_passes)
+        if (auto *pt = dynamic_cast<pt::WavefrontPTPass *>(p)) pt->ReleaseScene();
     m_passes.clear();
     m_pre_passes.clear();
     m_buffers.Destroy();
@@ -127,8 +129,12 @@ WavefrontPTPass::WavefrontPTPass(std::string_view n) noexcept : Pass(n) {
     m_params.rng = PT_RNG_REF_LCG;
 }
 
-WavefrontPTPass::~WavefrontPTPass() noexcept {
+WavefrontPTPass::~WavefrontPTPass() noexcept { ReleaseScene(); }
+
+void WavefrontPTPass::ReleaseScene() noexcept {
     if (m_scene) pt_scene_destroy(m_scene);
+    m_scene = nullptr;
+    m_fb = pt_frame_buffers{};
 }
 
 bool WavefrontPTPass::SetScene(resource::Scene *scene, pt_context *ctx, BufferManager &buffers) noexcept {

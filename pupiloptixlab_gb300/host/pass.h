@@ -93,6 +93,8 @@ public:
     void SetAccumulate(bool on) noexcept;
     void SetRng(uint32_t mode) noexcept { m_params.rng = mode; }
     void SetBvhOptions(const pt_bvh_opts &opts) noexcept { m_bvh = opts; }
+    // Frees the device scene (System::Destroy calls it before destroying the context).
+    void ReleaseScene() noexcept;
 
     int last_status() const { return m_status; }
     const std::string &last_error() const { return m_error; }
