@@ -297,6 +297,19 @@ int pt_bvh_get_stats(const pt_scene *scene, pt_bvh_stats *out);
 /* ---- rendering -------------------------------------------------------- */
 int pt_render(pt_scene *scene, const pt_render_params *params, const pt_frame_buffers *fb, void *stream);
 int pt_render_get_stats(const pt_scene *scene, pt_render_stats *out);
+/* No counterpart in the reference.  Same result as pt_render, for callers
+ * that cannot allocate device memory (hosts that hand out device memory only
+ * from their own fixed pools or budgets, and interactive callers that must not
+ * allocate per frame, since an allocation can synchronise the device).  The
+ * render's path state lives in a fixed device array inside the library (about
+ * 9.3 MiB, held by every GPU that loads the library until exit) instead of a
+ * workspace allocated on first use; the call makes no allocation.  Limit: at
+ * most 65,536 pixels (width * height) per call; larger images are rejected
+ * with PT_ERR_INVALID.  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress), so make that first call before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU (on
+ * different streams or threads) race.  No statistics are recorded. */
+int pt_render_noalloc(pt_scene *scene, const pt_render_params *params, const pt_frame_buffers *fb, void *stream);
 
 /* ---- query entry points used by the parity tests ---------------------- */
 /* rays: n * 8 floats (ox,oy,oz,tmin, dx,dy,dz,tmax), hits: n * 4 floats

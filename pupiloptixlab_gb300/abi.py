@@ -122,6 +122,7 @@ PROTOTYPES = [
     ("pt_bvh_get_stats", C.c_int, [C.c_void_p, C.POINTER(BvhStats)]),
     ("pt_render", C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.POINTER(FrameBuffers), C.c_void_p]),
     ("pt_render_get_stats", C.c_int, [C.c_void_p, C.POINTER(RenderStats)]),
+    ("pt_render_noalloc", C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.POINTER(FrameBuffers), C.c_void_p]),
     ("pt_trace_rays", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_int, C.c_void_p]),
     ("pt_bsdf_eval_batch", C.c_int, [C.c_void_p] * 5 + [C.c_uint32, C.c_void_p]),
     ("pt_bsdf_sample_batch", C.c_int, [C.c_void_p] * 7 + [C.c_uint32, C.c_void_p]),

@@ -25,6 +25,7 @@
 #include "pt_traverse.cuh"
 
 #include <algorithm>
+#include <mutex>
 
 namespace {
 using namespace ptd;
@@ -712,4 +713,169 @@ int pt_bsdf_sample_impl(const float *bsdf, const float *wo, uint32_t *rng, float
     PT_CUDA_TRY(cudaGetLastError());
     PT_CUDA_TRY(cudaStreamSynchronize(st));
     return PT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// pt_render_noalloc: the same wavefront render for callers that cannot
+// allocate device memory themselves (hosts that hand out device memory only
+// from their own fixed pools or budgets, and interactive callers that must
+// not allocate per frame, since an allocation can synchronise the device).
+// The path state lives in the file-scope array below instead of the scene's
+// workspace, so a call allocates nothing.  Limit: at most kNoAllocMaxPixels
+// pixels per call (frames are packed into waves of at most that many slots).
+// Every call shares the array; calls that overlap on the GPU (on different
+// streams or threads) race on it.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr uint32_t kNoAllocMaxPixels = 1u << 16;  // 65,536 path slots
+constexpr size_t kNoAllocCounterBytes = 256;
+constexpr size_t kNoAllocSlotBytes = 16 * 8 + 8 + 4 * 3;  // 8 float4 arrays, rng, meta, two queues = 148 B
+constexpr size_t kNoAllocScratchBytes = kNoAllocCounterBytes + kNoAllocSlotBytes * kNoAllocMaxPixels;
+
+// About 9.3 MiB, held by every GPU that loads the library until the process exits.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+std::mutex g_noalloc_mutex;
+void *g_noalloc_ptr[128] = {};  // device address of the array, per CUDA device
+
+// Device address of g_noalloc_scratch on the current device, looked up once
+// per device (the first call on a device does the look-up).
+int noalloc_scratch(int device, unsigned char **out) {
+    if (device < 0 || device >= 128) {
+        pt_set_error("device ordinal %d out of range", device);
+        return PT_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[device]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            pt_set_error("cudaGetSymbolAddress(g_noalloc_scratch) failed: %s", cudaGetErrorString(e));
+            return PT_ERR_CUDA;
+        }
+        g_noalloc_ptr[device] = p;
+    }
+    *out = static_cast<unsigned char *>(g_noalloc_ptr[device]);
+    return PT_OK;
+}
+
+template <int K>
+int render_noalloc(pt_scene *s, const pt_render_params *p, const pt_frame_buffers *fb, unsigned char *scratch,
+                   cudaStream_t st) {
+    const DevScene &d = s->dev;
+    const uint32_t npix = d.width_px * d.height_px;
+    const uint32_t max_depth = p->max_depth ? p->max_depth : s->desc_shallow.max_depth;
+    const uint32_t frames_per_wave = std::max<uint32_t>(1, std::min(kNoAllocMaxPixels / npix, p->spp));
+    const size_t cap = kNoAllocMaxPixels;
+    State stt;
+    unsigned char *q = scratch + kNoAllocCounterBytes;
+    auto take = [&](size_t bytes_per_slot) {
+        unsigned char *r = q;
+        q += bytes_per_slot * cap;
+        return r;
+    };
+    stt.counters = reinterpret_cast<uint32_t *>(scratch);
+    stt.stats = reinterpret_cast<unsigned long long *>(stt.counters + kStatBase);
+    stt.ray_o = reinterpret_cast<float4 *>(take(16));
+    stt.ray_d = reinterpret_cast<float4 *>(take(16));
+    stt.hit = reinterpret_cast<float4 *>(take(16));
+    stt.thr = reinterpret_cast<float4 *>(take(16));
+    stt.rad = reinterpret_cast<float4 *>(take(16));
+    stt.sh_o = reinterpret_cast<float4 *>(take(16));
+    stt.sh_d = reinterpret_cast<float4 *>(take(16));
+    stt.sh_c = reinterpret_cast<float4 *>(take(16));
+    stt.rng = reinterpret_cast<uint2 *>(take(8));
+    stt.meta = reinterpret_cast<uint32_t *>(take(4));
+    uint32_t *q0 = reinterpret_cast<uint32_t *>(take(4));
+    uint32_t *q1 = reinterpret_cast<uint32_t *>(take(4));
+    Outputs out;
+    out.accum = reinterpret_cast<float4 *>(fb->accum);
+    out.frame = reinterpret_cast<float4 *>(fb->frame);
+    out.albedo = fb->albedo;
+    out.normal = fb->normal;
+    out.test = fb->test;
+
+    const int tb = p->block_size ? (int)p->block_size : 128;
+    const size_t smem = (size_t)d.smem_nodes * 32 * K + (size_t)kShortStack * 8 * tb;
+    auto k_ext = k_trace_queue<K, false, false>;
+    auto k_sh = k_trace_queue<K, true, false>;
+    int e;
+    if ((e = set_smem(k_ext, smem)) != PT_OK || (e = set_smem(k_sh, smem)) != PT_OK) return e;
+    int occ_t = 0, occ_s = 0;
+    PT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_t, k_ext, tb, smem));
+    PT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, k_shade, 256, 0));
+    const uint32_t grid_trace = (uint32_t)std::max(1, occ_t) * s->num_sms;
+    const uint32_t grid_shade = (uint32_t)std::max(1, occ_s) * s->num_sms;
+
+    // the array keeps the previous call's contents: clear the counters and statistics
+    PT_CUDA_TRY(cudaMemsetAsync(scratch, 0, kNoAllocCounterBytes, st));
+    for (uint32_t f0 = 0; f0 < p->spp; f0 += frames_per_wave) {
+        Wave w;
+        w.npix = npix;
+        w.frames = std::min(frames_per_wave, p->spp - f0);
+        w.frame0 = f0;
+        w.seed0 = p->seed;
+        w.cnt0 = p->sample_cnt;
+        w.last_frame = p->spp - 1;
+        w.max_depth = max_depth;
+        w.rng_mode = p->rng;
+        w.accumulate = p->accumulate;
+        stt.q_in = q0;
+        stt.q_out = q1;
+        k_raygen<<<nblocks((size_t)w.frames * npix, 256), 256, 0, st>>>(d, stt, w);
+        for (uint32_t b = 0; b < max_depth; b++) {
+            k_ext<<<grid_trace, tb, smem, st>>>(d, stt);
+            k_shade<<<grid_shade, 256, 0, st>>>(d, stt, w, out);
+            k_sh<<<grid_trace, tb, smem, st>>>(d, stt);
+            k_advance<<<1, 1, 0, st>>>(stt.counters);
+            std::swap(stt.q_in, stt.q_out);
+        }
+        k_accumulate<<<nblocks(npix, 256), 256, 0, st>>>(stt, w, out);
+    }
+    PT_CUDA_TRY(cudaGetLastError());
+    uint32_t ovf = 0;
+    PT_CUDA_TRY(cudaMemcpyAsync(&ovf, stt.counters + kOverflow, sizeof(ovf), cudaMemcpyDeviceToHost, st));
+    PT_CUDA_TRY(cudaStreamSynchronize(st));
+    if (ovf) {
+        pt_set_error("traversal stack overflow");
+        return PT_ERR_OOB;
+    }
+    return PT_OK;
+}
+
+}  // namespace
+
+extern "C" int pt_render_noalloc(pt_scene *scene, const pt_render_params *params, const pt_frame_buffers *fb,
+                                 void *stream) {
+    if (!scene || !params || !fb || !fb->accum) {
+        pt_set_error("scene, params, buffers or accum is NULL");
+        return PT_ERR_INVALID;
+    }
+    if (!scene->bvh_built) {
+        pt_set_error("pt_render_noalloc before pt_bvh_build");
+        return PT_ERR_STATE;
+    }
+    if (params->rng != PT_RNG_REF_LCG && params->rng != PT_RNG_PCG32) {
+        pt_set_error("unknown rng mode");
+        return PT_ERR_INVALID;
+    }
+    const uint64_t npix = (uint64_t)scene->dev.width_px * scene->dev.height_px;
+    if (npix > kNoAllocMaxPixels) {
+        pt_set_error("pt_render_noalloc: %llu pixels exceed the limit of %u pixels per call "
+                     "(its path state lives in a fixed %zu-byte device array); use pt_render",
+                     (unsigned long long)npix, kNoAllocMaxPixels, kNoAllocScratchBytes);
+        return PT_ERR_INVALID;
+    }
+    if (params->spp == 0) return PT_OK;
+    PT_CUDA_TRY(cudaSetDevice(scene->device));
+    unsigned char *scratch = nullptr;
+    int e = noalloc_scratch(scene->device, &scratch);
+    if (e != PT_OK) return e;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    switch (scene->dev.width) {
+        case 2: return render_noalloc<2>(scene, params, fb, scratch, st);
+        case 4: return render_noalloc<4>(scene, params, fb, scratch, st);
+        default: return render_noalloc<8>(scene, params, fb, scratch, st);
+    }
 }

@@ -1,0 +1,68 @@
+"""pt_render_noalloc: the render entry point for callers that cannot allocate
+device memory (hosts that only hand out memory from their own fixed pools or
+budgets, and interactive callers that must not allocate per frame).  Its path
+state lives in a fixed device array inside the library, so it works for
+images of at most 65,536 pixels.  Called through the C-ABI and compared with
+pt_render on two calls in a row (the array keeps the previous call's contents,
+which must not leak into the next call).  The file is named so that pytest
+collects it last."""
+import ctypes as C
+
+import numpy as np
+import pytest
+import torch
+
+from pupiloptixlab_gb300 import abi, scenes
+from pupiloptixlab_gb300.api import GpuScene
+
+pytestmark = pytest.mark.gpu
+
+
+def noalloc_render(g, spp, seed, rng, accumulate=True):
+    bufs = g.alloc_buffers()
+    p = abi.RenderParams(spp, 0, seed, 0, 1 if accumulate else 0, rng, 0, 0, 0)
+    fb = abi.FrameBuffers(*[bufs[k].data_ptr() for k in ("accum", "frame", "albedo", "normal", "test")])
+    st = g.lib.pt_render_noalloc(g.handle, C.byref(p), C.byref(fb), C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    abi.check(st, "pt_render_noalloc", g.lib)
+    torch.cuda.synchronize()
+    return {k: v.cpu().numpy() for k, v in bufs.items()}
+
+
+def existing_render(g, spp, seed, rng, accumulate=True):
+    out = g.render(spp, seed=seed, rng=rng, accumulate=accumulate)
+    torch.cuda.synchronize()
+    return {k: v.cpu().numpy() for k, v in out.items()}
+
+
+def same(a, b):
+    # the test tolerance of the render parity tests (1e-4), and in fact identical bits
+    assert np.allclose(a, b, rtol=1e-4, atol=1e-4)
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+@pytest.mark.parametrize("make", [lambda: scenes.material_spheres(96, 64), lambda: scenes.cornell_box(128, 128)],
+                         ids=["materials", "cornell"])
+def test_noalloc_matches_pt_render_twice(cuda_ctx, make):
+    g = GpuScene(cuda_ctx, make())
+    # first call: 8 frames in waves of at most 65,536 path slots
+    a = noalloc_render(g, 8, 0, abi.RNG_PCG32)
+    ref_a = existing_render(g, 8, 0, abi.RNG_PCG32)
+    for k in ("accum", "frame", "albedo", "normal", "test"):
+        same(a[k], ref_a[k])
+    # second call right after, different seed, count and stream kind
+    b = noalloc_render(g, 3, 5, abi.RNG_REF_LCG)
+    ref_b = existing_render(g, 3, 5, abi.RNG_REF_LCG)
+    for k in ("accum", "frame", "albedo", "normal", "test"):
+        same(b[k], ref_b[k])
+    assert not np.array_equal(a["accum"], b["accum"])
+
+
+def test_noalloc_rejects_images_over_the_limit(cuda_ctx):
+    g = GpuScene(cuda_ctx, scenes.cornell_box(320, 240))  # 76,800 pixels > 65,536
+    bufs = g.alloc_buffers()
+    p = abi.RenderParams(1, 0, 0, 0, 1, abi.RNG_PCG32, 0, 0, 0)
+    fb = abi.FrameBuffers(*[bufs[k].data_ptr() for k in ("accum", "frame", "albedo", "normal", "test")])
+    st = g.lib.pt_render_noalloc(g.handle, C.byref(p), C.byref(fb), None)
+    assert st == 1  # PT_ERR_INVALID
+    msg = abi.last_error(g.lib)
+    assert "76800 pixels exceed the limit of 65536" in msg
