@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--smem-nodes", type=int, default=0)
     ap.add_argument("--block-size", type=int, default=0)
     ap.add_argument("--wave-spp", type=int, default=0)
+    ap.add_argument("--material-sort", action="store_true", help="bin hits by material before shading")
+    ap.add_argument("--no-graph", action="store_true", help="launch kernels directly instead of a CUDA graph")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -231,13 +233,14 @@ def main():
     bst = g.bvh_stats()
     buffers = g.alloc_buffers()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    base_flags = (abi.RENDER_MATERIAL_SORT if args.material_sort else 0) | (abi.RENDER_NO_GRAPH if args.no_graph else 0)
     kw = dict(rng=abi.RNG_PCG32, block_size=args.block_size, wave_spp=args.wave_spp, buffers=buffers)
 
     for w in range(args.warmup):
-        g.render(args.spp, seed=1000 + w * args.spp, **kw)
+        g.render(args.spp, seed=1000 + w * args.spp, flags=base_flags, **kw)
     torch.cuda.synchronize()
     # identical untimed render with traversal counters (same seeds as step 0)
-    g.render(args.spp, seed=0, flags=abi.RENDER_COUNTERS, **kw)
+    g.render(args.spp, seed=0, flags=abi.RENDER_COUNTERS | base_flags, **kw)
     torch.cuda.synchronize()
     cst = g.render_stats()
 
@@ -250,7 +253,7 @@ def main():
         flush.fill_(float(step))
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        g.render(args.spp, seed=step * args.spp, flags=abi.RENDER_KERNEL_TIMING, **kw)
+        g.render(args.spp, seed=step * args.spp, flags=abi.RENDER_KERNEL_TIMING | base_flags, **kw)
         e1.record(stream)
         e1.synchronize()
         step_ms.append(e0.elapsed_time(e1))
@@ -282,7 +285,7 @@ def main():
         for step in range(args.steps):
             cam = abi.CameraDesc.from_buffer_copy(host_cam.numpy().tobytes())  # camera from pinned host memory
             g.set_camera(cam)
-            g.render(args.spp, seed=step * args.spp, **kw)
+            g.render(args.spp, seed=step * args.spp, flags=base_flags, **kw)
             host_frame.copy_(buffers["accum"], non_blocking=True)
             torch.cuda.synchronize()
         barrier()
@@ -313,6 +316,7 @@ def main():
         "config": {"workload": WORKLOAD, "width": args.width, "height": args.height, "spp": args.spp,
                    "max_depth": args.depth, "rng": "pcg32", "bvh_width": args.bvh_width, "max_leaf": args.max_leaf,
                    "smem_nodes": args.smem_nodes, "triangles": int(bst.num_prims),
+                   "material_sort": bool(args.material_sort), "cuda_graph": not args.no_graph,
                    "l2": "flushed between steps (256 MiB write, outside the timed events)",
                    "parallelism": "replicas only" if ws > 1 else "single GPU"},
         "e2e": e2e,

@@ -49,6 +49,13 @@ struct MeshInstanceRef {  // where the world vertices of one mesh instance live
 struct RenderWorkspace {
     size_t capacity = 0;  // path slots
     DevBuf ray_o, ray_d, hit, thr, rad, rng, meta, q0, q1, sh_o, sh_d, sh_c, mat_key, counters, sort_tmp;
+    size_t sort_capacity = 0;
+    // CUDA-graph replay: an internal stream (the caller's may be the legacy
+    // default stream, which cannot be captured), events that order it after
+    // and before the caller's stream, and the instantiated graph.
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+    cudaGraphExec_t exec = nullptr;
 };
 
 struct pt_scene {

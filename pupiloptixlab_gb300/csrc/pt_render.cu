@@ -167,64 +167,83 @@ PT_DI size_t smem_node_bytes(const DevScene &s) {
     return (size_t)s.smem_nodes * 32 * K;
 }
 
-// Persistent traversal over a queue: warps take 32 entries at a time.
-// ANY = false: closest hit of the extension rays (q_in entries are path slots).
-// ANY = true: shadow rays (entries are shadow-queue positions).
+// Ray sources / result sinks of the persistent traversal.
+struct ExtendSrc {  // closest hit of the active queue (entries are path slots)
+    State st;
+    PT_DI uint32_t count() const { return st.counters[kNIn]; }
+    PT_DI void load(uint32_t i, float3 &o, float3 &d, float &tmin, float &tmax, uint32_t &tag) const {
+        uint32_t slot = st.q_in[i];
+        float4 o4 = st.ray_o[slot], d4 = st.ray_d[slot];
+        o = xyz(o4);
+        d = xyz(d4);
+        tmin = o4.w;
+        tmax = d4.w;
+        tag = slot;
+    }
+    PT_DI void store(uint32_t, uint32_t slot, const TraceResult &r) const {
+        st.hit[slot] = make_float4(r.t, __int_as_float(r.prim), r.u, r.v);
+    }
+};
+struct ShadowSrc {  // any hit of the shadow queue; unoccluded rays add their NEE radiance
+    State st;
+    PT_DI uint32_t count() const { return st.counters[kNShadow]; }
+    PT_DI void load(uint32_t i, float3 &o, float3 &d, float &tmin, float &tmax, uint32_t &tag) const {
+        float4 o4 = st.sh_o[i], d4 = st.sh_d[i];
+        o = xyz(o4);
+        d = xyz(d4);
+        tmin = o4.w;
+        tmax = d4.w;
+        tag = i;
+    }
+    PT_DI void store(uint32_t i, uint32_t, const TraceResult &r) const {
+        if (r.prim >= 0) return;
+        float4 c = st.sh_c[i];
+        uint32_t ps = __float_as_uint(c.w);
+        float4 rr = st.rad[ps];
+        st.rad[ps] = make_float4(rr.x + c.x, rr.y + c.y, rr.z + c.z, rr.w);
+    }
+};
+template <bool ANY>
+struct UserSrc {  // pt_trace_rays
+    const float4 *rays;
+    float4 *hits;
+    uint32_t n;
+    PT_DI uint32_t count() const { return n; }
+    PT_DI void load(uint32_t i, float3 &o, float3 &d, float &tmin, float &tmax, uint32_t &tag) const {
+        float4 o4 = rays[2 * (size_t)i], d4 = rays[2 * (size_t)i + 1];
+        o = xyz(o4);
+        d = xyz(d4);
+        tmin = o4.w;
+        tmax = d4.w;
+        tag = i;
+    }
+    PT_DI void store(uint32_t i, uint32_t, const TraceResult &r) const {
+        if (ANY) hits[i] = make_float4(r.prim >= 0 ? 1.f : 0.f, 0.f, 0.f, 0.f);
+        else hits[i] = make_float4(r.t, __int_as_float(r.prim), r.u, r.v);
+    }
+};
+
+// Stages the top smem_nodes nodes in shared memory; returns the stack base.
+template <int K>
+PT_DI int2 *stage_smem(const DevScene &s, float4 *smem) {
+    for (uint32_t i = threadIdx.x; i < s.smem_nodes * 2 * K; i += blockDim.x) smem[i] = __ldg(s.nodes + i);
+    __syncthreads();
+    return reinterpret_cast<int2 *>(smem + s.smem_nodes * 2 * K);
+}
+
+// ANY = false: closest hit of the extension rays; ANY = true: shadow rays.
 template <int K, bool ANY, bool COUNT>
 __global__ void k_trace_queue(DevScene s, State st) {
     extern __shared__ float4 smem[];
-    float4 *snodes = smem;
-    int2 *sstack = reinterpret_cast<int2 *>(smem + s.smem_nodes * 2 * K);
-    for (uint32_t i = threadIdx.x; i < s.smem_nodes * 2 * K; i += blockDim.x) snodes[i] = __ldg(s.nodes + i);
-    __syncthreads();
-    const uint32_t n = ANY ? st.counters[kNShadow] : st.counters[kNIn];
-    uint32_t *work = st.counters + (ANY ? kWorkShadow : kWorkExtend);
-    const int lane = threadIdx.x & 31;
-    uint32_t nodes = 0, prims = 0, ovf = 0, rays = 0;
-    for (;;) {
-        uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(work, 32u);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= n) break;
-        uint32_t i = base + lane;
-        if (i < n) {
-            float4 o4, d4;
-            uint32_t slot = 0;
-            if (ANY) {
-                o4 = st.sh_o[i];
-                d4 = st.sh_d[i];
-            } else {
-                slot = st.q_in[i];
-                o4 = st.ray_o[slot];
-                d4 = st.ray_d[slot];
-            }
-            TraceResult r = traverse<K, ANY, COUNT>(s, snodes, sstack + threadIdx.x, xyz(o4), xyz(d4), o4.w, d4.w, nodes,
-                                                    prims, ovf);
-            if (COUNT) rays++;
-            if (ANY) {
-                if (r.prim < 0) {  // unoccluded: add the NEE contribution
-                    float4 c = st.sh_c[i];
-                    uint32_t ps = __float_as_uint(c.w);
-                    float4 rr = st.rad[ps];
-                    st.rad[ps] = make_float4(rr.x + c.x, rr.y + c.y, rr.z + c.z, rr.w);
-                }
-            } else {
-                st.hit[slot] = make_float4(r.t, __int_as_float(r.prim), r.u, r.v);
-            }
-        }
-    }
-    if (ovf) atomicOr(st.counters + kOverflow, 1u);
-    if (COUNT) {
-        for (int o = 16; o > 0; o >>= 1) {
-            nodes += __shfl_xor_sync(0xffffffffu, nodes, o);
-            prims += __shfl_xor_sync(0xffffffffu, prims, o);
-            rays += __shfl_xor_sync(0xffffffffu, rays, o);
-        }
-        if (lane == 0) {
-            atomicAdd(st.stats + (ANY ? kStatShNodes : kStatExtNodes), (unsigned long long)nodes);
-            atomicAdd(st.stats + (ANY ? kStatShPrims : kStatExtPrims), (unsigned long long)prims);
-            atomicAdd(st.stats + (ANY ? kStatShRays : kStatExtRays), (unsigned long long)rays);
-        }
+    int2 *sstack = stage_smem<K>(s, smem);
+    if (ANY) {
+        ShadowSrc src{st};
+        trace_persistent<K, true, COUNT>(s, smem, sstack, src, st.counters + kWorkShadow, st.counters + kOverflow,
+                                         st.stats + kStatShNodes, st.stats + kStatShPrims, st.stats + kStatShRays);
+    } else {
+        ExtendSrc src{st};
+        trace_persistent<K, false, COUNT>(s, smem, sstack, src, st.counters + kWorkExtend, st.counters + kOverflow,
+                                          st.stats + kStatExtNodes, st.stats + kStatExtPrims, st.stats + kStatExtRays);
     }
 }
 
@@ -413,6 +432,58 @@ __global__ void __launch_bounds__(256) k_shade(DevScene s, State st, Wave w, Out
 }
 
 
+// Material-sorted shading (PT_RENDER_MATERIAL_SORT): the active queue is
+// binned by the material type of each hit (0 = miss) before k_shade, so that
+// warps run one BSDF at a time.  Counting pass (block histogram in shared
+// memory, one atomic per bin and block), a one-thread scan, and a scatter pass
+// with warp-aggregated atomics (__match_any_sync groups lanes with equal keys).
+constexpr int kNumBins = 8;
+enum : int { kBinCount = 24, kBinCursor = 40 };  // word offsets in the counters block
+
+__global__ void k_bin_count(DevScene s, State st, uint8_t *keys) {
+    __shared__ uint32_t h[kNumBins];
+    if (threadIdx.x < kNumBins) h[threadIdx.x] = 0;
+    __syncthreads();
+    const uint32_t n = st.counters[kNIn];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t slot = st.q_in[i];
+        int prim = __float_as_int(st.hit[slot].y);
+        uint32_t key = 0;
+        if (prim >= 0) key = s.mats[s.inst[s.prim_inst[prim]].material].type & (kNumBins - 1);
+        keys[i] = (uint8_t)key;
+        atomicAdd(&h[key], 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x < kNumBins && h[threadIdx.x]) atomicAdd(st.counters + kBinCount + threadIdx.x, h[threadIdx.x]);
+}
+
+__global__ void k_bin_scan(uint32_t *counters) {
+    uint32_t run = 0;
+    for (int k = 0; k < kNumBins; k++) {
+        uint32_t c = counters[kBinCount + k];
+        counters[kBinCursor + k] = run;
+        counters[kBinCount + k] = 0;  // ready for the next bounce
+        run += c;
+    }
+}
+
+__global__ void k_bin_scatter(State st, const uint8_t *keys, uint32_t *q_sorted) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const uint32_t n = st.counters[kNIn];
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        uint32_t i = base + threadIdx.x;
+        bool valid = i < n;
+        uint32_t key = valid ? keys[i] : 0xffu;
+        unsigned peers = __match_any_sync(FULL, key);
+        int leader = __ffs(peers) - 1;
+        uint32_t pos = 0;
+        if (valid && lane == leader) pos = atomicAdd(st.counters + kBinCursor + key, (uint32_t)__popc(peers));
+        pos = __shfl_sync(FULL, pos, leader);
+        if (valid) q_sorted[pos + __popc(peers & ((1u << lane) - 1u))] = st.q_in[i];
+    }
+}
+
 // Accumulation, main.cu:188-196: frames of the wave in order, per pixel.
 __global__ void k_accumulate(State st, Wave w, Outputs out) {
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < w.npix; p += gridDim.x * blockDim.x) {
@@ -436,26 +507,9 @@ __global__ void k_accumulate(State st, Wave w, Outputs out) {
 template <int K, bool ANY>
 __global__ void k_trace_rays(DevScene s, const float4 *rays, float4 *hits, uint32_t n, uint32_t *work, uint32_t *ovf_flag) {
     extern __shared__ float4 smem[];
-    float4 *snodes = smem;
-    int2 *sstack = reinterpret_cast<int2 *>(smem + s.smem_nodes * 2 * K);
-    for (uint32_t i = threadIdx.x; i < s.smem_nodes * 2 * K; i += blockDim.x) snodes[i] = __ldg(s.nodes + i);
-    __syncthreads();
-    const int lane = threadIdx.x & 31;
-    uint32_t nn = 0, np = 0, ovf = 0;
-    for (;;) {
-        uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(work, 32u);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= n) break;
-        uint32_t i = base + lane;
-        if (i < n) {
-            float4 o4 = rays[2 * (size_t)i], d4 = rays[2 * (size_t)i + 1];
-            TraceResult r = traverse<K, ANY, false>(s, snodes, sstack + threadIdx.x, xyz(o4), xyz(d4), o4.w, d4.w, nn, np, ovf);
-            if (ANY) hits[i] = make_float4(r.prim >= 0 ? 1.f : 0.f, 0.f, 0.f, 0.f);
-            else hits[i] = make_float4(r.prim >= 0 ? r.t : d4.w, __int_as_float(r.prim), r.prim >= 0 ? r.u : 0.f, r.prim >= 0 ? r.v : 0.f);
-        }
-    }
-    if (ovf) atomicOr(ovf_flag, 1u);
+    int2 *sstack = stage_smem<K>(s, smem);
+    UserSrc<ANY> src{rays, hits, n};
+    trace_persistent<K, ANY, false>(s, smem, sstack, src, work, ovf_flag, nullptr, nullptr, nullptr);
 }
 
 __global__ void k_bsdf_eval(const float *bsdf, const float *wo, const float *wi, float *f, float *pdf, uint32_t n) {
@@ -585,12 +639,36 @@ struct Launcher {
         const uint32_t grid_trace = (uint32_t)std::max(1, occ_t) * s->num_sms;
         const uint32_t grid_shade = (uint32_t)std::max(1, occ_s) * s->num_sms;
 
-        PT_CUDA_TRY(cudaMemsetAsync(ws.counters.ptr, 0, 256, st));
+        const bool sort = (p->flags & PT_RENDER_MATERIAL_SORT) != 0;
+        if (sort && ws.sort_capacity < cap) {
+            if ((e = ws.mat_key.ensure(cap)) != PT_OK || (e = ws.sort_tmp.ensure(4 * cap)) != PT_OK) return e;
+            ws.sort_capacity = cap;
+        }
+        int occ_b = 0;
+        PT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_b, k_bin_scatter, 256, 0));
+        const uint32_t grid_bin = (uint32_t)std::max(1, occ_b) * s->num_sms;
+
+        // The whole render is captured into a CUDA graph on the scene's own
+        // stream (ordered after and before the caller's stream by events) and
+        // replayed; later calls update the instantiated graph in place.
+        const bool graph = (p->flags & PT_RENDER_NO_GRAPH) == 0;
+        if (graph && !ws.stream) {
+            PT_CUDA_TRY(cudaStreamCreateWithFlags(&ws.stream, cudaStreamNonBlocking));
+            PT_CUDA_TRY(cudaEventCreateWithFlags(&ws.ev_in, cudaEventDisableTiming));
+            PT_CUDA_TRY(cudaEventCreateWithFlags(&ws.ev_out, cudaEventDisableTiming));
+        }
+        cudaStream_t ls = graph ? ws.stream : st;
+        if (graph) {
+            PT_CUDA_TRY(cudaEventRecord(ws.ev_in, st));
+            PT_CUDA_TRY(cudaStreamWaitEvent(ws.stream, ws.ev_in, 0));
+            PT_CUDA_TRY(cudaStreamBeginCapture(ws.stream, cudaStreamCaptureModeThreadLocal));
+        }
         Timer tm;
-        uint32_t launches = 1;
-        PT_CUDA_TRY(cudaEventRecord(s->ev0, st));
+        uint32_t launches = 0;
         uint32_t waves = 0;
-        for (uint32_t f0 = 0; f0 < p->spp; f0 += frames_per_wave) {
+        if (!graph) PT_CUDA_TRY(cudaEventRecord(s->ev0, st));
+        cudaError_t enq = cudaMemsetAsync(ws.counters.ptr, 0, 256, ls);
+        for (uint32_t f0 = 0; f0 < p->spp && enq == cudaSuccess; f0 += frames_per_wave) {
             Wave w;
             w.npix = npix;
             w.frames = std::min(frames_per_wave, p->spp - f0);
@@ -604,26 +682,78 @@ struct Launcher {
             stt.q_in = ws.q0.as<uint32_t>();
             stt.q_out = ws.q1.as<uint32_t>();
             const size_t slots = (size_t)w.frames * npix;
-            k_raygen<<<nblocks(slots, 256), 256, 0, st>>>(d, stt, w);
+            k_raygen<<<nblocks(slots, 256), 256, 0, ls>>>(d, stt, w);
             launches++;
             for (uint32_t b = 0; b < max_depth; b++) {
-                if (timing) tm.mark(0, st);
-                k_ext<<<grid_trace, tb, smem, st>>>(d, stt);
-                if (timing) { tm.mark(0, st); tm.mark(2, st); }
-                k_shade<<<grid_shade, 256, 0, st>>>(d, stt, w, out);
-                if (timing) { tm.mark(2, st); tm.mark(1, st); }
-                k_sh<<<grid_trace, tb, smem, st>>>(d, stt);
-                if (timing) tm.mark(1, st);
-                k_advance<<<1, 1, 0, st>>>(stt.counters);
+                if (timing) tm.mark(0, ls);
+                k_ext<<<grid_trace, tb, smem, ls>>>(d, stt);
+                if (timing) tm.mark(0, ls);
+                State shade_st = stt;
+                if (sort) {
+                    k_bin_count<<<grid_bin, 256, 0, ls>>>(d, stt, ws.mat_key.as<uint8_t>());
+                    k_bin_scan<<<1, 1, 0, ls>>>(stt.counters);
+                    k_bin_scatter<<<grid_bin, 256, 0, ls>>>(stt, ws.mat_key.as<uint8_t>(), ws.sort_tmp.as<uint32_t>());
+                    shade_st.q_in = ws.sort_tmp.as<uint32_t>();
+                    launches += 3;
+                }
+                if (timing) tm.mark(2, ls);
+                k_shade<<<grid_shade, 256, 0, ls>>>(d, shade_st, w, out);
+                if (timing) { tm.mark(2, ls); tm.mark(1, ls); }
+                k_sh<<<grid_trace, tb, smem, ls>>>(d, stt);
+                if (timing) tm.mark(1, ls);
+                k_advance<<<1, 1, 0, ls>>>(stt.counters);
                 launches += 4;
                 std::swap(stt.q_in, stt.q_out);
             }
-            k_accumulate<<<nblocks(npix, 256), 256, 0, st>>>(stt, w, out);
+            k_accumulate<<<nblocks(npix, 256), 256, 0, ls>>>(stt, w, out);
             launches++;
             waves++;
+            enq = cudaGetLastError();
+        }
+        if (graph) {
+            cudaGraph_t g = nullptr;
+            cudaError_t ec = cudaStreamEndCapture(ws.stream, &g);
+            if (enq != cudaSuccess || ec != cudaSuccess) {
+                if (g) cudaGraphDestroy(g);
+                pt_set_error("render capture failed: %s", cudaGetErrorString(enq != cudaSuccess ? enq : ec));
+                return PT_ERR_CUDA;
+            }
+            bool updated = false;
+            if (ws.exec) {
+                cudaGraphExecUpdateResultInfo info;
+                updated = cudaGraphExecUpdate(ws.exec, g, &info) == cudaSuccess;
+                if (!updated) {
+                    (void)cudaGetLastError();
+                    cudaGraphExecDestroy(ws.exec);
+                    ws.exec = nullptr;
+                }
+            }
+            if (!updated) {
+                cudaError_t ei = cudaGraphInstantiate(&ws.exec, g, 0);
+                if (ei != cudaSuccess) {
+                    cudaGraphDestroy(g);
+                    ws.exec = nullptr;
+                    pt_set_error("cudaGraphInstantiate failed: %s", cudaGetErrorString(ei));
+                    return PT_ERR_CUDA;
+                }
+            }
+            cudaGraphDestroy(g);
+            PT_CUDA_TRY(cudaEventRecord(s->ev0, ws.stream));
+            PT_CUDA_TRY(cudaGraphLaunch(ws.exec, ws.stream));
+            PT_CUDA_TRY(cudaEventRecord(s->ev1, ws.stream));
+            PT_CUDA_TRY(cudaEventRecord(ws.ev_out, ws.stream));
+            PT_CUDA_TRY(cudaStreamWaitEvent(st, ws.ev_out, 0));
+        } else {
+            if (enq != cudaSuccess) {
+                pt_set_error("kernel launch failed: %s", cudaGetErrorString(enq));
+                return PT_ERR_CUDA;
+            }
         }
         PT_CUDA_TRY(cudaGetLastError());
-        PT_CUDA_TRY(cudaEventRecord(s->ev1, st));
+        if (!graph) {
+            // direct launches: time the enqueued work with events around it on the caller's stream
+            PT_CUDA_TRY(cudaEventRecord(s->ev1, st));
+        }
         PT_CUDA_TRY(cudaEventSynchronize(s->ev1));
         pt_render_stats &rs = s->render_stats;
         rs = pt_render_stats{};

@@ -462,6 +462,10 @@ pt_scene::~pt_scene() {
                      &ws.rad, &ws.rng, &ws.meta, &ws.q0, &ws.q1, &ws.sh_o, &ws.sh_d, &ws.sh_c, &ws.mat_key,
                      &ws.counters, &ws.sort_tmp};
     for (DevBuf *b : all) b->release();
+    if (ws.exec) cudaGraphExecDestroy(ws.exec);
+    if (ws.ev_in) cudaEventDestroy(ws.ev_in);
+    if (ws.ev_out) cudaEventDestroy(ws.ev_out);
+    if (ws.stream) cudaStreamDestroy(ws.stream);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
 }

@@ -159,18 +159,19 @@ PT_DI void load_node_smem(const float4 *p, WideNode<K> &n) {
     }
 }
 
-// Per-thread traversal stack: kShortStack entries in shared memory (strided by
-// the block size to avoid bank conflicts), the rest in local memory.
+// Per-thread traversal stack of (item, entry distance): kShortStack entries
+// in shared memory (strided by the block size to avoid bank conflicts), the
+// rest in local memory.
 struct ShortStack {
     int2 *smem;  // base + threadIdx.x
     int stride;
     int2 spill[kSpillStack];
     int sp;
-    PT_DI void push(int node, float t, uint32_t &overflow) {
-        int2 e = make_int2(node, __float_as_int(t));
+    PT_DI void push(int item, float t, uint32_t &overflow) {
+        int2 e = make_int2(item, __float_as_int(t));
         if (sp < kShortStack) smem[sp * stride] = e;
         else if (sp < kShortStack + kSpillStack) spill[sp - kShortStack] = e;
-        else {  // cannot happen for trees of depth <= 16 (width 4); counted, entry dropped
+        else {  // cannot happen for trees of depth <= 21 (width 4); reported, entry dropped
             overflow = 1;
             return;
         }
@@ -182,47 +183,151 @@ struct ShortStack {
     }
 };
 
-template <int K, bool ANY, bool COUNT>
-PT_DI TraceResult traverse(const DevScene &s, const float4 *smem_nodes, int2 *smem_stack, float3 o, float3 d,
-                           float tmin, float tmax, uint32_t &n_nodes, uint32_t &n_prims, uint32_t &overflow) {
-    TraceResult best;
-    best.t = tmax;
-    best.prim = -1;
-    best.u = best.v = 0.f;
-    const RayWT w = ray_wt(d);
-    const float3 inv = safe_inv(d);
+// Traversal items: a node index (>= 0), a leaf (bit 31 | first << 4 | count)
+// or kNoItem.  Leaves must start below 2^27 - 1 (checked at scene upload).
+constexpr int kNoItem = -1;
+PT_DI int make_leaf(int first, int count) { return (int)(0x80000000u | ((uint32_t)first << 4) | (uint32_t)count); }
+PT_DI bool is_leaf(int item) { return item < 0 && item != kNoItem; }
+PT_DI int leaf_first(int item) { return (int)(((uint32_t)item >> 4) & 0x7ffffffu); }
+PT_DI int leaf_count(int item) { return item & 15; }
+
+// Lanes refill their ray when at most this many lanes of the warp are busy.
+constexpr int kRefillBusyMax = 20;
+
+// Persistent "while-while" traversal (after Aila & Laine, HPG 2009), adapted
+// to wide nodes with inline leaves.  Each warp keeps 32 rays in flight:
+//   refill   when at most kRefillBusyMax lanes are busy, the idle lanes take
+//            new rays with one atomic per warp;
+//   nodes    lanes step through inner nodes until every busy lane has found a
+//            leaf (it is postponed) or run out of work;
+//   leaves   lanes intersect their postponed leaf (and leaves that follow it
+//            on the stack);
+//   finish   lanes without work store their result and become idle.
+// Children are slab-tested (robust far bound), sorted by entry distance; the
+// nearest is the next item, the others go on the stack with their distance,
+// which is re-checked against the current closest hit when popped.
+//
+// Src provides: count(), load(i, o, d, tmin, tmax, tag), store(i, tag, result).
+template <int K, bool ANY, bool COUNT, class Src>
+PT_DI void trace_persistent(const DevScene &s, const float4 *snodes, int2 *sstack_base, Src &src, uint32_t *work,
+                            uint32_t *ovf_flag, unsigned long long *stat_nodes, unsigned long long *stat_prims,
+                            unsigned long long *stat_rays) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    const uint32_t n = src.count();
     ShortStack st;
-    st.smem = smem_stack;
+    st.smem = sstack_base + threadIdx.x;
     st.stride = blockDim.x;
     st.sp = 0;
-    int cur = 0;
+    bool active = false, exhausted = false;
+    uint32_t idx = 0, tag = 0;
+    float3 o = f3s(0.f), d = f3s(0.f), inv = f3s(0.f);
+    RayWT w{0, 1, 2, 0.f, 0.f, 1.f};
+    float tmin = 0.f, tmax = 0.f;
+    TraceResult best{0.f, -1, 0.f, 0.f};
+    int item = kNoItem, leaf = kNoItem;
+    uint32_t nodes = 0, prims = 0, rays = 0, ovf = 0;
+
+    auto pop_valid = [&]() -> int {
+        while (st.sp > 0) {
+            int2 e = st.pop();
+            if (__int_as_float(e.y) <= best.t * kSlabScale) return e.x;
+        }
+        return kNoItem;
+    };
+
     for (;;) {
-        WideNode<K> n;
-        if (cur < static_cast<int>(s.smem_nodes)) load_node_smem<K>(smem_nodes + (size_t)cur * 2 * K, n);
-        else load_node<K>(s.nodes + (size_t)cur * 2 * K, n);
-        if (COUNT) n_nodes++;
-        int ic[K];
-        float it[K];
+        unsigned busy = __ballot_sync(FULL, active);
+        if (!exhausted && __popc(busy) <= kRefillBusyMax) {
+            unsigned idle = ~busy;
+            uint32_t cnt = __popc(idle);
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(work, cnt);
+            base = __shfl_sync(FULL, base, 0);
+            if (!active) {
+                uint32_t r = base + __popc(idle & lt);
+                if (r < n) {
+                    idx = r;
+                    src.load(r, o, d, tmin, tmax, tag);
+                    w = ray_wt(d);
+                    inv = safe_inv(d);
+                    best.t = tmax;
+                    best.prim = -1;
+                    best.u = best.v = 0.f;
+                    item = 0;
+                    leaf = kNoItem;
+                    st.sp = 0;
+                    active = true;
+                    if (COUNT) rays++;
+                }
+            }
+            if (base + cnt >= n) exhausted = true;
+            busy = __ballot_sync(FULL, active);
+        }
+        if (busy == 0) break;
+
+        // inner nodes until every busy lane holds a leaf or has no work left
+        for (;;) {
+            bool ready = !active || leaf != kNoItem || item == kNoItem;
+            if (__all_sync(FULL, ready)) break;
+            if (ready) continue;
+            WideNode<K> nd;
+            if (item < static_cast<int>(s.smem_nodes)) load_node_smem<K>(snodes + (size_t)item * 2 * K, nd);
+            else load_node<K>(s.nodes + (size_t)item * 2 * K, nd);
+            if (COUNT) nodes++;
+            int ci[K];
+            float ct[K];
 #pragma unroll
-        for (int c = 0; c < K; c++) {
-            ic[c] = -1;
-            it[c] = __int_as_float(0x7f800000);
-            int ch = n.child(c);
-            if (ch < 0) continue;
-            float tx0 = (n.lox(c) - o.x) * inv.x, tx1 = (n.hix(c) - o.x) * inv.x;
-            float ty0 = (n.loy(c) - o.y) * inv.y, ty1 = (n.hiy(c) - o.y) * inv.y;
-            float tz0 = (n.loz(c) - o.z) * inv.z, tz1 = (n.hiz(c) - o.z) * inv.z;
-            float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
-            float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
-            tf = fminf(tf * kSlabScale, best.t * kSlabScale);
-            if (!(tn <= tf)) continue;
-            int cnt = n.count(c);
-            if (cnt > 0) {
+            for (int c = 0; c < K; c++) {
+                ci[c] = kNoItem;
+                ct[c] = __int_as_float(0x7f800000);
+                int ch = nd.child(c);
+                if (ch < 0) continue;
+                float tx0 = (nd.lox(c) - o.x) * inv.x, tx1 = (nd.hix(c) - o.x) * inv.x;
+                float ty0 = (nd.loy(c) - o.y) * inv.y, ty1 = (nd.hiy(c) - o.y) * inv.y;
+                float tz0 = (nd.loz(c) - o.z) * inv.z, tz1 = (nd.hiz(c) - o.z) * inv.z;
+                float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
+                float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
+                tf = fminf(tf * kSlabScale, best.t * kSlabScale);
+                if (!(tn <= tf)) continue;
+                int cnt = nd.count(c);
+                ci[c] = cnt > 0 ? make_leaf(ch, cnt) : ch;
+                ct[c] = tn;
+            }
+#pragma unroll
+            for (int i = 1; i < K; i++) {
+#pragma unroll
+                for (int j = i; j > 0; j--) {
+                    if (ct[j] < ct[j - 1]) {
+                        float tt = ct[j];
+                        ct[j] = ct[j - 1];
+                        ct[j - 1] = tt;
+                        int ti = ci[j];
+                        ci[j] = ci[j - 1];
+                        ci[j - 1] = ti;
+                    }
+                }
+            }
+#pragma unroll
+            for (int i = K - 1; i >= 1; i--)
+                if (ci[i] != kNoItem) st.push(ci[i], ct[i], ovf);
+            item = ci[0] != kNoItem ? ci[0] : pop_valid();
+            if (is_leaf(item)) {  // postpone it
+                leaf = item;
+                item = pop_valid();
+            }
+        }
+
+        // leaves
+        if (active) {
+            while (leaf != kNoItem) {
+                const int first = leaf_first(leaf), cnt = leaf_count(leaf);
                 for (int j = 0; j < cnt; j++) {
-                    const float4 *pr = s.prims + (size_t)(ch + j) * 3;
+                    const float4 *pr = s.prims + (size_t)(first + j) * 3;
                     float4 a = __ldg(pr);
                     float4 b = __ldg(pr + 1);
-                    if (COUNT) n_prims++;
+                    if (COUNT) prims++;
                     int pid = __float_as_int(a.w);
                     float t, u = 0.f, v = 0.f;
                     float tlim = best.prim < 0 ? tmax : __int_as_float(__float_as_int(best.t) + 1);
@@ -238,7 +343,7 @@ PT_DI TraceResult traverse(const DevScene &s, const float4 *smem_nodes, int2 *sm
                     if (ANY) {
                         best.t = t;
                         best.prim = pid;
-                        return best;
+                        break;
                     }
                     if (t < best.t || pid < best.prim) {
                         best.t = t;
@@ -247,46 +352,36 @@ PT_DI TraceResult traverse(const DevScene &s, const float4 *smem_nodes, int2 *sm
                         best.v = v;
                     }
                 }
-            } else {
-                ic[c] = ch;
-                it[c] = tn;
-            }
-        }
-        // order the inner children by entry distance (sorting network on K slots)
-#pragma unroll
-        for (int i = 1; i < K; i++) {
-#pragma unroll
-            for (int j = i; j > 0; j--) {
-                if (it[j] < it[j - 1]) {
-                    float tt = it[j];
-                    it[j] = it[j - 1];
-                    it[j - 1] = tt;
-                    int ti = ic[j];
-                    ic[j] = ic[j - 1];
-                    ic[j - 1] = ti;
+                leaf = kNoItem;
+                if (ANY && best.prim >= 0) {  // any hit ends the ray
+                    item = kNoItem;
+                    st.sp = 0;
+                    break;
+                }
+                if (is_leaf(item)) {
+                    leaf = item;
+                    item = pop_valid();
                 }
             }
-        }
-        // push the farther ones, descend into the nearest
-#pragma unroll
-        for (int i = K - 1; i >= 1; i--)
-            if (ic[i] >= 0 && it[i] <= best.t * kSlabScale) st.push(ic[i], it[i], overflow);
-        if (ic[0] >= 0 && it[0] <= best.t * kSlabScale) {
-            cur = ic[0];
-            continue;
-        }
-        bool found = false;
-        while (st.sp > 0) {
-            int2 e = st.pop();
-            if (__int_as_float(e.y) <= best.t * kSlabScale) {
-                cur = e.x;
-                found = true;
-                break;
+            if (item == kNoItem && leaf == kNoItem) {
+                src.store(idx, tag, best);
+                active = false;
             }
         }
-        if (!found) break;
     }
-    return best;
+    if (ovf) atomicOr(ovf_flag, 1u);
+    if (COUNT) {
+        for (int off = 16; off > 0; off >>= 1) {
+            nodes += __shfl_xor_sync(FULL, nodes, off);
+            prims += __shfl_xor_sync(FULL, prims, off);
+            rays += __shfl_xor_sync(FULL, rays, off);
+        }
+        if (lane == 0) {
+            atomicAdd(stat_nodes, (unsigned long long)nodes);
+            atomicAdd(stat_prims, (unsigned long long)prims);
+            atomicAdd(stat_rays, (unsigned long long)rays);
+        }
+    }
 }
 
 }  // namespace ptd

@@ -113,3 +113,18 @@ def test_icosphere_field_reduced(cuda_ctx):
     assert st.extension_rays >= st.samples
     assert st.nodes_visited > st.extension_rays
     assert st.overflow == 0
+
+
+def test_material_sort_and_graph_do_not_change_the_image(cuda_ctx):
+    """Binning hits by material and CUDA-graph replay only reorder work."""
+    sc = scenes.material_spheres(48, 32)
+    g = GpuScene(cuda_ctx, sc)
+    ref = gpu_render(g, 5, seed=2, flags=abi.RENDER_NO_GRAPH)["accum"]
+    for flags in (0, abi.RENDER_MATERIAL_SORT, abi.RENDER_MATERIAL_SORT | abi.RENDER_NO_GRAPH,
+                  abi.RENDER_KERNEL_TIMING | abi.RENDER_COUNTERS):
+        got = gpu_render(g, 5, seed=2, flags=flags)["accum"]
+        assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), flags
+    # the instantiated graph is updated in place by later calls with other parameters
+    a = gpu_render(g, 3, seed=7)["accum"]
+    b = gpu_render(g, 3, seed=7, flags=abi.RENDER_NO_GRAPH)["accum"]
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
