@@ -59,8 +59,9 @@ def parse():
     ap.add_argument("--smem-nodes", type=int, default=0)
     ap.add_argument("--block-size", type=int, default=0)
     ap.add_argument("--wave-spp", type=int, default=0)
-    ap.add_argument("--material-sort", action="store_true", help="bin hits by material before shading")
+    ap.add_argument("--no-material-sort", action="store_true", help="shade hits in queue order")
     ap.add_argument("--no-graph", action="store_true", help="launch kernels directly instead of a CUDA graph")
+    ap.add_argument("--autotune", action="store_true", help="run pt_autotune (2 spp renders) before measuring")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -230,10 +231,16 @@ def main():
     sc = scenes.icosphere_field(args.width, args.height, args.depth, args.instances)
     ctx = Context(local)
     g = GpuScene(ctx, sc, bvh_width=args.bvh_width, max_leaf=args.max_leaf, smem_nodes=args.smem_nodes)
-    bst = g.bvh_stats()
     buffers = g.alloc_buffers()
+    tune = None
+    if args.autotune:
+        t = g.autotune(spp=2, buffers=buffers)
+        tune = {"bvh_width": t.bvh_width, "block_size": t.block_size, "wave_paths": t.wave_paths, "trials": t.trials,
+                "tuning_msamples_per_s": t.msamples_per_s, "default_msamples_per_s": t.baseline_msamples_per_s}
+        args.bvh_width = t.bvh_width
+    bst = g.bvh_stats()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    base_flags = (abi.RENDER_MATERIAL_SORT if args.material_sort else 0) | (abi.RENDER_NO_GRAPH if args.no_graph else 0)
+    base_flags = (abi.RENDER_NO_MATERIAL_SORT if args.no_material_sort else 0) | (abi.RENDER_NO_GRAPH if args.no_graph else 0)
     kw = dict(rng=abi.RNG_PCG32, block_size=args.block_size, wave_spp=args.wave_spp, buffers=buffers)
 
     for w in range(args.warmup):
@@ -246,25 +253,32 @@ def main():
 
     clocks = ClockSampler(local)
     stream = torch.cuda.current_stream()
-    step_ms, ext_ms, ext_launches, sh_ms, shade_ms, launches = [], 0.0, 0, 0.0, 0.0, 0
+    step_ms, launches = [], 0
     barrier()
     clocks.start()
     for step in range(args.steps):
         flush.fill_(float(step))
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        g.render(args.spp, seed=step * args.spp, flags=abi.RENDER_KERNEL_TIMING | base_flags, **kw)
+        g.render(args.spp, seed=step * args.spp, flags=base_flags, **kw)
         e1.record(stream)
         e1.synchronize()
         step_ms.append(e0.elapsed_time(e1))
+        launches += g.render_stats().kernel_launches
+    barrier()
+    clk = clocks.stop()
+    # the same steps again with every traversal / shading launch timed by CUDA
+    # events on the launching stream (direct launches): durations for the roofline
+    ext_ms, ext_launches, sh_ms, shade_ms, timed_ms = 0.0, 0, 0.0, 0.0, []
+    for step in range(args.steps):
+        flush.fill_(float(step))
+        g.render(args.spp, seed=step * args.spp, flags=abi.RENDER_KERNEL_TIMING | base_flags, **kw)
         rs = g.render_stats()
         ext_ms += rs.extend_ms
         ext_launches += rs.extend_launches
         sh_ms += rs.shadow_ms
         shade_ms += rs.shade_ms
-        launches += rs.kernel_launches
-    barrier()
-    clk = clocks.stop()
+        timed_ms.append(rs.render_ms)
     t_max = sum(step_ms)
     if ws > 1:
         import torch.distributed as dist
@@ -316,7 +330,7 @@ def main():
         "config": {"workload": WORKLOAD, "width": args.width, "height": args.height, "spp": args.spp,
                    "max_depth": args.depth, "rng": "pcg32", "bvh_width": args.bvh_width, "max_leaf": args.max_leaf,
                    "smem_nodes": args.smem_nodes, "triangles": int(bst.num_prims),
-                   "material_sort": bool(args.material_sort), "cuda_graph": not args.no_graph,
+                   "material_sort": not args.no_material_sort, "autotune": tune, "cuda_graph": not args.no_graph,
                    "l2": "flushed between steps (256 MiB write, outside the timed events)",
                    "parallelism": "replicas only" if ws > 1 else "single GPU"},
         "e2e": e2e,
@@ -332,7 +346,8 @@ def main():
                      "nodes_per_ray": cst.nodes_visited / max(1, cst.extension_rays),
                      "prims_per_ray": cst.prims_tested / max(1, cst.extension_rays),
                      "extend_ms_per_step": ext_ms / args.steps, "shadow_ms_per_step": sh_ms / args.steps,
-                     "shade_ms_per_step": shade_ms / args.steps},
+                     "shade_ms_per_step": shade_ms / args.steps,
+                     "timed_launches_ms_per_step": sum(timed_ms) / args.steps},
         "rays_per_step": {"extension": cst.extension_rays, "shadow": cst.shadow_rays},
         "bvh": {"nodes": int(bst.num_nodes), "sah_cost": float(bst.sah_cost), "build_ms": float(bst.build_ms),
                 "depth": int(bst.max_depth)},

@@ -223,10 +223,11 @@ typedef struct pt_render_params {
 } pt_render_params;
 
 enum {
-    PT_RENDER_MATERIAL_SORT = 1, /* bin hit paths by material before shading */
+    PT_RENDER_NO_MATERIAL_SORT = 1, /* shade hits in queue order instead of binned by material */
     PT_RENDER_COUNTERS = 2,      /* count node visits and primitive tests */
     PT_RENDER_NO_GRAPH = 4,      /* launch the bounce kernels one by one instead of a CUDA graph */
-    PT_RENDER_KERNEL_TIMING = 8  /* time each traversal / shading launch with CUDA events */
+    PT_RENDER_KERNEL_TIMING = 8  /* time each traversal / shading launch with CUDA events
+                                    (launches directly, without the CUDA graph) */
 };
 
 /* Caller-owned DEVICE buffers (BufferManager buffers, framework/system/buffer.h:26-63):
@@ -310,6 +311,26 @@ int pt_render_get_stats(const pt_scene *scene, pt_render_stats *out);
  * capture.  All calls share the array: calls that overlap on the GPU (on
  * different streams or threads) race.  No statistics are recorded. */
 int pt_render_noalloc(pt_scene *scene, const pt_render_params *params, const pt_frame_buffers *fb, void *stream);
+
+/* Autotuner result: the configuration pt_autotune found fastest. */
+typedef struct pt_tune_result {
+    uint32_t bvh_width;       /* 2, 4 or 8 */
+    uint32_t block_size;      /* threads per block of the traversal kernels */
+    uint32_t wave_paths;      /* paths in flight per wave (the queue chunk) */
+    uint32_t trials;          /* configurations timed */
+    float msamples_per_s;     /* throughput of the winner on the tuning render */
+    float baseline_msamples_per_s; /* throughput of the configuration the scene had before */
+} pt_tune_result;
+
+/* No reference counterpart (the reference has a single OptiX configuration).
+ * Times `params` renders on this scene for every combination of BVH width
+ * {2, 4, 8} (the BVH is rebuilt), traversal block size {64, 128, 256} and wave
+ * size {1M, 4M, 16M paths, capped at spp frames}, then rebuilds the BVH with
+ * the winning width and makes its block size and wave size the scene's
+ * defaults (used when pt_render_params.block_size / wave_spp are 0).  fb is
+ * used as the output of the tuning renders.  Keep params.spp small (1-4). */
+int pt_autotune(pt_scene *scene, const pt_render_params *params, const pt_frame_buffers *fb,
+                pt_tune_result *out, void *stream);
 
 /* ---- query entry points used by the parity tests ---------------------- */
 /* rays: n * 8 floats (ox,oy,oz,tmin, dx,dy,dz,tmax), hits: n * 4 floats

@@ -25,7 +25,7 @@ SHAPE_MESH, SHAPE_SPHERE = 0, 1
 INST_FLIP_NORMALS, INST_FLIP_TEXCOORDS = 1, 2
 ENV_NONE, ENV_CONST = 0, 1
 RNG_REF_LCG, RNG_PCG32 = 0, 1
-RENDER_MATERIAL_SORT, RENDER_COUNTERS, RENDER_NO_GRAPH, RENDER_KERNEL_TIMING = 1, 2, 4, 8
+RENDER_NO_MATERIAL_SORT, RENDER_COUNTERS, RENDER_NO_GRAPH, RENDER_KERNEL_TIMING = 1, 2, 4, 8
 LOBE_DELTA = (1 << 5) | (1 << 6)
 
 
@@ -106,6 +106,11 @@ class RenderStats(C.Structure):
                 ("waves", C.c_uint32), ("overflow", C.c_uint32)]
 
 
+class TuneResult(C.Structure):
+    _fields_ = [("bvh_width", C.c_uint32), ("block_size", C.c_uint32), ("wave_paths", C.c_uint32),
+                ("trials", C.c_uint32), ("msamples_per_s", C.c_float), ("baseline_msamples_per_s", C.c_float)]
+
+
 # (name, restype, argtypes) of every entry point declared in include/pt_api.h.
 PROTOTYPES = [
     ("pt_api_version", C.c_int, []),
@@ -123,6 +128,8 @@ PROTOTYPES = [
     ("pt_render", C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.POINTER(FrameBuffers), C.c_void_p]),
     ("pt_render_get_stats", C.c_int, [C.c_void_p, C.POINTER(RenderStats)]),
     ("pt_render_noalloc", C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.POINTER(FrameBuffers), C.c_void_p]),
+    ("pt_autotune", C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.POINTER(FrameBuffers), C.POINTER(TuneResult),
+                              C.c_void_p]),
     ("pt_trace_rays", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_int, C.c_void_p]),
     ("pt_bsdf_eval_batch", C.c_int, [C.c_void_p] * 5 + [C.c_uint32, C.c_void_p]),
     ("pt_bsdf_sample_batch", C.c_int, [C.c_void_p] * 7 + [C.c_uint32, C.c_void_p]),

@@ -90,6 +90,8 @@ struct pt_scene {
     ptd::DevScene dev{};
     RenderWorkspace ws;
     pt_render_stats render_stats{};
+    uint32_t tuned_block = 0;       // autotuned defaults (0 = built-in defaults)
+    uint32_t tuned_wave_paths = 0;
 
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     ~pt_scene();
@@ -101,6 +103,8 @@ int pt_bvh_refit_impl(pt_scene *s, cudaStream_t stream);
 // pt_render.cu
 int pt_render_impl(pt_scene *s, const pt_render_params *p, const pt_frame_buffers *fb, cudaStream_t stream);
 int pt_trace_rays_impl(pt_scene *s, const float *rays, float *hits, uint32_t n, int anyhit, cudaStream_t stream);
+int pt_autotune_impl(pt_scene *s, const pt_render_params *p, const pt_frame_buffers *fb, pt_tune_result *out,
+                     cudaStream_t stream);
 int pt_bsdf_eval_impl(const float *bsdf, const float *wo, const float *wi, float *f, float *pdf, uint32_t n,
                       cudaStream_t stream);
 int pt_bsdf_sample_impl(const float *bsdf, const float *wo, uint32_t *rng, float *wi, float *f, float *pdf,

@@ -432,7 +432,7 @@ __global__ void __launch_bounds__(256) k_shade(DevScene s, State st, Wave w, Out
 }
 
 
-// Material-sorted shading (PT_RENDER_MATERIAL_SORT): the active queue is
+// Material-sorted shading (default; PT_RENDER_NO_MATERIAL_SORT turns it off): the active queue is
 // binned by the material type of each hit (0 = miss) before k_shade, so that
 // warps run one BSDF at a time.  Counting pass (block histogram in shared
 // memory, one atomic per bin and block), a one-thread scan, and a scatter pass
@@ -594,7 +594,8 @@ struct Launcher {
         const bool count = (p->flags & PT_RENDER_COUNTERS) != 0;
         const bool timing = (p->flags & PT_RENDER_KERNEL_TIMING) != 0;
         uint32_t frames_per_wave = p->wave_spp;
-        if (frames_per_wave == 0) frames_per_wave = std::max<uint32_t>(1, (uint32_t)(16u * 1024u * 1024u / std::max<uint32_t>(npix, 1)));
+        const uint32_t wave_paths = s->tuned_wave_paths ? s->tuned_wave_paths : 16u * 1024u * 1024u;
+        if (frames_per_wave == 0) frames_per_wave = std::max<uint32_t>(1, (uint32_t)(wave_paths / std::max<uint32_t>(npix, 1)));
         frames_per_wave = std::max<uint32_t>(1, std::min(frames_per_wave, std::max<uint32_t>(p->spp, 1)));
         const size_t cap = (size_t)frames_per_wave * npix;
         if (ws.capacity < cap) {
@@ -628,7 +629,7 @@ struct Launcher {
         out.normal = fb->normal;
         out.test = fb->test;
 
-        const int tb = p->block_size ? (int)p->block_size : 128;
+        const int tb = p->block_size ? (int)p->block_size : (s->tuned_block ? (int)s->tuned_block : 128);
         const size_t smem = (size_t)d.smem_nodes * 32 * K + (size_t)kShortStack * 8 * tb;
         auto k_ext = count ? k_trace_queue<K, false, true> : k_trace_queue<K, false, false>;
         auto k_sh = count ? k_trace_queue<K, true, true> : k_trace_queue<K, true, false>;
@@ -639,7 +640,7 @@ struct Launcher {
         const uint32_t grid_trace = (uint32_t)std::max(1, occ_t) * s->num_sms;
         const uint32_t grid_shade = (uint32_t)std::max(1, occ_s) * s->num_sms;
 
-        const bool sort = (p->flags & PT_RENDER_MATERIAL_SORT) != 0;
+        const bool sort = (p->flags & PT_RENDER_NO_MATERIAL_SORT) == 0;
         if (sort && ws.sort_capacity < cap) {
             if ((e = ws.mat_key.ensure(cap)) != PT_OK || (e = ws.sort_tmp.ensure(4 * cap)) != PT_OK) return e;
             ws.sort_capacity = cap;
@@ -651,7 +652,7 @@ struct Launcher {
         // The whole render is captured into a CUDA graph on the scene's own
         // stream (ordered after and before the caller's stream by events) and
         // replayed; later calls update the instantiated graph in place.
-        const bool graph = (p->flags & PT_RENDER_NO_GRAPH) == 0;
+        const bool graph = (p->flags & (PT_RENDER_NO_GRAPH | PT_RENDER_KERNEL_TIMING)) == 0;
         if (graph && !ws.stream) {
             PT_CUDA_TRY(cudaStreamCreateWithFlags(&ws.stream, cudaStreamNonBlocking));
             PT_CUDA_TRY(cudaEventCreateWithFlags(&ws.ev_in, cudaEventDisableTiming));
@@ -820,6 +821,71 @@ int pt_render_impl(pt_scene *s, const pt_render_params *p, const pt_frame_buffer
         case 4: return Launcher<4>::run(s, p, fb, st);
         default: return Launcher<8>::run(s, p, fb, st);
     }
+}
+
+// Autotuner: every (BVH width, block size, wave size) combination renders
+// params->spp frames; the fastest by device time is applied to the scene.
+int pt_autotune_impl(pt_scene *s, const pt_render_params *params, const pt_frame_buffers *fb, pt_tune_result *out,
+                     cudaStream_t st) {
+    const uint32_t npix = s->dev.width_px * s->dev.height_px;
+    const uint32_t spp = std::max<uint32_t>(1, params->spp);
+    pt_tune_result r{};
+    pt_bvh_opts opts = s->bvh_opts;
+    const uint32_t old_width = opts.width, old_block = s->tuned_block, old_wave = s->tuned_wave_paths;
+    pt_render_params p = *params;
+    p.spp = spp;
+    p.block_size = 0;
+    p.wave_spp = 0;
+    p.flags &= ~(uint32_t)(PT_RENDER_KERNEL_TIMING | PT_RENDER_COUNTERS);
+    auto time_render = [&](float &ms) -> int {
+        int e = pt_render_impl(s, &p, fb, st);  // first run: warm-up (graph instantiation, caches)
+        if (e != PT_OK) return e;
+        e = pt_render_impl(s, &p, fb, st);
+        ms = s->render_stats.render_ms;
+        return e;
+    };
+    float base_ms = 0.f;
+    int e = time_render(base_ms);
+    if (e != PT_OK) return e;
+    r.baseline_msamples_per_s = base_ms > 0.f ? (float)((double)npix * spp / (base_ms * 1e-3) / 1e6) : 0.f;
+    float best_ms = 1e30f;
+    uint32_t best_w = old_width, best_b = 128, best_wave = 16u << 20;
+    const uint32_t widths[3] = {2, 4, 8}, blocks[3] = {64, 128, 256}, waves[3] = {1u << 20, 4u << 20, 16u << 20};
+    for (uint32_t wd : widths) {
+        opts.width = wd;
+        if ((e = pt_bvh_build_impl(s, &opts, st)) != PT_OK) return e;
+        uint32_t prev_frames = 0;
+        for (uint32_t wv : waves) {
+            uint32_t frames = std::max<uint32_t>(1, std::min(spp, wv / std::max<uint32_t>(npix, 1)));
+            if (frames == prev_frames) continue;  // same effective wave size as the previous candidate
+            prev_frames = frames;
+            for (uint32_t bs : blocks) {
+                s->tuned_block = bs;
+                s->tuned_wave_paths = wv;
+                float ms = 0.f;
+                if ((e = time_render(ms)) != PT_OK) return e;
+                r.trials++;
+                if (ms < best_ms) {
+                    best_ms = ms;
+                    best_w = wd;
+                    best_b = bs;
+                    best_wave = wv;
+                }
+            }
+        }
+    }
+    opts.width = best_w;
+    if ((e = pt_bvh_build_impl(s, &opts, st)) != PT_OK) return e;
+    s->tuned_block = best_b;
+    s->tuned_wave_paths = best_wave;
+    (void)old_block;
+    (void)old_wave;
+    r.bvh_width = best_w;
+    r.block_size = best_b;
+    r.wave_paths = best_wave;
+    r.msamples_per_s = (float)((double)npix * spp / (best_ms * 1e-3) / 1e6);
+    if (out) *out = r;
+    return PT_OK;
 }
 
 int pt_trace_rays_impl(pt_scene *s, const float *rays, float *hits, uint32_t n, int anyhit, cudaStream_t st) {

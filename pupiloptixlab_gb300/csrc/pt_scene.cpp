@@ -598,6 +598,16 @@ int pt_render(pt_scene *scene, const pt_render_params *params, const pt_frame_bu
     return pt_render_impl(scene, params, fb, static_cast<cudaStream_t>(stream));
 }
 
+int pt_autotune(pt_scene *scene, const pt_render_params *params, const pt_frame_buffers *fb, pt_tune_result *out,
+                void *stream) {
+    clear_stale_cuda_error();
+    if (!scene || !params || !fb || !fb->accum) { pt_set_error("scene, params, buffers or accum is NULL"); return PT_ERR_INVALID; }
+    if (!scene->bvh_built) { pt_set_error("pt_autotune before pt_bvh_build"); return PT_ERR_STATE; }
+    if (params->rng != PT_RNG_REF_LCG && params->rng != PT_RNG_PCG32) { pt_set_error("unknown rng mode"); return PT_ERR_INVALID; }
+    PT_CUDA_TRY(cudaSetDevice(scene->device));
+    return pt_autotune_impl(scene, params, fb, out, static_cast<cudaStream_t>(stream));
+}
+
 int pt_render_get_stats(const pt_scene *scene, pt_render_stats *out) {
     if (!scene || !out) { pt_set_error("scene or out is NULL"); return PT_ERR_INVALID; }
     *out = scene->render_stats;

@@ -39,12 +39,13 @@ def test_library_exports_every_declared_symbol(ptlib):
 
 STRUCTS = ["pt_texture_desc", "pt_material_desc", "pt_mesh_desc", "pt_sphere_desc", "pt_instance_desc",
            "pt_camera_desc", "pt_env_desc", "pt_scene_desc", "pt_device_opts", "pt_bvh_opts", "pt_bvh_stats",
-           "pt_render_params", "pt_frame_buffers", "pt_render_stats"]
+           "pt_render_params", "pt_frame_buffers", "pt_render_stats", "pt_tune_result"]
 MIRROR = {"pt_texture_desc": abi.TextureDesc, "pt_material_desc": abi.MaterialDesc, "pt_mesh_desc": abi.MeshDesc,
           "pt_sphere_desc": abi.SphereDesc, "pt_instance_desc": abi.InstanceDesc, "pt_camera_desc": abi.CameraDesc,
           "pt_env_desc": abi.EnvDesc, "pt_scene_desc": abi.SceneDesc, "pt_device_opts": abi.DeviceOpts,
           "pt_bvh_opts": abi.BvhOpts, "pt_bvh_stats": abi.BvhStats, "pt_render_params": abi.RenderParams,
-          "pt_frame_buffers": abi.FrameBuffers, "pt_render_stats": abi.RenderStats}
+          "pt_frame_buffers": abi.FrameBuffers, "pt_render_stats": abi.RenderStats,
+          "pt_tune_result": abi.TuneResult}
 
 
 def test_ctypes_layouts_match_header(tmp_path):

@@ -120,7 +120,7 @@ def test_material_sort_and_graph_do_not_change_the_image(cuda_ctx):
     sc = scenes.material_spheres(48, 32)
     g = GpuScene(cuda_ctx, sc)
     ref = gpu_render(g, 5, seed=2, flags=abi.RENDER_NO_GRAPH)["accum"]
-    for flags in (0, abi.RENDER_MATERIAL_SORT, abi.RENDER_MATERIAL_SORT | abi.RENDER_NO_GRAPH,
+    for flags in (0, abi.RENDER_NO_MATERIAL_SORT, abi.RENDER_NO_MATERIAL_SORT | abi.RENDER_NO_GRAPH,
                   abi.RENDER_KERNEL_TIMING | abi.RENDER_COUNTERS):
         got = gpu_render(g, 5, seed=2, flags=flags)["accum"]
         assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), flags
@@ -128,3 +128,16 @@ def test_material_sort_and_graph_do_not_change_the_image(cuda_ctx):
     a = gpu_render(g, 3, seed=7)["accum"]
     b = gpu_render(g, 3, seed=7, flags=abi.RENDER_NO_GRAPH)["accum"]
     assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+def test_autotune_picks_a_configuration_and_keeps_the_image(cuda_ctx):
+    sc = scenes.material_spheres(64, 40)
+    g = GpuScene(cuda_ctx, sc)
+    before = gpu_render(g, 4, seed=1)["accum"]
+    r = g.autotune(spp=2)
+    assert r.bvh_width in (2, 4, 8) and r.block_size in (64, 128, 256)
+    assert r.wave_paths in (1 << 20, 4 << 20, 16 << 20)
+    assert r.trials >= 9 and r.msamples_per_s > 0
+    assert g.bvh_stats().width == r.bvh_width
+    after = gpu_render(g, 4, seed=1)["accum"]
+    assert np.array_equal(after.view(np.uint32), before.view(np.uint32))
