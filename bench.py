@@ -61,7 +61,7 @@ def parse():
     ap.add_argument("--wave-spp", type=int, default=0)
     ap.add_argument("--no-material-sort", action="store_true", help="shade hits in queue order")
     ap.add_argument("--no-graph", action="store_true", help="launch kernels directly instead of a CUDA graph")
-    ap.add_argument("--autotune", action="store_true", help="run pt_autotune (2 spp renders) before measuring")
+    ap.add_argument("--autotune", action="store_true", help="run pt_autotune at the benchmark's spp before measuring")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -234,7 +234,7 @@ def main():
     buffers = g.alloc_buffers()
     tune = None
     if args.autotune:
-        t = g.autotune(spp=2, buffers=buffers)
+        t = g.autotune(spp=args.spp, buffers=buffers)
         tune = {"bvh_width": t.bvh_width, "block_size": t.block_size, "wave_paths": t.wave_paths, "trials": t.trials,
                 "tuning_msamples_per_s": t.msamples_per_s, "default_msamples_per_s": t.baseline_msamples_per_s}
         args.bvh_width = t.bvh_width
@@ -348,7 +348,9 @@ def main():
                      "extend_ms_per_step": ext_ms / args.steps, "shadow_ms_per_step": sh_ms / args.steps,
                      "shade_ms_per_step": shade_ms / args.steps,
                      "timed_launches_ms_per_step": sum(timed_ms) / args.steps},
-        "rays_per_step": {"extension": cst.extension_rays, "shadow": cst.shadow_rays},
+        "rays_per_step": {"extension": cst.extension_rays, "shadow": cst.shadow_rays,
+                          "shadow_nodes_per_ray": cst.shadow_nodes_visited / max(1, cst.shadow_rays),
+                          "shadow_prims_per_ray": cst.shadow_prims_tested / max(1, cst.shadow_rays)},
         "bvh": {"nodes": int(bst.num_nodes), "sah_cost": float(bst.sah_cost), "build_ms": float(bst.build_ms),
                 "depth": int(bst.max_depth)},
         "cpu_baseline": cpu,

@@ -316,19 +316,21 @@ int pt_render_noalloc(pt_scene *scene, const pt_render_params *params, const pt_
 typedef struct pt_tune_result {
     uint32_t bvh_width;       /* 2, 4 or 8 */
     uint32_t block_size;      /* threads per block of the traversal kernels */
-    uint32_t wave_paths;      /* paths in flight per wave (the queue chunk) */
+    uint32_t wave_paths;      /* paths in flight per wave (the queue chunk, in path slots) */
     uint32_t trials;          /* configurations timed */
     float msamples_per_s;     /* throughput of the winner on the tuning render */
     float baseline_msamples_per_s; /* throughput of the configuration the scene had before */
 } pt_tune_result;
 
 /* No reference counterpart (the reference has a single OptiX configuration).
- * Times `params` renders on this scene for every combination of BVH width
- * {2, 4, 8} (the BVH is rebuilt), traversal block size {64, 128, 256} and wave
- * size {1M, 4M, 16M paths, capped at spp frames}, then rebuilds the BVH with
- * the winning width and makes its block size and wave size the scene's
- * defaults (used when pt_render_params.block_size / wave_spp are 0).  fb is
- * used as the output of the tuning renders.  Keep params.spp small (1-4). */
+ * Times `params` renders on this scene (coordinate search): every
+ * combination of BVH width {2, 4, 8} (the BVH is rebuilt) and traversal block
+ * size {64, 128, 256} at the default wave size, then wave sizes {4Mi, 16Mi,
+ * 64Mi paths} with the best pair.  The BVH is rebuilt with the winning width
+ * and its block size and wave size become the scene's defaults (used when
+ * pt_render_params.block_size / wave_spp are 0).  fb receives the tuning
+ * renders.  Use the spp of the renders to be tuned for: the best wave size
+ * depends on it. */
 int pt_autotune(pt_scene *scene, const pt_render_params *params, const pt_frame_buffers *fb,
                 pt_tune_result *out, void *stream);
 

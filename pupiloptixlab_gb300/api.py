@@ -115,7 +115,7 @@ class GpuScene:
         abi.check(self.lib.pt_render(self.handle, C.byref(p), C.byref(fb), _stream_ptr(stream)), "pt_render", self.lib)
         return b
 
-    def autotune(self, spp: int = 2, rng: int = abi.RNG_PCG32, buffers: dict | None = None, stream=None) -> abi.TuneResult:
+    def autotune(self, spp: int = 4, rng: int = abi.RNG_PCG32, buffers: dict | None = None, stream=None) -> abi.TuneResult:
         b = buffers if buffers is not None else self.alloc_buffers()
         p = abi.RenderParams(spp, 0, 0, 0, 1, rng, 0, 0, 0)
         fb = abi.FrameBuffers(*[b[k].data_ptr() if k in b else None for k in ("accum", "frame", "albedo", "normal", "test")])

@@ -30,6 +30,9 @@
 namespace {
 using namespace ptd;
 
+// Paths in flight per wave unless autotuned: 32 Mi slots (about 4.6 GiB of path state).
+constexpr uint32_t kDefaultWavePaths = 32u << 20;
+
 enum Counter : int {
     kNIn = 0,
     kNOut = 1,
@@ -594,7 +597,7 @@ struct Launcher {
         const bool count = (p->flags & PT_RENDER_COUNTERS) != 0;
         const bool timing = (p->flags & PT_RENDER_KERNEL_TIMING) != 0;
         uint32_t frames_per_wave = p->wave_spp;
-        const uint32_t wave_paths = s->tuned_wave_paths ? s->tuned_wave_paths : 16u * 1024u * 1024u;
+        const uint32_t wave_paths = s->tuned_wave_paths ? s->tuned_wave_paths : kDefaultWavePaths;
         if (frames_per_wave == 0) frames_per_wave = std::max<uint32_t>(1, (uint32_t)(wave_paths / std::max<uint32_t>(npix, 1)));
         frames_per_wave = std::max<uint32_t>(1, std::min(frames_per_wave, std::max<uint32_t>(p->spp, 1)));
         const size_t cap = (size_t)frames_per_wave * npix;
@@ -823,63 +826,68 @@ int pt_render_impl(pt_scene *s, const pt_render_params *p, const pt_frame_buffer
     }
 }
 
-// Autotuner: every (BVH width, block size, wave size) combination renders
-// params->spp frames; the fastest by device time is applied to the scene.
+// Autotuner (coordinate search): every (BVH width, block size) pair renders
+// params->spp frames at the default wave size, then the wave sizes are tried
+// with the best pair.  The fastest by device time is applied to the scene.
 int pt_autotune_impl(pt_scene *s, const pt_render_params *params, const pt_frame_buffers *fb, pt_tune_result *out,
                      cudaStream_t st) {
     const uint32_t npix = s->dev.width_px * s->dev.height_px;
     const uint32_t spp = std::max<uint32_t>(1, params->spp);
     pt_tune_result r{};
     pt_bvh_opts opts = s->bvh_opts;
-    const uint32_t old_width = opts.width, old_block = s->tuned_block, old_wave = s->tuned_wave_paths;
     pt_render_params p = *params;
     p.spp = spp;
     p.block_size = 0;
     p.wave_spp = 0;
     p.flags &= ~(uint32_t)(PT_RENDER_KERNEL_TIMING | PT_RENDER_COUNTERS);
     auto time_render = [&](float &ms) -> int {
-        int e = pt_render_impl(s, &p, fb, st);  // first run: warm-up (graph instantiation, caches)
+        int e = pt_render_impl(s, &p, fb, st);  // warm-up (graph instantiation, caches)
         if (e != PT_OK) return e;
         e = pt_render_impl(s, &p, fb, st);
         ms = s->render_stats.render_ms;
+        r.trials++;
         return e;
     };
+    const uint32_t default_wave = kDefaultWavePaths;
     float base_ms = 0.f;
     int e = time_render(base_ms);
     if (e != PT_OK) return e;
     r.baseline_msamples_per_s = base_ms > 0.f ? (float)((double)npix * spp / (base_ms * 1e-3) / 1e6) : 0.f;
     float best_ms = 1e30f;
-    uint32_t best_w = old_width, best_b = 128, best_wave = 16u << 20;
-    const uint32_t widths[3] = {2, 4, 8}, blocks[3] = {64, 128, 256}, waves[3] = {1u << 20, 4u << 20, 16u << 20};
+    uint32_t best_w = opts.width, best_b = 128, best_wave = default_wave;
+    const uint32_t widths[3] = {2, 4, 8}, blocks[3] = {64, 128, 256}, waves[3] = {4u << 20, 16u << 20, 64u << 20};
     for (uint32_t wd : widths) {
         opts.width = wd;
         if ((e = pt_bvh_build_impl(s, &opts, st)) != PT_OK) return e;
-        uint32_t prev_frames = 0;
-        for (uint32_t wv : waves) {
-            uint32_t frames = std::max<uint32_t>(1, std::min(spp, wv / std::max<uint32_t>(npix, 1)));
-            if (frames == prev_frames) continue;  // same effective wave size as the previous candidate
-            prev_frames = frames;
-            for (uint32_t bs : blocks) {
-                s->tuned_block = bs;
-                s->tuned_wave_paths = wv;
-                float ms = 0.f;
-                if ((e = time_render(ms)) != PT_OK) return e;
-                r.trials++;
-                if (ms < best_ms) {
-                    best_ms = ms;
-                    best_w = wd;
-                    best_b = bs;
-                    best_wave = wv;
-                }
+        for (uint32_t bs : blocks) {
+            s->tuned_block = bs;
+            s->tuned_wave_paths = default_wave;
+            float ms = 0.f;
+            if ((e = time_render(ms)) != PT_OK) return e;
+            if (ms < best_ms) {
+                best_ms = ms;
+                best_w = wd;
+                best_b = bs;
             }
         }
     }
     opts.width = best_w;
     if ((e = pt_bvh_build_impl(s, &opts, st)) != PT_OK) return e;
     s->tuned_block = best_b;
+    uint32_t prev_frames = std::max<uint32_t>(1, std::min(spp, default_wave / std::max<uint32_t>(npix, 1)));
+    for (uint32_t wv : waves) {
+        uint32_t frames = std::max<uint32_t>(1, std::min(spp, wv / std::max<uint32_t>(npix, 1)));
+        if (frames == prev_frames && wv != default_wave) continue;  // same effective wave as the default
+        if (wv == default_wave) continue;
+        s->tuned_wave_paths = wv;
+        float ms = 0.f;
+        if ((e = time_render(ms)) != PT_OK) return e;
+        if (ms < best_ms) {
+            best_ms = ms;
+            best_wave = wv;
+        }
+    }
     s->tuned_wave_paths = best_wave;
-    (void)old_block;
-    (void)old_wave;
     r.bvh_width = best_w;
     r.block_size = best_b;
     r.wave_paths = best_wave;
