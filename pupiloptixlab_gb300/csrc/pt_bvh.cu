@@ -669,6 +669,7 @@ int pt_bvh_build_impl(pt_scene *s, const pt_bvh_opts *o, cudaStream_t st) {
     d.num_nodes = bs.num_nodes;
     uint32_t max_smem = (uint32_t)std::max(0, s->max_smem_per_block - 64 * 1024) / (32 * K);
     d.smem_nodes = std::min<uint32_t>(std::min(o->smem_nodes, bs.num_nodes), max_smem);
+    d.pad_mag = s->scene_mag;
     s->bvh_built = true;
     return PT_OK;
 }

@@ -175,6 +175,7 @@ struct DevScene {
     uint32_t num_nodes;
     uint32_t root_is_leaf_count;  // >0: single leaf root with this many prims
     uint32_t smem_nodes;
+    float pad_mag;          // scene magnitude the box padding was computed for
     // shading data (indexed by primitive id / vertex id)
     const uint32_t *tri_vidx;   // 3 per triangle
     const float4 *vpos;         // world positions

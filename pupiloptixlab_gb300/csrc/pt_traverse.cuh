@@ -222,7 +222,8 @@ PT_DI void trace_persistent(const DevScene &s, const float4 *snodes, int2 *sstac
     st.sp = 0;
     bool active = false, exhausted = false;
     uint32_t idx = 0, tag = 0;
-    float3 o = f3s(0.f), d = f3s(0.f), inv = f3s(0.f);
+    float3 o = f3s(0.f), d = f3s(0.f), inv = f3s(0.f), oi = f3s(0.f);
+    bool fma_slab = false;
     RayWT w{0, 1, 2, 0.f, 0.f, 1.f};
     float tmin = 0.f, tmax = 0.f;
     TraceResult best{0.f, -1, 0.f, 0.f};
@@ -252,6 +253,10 @@ PT_DI void trace_persistent(const DevScene &s, const float4 *snodes, int2 *sstac
                     src.load(r, o, d, tmin, tmax, tag);
                     w = ray_wt(d);
                     inv = safe_inv(d);
+                    oi = f3(o.x * inv.x, o.y * inv.y, o.z * inv.z);
+                    // the FMA slab form is conservative for origins inside the
+                    // magnitude the boxes were padded for
+                    fma_slab = fmaxf(fmaxf(fabsf(o.x), fabsf(o.y)), fabsf(o.z)) <= s.pad_mag;
                     best.t = tmax;
                     best.prim = -1;
                     best.u = best.v = 0.f;
@@ -267,29 +272,48 @@ PT_DI void trace_persistent(const DevScene &s, const float4 *snodes, int2 *sstac
         }
         if (busy == 0) break;
 
-        // inner nodes until every busy lane holds a leaf or has no work left
+        // Inner nodes.  A lane keeps stepping while its current item is an
+        // inner node, even after it has postponed a leaf (speculative
+        // traversal); the phase ends when every busy lane holds a leaf or
+        // no lane can step.
         for (;;) {
-            bool ready = !active || leaf != kNoItem || item == kNoItem;
-            if (__all_sync(FULL, ready)) break;
-            if (ready) continue;
+            bool can_step = active && item >= 0;
+            bool satisfied = !active || leaf != kNoItem || item == kNoItem;
+            if (__all_sync(FULL, satisfied)) break;
+            if (!__any_sync(FULL, can_step)) break;
+            if (!can_step) continue;
             WideNode<K> nd;
             if (item < static_cast<int>(s.smem_nodes)) load_node_smem<K>(snodes + (size_t)item * 2 * K, nd);
             else load_node<K>(s.nodes + (size_t)item * 2 * K, nd);
             if (COUNT) nodes++;
             int ci[K];
             float ct[K];
+            const float tlimit = best.t * kSlabScale;
 #pragma unroll
             for (int c = 0; c < K; c++) {
                 ci[c] = kNoItem;
                 ct[c] = __int_as_float(0x7f800000);
                 int ch = nd.child(c);
                 if (ch < 0) continue;
-                float tx0 = (nd.lox(c) - o.x) * inv.x, tx1 = (nd.hix(c) - o.x) * inv.x;
-                float ty0 = (nd.loy(c) - o.y) * inv.y, ty1 = (nd.hiy(c) - o.y) * inv.y;
-                float tz0 = (nd.loz(c) - o.z) * inv.z, tz1 = (nd.hiz(c) - o.z) * inv.z;
+                float tx0, tx1, ty0, ty1, tz0, tz1;
+                if (fma_slab) {  // t = lo * inv - o * inv: one rounding, conservative within pad_mag
+                    tx0 = __fmaf_rn(nd.lox(c), inv.x, -oi.x);
+                    tx1 = __fmaf_rn(nd.hix(c), inv.x, -oi.x);
+                    ty0 = __fmaf_rn(nd.loy(c), inv.y, -oi.y);
+                    ty1 = __fmaf_rn(nd.hiy(c), inv.y, -oi.y);
+                    tz0 = __fmaf_rn(nd.loz(c), inv.z, -oi.z);
+                    tz1 = __fmaf_rn(nd.hiz(c), inv.z, -oi.z);
+                } else {
+                    tx0 = (nd.lox(c) - o.x) * inv.x;
+                    tx1 = (nd.hix(c) - o.x) * inv.x;
+                    ty0 = (nd.loy(c) - o.y) * inv.y;
+                    ty1 = (nd.hiy(c) - o.y) * inv.y;
+                    tz0 = (nd.loz(c) - o.z) * inv.z;
+                    tz1 = (nd.hiz(c) - o.z) * inv.z;
+                }
                 float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
                 float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
-                tf = fminf(tf * kSlabScale, best.t * kSlabScale);
+                tf = fminf(tf * kSlabScale, tlimit);
                 if (!(tn <= tf)) continue;
                 int cnt = nd.count(c);
                 ci[c] = cnt > 0 ? make_leaf(ch, cnt) : ch;
@@ -313,7 +337,7 @@ PT_DI void trace_persistent(const DevScene &s, const float4 *snodes, int2 *sstac
             for (int i = K - 1; i >= 1; i--)
                 if (ci[i] != kNoItem) st.push(ci[i], ct[i], ovf);
             item = ci[0] != kNoItem ? ci[0] : pop_valid();
-            if (is_leaf(item)) {  // postpone it
+            if (is_leaf(item) && leaf == kNoItem) {  // postpone the first leaf
                 leaf = item;
                 item = pop_valid();
             }
