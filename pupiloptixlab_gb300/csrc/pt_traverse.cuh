@@ -319,8 +319,10 @@ PT_DI void trace_persistent(const DevScene &s, const float4 *snodes, int2 *sstac
                 ci[c] = cnt > 0 ? make_leaf(ch, cnt) : ch;
                 ct[c] = tn;
             }
+            // closest hit: nearest child first (sorting network); any hit: order
+            // does not matter, the children are taken as they come
 #pragma unroll
-            for (int i = 1; i < K; i++) {
+            for (int i = 1; i < (ANY ? 1 : K); i++) {
 #pragma unroll
                 for (int j = i; j > 0; j--) {
                     if (ct[j] < ct[j - 1]) {
@@ -336,6 +338,14 @@ PT_DI void trace_persistent(const DevScene &s, const float4 *snodes, int2 *sstac
 #pragma unroll
             for (int i = K - 1; i >= 1; i--)
                 if (ci[i] != kNoItem) st.push(ci[i], ct[i], ovf);
+            if (ANY) {  // unsorted: the first hit child is descended, the others pushed
+#pragma unroll
+                for (int i = 1; i < K; i++)
+                    if (ci[0] == kNoItem && ci[i] != kNoItem) {
+                        ci[0] = ci[i];
+                        ci[i] = kNoItem;
+                    }
+            }
             item = ci[0] != kNoItem ? ci[0] : pop_valid();
             if (is_leaf(item) && leaf == kNoItem) {  // postpone the first leaf
                 leaf = item;
