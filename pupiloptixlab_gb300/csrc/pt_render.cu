@@ -235,8 +235,9 @@ PT_DI int2 *stage_smem(const DevScene &s, float4 *smem) {
 }
 
 // ANY = false: closest hit of the extension rays; ANY = true: shadow rays.
+// Widths 2 and 4 are capped at 72 registers (7 blocks of 128 threads per SM).
 template <int K, bool ANY, bool COUNT>
-__global__ void k_trace_queue(DevScene s, State st) {
+__global__ void __maxnreg__(K == 8 ? 128 : 72) k_trace_queue(DevScene s, State st) {
     extern __shared__ float4 smem[];
     int2 *sstack = stage_smem<K>(s, smem);
     if (ANY) {

@@ -335,9 +335,6 @@ PT_DI void trace_persistent(const DevScene &s, const float4 *snodes, int2 *sstac
                     }
                 }
             }
-#pragma unroll
-            for (int i = K - 1; i >= 1; i--)
-                if (ci[i] != kNoItem) st.push(ci[i], ct[i], ovf);
             if (ANY) {  // unsorted: the first hit child is descended, the others pushed
 #pragma unroll
                 for (int i = 1; i < K; i++)
@@ -346,6 +343,9 @@ PT_DI void trace_persistent(const DevScene &s, const float4 *snodes, int2 *sstac
                         ci[i] = kNoItem;
                     }
             }
+#pragma unroll
+            for (int i = K - 1; i >= 1; i--)
+                if (ci[i] != kNoItem) st.push(ci[i], ct[i], ovf);
             item = ci[0] != kNoItem ? ci[0] : pop_valid();
             if (is_leaf(item) && leaf == kNoItem) {  // postpone the first leaf
                 leaf = item;
