@@ -287,6 +287,13 @@ int pt_scene_set_camera(pt_scene *scene, const pt_camera_desc *camera);
  * re-transformed).  positions: num_vertices*3 host floats.  The BVH must be
  * refit or rebuilt afterwards. */
 int pt_scene_update_vertices(pt_scene *scene, uint32_t mesh, const float *positions, uint32_t num_vertices);
+/* Replace the object-space positions of every mesh at once: `positions` is
+ * the concatenation, in mesh order, of each mesh's num_vertices*3 floats, on
+ * the host (on_device = 0) or the device (on_device = 1).  All instances are
+ * re-transformed on the device.  The BVH must be refit or rebuilt afterwards.
+ * Same role as the per-instance GAS/IAS updates of
+ * framework/world/ias_manager.cpp:116-151, for animated vertices. */
+int pt_scene_update_all_vertices(pt_scene *scene, const float *positions, int on_device, void *stream);
 /* Number of primitives (triangles then spheres) in world order. */
 int pt_scene_num_prims(const pt_scene *scene, uint32_t *num_triangles, uint32_t *num_spheres);
 

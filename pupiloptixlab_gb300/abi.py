@@ -121,6 +121,7 @@ PROTOTYPES = [
     ("pt_scene_destroy", C.c_int, [C.c_void_p]),
     ("pt_scene_set_camera", C.c_int, [C.c_void_p, C.POINTER(CameraDesc)]),
     ("pt_scene_update_vertices", C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32]),
+    ("pt_scene_update_all_vertices", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     ("pt_scene_num_prims", C.c_int, [C.c_void_p, c_uint_p, c_uint_p]),
     ("pt_bvh_build", C.c_int, [C.c_void_p, C.POINTER(BvhOpts), C.c_void_p]),
     ("pt_bvh_refit", C.c_int, [C.c_void_p, C.c_void_p]),

@@ -78,6 +78,18 @@ class GpuScene:
         abi.check(self.lib.pt_scene_update_vertices(self.handle, mesh, p.ctypes.data_as(C.c_void_p), p.shape[0]),
                   "pt_scene_update_vertices", self.lib)
 
+    def update_all_vertices(self, positions, stream=None) -> None:
+        """positions: all meshes' object-space vertices concatenated in mesh
+        order, as a (N, 3) float32 CUDA tensor or host array."""
+        if isinstance(positions, torch.Tensor) and positions.is_cuda:
+            p = positions.contiguous()
+            st = self.lib.pt_scene_update_all_vertices(self.handle, C.c_void_p(p.data_ptr()), 1, _stream_ptr(stream))
+        else:
+            import numpy as np
+            p = np.ascontiguousarray(positions, np.float32)
+            st = self.lib.pt_scene_update_all_vertices(self.handle, p.ctypes.data_as(C.c_void_p), 0, _stream_ptr(stream))
+        abi.check(st, "pt_scene_update_all_vertices", self.lib)
+
     def bvh_stats(self) -> abi.BvhStats:
         st = abi.BvhStats()
         abi.check(self.lib.pt_bvh_get_stats(self.handle, C.byref(st)), "pt_bvh_get_stats", self.lib)

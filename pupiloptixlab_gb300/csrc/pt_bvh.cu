@@ -465,6 +465,47 @@ __global__ void k_rebuild_tri_records(const uint32_t *tri_vidx, const float4 *vp
     r[2] = make_float4(c.x, c.y, c.z, 0.f);
 }
 
+// All mesh instances at once: world vertex v belongs to the instance whose
+// range [vstart, vstart + count) holds it (binary search over vstart).
+struct XformRec {
+    uint32_t vstart, count, src;  // world vertex range, first object vertex of its mesh
+    uint32_t pad;
+    float4 m0, m1, m2;
+};
+__global__ void k_transform_all(const float *obj, const XformRec *recs, uint32_t nrec, uint32_t total, float4 *vpos) {
+    uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= total) return;
+    uint32_t lo = 0, hi = nrec - 1;
+    while (lo < hi) {
+        uint32_t mid = (lo + hi + 1) >> 1;
+        if (recs[mid].vstart <= v) lo = mid;
+        else hi = mid - 1;
+    }
+    const XformRec r = recs[lo];
+    uint32_t k = r.src + (v - r.vstart);
+    float x = obj[3 * (size_t)k], y = obj[3 * (size_t)k + 1], z = obj[3 * (size_t)k + 2];
+    float wx = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(r.m0.x, x), __fmul_rn(r.m0.y, y)), __fmul_rn(r.m0.z, z)), r.m0.w);
+    float wy = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(r.m1.x, x), __fmul_rn(r.m1.y, y)), __fmul_rn(r.m1.z, z)), r.m1.w);
+    float wz = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(r.m2.x, x), __fmul_rn(r.m2.y, y)), __fmul_rn(r.m2.z, z)), r.m2.w);
+    vpos[v] = make_float4(wx, wy, wz, 0.f);
+}
+
+// Root box area for the SAH normalisation: union of the root node's slots.
+template <int K>
+__global__ void k_root_area(const float *nodes, double *out) {
+    if (threadIdx.x || blockIdx.x) return;
+    float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    for (int c = 0; c < K; c++) {
+        if (__float_as_int(nodes[6 * K + c]) < 0) continue;
+        for (int a = 0; a < 3; a++) {
+            lo[a] = fminf(lo[a], nodes[2 * a * K + c]);
+            hi[a] = fmaxf(hi[a], nodes[(2 * a + 1) * K + c]);
+        }
+    }
+    double ex = hi[0] - lo[0], ey = hi[1] - lo[1], ez = hi[2] - lo[2];
+    *out = lo[0] <= hi[0] ? ex * ey + ey * ez + ez * ex : 0.0;
+}
+
 inline uint32_t blocks(size_t n, int b) { return (uint32_t)((n + b - 1) / b); }
 
 struct Scratch {
@@ -557,6 +598,23 @@ template <int K>
 void sah_launch(pt_scene *s, double *acc, cudaStream_t st) {
     uint32_t nn = s->level_start.back();
     k_sah<K><<<blocks(nn, 256), 256, 0, st>>>(s->nodes.as<float>(), nn, acc);
+    k_root_area<K><<<1, 1, 0, st>>>(s->nodes.as<float>(), acc + 1);
+}
+
+// SAH cost of the current wide tree (node cost 1.2, primitive cost 1),
+// normalised by the root box area.
+int compute_sah(pt_scene *s, double *scratch2, cudaStream_t st, float &out) {
+    PT_CUDA_TRY(cudaMemsetAsync(scratch2, 0, 2 * sizeof(double), st));
+    switch (s->bvh_opts.width) {
+        case 2: sah_launch<2>(s, scratch2, st); break;
+        case 4: sah_launch<4>(s, scratch2, st); break;
+        default: sah_launch<8>(s, scratch2, st); break;
+    }
+    double h[2] = {0.0, 0.0};
+    PT_CUDA_TRY(cudaMemcpyAsync(h, scratch2, sizeof(h), cudaMemcpyDeviceToHost, st));
+    PT_CUDA_TRY(cudaStreamSynchronize(st));
+    out = h[1] > 0 ? (float)((kCostNode * h[1] + h[0]) / h[1]) : 0.f;
+    return PT_OK;
 }
 
 }  // namespace
@@ -630,33 +688,20 @@ int pt_bvh_build_impl(pt_scene *s, const pt_bvh_opts *o, cudaStream_t st) {
     }
     if (e != PT_OK) return e;
     PT_CUDA_TRY(cudaEventRecord(s->ev1, st));
-    PT_CUDA_TRY(cudaMemsetAsync(sc.sah, 0, sizeof(double), st));
-    switch (K) {
-        case 2: sah_launch<2>(s, sc.sah, st); break;
-        case 4: sah_launch<4>(s, sc.sah, st); break;
-        default: sah_launch<8>(s, sc.sah, st); break;
-    }
-    double sah = 0.0;
-    float4 rlo = make_float4(0, 0, 0, 0), rhi = rlo;
-    PT_CUDA_TRY(cudaMemcpyAsync(&sah, sc.sah, sizeof(double), cudaMemcpyDeviceToHost, st));
-    if (n > 0) {
-        uint32_t root = n > 1 ? 0 : 0;
-        PT_CUDA_TRY(cudaMemcpyAsync(&rlo, sc.nlo + root, sizeof(float4), cudaMemcpyDeviceToHost, st));
-        PT_CUDA_TRY(cudaMemcpyAsync(&rhi, sc.nhi + root, sizeof(float4), cudaMemcpyDeviceToHost, st));
-    }
-    PT_CUDA_TRY(cudaStreamSynchronize(st));
+    PT_CUDA_TRY(cudaEventSynchronize(s->ev1));
     float ms = 0.f;
     PT_CUDA_TRY(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
-    float ex = rhi.x - rlo.x, ey = rhi.y - rlo.y, ez = rhi.z - rlo.z;
-    double root_area = (double)ex * ey + (double)ey * ez + (double)ez * ex;
-
     s->bvh_opts = *o;
+    float sah = 0.f;
+    if ((e = s->sah_scratch.ensure(64)) != PT_OK) return e;
+    if ((e = compute_sah(s, s->sah_scratch.as<double>(), st, sah)) != PT_OK) return e;
+
     pt_bvh_stats &bs = s->bvh_stats;
     bs.width = o->width;
     bs.num_nodes = s->level_start.back();
     bs.num_prims = n;
     bs.max_depth = (uint32_t)s->level_start.size() - 1;
-    bs.sah_cost = root_area > 0 ? (float)((kCostNode * root_area + sah) / root_area) : 0.f;
+    bs.sah_cost = sah;
     bs.build_ms = ms;
     bs.node_bytes = (uint64_t)bs.num_nodes * 32 * K;
     bs.prim_bytes = (uint64_t)n * 48;
@@ -691,6 +736,41 @@ int pt_bvh_refit_impl(pt_scene *s, cudaStream_t st) {
     float ms = 0.f;
     PT_CUDA_TRY(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
     s->bvh_stats.build_ms = ms;
+    int e = s->sah_scratch.ensure(64);
+    if (e != PT_OK) return e;
+    return compute_sah(s, s->sah_scratch.as<double>(), st, s->bvh_stats.sah_cost);
+}
+
+int pt_update_all_world_vertices(pt_scene *s, const float *d_obj_pos, cudaStream_t st) {
+    const uint32_t nrec = (uint32_t)s->mesh_instances.size();
+    if (nrec == 0) return PT_OK;
+    if (!s->xform_table.ptr) {
+        std::vector<uint64_t> mesh_start(s->mesh_num_vertices.size() + 1, 0);
+        for (size_t m = 0; m < s->mesh_num_vertices.size(); m++) mesh_start[m + 1] = mesh_start[m] + s->mesh_num_vertices[m];
+        std::vector<XformRec> recs(nrec);
+        for (uint32_t i = 0; i < nrec; i++) {
+            const MeshInstanceRef &r = s->mesh_instances[i];
+            const float *m = r.to_world;
+            recs[i].vstart = r.vertex_offset;
+            recs[i].count = s->mesh_num_vertices[r.mesh];
+            recs[i].src = (uint32_t)mesh_start[r.mesh];
+            recs[i].pad = 0;
+            recs[i].m0 = make_float4(m[0], m[1], m[2], m[3]);
+            recs[i].m1 = make_float4(m[4], m[5], m[6], m[7]);
+            recs[i].m2 = make_float4(m[8], m[9], m[10], m[11]);
+        }
+        int e = s->xform_table.ensure(sizeof(XformRec) * nrec);
+        if (e != PT_OK) return e;
+        PT_CUDA_TRY(cudaMemcpy(s->xform_table.ptr, recs.data(), sizeof(XformRec) * nrec, cudaMemcpyHostToDevice));
+    }
+    const uint32_t total = s->num_vertices;
+    if (total) k_transform_all<<<blocks(total, 256), 256, 0, st>>>(d_obj_pos, s->xform_table.as<XformRec>(), nrec, total,
+                                                                   s->vpos.as<float4>());
+    if (s->num_tris)
+        k_rebuild_tri_records<<<blocks(s->num_tris, 256), 256, 0, st>>>(s->tri_vidx.as<uint32_t>(), s->vpos.as<float4>(), 0,
+                                                                        s->num_tris, s->prims_world.as<float4>());
+    PT_CUDA_TRY(cudaGetLastError());
+    PT_CUDA_TRY(cudaStreamSynchronize(st));
     return PT_OK;
 }
 

@@ -82,6 +82,10 @@ struct pt_scene {
     // BVH build scratch and results
     DevBuf bvh_scratch;
     DevBuf bvh_order;  // primitive id of each leaf slot (sorted Morton order)
+    DevBuf sah_scratch;     // two doubles for the SAH reduction
+    DevBuf xform_table;     // per mesh instance: world vertex range + matrix (all-vertex updates)
+    DevBuf all_obj_pos;     // host positions staged for pt_scene_update_all_vertices
+    uint64_t total_mesh_vertices = 0;
     std::vector<uint32_t> level_start;  // first wide node of each level; back() = num_nodes
     pt_bvh_opts bvh_opts{};
     pt_bvh_stats bvh_stats{};
@@ -112,3 +116,4 @@ int pt_bsdf_sample_impl(const float *bsdf, const float *wo, uint32_t *rng, float
 // Re-transforms the world vertices / primitive records of mesh instances on the device.
 int pt_update_world_vertices(pt_scene *s, uint32_t mesh, const float *d_obj_pos, uint32_t num_vertices,
                              cudaStream_t stream);
+int pt_update_all_world_vertices(pt_scene *s, const float *d_obj_pos, cudaStream_t stream);

@@ -196,7 +196,11 @@ int build_scene(pt_scene *s, const pt_scene_desc *d) {
     std::vector<uint32_t> tri_vidx, prim_inst;
     std::vector<DevInstance> insts(d->num_instances);
     s->mesh_num_vertices.resize(d->num_meshes);
-    for (uint32_t i = 0; i < d->num_meshes; i++) s->mesh_num_vertices[i] = d->meshes[i].num_vertices;
+    s->total_mesh_vertices = 0;
+    for (uint32_t i = 0; i < d->num_meshes; i++) {
+        s->mesh_num_vertices[i] = d->meshes[i].num_vertices;
+        s->total_mesh_vertices += d->meshes[i].num_vertices;
+    }
 
     float mag = 0.f;
     uint32_t ntri = 0;
@@ -458,7 +462,7 @@ void DevBuf::release() {
 
 pt_scene::~pt_scene() {
     DevBuf *all[] = {&prims_world, &prims_bvh, &nodes, &tri_vidx, &vpos, &vnrm, &vuv, &prim_inst, &inst, &mats,
-                     &emitters, &emitter_cdf, &mesh_obj_pos, &bvh_scratch, &bvh_order, &ws.ray_o, &ws.ray_d, &ws.hit, &ws.thr,
+                     &emitters, &emitter_cdf, &mesh_obj_pos, &bvh_scratch, &bvh_order, &sah_scratch, &xform_table, &all_obj_pos, &ws.ray_o, &ws.ray_d, &ws.hit, &ws.thr,
                      &ws.rad, &ws.rng, &ws.meta, &ws.q0, &ws.q1, &ws.sh_o, &ws.sh_d, &ws.sh_c, &ws.mat_key,
                      &ws.counters, &ws.sort_tmp};
     for (DevBuf *b : all) b->release();
@@ -562,6 +566,24 @@ int pt_scene_update_vertices(pt_scene *scene, uint32_t mesh, const float *positi
     if (st != PT_OK) return st;
     PT_CUDA_TRY(cudaMemcpy(scene->mesh_obj_pos.ptr, positions, 12ull * num_vertices, cudaMemcpyHostToDevice));
     return pt_update_world_vertices(scene, mesh, scene->mesh_obj_pos.as<float>(), num_vertices, 0);
+}
+
+int pt_scene_update_all_vertices(pt_scene *scene, const float *positions, int on_device, void *stream) {
+    clear_stale_cuda_error();
+    if (!scene || !positions) { pt_set_error("scene or positions is NULL"); return PT_ERR_INVALID; }
+    PT_CUDA_TRY(cudaSetDevice(scene->device));
+    const float *src = positions;
+    if (!on_device) {
+        size_t n = 3 * scene->total_mesh_vertices;
+        for (size_t v = 0; v < n; v++)
+            if (!std::isfinite(positions[v])) { pt_set_error("non-finite vertex coordinate"); return PT_ERR_INVALID; }
+        int st = scene->all_obj_pos.ensure(std::max<size_t>(4 * n, 16));
+        if (st != PT_OK) return st;
+        PT_CUDA_TRY(cudaMemcpyAsync(scene->all_obj_pos.ptr, positions, 4 * n, cudaMemcpyHostToDevice,
+                                    static_cast<cudaStream_t>(stream)));
+        src = scene->all_obj_pos.as<float>();
+    }
+    return pt_update_all_world_vertices(scene, src, static_cast<cudaStream_t>(stream));
 }
 
 int pt_bvh_build(pt_scene *scene, const pt_bvh_opts *opts, void *stream) {
