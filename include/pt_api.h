@@ -291,6 +291,8 @@ int pt_scene_update_vertices(pt_scene *scene, uint32_t mesh, const float *positi
  * the concatenation, in mesh order, of each mesh's num_vertices*3 floats, on
  * the host (on_device = 0) or the device (on_device = 1).  All instances are
  * re-transformed on the device.  The BVH must be refit or rebuilt afterwards.
+ * When an emissive instance is a mesh, its light triangles (positions, areas,
+ * selection probabilities) are rebuilt too; the call then waits for `stream`.
  * Same role as the per-instance GAS/IAS updates of
  * framework/world/ias_manager.cpp:116-151, for animated vertices. */
 int pt_scene_update_all_vertices(pt_scene *scene, const float *positions, int on_device, void *stream);

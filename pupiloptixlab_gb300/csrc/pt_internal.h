@@ -46,6 +46,19 @@ struct MeshInstanceRef {  // where the world vertices of one mesh instance live
     float to_world[16];
 };
 
+// One emissive instance, kept so that the emitter table can be rebuilt after
+// vertex updates (instance order = emitter order).
+struct EmitterSource {
+    bool sphere = false;
+    float radiance[3] = {0, 0, 0};
+    uint32_t vertex_offset = 0;     // mesh: first world vertex of the instance
+    std::vector<uint32_t> indices;  // mesh: object-space triangle indices
+    std::vector<float> normals;     // mesh: object-space vertex normals (empty: geometric)
+    float nm[9] = {0};              // mesh: normal matrix
+    float center[3] = {0, 0, 0};    // sphere: world centre
+    float radius = 0.f;
+};
+
 struct RenderWorkspace {
     size_t capacity = 0;  // path slots
     DevBuf ray_o, ray_d, hit, thr, rad, rng, meta, q0, q1, sh_o, sh_d, sh_c, mat_key, counters, sort_tmp;
@@ -86,6 +99,10 @@ struct pt_scene {
     DevBuf xform_table;     // per mesh instance: world vertex range + matrix (all-vertex updates)
     DevBuf all_obj_pos;     // host positions staged for pt_scene_update_all_vertices
     uint64_t total_mesh_vertices = 0;
+    std::vector<EmitterSource> emitter_sources;
+    bool has_env = false;
+    float env_radiance[3] = {0, 0, 0};
+    bool has_emissive_mesh = false;
     std::vector<uint32_t> level_start;  // first wide node of each level; back() = num_nodes
     pt_bvh_opts bvh_opts{};
     pt_bvh_stats bvh_stats{};
@@ -117,3 +134,6 @@ int pt_bsdf_sample_impl(const float *bsdf, const float *wo, uint32_t *rng, float
 int pt_update_world_vertices(pt_scene *s, uint32_t mesh, const float *d_obj_pos, uint32_t num_vertices,
                              cudaStream_t stream);
 int pt_update_all_world_vertices(pt_scene *s, const float *d_obj_pos, cudaStream_t stream);
+// pt_scene.cpp: (re)build the emitter table from the world vertices on the
+// device (host_vpos, if given, holds them already).
+int pt_rebuild_emitters(pt_scene *s, const float4 *host_vpos);

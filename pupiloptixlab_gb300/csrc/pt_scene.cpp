@@ -308,37 +308,105 @@ int build_scene(pt_scene *s, const pt_scene_desc *d) {
         for (int k = 0; k < 4; k++) dm.tex[k] = to_dev(m.tex[k]);
     }
 
-    // area emitters in instance order (world/emitter.cpp:169-263)
-    std::vector<DevEmitter> ems;
-    std::vector<float> weights;  // Emitter::weight = GetWeight(radiance) * area
+    // emissive instances in instance order (world/emitter.cpp:169-263)
+    s->emitter_sources.clear();
+    s->has_emissive_mesh = false;
+    uint32_t n_area = 0;
     for (uint32_t ii = 0; ii < d->num_instances; ii++) {
         const pt_instance_desc &id = d->instances[ii];
         if (!id.is_emitter) continue;
         DevInstance &in = insts[ii];
-        in.emitter_offset = (int32_t)ems.size();
-        H3 rad = h3(id.radiance[0], id.radiance[1], id.radiance[2]);
-        float w = std::max(std::max(rad.x, rad.y), rad.z);  // GetWeight (emitter.cpp:77-101)
+        in.emitter_offset = (int32_t)n_area;
+        EmitterSource src;
+        memcpy(src.radiance, id.radiance, sizeof(src.radiance));
         if (id.shape_type == PT_SHAPE_MESH) {
             const pt_mesh_desc &m = d->meshes[id.shape_index];
             double inv[16];
             inverse4f(id.to_world, inv);
-            float nm[9];
-            normal_matrix(inv, nm);
-            uint32_t voff = 0;
+            normal_matrix(inv, src.nm);
             for (auto &r : s->mesh_instances)
-                if (r.instance == ii) voff = r.vertex_offset;
-            for (uint32_t t = 0; t < m.num_triangles; t++) {
+                if (r.instance == ii) src.vertex_offset = r.vertex_offset;
+            src.indices.assign(m.indices, m.indices + 3ull * m.num_triangles);
+            if (m.normals) src.normals.assign(m.normals, m.normals + 3ull * m.num_vertices);
+            n_area += m.num_triangles;
+            s->has_emissive_mesh = true;
+        } else {
+            src.sphere = true;
+            src.center[0] = in.sphere.x;
+            src.center[1] = in.sphere.y;
+            src.center[2] = in.sphere.z;
+            src.radius = in.sphere.w;
+            n_area += 1;
+        }
+        s->emitter_sources.push_back(std::move(src));
+    }
+    s->has_env = d->env.type == PT_ENV_CONST;
+    memcpy(s->env_radiance, d->env.radiance, sizeof(s->env_radiance));
+
+    int e;
+    if ((e = upload(s->prims_world, prims)) != PT_OK) return e;
+    if ((e = upload(s->tri_vidx, tri_vidx)) != PT_OK) return e;
+    if ((e = upload(s->vpos, vpos)) != PT_OK) return e;
+    if ((e = upload(s->vnrm, vnrm)) != PT_OK) return e;
+    if ((e = upload(s->vuv, vuv)) != PT_OK) return e;
+    if ((e = upload(s->prim_inst, prim_inst)) != PT_OK) return e;
+    if ((e = upload(s->inst, insts)) != PT_OK) return e;
+    if ((e = upload(s->mats, mats)) != PT_OK) return e;
+    s->h_prims_world = std::move(prims);
+
+    ptd::DevScene &dv = s->dev;
+    dv.tri_vidx = s->tri_vidx.as<uint32_t>();
+    dv.vpos = s->vpos.as<float4>();
+    dv.vnrm = s->vnrm.as<float4>();
+    dv.vuv = s->vuv.as<float2>();
+    dv.prim_inst = s->prim_inst.as<uint32_t>();
+    dv.inst = s->inst.as<DevInstance>();
+    dv.mats = s->mats.as<DevMaterial>();
+    dv.num_tris = ntri;
+    if ((e = pt_rebuild_emitters(s, vpos.data())) != PT_OK) return e;
+    dv.width_px = d->width;
+    dv.height_px = d->height;
+    set_camera(s, d->camera);
+    return PT_OK;
+}
+
+}  // namespace
+
+// Emitter table (world/emitter.cpp:169-243) and selection probabilities
+// (EmitterHelper::ComputeProbability, world/emitter.cpp:321-337), from the
+// current world vertices: host_vpos when the caller holds them, else a copy
+// of each emissive mesh instance's vertex range from the device.
+int pt_rebuild_emitters(pt_scene *s, const float4 *host_vpos) {
+    std::vector<DevEmitter> ems;
+    std::vector<float> weights;  // Emitter::weight = GetWeight(radiance) * area
+    std::vector<float4> fetched;
+    for (const EmitterSource &src : s->emitter_sources) {
+        H3 rad = h3(src.radiance[0], src.radiance[1], src.radiance[2]);
+        float w = std::max(std::max(rad.x, rad.y), rad.z);  // GetWeight (emitter.cpp:77-101)
+        if (!src.sphere) {
+            const float4 *vp;
+            if (host_vpos) {
+                vp = host_vpos + src.vertex_offset;
+            } else {
+                uint32_t nv = 0;
+                for (uint32_t i : src.indices) nv = std::max(nv, i + 1);
+                fetched.resize(std::max<uint32_t>(nv, 1));
+                PT_CUDA_TRY(cudaMemcpy(fetched.data(), s->vpos.as<float4>() + src.vertex_offset, 16ull * nv,
+                                       cudaMemcpyDeviceToHost));
+                vp = fetched.data();
+            }
+            for (size_t t = 0; 3 * t < src.indices.size(); t++) {
                 DevEmitter e{};
                 H3 P[3], N[3];
                 for (int k = 0; k < 3; k++) {
-                    uint32_t vi = m.indices[3 * t + k];
-                    float4 p = vpos[voff + vi];
+                    float4 p = vp[src.indices[3 * t + k]];
                     P[k] = h3(p.x, p.y, p.z);
                 }
                 for (int k = 0; k < 3; k++) {
-                    uint32_t vi = m.indices[3 * t + k];
-                    H3 nw = m.normals ? xform_vec(nm, h3(m.normals[3 * vi], m.normals[3 * vi + 1], m.normals[3 * vi + 2]))
-                                      : hcross(sub(P[1], P[0]), sub(P[2], P[0]));
+                    uint32_t vi = src.indices[3 * t + k];
+                    H3 nw = !src.normals.empty()
+                                ? xform_vec(src.nm, h3(src.normals[3 * vi], src.normals[3 * vi + 1], src.normals[3 * vi + 2]))
+                                : hcross(sub(P[1], P[0]), sub(P[2], P[0]));
                     float len = sqrtf(nw.x * nw.x + nw.y * nw.y + nw.z * nw.z);  // TransformNormal normalises
                     N[k] = h3(nw.x / len, nw.y / len, nw.z / len);
                 }
@@ -359,7 +427,7 @@ int build_scene(pt_scene *s, const pt_scene_desc *d) {
             }
         } else {
             DevEmitter e{};
-            float r = in.sphere.w;
+            float r = src.radius;
             float area = 4 * 3.14159265358979323846f * r * r;
             uint32_t type = ptd::kEmitSphere;
             float tf;
@@ -367,15 +435,13 @@ int build_scene(pt_scene *s, const pt_scene_desc *d) {
             e.a = make_float4(tf, 0.f, area, r);
             weights.push_back(w * area);
             e.rad = make_float4(rad.x, rad.y, rad.z, 0.f);
-            e.p0 = make_float4(in.sphere.x, in.sphere.y, in.sphere.z, 0.f);
+            e.p0 = make_float4(src.center[0], src.center[1], src.center[2], 0.f);
             ems.push_back(e);
         }
     }
-    // EmitterHelper::ComputeProbability (world/emitter.cpp:321-337)
-    bool has_env = d->env.type == PT_ENV_CONST;
     float wsum = 0.f;
     for (float w : weights) wsum += w;
-    size_t n_emit = (has_env ? 1 : 0) + ems.size();
+    size_t n_emit = (s->has_env ? 1 : 0) + ems.size();
     std::vector<float> cdf;
     float acc = 0.f;
     for (size_t i = 0; i < ems.size(); i++) {
@@ -386,48 +452,24 @@ int build_scene(pt_scene *s, const pt_scene_desc *d) {
         acc += p;
     }
     DevEmitter env{};
-    if (has_env) {
+    if (s->has_env) {
         uint32_t type = ptd::kEmitConstEnv;
         float tf;
         memcpy(&tf, &type, 4);
         env.a = make_float4(tf, 1.f / (float)n_emit, 0.f, 0.f);
-        env.rad = make_float4(d->env.radiance[0], d->env.radiance[1], d->env.radiance[2], 0.f);
+        env.rad = make_float4(s->env_radiance[0], s->env_radiance[1], s->env_radiance[2], 0.f);
     }
-
     int e;
-    if ((e = upload(s->prims_world, prims)) != PT_OK) return e;
-    if ((e = upload(s->tri_vidx, tri_vidx)) != PT_OK) return e;
-    if ((e = upload(s->vpos, vpos)) != PT_OK) return e;
-    if ((e = upload(s->vnrm, vnrm)) != PT_OK) return e;
-    if ((e = upload(s->vuv, vuv)) != PT_OK) return e;
-    if ((e = upload(s->prim_inst, prim_inst)) != PT_OK) return e;
-    if ((e = upload(s->inst, insts)) != PT_OK) return e;
-    if ((e = upload(s->mats, mats)) != PT_OK) return e;
     if ((e = upload(s->emitters, ems)) != PT_OK) return e;
     if ((e = upload(s->emitter_cdf, cdf)) != PT_OK) return e;
-    s->h_prims_world = std::move(prims);
-
     ptd::DevScene &dv = s->dev;
-    dv.tri_vidx = s->tri_vidx.as<uint32_t>();
-    dv.vpos = s->vpos.as<float4>();
-    dv.vnrm = s->vnrm.as<float4>();
-    dv.vuv = s->vuv.as<float2>();
-    dv.prim_inst = s->prim_inst.as<uint32_t>();
-    dv.inst = s->inst.as<DevInstance>();
-    dv.mats = s->mats.as<DevMaterial>();
     dv.emitters = s->emitters.as<DevEmitter>();
     dv.emitter_cdf = s->emitter_cdf.as<float>();
     dv.num_emitters = (uint32_t)ems.size();
-    dv.num_tris = ntri;
-    dv.has_env = has_env ? 1 : 0;
+    dv.has_env = s->has_env ? 1 : 0;
     dv.env = env;
-    dv.width_px = d->width;
-    dv.height_px = d->height;
-    set_camera(s, d->camera);
     return PT_OK;
 }
-
-}  // namespace
 
 // Entry points start by clearing the runtime's last-error state, so that an
 // error left behind by some other call in the process is not reported here.
@@ -565,7 +607,10 @@ int pt_scene_update_vertices(pt_scene *scene, uint32_t mesh, const float *positi
     int st = scene->mesh_obj_pos.ensure(std::max<size_t>(12ull * num_vertices, 16));
     if (st != PT_OK) return st;
     PT_CUDA_TRY(cudaMemcpy(scene->mesh_obj_pos.ptr, positions, 12ull * num_vertices, cudaMemcpyHostToDevice));
-    return pt_update_world_vertices(scene, mesh, scene->mesh_obj_pos.as<float>(), num_vertices, 0);
+    st = pt_update_world_vertices(scene, mesh, scene->mesh_obj_pos.as<float>(), num_vertices, 0);
+    if (st != PT_OK || !scene->has_emissive_mesh) return st;
+    PT_CUDA_TRY(cudaDeviceSynchronize());
+    return pt_rebuild_emitters(scene, nullptr);
 }
 
 int pt_scene_update_all_vertices(pt_scene *scene, const float *positions, int on_device, void *stream) {
@@ -583,7 +628,12 @@ int pt_scene_update_all_vertices(pt_scene *scene, const float *positions, int on
                                     static_cast<cudaStream_t>(stream)));
         src = scene->all_obj_pos.as<float>();
     }
-    return pt_update_all_world_vertices(scene, src, static_cast<cudaStream_t>(stream));
+    int st = pt_update_all_world_vertices(scene, src, static_cast<cudaStream_t>(stream));
+    if (st != PT_OK || !scene->has_emissive_mesh) return st;
+    // Light triangles moved: the emitter table is rebuilt from the new world
+    // vertices once the update kernels on `stream` have finished.
+    PT_CUDA_TRY(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)));
+    return pt_rebuild_emitters(scene, nullptr);
 }
 
 int pt_bvh_build(pt_scene *scene, const pt_bvh_opts *opts, void *stream) {

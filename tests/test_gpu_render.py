@@ -99,7 +99,7 @@ def test_no_accumulation_and_depth_override(cuda_ctx):
 
 
 def test_icosphere_field_reduced(cuda_ctx):
-    """The configs[1] scene (all 7 materials, env + sphere lights, depth 8) at
+    """The icosphere-field scene (all 7 materials, env + sphere lights, depth 8) at
     reduced resolution: same-stream agreement and counters."""
     sc = scenes.icosphere_field(96, 54)
     o = oracle.OracleScene(sc)

@@ -83,7 +83,7 @@ def test_leaf_sizes(cuda_ctx, max_leaf):
 
 
 def test_full_size_scene_primary_rays(cuda_ctx):
-    """configs[1] geometry (1,032,192 triangles + 4 spheres) at 1920x1080:
+    """Icosphere-field geometry (1,032,192 triangles + 4 spheres) at 1920x1080:
     every 16th primary ray against the oracle's BVH2 (itself equal to brute
     force, tests/test_oracle_host.py) and 192 rays against brute force."""
     sc = scenes.icosphere_field()
