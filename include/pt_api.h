@@ -357,6 +357,98 @@ int pt_bsdf_sample_batch(const float *bsdf, const float *wo, uint32_t *rng_state
                          float *out_wi, float *out_f, float *out_pdf, uint32_t *out_type,
                          uint32_t n, void *stream);
 
+/* ---- learned denoiser ------------------------------------------------- */
+/* Replaces the OptiX HDR denoiser of the reference's DenoisePass
+ * (framework/system/denoise_pass.cpp:50-75 -> optix::Denoiser::Execute,
+ * framework/optix/denoiser.cpp:171-267; inputs colour + albedo + normal guide
+ * layers of the path tracer) with a 5-level U-Net (14 convolutions, 3x3,
+ * widths 32-48-64-128-256, 1,259,072 parameters) trained by this library on
+ * pairs the tracer renders.  Weights and activations are BF16 with FP32
+ * accumulation; every convolution (forward, data and weight gradient) runs
+ * on the tensor cores (tcgen05) with TMA-staged operands.  The network works
+ * in the log domain: channels 0-2 of its input are log(1 + colour), its
+ * output is log(1 + denoised colour), the loss is L1 on log(1 + x).
+ *
+ * Training inputs are 9-channel FP16 pixels (colour RGB, albedo RGB, normal
+ * XYZ), targets FP32 RGB, both NHWC and on the device. */
+typedef struct pt_denoiser pt_denoiser;
+
+typedef struct pt_denoiser_opts {
+    float lr;          /* Adam step size (1e-3) */
+    float beta1;       /* 0.9 */
+    float beta2;       /* 0.999 */
+    float eps;         /* 1e-8 */
+    uint64_t seed;     /* weight initialisation (He-uniform) */
+} pt_denoiser_opts;
+
+typedef struct pt_denoise_io {
+    uint32_t width, height;
+    const float *color;   /* device, width*height float4 (the renderer's accum/frame buffer) */
+    const float *albedo;  /* device, width*height float3 */
+    const float *normal;  /* device, width*height float3 */
+    float *output;        /* device, width*height float4 (denoised, alpha 1) */
+    uint32_t tile;        /* fallback tile side in pixels (0: 16) */
+    float fallback_rel;   /* fall back to the raw colour where a tile's mean luminance moved by more */
+    float fallback_sigma; /* than max(fallback_rel * mean, fallback_sigma * standard error); <= 0: no fallback */
+    uint8_t *tile_fallback; /* device, optional: one byte per tile, 1 = raw colour kept */
+} pt_denoise_io;
+
+typedef struct pt_denoise_stats {
+    uint32_t tiles;          /* tiles of the last pt_denoise */
+    uint32_t fallback_tiles; /* of which kept the raw colour */
+    float last_ms;           /* device time of the last pt_denoise */
+} pt_denoise_stats;
+
+/* No reference counterpart (OptiX denoiser models are fixed).  opts may be
+ * NULL for the defaults. */
+int pt_denoiser_create(pt_context *ctx, const pt_denoiser_opts *opts, pt_denoiser **out);
+void pt_denoiser_destroy(pt_denoiser *dn);
+/* Number of FP32 parameters (per layer: weights [cout][9][cin] then bias[cout],
+ * layers in the order of pt_denoiser_layer); the first layer's cin is 16
+ * (9 used) and the last layer's cout is 16 (3 used). */
+int pt_denoiser_num_params(const pt_denoiser *dn, uint64_t *count);
+int pt_denoiser_layer(const pt_denoiser *dn, uint32_t index, uint32_t *cin, uint32_t *cout, uint64_t *offset);
+/* HOST pointers: copy the FP32 master parameters out / in (in: also resets Adam). */
+int pt_denoiser_get_params(const pt_denoiser *dn, float *params);
+int pt_denoiser_set_params(pt_denoiser *dn, const float *params);
+/* Forward + backward of the L1 log loss on a batch; gradients stay on the
+ * device (pt_denoiser_get_grads, HOST pointer), *loss (HOST) the batch mean. */
+int pt_denoiser_compute_grads(pt_denoiser *dn, const void *input_f16, const float *target, uint32_t n,
+                              uint32_t height, uint32_t width, float *loss, void *stream);
+int pt_denoiser_get_grads(const pt_denoiser *dn, float *grads);
+/* One Adam step on a batch (height = width = crop side, multiples of 16).
+ * The step runs as one CUDA graph; the batch loss is summed on the device
+ * and read (mean over the steps since the last read) by pt_denoiser_read_loss. */
+int pt_denoiser_train_step(pt_denoiser *dn, const void *input_f16, const float *target, uint32_t n, uint32_t crop,
+                           void *stream);
+int pt_denoiser_read_loss(pt_denoiser *dn, float *mean_loss);
+/* Network output for a batch: out = width*height*n*3 FP32 linear RGB (device). */
+int pt_denoiser_forward(pt_denoiser *dn, const void *input_f16, uint32_t n, uint32_t height, uint32_t width,
+                        float *out, void *stream);
+/* Denoise one rendered frame (any size; padded internally to multiples of 16),
+ * with the per-tile fallback to the raw colour. */
+int pt_denoise(pt_denoiser *dn, const pt_denoise_io *io, void *stream);
+int pt_denoise_get_stats(const pt_denoiser *dn, pt_denoise_stats *out);
+/* Pack a rendered frame (device float4 colour, float3 albedo, float3 normal)
+ * into the 9-channel FP16 training layout (device, width*height*9 halves). */
+int pt_denoise_pack(const float *color, const float *albedo, const float *normal, uint32_t width, uint32_t height,
+                    void *out_f16, void *stream);
+
+/* Convolution kernels of the denoiser, exposed for the gradient checks.
+ * DEVICE pointers, NHWC BF16 tensors (raw 16-bit), weights [cout_pad][9][cin]
+ * with cout_pad = cout rounded up to 16, cin a multiple of 16.
+ * forward: y = x (*) w + bias, ReLU if relu, y BF16 [n][h][w][cout] or FP32 if out_f32.
+ * backward_data: dx = dy (*) flip(w)^T, times (mask > 0) where mask (BF16, the
+ *   shape of dx) is given; dy has cout_pad channels.
+ * backward_weights: dw[cout][9][cin] += sum_p x (x) dy, db[cout] += sum_p dy
+ *   (FP32, caller zeroes); dy has cout channels (a multiple of 16). */
+int pt_conv3x3_forward(const void *x, uint32_t n, uint32_t h, uint32_t w, uint32_t cin, const void *weight,
+                       const float *bias, uint32_t cout, int relu, int out_f32, void *y, void *stream);
+int pt_conv3x3_backward_data(const void *dy, uint32_t n, uint32_t h, uint32_t w, uint32_t cout, const void *weight,
+                             uint32_t cin, const void *mask, void *dx, void *stream);
+int pt_conv3x3_backward_weights(const void *x, uint32_t n, uint32_t h, uint32_t w, uint32_t cin, const void *dy,
+                                uint32_t cout, float *dweight, float *dbias, void *stream);
+
 /* ---- host helpers (no GPU needed) ------------------------------------- */
 /* Camera matrices from a mitsuba-style sensor: fov_y in degrees,
  * to_world row-major 4x4 in Pupil's convention (+Z points away from the view).

@@ -112,6 +112,21 @@ class TuneResult(C.Structure):
 
 
 # (name, restype, argtypes) of every entry point declared in include/pt_api.h.
+class DenoiserOpts(C.Structure):
+    _fields_ = [("lr", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("eps", C.c_float),
+                ("seed", C.c_uint64)]
+
+
+class DenoiseIO(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("color", C.c_void_p), ("albedo", C.c_void_p),
+                ("normal", C.c_void_p), ("output", C.c_void_p), ("tile", C.c_uint32), ("fallback_rel", C.c_float),
+                ("fallback_sigma", C.c_float), ("tile_fallback", C.c_void_p)]
+
+
+class DenoiseStats(C.Structure):
+    _fields_ = [("tiles", C.c_uint32), ("fallback_tiles", C.c_uint32), ("last_ms", C.c_float)]
+
+
 PROTOTYPES = [
     ("pt_api_version", C.c_int, []),
     ("pt_last_error", C.c_int, [C.c_char_p, C.c_size_t]),
@@ -134,6 +149,29 @@ PROTOTYPES = [
     ("pt_trace_rays", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_int, C.c_void_p]),
     ("pt_bsdf_eval_batch", C.c_int, [C.c_void_p] * 5 + [C.c_uint32, C.c_void_p]),
     ("pt_bsdf_sample_batch", C.c_int, [C.c_void_p] * 7 + [C.c_uint32, C.c_void_p]),
+    ("pt_denoiser_create", C.c_int, [C.c_void_p, C.POINTER(DenoiserOpts), C.POINTER(C.c_void_p)]),
+    ("pt_denoiser_destroy", None, [C.c_void_p]),
+    ("pt_denoiser_num_params", C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),
+    ("pt_denoiser_layer", C.c_int, [C.c_void_p, C.c_uint32, c_uint_p, c_uint_p, C.POINTER(C.c_uint64)]),
+    ("pt_denoiser_get_params", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("pt_denoiser_set_params", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("pt_denoiser_compute_grads", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32,
+                                            C.POINTER(C.c_float), C.c_void_p]),
+    ("pt_denoiser_get_grads", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("pt_denoiser_train_step", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p]),
+    ("pt_denoiser_read_loss", C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
+    ("pt_denoiser_forward", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p,
+                                      C.c_void_p]),
+    ("pt_denoise", C.c_int, [C.c_void_p, C.POINTER(DenoiseIO), C.c_void_p]),
+    ("pt_denoise_get_stats", C.c_int, [C.c_void_p, C.POINTER(DenoiseStats)]),
+    ("pt_denoise_pack", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p,
+                                  C.c_void_p]),
+    ("pt_conv3x3_forward", C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p,
+                                     C.c_void_p, C.c_uint32, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
+    ("pt_conv3x3_backward_data", C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p,
+                                           C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("pt_conv3x3_backward_weights", C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p,
+                                              C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("pt_camera_make", C.c_int, [C.c_float, C.c_float, C.c_float, C.c_float, C.POINTER(C.c_float),
                                  C.POINTER(CameraDesc)]),
 ]

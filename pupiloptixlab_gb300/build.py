@@ -34,6 +34,8 @@ NVCC_COMMON = GENCODE + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,
 CU_SOURCES = {
     "pt_bvh.cu": [],
     "pt_render.cu": ["-fmad=false"],
+    "pt_conv.cu": [],
+    "pt_denoise.cu": [],
 }
 CPP_SOURCES = ["pt_scene.cpp"]
 # C++ host layer above the C-ABI (Pass / System / scene loader): its own

@@ -1,0 +1,794 @@
+// pt_conv.cu -- BF16 3x3 convolutions as implicit GEMMs on tcgen05 tensor
+// cores, operands brought into shared memory by TMA (no multicast), FP32
+// accumulators in tensor memory.  Interface and GEMM shapes: pt_conv.h.
+//
+// Tiling.  One CTA of 128 threads computes a 128-row accumulator tile:
+//   forward / data gradient: 128 pixels (one 128-wide row segment, or
+//     128 / W whole rows of a narrow image) x n_tile output channels;
+//   weight gradient: 128 (tap, input channel) rows x n_tile output channels,
+//     accumulated over a range of pixel tiles and added to the FP32 result.
+// Thread 0 issues the TMA loads into a ring of `stages` buffers, thread 32
+// issues the MMAs (one per 16-element K slice) and commits each buffer back
+// to the producer; after the last commit all four warps read the accumulator
+// (warp w owns TMEM lanes 32w..32w+31) and run the epilogue.
+//
+// Shared-memory operand layouts are the canonical swizzled ones for a row of
+// R = 2 * KC bytes (R = 32, 64, 128 B, TMA swizzle of the same width):
+//   K-major (forward A = pixels x channels, B = out channels x channels):
+//     rows R bytes apart, 8-row groups SBO = 8R apart; a 16-element K slice
+//     starts 32 B further along the row.
+//   MN-major (weight gradient, A = channels x pixels, B = channels x pixels):
+//     each TMA box holds 128 pixels (K) x KC channels (MN) as 128 rows of R
+//     bytes; 8-pixel groups are SBO = 8R apart, consecutive KC-channel blocks
+//     LBO = 128R apart; a 16-pixel K slice starts 16R further on.
+// The zero padding of the convolution comes from TMA's out-of-bounds fill:
+// the box for tap (dy, dx) starts at (x0 + dx - 1, y0 + dy - 1).
+//
+// Every wait is bounded (%globaltimer, 2 s): on expiry the kernel records a
+// code in *err, stops issuing work, lets issued copies and MMAs drain (again
+// with a bound), frees its tensor memory and returns.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+
+#include "pt_conv.h"
+#include "pt_internal.h"
+
+namespace ptconv {
+
+constexpr int kMaxStages = 8;
+constexpr uint64_t kWaitNs = 2000000000ull;
+
+// ---------------------------------------------------------------------------
+// device primitives (inline PTX)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ uint64_t gtimer() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait for the phase with the given parity to complete.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, bool backoff = false) {
+    if (mbar_try(bar, parity)) return true;
+    const uint64_t t0 = gtimer();
+    while (!mbar_try(bar, parity)) {
+        if (backoff) __nanosleep(128);
+        if (gtimer() - t0 > kWaitNs) return false;
+    }
+    return true;
+}
+__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap *map, uint32_t bar, int c0, int c1, int c2,
+                                            int c3) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
+        : "memory");
+}
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, uint32_t bar, int c0, int c1) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(bar)
+        : "memory");
+}
+__device__ __forceinline__ void tmem_alloc(uint32_t slot, uint32_t cols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot), "r"(cols) : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t cols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(cols) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void umma_bf16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                          uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(dtmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+__device__ __forceinline__ void umma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+// 32 lanes x 16 consecutive 32-bit columns: thread t of the warp gets lane
+// (warp base + t), columns col..col+15.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
+// Shared-memory matrix descriptor (tcgen05): start, leading and stride byte
+// offsets in 16-byte units, descriptor version 1 at bit 46, swizzle mode in
+// bits 61-63 (2 = 128 B, 4 = 64 B, 6 = 32 B).
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo, uint32_t swz) {
+    return static_cast<uint64_t>((addr >> 4) & 0x3FFFu) | (static_cast<uint64_t>((lbo >> 4) & 0x3FFFu) << 16) |
+           (static_cast<uint64_t>((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46) | (static_cast<uint64_t>(swz) << 61);
+}
+// Instruction descriptor, kind::f16: FP32 D, BF16 A and B, K-major (0) or
+// MN-major (1) operands, N >> 3 at bit 17, M >> 4 at bit 24.
+__host__ __device__ constexpr uint32_t idesc_bf16(int m, int n, bool a_mn, bool b_mn) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((a_mn ? 1u : 0u) << 15) | ((b_mn ? 1u : 0u) << 16) |
+           (static_cast<uint32_t>(n >> 3) << 17) | (static_cast<uint32_t>(m >> 4) << 24);
+}
+template <int KC>
+__host__ __device__ constexpr uint32_t swz_mode() {
+    return KC == 64 ? 2u : KC == 32 ? 4u : 6u;
+}
+
+__device__ __forceinline__ void record_error(unsigned *err, unsigned code) {
+    if (err) atomicOr(err, code);
+}
+
+__device__ __forceinline__ uint16_t f2bf(float f) {
+    __nv_bfloat16 h = __float2bfloat16_rn(f);
+    return *reinterpret_cast<uint16_t *>(&h);
+}
+
+// ---------------------------------------------------------------------------
+// forward / data-gradient kernel
+// ---------------------------------------------------------------------------
+template <int KC>
+__global__ void __launch_bounds__(128, 1)
+    k_conv_fwd(const __grid_constant__ CUtensorMap act, const __grid_constant__ CUtensorMap wgt, const FwdArgs a) {
+    constexpr int R = KC * 2;
+    constexpr uint32_t SWZ = swz_mode<KC>();
+    extern __shared__ uint8_t smem_raw[];
+    __shared__ __align__(8) uint64_t bars[2 * kMaxStages + 1];
+    __shared__ uint32_t tmem_slot;
+    __shared__ int s_issued, s_consumed, s_fail;
+
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
+    const int S = a.stages;
+    const int a_bytes = 128 * R, b_bytes = a.n_tile * R;
+    const uint32_t tx_bytes = static_cast<uint32_t>(a.tile_w * a.tile_rows * R + b_bytes);  // what the boxes deliver
+    const int tiles_img = a.tiles_x * a.tiles_y;
+    const int img = blockIdx.x / tiles_img, t = blockIdx.x - img * tiles_img;
+    const int x0 = (t % a.tiles_x) * a.tile_w, y0 = (t / a.tiles_x) * a.tile_rows;
+    const int n0 = blockIdx.y * a.n_tile;
+    const int nk = 9 * a.nchunks;
+    const uint32_t bar0 = smem_u32(bars);
+    auto full = [&](int s) { return bar0 + 8u * s; };
+    auto empty = [&](int s) { return bar0 + 8u * (kMaxStages + s); };
+    const uint32_t done = bar0 + 8u * (2 * kMaxStages);
+
+    if (warp == 0) tmem_alloc(smem_u32(&tmem_slot), a.tmem_cols);
+    if (tid == 32) {
+        for (int s = 0; s < S; s++) {
+            mbar_init(full(s), 1);
+            mbar_init(empty(s), 1);
+        }
+        mbar_init(done, 1);
+        mbar_fence_init();
+        s_issued = 0;
+        s_consumed = 0;
+        s_fail = 0;
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_slot;
+
+    if (tid == 0) {
+        int k = 0;
+        for (; k < nk; k++) {
+            const int s = k % S;
+            if (k >= S && !mbar_wait(empty(s), ((k / S) - 1) & 1)) {
+                record_error(a.err, 1u);
+                s_fail = 1;
+                break;
+            }
+            if (*reinterpret_cast<volatile int *>(&s_fail)) break;
+            const int tap = k / a.nchunks, ch = k - tap * a.nchunks;
+            const int dy = tap / 3, dx = tap - dy * 3;
+            const uint32_t sa = base + s * a.stage_bytes, sb = sa + a_bytes;
+            mbar_expect_tx(full(s), tx_bytes);
+            tma_load_4d(sa, &act, full(s), ch * KC, x0 + dx - 1, y0 + dy - 1, img);
+            tma_load_2d(sb, &wgt, full(s), tap * a.cin + ch * KC, n0);
+        }
+        s_issued = k;
+    } else if (tid == 32) {
+        const uint32_t idesc = idesc_bf16(128, a.n_tile, false, false);
+        int k = 0;
+        for (; k < nk; k++) {
+            const int s = k % S;
+            if (!mbar_wait(full(s), (k / S) & 1)) {
+                record_error(a.err, 2u);
+                s_fail = 1;
+                break;
+            }
+            tc_fence_after();
+            const uint32_t sa = base + s * a.stage_bytes, sb = sa + a_bytes;
+#pragma unroll
+            for (int j = 0; j < KC / 16; j++) {
+                const uint64_t da = sdesc(sa + 32u * j, 16u, 8u * R, SWZ);
+                const uint64_t db = sdesc(sb + 32u * j, 16u, 8u * R, SWZ);
+                umma_bf16(tmem, da, db, idesc, (k | j) != 0 ? 1u : 0u);
+            }
+            umma_commit(empty(s));
+        }
+        s_consumed = k;
+        umma_commit(done);
+    }
+    __syncwarp();
+    const bool ok = mbar_wait(done, 0, true);
+    if (!ok && tid == 0) record_error(a.err, 4u);
+    tc_fence_after();
+
+    // epilogue: accumulator row `tid` = pixel (x0 + tid % tile_w, y0 + tid / tile_w)
+    const int px = tid % a.tile_w, py = tid / a.tile_w;
+    const int x = x0 + px, y = y0 + py;
+    const bool valid = ok && py < a.tile_rows && x < a.W && y < a.H;
+    const size_t pix = ((size_t)img * a.H + (valid ? y : 0)) * a.W + (valid ? x : 0);
+    const uint32_t trow = tmem + (static_cast<uint32_t>(warp * 32) << 16);
+    for (int c = 0; c < a.n_tile; c += 16) {
+        float v[16];
+        tmem_ld16(trow + c, v);
+        const int ch0 = n0 + c;
+        if (!valid || ch0 >= a.cout) continue;
+        const int nvalid = min(16, a.cout - ch0);
+        if (a.epi == EPI_F32) {
+            float *o = static_cast<float *>(a.out) + pix * a.out_ctot + a.out_coff + ch0;
+            for (int i = 0; i < nvalid; i++) o[i] = v[i] + (a.bias ? a.bias[ch0 + i] : 0.f);
+            continue;
+        }
+        if (a.epi == EPI_BF16) {
+#pragma unroll
+            for (int i = 0; i < 16; i++) {
+                float f = v[i] + ((a.bias && i < nvalid) ? a.bias[ch0 + i] : 0.f);
+                v[i] = a.relu ? fmaxf(f, 0.f) : f;
+            }
+        } else {
+            const uint16_t *m = a.mask + pix * a.mask_ctot + a.mask_coff + ch0;
+            if (nvalid == 16) {
+                uint4 q0 = *reinterpret_cast<const uint4 *>(m), q1 = *reinterpret_cast<const uint4 *>(m + 8);
+                const uint16_t *h0 = reinterpret_cast<const uint16_t *>(&q0), *h1 = reinterpret_cast<const uint16_t *>(&q1);
+#pragma unroll
+                for (int i = 0; i < 8; i++) {
+                    if (!(h0[i] != 0 && (h0[i] & 0x8000u) == 0)) v[i] = 0.f;
+                    if (!(h1[i] != 0 && (h1[i] & 0x8000u) == 0)) v[i + 8] = 0.f;
+                }
+            } else {
+                for (int i = 0; i < nvalid; i++)
+                    if (!(m[i] != 0 && (m[i] & 0x8000u) == 0)) v[i] = 0.f;
+            }
+        }
+        uint16_t *o = static_cast<uint16_t *>(a.out) + pix * a.out_ctot + a.out_coff + ch0;
+        if (nvalid == 16) {
+            uint4 q0, q1;
+            uint32_t *w0 = reinterpret_cast<uint32_t *>(&q0), *w1 = reinterpret_cast<uint32_t *>(&q1);
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                w0[i] = f2bf(v[2 * i]) | (static_cast<uint32_t>(f2bf(v[2 * i + 1])) << 16);
+                w1[i] = f2bf(v[8 + 2 * i]) | (static_cast<uint32_t>(f2bf(v[8 + 2 * i + 1])) << 16);
+            }
+            reinterpret_cast<uint4 *>(o)[0] = q0;
+            reinterpret_cast<uint4 *>(o)[1] = q1;
+        } else {
+            for (int i = 0; i < nvalid; i++) o[i] = f2bf(v[i]);
+        }
+    }
+
+    tc_fence_before();
+    __syncthreads();
+    if (tid == 0 && s_fail) {  // let copies that were issued but never consumed land
+        for (int k = s_consumed; k < s_issued; k++) (void)mbar_wait(full(k % S), (k / S) & 1);
+    }
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, a.tmem_cols);
+}
+
+// ---------------------------------------------------------------------------
+// weight-gradient kernel
+// ---------------------------------------------------------------------------
+template <int KCA, int KCB>
+__global__ void __launch_bounds__(128, 1)
+    k_conv_wgrad(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap gmap, const WgradArgs a) {
+    constexpr int RA = KCA * 2, RB = KCB * 2;
+    constexpr uint32_t SWZA = swz_mode<KCA>(), SWZB = swz_mode<KCB>();
+    constexpr int A_BLOCKS = 128 / KCA;
+    extern __shared__ uint8_t smem_raw[];
+    __shared__ __align__(8) uint64_t bars[2 * kMaxStages + 1];
+    __shared__ uint32_t tmem_slot;
+    __shared__ int s_issued, s_consumed, s_fail;
+
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
+    const int S = a.stages;
+    const int blk0 = blockIdx.x * A_BLOCKS;
+    const int nblk = min(A_BLOCKS, 9 * a.nchunks_a - blk0);
+    const int n0 = blockIdx.y * a.n_tile;
+    const int nbb = a.n_tile / KCB;
+    const int t_begin = blockIdx.z * a.tiles_per_split;
+    const int nk = max(0, min(a.total_tiles, t_begin + a.tiles_per_split) - t_begin);
+    const int a_bytes = 128 * 128 * 2;
+    const int tile_px = a.tile_w * a.tile_rows;  // pixels one box delivers
+    const uint32_t tx_bytes = static_cast<uint32_t>(nblk * tile_px * RA + nbb * tile_px * RB);
+    const int tiles_img = a.tiles_x * a.tiles_y;
+    const uint32_t bar0 = smem_u32(bars);
+    auto full = [&](int s) { return bar0 + 8u * s; };
+    auto empty = [&](int s) { return bar0 + 8u * (kMaxStages + s); };
+    const uint32_t done = bar0 + 8u * (2 * kMaxStages);
+
+    if (a.zero_fill) {  // rows that no box covers must read as zero pixels
+        uint4 z = make_uint4(0, 0, 0, 0);
+        uint8_t *p = smem_raw + (base - smem_u32(smem_raw));
+        for (int i = tid; i < S * a.stage_bytes / 16; i += blockDim.x) reinterpret_cast<uint4 *>(p)[i] = z;
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == 0) tmem_alloc(smem_u32(&tmem_slot), a.tmem_cols);
+    if (tid == 32) {
+        for (int s = 0; s < S; s++) {
+            mbar_init(full(s), 1);
+            mbar_init(empty(s), 1);
+        }
+        mbar_init(done, 1);
+        mbar_fence_init();
+        s_issued = 0;
+        s_consumed = 0;
+        s_fail = 0;
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_slot;
+
+    if (tid == 0) {
+        int k = 0;
+        for (; k < nk; k++) {
+            const int s = k % S;
+            if (k >= S && !mbar_wait(empty(s), ((k / S) - 1) & 1)) {
+                record_error(a.err, 1u);
+                s_fail = 1;
+                break;
+            }
+            if (*reinterpret_cast<volatile int *>(&s_fail)) break;
+            const int tile = t_begin + k;
+            const int img = tile / tiles_img, t = tile - img * tiles_img;
+            const int x0 = (t % a.tiles_x) * a.tile_w, y0 = (t / a.tiles_x) * a.tile_rows;
+            const uint32_t sa = base + s * a.stage_bytes, sb = sa + a_bytes;
+            mbar_expect_tx(full(s), tx_bytes);
+            for (int q = 0; q < nblk; q++) {
+                const int b = blk0 + q;
+                const int tap = b / a.nchunks_a, ch = b - tap * a.nchunks_a;
+                const int dy = tap / 3, dx = tap - dy * 3;
+                tma_load_4d(sa + q * 128 * RA, &xmap, full(s), ch * KCA, x0 + dx - 1, y0 + dy - 1, img);
+            }
+            for (int q = 0; q < nbb; q++) tma_load_4d(sb + q * 128 * RB, &gmap, full(s), n0 + q * KCB, x0, y0, img);
+        }
+        s_issued = k;
+    } else if (tid == 32) {
+        const uint32_t idesc = idesc_bf16(128, a.n_tile, true, true);
+        int k = 0;
+        for (; k < nk; k++) {
+            const int s = k % S;
+            if (!mbar_wait(full(s), (k / S) & 1)) {
+                record_error(a.err, 2u);
+                s_fail = 1;
+                break;
+            }
+            tc_fence_after();
+            const uint32_t sa = base + s * a.stage_bytes, sb = sa + a_bytes;
+#pragma unroll
+            for (int j = 0; j < 8; j++) {  // 16 pixels per MMA
+                const uint64_t da = sdesc(sa + 16u * RA * j, 128u * RA, 8u * RA, SWZA);
+                const uint64_t db = sdesc(sb + 16u * RB * j, 128u * RB, 8u * RB, SWZB);
+                umma_bf16(tmem, da, db, idesc, (k | j) != 0 ? 1u : 0u);
+            }
+            umma_commit(empty(s));
+        }
+        s_consumed = k;
+        umma_commit(done);
+    }
+    __syncwarp();
+    const bool ok = nk > 0 && mbar_wait(done, 0, true);
+    if (!ok && nk > 0 && tid == 0) record_error(a.err, 4u);
+    tc_fence_after();
+
+    // epilogue: row tid = A row (tap, ci) index g; dw[co][g] += D[tid][co - n0]
+    const int g = blk0 * KCA + tid;
+    const bool valid = ok && tid < nblk * KCA;
+    const uint32_t trow = tmem + (static_cast<uint32_t>(warp * 32) << 16);
+    const size_t kdim = 9 * static_cast<size_t>(a.cin);
+    for (int c = 0; c < a.n_tile; c += 16) {
+        float v[16];
+        tmem_ld16(trow + c, v);
+        if (!valid) continue;
+        for (int i = 0; i < 16; i++) {
+            const int co = n0 + c + i;
+            if (co < a.cout) atomicAdd(a.dw + co * kdim + g, v[i]);
+        }
+    }
+
+    tc_fence_before();
+    __syncthreads();
+    if (tid == 0 && s_fail) {
+        for (int k = s_consumed; k < s_issued; k++) (void)mbar_wait(full(k % S), (k / S) & 1);
+    }
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, a.tmem_cols);
+}
+
+// ---------------------------------------------------------------------------
+// small kernels
+// ---------------------------------------------------------------------------
+__global__ void k_bias_grad(const uint16_t *g, int ctot, int coff, int c, long long npix, float *db) {
+    extern __shared__ float sacc[];
+    const int per = blockDim.x / c;  // pixels per pass
+    const int lane_c = threadIdx.x % c, lane_p = threadIdx.x / c;
+    float acc = 0.f;
+    if (lane_p < per) {
+        for (long long p = (long long)blockIdx.x * per + lane_p; p < npix; p += (long long)gridDim.x * per) {
+            uint32_t bits = static_cast<uint32_t>(g[p * ctot + coff + lane_c]) << 16;
+            acc += __uint_as_float(bits);
+        }
+    }
+    sacc[threadIdx.x] = acc;
+    __syncthreads();
+    if (threadIdx.x < c) {
+        float s = 0.f;
+        for (int i = 0; i < per; i++) s += sacc[i * c + threadIdx.x];
+        atomicAdd(db + threadIdx.x, s);
+    }
+}
+
+__global__ void k_flip_transpose(const uint16_t *w, int cout, int cin, uint16_t *wt) {
+    const long long n = 9ll * cout * cin;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int ci = static_cast<int>(i % cin);
+        const int tap = static_cast<int>((i / cin) % 9);
+        const int co = static_cast<int>(i / (9ll * cin));
+        wt[(static_cast<long long>(ci) * 9 + (8 - tap)) * cout + co] = w[i];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+namespace {
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    });
+    return fn;
+}
+
+CUtensorMapSwizzle swizzle_for(int kc) {
+    return kc == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : kc == 32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B;
+}
+
+struct Tiling {
+    int tile_w, tile_rows, tiles_x, tiles_y;
+};
+Tiling tiling_for(int h, int w) {
+    Tiling t;
+    if (w >= 128) {
+        t.tile_w = 128;
+        t.tile_rows = 1;
+    } else {
+        t.tile_w = w;
+        t.tile_rows = std::min(128 / w, h);
+    }
+    t.tiles_x = (w + t.tile_w - 1) / t.tile_w;
+    t.tiles_y = (h + t.tile_rows - 1) / t.tile_rows;
+    return t;
+}
+
+int act_map(CUtensorMap *m, const Act &a, int kc, const Tiling &t) {
+    auto fn = encode_fn();
+    if (!fn) {
+        pt_set_error("cuTensorMapEncodeTiled is not available from the driver");
+        return PT_ERR_CUDA;
+    }
+    char *p = static_cast<char *>(a.ptr) + 2ull * a.coff;
+    if ((reinterpret_cast<uintptr_t>(p) & 15) || (a.ctot % 8) || (a.c % kc)) {
+        pt_set_error("activation tensor: base, channel stride or channel count misaligned (ctot %d coff %d c %d)", a.ctot,
+                     a.coff, a.c);
+        return PT_ERR_INVALID;
+    }
+    cuuint64_t dims[4] = {(cuuint64_t)a.c, (cuuint64_t)a.w, (cuuint64_t)a.h, (cuuint64_t)a.n};
+    cuuint64_t strides[3] = {2ull * a.ctot, 2ull * a.ctot * a.w, 2ull * a.ctot * a.w * a.h};
+    cuuint32_t box[4] = {(cuuint32_t)kc, (cuuint32_t)t.tile_w, (cuuint32_t)t.tile_rows, 1};
+    cuuint32_t es[4] = {1, 1, 1, 1};
+    CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, p, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                    swizzle_for(kc), CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        pt_set_error("cuTensorMapEncodeTiled (activation %dx%dx%dx%d, box %d) failed: %d", a.n, a.h, a.w, a.c, kc,
+                     static_cast<int>(r));
+        return PT_ERR_CUDA;
+    }
+    return PT_OK;
+}
+
+int wgt_map(CUtensorMap *m, const void *w, int kdim, int rows, int kc, int n_tile) {
+    auto fn = encode_fn();
+    if (!fn) {
+        pt_set_error("cuTensorMapEncodeTiled is not available from the driver");
+        return PT_ERR_CUDA;
+    }
+    if ((reinterpret_cast<uintptr_t>(w) & 15) || (kdim % 8)) {
+        pt_set_error("weight tensor misaligned");
+        return PT_ERR_INVALID;
+    }
+    cuuint64_t dims[2] = {(cuuint64_t)kdim, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {2ull * kdim};
+    cuuint32_t box[2] = {(cuuint32_t)kc, (cuuint32_t)n_tile};
+    cuuint32_t es[2] = {1, 1};
+    CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(w), dims, strides, box, es,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle_for(kc), CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        pt_set_error("cuTensorMapEncodeTiled (weights %dx%d, box %dx%d) failed: %d", rows, kdim, kc, n_tile,
+                     static_cast<int>(r));
+        return PT_ERR_CUDA;
+    }
+    return PT_OK;
+}
+
+int pow2_cols(int n) {
+    int c = 32;
+    while (c < n) c <<= 1;
+    return c;
+}
+
+// Dynamic shared memory for `stages` buffers, raised where needed so that no
+// more CTAs share an SM than its 512 tensor-memory columns can hold.
+int smem_request(int stages, int stage_bytes, int tmem_cols) {
+    const int by_stages = stages * stage_bytes + 1024;
+    const int max_ctas = 512 / tmem_cols;
+    const int floor_bytes = (228 * 1024) / (max_ctas + 1) + 1024;
+    return std::max(by_stages, max_ctas >= 32 ? 0 : floor_bytes);
+}
+
+// Raises a kernel instantiation's dynamic shared-memory limit to `bytes`
+// when a launch needs more than it was given so far (per process).
+template <class K>
+int set_smem_attr(K kernel, int bytes) {
+    static std::mutex mu;
+    static std::map<const void *, int> raised;  // kernel -> limit set so far
+    std::lock_guard<std::mutex> lock(mu);
+    const void *key = reinterpret_cast<const void *>(kernel);
+    auto it = raised.find(key);
+    const int have = it == raised.end() ? 48 * 1024 : it->second;
+    if (bytes <= have) return PT_OK;
+    PT_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    raised[key] = bytes;
+    return PT_OK;
+}
+
+}  // namespace
+
+int pick_kc(int c) {
+    if (c % 64 == 0) return 64;
+    if (c % 32 == 0) return 32;
+    return 16;
+}
+
+int fwd_prepare(FwdOp *op, const Act &in, const void *w, int w_rows, int cout, const float *bias, int epi, int relu,
+                void *out, int out_ctot, int out_coff, const Act *mask, unsigned *err) {
+    if (in.c <= 0 || in.c % 16 || cout <= 0 || in.n <= 0 || in.h <= 0 || in.w <= 0) {
+        pt_set_error("conv forward: channel counts must be positive multiples of 16 (cin %d, cout %d)", in.c, cout);
+        return PT_ERR_INVALID;
+    }
+    if (epi == EPI_BF16_MASK && (!mask || mask->n != in.n || mask->h != in.h || mask->w != in.w)) {
+        pt_set_error("conv forward: mask tensor missing or of the wrong shape");
+        return PT_ERR_INVALID;
+    }
+    if (epi != EPI_F32 && ((out_ctot % 8) || (out_coff % 8))) {
+        pt_set_error("conv forward: bf16 output channel stride/offset must be multiples of 8");
+        return PT_ERR_INVALID;
+    }
+    const int kc = pick_kc(in.c);
+    const Tiling t = tiling_for(in.h, in.w);
+    const int cout_pad = (cout + 15) / 16 * 16;
+    int ntiles = (cout_pad + 255) / 256;
+    int n_tile = ((cout_pad / ntiles) + 15) / 16 * 16;
+    ntiles = (cout_pad + n_tile - 1) / n_tile;
+    int st;
+    if ((st = act_map(&op->act, in, kc, t)) != PT_OK) return st;
+    if ((st = wgt_map(&op->wgt, w, 9 * in.c, w_rows, kc, n_tile)) != PT_OK) return st;
+    FwdArgs &a = op->args;
+    memset(&a, 0, sizeof(a));
+    a.n_img = in.n;
+    a.H = in.h;
+    a.W = in.w;
+    a.tile_w = t.tile_w;
+    a.tile_rows = t.tile_rows;
+    a.tiles_x = t.tiles_x;
+    a.tiles_y = t.tiles_y;
+    a.cin = in.c;
+    a.nchunks = in.c / kc;
+    a.n_tile = n_tile;
+    a.cout = cout;
+    a.tmem_cols = pow2_cols(n_tile);
+    a.stage_bytes = (128 * 2 * kc + n_tile * 2 * kc + 1023) / 1024 * 1024;
+    const int target_ctas = std::min(512 / a.tmem_cols, 3);
+    const int budget = (225 * 1024) / target_ctas - 2048;
+    a.stages = std::max(2, std::min(6, budget / a.stage_bytes));
+    a.epi = epi;
+    a.relu = relu;
+    a.bias = bias;
+    a.out = out;
+    a.out_ctot = out_ctot;
+    a.out_coff = out_coff;
+    if (mask) {
+        a.mask = static_cast<const uint16_t *>(mask->ptr);
+        a.mask_ctot = mask->ctot;
+        a.mask_coff = mask->coff;
+    }
+    a.err = err;
+    op->kc = kc;
+    op->smem = smem_request(a.stages, a.stage_bytes, a.tmem_cols);
+    op->grid = dim3(static_cast<unsigned>(in.n * t.tiles_x * t.tiles_y), static_cast<unsigned>(ntiles), 1);
+    if (op->smem > 220 * 1024) {
+        pt_set_error("conv forward: shared memory request %d too large", op->smem);
+        return PT_ERR_INVALID;
+    }
+    return PT_OK;
+}
+
+int fwd_launch(const FwdOp &op, cudaStream_t stream) {
+    int st = PT_OK;
+    switch (op.kc) {
+        case 64:
+            st = set_smem_attr(k_conv_fwd<64>, op.smem);
+            if (st == PT_OK) k_conv_fwd<64><<<op.grid, 128, op.smem, stream>>>(op.act, op.wgt, op.args);
+            break;
+        case 32:
+            st = set_smem_attr(k_conv_fwd<32>, op.smem);
+            if (st == PT_OK) k_conv_fwd<32><<<op.grid, 128, op.smem, stream>>>(op.act, op.wgt, op.args);
+            break;
+        default:
+            st = set_smem_attr(k_conv_fwd<16>, op.smem);
+            if (st == PT_OK) k_conv_fwd<16><<<op.grid, 128, op.smem, stream>>>(op.act, op.wgt, op.args);
+            break;
+    }
+    if (st != PT_OK) return st;
+    PT_CUDA_TRY(cudaGetLastError());
+    return PT_OK;
+}
+
+int wgrad_prepare(WgradOp *op, const Act &x, const Act &gy, float *dw, int num_sms, unsigned *err) {
+    if (x.n != gy.n || x.h != gy.h || x.w != gy.w || x.c % 16 || gy.c % 16 || x.c <= 0 || gy.c <= 0) {
+        pt_set_error("conv weight gradient: shapes differ or channels not multiples of 16");
+        return PT_ERR_INVALID;
+    }
+    const int kca = pick_kc(x.c);
+    const Tiling t = tiling_for(x.h, x.w);
+    // output channels per CTA: a multiple of the dy chunk, at most 256
+    int kcb = pick_kc(gy.c);
+    int ntiles = (gy.c + 255) / 256;
+    while (gy.c % (ntiles * kcb) != 0 && kcb > 16) kcb /= 2;
+    while (gy.c % (ntiles * kcb) != 0) ntiles++;
+    const int n_tile = gy.c / ntiles;
+    int st;
+    if ((st = act_map(&op->act, x, kca, t)) != PT_OK) return st;
+    if ((st = act_map(&op->grad, gy, kcb, t)) != PT_OK) return st;
+    WgradArgs &a = op->args;
+    memset(&a, 0, sizeof(a));
+    a.n_img = x.n;
+    a.H = x.h;
+    a.W = x.w;
+    a.tile_w = t.tile_w;
+    a.tile_rows = t.tile_rows;
+    a.tiles_x = t.tiles_x;
+    a.tiles_y = t.tiles_y;
+    a.cin = x.c;
+    a.nchunks_a = x.c / kca;
+    a.cout = gy.c;
+    a.n_tile = n_tile;
+    a.tmem_cols = pow2_cols(n_tile);
+    a.stage_bytes = 128 * 128 * 2 + 256 * n_tile;
+    a.stages = std::max(2, std::min(4, (200 * 1024) / a.stage_bytes));
+    a.total_tiles = x.n * t.tiles_x * t.tiles_y;
+    a.zero_fill = t.tile_w * t.tile_rows < 128 ? 1 : 0;
+    const int m_tiles = (9 * a.nchunks_a * kca + 127) / 128;
+    const int base_ctas = m_tiles * ntiles;
+    int splits = std::max(1, (2 * std::max(num_sms, 1)) / base_ctas);
+    splits = std::min(splits, std::max(1, a.total_tiles / 4));
+    a.tiles_per_split = (a.total_tiles + splits - 1) / splits;
+    splits = (a.total_tiles + a.tiles_per_split - 1) / a.tiles_per_split;
+    a.dw = dw;
+    a.err = err;
+    op->kca = kca;
+    op->kcb = kcb;
+    op->smem = smem_request(a.stages, a.stage_bytes, a.tmem_cols);
+    op->grid = dim3(static_cast<unsigned>(m_tiles), static_cast<unsigned>(ntiles), static_cast<unsigned>(splits));
+    if (op->smem > 220 * 1024) {
+        pt_set_error("conv weight gradient: shared memory request %d too large", op->smem);
+        return PT_ERR_INVALID;
+    }
+    return PT_OK;
+}
+
+template <int KCA, int KCB>
+static int wgrad_go(const WgradOp &op, cudaStream_t stream) {
+    int st = set_smem_attr(k_conv_wgrad<KCA, KCB>, op.smem);
+    if (st != PT_OK) return st;
+    k_conv_wgrad<KCA, KCB><<<op.grid, 128, op.smem, stream>>>(op.act, op.grad, op.args);
+    PT_CUDA_TRY(cudaGetLastError());
+    return PT_OK;
+}
+
+int wgrad_launch(const WgradOp &op, cudaStream_t stream) {
+#define PT_WG(A, B) \
+    if (op.kca == A && op.kcb == B) return wgrad_go<A, B>(op, stream);
+    PT_WG(64, 64) PT_WG(64, 32) PT_WG(64, 16) PT_WG(32, 64) PT_WG(32, 32) PT_WG(32, 16) PT_WG(16, 64) PT_WG(16, 32)
+    PT_WG(16, 16)
+#undef PT_WG
+    pt_set_error("conv weight gradient: unsupported chunk pair %d/%d", op.kca, op.kcb);
+    return PT_ERR_INVALID;
+}
+
+int bias_grad_launch(const Act &g, float *db, cudaStream_t stream) {
+    if (g.c <= 0 || g.c > 512) {
+        pt_set_error("bias gradient: %d channels", g.c);
+        return PT_ERR_INVALID;
+    }
+    const int threads = std::max(g.c, (256 / g.c) * g.c);
+    const long long npix = (long long)g.n * g.h * g.w;
+    const int blocks = static_cast<int>(std::min<long long>(1024, (npix + 63) / 64));
+    k_bias_grad<<<blocks, threads, threads * sizeof(float), stream>>>(static_cast<const uint16_t *>(g.ptr), g.ctot,
+                                                                       g.coff, g.c, npix, db);
+    PT_CUDA_TRY(cudaGetLastError());
+    return PT_OK;
+}
+
+int flip_transpose_launch(const uint16_t *w, int cout, int cin, uint16_t *wt, cudaStream_t stream) {
+    const long long n = 9ll * cout * cin;
+    const int blocks = static_cast<int>(std::min<long long>(4096, (n + 255) / 256));
+    k_flip_transpose<<<blocks, 256, 0, stream>>>(w, cout, cin, wt);
+    PT_CUDA_TRY(cudaGetLastError());
+    return PT_OK;
+}
+
+}  // namespace ptconv

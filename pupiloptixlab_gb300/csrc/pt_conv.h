@@ -1,0 +1,99 @@
+// pt_conv.h -- 3x3 / stride 1 / padding 1 BF16 convolutions of NHWC tensors
+// as implicit GEMMs on the fifth-generation tensor cores (tcgen05.mma with
+// the FP32 accumulator in tensor memory, operands staged by TMA).  Host-side
+// interface used by the denoiser (pt_denoise.cu) and by the C-ABI test entry
+// points (pt_conv3x3_*).
+//
+// Forward:          y[p, co] = epi( sum_{tap, ci} x[p + off(tap), ci] * w[co][tap][ci] + b[co] )
+//                   GEMM M = 128 pixels, N = output channels, K = 9 * cin.
+// Data gradient:    the forward kernel over dy with the flipped, transposed
+//                   weights w'[ci][8 - tap][co] = w[co][tap][ci].
+// Weight gradient:  dw[co][tap][ci] += sum_p x[p + off(tap), ci] * dy[p, co]
+//                   GEMM M = 128 (tap, ci) rows, N = output channels, K = pixels,
+//                   both operands MN-major, split over pixel ranges (FP32 atomics).
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace ptconv {
+
+// Channels [coff, coff + c) of an NHWC bf16 tensor with ctot channels.
+struct Act {
+    void *ptr = nullptr;
+    int n = 0, h = 0, w = 0;
+    int ctot = 0, coff = 0, c = 0;
+};
+
+enum Epilogue : int {
+    EPI_BF16 = 0,       // bf16 out = x + bias, optional ReLU
+    EPI_F32 = 1,        // f32 out = x + bias
+    EPI_BF16_MASK = 2,  // bf16 out = x * (mask > 0)   (data gradient through a ReLU)
+};
+
+struct FwdArgs {
+    int n_img, H, W;
+    int tile_w, tile_rows, tiles_x, tiles_y;
+    int cin, nchunks;     // K = 9 * cin, in chunks of KC channels per tap
+    int n_tile, cout;     // N per CTA; valid output channels
+    int tmem_cols, stages, stage_bytes;
+    int epi, relu;
+    const float *bias;
+    void *out;
+    int out_ctot, out_coff;
+    const uint16_t *mask;
+    int mask_ctot, mask_coff;
+    unsigned *err;
+};
+
+struct WgradArgs {
+    int n_img, H, W;
+    int tile_w, tile_rows, tiles_x, tiles_y;
+    int cin, nchunks_a;   // A rows: (tap, chunk) blocks of KCA channels, 9 * nchunks_a blocks
+    int cout, n_tile;     // N per CTA (a multiple of KCB)
+    int tmem_cols, stages, stage_bytes;
+    int total_tiles, tiles_per_split;
+    int zero_fill;        // pixel tiles smaller than 128: clear the stages once
+    float *dw;            // [cout][9][cin] FP32, accumulated
+    unsigned *err;
+};
+
+struct FwdOp {
+    CUtensorMap act, wgt;
+    FwdArgs args;
+    dim3 grid;
+    int smem = 0, kc = 0;
+};
+
+struct WgradOp {
+    CUtensorMap act, grad;
+    WgradArgs args;
+    dim3 grid;
+    int smem = 0, kca = 0, kcb = 0;
+};
+
+// Largest chunk in {64, 32, 16} channels dividing c (c a multiple of 16).
+int pick_kc(int c);
+
+// Forward (or data-gradient) launch over `in`.  `w` holds rows [w_rows][9][in.c]
+// in bf16 (rows beyond w_rows read as zero); `cout` output channels are
+// written to channels [out_coff, out_coff + cout) of `out` (out_ctot channels,
+// same n/h/w as `in`).  `mask` (EPI_BF16_MASK) is a tensor of the output's shape.
+int fwd_prepare(FwdOp *op, const Act &in, const void *w, int w_rows, int cout, const float *bias, int epi,
+                int relu, void *out, int out_ctot, int out_coff, const Act *mask, unsigned *err);
+int fwd_launch(const FwdOp &op, cudaStream_t stream);
+
+// dw[co][tap][ci] += sum over pixels of x[p + off(tap), ci] * gy[p, co].
+int wgrad_prepare(WgradOp *op, const Act &x, const Act &gy, float *dw, int num_sms, unsigned *err);
+int wgrad_launch(const WgradOp &op, cudaStream_t stream);
+
+// db[c] += sum over pixels of g[p, c].
+int bias_grad_launch(const Act &g, float *db, cudaStream_t stream);
+
+// w'[ci][tap][co] = w[8 - tap ... ] flipped and transposed, bf16, rows padded
+// with zeros: w is [cout][9][cin], w' is [cin][9][cout].
+int flip_transpose_launch(const uint16_t *w, int cout, int cin, uint16_t *wt, cudaStream_t stream);
+
+}  // namespace ptconv

@@ -18,7 +18,7 @@ HEADER = ROOT / "include" / "pt_api.h"
 
 def declared_functions():
     text = HEADER.read_text()
-    return sorted(set(re.findall(r"^\s*int\s+(pt_\w+)\s*\(", text, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|void)\s+(pt_\w+)\s*\(", text, re.M)))
 
 
 def test_header_declares_expected_api():

@@ -1,0 +1,110 @@
+"""The learned denoiser on the GPU against its PyTorch-CPU restatement
+(oracle/denoiser_ref.py): forward output, loss and the gradient of every
+layer, then training and the per-tile fallback of pt_denoise.
+
+Tolerances: the GPU keeps activations and activation gradients in BF16 (the
+CPU restatement rounds activations the same way but keeps FP32 gradients), so
+per-layer weight gradients agree to a relative L2 error of 6e-2 and a cosine
+of 0.995, outputs to a relative L2 error of 2e-2."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def _batch(n, h, w, seed):
+    g = torch.Generator().manual_seed(seed)
+    tgt = torch.rand(n, h, w, 3, generator=g) * 2.0
+    noisy = tgt * torch.exp(0.5 * torch.randn(n, h, w, 3, generator=g))
+    albedo = torch.rand(n, h, w, 3, generator=g)
+    normal = torch.nn.functional.normalize(torch.randn(n, h, w, 3, generator=g), dim=-1)
+    inp = torch.cat([noisy, albedo, normal], dim=-1).to(torch.float16)
+    return inp, tgt
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+
+
+def _cos(a, b):
+    return float(np.dot(a, b) / max(np.linalg.norm(a) * np.linalg.norm(b), 1e-30))
+
+
+@pytest.fixture(scope="module")
+def dn(cuda_ctx):
+    from pupiloptixlab_gb300.denoiser import Denoiser
+    d = Denoiser(cuda_ctx, seed=3)
+    yield d
+    d.close()
+
+
+def test_parameter_count(dn):
+    from oracle import denoiser_ref
+    assert dn.num_params == 1_259_072
+    assert [(c[0], c[1]) for c in dn.layers] == [(l[0], l[1]) for l in denoiser_ref.LAYERS]
+
+
+def test_forward_matches_cpu(dn):
+    from oracle import denoiser_ref
+    inp, _ = _batch(2, 32, 48, 1)
+    out = dn.forward(inp.cuda()).cpu().numpy()
+    ref = denoiser_ref.denoise(dn.get_params(), inp.float().numpy())
+    assert np.isfinite(out).all()
+    assert _rel(out, ref) <= 2e-2
+
+
+def test_gradients_match_cpu(dn):
+    from oracle import denoiser_ref
+    inp, tgt = _batch(2, 32, 32, 2)
+    loss = dn.compute_grads(inp.cuda(), tgt.cuda())
+    g = dn.get_grads()
+    ref_loss, ref_g = denoiser_ref.loss_and_grads(dn.get_params(), inp.float().numpy(), tgt.numpy())
+    assert abs(loss - ref_loss) <= 1e-2 * ref_loss
+    off = 0
+    worst = []
+    for i, (cin, cout, _) in enumerate(denoiser_ref.LAYERS):
+        nw = 9 * cin * cout
+        a, b = g[off:off + nw], ref_g[off:off + nw]
+        worst.append((i, _rel(a, b), _cos(a, b)))
+        ab, bb = g[off + nw:off + nw + cout], ref_g[off + nw:off + nw + cout]
+        if np.linalg.norm(bb) > 0:
+            assert _cos(ab, bb) >= 0.99, (i, "bias")
+        off += nw + cout
+    for i, rel, cos in worst:
+        assert rel <= 6e-2 and cos >= 0.995, worst
+
+
+def test_training_reduces_loss(cuda_ctx):
+    from pupiloptixlab_gb300.denoiser import Denoiser
+    d = Denoiser(cuda_ctx, seed=5, lr=2e-3)
+    inp, tgt = _batch(4, 64, 64, 3)
+    inp, tgt = inp.cuda(), tgt.cuda()
+    d.train_step(inp, tgt)
+    first = d.read_loss()
+    for _ in range(60):
+        d.train_step(inp, tgt)
+    d.read_loss()
+    for _ in range(10):
+        d.train_step(inp, tgt)
+    last = d.read_loss()
+    d.close()
+    assert np.isfinite(first) and np.isfinite(last)
+    assert last < 0.8 * first, (first, last)
+
+
+def test_denoise_frame_and_fallback(cuda_ctx, dn):
+    from pupiloptixlab_gb300 import scenes
+    from pupiloptixlab_gb300.api import GpuScene
+    sc = scenes.cornell_box(72, 40)
+    g = GpuScene(cuda_ctx, sc)
+    buf = g.render(spp=4)
+    out, st, flags = dn.denoise(buf, 72, 40, fallback_sigma=0.0, want_tiles=True)
+    assert st.tiles == 5 * 3 and st.fallback_tiles == 0
+    assert torch.isfinite(out).all() and (out[:, 3] == 1).all()
+    # every tile falls back: the output is the raw colour
+    out2, st2, flags2 = dn.denoise(buf, 72, 40, fallback_rel=0.0, fallback_sigma=1e-12, want_tiles=True)
+    assert st2.fallback_tiles == int(flags2.sum()) >= st2.tiles - 1
+    fb = flags2.view(3, 5).repeat_interleave(16, 0).repeat_interleave(16, 1)[:40, :72].reshape(-1).bool()
+    assert torch.equal(out2[fb, :3], buf["accum"][fb, :3])
+    g.close()
