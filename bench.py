@@ -49,9 +49,20 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="headline", choices=["headline", "dynamic"],
+    ap.add_argument("--workload", default="headline", choices=["headline", "dynamic", "denoise", "batch"],
                     help="headline: the 1M-triangle 1080p frame; dynamic: 4M jittered triangles, rebuild vs refit")
     ap.add_argument("--frames", type=int, default=120, help="frames of the dynamic workload")
+    ap.add_argument("--batch-scenes", type=int, default=64, help="scenes of the multi-scene workload")
+    ap.add_argument("--batch-spp", type=int, default=16)
+    ap.add_argument("--dn-pairs", type=int, default=512, help="denoiser training pairs rendered by the tracer")
+    ap.add_argument("--dn-target-spp", type=int, default=1024, help="spp of the denoiser training targets")
+    ap.add_argument("--dn-steps", type=int, default=20000, help="denoiser training steps")
+    ap.add_argument("--dn-batch", type=int, default=16)
+    ap.add_argument("--dn-crop", type=int, default=256)
+    ap.add_argument("--dn-lr", type=float, default=1e-3)
+    ap.add_argument("--dn-ref-spp", type=int, default=4096, help="spp of the 1080p reference image")
+    ap.add_argument("--dn-train-only", action="store_true",
+                    help="time denoiser training steps on a seeded random batch (no rendering, no evaluation)")
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--spp", type=int, default=64)
@@ -256,6 +267,234 @@ def run_dynamic(args):
     print(json.dumps(line), flush=True)
 
 
+def run_batch(args):
+    """Multi-scene launches: `--batch-scenes` seeded icosphere fields with
+    triangle counts log-uniform in [10k, 2M] and resolutions drawn from
+    {256^2, 512^2, 1024^2, 1280x720}, `--batch-spp` spp at depth 8, rendered
+    (a) one pt_render call per scene, back to back, and (b) one
+    pt_render_batch call; aggregate Msamples/s of both, device-timed."""
+    import numpy as np
+    import torch
+
+    from pupiloptixlab_gb300 import abi, scenes
+    from pupiloptixlab_gb300.api import Context, GpuScene, render_batch, render_batch_stats
+    torch.cuda.set_device(0)
+    ctx = Context(0)
+    pool = scenes.mesh_pool(32)
+    rng = np.random.default_rng(2)
+    res = [(256, 256), (512, 512), (1024, 1024), (1280, 720)]
+    specs = []
+    for k in range(args.batch_scenes):
+        tris = float(np.exp(rng.uniform(np.log(1e4), np.log(2e6))))
+        inst = max(1, int(round((tris - 8192) / 5120)))
+        w, h = res[int(rng.integers(0, len(res)))]
+        specs.append((k, inst, w, h))
+    gs = [GpuScene(ctx, scenes.pooled_field(1000 + k, inst, w, h, args.depth, pool), bvh_width=args.bvh_width,
+                   max_leaf=args.max_leaf) for k, inst, w, h in specs]
+    tris = [g.num_prims()[0] for g in gs]
+    pixels = sum(g.width * g.height for g in gs)
+    samples = pixels * args.batch_spp
+    bufs_serial = [g.alloc_buffers() for g in gs]
+    bufs_batch = [g.alloc_buffers() for g in gs]
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+
+    def serial(seed):
+        a, z = ev(), ev()
+        a.record()
+        for g, b in zip(gs, bufs_serial):
+            g.render(spp=args.batch_spp, seed=seed, max_depth=args.depth, buffers=b)
+        z.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(z)
+
+    def batched(seed):
+        a, z = ev(), ev()
+        a.record()
+        render_batch(ctx, gs, spp=args.batch_spp, seed=seed, max_depth=args.depth, buffers=bufs_batch)
+        z.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(z)
+
+    for i in range(max(1, args.warmup)):
+        serial(i)
+        batched(i)
+    t_serial = [serial(100 + i) for i in range(args.steps)]
+    t_batch = [batched(100 + i) for i in range(args.steps)]
+    same = all(torch.equal(a["accum"], b["accum"]) for a, b in zip(bufs_serial, bufs_batch))
+    st = render_batch_stats(ctx)
+    ms_s, ms_b = statistics.median(t_serial), statistics.median(t_batch)
+    line = {"metric": "multi-scene aggregate Msamples/s (one launch per bounce vs serial renders)", "unit": "Msamples/s",
+            "value": samples / (ms_b * 1e-3) / 1e6, "serial_value": samples / (ms_s * 1e-3) / 1e6,
+            "speedup_vs_serial": ms_s / ms_b, "ms_batch": ms_b, "ms_serial": ms_s, "steps": args.steps,
+            "warmup": args.warmup, "images_identical_to_serial": bool(same), "batch_waves": st.waves,
+            "batch_kernel_launches": st.kernel_launches, "higher_is_better": True,
+            "workload": f"{len(gs)} icosphere fields, {min(tris)}-{max(tris)} triangles (total {sum(tris)}), "
+                        f"{pixels} pixels, {args.batch_spp} spp, depth {args.depth}, BVH{args.bvh_width}",
+            "dtype": "f32", "data": "synthetic (seeded procedural scenes)"}
+    print(json.dumps(line), flush=True)
+
+
+def unet_flops(layers, n: int, h: int, w: int) -> float:
+    """Algorithmic FLOPs of one denoiser training step (forward, data and
+    weight gradients of the 14 convolutions; 2 FLOPs per multiply-add).
+    layers: (cin, cout, offset) per convolution, as pt_denoiser_layer reports."""
+    levels = [0, 0, 1, 1, 2, 2, 3, 3, 4, 3, 2, 1, 0, 0]
+    tot = 0.0
+    for i, ((cin, cout, _), lv) in enumerate(zip(layers, levels)):
+        px = n * (h >> lv) * (w >> lv)
+        f = 2.0 * 9 * cin * cout * px
+        tot += 2 * f if i == 0 else 3 * f  # the first layer needs no data gradient
+    return tot
+
+
+def run_denoise(args):
+    """Learned denoiser: training pairs rendered by the tracer (seeded
+    icosphere-field scenes, random 256^2 views, 4-spp inputs, high-spp
+    targets), Adam training with the library's tcgen05 kernels, then on the
+    1080p headline frame the time to reach RMSE 0.01 against a high-spp
+    reference, plain accumulation vs render + denoise."""
+    import numpy as np
+    import torch
+
+    from pupiloptixlab_gb300 import abi, scenes
+    from pupiloptixlab_gb300.api import Context, GpuScene
+    from pupiloptixlab_gb300.denoise_data import render_pairs
+    from pupiloptixlab_gb300.denoiser import Denoiser
+    torch.cuda.set_device(0)
+    ctx = Context(0)
+    log = lambda m: print(m, file=sys.stderr, flush=True)  # noqa: E731
+    if args.dn_train_only:
+        gen = torch.Generator(device="cuda").manual_seed(0)
+        shape = (args.dn_batch, args.dn_crop, args.dn_crop)
+        inp = torch.rand(*shape, 9, device="cuda", generator=gen).half()
+        tgt = torch.rand(*shape, 3, device="cuda", generator=gen)
+        dn = Denoiser(ctx, lr=args.dn_lr, seed=1)
+        for _ in range(max(args.warmup, 3)):
+            dn.train_step(inp, tgt)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.dn_steps):
+            dn.train_step(inp, tgt)
+        e1.record()
+        torch.cuda.synchronize()
+        step_ms = e0.elapsed_time(e1) / max(args.dn_steps, 1)
+        flops = unet_flops(dn.layers, args.dn_batch, args.dn_crop, args.dn_crop)
+        print(json.dumps({"metric": "denoiser training step", "unit": "ms", "value": step_ms,
+                          "tflops": flops / (step_ms * 1e-3) / 1e12, "steps": args.dn_steps,
+                          "batch": args.dn_batch, "crop": args.dn_crop, "loss": dn.read_loss()}), flush=True)
+        return
+    inputs, targets, data_info = render_pairs(ctx, args.dn_pairs, crop=args.dn_crop, target_spp=args.dn_target_spp,
+                                              noisy_spp=(1, 2, 4, 4, 8, 16, 32, 64), log=log)
+    dn = Denoiser(ctx, lr=args.dn_lr, seed=1)
+    B, P = args.dn_batch, args.dn_pairs
+    nb = P // B
+    batches = [(inputs[i * B:(i + 1) * B], targets[i * B:(i + 1) * B]) for i in range(nb)]
+    for i in range(3):  # warm-up (graph capture)
+        dn.train_step(*batches[i % nb])
+    first_loss = dn.read_loss()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    losses = []
+    e0.record()
+    for k in range(args.dn_steps):
+        dn.train_step(*batches[k % nb])
+        if (k + 1) % 500 == 0:
+            losses.append((k + 1, dn.read_loss()))
+    e1.record()
+    torch.cuda.synchronize()
+    train_ms = e0.elapsed_time(e1)
+    step_ms = train_ms / max(args.dn_steps, 1)
+    flops = unet_flops(dn.layers, B, args.dn_crop, args.dn_crop)
+    pk_file = ROOT / "MEASURED_PEAKS.json"
+    bf16_peak, bf16_src = (float(json.loads(pk_file.read_text())["bf16_tflops_sustained"]), "measured") \
+        if pk_file.exists() else (1700.0, "fallback")
+    tf = flops / (step_ms * 1e-3) / 1e12
+    log(f"denoiser trained: {args.dn_steps} steps, {step_ms:.3f} ms/step, {tf:.1f} TFLOP/s, losses {losses[-3:]}")
+
+    # evaluation on the 1080p headline frame
+    W, H = args.width, args.height
+    sc = scenes.icosphere_field(W, H, args.depth)
+    g = GpuScene(ctx, sc, bvh_width=args.bvh_width, max_leaf=args.max_leaf)
+    flags = abi.RENDER_DROP_NONFINITE
+
+    def timed_render(spp, seed):
+        b = g.alloc_buffers()
+        torch.cuda.synchronize()
+        a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        g.render(spp=spp, seed=seed, flags=flags, buffers=b)
+        z.record()
+        torch.cuda.synchronize()
+        return b, a.elapsed_time(z) * 1e-3
+
+    ref, ref_s = timed_render(args.dn_ref_spp, 1 << 22)
+    R = ref["accum"][:, :3].clone()
+
+    def rmse(x):
+        x = x[:, :3]
+        lin = float((x.clamp(0, 1) - R.clamp(0, 1)).pow(2).mean().sqrt())
+        lg = float((torch.log1p(x.clamp(min=0)) - torch.log1p(R.clamp(min=0))).pow(2).mean().sqrt())
+        return lin, lg
+
+    plain = []
+    for spp in (1, 4, 16, 64, 256, 1024):
+        b, t = timed_render(spp, 0)
+        plain.append({"spp": spp, "s": t, "rmse": rmse(b["accum"])})
+    den = []
+    for spp in (1, 2, 4, 8, 16, 32, 48, 64, 96, 128):
+        b, t = timed_render(spp, 0)
+        dn.denoise(b, W, H)  # warm
+        out, st, _ = dn.denoise(b, W, H)
+        den.append({"spp": spp, "s": t + st.last_ms * 1e-3, "render_s": t, "denoise_ms": st.last_ms,
+                    "rmse": rmse(out), "rmse_input": rmse(b["accum"]), "fallback_tiles": st.fallback_tiles,
+                    "tiles": st.tiles})
+
+    def time_to(curve, k, thr=0.01, model=False):
+        """Denoised: the fastest measured point at or below thr.  Plain
+        accumulation (model=True): its MSE against the reference is
+        a / spp + a / ref_spp; a is fitted at the last point above thr (or the
+        last point), the spp that reaches thr is solved for and timed at the
+        per-spp rate of the nearest measured point above it."""
+        if not model:
+            hits = [c["s"] for c in curve if c["rmse"][k] <= thr]
+            return (min(hits), None) if hits else (None, None)
+        above = [c for c in curve if c["rmse"][k] > thr] or [curve[-1]]
+        fit = above[-1]
+        s, m = fit["spp"], fit["rmse"][k] ** 2
+        a = m * s * args.dn_ref_spp / (args.dn_ref_spp + s)
+        if thr * thr <= a / args.dn_ref_spp:
+            return None, None
+        need = a / (thr * thr - a / args.dn_ref_spp)
+        rate = [c for c in curve if c["spp"] >= need] or [curve[-1]]
+        return rate[0]["s"] / rate[0]["spp"] * need, need
+
+    out = {}
+    for k, name in ((0, "display_clamped"), (1, "log1p")):
+        tp, need = time_to(plain, k, model=True)
+        td, _ = time_to(den, k)
+        out[name] = {"plain_s": tp, "plain_spp_needed": need, "denoised_s": td,
+                     "speedup": (tp / td) if (tp and td) else None}
+    line = {"metric": "denoiser: time-to-RMSE 0.01 at 1080p, render+denoise vs plain accumulation", "unit": "s",
+            "value": out["display_clamped"]["denoised_s"], "higher_is_better": False,
+            "time_to_rmse_0.01": out, "rmse_spaces": {"display_clamped": "RGB clamped to [0,1], linear",
+                                                      "log1p": "log(1 + RGB)"},
+            "reference_image": {"spp": args.dn_ref_spp, "render_s": ref_s},
+            "plain_curve": plain, "denoised_curve": den,
+            "training": {"data": data_info, "steps": args.dn_steps, "batch": B, "crop": args.dn_crop,
+                         "step_ms": step_ms, "flops_per_step": flops, "tflops": tf,
+                         "first_loss": first_loss, "losses": losses},
+            "roofline": {"bound": "tensor", "achieved": tf, "peak": bf16_peak, "peak_source": bf16_src,
+                         "unit": "TFLOP/s", "frac": tf / bf16_peak, "traffic": None,
+                         "note": "whole training step (14 convolutions x forward, data and weight gradients, "
+                                 "pooling, up-sampling, loss, Adam) over its algorithmic convolution FLOPs; "
+                                 "peak = sustained cuBLAS bf16"},
+            "workload": f"U-Net 5 levels 32-256 ch, {dn.num_params} params, batch {B} x {args.dn_crop}^2; "
+                        f"eval on the {W}x{H} icosphere field",
+            "dtype": "bf16 (fp32 accumulate)", "data": "synthetic (rendered by the tracer from seeded scenes)"}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -263,6 +502,12 @@ def main():
         return
     if args.workload == "dynamic":
         run_dynamic(args)
+        return
+    if args.workload == "denoise":
+        run_denoise(args)
+        return
+    if args.workload == "batch":
+        run_batch(args)
         return
     ws, rank, local = dist_env()
     import numpy as np

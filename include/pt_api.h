@@ -226,8 +226,11 @@ enum {
     PT_RENDER_NO_MATERIAL_SORT = 1, /* shade hits in queue order instead of binned by material */
     PT_RENDER_COUNTERS = 2,      /* count node visits and primitive tests */
     PT_RENDER_NO_GRAPH = 4,      /* launch the bounce kernels one by one instead of a CUDA graph */
-    PT_RENDER_KERNEL_TIMING = 8  /* time each traversal / shading launch with CUDA events
+    PT_RENDER_KERNEL_TIMING = 8, /* time each traversal / shading launch with CUDA events
                                     (launches directly, without the CUDA graph) */
+    PT_RENDER_DROP_NONFINITE = 16 /* accumulate a sample whose radiance is NaN or infinite as zero.
+                                     Off by default: the reference's integrator (main.cu:97-101)
+                                     accumulates such samples, which then stay in the pixel. */
 };
 
 /* Caller-owned DEVICE buffers (BufferManager buffers, framework/system/buffer.h:26-63):
@@ -331,6 +334,19 @@ typedef struct pt_tune_result {
     float baseline_msamples_per_s; /* throughput of the configuration the scene had before */
 } pt_tune_result;
 
+/* Multi-scene launch (replaces n PTPass::OnRun frame loops,
+ * example/path_tracer/pt_pass.cpp:39-57, one per scene): renders params->spp
+ * frames of every scene -- each with its own camera, resolution and frame
+ * buffers fbs[k] -- with one launch per kernel per bounce.  The scenes' BVHs
+ * (all of one width) are merged into one node array for the launch, the
+ * path slots of a wave cover every scene's pixels, and the shading queues
+ * are shared and binned by (scene, material type).  Each scene gets the
+ * image pt_render with the same params would give it (same random streams).
+ * max_depth 0 means scene 0's depth.  Statistics: pt_render_batch_get_stats. */
+int pt_render_batch(pt_context *ctx, pt_scene *const *scenes, const pt_render_params *params,
+                    const pt_frame_buffers *fbs, uint32_t n, void *stream);
+int pt_render_batch_get_stats(const pt_context *ctx, pt_render_stats *out);
+
 /* No reference counterpart (the reference has a single OptiX configuration).
  * Times `params` renders on this scene (coordinate search): every
  * combination of BVH width {2, 4, 8} (the BVH is rebuilt) and traversal block
@@ -367,7 +383,8 @@ int pt_bsdf_sample_batch(const float *bsdf, const float *wo, uint32_t *rng_state
  * accumulation; every convolution (forward, data and weight gradient) runs
  * on the tensor cores (tcgen05) with TMA-staged operands.  The network works
  * in the log domain: channels 0-2 of its input are log(1 + colour), its
- * output is log(1 + denoised colour), the loss is L1 on log(1 + x).
+ * output is added to them to give log(1 + denoised colour), the loss is L1
+ * on log(1 + x).
  *
  * Training inputs are 9-channel FP16 pixels (colour RGB, albedo RGB, normal
  * XYZ), targets FP32 RGB, both NHWC and on the device. */

@@ -5,7 +5,8 @@ on the GPU (the reference's OptiX denoiser, framework/optix/denoiser.cpp:171-267
 is a closed model, so the network is this project's own and this module is its
 specification): 14 3x3 convolutions, 2x2 mean pooling, nearest 2x upsampling,
 concatenation [upsampled, skip], ReLU after every hidden convolution, log-domain
-input/output, L1 loss on log(1 + x).  With ``bf16=True`` every stored tensor
+input, output = the input's log colour plus the network's correction, L1 loss on
+log(1 + x).  With ``bf16=True`` every stored tensor
 (network input, weights, activations) is rounded to bfloat16 where the GPU stores
 it, and autograd passes gradients straight through the rounding.
 
@@ -91,7 +92,7 @@ def forward(params: list[tuple[torch.Tensor, torch.Tensor]], inp: torch.Tensor, 
     d1 = rconv(11, torch.cat([up(d2), e1], dim=1))
     d0 = rconv(12, torch.cat([up(d1), e0], dim=1))
     out = conv(13, d0)
-    return out[:, :3]
+    return out[:, :3] + x0[:, :3]  # residual: the network corrects the input's log colour
 
 
 def loss_and_grads(flat: np.ndarray, inp: np.ndarray, target: np.ndarray, bf16: bool = True):

@@ -26,6 +26,7 @@ INST_FLIP_NORMALS, INST_FLIP_TEXCOORDS = 1, 2
 ENV_NONE, ENV_CONST = 0, 1
 RNG_REF_LCG, RNG_PCG32 = 0, 1
 RENDER_NO_MATERIAL_SORT, RENDER_COUNTERS, RENDER_NO_GRAPH, RENDER_KERNEL_TIMING = 1, 2, 4, 8
+RENDER_DROP_NONFINITE = 16
 LOBE_DELTA = (1 << 5) | (1 << 6)
 
 
@@ -143,6 +144,9 @@ PROTOTYPES = [
     ("pt_bvh_get_stats", C.c_int, [C.c_void_p, C.POINTER(BvhStats)]),
     ("pt_render", C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.POINTER(FrameBuffers), C.c_void_p]),
     ("pt_render_get_stats", C.c_int, [C.c_void_p, C.POINTER(RenderStats)]),
+    ("pt_render_batch", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(RenderParams), C.c_void_p, C.c_uint32,
+                                  C.c_void_p]),
+    ("pt_render_batch_get_stats", C.c_int, [C.c_void_p, C.POINTER(RenderStats)]),
     ("pt_render_noalloc", C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.POINTER(FrameBuffers), C.c_void_p]),
     ("pt_autotune", C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.POINTER(FrameBuffers), C.POINTER(TuneResult),
                               C.c_void_p]),

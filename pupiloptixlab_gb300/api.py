@@ -145,6 +145,30 @@ class GpuScene:
         return hits
 
 
+def render_batch(ctx: Context, scenes: list, spp: int, seed: int = 0, sample_cnt: int = 0, accumulate: bool = True,
+                 rng: int = abi.RNG_PCG32, max_depth: int = 0, wave_spp: int = 0, block_size: int = 0, flags: int = 0,
+                 buffers: list | None = None, stream=None) -> list:
+    """pt_render_batch: every GpuScene of `scenes` rendered in one launch per
+    bounce; returns one buffer dict per scene."""
+    lib = ctx.lib
+    bufs = buffers if buffers is not None else [g.alloc_buffers() for g in scenes]
+    handles = (C.c_void_p * len(scenes))(*[g.handle.value if isinstance(g.handle, C.c_void_p) else g.handle
+                                            for g in scenes])
+    fbs = (abi.FrameBuffers * len(scenes))(*[
+        abi.FrameBuffers(*[b[k].data_ptr() if k in b else None for k in ("accum", "frame", "albedo", "normal", "test")])
+        for b in bufs])
+    p = abi.RenderParams(spp, max_depth, seed, sample_cnt, 1 if accumulate else 0, rng, wave_spp, block_size, flags)
+    abi.check(lib.pt_render_batch(ctx.handle, C.cast(handles, C.c_void_p), C.byref(p), C.cast(fbs, C.c_void_p),
+                                  len(scenes), _stream_ptr(stream)), "pt_render_batch", lib)
+    return bufs
+
+
+def render_batch_stats(ctx: Context) -> abi.RenderStats:
+    st = abi.RenderStats()
+    abi.check(ctx.lib.pt_render_batch_get_stats(ctx.handle, C.byref(st)), "pt_render_batch_get_stats", ctx.lib)
+    return st
+
+
 def bsdf_eval(bsdf: torch.Tensor, wo: torch.Tensor, wi: torch.Tensor):
     lib = abi.load()
     n = bsdf.shape[0]

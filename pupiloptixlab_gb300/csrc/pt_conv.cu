@@ -34,6 +34,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -165,6 +166,65 @@ __device__ __forceinline__ uint16_t f2bf(float f) {
     return *reinterpret_cast<uint16_t *>(&h);
 }
 
+// Forward epilogue: accumulator row `tid` = pixel (x0 + tid % tile_w,
+// y0 + tid / tile_w); warp w reads TMEM lanes 32w..32w+31, 16 columns at a time.
+__device__ __forceinline__ void fwd_epilogue(const FwdArgs &a, uint32_t tmem, int tid, int warp, int img, int x0, int y0,
+                                             int n0, bool ok) {
+    const int px = tid % a.tile_w, py = tid / a.tile_w;
+    const int x = x0 + px, y = y0 + py;
+    const bool valid = ok && py < a.tile_rows && x < a.W && y < a.H;
+    const size_t pix = ((size_t)img * a.H + (valid ? y : 0)) * a.W + (valid ? x : 0);
+    const uint32_t trow = tmem + (static_cast<uint32_t>(warp * 32) << 16);
+    for (int c = 0; c < a.n_tile; c += 16) {
+        float v[16];
+        tmem_ld16(trow + c, v);
+        const int ch0 = n0 + c;
+        if (!valid || ch0 >= a.cout) continue;
+        const int nvalid = min(16, a.cout - ch0);
+        if (a.epi == EPI_F32) {
+            float *o = static_cast<float *>(a.out) + pix * a.out_ctot + a.out_coff + ch0;
+            for (int i = 0; i < nvalid; i++) o[i] = v[i] + (a.bias ? a.bias[ch0 + i] : 0.f);
+            continue;
+        }
+        if (a.epi == EPI_BF16) {
+#pragma unroll
+            for (int i = 0; i < 16; i++) {
+                float f = v[i] + ((a.bias && i < nvalid) ? a.bias[ch0 + i] : 0.f);
+                v[i] = a.relu ? fmaxf(f, 0.f) : f;
+            }
+        } else {
+            const uint16_t *m = a.mask + pix * a.mask_ctot + a.mask_coff + ch0;
+            if (nvalid == 16) {
+                uint4 q0 = *reinterpret_cast<const uint4 *>(m), q1 = *reinterpret_cast<const uint4 *>(m + 8);
+                const uint16_t *h0 = reinterpret_cast<const uint16_t *>(&q0), *h1 = reinterpret_cast<const uint16_t *>(&q1);
+#pragma unroll
+                for (int i = 0; i < 8; i++) {
+                    if (!(h0[i] != 0 && (h0[i] & 0x8000u) == 0)) v[i] = 0.f;
+                    if (!(h1[i] != 0 && (h1[i] & 0x8000u) == 0)) v[i + 8] = 0.f;
+                }
+            } else {
+                for (int i = 0; i < nvalid; i++)
+                    if (!(m[i] != 0 && (m[i] & 0x8000u) == 0)) v[i] = 0.f;
+            }
+        }
+        uint16_t *o = static_cast<uint16_t *>(a.out) + pix * a.out_ctot + a.out_coff + ch0;
+        if (nvalid == 16) {
+            uint4 q0, q1;
+            uint32_t *w0 = reinterpret_cast<uint32_t *>(&q0), *w1 = reinterpret_cast<uint32_t *>(&q1);
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                w0[i] = f2bf(v[2 * i]) | (static_cast<uint32_t>(f2bf(v[2 * i + 1])) << 16);
+                w1[i] = f2bf(v[8 + 2 * i]) | (static_cast<uint32_t>(f2bf(v[8 + 2 * i + 1])) << 16);
+            }
+            reinterpret_cast<uint4 *>(o)[0] = q0;
+            reinterpret_cast<uint4 *>(o)[1] = q1;
+        } else {
+            for (int i = 0; i < nvalid; i++) o[i] = f2bf(v[i]);
+        }
+    }
+
+}
+
 // ---------------------------------------------------------------------------
 // forward / data-gradient kernel
 // ---------------------------------------------------------------------------
@@ -256,63 +316,132 @@ __global__ void __launch_bounds__(128, 1)
     if (!ok && tid == 0) record_error(a.err, 4u);
     tc_fence_after();
 
-    // epilogue: accumulator row `tid` = pixel (x0 + tid % tile_w, y0 + tid / tile_w)
-    const int px = tid % a.tile_w, py = tid / a.tile_w;
-    const int x = x0 + px, y = y0 + py;
-    const bool valid = ok && py < a.tile_rows && x < a.W && y < a.H;
-    const size_t pix = ((size_t)img * a.H + (valid ? y : 0)) * a.W + (valid ? x : 0);
-    const uint32_t trow = tmem + (static_cast<uint32_t>(warp * 32) << 16);
-    for (int c = 0; c < a.n_tile; c += 16) {
-        float v[16];
-        tmem_ld16(trow + c, v);
-        const int ch0 = n0 + c;
-        if (!valid || ch0 >= a.cout) continue;
-        const int nvalid = min(16, a.cout - ch0);
-        if (a.epi == EPI_F32) {
-            float *o = static_cast<float *>(a.out) + pix * a.out_ctot + a.out_coff + ch0;
-            for (int i = 0; i < nvalid; i++) o[i] = v[i] + (a.bias ? a.bias[ch0 + i] : 0.f);
-            continue;
-        }
-        if (a.epi == EPI_BF16) {
-#pragma unroll
-            for (int i = 0; i < 16; i++) {
-                float f = v[i] + ((a.bias && i < nvalid) ? a.bias[ch0 + i] : 0.f);
-                v[i] = a.relu ? fmaxf(f, 0.f) : f;
-            }
-        } else {
-            const uint16_t *m = a.mask + pix * a.mask_ctot + a.mask_coff + ch0;
-            if (nvalid == 16) {
-                uint4 q0 = *reinterpret_cast<const uint4 *>(m), q1 = *reinterpret_cast<const uint4 *>(m + 8);
-                const uint16_t *h0 = reinterpret_cast<const uint16_t *>(&q0), *h1 = reinterpret_cast<const uint16_t *>(&q1);
-#pragma unroll
-                for (int i = 0; i < 8; i++) {
-                    if (!(h0[i] != 0 && (h0[i] & 0x8000u) == 0)) v[i] = 0.f;
-                    if (!(h1[i] != 0 && (h1[i] & 0x8000u) == 0)) v[i + 8] = 0.f;
-                }
-            } else {
-                for (int i = 0; i < nvalid; i++)
-                    if (!(m[i] != 0 && (m[i] & 0x8000u) == 0)) v[i] = 0.f;
-            }
-        }
-        uint16_t *o = static_cast<uint16_t *>(a.out) + pix * a.out_ctot + a.out_coff + ch0;
-        if (nvalid == 16) {
-            uint4 q0, q1;
-            uint32_t *w0 = reinterpret_cast<uint32_t *>(&q0), *w1 = reinterpret_cast<uint32_t *>(&q1);
-#pragma unroll
-            for (int i = 0; i < 4; i++) {
-                w0[i] = f2bf(v[2 * i]) | (static_cast<uint32_t>(f2bf(v[2 * i + 1])) << 16);
-                w1[i] = f2bf(v[8 + 2 * i]) | (static_cast<uint32_t>(f2bf(v[8 + 2 * i + 1])) << 16);
-            }
-            reinterpret_cast<uint4 *>(o)[0] = q0;
-            reinterpret_cast<uint4 *>(o)[1] = q1;
-        } else {
-            for (int i = 0; i < nvalid; i++) o[i] = f2bf(v[i]);
-        }
-    }
+    fwd_epilogue(a, tmem, tid, warp, img, x0, y0, n0, ok);
 
     tc_fence_before();
     __syncthreads();
     if (tid == 0 && s_fail) {  // let copies that were issued but never consumed land
+        for (int k = s_consumed; k < s_issued; k++) (void)mbar_wait(full(k % S), (k / S) & 1);
+    }
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, a.tmem_cols);
+}
+
+// ---------------------------------------------------------------------------
+// forward / data-gradient kernel for images at least 128 pixels wide
+// ---------------------------------------------------------------------------
+// The pixel tile is a 128-pixel row segment.  Per 16-channel chunk one TMA box
+// brings its 3 x 130-pixel neighbourhood (the segment and a one-pixel border,
+// zero outside the image) into the non-swizzled K-major layout: two planes of
+// 8 channels, 16 bytes per pixel, pixels in row-major order.  The A operand of
+// tap (dy, dx) is the same planes read from row dy * 130 + dx on (leading
+// byte offset = plane size between the two 8-channel groups, stride byte
+// offset = 128 B between 8-row groups), so the input is read from L2 once per
+// chunk instead of once per tap.  B holds the chunk's weights for all nine
+// taps (32-byte swizzle, one TMA box per tap).
+constexpr int kHaloW = 130, kHaloRows = 3;
+constexpr int kHaloBoxBytes = kHaloW * kHaloRows * 16;       // one 8-channel plane as TMA writes it
+constexpr int kHaloPlaneBytes = (kHaloBoxBytes + 1023) / 1024 * 1024;  // plane stride: TMA destinations 1 KiB-aligned
+__host__ __device__ constexpr int halo_b_tap_bytes(int n_tile) { return (n_tile * 32 + 1023) / 1024 * 1024; }
+
+__global__ void __launch_bounds__(128, 1)
+    k_conv_fwd_halo(const __grid_constant__ CUtensorMap act, const __grid_constant__ CUtensorMap wgt, const FwdArgs a) {
+    constexpr int R = 32;  // B rows: 16 channels
+    constexpr uint32_t SWZB = swz_mode<16>();
+    extern __shared__ uint8_t smem_raw[];
+    __shared__ __align__(8) uint64_t bars[2 * kMaxStages + 1];
+    __shared__ uint32_t tmem_slot;
+    __shared__ int s_issued, s_consumed, s_fail;
+
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
+    const int S = a.stages;
+    const int a_bytes = a.halo_a_bytes;
+    const int b_tap = halo_b_tap_bytes(a.n_tile);  // region stride of one tap's weights
+    const uint32_t tx_bytes = static_cast<uint32_t>(2 * kHaloBoxBytes + 9 * a.n_tile * R);
+    const int tiles_img = a.tiles_x * a.tiles_y;
+    const int img = blockIdx.x / tiles_img, t = blockIdx.x - img * tiles_img;
+    const int x0 = (t % a.tiles_x) * 128, y0 = t / a.tiles_x;
+    const int n0 = blockIdx.y * a.n_tile;
+    const int nk = a.nchunks;
+    const uint32_t bar0 = smem_u32(bars);
+    auto full = [&](int s) { return bar0 + 8u * s; };
+    auto empty = [&](int s) { return bar0 + 8u * (kMaxStages + s); };
+    const uint32_t done = bar0 + 8u * (2 * kMaxStages);
+
+    if (warp == 0) tmem_alloc(smem_u32(&tmem_slot), a.tmem_cols);
+    if (tid == 32) {
+        for (int s = 0; s < S; s++) {
+            mbar_init(full(s), 1);
+            mbar_init(empty(s), 1);
+        }
+        mbar_init(done, 1);
+        mbar_fence_init();
+        s_issued = 0;
+        s_consumed = 0;
+        s_fail = 0;
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_slot;
+
+    if (tid == 0) {
+        int k = 0;
+        for (; k < nk; k++) {
+            const int s = k % S;
+            if (k >= S && !mbar_wait(empty(s), ((k / S) - 1) & 1)) {
+                record_error(a.err, 1u);
+                s_fail = 1;
+                break;
+            }
+            if (*reinterpret_cast<volatile int *>(&s_fail)) break;
+            const uint32_t sa = base + s * a.stage_bytes, sb = sa + a_bytes;
+            if (((sa | sb | static_cast<uint32_t>(kHaloPlaneBytes) | static_cast<uint32_t>(b_tap)) & 1023u) != 0) {
+                record_error(a.err, 8u);  // a TMA destination off its 1 KiB boundary: issue nothing
+                s_fail = 1;
+                break;
+            }
+            mbar_expect_tx(full(s), tx_bytes);
+            tma_load_4d(sa, &act, full(s), k * 16, x0 - 1, y0 - 1, img);
+            tma_load_4d(sa + kHaloPlaneBytes, &act, full(s), k * 16 + 8, x0 - 1, y0 - 1, img);
+            for (int tap = 0; tap < 9; tap++) tma_load_2d(sb + tap * b_tap, &wgt, full(s), tap * a.cin + k * 16, n0);
+        }
+        s_issued = k;
+    } else if (tid == 32) {
+        const uint32_t idesc = idesc_bf16(128, a.n_tile, false, false);
+        int k = 0;
+        for (; k < nk; k++) {
+            const int s = k % S;
+            if (!mbar_wait(full(s), (k / S) & 1)) {
+                record_error(a.err, 2u);
+                s_fail = 1;
+                break;
+            }
+            tc_fence_after();
+            const uint32_t sa = base + s * a.stage_bytes, sb = sa + a_bytes;
+#pragma unroll
+            for (int tap = 0; tap < 9; tap++) {
+                const int dy = tap / 3, dx = tap - 3 * (tap / 3);
+                const uint64_t da = sdesc(sa + 16u * (dy * kHaloW + dx), kHaloPlaneBytes, 128u, 0u);
+                const uint64_t db = sdesc(sb + tap * b_tap, 16u, 8u * R, SWZB);
+                umma_bf16(tmem, da, db, idesc, (k | tap) != 0 ? 1u : 0u);
+            }
+            umma_commit(empty(s));
+        }
+        s_consumed = k;
+        umma_commit(done);
+    }
+    __syncwarp();
+    const bool ok = mbar_wait(done, 0, true);
+    if (!ok && tid == 0) record_error(a.err, 4u);
+    tc_fence_after();
+
+    fwd_epilogue(a, tmem, tid, warp, img, x0, y0, n0, ok);
+
+    tc_fence_before();
+    __syncthreads();
+    if (tid == 0 && s_fail) {
         for (int k = s_consumed; k < s_issued; k++) (void)mbar_wait(full(k % S), (k / S) & 1);
     }
     __syncthreads();
@@ -523,7 +652,7 @@ Tiling tiling_for(int h, int w) {
     return t;
 }
 
-int act_map(CUtensorMap *m, const Act &a, int kc, const Tiling &t) {
+int act_map_box(CUtensorMap *m, const Act &a, int box_c, int box_w, int box_h, CUtensorMapSwizzle swz, int kc) {
     auto fn = encode_fn();
     if (!fn) {
         pt_set_error("cuTensorMapEncodeTiled is not available from the driver");
@@ -537,16 +666,21 @@ int act_map(CUtensorMap *m, const Act &a, int kc, const Tiling &t) {
     }
     cuuint64_t dims[4] = {(cuuint64_t)a.c, (cuuint64_t)a.w, (cuuint64_t)a.h, (cuuint64_t)a.n};
     cuuint64_t strides[3] = {2ull * a.ctot, 2ull * a.ctot * a.w, 2ull * a.ctot * a.w * a.h};
-    cuuint32_t box[4] = {(cuuint32_t)kc, (cuuint32_t)t.tile_w, (cuuint32_t)t.tile_rows, 1};
+    cuuint32_t box[4] = {(cuuint32_t)box_c, (cuuint32_t)box_w, (cuuint32_t)box_h, 1};
     cuuint32_t es[4] = {1, 1, 1, 1};
     CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, p, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                    swizzle_for(kc), CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                    swz, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) {
-        pt_set_error("cuTensorMapEncodeTiled (activation %dx%dx%dx%d, box %d) failed: %d", a.n, a.h, a.w, a.c, kc,
-                     static_cast<int>(r));
+        pt_set_error("cuTensorMapEncodeTiled (activation %dx%dx%dx%d, box %dx%dx%d) failed: %d", a.n, a.h, a.w, a.c,
+                     box_c, box_w, box_h, static_cast<int>(r));
         return PT_ERR_CUDA;
     }
     return PT_OK;
+}
+
+// Tile boxes: kc channels x the pixel tile, swizzled to the row width.
+int act_map(CUtensorMap *m, const Act &a, int kc, const Tiling &t) {
+    return act_map_box(m, a, kc, t.tile_w, t.tile_rows, swizzle_for(kc), kc);
 }
 
 int wgt_map(CUtensorMap *m, const void *w, int kdim, int rows, int kc, int n_tile) {
@@ -572,6 +706,11 @@ int wgt_map(CUtensorMap *m, const void *w, int kdim, int rows, int kc, int n_til
         return PT_ERR_CUDA;
     }
     return PT_OK;
+}
+
+bool getenv_flag(const char *name) {
+    const char *v = getenv(name);
+    return v && *v && *v != '0';
 }
 
 int pow2_cols(int n) {
@@ -627,14 +766,19 @@ int fwd_prepare(FwdOp *op, const Act &in, const void *w, int w_rows, int cout, c
         pt_set_error("conv forward: bf16 output channel stride/offset must be multiples of 8");
         return PT_ERR_INVALID;
     }
-    const int kc = pick_kc(in.c);
+    const bool halo = in.w >= 128 && !getenv_flag("PT_CONV_NO_HALO");
+    const int kc = halo ? 16 : pick_kc(in.c);
     const Tiling t = tiling_for(in.h, in.w);
     const int cout_pad = (cout + 15) / 16 * 16;
     int ntiles = (cout_pad + 255) / 256;
     int n_tile = ((cout_pad / ntiles) + 15) / 16 * 16;
     ntiles = (cout_pad + n_tile - 1) / n_tile;
     int st;
-    if ((st = act_map(&op->act, in, kc, t)) != PT_OK) return st;
+    if (halo) {
+        if ((st = act_map_box(&op->act, in, 8, kHaloW, kHaloRows, CU_TENSOR_MAP_SWIZZLE_NONE, 8)) != PT_OK) return st;
+    } else if ((st = act_map(&op->act, in, kc, t)) != PT_OK) {
+        return st;
+    }
     if ((st = wgt_map(&op->wgt, w, 9 * in.c, w_rows, kc, n_tile)) != PT_OK) return st;
     FwdArgs &a = op->args;
     memset(&a, 0, sizeof(a));
@@ -650,10 +794,18 @@ int fwd_prepare(FwdOp *op, const Act &in, const void *w, int w_rows, int cout, c
     a.n_tile = n_tile;
     a.cout = cout;
     a.tmem_cols = pow2_cols(n_tile);
-    a.stage_bytes = (128 * 2 * kc + n_tile * 2 * kc + 1023) / 1024 * 1024;
+    a.halo_a_bytes = 2 * kHaloPlaneBytes;
+    a.stage_bytes = halo ? a.halo_a_bytes + 9 * halo_b_tap_bytes(n_tile)
+                         : (128 * 2 * kc + n_tile * 2 * kc + 1023) / 1024 * 1024;
     const int target_ctas = std::min(512 / a.tmem_cols, 3);
     const int budget = (225 * 1024) / target_ctas - 2048;
     a.stages = std::max(2, std::min(6, budget / a.stage_bytes));
+    if (halo) {
+        a.tile_w = 128;
+        a.tile_rows = 1;
+        a.tiles_x = (in.w + 127) / 128;
+        a.tiles_y = in.h;
+    }
     a.epi = epi;
     a.relu = relu;
     a.bias = bias;
@@ -667,8 +819,9 @@ int fwd_prepare(FwdOp *op, const Act &in, const void *w, int w_rows, int cout, c
     }
     a.err = err;
     op->kc = kc;
+    op->halo = halo;
     op->smem = smem_request(a.stages, a.stage_bytes, a.tmem_cols);
-    op->grid = dim3(static_cast<unsigned>(in.n * t.tiles_x * t.tiles_y), static_cast<unsigned>(ntiles), 1);
+    op->grid = dim3(static_cast<unsigned>(in.n * a.tiles_x * a.tiles_y), static_cast<unsigned>(ntiles), 1);
     if (op->smem > 220 * 1024) {
         pt_set_error("conv forward: shared memory request %d too large", op->smem);
         return PT_ERR_INVALID;
@@ -678,6 +831,13 @@ int fwd_prepare(FwdOp *op, const Act &in, const void *w, int w_rows, int cout, c
 
 int fwd_launch(const FwdOp &op, cudaStream_t stream) {
     int st = PT_OK;
+    if (op.halo) {
+        st = set_smem_attr(k_conv_fwd_halo, op.smem);
+        if (st != PT_OK) return st;
+        k_conv_fwd_halo<<<op.grid, 128, op.smem, stream>>>(op.act, op.wgt, op.args);
+        PT_CUDA_TRY(cudaGetLastError());
+        return PT_OK;
+    }
     switch (op.kc) {
         case 64:
             st = set_smem_attr(k_conv_fwd<64>, op.smem);
@@ -733,7 +893,10 @@ int wgrad_prepare(WgradOp *op, const Act &x, const Act &gy, float *dw, int num_s
     a.zero_fill = t.tile_w * t.tile_rows < 128 ? 1 : 0;
     const int m_tiles = (9 * a.nchunks_a * kca + 127) / 128;
     const int base_ctas = m_tiles * ntiles;
-    int splits = std::max(1, (2 * std::max(num_sms, 1)) / base_ctas);
+    op->smem = smem_request(a.stages, a.stage_bytes, a.tmem_cols);
+    // split the pixel tiles so that the grid is one full wave of resident CTAs
+    const int per_sm = std::max(1, std::min((228 * 1024) / (op->smem + 1024), 512 / a.tmem_cols));
+    int splits = std::max(1, (per_sm * std::max(num_sms, 1)) / base_ctas);
     splits = std::min(splits, std::max(1, a.total_tiles / 4));
     a.tiles_per_split = (a.total_tiles + splits - 1) / splits;
     splits = (a.total_tiles + a.tiles_per_split - 1) / a.tiles_per_split;
@@ -741,7 +904,6 @@ int wgrad_prepare(WgradOp *op, const Act &x, const Act &gy, float *dw, int num_s
     a.err = err;
     op->kca = kca;
     op->kcb = kcb;
-    op->smem = smem_request(a.stages, a.stage_bytes, a.tmem_cols);
     op->grid = dim3(static_cast<unsigned>(m_tiles), static_cast<unsigned>(ntiles), static_cast<unsigned>(splits));
     if (op->smem > 220 * 1024) {
         pt_set_error("conv weight gradient: shared memory request %d too large", op->smem);

@@ -39,6 +39,7 @@ struct FwdArgs {
     int cin, nchunks;     // K = 9 * cin, in chunks of KC channels per tap
     int n_tile, cout;     // N per CTA; valid output channels
     int tmem_cols, stages, stage_bytes;
+    int halo_a_bytes;     // halo kernel: bytes of the A planes at the start of a stage
     int epi, relu;
     const float *bias;
     void *out;
@@ -65,6 +66,7 @@ struct FwdOp {
     FwdArgs args;
     dim3 grid;
     int smem = 0, kc = 0;
+    bool halo = false;  // k_conv_fwd_halo (width >= 128) instead of k_conv_fwd<kc>
 };
 
 struct WgradOp {
@@ -77,7 +79,10 @@ struct WgradOp {
 // Largest chunk in {64, 32, 16} channels dividing c (c a multiple of 16).
 int pick_kc(int c);
 
-// Forward (or data-gradient) launch over `in`.  `w` holds rows [w_rows][9][in.c]
+// Forward (or data-gradient) launch over `in`.  Images at least 128 pixels
+// wide use the halo kernel (one input load per 16-channel chunk for all nine
+// taps); the environment variable PT_CONV_NO_HALO=1 selects the per-tap kernel
+// for every width, for comparison runs.  `w` holds rows [w_rows][9][in.c]
 // in bf16 (rows beyond w_rows read as zero); `cout` output channels are
 // written to channels [out_coff, out_coff + cout) of `out` (out_ctot channels,
 // same n/h/w as `in`).  `mask` (EPI_BF16_MASK) is a tensor of the output's shape.

@@ -19,6 +19,8 @@
 //   L0  d0 80->32, out 32->3 (16 computed, FP32, no ReLU)
 // All hidden convolutions are followed by ReLU; pooling is the 2x2 mean.
 // Input channels: log(1 + max(rgb, 0)), albedo, normal, 7 zero channels.
+// Output: a log-domain correction; the denoised colour is
+// expm1(output + log(1 + max(rgb, 0))).
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -215,17 +217,18 @@ __global__ void k_skip_back(const uint16_t *cat, const uint16_t *gcat, int cat_c
     }
 }
 
-// L1 loss on log(1 + x): out holds the network's log-domain prediction.
-// g_out (16 channels) = sign(out - log1p(target)) / count; loss_sum += sum |.|.
-__global__ void k_loss(const float *out, const float *target, long long npix, float inv_count, uint16_t *gout,
-                       float *loss_sum) {
+// L1 loss on log(1 + x).  The prediction is the network's output plus the
+// input's log colour (x0 channels 0-2): the network learns a correction.
+// g_out (16 channels) = sign(prediction - log1p(target)) / count; loss_sum += sum |.|.
+__global__ void k_loss(const float *out, const uint16_t *x0, const float *target, long long npix, float inv_count,
+                       uint16_t *gout, float *loss_sum) {
     float acc = 0.f;
     for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npix; p += (long long)gridDim.x * blockDim.x) {
         uint16_t o[16];
 #pragma unroll
         for (int c = 0; c < 16; c++) o[c] = 0;
         for (int c = 0; c < kOutChannels; c++) {
-            const float d = out[p * 3 + c] - log1pf(fmaxf(target[p * 3 + c], 0.f));
+            const float d = out[p * 3 + c] + bf2f(x0[p * 16 + c]) - log1pf(fmaxf(target[p * 3 + c], 0.f));
             acc += fabsf(d);
             o[c] = f2bf(d > 0.f ? inv_count : d < 0.f ? -inv_count : 0.f);
         }
@@ -282,32 +285,40 @@ __global__ void k_weights_to_bf16(const float *p, long long nw, int cout, int ci
     }
 }
 
-// network output (log domain, [n][h][w][3] over the padded frame) -> colour
-__global__ void k_expm1(const float *o, long long n, float *out) {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        out[i] = fmaxf(expm1f(o[i]), 0.f);
+// network output + input log colour -> linear colour, [n][h][w][3]
+__global__ void k_expm1(const float *o, const uint16_t *x0, long long npix, float *out) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npix * 3;
+         i += (long long)gridDim.x * blockDim.x)
+        out[i] = fmaxf(expm1f(o[i] + bf2f(x0[(i / 3) * 16 + i % 3])), 0.f);
 }
 
 __device__ __forceinline__ float lum(float r, float g, float b) { return 0.2126f * r + 0.7152f * g + 0.0722f * b; }
 
+// linear colour of padded-frame pixel q: expm1(network output + input log colour)
+__device__ __forceinline__ float3 denoised(const float *o, const uint16_t *x0, long long q) {
+    return make_float3(fmaxf(expm1f(o[q * 3] + bf2f(x0[q * 16])), 0.f),
+                       fmaxf(expm1f(o[q * 3 + 1] + bf2f(x0[q * 16 + 1])), 0.f),
+                       fmaxf(expm1f(o[q * 3 + 2] + bf2f(x0[q * 16 + 2])), 0.f));
+}
+
 // One block per tile: mean luminance of the raw and the denoised colour and
 // the raw colour's standard error; write the tile's pixels, falling back to
 // the raw colour where the denoised mean moved by more than the threshold.
-__global__ void k_denoise_out(const float4 *color, const float *o, int w, int h, int wp, int tile, float rel, float sig,
-                              float4 *out, uint8_t *tile_flag, unsigned *fallback_count) {
+__global__ void k_denoise_out(const float4 *color, const float *o, const uint16_t *xin, int w, int h, int wp, int tile,
+                              float rel, float sig, float4 *out, uint8_t *tile_flag, unsigned *fallback_count) {
     const int tiles_x = (w + tile - 1) / tile;
     const int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
-    const int x0 = tx * tile, y0 = ty * tile;
-    const int tw = min(tile, w - x0), th = min(tile, h - y0);
+    const int tx0 = tx * tile, ty0 = ty * tile;
+    const int tw = min(tile, w - tx0), th = min(tile, h - ty0);
     float s_raw = 0.f, s_raw2 = 0.f, s_den = 0.f;
     for (int i = threadIdx.x; i < tw * th; i += blockDim.x) {
-        const int x = x0 + i % tw, y = y0 + i / tw;
+        const int x = tx0 + i % tw, y = ty0 + i / tw;
         const float4 c = color[(long long)y * w + x];
-        const float *d = o + ((long long)y * wp + x) * 3;
+        const float3 dc = denoised(o, xin, (long long)y * wp + x);
         const float lr = lum(c.x, c.y, c.z);
         s_raw += lr;
         s_raw2 += lr * lr;
-        s_den += lum(fmaxf(expm1f(d[0]), 0.f), fmaxf(expm1f(d[1]), 0.f), fmaxf(expm1f(d[2]), 0.f));
+        s_den += lum(dc.x, dc.y, dc.z);
     }
     __shared__ float red[3][32];
     for (int off = 16; off > 0; off >>= 1) {
@@ -339,14 +350,14 @@ __global__ void k_denoise_out(const float4 *color, const float *o, int w, int h,
     }
     __syncthreads();
     for (int i = threadIdx.x; i < tw * th; i += blockDim.x) {
-        const int x = x0 + i % tw, y = y0 + i / tw;
+        const int x = tx0 + i % tw, y = ty0 + i / tw;
         const long long q = (long long)y * w + x;
         if (fallback) {
             const float4 c = color[q];
             out[q] = make_float4(c.x, c.y, c.z, 1.f);
         } else {
-            const float *d = o + ((long long)y * wp + x) * 3;
-            out[q] = make_float4(fmaxf(expm1f(d[0]), 0.f), fmaxf(expm1f(d[1]), 0.f), fmaxf(expm1f(d[2]), 0.f), 1.f);
+            const float3 dc = denoised(o, xin, (long long)y * wp + x);
+            out[q] = make_float4(dc.x, dc.y, dc.z, 1.f);
         }
     }
 }
@@ -565,8 +576,8 @@ int run_backward(pt_denoiser *dn, Plan &P, const float *target, cudaStream_t s) 
     const int n = P.n, h = P.h, w = P.w;
     const long long npix = (long long)n * h * w;
     PT_CUDA_TRY(cudaMemsetAsync(dn->grads.ptr, 0, dn->nparams * sizeof(float), s));
-    k_loss<<<grid_for(npix), 256, 0, s>>>(P.out.as<float>(), target, npix, 1.f / (3.f * npix), P.g_out.as<uint16_t>(),
-                                          dn->loss.as<float>());
+    k_loss<<<grid_for(npix), 256, 0, s>>>(P.out.as<float>(), P.x0.as<uint16_t>(), target, npix, 1.f / (3.f * npix),
+                                          P.g_out.as<uint16_t>(), dn->loss.as<float>());
     auto layer = [&](int l) -> int {
         PT_TRY(ptconv::wgrad_launch(P.wg[l], s));
         PT_TRY(ptconv::bias_grad_launch(P.g_of[l], dn->grads.as<float>() + dn->b_off[l], s));
@@ -678,7 +689,9 @@ void init_params(pt_denoiser *dn, std::vector<float> &p) {
         const LayerSpec &L = kSpec[l];
         const int cin_used = l == E0A ? 9 : L.cin;
         const int cout_used = l == OUT ? kOutChannels : L.cout;
-        const double bound = std::sqrt((L.relu ? 6.0 : 3.0) / (9.0 * cin_used));  // He-uniform
+        // He-uniform; the output layer starts at zero so that the network
+        // starts as the identity on the noisy colour (residual output)
+        const double bound = l == OUT ? 0.0 : std::sqrt(6.0 / (9.0 * cin_used));
         for (int co = 0; co < L.cout; co++)
             for (int t = 0; t < 9; t++)
                 for (int ci = 0; ci < L.cin; ci++) {
@@ -934,7 +947,7 @@ int pt_denoiser_forward(pt_denoiser *dn, const void *input_f16, uint32_t n, uint
     const long long npix = (long long)n * height * width;
     k_pack_input<<<grid_for(npix), 256, 0, s>>>(static_cast<const __half *>(input_f16), npix, P.x0.as<uint16_t>());
     PT_TRY(run_forward(dn, P, s));
-    k_expm1<<<grid_for(npix * 3), 256, 0, s>>>(P.out.as<float>(), npix * 3, out);
+    k_expm1<<<grid_for(npix * 3), 256, 0, s>>>(P.out.as<float>(), P.x0.as<uint16_t>(), npix, out);
     PT_CUDA_TRY(cudaGetLastError());
     PT_CUDA_TRY(cudaStreamSynchronize(s));
     PT_TRY(check_err(dn));
@@ -961,7 +974,8 @@ int pt_denoise(pt_denoiser *dn, const pt_denoise_io *io, void *stream) {
     k_pack_frame<<<grid_for((long long)wp * hp), 256, 0, s>>>(reinterpret_cast<const float4 *>(io->color), io->albedo,
                                                                io->normal, w, h, wp, hp, P.x0.as<uint16_t>());
     PT_TRY(run_forward(dn, P, s));
-    k_denoise_out<<<tiles, 256, 0, s>>>(reinterpret_cast<const float4 *>(io->color), P.out.as<float>(), w, h, wp, tile,
+    k_denoise_out<<<tiles, 256, 0, s>>>(reinterpret_cast<const float4 *>(io->color), P.out.as<float>(),
+                                        P.x0.as<uint16_t>(), w, h, wp, tile,
                                         io->fallback_rel, io->fallback_sigma, reinterpret_cast<float4 *>(io->output),
                                         io->tile_fallback, dn->fallback.as<unsigned>());
     PT_CUDA_TRY(cudaGetLastError());

@@ -32,10 +32,15 @@ struct DevBuf {
     template <class T> T *as() const { return static_cast<T *>(ptr); }
 };
 
+struct BatchWorkspace;  // pt_render_batch state (pt_render.cu)
+void pt_batch_release(BatchWorkspace *b);
+
 struct pt_context {
     int device = 0;
     int num_sms = 0;
     int max_smem_per_block = 0;
+    BatchWorkspace *batch = nullptr;
+    ~pt_context() { pt_batch_release(batch); }
 };
 
 struct MeshInstanceRef {  // where the world vertices of one mesh instance live
@@ -123,6 +128,9 @@ int pt_bvh_build_impl(pt_scene *s, const pt_bvh_opts *opts, cudaStream_t stream)
 int pt_bvh_refit_impl(pt_scene *s, cudaStream_t stream);
 // pt_render.cu
 int pt_render_impl(pt_scene *s, const pt_render_params *p, const pt_frame_buffers *fb, cudaStream_t stream);
+int pt_render_batch_impl(pt_context *ctx, pt_scene *const *scenes, const pt_render_params *p,
+                         const pt_frame_buffers *fbs, uint32_t n, cudaStream_t stream);
+int pt_render_batch_stats(const pt_context *ctx, pt_render_stats *out);
 int pt_trace_rays_impl(pt_scene *s, const float *rays, float *hits, uint32_t n, int anyhit, cudaStream_t stream);
 int pt_autotune_impl(pt_scene *s, const pt_render_params *p, const pt_frame_buffers *fb, pt_tune_result *out,
                      cudaStream_t stream);

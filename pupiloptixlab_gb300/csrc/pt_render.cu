@@ -69,7 +69,31 @@ struct State {
 struct Outputs {
     float4 *accum, *frame;
     float *albedo, *normal, *test;
+    uint32_t drop_nonfinite;  // PT_RENDER_DROP_NONFINITE
 };
+
+// Multi-scene launch (pt_render_batch): the wave's pixel range is the
+// concatenation of every scene's pixels; pix_off[k] is scene k's first.  The
+// BVHs are merged into one node / primitive array, roots[k] is scene k's root.
+struct Batch {
+    const DevScene *scenes;
+    const Outputs *outs;
+    const uint32_t *pix_off;  // n + 1 entries
+    const int *roots;
+    uint32_t n;
+    uint32_t *bins;           // 2 * nbins words: per-(scene, material type) counts, then cursors
+    uint32_t nbins;
+};
+// Scene of the wave-pixel q: the last k with pix_off[k] <= q.
+PT_DI uint32_t batch_scene(const Batch &b, uint32_t q) {
+    uint32_t lo = 0, hi = b.n;  // pix_off[lo] <= q < pix_off[hi]
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(b.pix_off + mid) <= q) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
 
 PT_DI void save_rng(uint2 *dst, const Sampler &s) {
     *dst = make_uint2((uint32_t)s.state, (uint32_t)(s.state >> 32));
@@ -131,14 +155,25 @@ PT_DI void camera_ray(const DevScene &s, uint32_t x, uint32_t y, Sampler &rng, f
     o = f3(s.c2w[0].w, s.c2w[1].w, s.c2w[2].w);
 }
 
-__global__ void k_raygen(DevScene s, State st, Wave w) {
+PT_DI void raygen_one(const DevScene &s, uint32_t p, uint32_t frame_seed, uint32_t rng_mode, float3 &o, float3 &d,
+                      Sampler &rng) {
+    rng.init(rng_mode, p, frame_seed);
+    camera_ray(s, p % s.width_px, p / s.width_px, rng, o, d);
+}
+
+template <bool BATCH>
+__global__ void k_raygen(DevScene s, Batch bt, State st, Wave w) {
     const uint32_t total = w.frames * w.npix;
     for (uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x; slot < total; slot += gridDim.x * blockDim.x) {
         uint32_t fl = slot / w.npix, p = slot - fl * w.npix;
         Sampler rng;
-        rng.init(w.rng_mode, p, w.seed0 + w.frame0 + fl);
         float3 o, d;
-        camera_ray(s, p % s.width_px, p / s.width_px, rng, o, d);
+        if (BATCH) {
+            const uint32_t k = batch_scene(bt, p);
+            raygen_one(bt.scenes[k], p - bt.pix_off[k], w.seed0 + w.frame0 + fl, w.rng_mode, o, d, rng);
+        } else {
+            raygen_one(s, p, w.seed0 + w.frame0 + fl, w.rng_mode, o, d, rng);
+        }
         st.ray_o[slot] = make_float4(o.x, o.y, o.z, 0.001f);
         st.ray_d[slot] = make_float4(d.x, d.y, d.z, 1e16f);
         st.thr[slot] = make_float4(1.f, 1.f, 1.f, 0.f);
@@ -173,6 +208,7 @@ PT_DI size_t smem_node_bytes(const DevScene &s) {
 // Ray sources / result sinks of the persistent traversal.
 struct ExtendSrc {  // closest hit of the active queue (entries are path slots)
     State st;
+    PT_DI int root(uint32_t) const { return 0; }
     PT_DI uint32_t count() const { return st.counters[kNIn]; }
     PT_DI void load(uint32_t i, float3 &o, float3 &d, float &tmin, float &tmax, uint32_t &tag) const {
         uint32_t slot = st.q_in[i];
@@ -189,6 +225,7 @@ struct ExtendSrc {  // closest hit of the active queue (entries are path slots)
 };
 struct ShadowSrc {  // any hit of the shadow queue; unoccluded rays add their NEE radiance
     State st;
+    PT_DI int root(uint32_t) const { return 0; }
     PT_DI uint32_t count() const { return st.counters[kNShadow]; }
     PT_DI void load(uint32_t i, float3 &o, float3 &d, float &tmin, float &tmax, uint32_t &tag) const {
         float4 o4 = st.sh_o[i], d4 = st.sh_d[i];
@@ -206,11 +243,26 @@ struct ShadowSrc {  // any hit of the shadow queue; unoccluded rays add their NE
         st.rad[ps] = make_float4(rr.x + c.x, rr.y + c.y, rr.z + c.z, rr.w);
     }
 };
+// Multi-scene sources: the ray starts at its scene's root of the merged BVH.
+struct BatchExtendSrc : ExtendSrc {
+    Batch bt;
+    uint32_t npix;
+    PT_DI int root(uint32_t slot) const { return __ldg(bt.roots + batch_scene(bt, slot % npix)); }
+};
+struct BatchShadowSrc : ShadowSrc {
+    Batch bt;
+    uint32_t npix;
+    PT_DI int root(uint32_t i) const {
+        const uint32_t slot = __float_as_uint(st.sh_c[i].w);
+        return __ldg(bt.roots + batch_scene(bt, slot % npix));
+    }
+};
 template <bool ANY>
 struct UserSrc {  // pt_trace_rays
     const float4 *rays;
     float4 *hits;
     uint32_t n;
+    PT_DI int root(uint32_t) const { return 0; }
     PT_DI uint32_t count() const { return n; }
     PT_DI void load(uint32_t i, float3 &o, float3 &d, float &tmin, float &tmax, uint32_t &tag) const {
         float4 o4 = rays[2 * (size_t)i], d4 = rays[2 * (size_t)i + 1];
@@ -236,18 +288,36 @@ PT_DI int2 *stage_smem(const DevScene &s, float4 *smem) {
 
 // ANY = false: closest hit of the extension rays; ANY = true: shadow rays.
 // Widths 2 and 4 are capped at 72 registers (7 blocks of 128 threads per SM).
-template <int K, bool ANY, bool COUNT>
-__global__ void __maxnreg__(K == 8 ? 128 : 72) k_trace_queue(DevScene s, State st) {
+template <int K, bool ANY, bool COUNT, bool BATCH = false>
+__global__ void __maxnreg__(K == 8 ? 128 : 72) k_trace_queue(DevScene s, State st, Batch bt, uint32_t npix) {
     extern __shared__ float4 smem[];
     int2 *sstack = stage_smem<K>(s, smem);
     if (ANY) {
-        ShadowSrc src{st};
-        trace_persistent<K, true, COUNT>(s, smem, sstack, src, st.counters + kWorkShadow, st.counters + kOverflow,
-                                         st.stats + kStatShNodes, st.stats + kStatShPrims, st.stats + kStatShRays);
+        if (BATCH) {
+            BatchShadowSrc src;
+            src.st = st;
+            src.bt = bt;
+            src.npix = npix;
+            trace_persistent<K, true, COUNT>(s, smem, sstack, src, st.counters + kWorkShadow, st.counters + kOverflow,
+                                             st.stats + kStatShNodes, st.stats + kStatShPrims, st.stats + kStatShRays);
+        } else {
+            ShadowSrc src{st};
+            trace_persistent<K, true, COUNT>(s, smem, sstack, src, st.counters + kWorkShadow, st.counters + kOverflow,
+                                             st.stats + kStatShNodes, st.stats + kStatShPrims, st.stats + kStatShRays);
+        }
     } else {
-        ExtendSrc src{st};
-        trace_persistent<K, false, COUNT>(s, smem, sstack, src, st.counters + kWorkExtend, st.counters + kOverflow,
-                                          st.stats + kStatExtNodes, st.stats + kStatExtPrims, st.stats + kStatExtRays);
+        if (BATCH) {
+            BatchExtendSrc src;
+            src.st = st;
+            src.bt = bt;
+            src.npix = npix;
+            trace_persistent<K, false, COUNT>(s, smem, sstack, src, st.counters + kWorkExtend, st.counters + kOverflow,
+                                              st.stats + kStatExtNodes, st.stats + kStatExtPrims, st.stats + kStatExtRays);
+        } else {
+            ExtendSrc src{st};
+            trace_persistent<K, false, COUNT>(s, smem, sstack, src, st.counters + kWorkExtend, st.counters + kOverflow,
+                                              st.stats + kStatExtNodes, st.stats + kStatExtPrims, st.stats + kStatExtRays);
+        }
     }
 }
 
@@ -290,147 +360,164 @@ PT_DI void hit_geometry(const DevScene &s, float4 h, float3 o, float3 d, const D
 }
 
 // One bounce of shading for every entry of the active queue.
-__global__ void __launch_bounds__(256) k_shade(DevScene s, State st, Wave w, Outputs out) {
+struct ShadeOut {
+    bool push_ext = false, push_sh = false;
+    float3 hit_pos = f3s(0.f), sh_d = f3s(0.f), sh_c = f3s(0.f);
+    float sh_tmax = 0.f;
+};
+
+// One path slot of k_shade: frame fl of the wave, pixel p of scene s.
+PT_DI void shade_one(const DevScene &s, const Outputs &out, const State &st, const Wave &w, uint32_t slot, uint32_t fl,
+                     uint32_t p, float env_pdf, ShadeOut &so) {
+    float3 new_d = f3s(0.f);
+    uint32_t meta = st.meta[slot];
+    uint32_t depth = meta & 0xffffu;
+    bool prev_delta = (meta >> 16) & 1u;
+    uint32_t frame = w.frame0 + fl;
+    bool last = frame == w.last_frame;
+    float4 h = st.hit[slot];
+    float3 ro = xyz(st.ray_o[slot]), rd = xyz(st.ray_d[slot]);
+    float4 t4 = st.thr[slot];
+    float3 thr = xyz(t4);
+    float prev_pdf = t4.w;
+    float4 r4 = st.rad[slot];
+    float3 rad = xyz(r4);
+    Sampler rng = load_rng(st.rng + slot, w.rng_mode, w.seed0 + frame);
+    int prim = __float_as_int(h.y);
+    bool alive = prim >= 0;
+    HitGeo g;
+    LocalBsdf bsdf;
+    if (!alive) {  // __miss__default (main.cu:199-215)
+        if (s.has_env) {
+            float3 le = xyz(s.env.rad);
+            if (depth == 0) rad = rad + le;
+            else rad = rad + le * (thr * mis_weight(prev_pdf, env_pdf));
+        }
+        if (depth == 0 && last) {
+            if (out.albedo) { out.albedo[3 * p] = 0.f; out.albedo[3 * p + 1] = 0.f; out.albedo[3 * p + 2] = 0.f; }
+            if (out.normal) { out.normal[3 * p] = 0.f; out.normal[3 * p + 1] = 0.f; out.normal[3 * p + 2] = 0.f; }
+        }
+    } else {  // ClosestHit (main.cu:220-234)
+        const DevInstance &in = s.inst[s.prim_inst[prim]];
+        const DevMaterial &m = s.mats[in.material];
+        hit_geometry(s, h, ro, rd, in, m.twosided != 0, g);
+        bsdf = material_local(m, g.uv);
+        int ei = in.emitter_offset >= 0 ? in.emitter_offset + (prim - (int)in.prim_offset) : -1;
+        if (depth == 0) {  // main.cu:90-98
+            if (ei >= 0) rad = rad + xyz(s.emitters[ei].rad);
+            if (last) {
+                float3 al = bsdf.albedo();
+                if (out.albedo) { out.albedo[3 * p] = al.x; out.albedo[3 * p + 1] = al.y; out.albedo[3 * p + 2] = al.z; }
+                if (out.normal) { out.normal[3 * p] = g.nrm.x; out.normal[3 * p + 1] = g.nrm.y; out.normal[3 * p + 2] = g.nrm.z; }
+            }
+        } else if (ei >= 0) {  // emitter hit with MIS (main.cu:175-185)
+            const DevEmitter &e = s.emitters[ei];
+            float epdf = emitter_eval_pdf(e, g.pos, g.nrm, ro);
+            if (!is_zero(epdf)) {
+                float mis = prev_delta ? 1.f : mis_weight(prev_pdf, epdf * e.a.y);
+                rad = rad + thr * xyz(e.rad) * mis;
+            }
+        }
+    }
+    if (depth == 0) {  // main.cu:104
+        float tv = rng.next();
+        if (last && out.test) out.test[p] = tv;
+    }
+    if (alive) {  // main.cu:107-109
+        depth++;
+        if (depth >= w.max_depth) alive = false;
+    }
+    if (alive) {  // Russian roulette, main.cu:111-114
+        float rr = depth > 2 ? 0.95f : 1.0f;
+        if (rng.next() > rr) alive = false;
+        else thr = thr / rr;
+    }
+    if (alive) {  // next-event estimation, main.cu:117-144
+        float sel = rng.next();
+        float2 xi = rng.next2();
+        int ei = select_emitter(s, sel);
+        if (ei != -2) {
+            const DevEmitter &e = ei >= 0 ? s.emitters[ei] : s.env;
+            EmitterSample es;
+            emitter_sample_direct(e, g.pos, g.nrm, xi, es);
+            if (es.pdf != 0.f) {
+                BsdfRecord er;
+                er.wi = to_local(es.wi, g.nrm);
+                er.wo = to_local(-rd, g.nrm);
+                er.f = f3s(0.f);
+                er.pdf = 0.f;
+                er.type = 0;
+                bsdf.eval(er);
+                if (!is_zero(er.f * es.pdf)) {
+                    float NoL = dot(g.nrm, es.wi);
+                    if (NoL > 0.f) {
+                        float mis = mis_weight(es.pdf, er.pdf);
+                        float pdf = es.pdf * e.a.y;
+                        so.sh_c = thr * es.radiance * er.f * NoL * mis / pdf;
+                        so.sh_d = es.wi;
+                        so.sh_tmax = es.distance - 0.0001f;
+                        so.push_sh = true;
+                    }
+                }
+            }
+        }
+    }
+    if (alive) {  // BSDF sampling, main.cu:146-166
+        BsdfRecord br;
+        br.wo = to_local(-rd, g.nrm);
+        br.wi = f3s(0.f);
+        br.f = f3s(0.f);
+        br.pdf = 0.f;
+        br.type = 0;
+        bsdf.sample(br, rng);
+        if (is_zero(br.f * fabsf(br.wi.z)) || is_zero(br.pdf)) {
+            alive = false;
+        } else {
+            thr = thr * (br.f * fabsf(br.wi.z) / br.pdf);
+            new_d = to_world(br.wi, g.nrm);
+            prev_pdf = br.pdf;
+            prev_delta = (br.type & kDelta) != 0;
+            so.push_ext = true;
+        }
+    }
+    if (prim >= 0) so.hit_pos = g.pos;
+    st.rad[slot] = make_float4(rad.x, rad.y, rad.z, r4.w);
+    if (alive) {
+        st.thr[slot] = make_float4(thr.x, thr.y, thr.z, prev_pdf);
+        st.meta[slot] = depth | (prev_delta ? (1u << 16) : 0u);
+        save_rng(st.rng + slot, rng);
+        st.ray_o[slot] = make_float4(so.hit_pos.x, so.hit_pos.y, so.hit_pos.z, 0.001f);
+        st.ray_d[slot] = make_float4(new_d.x, new_d.y, new_d.z, 1e16f);
+    }
+}
+
+template <bool BATCH>
+__global__ void __launch_bounds__(256) k_shade(DevScene s, Batch bt, State st, Wave w, Outputs out) {
     __shared__ uint32_t push_smem[72];
     const uint32_t n = st.counters[kNIn];
     const float env_pdf = 0.25f * kInvPi;  // ConstEnvEmitter::Eval (env.h:82-85)
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         uint32_t i = base + threadIdx.x;
         bool valid = i < n;
-        bool push_ext = false, push_sh = false;
         uint32_t slot = 0;
-        float3 hit_pos = f3s(0.f), new_d = f3s(0.f), sh_d = f3s(0.f), sh_c = f3s(0.f);
-        float sh_tmax = 0.f;
+        ShadeOut so;
         if (valid) {
             slot = st.q_in[i];
-            uint32_t meta = st.meta[slot];
-            uint32_t depth = meta & 0xffffu;
-            bool prev_delta = (meta >> 16) & 1u;
-            uint32_t fl = slot / w.npix, p = slot - fl * w.npix;
-            uint32_t frame = w.frame0 + fl;
-            bool last = frame == w.last_frame;
-            float4 h = st.hit[slot];
-            float3 ro = xyz(st.ray_o[slot]), rd = xyz(st.ray_d[slot]);
-            float4 t4 = st.thr[slot];
-            float3 thr = xyz(t4);
-            float prev_pdf = t4.w;
-            float4 r4 = st.rad[slot];
-            float3 rad = xyz(r4);
-            Sampler rng = load_rng(st.rng + slot, w.rng_mode, w.seed0 + frame);
-            int prim = __float_as_int(h.y);
-            bool alive = prim >= 0;
-            HitGeo g;
-            LocalBsdf bsdf;
-            if (!alive) {  // __miss__default (main.cu:199-215)
-                if (s.has_env) {
-                    float3 le = xyz(s.env.rad);
-                    if (depth == 0) rad = rad + le;
-                    else rad = rad + le * (thr * mis_weight(prev_pdf, env_pdf));
-                }
-                if (depth == 0 && last) {
-                    if (out.albedo) { out.albedo[3 * p] = 0.f; out.albedo[3 * p + 1] = 0.f; out.albedo[3 * p + 2] = 0.f; }
-                    if (out.normal) { out.normal[3 * p] = 0.f; out.normal[3 * p + 1] = 0.f; out.normal[3 * p + 2] = 0.f; }
-                }
-            } else {  // ClosestHit (main.cu:220-234)
-                const DevInstance &in = s.inst[s.prim_inst[prim]];
-                const DevMaterial &m = s.mats[in.material];
-                hit_geometry(s, h, ro, rd, in, m.twosided != 0, g);
-                bsdf = material_local(m, g.uv);
-                int ei = in.emitter_offset >= 0 ? in.emitter_offset + (prim - (int)in.prim_offset) : -1;
-                if (depth == 0) {  // main.cu:90-98
-                    if (ei >= 0) rad = rad + xyz(s.emitters[ei].rad);
-                    if (last) {
-                        float3 al = bsdf.albedo();
-                        if (out.albedo) { out.albedo[3 * p] = al.x; out.albedo[3 * p + 1] = al.y; out.albedo[3 * p + 2] = al.z; }
-                        if (out.normal) { out.normal[3 * p] = g.nrm.x; out.normal[3 * p + 1] = g.nrm.y; out.normal[3 * p + 2] = g.nrm.z; }
-                    }
-                } else if (ei >= 0) {  // emitter hit with MIS (main.cu:175-185)
-                    const DevEmitter &e = s.emitters[ei];
-                    float epdf = emitter_eval_pdf(e, g.pos, g.nrm, ro);
-                    if (!is_zero(epdf)) {
-                        float mis = prev_delta ? 1.f : mis_weight(prev_pdf, epdf * e.a.y);
-                        rad = rad + thr * xyz(e.rad) * mis;
-                    }
-                }
-            }
-            if (depth == 0) {  // main.cu:104
-                float tv = rng.next();
-                if (last && out.test) out.test[p] = tv;
-            }
-            if (alive) {  // main.cu:107-109
-                depth++;
-                if (depth >= w.max_depth) alive = false;
-            }
-            if (alive) {  // Russian roulette, main.cu:111-114
-                float rr = depth > 2 ? 0.95f : 1.0f;
-                if (rng.next() > rr) alive = false;
-                else thr = thr / rr;
-            }
-            if (alive) {  // next-event estimation, main.cu:117-144
-                float sel = rng.next();
-                float2 xi = rng.next2();
-                int ei = select_emitter(s, sel);
-                if (ei != -2) {
-                    const DevEmitter &e = ei >= 0 ? s.emitters[ei] : s.env;
-                    EmitterSample es;
-                    emitter_sample_direct(e, g.pos, g.nrm, xi, es);
-                    if (es.pdf != 0.f) {
-                        BsdfRecord er;
-                        er.wi = to_local(es.wi, g.nrm);
-                        er.wo = to_local(-rd, g.nrm);
-                        er.f = f3s(0.f);
-                        er.pdf = 0.f;
-                        er.type = 0;
-                        bsdf.eval(er);
-                        if (!is_zero(er.f * es.pdf)) {
-                            float NoL = dot(g.nrm, es.wi);
-                            if (NoL > 0.f) {
-                                float mis = mis_weight(es.pdf, er.pdf);
-                                float pdf = es.pdf * e.a.y;
-                                sh_c = thr * es.radiance * er.f * NoL * mis / pdf;
-                                sh_d = es.wi;
-                                sh_tmax = es.distance - 0.0001f;
-                                push_sh = true;
-                            }
-                        }
-                    }
-                }
-            }
-            if (alive) {  // BSDF sampling, main.cu:146-166
-                BsdfRecord br;
-                br.wo = to_local(-rd, g.nrm);
-                br.wi = f3s(0.f);
-                br.f = f3s(0.f);
-                br.pdf = 0.f;
-                br.type = 0;
-                bsdf.sample(br, rng);
-                if (is_zero(br.f * fabsf(br.wi.z)) || is_zero(br.pdf)) {
-                    alive = false;
-                } else {
-                    thr = thr * (br.f * fabsf(br.wi.z) / br.pdf);
-                    new_d = to_world(br.wi, g.nrm);
-                    prev_pdf = br.pdf;
-                    prev_delta = (br.type & kDelta) != 0;
-                    push_ext = true;
-                }
-            }
-            if (prim >= 0) hit_pos = g.pos;
-            st.rad[slot] = make_float4(rad.x, rad.y, rad.z, r4.w);
-            if (alive) {
-                st.thr[slot] = make_float4(thr.x, thr.y, thr.z, prev_pdf);
-                st.meta[slot] = depth | (prev_delta ? (1u << 16) : 0u);
-                save_rng(st.rng + slot, rng);
-                st.ray_o[slot] = make_float4(hit_pos.x, hit_pos.y, hit_pos.z, 0.001f);
-                st.ray_d[slot] = make_float4(new_d.x, new_d.y, new_d.z, 1e16f);
+            const uint32_t fl = slot / w.npix, q = slot - fl * w.npix;
+            if (BATCH) {
+                const uint32_t k = batch_scene(bt, q);
+                shade_one(bt.scenes[k], bt.outs[k], st, w, slot, fl, q - bt.pix_off[k], env_pdf, so);
+            } else {
+                shade_one(s, out, st, w, slot, fl, q, env_pdf, so);
             }
         }
         uint32_t pos_ext, pos_sh;
-        block_push2(push_ext, push_sh, st.counters + kNOut, st.counters + kNShadow, pos_ext, pos_sh, push_smem);
-        if (push_ext) st.q_out[pos_ext] = slot;
-        if (push_sh) {  // shadow ray from the hit point, tmin 1e-4, tmax distance - 1e-4 (main.cu:122-126)
-            st.sh_o[pos_sh] = make_float4(hit_pos.x, hit_pos.y, hit_pos.z, 0.0001f);
-            st.sh_d[pos_sh] = make_float4(sh_d.x, sh_d.y, sh_d.z, sh_tmax);
-            st.sh_c[pos_sh] = make_float4(sh_c.x, sh_c.y, sh_c.z, __uint_as_float(slot));
+        block_push2(so.push_ext, so.push_sh, st.counters + kNOut, st.counters + kNShadow, pos_ext, pos_sh, push_smem);
+        if (so.push_ext) st.q_out[pos_ext] = slot;
+        if (so.push_sh) {  // shadow ray from the hit point, tmin 1e-4, tmax distance - 1e-4 (main.cu:122-126)
+            st.sh_o[pos_sh] = make_float4(so.hit_pos.x, so.hit_pos.y, so.hit_pos.z, 0.0001f);
+            st.sh_d[pos_sh] = make_float4(so.sh_d.x, so.sh_d.y, so.sh_d.z, so.sh_tmax);
+            st.sh_c[pos_sh] = make_float4(so.sh_c.x, so.sh_c.y, so.sh_c.z, __uint_as_float(slot));
         }
     }
 }
@@ -444,7 +531,12 @@ __global__ void __launch_bounds__(256) k_shade(DevScene s, State st, Wave w, Out
 constexpr int kNumBins = 8;
 enum : int { kBinCount = 24, kBinCursor = 40 };  // word offsets in the counters block
 
-__global__ void k_bin_count(DevScene s, State st, uint8_t *keys) {
+PT_DI uint32_t material_bin(const DevScene &s, int prim) {
+    return prim >= 0 ? (s.mats[s.inst[s.prim_inst[prim]].material].type & (kNumBins - 1)) : 0u;
+}
+
+template <bool BATCH>
+__global__ void k_bin_count(DevScene s, Batch bt, uint32_t npix, State st, uint8_t *keys) {
     __shared__ uint32_t h[kNumBins];
     if (threadIdx.x < kNumBins) h[threadIdx.x] = 0;
     __syncthreads();
@@ -452,8 +544,7 @@ __global__ void k_bin_count(DevScene s, State st, uint8_t *keys) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         uint32_t slot = st.q_in[i];
         int prim = __float_as_int(st.hit[slot].y);
-        uint32_t key = 0;
-        if (prim >= 0) key = s.mats[s.inst[s.prim_inst[prim]].material].type & (kNumBins - 1);
+        const uint32_t key = BATCH ? material_bin(bt.scenes[batch_scene(bt, slot % npix)], prim) : material_bin(s, prim);
         keys[i] = (uint8_t)key;
         atomicAdd(&h[key], 1u);
     }
@@ -488,13 +579,90 @@ __global__ void k_bin_scatter(State st, const uint8_t *keys, uint32_t *q_sorted)
     }
 }
 
+// Multi-scene binning: key = scene * 8 + material type, so that after the
+// scatter a scene's paths stay together (each scene's BVH and shading data
+// are then read by neighbouring warps) and are grouped by BSDF inside it.
+__global__ void k_bin_count_batch(Batch bt, uint32_t npix, State st, uint16_t *keys) {
+    extern __shared__ uint32_t hb[];
+    for (uint32_t k = threadIdx.x; k < bt.nbins; k += blockDim.x) hb[k] = 0;
+    __syncthreads();
+    const uint32_t n = st.counters[kNIn];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t slot = st.q_in[i];
+        const int prim = __float_as_int(st.hit[slot].y);
+        const uint32_t sc = batch_scene(bt, slot % npix);
+        const uint32_t key = sc * kNumBins + material_bin(bt.scenes[sc], prim);
+        keys[i] = static_cast<uint16_t>(key);
+        atomicAdd(&hb[key], 1u);
+    }
+    __syncthreads();
+    for (uint32_t k = threadIdx.x; k < bt.nbins; k += blockDim.x)
+        if (hb[k]) atomicAdd(bt.bins + k, hb[k]);
+}
+
+// One block of 1024 threads: exclusive scan of the counts into the cursors,
+// counts cleared for the next bounce (nbins <= 1024).
+__global__ void __launch_bounds__(1024) k_bin_scan_batch(Batch bt) {
+    __shared__ uint32_t warp_sum[32];
+    const uint32_t t = threadIdx.x, lane = t & 31, wid = t >> 5;
+    const uint32_t c = t < bt.nbins ? bt.bins[t] : 0u;
+    uint32_t x = c;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= (uint32_t)o) x += y;
+    }
+    if (lane == 31) warp_sum[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        uint32_t w = warp_sum[lane];
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= (uint32_t)o) w += y;
+        }
+        warp_sum[lane] = w;
+    }
+    __syncthreads();
+    const uint32_t incl = x + (wid > 0 ? warp_sum[wid - 1] : 0u);
+    if (t < bt.nbins) {
+        bt.bins[bt.nbins + t] = incl - c;
+        bt.bins[t] = 0;
+    }
+}
+
+__global__ void k_bin_scatter_batch(Batch bt, State st, const uint16_t *keys, uint32_t *q_sorted) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const uint32_t n = st.counters[kNIn];
+    uint32_t *cursor = bt.bins + bt.nbins;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        const bool valid = i < n;
+        const uint32_t key = valid ? keys[i] : 0xffffffffu;
+        const unsigned peers = __match_any_sync(FULL, key);
+        const int leader = __ffs(peers) - 1;
+        uint32_t pos = 0;
+        if (valid && lane == leader) pos = atomicAdd(cursor + key, (uint32_t)__popc(peers));
+        pos = __shfl_sync(FULL, pos, leader);
+        if (valid) q_sorted[pos + __popc(peers & ((1u << lane) - 1u))] = st.q_in[i];
+    }
+}
+
 // Accumulation, main.cu:188-196: frames of the wave in order, per pixel.
-__global__ void k_accumulate(State st, Wave w, Outputs out) {
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < w.npix; p += gridDim.x * blockDim.x) {
+template <bool BATCH>
+__global__ void k_accumulate(State st, Wave w, Outputs out0, Batch bt) {
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < w.npix; q += gridDim.x * blockDim.x) {
+        uint32_t p = q;
+        Outputs out = out0;
+        if (BATCH) {
+            const uint32_t k = batch_scene(bt, q);
+            out = bt.outs[k];
+            p = q - bt.pix_off[k];
+        }
         float4 acc = out.accum[p];
         float3 a = xyz(acc);
         for (uint32_t fl = 0; fl < w.frames; fl++) {
-            float3 L = xyz(st.rad[(size_t)fl * w.npix + p]);
+            float3 L = xyz(st.rad[(size_t)fl * w.npix + q]);
+            if (out.drop_nonfinite && !(isfinite(L.x) && isfinite(L.y) && isfinite(L.z))) L = f3s(0.f);
             uint32_t cnt = w.cnt0 + w.frame0 + fl;
             if (w.accumulate && cnt > 0) {
                 const float t = 1.f / (cnt + 1.f);
@@ -588,17 +756,47 @@ struct Timer {
     }
 };
 
+// Where a render's workspace, events and statistics live: the scene for
+// pt_render, the context for pt_render_batch.
+struct RunTarget {
+    RenderWorkspace *wsp;
+    cudaEvent_t ev0, ev1;
+    int num_sms;
+    uint32_t tuned_block, tuned_wave_paths;
+    pt_render_stats *rs;
+};
+
+static Outputs make_outputs(const pt_frame_buffers *fb, uint32_t flags) {
+    Outputs out;
+    out.accum = reinterpret_cast<float4 *>(fb->accum);
+    out.frame = reinterpret_cast<float4 *>(fb->frame);
+    out.albedo = fb->albedo;
+    out.normal = fb->normal;
+    out.test = fb->test;
+    out.drop_nonfinite = (flags & PT_RENDER_DROP_NONFINITE) ? 1u : 0u;
+    return out;
+}
+
 template <int K>
 struct Launcher {
     static int run(pt_scene *s, const pt_render_params *p, const pt_frame_buffers *fb, cudaStream_t st) {
-        const DevScene &d = s->dev;
-        RenderWorkspace &ws = s->ws;
-        const uint32_t npix = d.width_px * d.height_px;
+        RunTarget t{&s->ws, s->ev0, s->ev1, s->num_sms, s->tuned_block, s->tuned_wave_paths, &s->render_stats};
         const uint32_t max_depth = p->max_depth ? p->max_depth : s->desc_shallow.max_depth;
+        const uint32_t npix = s->dev.width_px * s->dev.height_px;
+        return run_waves<false>(t, s->dev, Batch{}, npix, max_depth, p, make_outputs(fb, p->flags), st);
+    }
+
+    // Waves of frames over npix pixels (one scene, or the concatenated
+    // pixels of a batch), each captured in a CUDA graph unless timing or
+    // NO_GRAPH asks for direct launches.
+    template <bool BATCH>
+    static int run_waves(const RunTarget &t, const DevScene &d, const Batch &bt, uint32_t npix, uint32_t max_depth,
+                         const pt_render_params *p, const Outputs &out, cudaStream_t st) {
+        RenderWorkspace &ws = *t.wsp;
         const bool count = (p->flags & PT_RENDER_COUNTERS) != 0;
         const bool timing = (p->flags & PT_RENDER_KERNEL_TIMING) != 0;
         uint32_t frames_per_wave = p->wave_spp;
-        const uint32_t wave_paths = s->tuned_wave_paths ? s->tuned_wave_paths : kDefaultWavePaths;
+        const uint32_t wave_paths = t.tuned_wave_paths ? t.tuned_wave_paths : kDefaultWavePaths;
         if (frames_per_wave == 0) frames_per_wave = std::max<uint32_t>(1, (uint32_t)(wave_paths / std::max<uint32_t>(npix, 1)));
         frames_per_wave = std::max<uint32_t>(1, std::min(frames_per_wave, std::max<uint32_t>(p->spp, 1)));
         const size_t cap = (size_t)frames_per_wave * npix;
@@ -626,32 +824,26 @@ struct Launcher {
         stt.sh_c = ws.sh_c.as<float4>();
         stt.counters = ws.counters.as<uint32_t>();
         stt.stats = reinterpret_cast<unsigned long long *>(ws.counters.as<uint32_t>() + kStatBase);
-        Outputs out;
-        out.accum = reinterpret_cast<float4 *>(fb->accum);
-        out.frame = reinterpret_cast<float4 *>(fb->frame);
-        out.albedo = fb->albedo;
-        out.normal = fb->normal;
-        out.test = fb->test;
 
-        const int tb = p->block_size ? (int)p->block_size : (s->tuned_block ? (int)s->tuned_block : 128);
+        const int tb = p->block_size ? (int)p->block_size : (t.tuned_block ? (int)t.tuned_block : 128);
         const size_t smem = (size_t)d.smem_nodes * 32 * K + (size_t)kShortStack * 8 * tb;
-        auto k_ext = count ? k_trace_queue<K, false, true> : k_trace_queue<K, false, false>;
-        auto k_sh = count ? k_trace_queue<K, true, true> : k_trace_queue<K, true, false>;
+        auto k_ext = count ? k_trace_queue<K, false, true, BATCH> : k_trace_queue<K, false, false, BATCH>;
+        auto k_sh = count ? k_trace_queue<K, true, true, BATCH> : k_trace_queue<K, true, false, BATCH>;
         if ((e = set_smem(k_ext, smem)) != PT_OK || (e = set_smem(k_sh, smem)) != PT_OK) return e;
         int occ_t = 0, occ_s = 0;
         PT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_t, k_ext, tb, smem));
-        PT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, k_shade, 256, 0));
-        const uint32_t grid_trace = (uint32_t)std::max(1, occ_t) * s->num_sms;
-        const uint32_t grid_shade = (uint32_t)std::max(1, occ_s) * s->num_sms;
+        PT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, k_shade<BATCH>, 256, 0));
+        const uint32_t grid_trace = (uint32_t)std::max(1, occ_t) * t.num_sms;
+        const uint32_t grid_shade = (uint32_t)std::max(1, occ_s) * t.num_sms;
 
         const bool sort = (p->flags & PT_RENDER_NO_MATERIAL_SORT) == 0;
         if (sort && ws.sort_capacity < cap) {
-            if ((e = ws.mat_key.ensure(cap)) != PT_OK || (e = ws.sort_tmp.ensure(4 * cap)) != PT_OK) return e;
+            if ((e = ws.mat_key.ensure(2 * cap)) != PT_OK || (e = ws.sort_tmp.ensure(4 * cap)) != PT_OK) return e;
             ws.sort_capacity = cap;
         }
         int occ_b = 0;
         PT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_b, k_bin_scatter, 256, 0));
-        const uint32_t grid_bin = (uint32_t)std::max(1, occ_b) * s->num_sms;
+        const uint32_t grid_bin = (uint32_t)std::max(1, occ_b) * t.num_sms;
 
         // The whole render is captured into a CUDA graph on the scene's own
         // stream (ordered after and before the caller's stream by events) and
@@ -671,7 +863,7 @@ struct Launcher {
         Timer tm;
         uint32_t launches = 0;
         uint32_t waves = 0;
-        if (!graph) PT_CUDA_TRY(cudaEventRecord(s->ev0, st));
+        if (!graph) PT_CUDA_TRY(cudaEventRecord(t.ev0, st));
         cudaError_t enq = cudaMemsetAsync(ws.counters.ptr, 0, 256, ls);
         for (uint32_t f0 = 0; f0 < p->spp && enq == cudaSuccess; f0 += frames_per_wave) {
             Wave w;
@@ -687,30 +879,37 @@ struct Launcher {
             stt.q_in = ws.q0.as<uint32_t>();
             stt.q_out = ws.q1.as<uint32_t>();
             const size_t slots = (size_t)w.frames * npix;
-            k_raygen<<<nblocks(slots, 256), 256, 0, ls>>>(d, stt, w);
+            k_raygen<BATCH><<<nblocks(slots, 256), 256, 0, ls>>>(d, bt, stt, w);
             launches++;
             for (uint32_t b = 0; b < max_depth; b++) {
                 if (timing) tm.mark(0, ls);
-                k_ext<<<grid_trace, tb, smem, ls>>>(d, stt);
+                k_ext<<<grid_trace, tb, smem, ls>>>(d, stt, bt, npix);
                 if (timing) tm.mark(0, ls);
                 State shade_st = stt;
-                if (sort) {
-                    k_bin_count<<<grid_bin, 256, 0, ls>>>(d, stt, ws.mat_key.as<uint8_t>());
+                if (sort && BATCH) {
+                    k_bin_count_batch<<<grid_bin, 256, bt.nbins * 4, ls>>>(bt, npix, stt, ws.mat_key.as<uint16_t>());
+                    k_bin_scan_batch<<<1, 1024, 0, ls>>>(bt);
+                    k_bin_scatter_batch<<<grid_bin, 256, 0, ls>>>(bt, stt, ws.mat_key.as<uint16_t>(),
+                                                                  ws.sort_tmp.as<uint32_t>());
+                    shade_st.q_in = ws.sort_tmp.as<uint32_t>();
+                    launches += 3;
+                } else if (sort) {
+                    k_bin_count<BATCH><<<grid_bin, 256, 0, ls>>>(d, bt, npix, stt, ws.mat_key.as<uint8_t>());
                     k_bin_scan<<<1, 1, 0, ls>>>(stt.counters);
                     k_bin_scatter<<<grid_bin, 256, 0, ls>>>(stt, ws.mat_key.as<uint8_t>(), ws.sort_tmp.as<uint32_t>());
                     shade_st.q_in = ws.sort_tmp.as<uint32_t>();
                     launches += 3;
                 }
                 if (timing) tm.mark(2, ls);
-                k_shade<<<grid_shade, 256, 0, ls>>>(d, shade_st, w, out);
+                k_shade<BATCH><<<grid_shade, 256, 0, ls>>>(d, bt, shade_st, w, out);
                 if (timing) { tm.mark(2, ls); tm.mark(1, ls); }
-                k_sh<<<grid_trace, tb, smem, ls>>>(d, stt);
+                k_sh<<<grid_trace, tb, smem, ls>>>(d, stt, bt, npix);
                 if (timing) tm.mark(1, ls);
                 k_advance<<<1, 1, 0, ls>>>(stt.counters);
                 launches += 4;
                 std::swap(stt.q_in, stt.q_out);
             }
-            k_accumulate<<<nblocks(npix, 256), 256, 0, ls>>>(stt, w, out);
+            k_accumulate<BATCH><<<nblocks(npix, 256), 256, 0, ls>>>(stt, w, out, bt);
             launches++;
             waves++;
             enq = cudaGetLastError();
@@ -743,9 +942,9 @@ struct Launcher {
                 }
             }
             cudaGraphDestroy(g);
-            PT_CUDA_TRY(cudaEventRecord(s->ev0, ws.stream));
+            PT_CUDA_TRY(cudaEventRecord(t.ev0, ws.stream));
             PT_CUDA_TRY(cudaGraphLaunch(ws.exec, ws.stream));
-            PT_CUDA_TRY(cudaEventRecord(s->ev1, ws.stream));
+            PT_CUDA_TRY(cudaEventRecord(t.ev1, ws.stream));
             PT_CUDA_TRY(cudaEventRecord(ws.ev_out, ws.stream));
             PT_CUDA_TRY(cudaStreamWaitEvent(st, ws.ev_out, 0));
         } else {
@@ -757,12 +956,12 @@ struct Launcher {
         PT_CUDA_TRY(cudaGetLastError());
         if (!graph) {
             // direct launches: time the enqueued work with events around it on the caller's stream
-            PT_CUDA_TRY(cudaEventRecord(s->ev1, st));
+            PT_CUDA_TRY(cudaEventRecord(t.ev1, st));
         }
-        PT_CUDA_TRY(cudaEventSynchronize(s->ev1));
-        pt_render_stats &rs = s->render_stats;
+        PT_CUDA_TRY(cudaEventSynchronize(t.ev1));
+        pt_render_stats &rs = *t.rs;
         rs = pt_render_stats{};
-        PT_CUDA_TRY(cudaEventElapsedTime(&rs.render_ms, s->ev0, s->ev1));
+        PT_CUDA_TRY(cudaEventElapsedTime(&rs.render_ms, t.ev0, t.ev1));
         for (size_t i = 0; i + 1 < tm.used; i += 2) {
             float ms = 0.f;
             cudaEventElapsedTime(&ms, tm.ev[i], tm.ev[i + 1]);
@@ -816,7 +1015,158 @@ struct Launcher {
     }
 };
 
+// Merged-BVH child rebasing: inner children move by the scene's first node,
+// leaf children (count > 0) by its first primitive slot.
+template <int K>
+__global__ void k_rebase_nodes(float4 *nodes, uint32_t num_nodes, int node_off, int prim_off) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < num_nodes; i += gridDim.x * blockDim.x) {
+        float *f = reinterpret_cast<float *>(nodes + (size_t)i * 2 * K);
+#pragma unroll
+        for (int c = 0; c < K; c++) {
+            int ch = __float_as_int(f[6 * K + c]);
+            const int cnt = __float_as_int(f[7 * K + c]);
+            if (ch < 0) continue;
+            ch += cnt > 0 ? prim_off : node_off;
+            f[6 * K + c] = __int_as_float(ch);
+        }
+    }
+}
+
 }  // namespace
+
+// pt_render_batch state, owned by the context: merged BVH, per-scene tables,
+// the wave workspace (with its CUDA graph) and the last call's statistics.
+struct BatchWorkspace {
+    RenderWorkspace ws;
+    DevBuf nodes, prims, scenes, outs, pix_off, roots, bins;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    pt_render_stats stats{};
+};
+
+void pt_batch_release(BatchWorkspace *b) {
+    if (!b) return;
+    DevBuf *bufs[] = {&b->nodes, &b->prims, &b->scenes, &b->outs, &b->pix_off, &b->roots, &b->bins};
+    for (DevBuf *d : bufs) d->release();
+    RenderWorkspace &w = b->ws;
+    DevBuf *wb[] = {&w.ray_o, &w.ray_d, &w.hit, &w.thr, &w.rad, &w.rng, &w.meta, &w.q0,
+                    &w.q1, &w.sh_o, &w.sh_d, &w.sh_c, &w.mat_key, &w.counters, &w.sort_tmp};
+    for (DevBuf *d : wb) d->release();
+    if (w.exec) cudaGraphExecDestroy(w.exec);
+    if (w.ev_in) cudaEventDestroy(w.ev_in);
+    if (w.ev_out) cudaEventDestroy(w.ev_out);
+    if (w.stream) cudaStreamDestroy(w.stream);
+    if (b->ev0) cudaEventDestroy(b->ev0);
+    if (b->ev1) cudaEventDestroy(b->ev1);
+    delete b;
+}
+
+namespace {
+
+template <int K>
+int render_batch(pt_context *ctx, pt_scene *const *scenes, const pt_render_params *p, const pt_frame_buffers *fbs,
+                 uint32_t n, cudaStream_t st) {
+    if (!ctx->batch) {
+        ctx->batch = new BatchWorkspace();
+        PT_CUDA_TRY(cudaEventCreate(&ctx->batch->ev0));
+        PT_CUDA_TRY(cudaEventCreate(&ctx->batch->ev1));
+    }
+    BatchWorkspace &b = *ctx->batch;
+    // merged BVH: every scene's nodes and leaf-order primitive records, rebased
+    std::vector<DevScene> hs(n);
+    std::vector<Outputs> ho(n);
+    std::vector<uint32_t> pix_off(n + 1, 0);
+    std::vector<int> roots(n);
+    uint64_t total_nodes = 0, total_prims = 0, total_pix = 0;
+    float pad_mag = 0.f;
+    for (uint32_t k = 0; k < n; k++) {
+        const pt_scene *s = scenes[k];
+        roots[k] = static_cast<int>(total_nodes);
+        pix_off[k] = static_cast<uint32_t>(total_pix);
+        total_nodes += s->dev.num_nodes;
+        total_prims += s->num_prims;
+        total_pix += (uint64_t)s->dev.width_px * s->dev.height_px;
+        pad_mag = std::max(pad_mag, s->dev.pad_mag);
+        hs[k] = s->dev;
+        ho[k] = make_outputs(&fbs[k], p->flags);
+    }
+    if (n * kNumBins > 1024) {
+        pt_set_error("pt_render_batch: at most %d scenes per call", 1024 / kNumBins);
+        return PT_ERR_INVALID;
+    }
+    if (total_prims >= (1u << 27) || total_nodes >= (1u << 31) || total_pix >= (1ull << 31)) {
+        pt_set_error("pt_render_batch: batch too large (%llu primitives, %llu pixels)",
+                     (unsigned long long)total_prims, (unsigned long long)total_pix);
+        return PT_ERR_INVALID;
+    }
+    pix_off[n] = static_cast<uint32_t>(total_pix);
+    int e;
+    if ((e = b.nodes.ensure(std::max<uint64_t>(total_nodes, 1) * 32 * K)) != PT_OK ||
+        (e = b.prims.ensure(std::max<uint64_t>(total_prims, 1) * 48)) != PT_OK ||
+        (e = b.scenes.ensure(n * sizeof(DevScene))) != PT_OK || (e = b.outs.ensure(n * sizeof(Outputs))) != PT_OK ||
+        (e = b.pix_off.ensure((n + 1) * sizeof(uint32_t))) != PT_OK || (e = b.roots.ensure(n * sizeof(int))) != PT_OK ||
+        (e = b.bins.ensure(2 * 1024 * sizeof(uint32_t))) != PT_OK)
+        return e;
+    PT_CUDA_TRY(cudaMemsetAsync(b.bins.ptr, 0, 2 * 1024 * sizeof(uint32_t), st));
+    uint64_t node_off = 0, prim_off = 0;
+    for (uint32_t k = 0; k < n; k++) {
+        const pt_scene *s = scenes[k];
+        float4 *dn = b.nodes.as<float4>() + node_off * 2 * K;
+        PT_CUDA_TRY(cudaMemcpyAsync(dn, s->dev.nodes, (size_t)s->dev.num_nodes * 32 * K, cudaMemcpyDeviceToDevice, st));
+        PT_CUDA_TRY(cudaMemcpyAsync(b.prims.as<float4>() + prim_off * 3, s->dev.prims, (size_t)s->num_prims * 48,
+                                    cudaMemcpyDeviceToDevice, st));
+        k_rebase_nodes<K><<<nblocks(s->dev.num_nodes, 256), 256, 0, st>>>(dn, s->dev.num_nodes, (int)node_off,
+                                                                          (int)prim_off);
+        PT_CUDA_TRY(cudaGetLastError());
+        node_off += s->dev.num_nodes;
+        prim_off += s->num_prims;
+    }
+    PT_CUDA_TRY(cudaMemcpyAsync(b.scenes.ptr, hs.data(), n * sizeof(DevScene), cudaMemcpyHostToDevice, st));
+    PT_CUDA_TRY(cudaMemcpyAsync(b.outs.ptr, ho.data(), n * sizeof(Outputs), cudaMemcpyHostToDevice, st));
+    PT_CUDA_TRY(cudaMemcpyAsync(b.pix_off.ptr, pix_off.data(), (n + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    PT_CUDA_TRY(cudaMemcpyAsync(b.roots.ptr, roots.data(), n * sizeof(int), cudaMemcpyHostToDevice, st));
+    // the host tables above are pageable: finish the copies before they go out of scope
+    PT_CUDA_TRY(cudaStreamSynchronize(st));
+
+    DevScene dt = scenes[0]->dev;  // traversal view: merged arrays, no shared-memory top levels
+    dt.nodes = b.nodes.as<float4>();
+    dt.prims = b.prims.as<float4>();
+    dt.num_nodes = static_cast<uint32_t>(total_nodes);
+    dt.smem_nodes = 0;
+    dt.pad_mag = pad_mag;
+    Batch bt;
+    bt.scenes = b.scenes.as<DevScene>();
+    bt.outs = b.outs.as<Outputs>();
+    bt.pix_off = b.pix_off.as<uint32_t>();
+    bt.roots = b.roots.as<int>();
+    bt.n = n;
+    bt.bins = b.bins.as<uint32_t>();
+    bt.nbins = n * kNumBins;
+    const uint32_t max_depth = p->max_depth ? p->max_depth : scenes[0]->desc_shallow.max_depth;
+    RunTarget t{&b.ws, b.ev0, b.ev1, ctx->num_sms, 0, 0, &b.stats};
+    Outputs none{};
+    return Launcher<K>::template run_waves<true>(t, dt, bt, static_cast<uint32_t>(total_pix), max_depth, p, none, st);
+}
+
+}  // namespace
+
+int pt_render_batch_impl(pt_context *ctx, pt_scene *const *scenes, const pt_render_params *p,
+                         const pt_frame_buffers *fbs, uint32_t n, cudaStream_t st) {
+    if (p->spp == 0 || n == 0) return PT_OK;
+    switch (scenes[0]->dev.width) {
+        case 2: return render_batch<2>(ctx, scenes, p, fbs, n, st);
+        case 4: return render_batch<4>(ctx, scenes, p, fbs, n, st);
+        default: return render_batch<8>(ctx, scenes, p, fbs, n, st);
+    }
+}
+
+int pt_render_batch_stats(const pt_context *ctx, pt_render_stats *out) {
+    if (!ctx->batch) {
+        pt_set_error("pt_render_batch_get_stats: no batch rendered on this context");
+        return PT_ERR_STATE;
+    }
+    *out = ctx->batch->stats;
+    return PT_OK;
+}
 
 int pt_render_impl(pt_scene *s, const pt_render_params *p, const pt_frame_buffers *fb, cudaStream_t st) {
     if (p->spp == 0) return PT_OK;
@@ -1000,6 +1350,7 @@ int render_noalloc(pt_scene *s, const pt_render_params *p, const pt_frame_buffer
     out.albedo = fb->albedo;
     out.normal = fb->normal;
     out.test = fb->test;
+    out.drop_nonfinite = (p->flags & PT_RENDER_DROP_NONFINITE) ? 1u : 0u;
 
     const int tb = p->block_size ? (int)p->block_size : 128;
     const size_t smem = (size_t)d.smem_nodes * 32 * K + (size_t)kShortStack * 8 * tb;
@@ -1009,7 +1360,7 @@ int render_noalloc(pt_scene *s, const pt_render_params *p, const pt_frame_buffer
     if ((e = set_smem(k_ext, smem)) != PT_OK || (e = set_smem(k_sh, smem)) != PT_OK) return e;
     int occ_t = 0, occ_s = 0;
     PT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_t, k_ext, tb, smem));
-    PT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, k_shade, 256, 0));
+    PT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, k_shade<false>, 256, 0));
     const uint32_t grid_trace = (uint32_t)std::max(1, occ_t) * s->num_sms;
     const uint32_t grid_shade = (uint32_t)std::max(1, occ_s) * s->num_sms;
 
@@ -1028,15 +1379,15 @@ int render_noalloc(pt_scene *s, const pt_render_params *p, const pt_frame_buffer
         w.accumulate = p->accumulate;
         stt.q_in = q0;
         stt.q_out = q1;
-        k_raygen<<<nblocks((size_t)w.frames * npix, 256), 256, 0, st>>>(d, stt, w);
+        k_raygen<false><<<nblocks((size_t)w.frames * npix, 256), 256, 0, st>>>(d, Batch{}, stt, w);
         for (uint32_t b = 0; b < max_depth; b++) {
-            k_ext<<<grid_trace, tb, smem, st>>>(d, stt);
-            k_shade<<<grid_shade, 256, 0, st>>>(d, stt, w, out);
-            k_sh<<<grid_trace, tb, smem, st>>>(d, stt);
+            k_ext<<<grid_trace, tb, smem, st>>>(d, stt, Batch{}, npix);
+            k_shade<false><<<grid_shade, 256, 0, st>>>(d, Batch{}, stt, w, out);
+            k_sh<<<grid_trace, tb, smem, st>>>(d, stt, Batch{}, npix);
             k_advance<<<1, 1, 0, st>>>(stt.counters);
             std::swap(stt.q_in, stt.q_out);
         }
-        k_accumulate<<<nblocks(npix, 256), 256, 0, st>>>(stt, w, out);
+        k_accumulate<false><<<nblocks(npix, 256), 256, 0, st>>>(stt, w, out, Batch{});
     }
     PT_CUDA_TRY(cudaGetLastError());
     uint32_t ovf = 0;

@@ -670,6 +670,30 @@ int pt_render(pt_scene *scene, const pt_render_params *params, const pt_frame_bu
     return pt_render_impl(scene, params, fb, static_cast<cudaStream_t>(stream));
 }
 
+int pt_render_batch(pt_context *ctx, pt_scene *const *scenes, const pt_render_params *params,
+                    const pt_frame_buffers *fbs, uint32_t n, void *stream) {
+    clear_stale_cuda_error();
+    if (!ctx || !params || (n && (!scenes || !fbs))) { pt_set_error("context, scenes, params or buffers is NULL"); return PT_ERR_INVALID; }
+    if (params->rng != PT_RNG_REF_LCG && params->rng != PT_RNG_PCG32) { pt_set_error("unknown rng mode"); return PT_ERR_INVALID; }
+    for (uint32_t k = 0; k < n; k++) {
+        const pt_scene *s = scenes[k];
+        if (!s || !fbs[k].accum) { pt_set_error("scene %u or its accum buffer is NULL", k); return PT_ERR_INVALID; }
+        if (s->device != ctx->device) { pt_set_error("scene %u lives on another device", k); return PT_ERR_INVALID; }
+        if (!s->bvh_built) { pt_set_error("pt_render_batch: scene %u has no BVH", k); return PT_ERR_STATE; }
+        if (s->dev.width != scenes[0]->dev.width) {
+            pt_set_error("pt_render_batch: scene %u has BVH width %u, scene 0 has %u", k, s->dev.width, scenes[0]->dev.width);
+            return PT_ERR_INVALID;
+        }
+    }
+    PT_CUDA_TRY(cudaSetDevice(ctx->device));
+    return pt_render_batch_impl(ctx, scenes, params, fbs, n, static_cast<cudaStream_t>(stream));
+}
+
+int pt_render_batch_get_stats(const pt_context *ctx, pt_render_stats *out) {
+    if (!ctx || !out) { pt_set_error("context or out is NULL"); return PT_ERR_INVALID; }
+    return pt_render_batch_stats(ctx, out);
+}
+
 int pt_autotune(pt_scene *scene, const pt_render_params *params, const pt_frame_buffers *fb, pt_tune_result *out,
                 void *stream) {
     clear_stale_cuda_error();

@@ -207,7 +207,8 @@ constexpr int kRefillBusyMax = 20;
 // nearest is the next item, the others go on the stack with their distance,
 // which is re-checked against the current closest hit when popped.
 //
-// Src provides: count(), load(i, o, d, tmin, tmax, tag), store(i, tag, result).
+// Src provides: count(), load(i, o, d, tmin, tmax, tag), root(tag) (the node
+// the ray starts at), store(i, tag, result).
 template <int K, bool ANY, bool COUNT, class Src>
 PT_DI void trace_persistent(const DevScene &s, const float4 *snodes, int2 *sstack_base, Src &src, uint32_t *work,
                             uint32_t *ovf_flag, unsigned long long *stat_nodes, unsigned long long *stat_prims,
@@ -260,7 +261,7 @@ PT_DI void trace_persistent(const DevScene &s, const float4 *snodes, int2 *sstac
                     best.t = tmax;
                     best.prim = -1;
                     best.u = best.v = 0.f;
-                    item = 0;
+                    item = src.root(tag);
                     leaf = kNoItem;
                     st.sp = 0;
                     active = true;

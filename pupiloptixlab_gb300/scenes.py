@@ -496,6 +496,43 @@ def icosphere_field(width: int = 1920, height: int = 1080, max_depth: int = 8, n
     return s
 
 
+def mesh_pool(count: int = 32, subdivisions: int = 4, amplitude: float = 0.1, seed: int = 0) -> list:
+    """`count` seeded displaced icospheres that several scenes can instance."""
+    base = icosphere(subdivisions)
+    return [displaced_icosphere(seed * 100003 + i, amplitude, subdivisions, base) for i in range(count)]
+
+
+def pooled_field(seed: int, num_instances: int, width: int, height: int, max_depth: int = 8, pool=None) -> Scene:
+    """An icosphere field like icosphere_field (7 random materials, ground,
+    constant environment 0.5, 4 sphere lights) whose instances reuse the
+    meshes of `pool`; the field's box grows with the instance count so the
+    density stays that of the 200-instance field."""
+    pool = pool if pool is not None else mesh_pool()
+    s = Scene(width, height, max_depth, name=f"pooled_field_{seed}_{num_instances}")
+    rng = np.random.default_rng(seed)
+    half = 10.0 * (max(num_instances, 1) / 200.0) ** (1.0 / 3.0)
+    ground_mat = s.add_material(diffuse(0.5))
+    s.add_instance(abi.SHAPE_MESH, s.add_mesh(grid(64, 64, 4.0 * half, 0.0)), ground_mat)
+    mesh_ids = {}
+    for i in range(num_instances):
+        j = int(rng.integers(0, len(pool)))
+        if j not in mesh_ids:
+            mesh_ids[j] = s.add_mesh(pool[j])
+        mat = s.add_material(random_material(rng, int(rng.integers(1, 8))))
+        pos = (rng.uniform(-half, half), rng.uniform(1.5, 1.5 + 2 * half), rng.uniform(-half, half))
+        tw = translate(*pos) @ random_rotation(rng) @ scale(float(rng.uniform(0.6, 1.4)))
+        s.add_instance(abi.SHAPE_MESH, mesh_ids[j], mat, tw)
+    light_mat = s.add_material(diffuse(0.0))
+    l = 0.8 * half
+    sphere = s.add_sphere((0.0, 0.0, 0.0), 1.0)
+    for (x, z) in [(-l, -l), (l, -l), (-l, l), (l, l)]:
+        s.add_instance(abi.SHAPE_SPHERE, sphere, light_mat, translate(x, 2.4 * half, z) @ scale(0.15 * half),
+                       radiance=(12.0, 11.0, 9.0))
+    s.env = (0.5, 0.5, 0.5)
+    s.camera = camera(40.0, width / height, look_at_to_world((0.0, 1.4 * half, 3.8 * half), (0.0, half, 0.0)))
+    return s
+
+
 def material_spheres(width: int = 96, height: int = 64, max_depth: int = 6) -> Scene:
     """Seven spheres (mesh icospheres, one per material) over a checkerboard
     floor, lit by the environment and one emissive sphere: small parity scene."""

@@ -33,8 +33,17 @@ def _cos(a, b):
 
 @pytest.fixture(scope="module")
 def dn(cuda_ctx):
+    """A denoiser whose output layer (zero at initialisation) is randomised,
+    so that every layer's gradient is non-zero."""
     from pupiloptixlab_gb300.denoiser import Denoiser
     d = Denoiser(cuda_ctx, seed=3)
+    p = d.get_params()
+    cin, cout, off = d.layers[-1]
+    assert not p[off:off + 9 * cin * cout + cout].any()
+    w = np.random.default_rng(4).uniform(-0.1, 0.1, (cout, 9, cin)).astype(np.float32)
+    w[3:] = 0.0
+    p[off:off + 9 * cin * cout] = w.ravel()
+    d.set_params(p)
     yield d
     d.close()
 
@@ -76,10 +85,18 @@ def test_gradients_match_cpu(dn):
 
 
 def test_training_reduces_loss(cuda_ctx):
+    """A smooth target under strong multiplicative noise: the network starts as
+    the identity (zero output layer) and must learn to smooth."""
     from pupiloptixlab_gb300.denoiser import Denoiser
     d = Denoiser(cuda_ctx, seed=5, lr=2e-3)
-    inp, tgt = _batch(4, 64, 64, 3)
-    inp, tgt = inp.cuda(), tgt.cuda()
+    g = torch.Generator().manual_seed(3)
+    coarse = torch.rand(4, 3, 8, 8, generator=g) * 2.0
+    tgt = torch.nn.functional.interpolate(coarse, size=(64, 64), mode="bilinear", align_corners=False)
+    tgt = tgt.permute(0, 2, 3, 1).contiguous()
+    noisy = tgt * torch.exp(0.7 * torch.randn(4, 64, 64, 3, generator=g))
+    guides = torch.rand(4, 64, 64, 6, generator=g)
+    inp = torch.cat([noisy, guides], dim=-1).to(torch.float16).cuda()
+    tgt = tgt.cuda()
     d.train_step(inp, tgt)
     first = d.read_loss()
     for _ in range(60):
@@ -90,7 +107,7 @@ def test_training_reduces_loss(cuda_ctx):
     last = d.read_loss()
     d.close()
     assert np.isfinite(first) and np.isfinite(last)
-    assert last < 0.8 * first, (first, last)
+    assert last < 0.6 * first, (first, last)
 
 
 def test_denoise_frame_and_fallback(cuda_ctx, dn):

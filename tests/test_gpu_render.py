@@ -116,12 +116,13 @@ def test_icosphere_field_reduced(cuda_ctx):
 
 
 def test_material_sort_and_graph_do_not_change_the_image(cuda_ctx):
-    """Binning hits by material and CUDA-graph replay only reorder work."""
+    """Binning hits by material and CUDA-graph replay only reorder work; dropping
+    non-finite samples changes nothing in an image that has none."""
     sc = scenes.material_spheres(48, 32)
     g = GpuScene(cuda_ctx, sc)
     ref = gpu_render(g, 5, seed=2, flags=abi.RENDER_NO_GRAPH)["accum"]
     for flags in (0, abi.RENDER_NO_MATERIAL_SORT, abi.RENDER_NO_MATERIAL_SORT | abi.RENDER_NO_GRAPH,
-                  abi.RENDER_KERNEL_TIMING | abi.RENDER_COUNTERS):
+                  abi.RENDER_KERNEL_TIMING | abi.RENDER_COUNTERS, abi.RENDER_DROP_NONFINITE):
         got = gpu_render(g, 5, seed=2, flags=flags)["accum"]
         assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), flags
     # the instantiated graph is updated in place by later calls with other parameters
