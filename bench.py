@@ -27,6 +27,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -385,7 +386,7 @@ def run_denoise(args):
                           "batch": args.dn_batch, "crop": args.dn_crop, "loss": dn.read_loss()}), flush=True)
         return
     inputs, targets, data_info = render_pairs(ctx, args.dn_pairs, crop=args.dn_crop, target_spp=args.dn_target_spp,
-                                              noisy_spp=(1, 2, 4, 4, 8, 16, 32, 64), log=log)
+                                              noisy_spp=(1, 2, 4, 4, 8, 16, 32, 64, 128, 256), log=log)
     dn = Denoiser(ctx, lr=args.dn_lr, seed=1)
     B, P = args.dn_batch, args.dn_pairs
     nb = P // B
@@ -398,6 +399,8 @@ def run_denoise(args):
     losses = []
     e0.record()
     for k in range(args.dn_steps):
+        if k % 250 == 0:  # cosine decay of the Adam step size to 5 % over the run
+            dn.set_lr(args.dn_lr * (0.05 + 0.95 * 0.5 * (1.0 + math.cos(math.pi * k / max(args.dn_steps, 1)))))
         dn.train_step(*batches[k % nb])
         if (k + 1) % 500 == 0:
             losses.append((k + 1, dn.read_loss()))

@@ -439,6 +439,8 @@ int pt_denoiser_get_grads(const pt_denoiser *dn, float *grads);
 int pt_denoiser_train_step(pt_denoiser *dn, const void *input_f16, const float *target, uint32_t n, uint32_t crop,
                            void *stream);
 int pt_denoiser_read_loss(pt_denoiser *dn, float *mean_loss);
+/* Adam step size of the following training steps (e.g. a decay schedule). */
+int pt_denoiser_set_lr(pt_denoiser *dn, float lr);
 /* Network output for a batch: out = width*height*n*3 FP32 linear RGB (device). */
 int pt_denoiser_forward(pt_denoiser *dn, const void *input_f16, uint32_t n, uint32_t height, uint32_t width,
                         float *out, void *stream);

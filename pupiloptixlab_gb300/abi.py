@@ -164,6 +164,7 @@ PROTOTYPES = [
     ("pt_denoiser_get_grads", C.c_int, [C.c_void_p, C.c_void_p]),
     ("pt_denoiser_train_step", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p]),
     ("pt_denoiser_read_loss", C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
+    ("pt_denoiser_set_lr", C.c_int, [C.c_void_p, C.c_float]),
     ("pt_denoiser_forward", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p,
                                       C.c_void_p]),
     ("pt_denoise", C.c_int, [C.c_void_p, C.POINTER(DenoiseIO), C.c_void_p]),

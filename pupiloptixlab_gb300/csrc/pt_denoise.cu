@@ -240,7 +240,9 @@ __global__ void k_loss(const float *out, const uint16_t *x0, const float *target
     if ((threadIdx.x & 31) == 0) atomicAdd(loss_sum, acc);
 }
 
-// Adam bias corrections for the step about to run: state = {step, 1/(1-b1^t), 1/(1-b2^t)}
+// Adam bias corrections for the step about to run: state = {step, 1/(1-b1^t),
+// 1/(1-b2^t), step size}; the step size lives on the device so that the
+// captured training graph follows pt_denoiser_set_lr.
 __global__ void k_adam_begin(float *state, float beta1, float beta2) {
     const float t = state[0] + 1.f;
     state[0] = t;
@@ -251,9 +253,8 @@ __global__ void k_adam_begin(float *state, float beta1, float beta2) {
 // One layer: weights [cout][9][cin] then bias[cout].  Also writes the BF16
 // weights and their flipped transpose [cin][9][cout] for the data gradient.
 __global__ void k_adam(float *p, float *m, float *v, const float *g, long long nw, int nb, int cout, int cin,
-                       const float *state, float lr, float beta1, float beta2, float eps, uint16_t *wbf,
-                       uint16_t *wtbf) {
-    const float c1 = state[1], c2 = state[2];
+                       const float *state, float beta1, float beta2, float eps, uint16_t *wbf, uint16_t *wtbf) {
+    const float c1 = state[1], c2 = state[2], lr = state[3];
     const long long n = nw + nb;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const float gi = g[i];
@@ -632,8 +633,8 @@ int run_adam(pt_denoiser *dn, cudaStream_t s) {
         const uint64_t off = dn->w_off[l];
         k_adam<<<grid_for(nw + L.cout), 256, 0, s>>>(
             dn->params.as<float>() + off, dn->adam_m.as<float>() + off, dn->adam_v.as<float>() + off,
-            dn->grads.as<float>() + off, nw, L.cout, L.cout, L.cin, dn->adam_state.as<float>(), o.lr, o.beta1, o.beta2,
-            o.eps, dn->wbf.as<uint16_t>() + dn->wbf_off[l], dn->wtbf.as<uint16_t>() + dn->wbf_off[l]);
+            dn->grads.as<float>() + off, nw, L.cout, L.cout, L.cin, dn->adam_state.as<float>(), o.beta1, o.beta2, o.eps,
+            dn->wbf.as<uint16_t>() + dn->wbf_off[l], dn->wtbf.as<uint16_t>() + dn->wbf_off[l]);
     }
     PT_CUDA_TRY(cudaGetLastError());
     return PT_OK;
@@ -706,7 +707,8 @@ int upload_params(pt_denoiser *dn, const float *host) {
     PT_CUDA_TRY(cudaMemcpy(dn->params.ptr, host, dn->nparams * sizeof(float), cudaMemcpyHostToDevice));
     PT_CUDA_TRY(cudaMemset(dn->adam_m.ptr, 0, dn->nparams * sizeof(float)));
     PT_CUDA_TRY(cudaMemset(dn->adam_v.ptr, 0, dn->nparams * sizeof(float)));
-    PT_CUDA_TRY(cudaMemset(dn->adam_state.ptr, 0, 4 * sizeof(float)));
+    const float state[4] = {0.f, 0.f, 0.f, dn->opts.lr};
+    PT_CUDA_TRY(cudaMemcpy(dn->adam_state.ptr, state, sizeof(state), cudaMemcpyHostToDevice));
     PT_TRY(sync_weights(dn, 0));
     PT_CUDA_TRY(cudaDeviceSynchronize());
     return PT_OK;
@@ -829,6 +831,19 @@ int pt_denoiser_set_params(pt_denoiser *dn, const float *params) {
     PT_CUDA_TRY(cudaSetDevice(dn->device));
     PT_CUDA_TRY(cudaStreamSynchronize(dn->stream));
     return upload_params(dn, params);
+}
+
+int pt_denoiser_set_lr(pt_denoiser *dn, float lr) {
+    (void)cudaGetLastError();
+    if (!dn || !(lr >= 0.f)) {
+        pt_set_error("pt_denoiser_set_lr: bad denoiser or step size");
+        return PT_ERR_INVALID;
+    }
+    PT_CUDA_TRY(cudaSetDevice(dn->device));
+    PT_CUDA_TRY(cudaMemcpyAsync(dn->adam_state.as<float>() + 3, &lr, sizeof(float), cudaMemcpyHostToDevice, dn->stream));
+    PT_CUDA_TRY(cudaStreamSynchronize(dn->stream));
+    dn->opts.lr = lr;
+    return PT_OK;
 }
 
 int pt_denoiser_get_grads(const pt_denoiser *dn, float *grads) {

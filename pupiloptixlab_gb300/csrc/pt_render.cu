@@ -492,7 +492,8 @@ PT_DI void shade_one(const DevScene &s, const Outputs &out, const State &st, con
 }
 
 template <bool BATCH>
-__global__ void __launch_bounds__(256) k_shade(DevScene s, Batch bt, State st, Wave w, Outputs out) {
+// 3 blocks of 256 threads per SM: at most 85 registers per thread.
+__global__ void __launch_bounds__(256, 3) k_shade(DevScene s, Batch bt, State st, Wave w, Outputs out) {
     __shared__ uint32_t push_smem[72];
     const uint32_t n = st.counters[kNIn];
     const float env_pdf = 0.25f * kInvPi;  // ConstEnvEmitter::Eval (env.h:82-85)

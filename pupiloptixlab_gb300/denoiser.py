@@ -138,6 +138,9 @@ class Denoiser:
         abi.check(self.lib.pt_denoiser_train_step(self.handle, _p(inputs), _p(targets), n, h, _stream_ptr()),
                   "pt_denoiser_train_step", self.lib)
 
+    def set_lr(self, lr: float) -> None:
+        abi.check(self.lib.pt_denoiser_set_lr(self.handle, lr), "pt_denoiser_set_lr", self.lib)
+
     def read_loss(self) -> float:
         v = C.c_float()
         abi.check(self.lib.pt_denoiser_read_loss(self.handle, C.byref(v)), "pt_denoiser_read_loss", self.lib)
