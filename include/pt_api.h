@@ -87,14 +87,28 @@ typedef enum pt_texture_type { PT_TEX_RGB = 0, PT_TEX_BITMAP = 1, PT_TEX_CHECKER
  * seed, 24-bit float output.  Both are drawn in the reference's order. */
 typedef enum pt_rng_mode { PT_RNG_REF_LCG = 0, PT_RNG_PCG32 = 1 } pt_rng_mode;
 
+/* Bitmap sampling modes: the values of cudaTextureAddressMode /
+ * cudaTextureFilterMode, as the reference casts its own enums to them
+ * (framework/cuda/texture.cpp:82-84). */
+enum { PT_TEX_ADDRESS_WRAP = 0, PT_TEX_ADDRESS_CLAMP = 1, PT_TEX_ADDRESS_MIRROR = 2 };
+enum { PT_TEX_FILTER_POINT = 0, PT_TEX_FILTER_LINEAR = 1 };
+
 /* One texture: cuda::Texture (framework/cuda/texture.h:10-57).  color0 is the
  * RGB value or checkerboard patch1, color1 is patch2.  uv_transform holds
- * the first two rows of the 4x4 texture-coordinate transform (row-major). */
+ * the first two rows of the 4x4 texture-coordinate transform (row-major).
+ * PT_TEX_BITMAP: pixels are RGBA floats, width*height*4, row-major, in HOST
+ * memory during pt_scene_upload (util::BitmapTexture, framework/util/texture.h);
+ * they are sampled like the reference's float4 CUDA texture object
+ * (normalized coordinates, framework/cuda/texture.cpp:60-102). */
 typedef struct pt_texture_desc {
     uint32_t type;
     float color0[3];
     float color1[3];
     float uv_transform[8];
+    const float *pixels;
+    uint32_t width, height;
+    uint32_t address_mode;  /* PT_TEX_ADDRESS_* */
+    uint32_t filter;        /* PT_TEX_FILTER_* */
 } pt_texture_desc;
 
 /* Texture slots per material type (tex[i]):
@@ -153,10 +167,19 @@ typedef struct pt_camera_desc {
     float camera_to_world[16];
 } pt_camera_desc;
 
-enum { PT_ENV_NONE = 0, PT_ENV_CONST = 1 };
+enum { PT_ENV_NONE = 0, PT_ENV_CONST = 1, PT_ENV_MAP = 2 };
+/* PT_ENV_CONST: ConstEnvEmitter (framework/render/emitter/env.h:67-86), radiance.
+ * PT_ENV_MAP: EnvMapEmitter (env.h:6-65): an equirectangular RGBA float map
+ * (pixels in HOST memory, width*height*4), times scale, oriented by the upper
+ * 3x3 of to_world (row-major); sampled by luminance (the CDF tables of
+ * framework/world/emitter.cpp:107-149), filtered bilinearly with wrap-around. */
 typedef struct pt_env_desc {
-    uint32_t type;      /* PT_ENV_* (ConstEnvEmitter, framework/render/emitter/env.h:67-86) */
+    uint32_t type;
     float radiance[3];
+    const float *pixels;
+    uint32_t width, height;
+    float scale;
+    float to_world[16];
 } pt_env_desc;
 
 typedef struct pt_scene_desc {

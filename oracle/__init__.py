@@ -64,6 +64,8 @@ def load() -> C.CDLL:
             getattr(lib, nm).argtypes = [_VP, _VP, C.c_uint32]
         lib.oracle_emitter_sample_raw.argtypes = [C.c_int, _VP, _VP, _VP, C.c_uint32]
         lib.oracle_select_emitter.argtypes = [_VP, C.c_uint32, C.c_int, _VP, _VP, C.c_uint32]
+        lib.oracle_envmap.argtypes = [C.c_int, _VP, C.c_uint32, C.c_uint32, C.c_float, _VP, _VP, _VP, _VP,
+                                      C.c_uint32, _VP]
         lib.oracle_camera_make.argtypes = [C.c_float, C.c_float, C.c_float, C.c_float, _VP,
                                            C.POINTER(abi.CameraDesc)]
         _lib = lib
@@ -85,6 +87,8 @@ def load_ref() -> C.CDLL | None:
         r.ref_sampling.argtypes = [_VP, _VP, C.c_uint32]
         r.ref_emitter_sample.argtypes = [C.c_int, _VP, _VP, _VP, C.c_uint32]
         r.ref_select_emitter.argtypes = [_VP, C.c_uint32, C.c_int, _VP, _VP, C.c_uint32]
+        r.ref_envmap.argtypes = [C.c_int, _VP, C.c_uint32, C.c_uint32, C.c_float, _VP, _VP, _VP, _VP, _VP,
+                                 C.c_float, _VP, _VP, C.c_uint32]
         _ref = r
     return _ref
 
@@ -167,6 +171,25 @@ class OracleScene:
         buf = np.zeros((4096, 2), np.float32)
         self.lib.oracle_emitter_table(self.handle, C.byref(cnt), _ptr(buf), 4096)
         return buf[: min(cnt.value, 4096)]
+
+
+def envmap(mode: int, pixels: np.ndarray, scale: float, to_world3: np.ndarray, to_local3: np.ndarray,
+           inp: np.ndarray):
+    """EnvMapEmitter sample (mode 0, inp (n, 2) xi -> (n, 7)) or eval (mode 1,
+    inp (n, 6) origin+direction -> (n, 4)); also returns the CDF tables."""
+    lib = load()
+    px = np.ascontiguousarray(pixels, np.float32)
+    h, w = px.shape[:2]
+    inp = np.ascontiguousarray(inp, np.float32)
+    n = inp.shape[0]
+    out = np.zeros((n, 7 if mode == 0 else 4), np.float32)
+    tables = np.zeros((h + 1) + (w + 1) * h + h + 1, np.float32)
+    tw = np.ascontiguousarray(to_world3, np.float32)
+    tl = np.ascontiguousarray(to_local3, np.float32)
+    st = lib.oracle_envmap(mode, _ptr(px), w, h, scale, _ptr(tw), _ptr(tl), _ptr(inp), _ptr(out), n, _ptr(tables))
+    if st != 0:
+        raise RuntimeError(f"oracle_envmap failed: {st}")
+    return out, tables
 
 
 def bsdf_eval(bsdf, wo, wi):

@@ -26,6 +26,7 @@
 //    the smaller primitive id.
 
 #include "pt_oracle.h"
+#include "tex_fetch.h"
 
 #include <algorithm>
 #include <atomic>
@@ -568,13 +569,24 @@ struct LocalBsdf {
 };
 
 // ---------------------------------------------------------------- textures / materials
+struct Bitmap {  // RGBA float pixels + sampling modes (util::BitmapTexture)
+    std::vector<float> px;
+    uint32_t w = 0, h = 0, address = 0, filter = 1;
+    V3 fetch(float u, float v) const {
+        texfetch::Float4 c = texfetch::fetch(px.data(), w, h, address, filter, u, v);
+        return {c.x, c.y, c.z};
+    }
+};
+
 struct Texture {  // cuda::Texture::Sample, framework/cuda/texture.h:33-57
     uint32_t type = PT_TEX_RGB;
     V3 c0{0, 0, 0}, c1{0, 0, 0};
     V4 r0{1, 0, 0, 0}, r1{0, 1, 0, 0};
+    std::shared_ptr<Bitmap> bitmap;
     V3 sample(V2 uv) const {
         V4 tex{uv.x, uv.y, 0.f, 1.f};
         float tx = dot4(r0, tex), ty = dot4(r1, tex);
+        if (type == PT_TEX_BITMAP && bitmap) return bitmap->fetch(tx, ty);  // tex2D<float4>
         if (type == PT_TEX_CHECKERBOARD) {
             tx = tx - (tx > 0.f ? floorf(tx) : ceilf(tx));
             ty = ty - (ty > 0.f ? floorf(ty) : ceilf(ty));
@@ -587,6 +599,19 @@ struct Texture {  // cuda::Texture::Sample, framework/cuda/texture.h:33-57
     }
     V3 average() const {  // GetPixelAverage, optix_material.cpp:8-35
         if (type == PT_TEX_CHECKERBOARD) return v3(c0.x + c1.x, c0.y + c1.y, c0.z + c1.z) * 0.5f;
+        if (type == PT_TEX_BITMAP && bitmap) {
+            float r = 0.f, g = 0.f, b = 0.f;
+            size_t idx = 0;
+            for (uint32_t y = 0; y < bitmap->h; y++)
+                for (uint32_t x = 0; x < bitmap->w; x++) {
+                    r += bitmap->px[idx++];
+                    g += bitmap->px[idx++];
+                    b += bitmap->px[idx++];
+                    idx++;
+                }
+            const float n = 1.f * bitmap->h * bitmap->w;
+            return {r / n, g / n, b / n};
+        }
         return c0;
     }
     float max_weight() const {  // GetWeight, world/emitter.cpp:77-101
@@ -601,6 +626,14 @@ struct Texture {  // cuda::Texture::Sample, framework/cuda/texture.h:33-57
         t.c1 = {d.color1[0], d.color1[1], d.color1[2]};
         t.r0 = {d.uv_transform[0], d.uv_transform[1], d.uv_transform[2], d.uv_transform[3]};
         t.r1 = {d.uv_transform[4], d.uv_transform[5], d.uv_transform[6], d.uv_transform[7]};
+        if (d.type == PT_TEX_BITMAP && d.pixels) {
+            t.bitmap = std::make_shared<Bitmap>();
+            t.bitmap->px.assign(d.pixels, d.pixels + 4ull * d.width * d.height);
+            t.bitmap->w = d.width;
+            t.bitmap->h = d.height;
+            t.bitmap->address = d.address_mode;
+            t.bitmap->filter = d.filter;
+        }
         return t;
     }
 };
@@ -680,10 +713,95 @@ struct Hit {
     float u = 0.f, v = 0.f;
 };
 
-enum : uint32_t { kEmitNone = 0, kEmitTri = 1, kEmitSphere = 2, kEmitConstEnv = 3 };
+enum : uint32_t { kEmitNone = 0, kEmitTri = 1, kEmitSphere = 2, kEmitConstEnv = 3, kEmitEnvMap = 4 };
+
+// EnvMapEmitter (framework/render/emitter/env.h:6-65) with the tables of
+// BuildEnvMapCdfTable (framework/world/emitter.cpp:107-149).
+struct EnvMapData {
+    Bitmap map;  // bilinear, wrap
+    std::vector<float> row_cdf, col_cdf, row_weight;
+    float normalization = 0.f, scale = 1.f;
+    V3 to_world[3], to_local[3];
+
+    void build(const float *pixels, uint32_t width, uint32_t height, float sc, const float *tw, const float *tl) {
+        map.px.assign(pixels, pixels + 4ull * width * height);
+        map.w = width;
+        map.h = height;
+        map.address = texfetch::kWrap;
+        map.filter = texfetch::kLinear;
+        scale = sc;
+        const size_t w = width, h = height;
+        col_cdf.assign((w + 1) * h, 0.f);
+        row_cdf.assign(h + 1, 0.f);
+        row_weight.assign(h, 0.f);
+        size_t ci = 0, ri = 0;
+        float row_sum = 0.f;
+        row_cdf[ri++] = 0.f;
+        for (size_t y = 0; y < h; ++y) {
+            float col_sum = 0.f;
+            col_cdf[ci++] = 0.f;
+            for (size_t x = 0; x < w; ++x) {
+                const size_t p = y * w + x;
+                col_sum += luminance(v3(pixels[p * 4], pixels[p * 4 + 1], pixels[p * 4 + 2]));
+                col_cdf[ci++] = col_sum;
+            }
+            for (size_t x = 1; x < w; ++x) col_cdf[ci - x - 1] /= col_sum;
+            col_cdf[ci - 1] = 1.f;
+            const float weight = std::sin((y + 0.5f) * kPi / h);
+            row_weight[y] = weight;
+            row_sum += col_sum * weight;
+            row_cdf[ri++] = row_sum;
+        }
+        for (size_t y = 1; y < h; ++y) row_cdf[ri - y - 1] /= row_sum;
+        row_cdf[ri - 1] = 1.f;
+        normalization = 1.f / (row_sum * (2.f * kPi / w) * (kPi / h));
+        for (int r = 0; r < 3; r++) {
+            to_world[r] = {tw[3 * r], tw[3 * r + 1], tw[3 * r + 2]};
+            to_local[r] = {tl[3 * r], tl[3 * r + 1], tl[3 * r + 2]};
+        }
+    }
+    // first i in [0, n) with x <= cdf[i], else n (the linear scans of env.h:24-31)
+    static uint32_t scan(const float *cdf, uint32_t n, float x) {
+        uint32_t i = 0;
+        for (; i < n; ++i)
+            if (x <= cdf[i]) break;
+        return i;
+    }
+    V3 lookup(float u, float v) const { return map.fetch(u, v) * scale; }
+    // SampleDirect (env.h:23-49); the reads the reference makes past its
+    // tables when the last row is drawn use row h - 1
+    void sample(V2 xi, V3 &wi, V3 &rad, float &pdf) const {
+        const uint32_t row = scan(row_cdf.data(), map.h, xi.x);
+        const uint32_t crow = std::min(row, map.h - 1);
+        const uint32_t col = scan(col_cdf.data() + (size_t)crow * (map.w + 1), map.w - 1, xi.y);
+        const float phi = static_cast<float>(col) * kPi * 2.f / static_cast<float>(map.w);
+        const float theta = static_cast<float>(row) * kPi / static_cast<float>(map.h);
+        const float st = std::sin(theta);
+        const V3 local{st * std::sin(kPi - phi), std::cos(theta), st * std::cos(kPi - phi)};
+        wi = {dot(to_world[0], local), dot(to_world[1], local), dot(to_world[2], local)};
+        rad = lookup(phi * 0.5f * kInvPi, theta * kInvPi);
+        pdf = luminance(rad) * row_weight[crow] * normalization / std::max(1e-4f, std::fabs(st));
+        if (pdf < 0.f) pdf = 0.f;
+    }
+    // Eval (env.h:51-64) for the emitter point scatter_pos + d
+    void eval(V3 scatter_pos, V3 emit_pos, V3 &rad, float &pdf) const {
+        V3 dir = normalize(emit_pos - scatter_pos);
+        dir = {dot(to_local[0], dir), dot(to_local[1], dir), dot(to_local[2], dir)};
+        const float phi = kPi - std::atan2(dir.x, dir.z);
+        const float theta = std::acos(dir.y);
+        const float tu = phi * 0.5f * kInvPi, tv = theta * kInvPi;
+        uint32_t row = static_cast<uint32_t>(tv * static_cast<float>(map.h));
+        row = std::min(row, map.h - 2u);
+        rad = lookup(tu, tv);
+        const float t = tv * static_cast<float>(map.h) - 1.f * static_cast<float>(row);
+        pdf = luminance(rad) * (row_weight[row] + t * (row_weight[row + 1] - row_weight[row])) * normalization /
+              std::max(1e-4f, std::fabs(std::sin(theta)));
+    }
+};
 
 struct Emitter {  // optix::Emitter, framework/render/emitter.h:13-29
     uint32_t type = kEmitNone;
+    std::shared_ptr<EnvMapData> envmap;
     float weight = 0.f, select_probability = 0.f;
     V3 radiance{0, 0, 0};
     float area = 0.f;
@@ -736,6 +854,13 @@ struct Emitter {  // optix::Emitter, framework/render/emitter.h:13-29
                 ret.pos = position;
                 ret.normal = normal;
             } break;
+            case kEmitEnvMap: {  // emitter/env.h:23-49
+                envmap->sample(xi, ret.wi, ret.radiance, ret.pdf);
+                ret.distance = kMaxDistance;
+                ret.distance_set = true;
+                ret.is_delta = false;
+                ret.pos = hit.position + ret.wi * ret.distance;
+            } break;
             case kEmitConstEnv: {  // emitter/env.h:69-80
                 V3 local_wi = uniform_sample_hemisphere(xi.x, xi.y);
                 ret.wi = to_world(local_wi, hit.normal);
@@ -766,6 +891,8 @@ struct Emitter {  // optix::Emitter, framework/render/emitter.h:13-29
         } else if (type == kEmitConstEnv) {
             out_pdf = 0.25f * kInvPi;
             out_radiance = radiance;
+        } else if (type == kEmitEnvMap) {
+            envmap->eval(scatter_pos, g.position, out_radiance, out_pdf);
         }
     }
 };
@@ -1294,6 +1421,20 @@ static int build_scene(const pt_scene_desc *d, Scene &s) {
         s.env.type = kEmitConstEnv;
         s.env.radiance = {d->env.radiance[0], d->env.radiance[1], d->env.radiance[2]};
         s.env.weight = 1.f;
+    } else if (d->env.type == PT_ENV_MAP && d->env.pixels && d->env.width >= 2 && d->env.height >= 2) {
+        s.has_env = true;
+        s.env.type = kEmitEnvMap;
+        s.env.weight = 1.f;
+        float tw[9], tl[9];
+        double inv[16];
+        mat_inverse_double(d->env.to_world, inv);
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 3; c++) {
+                tw[3 * r + c] = d->env.to_world[4 * r + c];
+                tl[3 * r + c] = static_cast<float>(inv[4 * r + c]);
+            }
+        s.env.envmap = std::make_shared<EnvMapData>();
+        s.env.envmap->build(d->env.pixels, d->env.width, d->env.height, d->env.scale, tw, tl);
     }
     // EmitterHelper::ComputeProbability (world/emitter.cpp:321-337)
     float wsum = 0.f;
@@ -1821,6 +1962,49 @@ int oracle_emitter_sample_raw(int kind, const float *params, const float *in, fl
     }
     return PT_OK;
 }
+// EnvMapEmitter KAT counterpart of ref_envmap: builds the CDF tables from the
+// map (written to tables: row_cdf h+1, col_cdf (w+1)*h, row_weight h,
+// normalization 1), then samples (mode 0) or evaluates (mode 1) as
+// ref_envmap does.
+int oracle_envmap(int mode, const float *pixels, uint32_t w, uint32_t h, float scale, const float *tw, const float *tl,
+                  const float *in, float *out, uint32_t n, float *tables) {
+    if (!pixels || w < 2 || h < 2) return PT_ERR_INVALID;
+    EnvMapData m;
+    m.build(pixels, w, h, scale, tw, tl);
+    if (tables) {
+        float *t = tables;
+        std::copy(m.row_cdf.begin(), m.row_cdf.end(), t);
+        t += m.row_cdf.size();
+        std::copy(m.col_cdf.begin(), m.col_cdf.end(), t);
+        t += m.col_cdf.size();
+        std::copy(m.row_weight.begin(), m.row_weight.end(), t);
+        t += m.row_weight.size();
+        *t = m.normalization;
+    }
+    for (uint32_t i = 0; i < n; i++) {
+        if (mode == 0) {
+            V3 wi, rad;
+            float pdf;
+            m.sample({in[2 * i], in[2 * i + 1]}, wi, rad, pdf);
+            float *o = out + 7 * (size_t)i;
+            o[0] = rad.x; o[1] = rad.y; o[2] = rad.z;
+            o[3] = wi.x; o[4] = wi.y; o[5] = wi.z;
+            o[6] = pdf;
+        } else {
+            const float *q = in + 6 * (size_t)i;
+            const V3 o3{q[0], q[1], q[2]};
+            const V3 d = normalize(V3{q[3], q[4], q[5]});
+            V3 rad;
+            float pdf;
+            m.eval(o3, o3 + d, rad, pdf);
+            float *o = out + 4 * (size_t)i;
+            o[0] = rad.x; o[1] = rad.y; o[2] = rad.z;
+            o[3] = pdf;
+        }
+    }
+    return PT_OK;
+}
+
 // SelectOneEmiiter over a probability list (same running sums as the scene table).
 int oracle_select_emitter(const float *probs, uint32_t num, int has_env, const float *p, int32_t *out, uint32_t n) {
     std::vector<float> cdf;

@@ -76,6 +76,8 @@ int oracle_fresnel_diffuse(const float *eta, float *out, uint32_t n);
 int oracle_ggx(const float *in, float *out, uint32_t n);
 int oracle_sampling(const float *in, float *out, uint32_t n);
 int oracle_emitter_sample_raw(int kind, const float *params, const float *in, float *out, uint32_t n);
+int oracle_envmap(int mode, const float *pixels, uint32_t w, uint32_t h, float scale, const float *tw, const float *tl,
+                  const float *in, float *out, uint32_t n, float *tables);
 int oracle_select_emitter(const float *probs, uint32_t num, int has_env, const float *p, int32_t *out, uint32_t n);
 
 int oracle_camera_make(float fov_y_deg, float aspect, float near_clip, float far_clip,

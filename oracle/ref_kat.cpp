@@ -216,6 +216,7 @@ int ref_sampling(const float *in, float *out, uint32_t n) {
 // in: shading point pos(3) normal(3) xi(2); out as oracle_emitter_sample.
 int ref_emitter_sample(int kind, const float *params, const float *in, float *out, uint32_t n) {
     Emitter e;
+    std::memset(static_cast<void *>(&e), 0, sizeof(e));  // the union leaves the shim texture's fields unset
     switch (kind) {
         case 1:
             e.type = EEmitterType::TriArea;
@@ -262,6 +263,59 @@ int ref_emitter_sample(int kind, const float *params, const float *in, float *ou
         o[7] = r.distance >= 0.f ? r.distance : 0.f;
         put3(o + 8, r.pos);
         o[11] = r.distance >= 0.f ? 1.f : 0.f;
+    }
+    return 0;
+}
+
+// EnvMapEmitter KAT (render/emitter/env.h): the reference's SampleDirect
+// (mode 0; in: xi 2 per query; out: radiance 3, wi 3, pdf 1) and Eval
+// (mode 1; in: scatter point 3, direction 3; out: radiance 3, pdf 1) over a
+// bilinear, wrapping RGBA float map and CDF tables given by the caller.
+int ref_envmap(int mode, const float *pixels, uint32_t w, uint32_t h, float scale, const float *tw, const float *tl,
+               const float *row_cdf, const float *col_cdf, const float *row_weight, float normalization,
+               const float *in, float *out, uint32_t n) {
+    EnvMapEmitter e{};
+    e.radiance.pixels = pixels;
+    e.radiance.w = w;
+    e.radiance.h = h;
+    e.radiance.address = 0;
+    e.radiance.filter = 1;
+    e.center = make_float3(0.f);
+    e.map_size = make_uint2(w, h);
+    e.row_cdf.SetData(reinterpret_cast<CUdeviceptr>(row_cdf), h + 1);
+    e.col_cdf.SetData(reinterpret_cast<CUdeviceptr>(col_cdf), (size_t)(w + 1) * h);
+    e.row_weight.SetData(reinterpret_cast<CUdeviceptr>(row_weight), h);
+    e.to_world.r0 = col(tw);
+    e.to_world.r1 = col(tw + 3);
+    e.to_world.r2 = col(tw + 6);
+    e.to_local.r0 = col(tl);
+    e.to_local.r1 = col(tl + 3);
+    e.to_local.r2 = col(tl + 6);
+    e.normalization = normalization;
+    e.scale = scale;
+    for (uint32_t i = 0; i < n; i++) {
+        if (mode == 0) {
+            const float *q = in + 2 * i;
+            LocalGeometry g;
+            g.position = make_float3(0.f);
+            g.normal = make_float3(0.f, 1.f, 0.f);
+            EmitterSampleRecord r;
+            e.SampleDirect(r, g, make_float2(q[0], q[1]));
+            float *o = out + 7 * i;
+            put3(o, r.radiance);
+            put3(o + 3, r.wi);
+            o[6] = r.pdf;
+        } else {
+            const float *q = in + 6 * i;
+            LocalGeometry g;
+            const float3 o3 = col(q), d = normalize(col(q + 3));
+            g.position = o3 + d;  // as __miss__default builds it (main.cu:204-208)
+            EmitEvalRecord r;
+            e.Eval(r, g, o3);
+            float *o = out + 4 * i;
+            put3(o, r.radiance);
+            o[3] = r.pdf;
+        }
     }
     return 0;
 }

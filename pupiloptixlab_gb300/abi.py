@@ -23,7 +23,9 @@ MATERIAL_NAMES = {1: "diffuse", 2: "dielectric", 3: "roughdielectric", 4: "condu
 TEX_RGB, TEX_BITMAP, TEX_CHECKERBOARD = 0, 1, 2
 SHAPE_MESH, SHAPE_SPHERE = 0, 1
 INST_FLIP_NORMALS, INST_FLIP_TEXCOORDS = 1, 2
-ENV_NONE, ENV_CONST = 0, 1
+ENV_NONE, ENV_CONST, ENV_MAP = 0, 1, 2
+TEX_ADDRESS_WRAP, TEX_ADDRESS_CLAMP, TEX_ADDRESS_MIRROR = 0, 1, 2
+TEX_FILTER_POINT, TEX_FILTER_LINEAR = 0, 1
 RNG_REF_LCG, RNG_PCG32 = 0, 1
 RENDER_NO_MATERIAL_SORT, RENDER_COUNTERS, RENDER_NO_GRAPH, RENDER_KERNEL_TIMING = 1, 2, 4, 8
 RENDER_DROP_NONFINITE = 16
@@ -32,7 +34,8 @@ LOBE_DELTA = (1 << 5) | (1 << 6)
 
 class TextureDesc(C.Structure):
     _fields_ = [("type", C.c_uint32), ("color0", C.c_float * 3), ("color1", C.c_float * 3),
-                ("uv_transform", C.c_float * 8)]
+                ("uv_transform", C.c_float * 8), ("pixels", C.c_void_p), ("width", C.c_uint32),
+                ("height", C.c_uint32), ("address_mode", C.c_uint32), ("filter", C.c_uint32)]
 
 
 class MaterialDesc(C.Structure):
@@ -60,7 +63,8 @@ class CameraDesc(C.Structure):
 
 
 class EnvDesc(C.Structure):
-    _fields_ = [("type", C.c_uint32), ("radiance", C.c_float * 3)]
+    _fields_ = [("type", C.c_uint32), ("radiance", C.c_float * 3), ("pixels", C.c_void_p), ("width", C.c_uint32),
+                ("height", C.c_uint32), ("scale", C.c_float), ("to_world", C.c_float * 16)]
 
 
 class SceneDesc(C.Structure):

@@ -433,6 +433,10 @@ PT_DI float3 texture_sample(const DevTexture &t, float2 uv) {
         bool first = tx > 0.5f ? ty > 0.5f : !(ty > 0.5f);
         return first ? f3(t.c0[0], t.c0[1], t.c0[2]) : f3(t.c1[0], t.c1[1], t.c1[2]);
     }
+    if (t.type == PT_TEX_BITMAP) {
+        const float4 c = tex2D<float4>(static_cast<cudaTextureObject_t>(t.obj), tx, ty);
+        return f3(c.x, c.y, c.z);
+    }
     return f3(t.c0[0], t.c0[1], t.c0[2]);
 }
 
@@ -521,6 +525,61 @@ PT_DI void emitter_sample_direct(const DevEmitter &e, float3 pos, float3 nrm, fl
         r.distance = kMaxDistance;
         r.radiance = xyz(e.rad);
     }
+}
+
+// First i in [0, n) with x <= cdf[i], else n (the linear scans of
+// EnvMapEmitter::SampleDirect, env.h:24-31, over non-decreasing running sums).
+PT_DI uint32_t cdf_first_geq(const float *cdf, uint32_t n, float x) {
+    uint32_t lo = 0, hi = n;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (x <= __ldg(cdf + mid)) hi = mid;
+        else lo = mid + 1;
+    }
+    return lo;
+}
+
+PT_DI float3 envmap_lookup(const DevEnvMap &m, float2 tex) {
+    const float4 c = tex2D<float4>(static_cast<cudaTextureObject_t>(m.tex), tex.x, tex.y);
+    return f3(c.x, c.y, c.z) * m.scale;
+}
+
+// EnvMapEmitter::SampleDirect (env.h:23-49).  As in the reference the search
+// returns the index after the interval xi falls in (row_cdf[0] = 0), so the
+// last row selects index h; the reference then reads one row past the column
+// table and row_weight[h], past their ends.  Here those two reads use row
+// h - 1 instead.
+PT_DI void envmap_sample_direct(const DevEnvMap &m, float2 xi, EmitterSample &r) {
+    const uint32_t row = cdf_first_geq(m.row_cdf, m.h, xi.x);
+    const uint32_t crow = min(row, m.h - 1);
+    const uint32_t col = cdf_first_geq(m.col_cdf + (size_t)crow * (m.w + 1), m.w - 1, xi.y);
+    const float phi = static_cast<float>(col) * kPi * 2.f / static_cast<float>(m.w);
+    const float theta = static_cast<float>(row) * kPi / static_cast<float>(m.h);
+    const float st = sinf(theta);
+    const float3 local = f3(st * sinf(kPi - phi), cosf(theta), st * cosf(kPi - phi));
+    r.wi = f3(dot(xyz(m.to_world[0]), local), dot(xyz(m.to_world[1]), local), dot(xyz(m.to_world[2]), local));
+    r.distance = kMaxDistance;
+    r.radiance = envmap_lookup(m, make_float2(phi * 0.5f * kInvPi, theta * kInvPi));
+    r.pdf = luminance(r.radiance) * __ldg(m.row_weight + crow) * m.normalization / fmaxf(1e-4f, fabsf(st));
+    if (r.pdf < 0.f) r.pdf = 0.f;
+}
+
+// EnvMapEmitter::Eval (env.h:51-64) for a ray leaving scatter_pos along d:
+// the emitter point is scatter_pos + d, as the miss program builds it
+// (main.cu:204-208).
+PT_DI void envmap_eval(const DevEnvMap &m, float3 scatter_pos, float3 d, float3 &radiance, float &pdf) {
+    const float3 pos = scatter_pos + d;
+    float3 dir = normalize(pos - scatter_pos);
+    dir = f3(dot(xyz(m.to_local[0]), dir), dot(xyz(m.to_local[1]), dir), dot(xyz(m.to_local[2]), dir));
+    const float phi = kPi - atan2f(dir.x, dir.z);
+    const float theta = acosf(dir.y);
+    const float2 tex = make_float2(phi * 0.5f * kInvPi, theta * kInvPi);
+    uint32_t row = static_cast<uint32_t>(tex.y * static_cast<float>(m.h));
+    row = min(row, m.h - 2u);
+    radiance = envmap_lookup(m, tex);
+    const float w0 = __ldg(m.row_weight + row), w1 = __ldg(m.row_weight + row + 1);
+    const float t = tex.y * static_cast<float>(m.h) - 1.f * static_cast<float>(row);
+    pdf = luminance(radiance) * (w0 + t * (w1 - w0)) * m.normalization / fmaxf(1e-4f, fabsf(sinf(theta)));
 }
 
 // Emitter::Eval at an emitter hit (area.h:37-45, sphere.h:34-42): pdf 0 if it faces away.

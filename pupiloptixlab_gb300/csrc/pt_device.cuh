@@ -129,7 +129,9 @@ struct DevTexture {
     float c0[3];
     float c1[3];
     float pad;
-    float4 r0, r1;  // rows 0 and 1 of the uv transform
+    float4 r0, r1;          // rows 0 and 1 of the uv transform
+    unsigned long long obj; // bitmap: cudaTextureObject_t (float4, normalized coordinates)
+    unsigned long long pad2;
 };
 
 // Material (optix::material::Material + host precompute): 8 + 4*16 words.
@@ -144,7 +146,19 @@ struct DevMaterial {
     DevTexture tex[4];
 };
 
-enum : uint32_t { kEmitNone = 0, kEmitTri = 1, kEmitSphere = 2, kEmitConstEnv = 3 };
+enum : uint32_t { kEmitNone = 0, kEmitTri = 1, kEmitSphere = 2, kEmitConstEnv = 3, kEmitEnvMap = 4 };
+
+// EnvMapEmitter (framework/render/emitter/env.h:6-65) and its CDF tables
+// (framework/world/emitter.cpp:107-149).
+struct DevEnvMap {
+    unsigned long long tex;  // cudaTextureObject_t: float4, bilinear, wrap, normalized coordinates
+    const float *row_cdf;    // h + 1
+    const float *col_cdf;    // (w + 1) * h
+    const float *row_weight; // h
+    uint32_t w, h;
+    float normalization, scale;
+    float4 to_world[3], to_local[3];  // rows (xyz)
+};
 
 // Emitter (optix::Emitter, framework/render/emitter.h:13-29): 8 float4.
 struct DevEmitter {
@@ -189,7 +203,8 @@ struct DevScene {
     uint32_t num_emitters;
     uint32_t num_tris;
     uint32_t has_env;
-    DevEmitter env;
+    DevEmitter env;        // type kEmitConstEnv or kEmitEnvMap (then envmap holds the map)
+    DevEnvMap envmap;
     // camera (row-major 4x4 each)
     float4 s2c[4];
     float4 c2w[4];

@@ -105,6 +105,16 @@ struct pt_scene {
     DevBuf all_obj_pos;     // host positions staged for pt_scene_update_all_vertices
     uint64_t total_mesh_vertices = 0;
     std::vector<EmitterSource> emitter_sources;
+    // bitmap textures: one CUDA texture object per distinct (pixels, size, modes)
+    struct BitmapTexture {
+        const float *pixels;
+        uint32_t w, h, address, filter;
+        cudaArray_t array;
+        cudaTextureObject_t obj;
+    };
+    std::vector<BitmapTexture> bitmaps;
+    DevBuf env_row_cdf, env_col_cdf, env_row_weight;
+    uint32_t env_type = 0;  // PT_ENV_*
     bool has_env = false;
     float env_radiance[3] = {0, 0, 0};
     bool has_emissive_mesh = false;

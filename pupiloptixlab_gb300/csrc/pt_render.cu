@@ -389,9 +389,12 @@ PT_DI void shade_one(const DevScene &s, const Outputs &out, const State &st, con
     LocalBsdf bsdf;
     if (!alive) {  // __miss__default (main.cu:199-215)
         if (s.has_env) {
-            float3 le = xyz(s.env.rad);
+            float3 le;
+            float epdf = env_pdf;
+            if (emitter_type(s.env) == kEmitEnvMap) envmap_eval(s.envmap, ro, normalize(rd), le, epdf);
+            else le = xyz(s.env.rad);
             if (depth == 0) rad = rad + le;
-            else rad = rad + le * (thr * mis_weight(prev_pdf, env_pdf));
+            else rad = rad + le * (thr * mis_weight(prev_pdf, epdf));
         }
         if (depth == 0 && last) {
             if (out.albedo) { out.albedo[3 * p] = 0.f; out.albedo[3 * p + 1] = 0.f; out.albedo[3 * p + 2] = 0.f; }
@@ -439,7 +442,8 @@ PT_DI void shade_one(const DevScene &s, const Outputs &out, const State &st, con
         if (ei != -2) {
             const DevEmitter &e = ei >= 0 ? s.emitters[ei] : s.env;
             EmitterSample es;
-            emitter_sample_direct(e, g.pos, g.nrm, xi, es);
+            if (ei < 0 && emitter_type(e) == kEmitEnvMap) envmap_sample_direct(s.envmap, xi, es);
+            else emitter_sample_direct(e, g.pos, g.nrm, xi, es);
             if (es.pdf != 0.f) {
                 BsdfRecord er;
                 er.wi = to_local(es.wi, g.nrm);

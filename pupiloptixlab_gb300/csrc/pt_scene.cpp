@@ -85,7 +85,56 @@ float diffuse_reflectance(float eta) {
 H3 tex_average(const pt_texture_desc &t) {  // GetPixelAverage (optix_material.cpp:8-35)
     if (t.type == PT_TEX_CHECKERBOARD)
         return {(t.color0[0] + t.color1[0]) * 0.5f, (t.color0[1] + t.color1[1]) * 0.5f, (t.color0[2] + t.color1[2]) * 0.5f};
+    if (t.type == PT_TEX_BITMAP) {  // RGB sums in row-major order, divided by (1.f * h) * w
+        float r = 0.f, g = 0.f, b = 0.f;
+        size_t idx = 0;
+        for (uint32_t y = 0; y < t.height; y++)
+            for (uint32_t x = 0; x < t.width; x++) {
+                r += t.pixels[idx++];
+                g += t.pixels[idx++];
+                b += t.pixels[idx++];
+                idx++;
+            }
+        const float n = 1.f * t.height * t.width;
+        return {r / n, g / n, b / n};
+    }
     return {t.color0[0], t.color0[1], t.color0[2]};
+}
+
+// A float4 CUDA texture object over an RGBA float bitmap, made as the
+// reference makes it (framework/cuda/texture.cpp:60-102): normalized
+// coordinates, element reads, the given address and filter modes.
+int bitmap_texture(pt_scene *s, const float *pixels, uint32_t w, uint32_t h, uint32_t address, uint32_t filter,
+                   cudaTextureObject_t *out) {
+    for (const auto &b : s->bitmaps)
+        if (b.pixels == pixels && b.w == w && b.h == h && b.address == address && b.filter == filter) {
+            *out = b.obj;
+            return PT_OK;
+        }
+    pt_scene::BitmapTexture b{pixels, w, h, address, filter, nullptr, 0};
+    cudaChannelFormatDesc ch = cudaCreateChannelDesc<float4>();
+    PT_CUDA_TRY(cudaMallocArray(&b.array, &ch, w, h));
+    s->bitmaps.push_back(b);  // owned from here on (freed with the scene)
+    const size_t pitch = (size_t)w * 4 * sizeof(float);
+    PT_CUDA_TRY(cudaMemcpy2DToArray(b.array, 0, 0, pixels, pitch, pitch, h, cudaMemcpyHostToDevice));
+    cudaResourceDesc rd{};
+    rd.resType = cudaResourceTypeArray;
+    rd.res.array.array = b.array;
+    cudaTextureDesc td{};
+    td.addressMode[0] = static_cast<cudaTextureAddressMode>(address);
+    td.addressMode[1] = static_cast<cudaTextureAddressMode>(address);
+    td.filterMode = static_cast<cudaTextureFilterMode>(filter);
+    td.readMode = cudaReadModeElementType;
+    td.normalizedCoords = 1;
+    td.maxAnisotropy = 1;
+    td.maxMipmapLevelClamp = 99;
+    td.minMipmapLevelClamp = 0;
+    td.mipmapFilterMode = cudaFilterModePoint;
+    td.borderColor[0] = 1.0f;
+    td.sRGB = 0;
+    PT_CUDA_TRY(cudaCreateTextureObject(&s->bitmaps.back().obj, &rd, &td, nullptr));
+    *out = s->bitmaps.back().obj;
+    return PT_OK;
 }
 
 DevTexture to_dev(const pt_texture_desc &t) {
@@ -125,11 +174,18 @@ int validate(const pt_scene_desc *d) {
             pt_set_error("material %u has unknown type %u", i, m.type);
             return PT_ERR_INVALID;
         }
-        for (int k = 0; k < 4; k++)
-            if (m.tex[k].type != PT_TEX_RGB && m.tex[k].type != PT_TEX_CHECKERBOARD) {
-                pt_set_error("material %u texture %d: only RGB and checkerboard textures are supported", i, k);
-                return PT_ERR_UNSUPPORTED;
+        for (int k = 0; k < 4; k++) {
+            const pt_texture_desc &t = m.tex[k];
+            if (t.type != PT_TEX_RGB && t.type != PT_TEX_CHECKERBOARD && t.type != PT_TEX_BITMAP) {
+                pt_set_error("material %u texture %d: unknown texture type %u", i, k, t.type);
+                return PT_ERR_INVALID;
             }
+            if (t.type == PT_TEX_BITMAP &&
+                (!t.pixels || !t.width || !t.height || t.address_mode > PT_TEX_ADDRESS_MIRROR || t.filter > PT_TEX_FILTER_LINEAR)) {
+                pt_set_error("material %u texture %d: bitmap without pixels, of zero size or with unknown modes", i, k);
+                return PT_ERR_INVALID;
+            }
+        }
     }
     for (uint32_t i = 0; i < d->num_meshes; i++) {
         const pt_mesh_desc &m = d->meshes[i];
@@ -164,9 +220,13 @@ int validate(const pt_scene_desc *d) {
         for (int k = 0; k < 16; k++)
             if (!std::isfinite(in.to_world[k])) { pt_set_error("instance %u: non-finite transform", i); return PT_ERR_INVALID; }
     }
-    if (d->env.type != PT_ENV_NONE && d->env.type != PT_ENV_CONST) {
+    if (d->env.type != PT_ENV_NONE && d->env.type != PT_ENV_CONST && d->env.type != PT_ENV_MAP) {
         pt_set_error("environment type %u not supported", d->env.type);
         return PT_ERR_UNSUPPORTED;
+    }
+    if (d->env.type == PT_ENV_MAP && (!d->env.pixels || d->env.width < 2 || d->env.height < 2)) {
+        pt_set_error("environment map without pixels or smaller than 2x2");
+        return PT_ERR_INVALID;
     }
     return PT_OK;
 }
@@ -180,6 +240,58 @@ void set_camera(pt_scene *s, const pt_camera_desc &c) {
     }
     float cm = std::max({fabsf(c.camera_to_world[3]), fabsf(c.camera_to_world[7]), fabsf(c.camera_to_world[11])});
     s->scene_mag = std::max(s->scene_mag, cm);
+}
+
+// Environment map: texture object (bilinear, wrap) and the luminance CDF
+// tables of BuildEnvMapCdfTable (framework/world/emitter.cpp:107-149), with
+// the same float arithmetic in the same order.
+int build_env_map(pt_scene *s, const pt_env_desc &e) {
+    const size_t w = e.width, h = e.height;
+    std::vector<float> col_cdf((w + 1) * h), row_cdf(h + 1), row_weight(h);
+    size_t ci = 0, ri = 0;
+    float row_sum = 0.f;
+    row_cdf[ri++] = 0.f;
+    for (size_t y = 0; y < h; ++y) {
+        float col_sum = 0.f;
+        col_cdf[ci++] = 0.f;
+        for (size_t x = 0; x < w; ++x) {
+            const size_t px = y * w + x;
+            const float r = e.pixels[px * 4 + 0], g = e.pixels[px * 4 + 1], b = e.pixels[px * 4 + 2];
+            col_sum += 0.2126f * r + 0.7152f * g + 0.0722f * b;  // GetLuminance
+            col_cdf[ci++] = col_sum;
+        }
+        for (size_t x = 1; x < w; ++x) col_cdf[ci - x - 1] /= col_sum;
+        col_cdf[ci - 1] = 1.f;
+        const float weight = std::sin((y + 0.5f) * 3.14159265358979323846f / h);
+        row_weight[y] = weight;
+        row_sum += col_sum * weight;
+        row_cdf[ri++] = row_sum;
+    }
+    for (size_t y = 1; y < h; ++y) row_cdf[ri - y - 1] /= row_sum;
+    row_cdf[ri - 1] = 1.f;
+    int st;
+    if ((st = upload(s->env_row_cdf, row_cdf)) != PT_OK || (st = upload(s->env_col_cdf, col_cdf)) != PT_OK ||
+        (st = upload(s->env_row_weight, row_weight)) != PT_OK)
+        return st;
+    cudaTextureObject_t obj = 0;
+    if ((st = bitmap_texture(s, e.pixels, e.width, e.height, PT_TEX_ADDRESS_WRAP, PT_TEX_FILTER_LINEAR, &obj)) != PT_OK)
+        return st;
+    ptd::DevEnvMap &m = s->dev.envmap;
+    m.tex = static_cast<unsigned long long>(obj);
+    m.row_cdf = s->env_row_cdf.as<float>();
+    m.col_cdf = s->env_col_cdf.as<float>();
+    m.row_weight = s->env_row_weight.as<float>();
+    m.w = e.width;
+    m.h = e.height;
+    m.normalization = 1.f / (row_sum * (2.f * 3.14159265358979323846f / w) * (3.14159265358979323846f / h));
+    m.scale = e.scale;
+    double inv[16];
+    inverse4f(e.to_world, inv);
+    for (int r = 0; r < 3; r++) {
+        m.to_world[r] = make_float4(e.to_world[4 * r], e.to_world[4 * r + 1], e.to_world[4 * r + 2], 0.f);
+        m.to_local[r] = make_float4((float)inv[4 * r], (float)inv[4 * r + 1], (float)inv[4 * r + 2], 0.f);
+    }
+    return PT_OK;
 }
 
 int build_scene(pt_scene *s, const pt_scene_desc *d) {
@@ -305,7 +417,16 @@ int build_scene(pt_scene *s, const pt_scene_desc *d) {
             dm.spec_weight = sl / (sl + dl);
             dm.int_fdr = diffuse_reflectance(1.f / dm.eta);
         }
-        for (int k = 0; k < 4; k++) dm.tex[k] = to_dev(m.tex[k]);
+        for (int k = 0; k < 4; k++) {
+            dm.tex[k] = to_dev(m.tex[k]);
+            if (m.tex[k].type == PT_TEX_BITMAP) {
+                cudaTextureObject_t obj = 0;
+                const pt_texture_desc &t = m.tex[k];
+                int st = bitmap_texture(s, t.pixels, t.width, t.height, t.address_mode, t.filter, &obj);
+                if (st != PT_OK) return st;
+                dm.tex[k].obj = static_cast<unsigned long long>(obj);
+            }
+        }
     }
 
     // emissive instances in instance order (world/emitter.cpp:169-263)
@@ -340,8 +461,13 @@ int build_scene(pt_scene *s, const pt_scene_desc *d) {
         }
         s->emitter_sources.push_back(std::move(src));
     }
-    s->has_env = d->env.type == PT_ENV_CONST;
+    s->has_env = d->env.type != PT_ENV_NONE;
+    s->env_type = d->env.type;
     memcpy(s->env_radiance, d->env.radiance, sizeof(s->env_radiance));
+    if (d->env.type == PT_ENV_MAP) {
+        int st = build_env_map(s, d->env);
+        if (st != PT_OK) return st;
+    }
 
     int e;
     if ((e = upload(s->prims_world, prims)) != PT_OK) return e;
@@ -453,7 +579,7 @@ int pt_rebuild_emitters(pt_scene *s, const float4 *host_vpos) {
     }
     DevEmitter env{};
     if (s->has_env) {
-        uint32_t type = ptd::kEmitConstEnv;
+        uint32_t type = s->env_type == PT_ENV_MAP ? ptd::kEmitEnvMap : ptd::kEmitConstEnv;
         float tf;
         memcpy(&tf, &type, 4);
         env.a = make_float4(tf, 1.f / (float)n_emit, 0.f, 0.f);
@@ -508,6 +634,13 @@ pt_scene::~pt_scene() {
                      &ws.rad, &ws.rng, &ws.meta, &ws.q0, &ws.q1, &ws.sh_o, &ws.sh_d, &ws.sh_c, &ws.mat_key,
                      &ws.counters, &ws.sort_tmp};
     for (DevBuf *b : all) b->release();
+    env_row_cdf.release();
+    env_col_cdf.release();
+    env_row_weight.release();
+    for (auto &b : bitmaps) {
+        if (b.obj) cudaDestroyTextureObject(b.obj);
+        if (b.array) cudaFreeArray(b.array);
+    }
     if (ws.exec) cudaGraphExecDestroy(ws.exec);
     if (ws.ev_in) cudaEventDestroy(ws.ev_in);
     if (ws.ev_out) cudaEventDestroy(ws.ev_out);

@@ -1,0 +1,23 @@
+// image.h -- image readers for bitmap textures and environment maps.
+//
+// The reference loads images through stb_image (PNG/JPEG/... and Radiance
+// .hdr) and tinyexr (framework/util/texture.cpp:87-151); neither library is
+// part of this project.  This reader covers the floating-point formats:
+//   .hdr  Radiance RGBE (flat or run-length encoded scanlines): value =
+//         mantissa * 2^(exponent - 136), 0 when the exponent byte is 0;
+//   .pfm  portable float map (PF colour / Pf grey, either byte order, rows
+//         stored bottom-up in the file);
+// both returned as RGBA floats, alpha 1, first row = top of the image, as
+// util::BitmapTexture holds them.  Other formats are reported as unsupported.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace Pupil::util {
+
+bool LoadImageRGBA(const std::string &path, std::vector<float> &rgba, uint32_t &width, uint32_t &height,
+                   std::string &error);
+
+}  // namespace Pupil::util

@@ -7,6 +7,7 @@
 // 128-210 (transforms: matrix of 16 or 9 values, lookat, or scale then rotate
 // then translate, each left-multiplied).
 #include "scene.h"
+#include "image.h"
 
 #include <cmath>
 #include <cstring>
@@ -158,6 +159,30 @@ struct Loader {
         }
         return true;
     }
+    // the scale of a texture's to_uv transform
+    void uv_scale(const xml::Node *c, pt_texture_desc &out) {
+        for (auto &t : c->children)
+            if (t->name == "transform" && t->attr_or("name", "") == "to_uv") {
+                for (auto &sc : t->children)
+                    if (sc->name == "scale") {
+                        float x = 1.f, y = 1.f;
+                        if (sc->attr("value")) {
+                            auto v = numbers(value(sc.get()));
+                            x = v.empty() ? 1.f : v[0];
+                            y = v.size() > 1 ? v[1] : x;
+                        } else {
+                            x = std::stof(sc->attr_or("x", "1"));
+                            y = std::stof(sc->attr_or("y", "1"));
+                        }
+                        out.uv_transform[0] = x;
+                        out.uv_transform[5] = y;
+                    }
+            }
+    }
+    std::string m_root_path(const std::string &file) {
+        if (file.empty() || file[0] == '/' || s.m_root.empty()) return file;
+        return s.m_root + "/" + file;
+    }
     // rgb / float / checkerboard texture (LoadTextureOrRGB)
     bool get_texture(const xml::Node *n, const char *name, pt_texture_desc &out, pt_texture_desc fallback) {
         out = fallback;
@@ -176,6 +201,29 @@ struct Loader {
                 out = rgb(v[0], v[0], v[0]);
                 return true;
             }
+            if (c->name == "texture" && c->attr_or("type", "") == "bitmap") {  // scene.cpp:143-166
+                const xml::Node *fn = prop(c.get(), "string", "filename");
+                if (!fn) return fail(c.get(), "bitmap texture without a filename");
+                std::vector<float> px;
+                uint32_t w = 0, h = 0;
+                std::string e;
+                if (!util::LoadImageRGBA(m_root_path(value(fn)), px, w, h, e)) return fail(c.get(), e);
+                s.images.push_back(std::move(px));
+                out = rgb(0.f, 0.f, 0.f);
+                out.type = PT_TEX_BITMAP;
+                out.pixels = s.images.back().data();
+                out.width = w;
+                out.height = h;
+                const xml::Node *ft = prop(c.get(), "string", "filter_type");
+                out.filter = (ft && value(ft) == "bilinear") ? PT_TEX_FILTER_LINEAR : PT_TEX_FILTER_POINT;
+                const xml::Node *wm = prop(c.get(), "string", "wrap_mode");
+                const std::string mode = wm ? value(wm) : "repeat";
+                out.address_mode = mode == "mirror" ? PT_TEX_ADDRESS_MIRROR
+                                   : mode == "clamp" ? PT_TEX_ADDRESS_CLAMP
+                                                     : PT_TEX_ADDRESS_WRAP;
+                uv_scale(c.get(), out);
+                return true;
+            }
             if (c->name == "texture") {
                 std::string type = c->attr_or("type", "");
                 if (type != "checkerboard") return fail(c.get(), "texture type '" + type + "' is not supported");
@@ -186,23 +234,7 @@ struct Loader {
                 if (!get_texture(c.get(), "color1", c1, rgb(0.2f, 0.2f, 0.2f))) return false;
                 memcpy(out.color0, c0.color0, sizeof(out.color0));
                 memcpy(out.color1, c1.color0, sizeof(out.color1));
-                for (auto &t : c->children)
-                    if (t->name == "transform" && t->attr_or("name", "") == "to_uv") {
-                        for (auto &sc : t->children)
-                            if (sc->name == "scale") {
-                                float x = 1.f, y = 1.f;
-                                if (sc->attr("value")) {
-                                    auto v = numbers(value(sc.get()));
-                                    x = v.empty() ? 1.f : v[0];
-                                    y = v.size() > 1 ? v[1] : x;
-                                } else {
-                                    x = std::stof(sc->attr_or("x", "1"));
-                                    y = std::stof(sc->attr_or("y", "1"));
-                                }
-                                out.uv_transform[0] = x;
-                                out.uv_transform[5] = y;
-                            }
-                    }
+                uv_scale(c.get(), out);
                 return true;
             }
         }
@@ -544,6 +576,26 @@ struct Loader {
                     if (!get_texture(n, "radiance", r, rgb(1, 1, 1))) return false;
                     s.has_env = true;
                     memcpy(s.env_radiance, r.color0, sizeof(s.env_radiance));
+                } else if (et == "envmap") {  // scene.cpp:208-221
+                    const xml::Node *fn = prop(n, "string", "filename");
+                    if (!fn) return fail(n, "envmap emitter without a filename");
+                    std::vector<float> px;
+                    uint32_t w = 0, h = 0;
+                    std::string e;
+                    if (!util::LoadImageRGBA(m_root_path(value(fn)), px, w, h, e)) return fail(n, e);
+                    s.images.push_back(std::move(px));
+                    s.env_map.on = true;
+                    s.env_map.image = s.images.size() - 1;
+                    s.env_map.width = w;
+                    s.env_map.height = h;
+                    s.env_map.scale = 1.f;
+                    if (const xml::Node *sc = prop(n, "float", "scale")) {
+                        auto v = numbers(value(sc));
+                        if (v.size() == 1) s.env_map.scale = v[0];
+                    }
+                    for (auto &t : n->children)
+                        if (t->name == "transform" && !transform(t.get(), s.env_map.to_world)) return false;
+                    s.has_env = true;
                 } else {
                     return fail(n, "emitter '" + et + "' is not supported");
                 }
@@ -615,6 +667,14 @@ const pt_scene_desc &Scene::Desc() {
     m_desc.num_instances = (uint32_t)m_inst_descs.size();
     m_desc.env.type = has_env ? PT_ENV_CONST : PT_ENV_NONE;
     memcpy(m_desc.env.radiance, env_radiance, sizeof(env_radiance));
+    if (env_map.on) {
+        m_desc.env.type = PT_ENV_MAP;
+        m_desc.env.pixels = images[env_map.image].data();
+        m_desc.env.width = env_map.width;
+        m_desc.env.height = env_map.height;
+        m_desc.env.scale = env_map.scale;
+        memcpy(m_desc.env.to_world, env_map.to_world, sizeof(env_map.to_world));
+    }
     m_desc.camera = Camera();
     m_desc.width = sensor.width;
     m_desc.height = sensor.height;

@@ -51,6 +51,15 @@ public:
     std::vector<ShapeInstance> shape_instances;
     bool has_env = false;
     float env_radiance[3] = {0, 0, 0};
+    // decoded bitmap images (RGBA float); textures and the environment map point into them
+    std::vector<std::vector<float>> images;
+    struct EnvMap {
+        bool on = false;
+        size_t image = 0;
+        uint32_t width = 0, height = 0;
+        float scale = 1.f;
+        float to_world[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+    } env_map;
 
     bool LoadFromXML(const std::string &path);
     bool LoadFromString(const std::string &text, const std::string &root_dir);

@@ -51,6 +51,36 @@ def checkerboard(patch1=(0.4, 0.4, 0.4), patch2=(0.2, 0.2, 0.2), uv_scale=1.0) -
     return t
 
 
+def bitmap(pixels: np.ndarray, address=abi.TEX_ADDRESS_WRAP, filter=abi.TEX_FILTER_LINEAR,
+           uv_scale=1.0) -> abi.TextureDesc:
+    """A bitmap texture over (h, w, 4) RGBA float32 pixels (row 0 first).  The
+    array must stay alive until the scene is uploaded: Scene.add_material keeps
+    it when the material is added through Scene."""
+    px = np.ascontiguousarray(pixels, np.float32)
+    assert px.ndim == 3 and px.shape[2] == 4
+    t = abi.TextureDesc()
+    t.type = abi.TEX_BITMAP
+    t.uv_transform[:] = (uv_scale, 0.0, 0.0, 0.0, 0.0, uv_scale, 0.0, 0.0)
+    t.pixels = px.ctypes.data
+    t.height, t.width = px.shape[0], px.shape[1]
+    t.address_mode = address
+    t.filter = filter
+    _BITMAP_KEEP[t.pixels] = px
+    return t
+
+
+# pixels of bitmap textures by address, kept alive for the scenes that use them
+_BITMAP_KEEP: dict = {}
+
+
+@dataclass
+class EnvMap:
+    """An equirectangular environment map: (h, w, 4) RGBA float32 radiance."""
+    pixels: np.ndarray
+    scale: float = 1.0
+    to_world: np.ndarray | None = None
+
+
 def _mat(type_, texs, int_ior=1.0, ext_ior=1.0, nonlinear=False, twosided=False) -> abi.MaterialDesc:
     m = abi.MaterialDesc()
     m.type = type_
@@ -191,7 +221,7 @@ class Scene:
     spheres: list = field(default_factory=list)     # (center(3), radius)
     materials: list = field(default_factory=list)   # abi.MaterialDesc
     instances: list = field(default_factory=list)   # dicts
-    env: tuple | None = None                         # constant environment radiance
+    env: tuple | EnvMap | None = None                # constant environment radiance or a map
     camera: abi.CameraDesc | None = None
     name: str = "scene"
 
@@ -257,7 +287,16 @@ class Scene:
         sd.num_materials = len(self.materials)
         sd.instances = C.cast(insts, C.POINTER(abi.InstanceDesc))
         sd.num_instances = len(self.instances)
-        if self.env is not None:
+        if isinstance(self.env, EnvMap):
+            px = np.ascontiguousarray(self.env.pixels, np.float32)
+            keep.append(px)
+            sd.env.type = abi.ENV_MAP
+            sd.env.pixels = px.ctypes.data
+            sd.env.height, sd.env.width = px.shape[0], px.shape[1]
+            sd.env.scale = float(self.env.scale)
+            tw = np.eye(4) if self.env.to_world is None else np.asarray(self.env.to_world, np.float64)
+            sd.env.to_world[:] = [float(v) for v in tw.astype(np.float32).reshape(-1)]
+        elif self.env is not None:
             sd.env.type = abi.ENV_CONST
             sd.env.radiance[:] = [float(v) for v in self.env]
         if self.camera is not None:

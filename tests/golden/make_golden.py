@@ -157,6 +157,36 @@ def main():
     ref.ref_select_emitter(P(probs), len(probs), 0, P(pv), P(sel_noenv), 2000)
     g.update(select_probs=probs, select_p=pv, select_env=sel_env, select_noenv=sel_noenv)
 
+    # environment map: a 24 x 12 map with a bright patch, rotated 30 degrees
+    # about y, sampled (xi drawn below the last row's interval: the reference
+    # reads past its tables for that row) and evaluated in random directions
+    import oracle as orc
+    ew, eh = 24, 12
+    emap = rng.uniform(0.05, 0.5, (eh, ew, 4)).astype(np.float32)
+    emap[3:5, 15:18, :3] = [[30.0, 25.0, 20.0]]
+    emap[:, :, 3] = 1.0
+    ang = np.radians(30.0)
+    tw = np.array([[np.cos(ang), 0, np.sin(ang)], [0, 1, 0], [-np.sin(ang), 0, np.cos(ang)]], np.float32)
+    tl = np.linalg.inv(tw.astype(np.float64)).astype(np.float32)
+    _, tables = orc.envmap(0, emap, 1.5, tw, tl, np.zeros((1, 2), np.float32))
+    row_cdf = tables[:eh + 1].copy()
+    col_cdf = tables[eh + 1:eh + 1 + (ew + 1) * eh].copy()
+    row_weight = tables[eh + 1 + (ew + 1) * eh:eh + 1 + (ew + 1) * eh + eh].copy()
+    norm = float(tables[-1])
+    xi = rng.uniform(0, 1, (m, 2)).astype(np.float32)
+    xi[:, 0] *= row_cdf[eh - 1]
+    xi[:4] = [[0.0, 0.0], [row_cdf[3], 0.5], [0.5, 0.0], [row_cdf[eh - 1], 0.999]]
+    es = np.zeros((m, 7), np.float32)
+    ref.ref_envmap(0, P(emap), ew, eh, 1.5, P(tw), P(tl), P(row_cdf), P(col_cdf), P(row_weight), norm, P(xi), P(es), m)
+    ev_in = np.zeros((m, 6), np.float32)
+    ev_in[:, 0:3] = rng.uniform(-2, 2, (m, 3))
+    ev_in[:, 3:6] = unit(rng.normal(size=(m, 3)))
+    ev = np.zeros((m, 4), np.float32)
+    ref.ref_envmap(1, P(emap), ew, eh, 1.5, P(tw), P(tl), P(row_cdf), P(col_cdf), P(row_weight), norm, P(ev_in),
+                   P(ev), m)
+    g.update(envmap_pixels=emap, envmap_tw=tw, envmap_tl=tl, envmap_xi=xi, envmap_sample=es, envmap_eval_in=ev_in,
+             envmap_eval=ev)
+
     np.savez_compressed(OUT, **g)
     print(f"wrote {OUT} ({OUT.stat().st_size} bytes, {len(g)} arrays)")
 

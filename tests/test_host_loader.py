@@ -121,9 +121,12 @@ def test_obj_mesh(host):
     ("<scene><shape type='cube'>", "unexpected end"),
     ("<scene><bsdf type='velvet' id='a'/></scene>", "unknown bsdf"),
     ("<scene><shape type='cube'><ref id='nope'/></shape></scene>", "unknown bsdf id"),
-    ("<scene><emitter type='envmap'/></scene>", "not supported"),
+    ("<scene><emitter type='envmap'/></scene>", "without a filename"),
+    ("<scene><emitter type='point'/></scene>", "not supported"),
     ("<scene><shape type='rectangle'><bsdf type='diffuse'><texture type='bitmap' name='reflectance'/>"
-     "</bsdf></shape></scene>", "not supported"),
+     "</bsdf></shape></scene>", "without a filename"),
+    ("<scene><shape type='rectangle'><bsdf type='diffuse'><texture type='bitmap' name='reflectance'>"
+     "<string name='filename' value='a.png'/></texture></bsdf></shape></scene>", ".hdr (RGBE) and .pfm"),
     ("<scene><sensor type='thinlens'/></scene>", "perspective"),
     ("<notascene/>", "<scene>"),
     ("<scene><a></b></scene>", "mismatched"),
@@ -142,3 +145,96 @@ def test_loaded_scene_feeds_the_oracle(host):
     assert nt == 5 * 2 + 2 * 12 + 2 and ns == 0
     out = o.render(abi.RenderParams(spp=2, seed=0, accumulate=1, rng=abi.RNG_REF_LCG))
     assert np.isfinite(out["accum"]).all() and out["accum"][:, :3].mean() > 0
+
+
+def _write_pfm(path, img, little=True):
+    """img (h, w, 3) float32, top row first; PFM stores rows bottom-up."""
+    h, w, _ = img.shape
+    data = img[::-1].astype("<f4" if little else ">f4").tobytes()
+    path.write_bytes(f"PF\n{w} {h}\n{-1.0 if little else 1.0}\n".encode() + data)
+
+
+def _rgbe(rgb):
+    """float RGB -> RGBE bytes (mantissa = value * 2^(136 - e))."""
+    out = np.zeros(rgb.shape[:-1] + (4,), np.uint8)
+    m = rgb.max(axis=-1)
+    nz = m > 1e-32
+    e = np.floor(np.log2(np.where(nz, m, 1.0))).astype(np.int32) + 1
+    scale = np.ldexp(1.0, 8 - e)
+    out[..., :3] = np.where(nz[..., None], np.clip(np.floor(rgb * scale[..., None]), 0, 255), 0).astype(np.uint8)
+    out[..., 3] = np.where(nz, e + 128, 0).astype(np.uint8)
+    return out
+
+
+def _write_hdr(path, img, rle=True):
+    h, w, _ = img.shape
+    px = _rgbe(img)
+    body = bytearray()
+    for y in range(h):
+        if rle:
+            body += bytes([2, 2, w >> 8, w & 255])
+            for c in range(4):
+                row = px[y, :, c]
+                x = 0
+                while x < w:  # runs of equal bytes (>= 3) or literals
+                    run = 1
+                    while x + run < w and run < 127 and row[x + run] == row[x]:
+                        run += 1
+                    if run >= 3:
+                        body += bytes([128 + run, int(row[x])])
+                        x += run
+                    else:
+                        n = min(128, w - x)
+                        body += bytes([n]) + bytes(int(v) for v in row[x:x + n])
+                        x += n
+        else:
+            body += px[y].tobytes()
+    path.write_bytes(b"#?RADIANCE\nFORMAT=32-bit_rle_rgbe\n\n" + f"-Y {h} +X {w}\n".encode() + bytes(body))
+
+
+def test_bitmap_texture_and_envmap_images(host, tmp_path):
+    """bitmap textures (.pfm) and an envmap emitter (.hdr, RLE and flat) load
+    into the descriptor with the reference's sampling modes."""
+    rng = np.random.default_rng(3)
+    tex = rng.uniform(0, 1, (6, 9, 3)).astype(np.float32)
+    env = rng.uniform(0, 4, (8, 16, 3)).astype(np.float32)
+    env[2, 3:9] = [5.0, 5.0, 5.0]  # a run for the RLE encoder
+    _write_pfm(tmp_path / "tex.pfm", tex)
+    _write_pfm(tmp_path / "texbig.pfm", tex, little=False)
+    _write_hdr(tmp_path / "env.hdr", env, rle=True)
+    _write_hdr(tmp_path / "envflat.hdr", env, rle=False)
+    for envfile in ("env.hdr", "envflat.hdr"):
+        xml = f"""<scene version="3.0.0">
+          <integrator type="path"><integer name="max_depth" value="4"/></integrator>
+          <sensor type="perspective"><float name="fov" value="40"/>
+            <film type="hdrfilm"><integer name="width" value="32"/><integer name="height" value="24"/></film></sensor>
+          <bsdf type="diffuse" id="floor"><texture type="bitmap" name="reflectance">
+            <string name="filename" value="tex.pfm"/><string name="filter_type" value="bilinear"/>
+            <string name="wrap_mode" value="mirror"/>
+            <transform name="to_uv"><scale value="3"/></transform></texture></bsdf>
+          <bsdf type="diffuse" id="wall"><texture type="bitmap" name="reflectance">
+            <string name="filename" value="texbig.pfm"/><string name="filter_type" value="nearest"/></texture></bsdf>
+          <shape type="rectangle"><ref id="floor"/></shape>
+          <shape type="rectangle"><ref id="wall"/></shape>
+          <emitter type="envmap"><string name="filename" value="{envfile}"/><float name="scale" value="2.5"/>
+            <transform name="to_world"><rotate y="1" angle="90"/></transform></emitter>
+        </scene>"""
+        (tmp_path / "s.xml").write_text(xml)
+        s = host.XmlScene(str(tmp_path / "s.xml"))
+        d = s.desc()
+        t0, t1 = d.materials[0].tex[0], d.materials[1].tex[0]
+        assert (t0.type, t0.width, t0.height) == (abi.TEX_BITMAP, 9, 6)
+        assert (t0.filter, t0.address_mode) == (abi.TEX_FILTER_LINEAR, abi.TEX_ADDRESS_MIRROR)
+        assert (t1.filter, t1.address_mode) == (abi.TEX_FILTER_POINT, abi.TEX_ADDRESS_WRAP)
+        assert t0.uv_transform[0] == 3.0 and t0.uv_transform[5] == 3.0
+        for t in (t0, t1):
+            px = np.ctypeslib.as_array(C.cast(t.pixels, C.POINTER(C.c_float)), shape=(6, 9, 4))
+            assert np.array_equal(px[..., :3], tex) and np.all(px[..., 3] == 1.0)
+        e = d.env
+        assert (e.type, e.width, e.height, e.scale) == (abi.ENV_MAP, 16, 8, 2.5)
+        px = np.ctypeslib.as_array(C.cast(e.pixels, C.POINTER(C.c_float)), shape=(8, 16, 4))
+        q = _rgbe(env).astype(np.float64)
+        expect = q[..., :3] * np.ldexp(1.0, q[..., 3:4].astype(np.int32) - 136)
+        assert np.allclose(px[..., :3], expect, rtol=0, atol=0)
+        tw = np.array(e.to_world[:]).reshape(4, 4)
+        assert np.allclose(tw[:3, :3], [[0, 0, 1], [0, 1, 0], [-1, 0, 0]], atol=1e-6)
