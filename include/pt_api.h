@@ -364,8 +364,9 @@ typedef struct pt_tune_result {
  * (all of one width) are merged into one node array for the launch, the
  * path slots of a wave cover every scene's pixels, and the shading queues
  * are shared and binned by (scene, material type).  Each scene gets the
- * image pt_render with the same params would give it (same random streams).
- * max_depth 0 means scene 0's depth.  Statistics: pt_render_batch_get_stats. */
+ * image pt_render with the same params would give it (same random streams);
+ * max_depth 0 means each scene's own depth.  Statistics:
+ * pt_render_batch_get_stats. */
 int pt_render_batch(pt_context *ctx, pt_scene *const *scenes, const pt_render_params *params,
                     const pt_frame_buffers *fbs, uint32_t n, void *stream);
 int pt_render_batch_get_stats(const pt_context *ctx, pt_render_stats *out);

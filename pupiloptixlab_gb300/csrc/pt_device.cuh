@@ -209,6 +209,7 @@ struct DevScene {
     float4 s2c[4];
     float4 c2w[4];
     uint32_t width_px, height_px;
+    uint32_t max_depth;  // the scene's integrator depth (used when a render asks for depth 0)
 };
 
 }  // namespace ptd

@@ -428,7 +428,7 @@ PT_DI void shade_one(const DevScene &s, const Outputs &out, const State &st, con
     }
     if (alive) {  // main.cu:107-109
         depth++;
-        if (depth >= w.max_depth) alive = false;
+        if (depth >= (w.max_depth ? w.max_depth : s.max_depth)) alive = false;
     }
     if (alive) {  // Russian roulette, main.cu:111-114
         float rr = depth > 2 ? 0.95f : 1.0f;
@@ -788,14 +788,17 @@ struct Launcher {
         RunTarget t{&s->ws, s->ev0, s->ev1, s->num_sms, s->tuned_block, s->tuned_wave_paths, &s->render_stats};
         const uint32_t max_depth = p->max_depth ? p->max_depth : s->desc_shallow.max_depth;
         const uint32_t npix = s->dev.width_px * s->dev.height_px;
-        return run_waves<false>(t, s->dev, Batch{}, npix, max_depth, p, make_outputs(fb, p->flags), st);
+        return run_waves<false>(t, s->dev, Batch{}, npix, max_depth, max_depth, p, make_outputs(fb, p->flags), st);
     }
 
     // Waves of frames over npix pixels (one scene, or the concatenated
     // pixels of a batch), each captured in a CUDA graph unless timing or
     // NO_GRAPH asks for direct launches.
     template <bool BATCH>
+    // max_depth goes to the kernels (0: each scene's own depth), bounces is the
+    // number of bounce launches per wave (the largest depth of the scenes).
     static int run_waves(const RunTarget &t, const DevScene &d, const Batch &bt, uint32_t npix, uint32_t max_depth,
+                         uint32_t bounces,
                          const pt_render_params *p, const Outputs &out, cudaStream_t st) {
         RenderWorkspace &ws = *t.wsp;
         const bool count = (p->flags & PT_RENDER_COUNTERS) != 0;
@@ -886,7 +889,7 @@ struct Launcher {
             const size_t slots = (size_t)w.frames * npix;
             k_raygen<BATCH><<<nblocks(slots, 256), 256, 0, ls>>>(d, bt, stt, w);
             launches++;
-            for (uint32_t b = 0; b < max_depth; b++) {
+            for (uint32_t b = 0; b < bounces; b++) {
                 if (timing) tm.mark(0, ls);
                 k_ext<<<grid_trace, tb, smem, ls>>>(d, stt, bt, npix);
                 if (timing) tm.mark(0, ls);
@@ -1146,10 +1149,14 @@ int render_batch(pt_context *ctx, pt_scene *const *scenes, const pt_render_param
     bt.n = n;
     bt.bins = b.bins.as<uint32_t>();
     bt.nbins = n * kNumBins;
-    const uint32_t max_depth = p->max_depth ? p->max_depth : scenes[0]->desc_shallow.max_depth;
+    const uint32_t max_depth = p->max_depth;  // 0: each scene's own depth (DevScene::max_depth)
+    uint32_t bounces = max_depth;
+    if (!bounces)
+        for (uint32_t k = 0; k < n; k++) bounces = std::max(bounces, scenes[k]->dev.max_depth);
     RunTarget t{&b.ws, b.ev0, b.ev1, ctx->num_sms, 0, 0, &b.stats};
     Outputs none{};
-    return Launcher<K>::template run_waves<true>(t, dt, bt, static_cast<uint32_t>(total_pix), max_depth, p, none, st);
+    return Launcher<K>::template run_waves<true>(t, dt, bt, static_cast<uint32_t>(total_pix), max_depth, bounces, p,
+                                                 none, st);
 }
 
 }  // namespace

@@ -492,6 +492,7 @@ int build_scene(pt_scene *s, const pt_scene_desc *d) {
     if ((e = pt_rebuild_emitters(s, vpos.data())) != PT_OK) return e;
     dv.width_px = d->width;
     dv.height_px = d->height;
+    dv.max_depth = d->max_depth;
     set_camera(s, d->camera);
     return PT_OK;
 }

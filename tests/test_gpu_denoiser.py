@@ -84,30 +84,51 @@ def test_gradients_match_cpu(dn):
         assert rel <= 6e-2 and cos >= 0.995, worst
 
 
-def test_training_reduces_loss(cuda_ctx):
-    """A smooth target under strong multiplicative noise: the network starts as
-    the identity (zero output layer) and must learn to smooth."""
+def test_training_follows_cpu_adam(cuda_ctx):
+    """Training end to end (forward, backward, Adam in the captured graph)
+    against PyTorch-CPU Adam on the CPU restatement of the network, from the
+    same initial weights: a smooth target under strong multiplicative noise.
+    The first 10 losses agree to 0.5 %; the run then drifts apart (BF16
+    activation gradients, chaotic dynamics) but both fall below half the
+    starting loss by step 70."""
+    from oracle import denoiser_ref as R
     from pupiloptixlab_gb300.denoiser import Denoiser
-    d = Denoiser(cuda_ctx, seed=5, lr=2e-3)
     g = torch.Generator().manual_seed(3)
     coarse = torch.rand(4, 3, 8, 8, generator=g) * 2.0
     tgt = torch.nn.functional.interpolate(coarse, size=(64, 64), mode="bilinear", align_corners=False)
     tgt = tgt.permute(0, 2, 3, 1).contiguous()
     noisy = tgt * torch.exp(0.7 * torch.randn(4, 64, 64, 3, generator=g))
-    guides = torch.rand(4, 64, 64, 6, generator=g)
-    inp = torch.cat([noisy, guides], dim=-1).to(torch.float16).cuda()
-    tgt = tgt.cuda()
-    d.train_step(inp, tgt)
-    first = d.read_loss()
-    for _ in range(60):
-        d.train_step(inp, tgt)
-    d.read_loss()
-    for _ in range(10):
-        d.train_step(inp, tgt)
-    last = d.read_loss()
+    inp = torch.cat([noisy, torch.rand(4, 64, 64, 6, generator=g)], dim=-1).to(torch.float16)
+    rng = np.random.default_rng(5)
+    ws, flat = [], []
+    for i, (cin, cout, _) in enumerate(R.LAYERS):
+        bound = 0.0 if i == len(R.LAYERS) - 1 else np.sqrt(6.0 / (9 * (9 if i == 0 else cin)))
+        w = rng.uniform(-bound, bound, (cout, cin, 3, 3)).astype(np.float32)
+        if i == 0:
+            w[:, 9:] = 0.0
+        ws.append(w)
+        flat += [R.from_torch_weight(torch.from_numpy(w)).ravel(), np.zeros(cout, np.float32)]
+    params = [(torch.tensor(w, requires_grad=True), torch.zeros(w.shape[0], requires_grad=True)) for w in ws]
+    opt = torch.optim.Adam([t for pr in params for t in pr], lr=2e-3)
+    target_log = torch.log1p(tgt).permute(0, 3, 1, 2)
+    cpu = []
+    for _ in range(71):
+        loss = (R.forward(params, inp.float(), bf16=True) - target_log).abs().mean()
+        opt.zero_grad()
+        loss.backward()
+        opt.step()
+        cpu.append(float(loss))
+    d = Denoiser(cuda_ctx, seed=5, lr=2e-3)
+    d.set_params(np.concatenate(flat))
+    i, t = inp.cuda(), tgt.cuda()
+    gpu = []
+    for _ in range(71):
+        d.train_step(i, t)
+        gpu.append(d.read_loss())
     d.close()
-    assert np.isfinite(first) and np.isfinite(last)
-    assert last < 0.6 * first, (first, last)
+    assert np.allclose(gpu[:10], cpu[:10], rtol=5e-3), (gpu[:10], cpu[:10])
+    assert np.isfinite(gpu).all()
+    assert np.mean(gpu[-5:]) < 0.5 * gpu[0] and np.mean(cpu[-5:]) < 0.5 * cpu[0], (gpu[-5:], cpu[-5:])
 
 
 def test_denoise_frame_and_fallback(cuda_ctx, dn):

@@ -6,7 +6,8 @@ The kernels fetch texels through the texture unit; the oracle restates the
 fetch on the CPU (oracle/tex_fetch.h).  The two agree to a few units in the
 last place of the filter weights, so paths that read a texture are compared
 with a tolerance: same random streams, >= 90 % of pixels within 1e-3
-(relative) at 4 spp, and RMSE <= 3e-3 of the converged images at 512 spp."""
+(relative) at 4 spp; converged images (512 spp, independent streams) differ
+by no more than the noise between two GPU seeds, mean radiance within 1 %."""
 import numpy as np
 import pytest
 import torch
@@ -71,16 +72,20 @@ def test_same_stream_agreement(cuda_ctx, env_map, filter):
 
 
 def test_converged_env_map_render(cuda_ctx):
+    """Independent random streams: the GPU-oracle difference must look like
+    the noise between two GPU renders with different seeds, and the mean
+    radiance must agree to 1 % (no bias)."""
     sc = textured_scene(env_map=True)
     o = oracle.OracleScene(sc)
     g = GpuScene(cuda_ctx, sc)
     p = abi.RenderParams(spp=512, max_depth=0, seed=100, sample_cnt=0, accumulate=1, rng=abi.RNG_PCG32)
-    ref = o.render(p)["accum"][:, :3]
-    got = g.render(512, seed=7)
-    torch.cuda.synchronize()
-    acc = got["accum"].cpu().numpy()[:, :3]
-    err = float(np.sqrt(np.mean((acc.astype(np.float64) - ref) ** 2)))
-    assert err <= 3e-3 * max(1.0, float(np.abs(ref).mean())), err
+    ref = o.render(p)["accum"][:, :3].astype(np.float64)
+    a = g.render(512, seed=7)["accum"].cpu().numpy()[:, :3].astype(np.float64)
+    b = g.render(512, seed=20000)["accum"].cpu().numpy()[:, :3].astype(np.float64)
+    noise = float(np.sqrt(np.mean((a - b) ** 2)))
+    err = float(np.sqrt(np.mean((a - ref) ** 2)))
+    assert err <= 1.3 * noise + 1e-4, (err, noise)
+    assert abs(a.mean() - ref.mean()) <= 0.01 * ref.mean()
     g.close()
 
 
