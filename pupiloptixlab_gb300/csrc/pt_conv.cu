@@ -2,15 +2,17 @@
 // cores, operands brought into shared memory by TMA (no multicast), FP32
 // accumulators in tensor memory.  Interface and GEMM shapes: pt_conv.h.
 //
-// Tiling.  One CTA of 128 threads computes a 128-row accumulator tile:
+// Tiling.  Accumulator tiles have 128 rows:
 //   forward / data gradient: 128 pixels (one 128-wide row segment, or
-//     128 / W whole rows of a narrow image) x n_tile output channels;
+//     128 / W whole rows of a narrow image) x n_tile output channels.  Persistent
+//     CTAs of 6 warps walk the tiles: warp 0 streams operands into a ring of
+//     `stages` buffers, warp 1 issues the MMAs into one of two accumulators,
+//     warps 2-5 run the epilogue of the other (k_conv_fwd_persistent);
 //   weight gradient: 128 (tap, input channel) rows x n_tile output channels,
-//     accumulated over a range of pixel tiles and added to the FP32 result.
-// Thread 0 issues the TMA loads into a ring of `stages` buffers, thread 32
-// issues the MMAs (one per 16-element K slice) and commits each buffer back
-// to the producer; after the last commit all four warps read the accumulator
-// (warp w owns TMEM lanes 32w..32w+31) and run the epilogue.
+//     accumulated over a range of pixel tiles and added to the FP32 result,
+//     one CTA of 4 warps per (row tile, channel tile, pixel range): thread 0
+//     loads, thread 32 issues the MMAs, all four warps read the accumulator
+//     (warp w owns TMEM lanes 32w..32w+31).
 //
 // Shared-memory operand layouts are the canonical swizzled ones for a row of
 // R = 2 * KC bytes (R = 32, 64, 128 B, TMA swizzle of the same width):
@@ -66,6 +68,9 @@ __device__ __forceinline__ void mbar_fence_init() {
 }
 __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
     uint32_t ok;
@@ -226,109 +231,7 @@ __device__ __forceinline__ void fwd_epilogue(const FwdArgs &a, uint32_t tmem, in
 }
 
 // ---------------------------------------------------------------------------
-// forward / data-gradient kernel
-// ---------------------------------------------------------------------------
-template <int KC>
-__global__ void __launch_bounds__(128, 1)
-    k_conv_fwd(const __grid_constant__ CUtensorMap act, const __grid_constant__ CUtensorMap wgt, const FwdArgs a) {
-    constexpr int R = KC * 2;
-    constexpr uint32_t SWZ = swz_mode<KC>();
-    extern __shared__ uint8_t smem_raw[];
-    __shared__ __align__(8) uint64_t bars[2 * kMaxStages + 1];
-    __shared__ uint32_t tmem_slot;
-    __shared__ int s_issued, s_consumed, s_fail;
-
-    const int tid = threadIdx.x, warp = tid >> 5;
-    const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
-    const int S = a.stages;
-    const int a_bytes = 128 * R, b_bytes = a.n_tile * R;
-    const uint32_t tx_bytes = static_cast<uint32_t>(a.tile_w * a.tile_rows * R + b_bytes);  // what the boxes deliver
-    const int tiles_img = a.tiles_x * a.tiles_y;
-    const int img = blockIdx.x / tiles_img, t = blockIdx.x - img * tiles_img;
-    const int x0 = (t % a.tiles_x) * a.tile_w, y0 = (t / a.tiles_x) * a.tile_rows;
-    const int n0 = blockIdx.y * a.n_tile;
-    const int nk = 9 * a.nchunks;
-    const uint32_t bar0 = smem_u32(bars);
-    auto full = [&](int s) { return bar0 + 8u * s; };
-    auto empty = [&](int s) { return bar0 + 8u * (kMaxStages + s); };
-    const uint32_t done = bar0 + 8u * (2 * kMaxStages);
-
-    if (warp == 0) tmem_alloc(smem_u32(&tmem_slot), a.tmem_cols);
-    if (tid == 32) {
-        for (int s = 0; s < S; s++) {
-            mbar_init(full(s), 1);
-            mbar_init(empty(s), 1);
-        }
-        mbar_init(done, 1);
-        mbar_fence_init();
-        s_issued = 0;
-        s_consumed = 0;
-        s_fail = 0;
-    }
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-    const uint32_t tmem = tmem_slot;
-
-    if (tid == 0) {
-        int k = 0;
-        for (; k < nk; k++) {
-            const int s = k % S;
-            if (k >= S && !mbar_wait(empty(s), ((k / S) - 1) & 1)) {
-                record_error(a.err, 1u);
-                s_fail = 1;
-                break;
-            }
-            if (*reinterpret_cast<volatile int *>(&s_fail)) break;
-            const int tap = k / a.nchunks, ch = k - tap * a.nchunks;
-            const int dy = tap / 3, dx = tap - dy * 3;
-            const uint32_t sa = base + s * a.stage_bytes, sb = sa + a_bytes;
-            mbar_expect_tx(full(s), tx_bytes);
-            tma_load_4d(sa, &act, full(s), ch * KC, x0 + dx - 1, y0 + dy - 1, img);
-            tma_load_2d(sb, &wgt, full(s), tap * a.cin + ch * KC, n0);
-        }
-        s_issued = k;
-    } else if (tid == 32) {
-        const uint32_t idesc = idesc_bf16(128, a.n_tile, false, false);
-        int k = 0;
-        for (; k < nk; k++) {
-            const int s = k % S;
-            if (!mbar_wait(full(s), (k / S) & 1)) {
-                record_error(a.err, 2u);
-                s_fail = 1;
-                break;
-            }
-            tc_fence_after();
-            const uint32_t sa = base + s * a.stage_bytes, sb = sa + a_bytes;
-#pragma unroll
-            for (int j = 0; j < KC / 16; j++) {
-                const uint64_t da = sdesc(sa + 32u * j, 16u, 8u * R, SWZ);
-                const uint64_t db = sdesc(sb + 32u * j, 16u, 8u * R, SWZ);
-                umma_bf16(tmem, da, db, idesc, (k | j) != 0 ? 1u : 0u);
-            }
-            umma_commit(empty(s));
-        }
-        s_consumed = k;
-        umma_commit(done);
-    }
-    __syncwarp();
-    const bool ok = mbar_wait(done, 0, true);
-    if (!ok && tid == 0) record_error(a.err, 4u);
-    tc_fence_after();
-
-    fwd_epilogue(a, tmem, tid, warp, img, x0, y0, n0, ok);
-
-    tc_fence_before();
-    __syncthreads();
-    if (tid == 0 && s_fail) {  // let copies that were issued but never consumed land
-        for (int k = s_consumed; k < s_issued; k++) (void)mbar_wait(full(k % S), (k / S) & 1);
-    }
-    __syncthreads();
-    if (warp == 0) tmem_dealloc(tmem, a.tmem_cols);
-}
-
-// ---------------------------------------------------------------------------
-// forward / data-gradient kernel for images at least 128 pixels wide
+// halo operand layout (forward / data gradient, images at least 128 pixels wide)
 // ---------------------------------------------------------------------------
 // The pixel tile is a 128-pixel row segment.  Per 16-channel chunk one TMA box
 // brings its 3 x 130-pixel neighbourhood (the segment and a one-pixel border,
@@ -344,30 +247,52 @@ constexpr int kHaloBoxBytes = kHaloW * kHaloRows * 16;       // one 8-channel pl
 constexpr int kHaloPlaneBytes = (kHaloBoxBytes + 1023) / 1024 * 1024;  // plane stride: TMA destinations 1 KiB-aligned
 __host__ __device__ constexpr int halo_b_tap_bytes(int n_tile) { return (n_tile * 32 + 1023) / 1024 * 1024; }
 
-__global__ void __launch_bounds__(128, 1)
-    k_conv_fwd_halo(const __grid_constant__ CUtensorMap act, const __grid_constant__ CUtensorMap wgt, const FwdArgs a) {
-    constexpr int R = 32;  // B rows: 16 channels
-    constexpr uint32_t SWZB = swz_mode<16>();
+// ---------------------------------------------------------------------------
+// persistent forward / data-gradient kernel
+// ---------------------------------------------------------------------------
+// One CTA per SM slot walks the output tiles (pixel tile x output-channel
+// tile) with a stride of gridDim.x.  Warp 0 streams operands into a ring of
+// `stages` buffers across tile boundaries, warp 1 issues the MMAs into one of
+// two accumulators in tensor memory (2 x n_tile columns), and warps 2-5 run
+// the epilogue of tile i from one accumulator while the MMAs of tile i + 1
+// fill the other.  Warp w of the epilogue reads TMEM lanes 32 * (w % 4) + 0..31.
+// HALO: the A operand comes from one 3 x 130-pixel halo box per 16-channel
+// chunk (width >= 128, see above); otherwise one box per (tap, chunk).
+template <int KC, bool HALO>
+__global__ void __launch_bounds__(192, 1)
+    k_conv_fwd_persistent(const __grid_constant__ CUtensorMap act, const __grid_constant__ CUtensorMap wgt,
+                          const FwdArgs a) {
+    constexpr int R = KC * 2;
+    constexpr uint32_t SWZ = swz_mode<KC>();
     extern __shared__ uint8_t smem_raw[];
-    __shared__ __align__(8) uint64_t bars[2 * kMaxStages + 1];
+    __shared__ __align__(8) uint64_t bars[2 * kMaxStages + 4];
     __shared__ uint32_t tmem_slot;
-    __shared__ int s_issued, s_consumed, s_fail;
+    __shared__ int s_fail;
 
-    const int tid = threadIdx.x, warp = tid >> 5;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
     const int S = a.stages;
-    const int a_bytes = a.halo_a_bytes;
-    const int b_tap = halo_b_tap_bytes(a.n_tile);  // region stride of one tap's weights
-    const uint32_t tx_bytes = static_cast<uint32_t>(2 * kHaloBoxBytes + 9 * a.n_tile * R);
     const int tiles_img = a.tiles_x * a.tiles_y;
-    const int img = blockIdx.x / tiles_img, t = blockIdx.x - img * tiles_img;
-    const int x0 = (t % a.tiles_x) * 128, y0 = t / a.tiles_x;
-    const int n0 = blockIdx.y * a.n_tile;
-    const int nk = a.nchunks;
+    const int n_n = a.n_tiles_n;
+    const int total = a.n_img * tiles_img * n_n;
+    const int nk = HALO ? a.nchunks : 9 * a.nchunks;  // stages per tile
+    const int a_bytes = HALO ? a.halo_a_bytes : 128 * R;
+    const int b_tap = HALO ? halo_b_tap_bytes(a.n_tile) : 0;
+    const uint32_t tx_bytes = HALO ? static_cast<uint32_t>(2 * kHaloBoxBytes + 9 * a.n_tile * R)
+                                   : static_cast<uint32_t>(a.tile_w * a.tile_rows * R + a.n_tile * R);
     const uint32_t bar0 = smem_u32(bars);
     auto full = [&](int s) { return bar0 + 8u * s; };
     auto empty = [&](int s) { return bar0 + 8u * (kMaxStages + s); };
-    const uint32_t done = bar0 + 8u * (2 * kMaxStages);
+    auto acc_full = [&](int b) { return bar0 + 8u * (2 * kMaxStages + b); };
+    auto acc_empty = [&](int b) { return bar0 + 8u * (2 * kMaxStages + 2 + b); };
+    auto tile_of = [&](int t, int &img, int &x0, int &y0, int &n0) {
+        const int pt = t / n_n;
+        n0 = (t - pt * n_n) * a.n_tile;
+        img = pt / tiles_img;
+        const int r = pt - img * tiles_img;
+        x0 = (r % a.tiles_x) * a.tile_w;
+        y0 = (r / a.tiles_x) * a.tile_rows;
+    };
 
     if (warp == 0) tmem_alloc(smem_u32(&tmem_slot), a.tmem_cols);
     if (tid == 32) {
@@ -375,75 +300,116 @@ __global__ void __launch_bounds__(128, 1)
             mbar_init(full(s), 1);
             mbar_init(empty(s), 1);
         }
-        mbar_init(done, 1);
+        for (int b = 0; b < 2; b++) {
+            mbar_init(acc_full(b), 1);
+            mbar_init(acc_empty(b), 128);
+        }
         mbar_fence_init();
-        s_issued = 0;
-        s_consumed = 0;
         s_fail = 0;
     }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = tmem_slot;
+    volatile int *fail = &s_fail;
 
-    if (tid == 0) {
-        int k = 0;
-        for (; k < nk; k++) {
-            const int s = k % S;
-            if (k >= S && !mbar_wait(empty(s), ((k / S) - 1) & 1)) {
-                record_error(a.err, 1u);
-                s_fail = 1;
-                break;
+    if (warp == 0) {
+        if (lane == 0) {  // producer
+            int kg = 0;  // stages issued so far (ring position and phase)
+            for (int t = blockIdx.x; t < total && !*fail; t += gridDim.x) {
+                int img, x0, y0, n0;
+                tile_of(t, img, x0, y0, n0);
+                for (int k = 0; k < nk; k++, kg++) {
+                    const int s = kg % S;
+                    if (kg >= S && !mbar_wait(empty(s), ((kg / S) - 1) & 1)) {
+                        record_error(a.err, 1u);
+                        *fail = 1;
+                        break;
+                    }
+                    const uint32_t sa = base + s * a.stage_bytes, sb = sa + a_bytes;
+                    mbar_expect_tx(full(s), tx_bytes);
+                    if (HALO) {
+                        tma_load_4d(sa, &act, full(s), k * 16, x0 - 1, y0 - 1, img);
+                        tma_load_4d(sa + kHaloPlaneBytes, &act, full(s), k * 16 + 8, x0 - 1, y0 - 1, img);
+                        for (int tap = 0; tap < 9; tap++)
+                            tma_load_2d(sb + tap * b_tap, &wgt, full(s), tap * a.cin + k * 16, n0);
+                    } else {
+                        const int tap = k / a.nchunks, ch = k - tap * a.nchunks;
+                        const int dy = tap / 3, dx = tap - dy * 3;
+                        tma_load_4d(sa, &act, full(s), ch * KC, x0 + dx - 1, y0 + dy - 1, img);
+                        tma_load_2d(sb, &wgt, full(s), tap * a.cin + ch * KC, n0);
+                    }
+                }
             }
-            if (*reinterpret_cast<volatile int *>(&s_fail)) break;
-            const uint32_t sa = base + s * a.stage_bytes, sb = sa + a_bytes;
-            if (((sa | sb | static_cast<uint32_t>(kHaloPlaneBytes) | static_cast<uint32_t>(b_tap)) & 1023u) != 0) {
-                record_error(a.err, 8u);  // a TMA destination off its 1 KiB boundary: issue nothing
-                s_fail = 1;
-                break;
-            }
-            mbar_expect_tx(full(s), tx_bytes);
-            tma_load_4d(sa, &act, full(s), k * 16, x0 - 1, y0 - 1, img);
-            tma_load_4d(sa + kHaloPlaneBytes, &act, full(s), k * 16 + 8, x0 - 1, y0 - 1, img);
-            for (int tap = 0; tap < 9; tap++) tma_load_2d(sb + tap * b_tap, &wgt, full(s), tap * a.cin + k * 16, n0);
+            // drain: wait until every issued stage has been consumed
+            for (int k = kg - S; k < kg; k++)
+                if (k >= 0) (void)mbar_wait(empty(k % S), (k / S) & 1, true);
         }
-        s_issued = k;
-    } else if (tid == 32) {
-        const uint32_t idesc = idesc_bf16(128, a.n_tile, false, false);
-        int k = 0;
-        for (; k < nk; k++) {
-            const int s = k % S;
-            if (!mbar_wait(full(s), (k / S) & 1)) {
-                record_error(a.err, 2u);
-                s_fail = 1;
+    } else if (warp == 1) {
+        if (lane == 0) {  // MMA issuer
+            const uint32_t idesc = idesc_bf16(128, a.n_tile, false, false);
+            int kg = 0, j = 0;
+            for (int t = blockIdx.x; t < total && !*fail; t += gridDim.x, j++) {
+                const int buf = j & 1;
+                if (!mbar_wait(acc_empty(buf), ((j >> 1) & 1) ^ 1)) {  // epilogue of tile j - 2 done
+                    record_error(a.err, 2u);
+                    *fail = 1;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t d = tmem + static_cast<uint32_t>(buf * a.n_tile);
+                for (int k = 0; k < nk; k++, kg++) {
+                    const int s = kg % S;
+                    if (!mbar_wait(full(s), (kg / S) & 1)) {
+                        record_error(a.err, 2u);
+                        *fail = 1;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t sa = base + s * a.stage_bytes, sb = sa + a_bytes;
+                    if (HALO) {
+#pragma unroll
+                        for (int tap = 0; tap < 9; tap++) {
+                            const int dy = tap / 3, dx = tap - 3 * (tap / 3);
+                            const uint64_t da = sdesc(sa + 16u * (dy * kHaloW + dx), kHaloPlaneBytes, 128u, 0u);
+                            const uint64_t db = sdesc(sb + tap * b_tap, 16u, 8u * R, SWZ);
+                            umma_bf16(d, da, db, idesc, (k | tap) != 0 ? 1u : 0u);
+                        }
+                    } else {
+#pragma unroll
+                        for (int q = 0; q < KC / 16; q++) {
+                            const uint64_t da = sdesc(sa + 32u * q, 16u, 8u * R, SWZ);
+                            const uint64_t db = sdesc(sb + 32u * q, 16u, 8u * R, SWZ);
+                            umma_bf16(d, da, db, idesc, (k | q) != 0 ? 1u : 0u);
+                        }
+                    }
+                    umma_commit(empty(s));
+                }
+                if (*fail) break;
+                umma_commit(acc_full(buf));
+            }
+        }
+    } else {  // epilogue warps 2-5
+        const int quad = warp & 3;
+        const int row = quad * 32 + lane;
+        int j = 0;
+        for (int t = blockIdx.x; t < total; t += gridDim.x, j++) {
+            const int buf = j & 1;
+            const bool ok = mbar_wait(acc_full(buf), (j >> 1) & 1, true);
+            if (!ok) {
+                if (row == 0) record_error(a.err, 4u);
                 break;
             }
             tc_fence_after();
-            const uint32_t sa = base + s * a.stage_bytes, sb = sa + a_bytes;
-#pragma unroll
-            for (int tap = 0; tap < 9; tap++) {
-                const int dy = tap / 3, dx = tap - 3 * (tap / 3);
-                const uint64_t da = sdesc(sa + 16u * (dy * kHaloW + dx), kHaloPlaneBytes, 128u, 0u);
-                const uint64_t db = sdesc(sb + tap * b_tap, 16u, 8u * R, SWZB);
-                umma_bf16(tmem, da, db, idesc, (k | tap) != 0 ? 1u : 0u);
-            }
-            umma_commit(empty(s));
+            int img, x0, y0, n0;
+            tile_of(t, img, x0, y0, n0);
+            fwd_epilogue(a, tmem + static_cast<uint32_t>(buf * a.n_tile), row, quad, img, x0, y0, n0, true);
+            tc_fence_before();
+            mbar_arrive(acc_empty(buf));
         }
-        s_consumed = k;
-        umma_commit(done);
     }
     __syncwarp();
-    const bool ok = mbar_wait(done, 0, true);
-    if (!ok && tid == 0) record_error(a.err, 4u);
-    tc_fence_after();
-
-    fwd_epilogue(a, tmem, tid, warp, img, x0, y0, n0, ok);
-
     tc_fence_before();
-    __syncthreads();
-    if (tid == 0 && s_fail) {
-        for (int k = s_consumed; k < s_issued; k++) (void)mbar_wait(full(k % S), (k / S) & 1);
-    }
     __syncthreads();
     if (warp == 0) tmem_dealloc(tmem, a.tmem_cols);
 }
@@ -708,6 +674,17 @@ int wgt_map(CUtensorMap *m, const void *w, int kdim, int rows, int kc, int n_til
     return PT_OK;
 }
 
+int sm_count() {
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
+            n = 1;
+    }
+    return n;
+}
+
 bool getenv_flag(const char *name) {
     const char *v = getenv(name);
     return v && *v && *v != '0';
@@ -793,13 +770,14 @@ int fwd_prepare(FwdOp *op, const Act &in, const void *w, int w_rows, int cout, c
     a.nchunks = in.c / kc;
     a.n_tile = n_tile;
     a.cout = cout;
-    a.tmem_cols = pow2_cols(n_tile);
+    a.n_tiles_n = ntiles;
+    a.tmem_cols = pow2_cols(2 * n_tile);  // two accumulators
     a.halo_a_bytes = 2 * kHaloPlaneBytes;
     a.stage_bytes = halo ? a.halo_a_bytes + 9 * halo_b_tap_bytes(n_tile)
                          : (128 * 2 * kc + n_tile * 2 * kc + 1023) / 1024 * 1024;
-    const int target_ctas = std::min(512 / a.tmem_cols, 3);
+    const int target_ctas = std::min(512 / a.tmem_cols, 2);
     const int budget = (225 * 1024) / target_ctas - 2048;
-    a.stages = std::max(2, std::min(6, budget / a.stage_bytes));
+    a.stages = std::max(2, std::min(kMaxStages, budget / a.stage_bytes));
     if (halo) {
         a.tile_w = 128;
         a.tile_rows = 1;
@@ -821,7 +799,9 @@ int fwd_prepare(FwdOp *op, const Act &in, const void *w, int w_rows, int cout, c
     op->kc = kc;
     op->halo = halo;
     op->smem = smem_request(a.stages, a.stage_bytes, a.tmem_cols);
-    op->grid = dim3(static_cast<unsigned>(in.n * a.tiles_x * a.tiles_y), static_cast<unsigned>(ntiles), 1);
+    const long long total = (long long)in.n * a.tiles_x * a.tiles_y * ntiles;
+    const int per_sm = std::max(1, std::min((228 * 1024) / (op->smem + 1024), 512 / a.tmem_cols));
+    op->grid = dim3(static_cast<unsigned>(std::min<long long>(total, (long long)per_sm * sm_count())), 1, 1);
     if (op->smem > 220 * 1024) {
         pt_set_error("conv forward: shared memory request %d too large", op->smem);
         return PT_ERR_INVALID;
@@ -829,32 +809,20 @@ int fwd_prepare(FwdOp *op, const Act &in, const void *w, int w_rows, int cout, c
     return PT_OK;
 }
 
-int fwd_launch(const FwdOp &op, cudaStream_t stream) {
-    int st = PT_OK;
-    if (op.halo) {
-        st = set_smem_attr(k_conv_fwd_halo, op.smem);
-        if (st != PT_OK) return st;
-        k_conv_fwd_halo<<<op.grid, 128, op.smem, stream>>>(op.act, op.wgt, op.args);
-        PT_CUDA_TRY(cudaGetLastError());
-        return PT_OK;
-    }
-    switch (op.kc) {
-        case 64:
-            st = set_smem_attr(k_conv_fwd<64>, op.smem);
-            if (st == PT_OK) k_conv_fwd<64><<<op.grid, 128, op.smem, stream>>>(op.act, op.wgt, op.args);
-            break;
-        case 32:
-            st = set_smem_attr(k_conv_fwd<32>, op.smem);
-            if (st == PT_OK) k_conv_fwd<32><<<op.grid, 128, op.smem, stream>>>(op.act, op.wgt, op.args);
-            break;
-        default:
-            st = set_smem_attr(k_conv_fwd<16>, op.smem);
-            if (st == PT_OK) k_conv_fwd<16><<<op.grid, 128, op.smem, stream>>>(op.act, op.wgt, op.args);
-            break;
-    }
+template <int KC, bool HALO>
+static int fwd_persistent_go(const FwdOp &op, cudaStream_t stream) {
+    int st = set_smem_attr(k_conv_fwd_persistent<KC, HALO>, op.smem);
     if (st != PT_OK) return st;
+    k_conv_fwd_persistent<KC, HALO><<<op.grid, 192, op.smem, stream>>>(op.act, op.wgt, op.args);
     PT_CUDA_TRY(cudaGetLastError());
     return PT_OK;
+}
+
+int fwd_launch(const FwdOp &op, cudaStream_t stream) {
+    if (op.halo) return fwd_persistent_go<16, true>(op, stream);
+    if (op.kc == 64) return fwd_persistent_go<64, false>(op, stream);
+    if (op.kc == 32) return fwd_persistent_go<32, false>(op, stream);
+    return fwd_persistent_go<16, false>(op, stream);
 }
 
 int wgrad_prepare(WgradOp *op, const Act &x, const Act &gy, float *dw, int num_sms, unsigned *err) {

@@ -40,6 +40,7 @@ struct FwdArgs {
     int n_tile, cout;     // N per CTA; valid output channels
     int tmem_cols, stages, stage_bytes;
     int halo_a_bytes;     // halo kernel: bytes of the A planes at the start of a stage
+    int n_tiles_n;        // output-channel tiles (persistent kernel: tile = pixel tile x channel tile)
     int epi, relu;
     const float *bias;
     void *out;
@@ -66,7 +67,7 @@ struct FwdOp {
     FwdArgs args;
     dim3 grid;
     int smem = 0, kc = 0;
-    bool halo = false;  // k_conv_fwd_halo (width >= 128) instead of k_conv_fwd<kc>
+    bool halo = false;  // halo loads (width >= 128)
 };
 
 struct WgradOp {
