@@ -83,6 +83,21 @@ def parse():
     return ap.parse_args()
 
 
+def replica_throughput(local_ms: float, units_per_rank: float, ws: int, device: str = "cuda"):
+    """Whole-job throughput of `ws` independent replicas (one per GPU, each
+    processing units_per_rank): all units over the slowest rank's time
+    (max over ranks, all-reduced), in millions per second.  Returns
+    (value, max_ms)."""
+    t_max = float(local_ms)
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([t_max], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+    return ws * units_per_rank / (t_max / 1e3) / 1e6, t_max
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -580,14 +595,8 @@ def main():
         sh_ms += rs.shadow_ms
         shade_ms += rs.shade_ms
         timed_ms.append(rs.render_ms)
-    t_max = sum(step_ms)
-    if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([t_max], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
     samples_per_step = args.width * args.height * args.spp
-    value = ws * samples_per_step * args.steps / (t_max / 1e3) / 1e6
+    value, t_max = replica_throughput(sum(step_ms), samples_per_step * args.steps, ws, device="cuda")
 
     e2e = None
     if not args.no_e2e:
