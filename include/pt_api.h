@@ -45,7 +45,7 @@ typedef enum pt_status {
     PT_ERR_CUDA = 2,        /* a CUDA runtime call failed */
     PT_ERR_OOM = 3,         /* device allocation failed */
     PT_ERR_TIMEOUT = 4,     /* a bounded device wait ran out */
-    PT_ERR_NAN = 5,         /* NaN/Inf detected in a checked build */
+    PT_ERR_NAN = 5,         /* NaN/Inf radiance (PT_RENDER_CHECK_FINITE) */
     PT_ERR_UNSUPPORTED = 6, /* feature not available (e.g. no GPU) */
     PT_ERR_OOB = 7,         /* index out of range in the scene data */
     PT_ERR_STATE = 8        /* call made in the wrong order (e.g. render before BVH build) */
@@ -251,6 +251,8 @@ enum {
     PT_RENDER_NO_GRAPH = 4,      /* launch the bounce kernels one by one instead of a CUDA graph */
     PT_RENDER_KERNEL_TIMING = 8, /* time each traversal / shading launch with CUDA events
                                     (launches directly, without the CUDA graph) */
+    PT_RENDER_CHECK_FINITE = 32,  /* return PT_ERR_NAN when a sample's radiance was NaN or infinite
+                                     (after the render; counted in pt_render_stats either way) */
     PT_RENDER_DROP_NONFINITE = 16 /* accumulate a sample whose radiance is NaN or infinite as zero.
                                      Off by default: the reference's integrator (main.cu:97-101)
                                      accumulates such samples, which then stay in the pixel. */
@@ -286,6 +288,7 @@ typedef struct pt_render_stats {
     uint32_t kernel_launches;     /* all kernels launched by the last pt_render */
     uint32_t waves;
     uint32_t overflow;            /* traversal stack overflows (must be 0) */
+    uint32_t nonfinite_samples;   /* samples whose radiance was NaN or infinite */
 } pt_render_stats;
 
 /* Flat local BSDF record used by the BSDF batch entry points (16 floats):

@@ -29,6 +29,7 @@ TEX_FILTER_POINT, TEX_FILTER_LINEAR = 0, 1
 RNG_REF_LCG, RNG_PCG32 = 0, 1
 RENDER_NO_MATERIAL_SORT, RENDER_COUNTERS, RENDER_NO_GRAPH, RENDER_KERNEL_TIMING = 1, 2, 4, 8
 RENDER_DROP_NONFINITE = 16
+RENDER_CHECK_FINITE = 32
 LOBE_DELTA = (1 << 5) | (1 << 6)
 
 
@@ -108,7 +109,7 @@ class RenderStats(C.Structure):
                 ("shadow_prims_tested", C.c_uint64), ("render_ms", C.c_float), ("extend_ms", C.c_float),
                 ("shadow_ms", C.c_float), ("shade_ms", C.c_float), ("extend_launches", C.c_uint32),
                 ("shadow_launches", C.c_uint32), ("shade_launches", C.c_uint32), ("kernel_launches", C.c_uint32),
-                ("waves", C.c_uint32), ("overflow", C.c_uint32)]
+                ("waves", C.c_uint32), ("overflow", C.c_uint32), ("nonfinite_samples", C.c_uint32)]
 
 
 class TuneResult(C.Structure):

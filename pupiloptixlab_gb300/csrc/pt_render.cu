@@ -40,6 +40,7 @@ enum Counter : int {
     kWorkExtend = 3,
     kWorkShadow = 4,
     kOverflow = 5,
+    kNonFinite = 6,  // samples whose radiance was NaN or infinite
     kStatBase = 8,  // uint64 statistics start at counters + 8 (32-byte offset)
 };
 enum Stat : int { kStatExtNodes = 0, kStatExtPrims, kStatShNodes, kStatShPrims, kStatExtRays, kStatShRays, kNumStats };
@@ -667,7 +668,10 @@ __global__ void k_accumulate(State st, Wave w, Outputs out0, Batch bt) {
         float3 a = xyz(acc);
         for (uint32_t fl = 0; fl < w.frames; fl++) {
             float3 L = xyz(st.rad[(size_t)fl * w.npix + q]);
-            if (out.drop_nonfinite && !(isfinite(L.x) && isfinite(L.y) && isfinite(L.z))) L = f3s(0.f);
+            if (!(isfinite(L.x) && isfinite(L.y) && isfinite(L.z))) {
+                atomicAdd(st.counters + kNonFinite, 1u);
+                if (out.drop_nonfinite) L = f3s(0.f);
+            }
             uint32_t cnt = w.cnt0 + w.frame0 + fl;
             if (w.accumulate && cnt > 0) {
                 const float t = 1.f / (cnt + 1.f);
@@ -990,9 +994,14 @@ struct Launcher {
         rs.kernel_launches = launches;
         rs.waves = waves;
         rs.overflow = hc[kOverflow];
+        rs.nonfinite_samples = hc[kNonFinite];
         if (rs.overflow) {
             pt_set_error("traversal stack overflow");
             return PT_ERR_OOB;
+        }
+        if (rs.nonfinite_samples && (p->flags & PT_RENDER_CHECK_FINITE)) {
+            pt_set_error("%u samples had NaN or infinite radiance", rs.nonfinite_samples);
+            return PT_ERR_NAN;
         }
         return PT_OK;
     }

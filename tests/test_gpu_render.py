@@ -142,3 +142,26 @@ def test_autotune_picks_a_configuration_and_keeps_the_image(cuda_ctx):
     assert g.bvh_stats().width == r.bvh_width
     after = gpu_render(g, 4, seed=1)["accum"]
     assert np.array_equal(after.view(np.uint32), before.view(np.uint32))
+
+
+def test_nonfinite_samples_are_counted_dropped_or_reported(cuda_ctx):
+    """A material whose reflectance is NaN poisons the paths that bounce off
+    it: the samples are counted, PT_RENDER_DROP_NONFINITE accumulates them as
+    zero, PT_RENDER_CHECK_FINITE turns the render into PT_ERR_NAN."""
+    sc = scenes.cornell_box(24, 24)
+    sc.materials[0].tex[0].color0[:] = [float("nan")] * 3
+    g = GpuScene(cuda_ctx, sc)
+    out = gpu_render(g, 2, seed=1)
+    st = g.render_stats()
+    assert st.nonfinite_samples > 0 and not np.isfinite(out["accum"]).all()
+    out = gpu_render(g, 2, seed=1, flags=abi.RENDER_DROP_NONFINITE)
+    assert g.render_stats().nonfinite_samples == st.nonfinite_samples
+    assert np.isfinite(out["accum"]).all()
+    with pytest.raises(abi.PtError) as e:
+        g.render(2, seed=1, flags=abi.RENDER_CHECK_FINITE)
+    assert e.value.status == 5 and "PT_ERR_NAN" in str(e.value)
+    g.close()
+    clean = GpuScene(cuda_ctx, scenes.cornell_box(24, 24))
+    gpu_render(clean, 2, seed=1, flags=abi.RENDER_CHECK_FINITE)
+    assert clean.render_stats().nonfinite_samples == 0
+    clean.close()
