@@ -11,6 +11,7 @@
 
 #include "pass.h"
 #include "scene.h"
+#include "image.h"
 
 namespace {
 thread_local std::string g_err;
@@ -90,6 +91,15 @@ int pupil_write_pfm(const char *path, const float *rgba, uint32_t w, uint32_t h)
     fprintf(f, "PF\n%u %u\n-1.0\n", w, h);
     for (size_t i = 0; i < (size_t)w * h; i++) fwrite(rgba + 4 * i, sizeof(float), 3, f);
     fclose(f);
+    return PT_OK;
+}
+
+// Headless image save (the GUI's screenshot, framework/system/gui.cpp:475-482,
+// writes EXR through tinyexr): uncompressed scanline OpenEXR, RGBA floats.
+int pupil_write_exr(const char *path, const float *rgba, uint32_t w, uint32_t h) {
+    std::string e;
+    if (!path || !rgba || !w || !h) return fail("pupil_write_exr: bad arguments");
+    if (!Pupil::util::SaveExrRGBA(path, rgba, w, h, e)) return fail(e);
     return PT_OK;
 }
 

@@ -1,7 +1,9 @@
-// image.cpp -- Radiance RGBE and PFM readers (see image.h).
+// image.cpp -- Radiance RGBE, PFM and uncompressed OpenEXR readers, OpenEXR
+// writer (see image.h).
 #include "image.h"
 
 #include <algorithm>
+#include <cstdint>
 #include <cctype>
 #include <cmath>
 #include <cstring>
@@ -168,18 +170,233 @@ bool load_pfm(const std::vector<uint8_t> &d, std::vector<float> &rgba, uint32_t 
     return true;
 }
 
+// ---- OpenEXR (scanline, NO_COMPRESSION) ----------------------------------
+// Layout per the OpenEXR file format description: magic 20000630, version 2,
+// header = attributes (name\0 type\0 int32 size, value) ending with \0, a
+// table of uint64 offsets (one per scanline block), then blocks of
+// (int32 y, int32 byte count, channel data in the header's channel order).
+
+void put_u32(std::vector<uint8_t> &b, uint32_t v) {
+    for (int i = 0; i < 4; i++) b.push_back(static_cast<uint8_t>(v >> (8 * i)));
+}
+void put_u64(std::vector<uint8_t> &b, uint64_t v) {
+    for (int i = 0; i < 8; i++) b.push_back(static_cast<uint8_t>(v >> (8 * i)));
+}
+void put_f32(std::vector<uint8_t> &b, float f) {
+    uint32_t v;
+    std::memcpy(&v, &f, 4);
+    put_u32(b, v);
+}
+void put_str(std::vector<uint8_t> &b, const char *s) {
+    while (*s) b.push_back(static_cast<uint8_t>(*s++));
+    b.push_back(0);
+}
+void attr(std::vector<uint8_t> &b, const char *name, const char *type, const std::vector<uint8_t> &value) {
+    put_str(b, name);
+    put_str(b, type);
+    put_u32(b, static_cast<uint32_t>(value.size()));
+    b.insert(b.end(), value.begin(), value.end());
+}
+
+uint32_t get_u32(const std::vector<uint8_t> &d, size_t p) {
+    return d[p] | (d[p + 1] << 8) | (d[p + 2] << 16) | (static_cast<uint32_t>(d[p + 3]) << 24);
+}
+uint64_t get_u64(const std::vector<uint8_t> &d, size_t p) { return get_u32(d, p) | (uint64_t)get_u32(d, p + 4) << 32; }
+
+float half_to_float(uint16_t h) {  // IEEE 754 binary16
+    const uint32_t sign = (h >> 15) & 1, e = (h >> 10) & 31, m = h & 1023;
+    float v;
+    if (e == 0) v = std::ldexp(static_cast<float>(m), -24);
+    else if (e == 31) v = m ? NAN : INFINITY;
+    else v = std::ldexp(static_cast<float>(m | 1024), static_cast<int>(e) - 25);
+    return sign ? -v : v;
+}
+
+bool load_exr(const std::vector<uint8_t> &d, std::vector<float> &rgba, uint32_t &w, uint32_t &h, std::string &error) {
+    if (d.size() < 8 || get_u32(d, 0) != 20000630u) {
+        error = "not an OpenEXR file";
+        return false;
+    }
+    if ((get_u32(d, 4) & 0xff) != 2 || (get_u32(d, 4) & 0x200)) {
+        error = "only single-part scanline OpenEXR files are supported";
+        return false;
+    }
+    struct Chan {
+        std::string name;
+        uint32_t type;
+    };
+    std::vector<Chan> chans;
+    int32_t xmin = 0, ymin = 0, xmax = -1, ymax = -1;
+    int compression = -1;
+    size_t p = 8;
+    auto cstr = [&](std::string &out) {
+        out.clear();
+        while (p < d.size() && d[p]) out.push_back(static_cast<char>(d[p++]));
+        p++;
+        return p <= d.size();
+    };
+    for (;;) {
+        std::string name, type;
+        if (p >= d.size()) {
+            error = "OpenEXR header truncated";
+            return false;
+        }
+        if (d[p] == 0) {
+            p++;
+            break;
+        }
+        cstr(name);
+        cstr(type);
+        if (p + 4 > d.size()) {
+            error = "OpenEXR header truncated";
+            return false;
+        }
+        const uint32_t size = get_u32(d, p);
+        p += 4;
+        if (p + size > d.size()) {
+            error = "OpenEXR header truncated";
+            return false;
+        }
+        const size_t end = p + size;
+        if (name == "channels") {
+            while (p < end && d[p]) {
+                Chan c;
+                cstr(c.name);
+                c.type = get_u32(d, p);
+                p += 16;  // type, pLinear + 3 reserved, xSampling, ySampling
+                chans.push_back(c);
+            }
+        } else if (name == "compression") {
+            compression = d[p];
+        } else if (name == "dataWindow") {
+            xmin = static_cast<int32_t>(get_u32(d, p));
+            ymin = static_cast<int32_t>(get_u32(d, p + 4));
+            xmax = static_cast<int32_t>(get_u32(d, p + 8));
+            ymax = static_cast<int32_t>(get_u32(d, p + 12));
+        }
+        p = end;
+    }
+    if (compression != 0) {
+        error = "compressed OpenEXR files are not supported (only NO_COMPRESSION)";
+        return false;
+    }
+    if (xmax < xmin || ymax < ymin) {
+        error = "OpenEXR data window empty";
+        return false;
+    }
+    w = static_cast<uint32_t>(xmax - xmin + 1);
+    h = static_cast<uint32_t>(ymax - ymin + 1);
+    size_t line_bytes = 0;
+    for (auto &c : chans) {
+        if (c.type != 1 && c.type != 2) {
+            error = "OpenEXR channel '" + c.name + "' is neither HALF nor FLOAT";
+            return false;
+        }
+        line_bytes += (c.type == 1 ? 2 : 4) * (size_t)w;
+    }
+    rgba.assign(4ull * w * h, 0.f);
+    for (size_t i = 0; i < (size_t)w * h; i++) rgba[4 * i + 3] = 1.f;
+    const size_t table = p;
+    if (table + 8ull * h > d.size()) {
+        error = "OpenEXR offset table truncated";
+        return false;
+    }
+    for (uint32_t line = 0; line < h; line++) {
+        const uint64_t off = get_u64(d, table + 8ull * line);
+        if (off + 8 + line_bytes > d.size()) {
+            error = "OpenEXR scanline out of range";
+            return false;
+        }
+        const int32_t y = static_cast<int32_t>(get_u32(d, off)) - ymin;
+        if (y < 0 || y >= static_cast<int32_t>(h) || get_u32(d, off + 4) != line_bytes) {
+            error = "OpenEXR scanline block malformed";
+            return false;
+        }
+        size_t q = off + 8;
+        for (auto &c : chans) {
+            const int ch = c.name == "R" ? 0 : c.name == "G" ? 1 : c.name == "B" ? 2 : c.name == "A" ? 3 : -1;
+            for (uint32_t x = 0; x < w; x++) {
+                float v;
+                if (c.type == 1) {
+                    v = half_to_float(static_cast<uint16_t>(d[q] | (d[q + 1] << 8)));
+                    q += 2;
+                } else {
+                    const uint32_t u = get_u32(d, q);
+                    std::memcpy(&v, &u, 4);
+                    q += 4;
+                }
+                if (ch >= 0) rgba[4 * ((size_t)y * w + x) + ch] = v;
+            }
+        }
+    }
+    return true;
+}
+
 }  // namespace
+
+bool SaveExrRGBA(const std::string &path, const float *rgba, uint32_t width, uint32_t height, std::string &error) {
+    std::vector<uint8_t> b, v;
+    put_u32(b, 20000630u);
+    put_u32(b, 2u);
+    for (const char *c : {"A", "B", "G", "R"}) {  // channel list, sorted by name
+        put_str(v, c);
+        put_u32(v, 2u);          // FLOAT
+        put_u32(v, 0u);          // pLinear + reserved
+        put_u32(v, 1u);          // xSampling
+        put_u32(v, 1u);          // ySampling
+    }
+    v.push_back(0);
+    attr(b, "channels", "chlist", v);
+    attr(b, "compression", "compression", {0});
+    v.clear();
+    put_u32(v, 0);
+    put_u32(v, 0);
+    put_u32(v, width - 1);
+    put_u32(v, height - 1);
+    attr(b, "dataWindow", "box2i", v);
+    attr(b, "displayWindow", "box2i", v);
+    attr(b, "lineOrder", "lineOrder", {0});
+    v.clear();
+    put_f32(v, 1.f);
+    attr(b, "pixelAspectRatio", "float", v);
+    v.clear();
+    put_f32(v, 0.f);
+    put_f32(v, 0.f);
+    attr(b, "screenWindowCenter", "v2f", v);
+    v.clear();
+    put_f32(v, 1.f);
+    attr(b, "screenWindowWidth", "float", v);
+    b.push_back(0);  // end of header
+    const uint64_t line_bytes = 4ull * 4 * width;
+    const uint64_t first = b.size() + 8ull * height;
+    for (uint32_t y = 0; y < height; y++) put_u64(b, first + y * (8 + line_bytes));
+    for (uint32_t y = 0; y < height; y++) {
+        put_u32(b, y);
+        put_u32(b, static_cast<uint32_t>(line_bytes));
+        for (int ch : {3, 2, 1, 0})  // A, B, G, R
+            for (uint32_t x = 0; x < width; x++) put_f32(b, rgba[4 * ((size_t)y * width + x) + ch]);
+    }
+    std::ofstream f(path, std::ios::binary);
+    if (!f) {
+        error = "cannot write '" + path + "'";
+        return false;
+    }
+    f.write(reinterpret_cast<const char *>(b.data()), static_cast<std::streamsize>(b.size()));
+    return static_cast<bool>(f);
+}
 
 bool LoadImageRGBA(const std::string &path, std::vector<float> &rgba, uint32_t &width, uint32_t &height,
                    std::string &error) {
     const std::string ext = lower_ext(path);
-    if (ext != "hdr" && ext != "pfm") {
-        error = "image '" + path + "': only .hdr (RGBE) and .pfm images can be read";
+    if (ext != "hdr" && ext != "pfm" && ext != "exr") {
+        error = "image '" + path + "': only .hdr (RGBE), .pfm and uncompressed .exr images can be read";
         return false;
     }
     std::vector<uint8_t> data;
     if (!read_all(path, data, error)) return false;
-    const bool ok = ext == "hdr" ? load_hdr(data, rgba, width, height, error) : load_pfm(data, rgba, width, height, error);
+    const bool ok = ext == "hdr"   ? load_hdr(data, rgba, width, height, error)
+                    : ext == "exr" ? load_exr(data, rgba, width, height, error)
+                                   : load_pfm(data, rgba, width, height, error);
     if (!ok) error = "image '" + path + "': " + error;
     return ok;
 }

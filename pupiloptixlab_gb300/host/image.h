@@ -7,7 +7,9 @@
 //         mantissa * 2^(exponent - 136), 0 when the exponent byte is 0;
 //   .pfm  portable float map (PF colour / Pf grey, either byte order, rows
 //         stored bottom-up in the file);
-// both returned as RGBA floats, alpha 1, first row = top of the image, as
+//   .exr  OpenEXR scanline images without compression (HALF or FLOAT R, G, B
+//         and optional A channels; compressed files are reported as such);
+// all returned as RGBA floats, alpha 1, first row = top of the image, as
 // util::BitmapTexture holds them.  Other formats are reported as unsupported.
 #pragma once
 
@@ -19,5 +21,10 @@ namespace Pupil::util {
 
 bool LoadImageRGBA(const std::string &path, std::vector<float> &rgba, uint32_t &width, uint32_t &height,
                    std::string &error);
+
+// OpenEXR, scanline, uncompressed, channels A B G R as 32-bit floats, one
+// scanline per block (the headless counterpart of the GUI's image save,
+// framework/util/texture.cpp SaveExr).  rgba: width*height*4, first row = top.
+bool SaveExrRGBA(const std::string &path, const float *rgba, uint32_t width, uint32_t height, std::string &error);
 
 }  // namespace Pupil::util

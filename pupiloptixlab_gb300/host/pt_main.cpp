@@ -1,6 +1,7 @@
 // pt_main.cpp -- headless counterpart of example/path_tracer/main.cpp: load a
-// mitsuba-style scene, run the WavefrontPTPass for N frames, write a PFM.
-//   pupil_pt <scene.xml> <out.pfm> [frames=64] [rng: lcg|pcg32]
+// mitsuba-style scene, run the WavefrontPTPass for N frames, write the frame
+// as PFM or (by the .exr extension) uncompressed OpenEXR.
+//   pupil_pt <scene.xml> <out.pfm|out.exr> [frames=64] [rng: lcg|pcg32]
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -11,10 +12,11 @@
 #include "pass.h"
 
 extern "C" int pupil_write_pfm(const char *path, const float *rgba, uint32_t w, uint32_t h);
+extern "C" int pupil_write_exr(const char *path, const float *rgba, uint32_t w, uint32_t h);
 
 int main(int argc, char **argv) {
     if (argc < 3) {
-        fprintf(stderr, "usage: %s <scene.xml> <out.pfm> [frames] [lcg|pcg32]\n", argv[0]);
+        fprintf(stderr, "usage: %s <scene.xml> <out.pfm|out.exr> [frames] [lcg|pcg32]\n", argv[0]);
         return 2;
     }
     uint32_t frames = argc > 3 ? (uint32_t)std::stoul(argv[3]) : 64;
@@ -39,7 +41,21 @@ int main(int argc, char **argv) {
     uint32_t w = sys->scene()->sensor.width, h = sys->scene()->sensor.height;
     std::vector<float> img((size_t)w * h * 4);
     cudaMemcpy(img.data(), sys->buffers().GetBuffer("final result")->device, img.size() * 4, cudaMemcpyDeviceToHost);
-    pupil_write_pfm(argv[2], img.data(), w, h);
+    const std::string out = argv[2];
+    int st;
+    if (out.size() > 4 && out.compare(out.size() - 4, 4, ".exr") == 0) {
+        // the frame's row 0 is the bottom of the image (PFM order); EXR stores the top first
+        std::vector<float> top((size_t)w * h * 4);
+        for (uint32_t y = 0; y < h; y++)
+            memcpy(&top[(size_t)y * w * 4], &img[(size_t)(h - 1 - y) * w * 4], (size_t)w * 4 * sizeof(float));
+        st = pupil_write_exr(argv[2], top.data(), w, h);
+    } else {
+        st = pupil_write_pfm(argv[2], img.data(), w, h);
+    }
+    if (st != PT_OK) {
+        fprintf(stderr, "cannot write %s\n", argv[2]);
+        return 1;
+    }
     printf("%s: %ux%u, %u frames, last frame %.2f ms\n", argv[2], w, h, frames, pass.last_exec_ms);
     sys->Destroy();
     return 0;

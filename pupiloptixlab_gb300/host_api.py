@@ -28,6 +28,7 @@ def load() -> C.CDLL:
         lib.pupil_run_scene.argtypes = [C.c_char_p, C.c_int, C.c_uint32, C.c_uint32, C.c_void_p,
                                         C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
         lib.pupil_write_pfm.argtypes = [C.c_char_p, C.c_void_p, C.c_uint32, C.c_uint32]
+        lib.pupil_write_exr.argtypes = [C.c_char_p, C.c_void_p, C.c_uint32, C.c_uint32]
         _lib = lib
     return _lib
 
@@ -74,3 +75,12 @@ def run_scene(path_or_text: str, frames: int, rng: int = abi.RNG_REF_LCG, is_tex
     if st != 0:
         raise abi.PtError(st, "pupil_run_scene", last_error())
     return out
+
+
+def write_exr(path: str, rgba: np.ndarray) -> None:
+    """(h, w, 4) float32, first row = top -> uncompressed scanline OpenEXR."""
+    lib = load()
+    px = np.ascontiguousarray(rgba, np.float32)
+    st = lib.pupil_write_exr(str(path).encode(), px.ctypes.data_as(C.c_void_p), px.shape[1], px.shape[0])
+    if st != 0:
+        raise abi.PtError(st, "pupil_write_exr", last_error())
