@@ -126,7 +126,7 @@ def test_obj_mesh(host):
     ("<scene><shape type='rectangle'><bsdf type='diffuse'><texture type='bitmap' name='reflectance'/>"
      "</bsdf></shape></scene>", "without a filename"),
     ("<scene><shape type='rectangle'><bsdf type='diffuse'><texture type='bitmap' name='reflectance'>"
-     "<string name='filename' value='a.png'/></texture></bsdf></shape></scene>", ".hdr (RGBE) and .pfm"),
+     "<string name='filename' value='a.png'/></texture></bsdf></shape></scene>", "uncompressed .exr images can be read"),
     ("<scene><sensor type='thinlens'/></scene>", "perspective"),
     ("<notascene/>", "<scene>"),
     ("<scene><a></b></scene>", "mismatched"),
