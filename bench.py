@@ -42,6 +42,9 @@ sys.path.insert(0, str(ROOT))
 WORKLOAD = "1M-triangle displaced-icosphere field (200 x 5120 tris + 8192 ground tris + 4 sphere lights), " \
            "1920x1080, 64 spp, max depth 8, NEE+MIS, 7 materials"
 METRIC = "Msamples/s at 1080p depth 8 (1 GB300)"
+HAIR_WORKLOAD = "{n} strands x 16 points (curve type {t}, radius 0.003) on a head sphere + floor + sphere light, " \
+                "1920x1080, 64 spp, max depth 8, NEE+MIS"
+HAIR_METRIC = "Msamples/s at 1080p depth 8, hair (1 GB300)"
 
 
 def parse():
@@ -50,8 +53,11 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="headline", choices=["headline", "dynamic", "denoise", "batch"],
-                    help="headline: the 1M-triangle 1080p frame; dynamic: 4M jittered triangles, rebuild vs refit")
+    ap.add_argument("--workload", default="headline", choices=["headline", "dynamic", "denoise", "batch", "hair"],
+                    help="headline: the 1M-triangle 1080p frame; dynamic: 4M jittered triangles, rebuild vs refit; "
+                         "hair: cubic B-spline strands on a head, the same 1080p frame measurement")
+    ap.add_argument("--hair-strands", type=int, default=50000, help="strands of the hair workload")
+    ap.add_argument("--hair-type", type=int, default=2, help="curve type of the hair workload (0..3, PT_CURVE_*)")
     ap.add_argument("--frames", type=int, default=120, help="frames of the dynamic workload")
     ap.add_argument("--batch-scenes", type=int, default=64, help="scenes of the multi-scene workload")
     ap.add_argument("--batch-spp", type=int, default=16)
@@ -544,7 +550,13 @@ def main():
             dist.barrier()
         torch.cuda.synchronize()
 
-    sc = scenes.icosphere_field(args.width, args.height, args.depth, args.instances)
+    if args.workload == "hair":
+        sc = scenes.hair_scene(args.width, args.height, curve_type=args.hair_type, num_strands=args.hair_strands,
+                               points=16, radius=0.003, max_depth=args.depth, curl=0.08)
+        metric, workload = HAIR_METRIC, HAIR_WORKLOAD.format(n=args.hair_strands, t=args.hair_type)
+    else:
+        sc = scenes.icosphere_field(args.width, args.height, args.depth, args.instances)
+        metric, workload = METRIC, WORKLOAD
     ctx = Context(local)
     g = GpuScene(ctx, sc, bvh_width=args.bvh_width, max_leaf=args.max_leaf, smem_nodes=args.smem_nodes)
     buffers = g.alloc_buffers()
@@ -634,12 +646,13 @@ def main():
     if not args.no_cpu_baseline:
         cpu = cpu_baseline(sc, 0, args.cpu_seconds, args.depth)
     line = {
-        "metric": METRIC, "value": value, "unit": "Msamples/s", "n_gpus": ws, "steps": args.steps,
+        "metric": metric, "value": value, "unit": "Msamples/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
-        "config": {"workload": WORKLOAD, "width": args.width, "height": args.height, "spp": args.spp,
+        "config": {"workload": workload, "width": args.width, "height": args.height, "spp": args.spp,
                    "max_depth": args.depth, "rng": "pcg32", "bvh_width": args.bvh_width, "max_leaf": args.max_leaf,
-                   "smem_nodes": args.smem_nodes, "triangles": int(bst.num_prims),
+                   "smem_nodes": args.smem_nodes, "primitives": int(bst.num_prims),
+                   "curve_segments_pieces": list(g.num_curves()) if args.workload == "hair" else None,
                    "material_sort": not args.no_material_sort, "autotune": tune, "cuda_graph": not args.no_graph,
                    "l2": "flushed between steps (256 MiB write, outside the timed events)",
                    "parallelism": "replicas only" if ws > 1 else "single GPU"},

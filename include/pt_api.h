@@ -144,16 +144,43 @@ typedef struct pt_sphere_desc {
     float radius;
 } pt_sphere_desc;
 
-enum { PT_SHAPE_MESH = 0, PT_SHAPE_SPHERE = 1 };
+/* Curve strands (hair) in object space: resource::Shape _hair
+ * (framework/resource/shape.cpp:369-420) as handed to the OptiX curve build
+ * input (framework/world/gas_manager.cpp:112-150).  Segment i uses the
+ * control points segments[i] .. segments[i] + degree (degree 1 linear,
+ * 2 quadratic B-spline, 3 cubic B-spline and Catmull-Rom); radii are the
+ * per-point radii the reference calls widths.  Segments of one strand are
+ * consecutive control-point indices, so a strand ends where segments[i+1] !=
+ * segments[i] + 1.  Round segments: linear segments have spherical caps at
+ * both ends; the spline types are open at strand ends (OptiX's default end
+ * caps).  Only hits entering the tube from outside are reported. */
+enum {
+    PT_CURVE_LINEAR = 0,
+    PT_CURVE_QUADRATIC_BSPLINE = 1,
+    PT_CURVE_CUBIC_BSPLINE = 2,
+    PT_CURVE_CATMULL_ROM = 3
+};
+typedef struct pt_curves_desc {
+    const float *positions;   /* num_points * 3 */
+    const float *radii;       /* num_points */
+    const uint32_t *segments; /* num_segments: first control point of each segment */
+    uint32_t num_points;
+    uint32_t num_segments;
+    uint32_t type;            /* PT_CURVE_* */
+} pt_curves_desc;
+
+enum { PT_SHAPE_MESH = 0, PT_SHAPE_SPHERE = 1, PT_SHAPE_CURVES = 2 };
 enum { PT_INST_FLIP_NORMALS = 1, PT_INST_FLIP_TEXCOORDS = 2 };
 
 /* One shape instance (resource::ShapeInstance; world::RenderObject,
  * framework/world/render_object.h:11-38).  to_world is a row-major 4x4 with
  * the translation in the last column (util::Transform).  Spheres accept
- * similarity transforms only (rotation, uniform scale, translation). */
+ * similarity transforms only (rotation, uniform scale, translation); curve
+ * radii scale by the length of the transformed x axis.  Curves cannot be
+ * emitters. */
 typedef struct pt_instance_desc {
     uint32_t shape_type;  /* PT_SHAPE_* */
-    uint32_t shape_index; /* into meshes[] or spheres[] */
+    uint32_t shape_index; /* into meshes[], spheres[] or curves[] */
     uint32_t material;    /* into materials[] */
     uint32_t flags;       /* PT_INST_* */
     float to_world[16];
@@ -196,6 +223,8 @@ typedef struct pt_scene_desc {
     uint32_t width;     /* film size (resource::Film) */
     uint32_t height;
     uint32_t max_depth; /* integrator max_depth (resource::Integrator) */
+    const pt_curves_desc *curves;
+    uint32_t num_curves;
 } pt_scene_desc;
 
 typedef struct pt_context pt_context;
@@ -327,6 +356,9 @@ int pt_scene_update_vertices(pt_scene *scene, uint32_t mesh, const float *positi
 int pt_scene_update_all_vertices(pt_scene *scene, const float *positions, int on_device, void *stream);
 /* Number of primitives (triangles then spheres) in world order. */
 int pt_scene_num_prims(const pt_scene *scene, uint32_t *num_triangles, uint32_t *num_spheres);
+/* Curve segments of all curve instances and the round-cone pieces they were
+ * split into (each piece is one acceleration-structure primitive). */
+int pt_scene_num_curves(const pt_scene *scene, uint32_t *num_segments, uint32_t *num_pieces);
 
 /* ---- acceleration structure ------------------------------------------ */
 int pt_bvh_build(pt_scene *scene, const pt_bvh_opts *opts, void *stream);

@@ -45,6 +45,9 @@ def load() -> C.CDLL:
         lib.oracle_scene_destroy.argtypes = [_VP]
         lib.oracle_scene_destroy.restype = None
         lib.oracle_scene_num_prims.argtypes = [_VP, _VP, _VP]
+        lib.oracle_scene_num_curves.argtypes = [_VP, _VP, _VP]
+        lib.oracle_curve.argtypes = [C.c_uint32, _VP, _VP, _VP, _VP, C.c_uint32]
+        lib.oracle_scene_curve_pieces.argtypes = [_VP, _VP]
         lib.oracle_scene_world_triangles.argtypes = [_VP, _VP]
         lib.oracle_trace_rays.argtypes = [_VP, _VP, _VP, C.c_uint32, C.c_int, C.c_int, C.c_int]
         lib.oracle_camera_rays.argtypes = [_VP, C.c_uint32, C.c_uint32, _VP]
@@ -89,6 +92,7 @@ def load_ref() -> C.CDLL | None:
         r.ref_select_emitter.argtypes = [_VP, C.c_uint32, C.c_int, _VP, _VP, C.c_uint32]
         r.ref_envmap.argtypes = [C.c_int, _VP, C.c_uint32, C.c_uint32, C.c_float, _VP, _VP, _VP, _VP, _VP,
                                  C.c_float, _VP, _VP, C.c_uint32]
+        r.ref_curve.argtypes = [C.c_uint32, _VP, _VP, _VP, _VP, C.c_uint32]
         _ref = r
     return _ref
 
@@ -117,6 +121,19 @@ class OracleScene:
         a, b = C.c_uint32(), C.c_uint32()
         self.lib.oracle_scene_num_prims(self.handle, C.byref(a), C.byref(b))
         return a.value, b.value
+
+    def num_curves(self):
+        a, b = C.c_uint32(), C.c_uint32()
+        self.lib.oracle_scene_num_curves(self.handle, C.byref(a), C.byref(b))
+        return a.value, b.value
+
+    def curve_pieces(self) -> np.ndarray:
+        """(pieces, 12): c0 xyz, r0, c1 xyz, r1, u0, u1, kind, segment."""
+        _, n = self.num_curves()
+        out = np.zeros((n, 12), np.float32)
+        if n:
+            self.lib.oracle_scene_curve_pieces(self.handle, _ptr(out))
+        return out
 
     def world_triangles(self) -> np.ndarray:
         nt, _ = self.num_prims()
@@ -190,6 +207,24 @@ def envmap(mode: int, pixels: np.ndarray, scale: float, to_world3: np.ndarray, t
     if st != 0:
         raise RuntimeError(f"oracle_envmap failed: {st}")
     return out, tables
+
+
+def curve(curve_type: int, ctrl: np.ndarray, u: np.ndarray, ps: np.ndarray, lib=None) -> np.ndarray:
+    """Curve evaluation KAT: ctrl (n, 4, 4) control points, u (n,), ps (n, 3)
+    -> (n, 15) position4, velocity4, acceleration3, surface normal3, 0.
+    lib = load_ref() evaluates the reference's own interpolators instead."""
+    ctrl = np.ascontiguousarray(ctrl, np.float32)
+    u = np.ascontiguousarray(u, np.float32)
+    ps = np.ascontiguousarray(ps, np.float32)
+    n = u.shape[0]
+    out = np.zeros((n, 15), np.float32)
+    if lib is None:
+        st = load().oracle_curve(curve_type, _ptr(ctrl), _ptr(u), _ptr(ps), _ptr(out), n)
+    else:
+        st = lib.ref_curve(curve_type, _ptr(ctrl), _ptr(u), _ptr(ps), _ptr(out), n)
+    if st != 0:
+        raise RuntimeError(f"curve KAT failed: {st}")
+    return out
 
 
 def bsdf_eval(bsdf, wo, wi):

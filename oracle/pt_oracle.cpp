@@ -906,6 +906,7 @@ struct Instance {
     float inv[12]{};             // world -> object (spheres: texcoords)
     V3 center{0, 0, 0};
     float radius = 0.f;
+    uint32_t curve_type = 0;     // PT_CURVE_* of a curves instance
 };
 
 static void mat_inverse_dd(const double *a, double out[16]) {
@@ -1023,6 +1024,189 @@ static inline bool intersect_sphere(const Ray &ray, V3 c, float r, float tmax, f
     return false;
 }
 
+// ---------------------------------------------------------------- curves
+// Round curve segments (hair).  Evaluation and the hit-point normal restate
+// the reference's interpolators and SurfaceNormal (framework/render/curve.h:
+// 35-342) in their operation order, as Geometry::GetHitLocalGeometry uses
+// them per curve type (framework/render/geometry.h:101-172).  OptiX's curve
+// intersector is closed, so a segment is intersected the way the library
+// does it: as round-cone pieces (lateral frustum surface plus joint spheres,
+// entering hits only), its curve parameter the projection onto the axis.
+
+static inline V4 v4add(V4 a, V4 b) { return {a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w}; }
+static inline V4 v4sub(V4 a, V4 b) { return {a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w}; }
+static inline V4 v4scale(float s, V4 a) { return {a.x * s, a.y * s, a.z * s, a.w * s}; }
+static inline V4 v4over(V4 a, float s) { float inv = 1.0f / s; return v4scale(inv, a); }  // vec_math: times 1/s
+static inline V3 v4xyz(V4 a) { return {a.x, a.y, a.z}; }
+
+enum : int { kPieceCurve = 1, kPieceSphere0 = 2, kPieceSphere1 = 4, kPieceClampU = 8 };
+constexpr float kCurveUMin = 9.5367431640625e-07f;     // 2^-20
+constexpr float kCurveUMax = 0.99999904632568359375f;  // 1 - 2^-20
+
+struct CurvePoly {
+    uint32_t degree = 1;
+    V4 p[4]{};  // power basis, highest power first (LinearInterpolator p[0] + u p[1], ...)
+};
+
+static CurvePoly curve_poly(uint32_t type, const V4 *q) {
+    CurvePoly c;
+    switch (type) {
+        case PT_CURVE_LINEAR:  // LinearInterpolator::Initialize (curve.h:39-42)
+            c.degree = 1;
+            c.p[0] = q[0];
+            c.p[1] = v4sub(q[1], q[0]);
+            break;
+        case PT_CURVE_QUADRATIC_BSPLINE:  // QuadraticInterpolator::InitializeFromBSpline (curve.h:81-89)
+            c.degree = 2;
+            c.p[0] = v4over(v4add(v4sub(q[0], v4scale(2.0f, q[1])), q[2]), 2.0f);
+            c.p[1] = v4over(v4add(v4scale(-2.0f, q[0]), v4scale(2.0f, q[1])), 2.0f);
+            c.p[2] = v4over(v4add(q[0], q[1]), 2.0f);
+            break;
+        case PT_CURVE_CUBIC_BSPLINE:  // CubicInterpolator::InitializeFromBSpline (curve.h:150-159)
+            c.degree = 3;
+            c.p[0] = v4over(v4add(v4add(v4add(v4scale(-1.0f, q[0]), v4scale(3.0f, q[1])), v4scale(-3.0f, q[2])), q[3]), 6.0f);
+            c.p[1] = v4over(v4add(v4add(v4scale(3.0f, q[0]), v4scale(-6.0f, q[1])), v4scale(3.0f, q[2])), 6.0f);
+            c.p[2] = v4over(v4add(v4scale(-3.0f, q[0]), v4scale(3.0f, q[2])), 6.0f);
+            c.p[3] = v4over(v4add(v4add(v4scale(1.0f, q[0]), v4scale(4.0f, q[1])), v4scale(1.0f, q[2])), 6.0f);
+            break;
+        default:  // CubicInterpolator::InitializeFromCatrom (curve.h:180-189)
+            c.degree = 3;
+            c.p[0] = v4over(v4add(v4add(v4add(v4scale(-1.0f, q[0]), v4scale(3.0f, q[1])), v4scale(-3.0f, q[2])), v4scale(1.0f, q[3])), 2.0f);
+            c.p[1] = v4over(v4add(v4add(v4add(v4scale(2.0f, q[0]), v4scale(-5.0f, q[1])), v4scale(4.0f, q[2])), v4scale(-1.0f, q[3])), 2.0f);
+            c.p[2] = v4over(v4add(v4scale(-1.0f, q[0]), v4scale(1.0f, q[2])), 2.0f);
+            c.p[3] = v4over(v4scale(2.0f, q[1]), 2.0f);
+            break;
+    }
+    return c;
+}
+
+static V4 curve_position4(const CurvePoly &c, float u) {  // Position4 (Horner)
+    if (c.degree == 1) return v4add(c.p[0], v4scale(u, c.p[1]));
+    if (c.degree == 2) return v4add(v4scale(u, v4add(v4scale(u, c.p[0]), c.p[1])), c.p[2]);
+    return v4add(v4scale(u, v4add(v4scale(u, v4add(v4scale(u, c.p[0]), c.p[1])), c.p[2])), c.p[3]);
+}
+static V4 curve_velocity4(const CurvePoly &c, float u) {  // Velocity4
+    if (c.degree == 1) return c.p[1];
+    if (c.degree == 2) return v4add(v4scale(u, v4scale(2.0f, c.p[0])), c.p[1]);
+    if (u == 0) u = 0.000001f;  // curve.h:207-211 (triple knots)
+    if (u == 1) u = 0.999999f;
+    return v4add(v4scale(u, v4add(v4scale(u, v4scale(3.0f, c.p[0])), v4scale(2.0f, c.p[1]))), c.p[2]);
+}
+static V3 curve_acceleration3(const CurvePoly &c, float u) {  // Acceleration3
+    if (c.degree == 1) return v3s(0.f);
+    if (c.degree == 2) return v4xyz(v4scale(2.0f, c.p[0]));
+    return v4xyz(v4add(v4scale(u, v4scale(6.0f, c.p[0])), v4scale(2.0f, c.p[1])));
+}
+
+// SurfaceNormal (curve.h:261-292 for the splines, 295-326 for linear segments).
+static V3 curve_surface_normal(const CurvePoly &c, float u, V3 ps) {
+    V3 normal;
+    const bool linear = c.degree == 1;
+    if (u == 0.0f) {
+        normal = linear ? ps - v4xyz(c.p[0]) : -v4xyz(curve_velocity4(c, 0));
+    } else if (linear ? u >= 1.0f : u == 1.0f) {
+        normal = linear ? ps - (v4xyz(c.p[1]) + v4xyz(c.p[0])) : v4xyz(curve_velocity4(c, 1));
+    } else {
+        V4 p4 = curve_position4(c, u);
+        V3 p = v4xyz(p4);
+        float r = p4.w;
+        V4 d4 = curve_velocity4(c, u);
+        V3 d = v4xyz(d4);
+        float dr = d4.w;
+        float dd = dot(d, d);
+        V3 o1 = ps - p;
+        o1 = o1 - (dot(o1, d) / dd) * d;
+        o1 = o1 * (r / length(o1));
+        if (!linear) dd -= dot(curve_acceleration3(c, u), o1);
+        normal = dd * o1 - (dr * r) * d;
+    }
+    return normalize(normal);
+}
+
+// Pieces per segment: chord deviation h^2/8 max|P''| <= 0.05 max radius,
+// 1 .. 16 pieces, linear segments in one piece.
+static uint32_t curve_pieces(const CurvePoly &c, float rmax) {
+    if (c.degree == 1) return 1;
+    V3 a0, a1;
+    if (c.degree == 2) {
+        a0 = a1 = v4xyz(v4scale(2.0f, c.p[0]));
+    } else {
+        a0 = v4xyz(v4scale(2.0f, c.p[1]));
+        a1 = v4xyz(v4add(v4scale(6.0f, c.p[0]), v4scale(2.0f, c.p[1])));
+    }
+    float acc = std::max(length(a0), length(a1));
+    float tol = 0.05f * rmax;
+    if (!(tol > 0.f) || !(acc > 0.f)) return 1;
+    float q = sqrtf(acc / (8.0f * tol));
+    if (!(q < 16.0f)) return 16;
+    uint32_t n = (uint32_t)ceilf(q);
+    return n < 1 ? 1 : n;
+}
+
+struct CurvePiece {
+    V3 c0, c1;
+    float r0 = 0.f, r1 = 0.f, u0 = 0.f, u1 = 0.f;
+    int kind = 0;
+    uint32_t segment = 0;
+};
+
+// Sphere entry with the origin moved to the closest approach first.
+static bool curve_sphere_entry(const Ray &ray, float dd, V3 c, float r, float tmax, float &t_out) {
+    V3 f = ray.o - c;
+    float tc = -dot(f, ray.d) / dd;
+    V3 l = f + tc * ray.d;
+    float h = r * r - dot(l, l);
+    if (!(h >= 0.f)) return false;
+    float t = tc - sqrtf(h / dd);
+    if (!(t > ray.tmin && t < tmax)) return false;
+    t_out = t;
+    return true;
+}
+
+// Round-cone piece: entering root of the frustum quadratic formed from the
+// components normal to the axis, s = projection onto the axis in [0, len],
+// plus the end spheres the kind bits ask for; the smallest entering t wins.
+static bool intersect_curve_piece(const Ray &ray, const CurvePiece &pc, float tmax, float &t_out, float &u_out) {
+    const float dd = dot(ray.d, ray.d);
+    bool hit = false;
+    float best = tmax, bu = 0.f, t;
+    if ((pc.kind & kPieceSphere0) && curve_sphere_entry(ray, dd, pc.c0, pc.r0, best, t)) { hit = true; best = t; bu = pc.u0; }
+    if ((pc.kind & kPieceSphere1) && curve_sphere_entry(ray, dd, pc.c1, pc.r1, best, t)) { hit = true; best = t; bu = pc.u1; }
+    V3 e = pc.c1 - pc.c0;
+    float len = sqrtf(dot(e, e));
+    if (len > 0.f) {
+        float inv_len = 1.0f / len;
+        V3 ax = {e.x * inv_len, e.y * inv_len, e.z * inv_len};
+        float k = (pc.r1 - pc.r0) * inv_len;
+        V3 f = ray.o - pc.c0;
+        float tc = -dot(f, ray.d) / dd;
+        V3 w = f + tc * ray.d;
+        float we = dot(w, ax), de = dot(ray.d, ax);
+        V3 wp = w + (-we) * ax, dp = ray.d + (-de) * ax;
+        float rz = pc.r0 + k * we;
+        float kde = k * de;
+        float A = dot(dp, dp) - kde * kde;
+        float B = dot(wp, dp) - kde * rz;
+        float C = dot(wp, wp) - rz * rz;
+        float disc = B * B - A * C;
+        if (disc >= 0.f && A != 0.f) {
+            float tp = (-B - sqrtf(disc)) / A;
+            float z = we + tp * de;
+            float tt = tc + tp;
+            if (z >= 0.f && z <= len && tt > ray.tmin && tt < best) {
+                hit = true;
+                best = tt;
+                bu = pc.u0 + (z * inv_len) * (pc.u1 - pc.u0);
+            }
+        }
+    }
+    if (!hit) return false;
+    if (pc.kind & kPieceClampU) bu = std::min(std::max(bu, kCurveUMin), kCurveUMax);
+    t_out = best;
+    u_out = bu;
+    return true;
+}
+
 struct Box {
     V3 lo{INFINITY, INFINITY, INFINITY}, hi{-INFINITY, -INFINITY, -INFINITY};
     void grow(V3 p) {
@@ -1060,8 +1244,11 @@ struct Scene {
     // World-space vertex data (per mesh instance).
     std::vector<V3> vpos, vnrm;
     std::vector<V2> vuv;
-    // Primitives in world order: triangles then spheres.
-    uint32_t num_tris = 0, num_spheres = 0;
+    // Primitives in world order: triangles, spheres, then curve pieces.
+    uint32_t num_tris = 0, num_spheres = 0, num_pieces = 0;
+    std::vector<CurvePiece> pieces;
+    std::vector<V4> curve_cp;             // 4 world control points per segment
+    uint32_t num_prims() const { return num_tris + num_spheres + num_pieces; }
     std::vector<uint32_t> tri_vidx;       // 3 per triangle, global vertex ids
     std::vector<uint32_t> prim_instance;  // per primitive
     std::vector<uint32_t> prim_local;     // index within its mesh
@@ -1078,6 +1265,12 @@ struct Scene {
         Box b;
         if (p < num_tris) {
             b.grow(tri_p[3 * p]); b.grow(tri_p[3 * p + 1]); b.grow(tri_p[3 * p + 2]);
+        } else if (p >= num_tris + num_spheres) {
+            const CurvePiece &pc = pieces[p - num_tris - num_spheres];
+            b.grow(pc.c0 - v3s(pc.r0));
+            b.grow(pc.c0 + v3s(pc.r0));
+            b.grow(pc.c1 - v3s(pc.r1));
+            b.grow(pc.c1 + v3s(pc.r1));
         } else {
             const Instance &in = instances[prim_instance[p]];
             b.grow(in.center - v3s(in.radius));
@@ -1088,8 +1281,9 @@ struct Scene {
 
     bool intersect_prim(uint32_t p, const Ray &ray, const RayWT &w, float tmax, float &t, float &u, float &v) const {
         if (p < num_tris) return intersect_triangle(ray, w, tri_p[3 * p], tri_p[3 * p + 1], tri_p[3 * p + 2], tmax, t, u, v);
-        const Instance &in = instances[prim_instance[p]];
         u = v = 0.f;
+        if (p >= num_tris + num_spheres) return intersect_curve_piece(ray, pieces[p - num_tris - num_spheres], tmax, t, u);
+        const Instance &in = instances[prim_instance[p]];
         return intersect_sphere(ray, in.center, in.radius, tmax, t);
     }
 
@@ -1098,7 +1292,7 @@ struct Scene {
         Hit best;
         best.t = ray.tmax;
         RayWT w = ray_wt(ray.d);
-        uint32_t np = num_tris + num_spheres;
+        uint32_t np = num_prims();
         for (uint32_t p = 0; p < np; p++) {
             float t, u, v;
             if (!intersect_prim(p, ray, w, ray.tmax, t, u, v)) continue;
@@ -1165,7 +1359,7 @@ struct Scene {
 
     // Binned-SAH BVH2 (16 bins on centroids, leaves of up to 4 primitives).
     void build_bvh() {
-        uint32_t np = num_tris + num_spheres;
+        uint32_t np = num_prims();
         nodes.clear();
         prim_order.resize(np);
         if (np == 0) return;
@@ -1256,7 +1450,12 @@ struct Scene {
         uint32_t p = (uint32_t)h.prim;
         const Instance &in = instances[prim_instance[p]];
         const Material &m = materials[in.material];
-        if (p < num_tris) {
+        if (p >= num_tris + num_spheres) {  // geometry.h:101-172 (world space)
+            g.position = ray.o + h.t * ray.d;
+            const CurvePiece &pc = pieces[p - num_tris - num_spheres];
+            CurvePoly c = curve_poly(in.curve_type, &curve_cp[4 * (size_t)pc.segment]);
+            g.normal = curve_surface_normal(c, h.u, g.position);
+        } else if (p < num_tris) {
             uint32_t i0 = tri_vidx[3 * p], i1 = tri_vidx[3 * p + 1], i2 = tri_vidx[3 * p + 2];
             float w0 = 1.f - h.u - h.v;
             g.position = w0 * vpos[i0] + h.u * vpos[i1] + h.v * vpos[i2];
@@ -1352,6 +1551,9 @@ static int build_scene(const pt_scene_desc *d, Scene &s) {
             s.num_tris += m.num_triangles;
         } else if (id.shape_type == PT_SHAPE_SPHERE) {
             if (id.shape_index >= d->num_spheres) return PT_ERR_OOB;
+        } else if (id.shape_type == PT_SHAPE_CURVES) {
+            if (id.shape_index >= d->num_curves || id.is_emitter) return PT_ERR_INVALID;
+            in.curve_type = d->curves[id.shape_index].type;
         } else {
             return PT_ERR_INVALID;
         }
@@ -1372,6 +1574,58 @@ static int build_scene(const pt_scene_desc *d, Scene &s) {
         s.prim_instance.push_back(ii);
         s.prim_local.push_back(0);
         s.num_spheres++;
+    }
+    // pass 3: curve segments as round-cone pieces, after the spheres
+    uint32_t nseg = 0;
+    for (uint32_t ii = 0; ii < d->num_instances; ii++) {
+        const pt_instance_desc &id = d->instances[ii];
+        if (id.shape_type != PT_SHAPE_CURVES) continue;
+        Instance &in = s.instances[ii];
+        const pt_curves_desc &cv = d->curves[id.shape_index];
+        if (cv.type > PT_CURVE_CATMULL_ROM) return PT_ERR_INVALID;
+        in.prim_offset = s.num_tris + s.num_spheres + s.num_pieces;
+        const float *m = id.to_world;
+        const float scale = length(v3(m[0], m[4], m[8]));
+        const uint32_t deg = cv.type > 2 ? 3u : cv.type + 1u;  // shape.cpp:383
+        for (uint32_t i = 0; i < cv.num_segments; i++, nseg++) {
+            const uint32_t first = cv.segments[i];
+            if ((uint64_t)first + deg >= cv.num_points) return PT_ERR_OOB;
+            V4 q[4]{};
+            float rmax = 0.f;
+            for (uint32_t j = 0; j <= deg; j++) {
+                const uint32_t v = first + j;
+                V3 pw = xform_point(m, v3(cv.positions[3 * v], cv.positions[3 * v + 1], cv.positions[3 * v + 2]));
+                q[j] = {pw.x, pw.y, pw.z, cv.radii[v] * scale};
+                rmax = std::max(rmax, q[j].w);
+            }
+            for (int j = 0; j < 4; j++) s.curve_cp.push_back(q[j]);
+            if (!(rmax > 0.f)) continue;
+            const bool strand_first = i == 0 || cv.segments[i - 1] + 1 != first;
+            const bool strand_last = i + 1 == cv.num_segments || cv.segments[i + 1] != first + 1;
+            CurvePoly c = curve_poly(cv.type, q);
+            uint32_t np = curve_pieces(c, rmax);
+            for (uint32_t k = 0; k < np; k++) {
+                CurvePiece pc;
+                pc.u0 = (float)k / (float)np;
+                pc.u1 = (float)(k + 1) / (float)np;
+                V4 a = curve_position4(c, pc.u0), b = curve_position4(c, pc.u1);
+                pc.c0 = v4xyz(a);
+                pc.c1 = v4xyz(b);
+                pc.r0 = std::max(a.w, 0.f);
+                pc.r1 = std::max(b.w, 0.f);
+                pc.kind = kPieceCurve;
+                if (cv.type == PT_CURVE_LINEAR) {
+                    pc.kind |= kPieceSphere0 | (strand_last ? kPieceSphere1 : 0);
+                } else {
+                    pc.kind |= kPieceClampU | ((k > 0 || !strand_first) ? kPieceSphere0 : 0);
+                }
+                pc.segment = nseg;
+                s.pieces.push_back(pc);
+                s.prim_instance.push_back(ii);
+                s.prim_local.push_back(k);
+                s.num_pieces++;
+            }
+        }
     }
     // emitters in instance order (world/emitter.cpp:169-263)
     for (uint32_t ii = 0; ii < d->num_instances; ii++) {
@@ -1654,6 +1908,47 @@ int oracle_scene_num_prims(const oracle_scene *scene, uint32_t *nt, uint32_t *ns
     if (!scene) return PT_ERR_INVALID;
     if (nt) *nt = scene->s.num_tris;
     if (ns) *ns = scene->s.num_spheres;
+    return PT_OK;
+}
+
+int oracle_scene_num_curves(const oracle_scene *scene, uint32_t *segments, uint32_t *pieces) {
+    if (!scene) return PT_ERR_INVALID;
+    if (segments) *segments = (uint32_t)(scene->s.curve_cp.size() / 4);
+    if (pieces) *pieces = scene->s.num_pieces;
+    return PT_OK;
+}
+
+// Piece table: 12 floats per piece (c0 xyz, r0, c1 xyz, r1, u0, u1, kind, segment).
+int oracle_scene_curve_pieces(const oracle_scene *scene, float *out) {
+    if (!scene || !out) return PT_ERR_INVALID;
+    for (size_t i = 0; i < scene->s.pieces.size(); i++) {
+        const CurvePiece &p = scene->s.pieces[i];
+        float *o = out + 12 * i;
+        o[0] = p.c0.x; o[1] = p.c0.y; o[2] = p.c0.z; o[3] = p.r0;
+        o[4] = p.c1.x; o[5] = p.c1.y; o[6] = p.c1.z; o[7] = p.r1;
+        o[8] = p.u0; o[9] = p.u1; o[10] = (float)p.kind; o[11] = (float)p.segment;
+    }
+    return PT_OK;
+}
+
+// Curve KAT (layout of ref_curve in oracle/ref_kat.cpp): per case 16 floats of
+// control points (4 x xyzw), u, and a point ps; out 15 floats: position4,
+// velocity4, acceleration3, surface normal3 (ps projected as the reference does).
+int oracle_curve(uint32_t type, const float *ctrl, const float *u, const float *ps, float *out, uint32_t n) {
+    if (type > PT_CURVE_CATMULL_ROM) return PT_ERR_INVALID;
+    for (uint32_t i = 0; i < n; i++) {
+        V4 q[4];
+        for (int j = 0; j < 4; j++) q[j] = {ctrl[16 * i + 4 * j], ctrl[16 * i + 4 * j + 1], ctrl[16 * i + 4 * j + 2], ctrl[16 * i + 4 * j + 3]};
+        CurvePoly c = curve_poly(type, q);
+        V4 p4 = curve_position4(c, u[i]), d4 = curve_velocity4(c, u[i]);
+        V3 a3 = curve_acceleration3(c, u[i]);
+        V3 nrm = curve_surface_normal(c, u[i], v3(ps[3 * i], ps[3 * i + 1], ps[3 * i + 2]));
+        float *o = out + 15 * (size_t)i;
+        o[0] = p4.x; o[1] = p4.y; o[2] = p4.z; o[3] = p4.w;
+        o[4] = d4.x; o[5] = d4.y; o[6] = d4.z; o[7] = d4.w;
+        o[8] = a3.x; o[9] = a3.y; o[10] = a3.z;
+        o[11] = nrm.x; o[12] = nrm.y; o[13] = nrm.z; o[14] = 0.f;
+    }
     return PT_OK;
 }
 

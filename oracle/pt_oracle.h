@@ -26,6 +26,13 @@ typedef struct oracle_scene oracle_scene;
 int oracle_scene_create(const pt_scene_desc *desc, int build_bvh, oracle_scene **out);
 void oracle_scene_destroy(oracle_scene *scene);
 int oracle_scene_num_prims(const oracle_scene *scene, uint32_t *num_triangles, uint32_t *num_spheres);
+/* Curve segments of all curve instances and the round-cone pieces (primitives) they became. */
+int oracle_scene_num_curves(const oracle_scene *scene, uint32_t *segments, uint32_t *pieces);
+/* Piece table, 12 floats per piece: c0 xyz, r0, c1 xyz, r1, u0, u1, kind bits, segment. */
+int oracle_scene_curve_pieces(const oracle_scene *scene, float *out);
+/* Curve evaluation KAT: ctrl n*16 (4 control points xyzw), u n, ps n*3;
+ * out n*15 = position4, velocity4, acceleration3, normal3, 0. */
+int oracle_curve(uint32_t type, const float *ctrl, const float *u, const float *ps, float *out, uint32_t n);
 /* World-space triangle vertices in primitive order: n_tri * 9 floats. */
 int oracle_scene_world_triangles(const oracle_scene *scene, float *out);
 

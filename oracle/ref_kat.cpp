@@ -14,6 +14,7 @@
 //   framework/render/material/{fresnel,ggx}.h
 //   framework/optix/util.h
 //   framework/render/emitter.h, framework/render/emitter/{area,sphere,env}.h
+//   framework/render/curve.h (curve interpolators, SurfaceNormal)
 // Shims (oracle/ref_shims): optix.h, cuda/texture.h, cuda/random.h.
 // The material dispatch (optix_material.h:70-91) uses MSVC-only token pasting,
 // so the switch over the seven Local types below restates it.
@@ -23,6 +24,7 @@
 #include "render/material/ggx.h"
 #include "optix/util.h"
 #include "render/emitter.h"
+#include "render/curve.h"
 
 #include <cstdint>
 #include <cstring>
@@ -323,6 +325,45 @@ int ref_envmap(int mode, const float *pixels, uint32_t w, uint32_t h, float scal
 // EmitterGroup::SelectOneEmiiter over an area list with the given select
 // probabilities (and an optional env); returns the selected index per p
 // (-1 = env).
+// Curve interpolators and SurfaceNormal as Geometry::GetHitLocalGeometry
+// (framework/render/geometry.h:101-172) picks them per curve type.  Per case:
+// ctrl 16 floats (4 control points xyzw), u, ps xyz; out 15 floats: Position4,
+// Velocity4, Acceleration3, SurfaceNormal (of a copy of ps), 0.
+int ref_curve(uint32_t type, const float *ctrl, const float *u, const float *ps, float *out, uint32_t n) {
+    for (uint32_t i = 0; i < n; i++) {
+        float4 q[4];
+        for (int j = 0; j < 4; j++)
+            q[j] = make_float4(ctrl[16 * i + 4 * j], ctrl[16 * i + 4 * j + 1], ctrl[16 * i + 4 * j + 2], ctrl[16 * i + 4 * j + 3]);
+        float3 p = make_float3(ps[3 * i], ps[3 * i + 1], ps[3 * i + 2]);
+        float4 p4, d4;
+        float3 a3, nrm;
+        const float t = u[i];
+        if (type == 0) {
+            LinearInterpolator c;
+            c.Initialize(q);
+            p4 = c.Position4(t); d4 = c.Velocity4(t); a3 = c.Acceleration3(t);
+            nrm = SurfaceNormal(c, t, p);
+        } else if (type == 1) {
+            QuadraticInterpolator c;
+            c.InitializeFromBSpline(q);
+            p4 = c.Position4(t); d4 = c.Velocity4(t); a3 = c.Acceleration3(t);
+            nrm = SurfaceNormal(c, t, p);
+        } else {
+            CubicInterpolator c;
+            if (type == 2) c.InitializeFromBSpline(q);
+            else c.InitializeFromCatrom(q);
+            p4 = c.Position4(t); d4 = c.Velocity4(t); a3 = c.Acceleration3(t);
+            nrm = SurfaceNormal(c, t, p);
+        }
+        float *o = out + 15 * (size_t)i;
+        o[0] = p4.x; o[1] = p4.y; o[2] = p4.z; o[3] = p4.w;
+        o[4] = d4.x; o[5] = d4.y; o[6] = d4.z; o[7] = d4.w;
+        o[8] = a3.x; o[9] = a3.y; o[10] = a3.z;
+        o[11] = nrm.x; o[12] = nrm.y; o[13] = nrm.z; o[14] = 0.f;
+    }
+    return 0;
+}
+
 int ref_select_emitter(const float *probs, uint32_t num, int has_env, const float *p, int32_t *out, uint32_t n) {
     static thread_local Emitter *areas = nullptr;
     delete[] areas;

@@ -21,7 +21,8 @@ MAT_DIFFUSE, MAT_DIELECTRIC, MAT_ROUGH_DIELECTRIC, MAT_CONDUCTOR, MAT_ROUGH_COND
 MATERIAL_NAMES = {1: "diffuse", 2: "dielectric", 3: "roughdielectric", 4: "conductor", 5: "roughconductor",
                   6: "plastic", 7: "roughplastic"}
 TEX_RGB, TEX_BITMAP, TEX_CHECKERBOARD = 0, 1, 2
-SHAPE_MESH, SHAPE_SPHERE = 0, 1
+SHAPE_MESH, SHAPE_SPHERE, SHAPE_CURVES = 0, 1, 2
+CURVE_LINEAR, CURVE_QUADRATIC_BSPLINE, CURVE_CUBIC_BSPLINE, CURVE_CATMULL_ROM = 0, 1, 2, 3
 INST_FLIP_NORMALS, INST_FLIP_TEXCOORDS = 1, 2
 ENV_NONE, ENV_CONST, ENV_MAP = 0, 1, 2
 TEX_ADDRESS_WRAP, TEX_ADDRESS_CLAMP, TEX_ADDRESS_MIRROR = 0, 1, 2
@@ -68,13 +69,19 @@ class EnvDesc(C.Structure):
                 ("height", C.c_uint32), ("scale", C.c_float), ("to_world", C.c_float * 16)]
 
 
+class CurvesDesc(C.Structure):
+    _fields_ = [("positions", c_float_p), ("radii", c_float_p), ("segments", c_uint_p),
+                ("num_points", C.c_uint32), ("num_segments", C.c_uint32), ("type", C.c_uint32)]
+
+
 class SceneDesc(C.Structure):
     _fields_ = [("meshes", C.POINTER(MeshDesc)), ("num_meshes", C.c_uint32),
                 ("spheres", C.POINTER(SphereDesc)), ("num_spheres", C.c_uint32),
                 ("materials", C.POINTER(MaterialDesc)), ("num_materials", C.c_uint32),
                 ("instances", C.POINTER(InstanceDesc)), ("num_instances", C.c_uint32),
                 ("env", EnvDesc), ("camera", CameraDesc),
-                ("width", C.c_uint32), ("height", C.c_uint32), ("max_depth", C.c_uint32)]
+                ("width", C.c_uint32), ("height", C.c_uint32), ("max_depth", C.c_uint32),
+                ("curves", C.POINTER(CurvesDesc)), ("num_curves", C.c_uint32)]
 
 
 class DeviceOpts(C.Structure):
@@ -144,6 +151,7 @@ PROTOTYPES = [
     ("pt_scene_update_vertices", C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32]),
     ("pt_scene_update_all_vertices", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     ("pt_scene_num_prims", C.c_int, [C.c_void_p, c_uint_p, c_uint_p]),
+    ("pt_scene_num_curves", C.c_int, [C.c_void_p, c_uint_p, c_uint_p]),
     ("pt_bvh_build", C.c_int, [C.c_void_p, C.POINTER(BvhOpts), C.c_void_p]),
     ("pt_bvh_refit", C.c_int, [C.c_void_p, C.c_void_p]),
     ("pt_bvh_get_stats", C.c_int, [C.c_void_p, C.POINTER(BvhStats)]),

@@ -105,6 +105,12 @@ class GpuScene:
         abi.check(self.lib.pt_scene_num_prims(self.handle, C.byref(a), C.byref(b)), "pt_scene_num_prims", self.lib)
         return a.value, b.value
 
+    def num_curves(self) -> tuple[int, int]:
+        """(curve segments, round-cone pieces) of the scene's curve instances."""
+        a, b = C.c_uint32(), C.c_uint32()
+        abi.check(self.lib.pt_scene_num_curves(self.handle, C.byref(a), C.byref(b)), "pt_scene_num_curves", self.lib)
+        return a.value, b.value
+
     def set_camera(self, cam: abi.CameraDesc) -> None:
         abi.check(self.lib.pt_scene_set_camera(self.handle, C.byref(cam)), "pt_scene_set_camera", self.lib)
 

@@ -49,10 +49,15 @@ __device__ __forceinline__ void prim_box(const float4 *prims, uint32_t p, float3
         float4 c = prims[3 * (size_t)p + 2];
         lo = f3(fminf(a.x, fminf(b.x, c.x)), fminf(a.y, fminf(b.y, c.y)), fminf(a.z, fminf(b.z, c.z)));
         hi = f3(fmaxf(a.x, fmaxf(b.x, c.x)), fmaxf(a.y, fmaxf(b.y, c.y)), fmaxf(a.z, fmaxf(b.z, c.z)));
-    } else {
+    } else if (__float_as_int(b.w) == 0) {  // sphere
         float r = b.x;
         lo = f3(a.x - r, a.y - r, a.z - r);
         hi = f3(a.x + r, a.y + r, a.z + r);
+    } else {  // round-cone curve piece: the boxes of its two end spheres
+        float4 c = prims[3 * (size_t)p + 2];
+        float r0 = b.x, r1 = b.y;
+        lo = f3(fminf(a.x - r0, c.x - r1), fminf(a.y - r0, c.y - r1), fminf(a.z - r0, c.z - r1));
+        hi = f3(fmaxf(a.x + r0, c.x + r1), fmaxf(a.y + r0, c.y + r1), fmaxf(a.z + r0, c.z + r1));
     }
 }
 

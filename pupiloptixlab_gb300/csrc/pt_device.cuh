@@ -171,14 +171,15 @@ struct DevEmitter {
 // Per-instance data used when shading a hit.
 struct DevInstance {
     uint32_t material;
-    uint32_t flags;         // PT_INST_* | kInstHasNormals | kInstHasUvs | kInstSphere
+    uint32_t flags;         // PT_INST_* | kInstHasNormals | kInstHasUvs | kInstSphere | kInstCurve | curve type << kInstCurveTypeShift
     uint32_t prim_offset;   // first primitive id
     int32_t emitter_offset; // first area emitter, or -1
     float4 sphere;          // world centre, radius
     float4 inv0, inv1, inv2;    // world -> object (sphere texcoords)
     float4 obj_center;      // object-space sphere centre
 };
-enum : uint32_t { kInstHasNormals = 1u << 8, kInstHasUvs = 1u << 9, kInstSphere = 1u << 10 };
+enum : uint32_t { kInstHasNormals = 1u << 8, kInstHasUvs = 1u << 9, kInstSphere = 1u << 10, kInstCurve = 1u << 11 };
+constexpr uint32_t kInstCurveTypeShift = 12;  // 2 bits: PT_CURVE_*
 
 // Everything a kernel needs, passed by value.
 struct DevScene {
@@ -196,6 +197,9 @@ struct DevScene {
     const float4 *vnrm;         // world normals (not normalised)
     const float2 *vuv;
     const uint32_t *prim_inst;  // primitive -> instance
+    const uint32_t *curve_seg;  // curve piece (primitive id - curve_prim0) -> segment
+    const float4 *curve_cp;     // 4 world control points (xyz, radius) per segment
+    uint32_t curve_prim0;       // first curve piece primitive id (after triangles and spheres)
     const DevInstance *inst;
     const DevMaterial *mats;
     const DevEmitter *emitters; // area emitters

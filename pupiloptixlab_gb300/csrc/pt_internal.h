@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "../../include/pt_api.h"
+#include "pt_curve.h"
 #include "pt_device.cuh"
 
 // Thread-local last error (pt_last_error).
@@ -83,6 +84,7 @@ struct pt_scene {
     int max_smem_per_block = 0;
     pt_scene_desc desc_shallow{};  // sizes only (pointers are not kept)
     uint32_t num_tris = 0, num_spheres = 0, num_prims = 0;
+    uint32_t num_curve_segments = 0, num_curve_pieces = 0;  // pieces follow the spheres in primitive order
     uint32_t num_vertices = 0;
     std::vector<MeshInstanceRef> mesh_instances;
     std::vector<uint32_t> mesh_num_vertices;
@@ -96,6 +98,7 @@ struct pt_scene {
     DevBuf prims_bvh;    // 3 float4 per prim (leaf order)
     DevBuf nodes;
     DevBuf tri_vidx, vpos, vnrm, vuv, prim_inst, inst, mats, emitters, emitter_cdf;
+    DevBuf curve_seg, curve_cp;  // piece -> segment; 4 world control points per segment
     DevBuf mesh_obj_pos;  // scratch for pt_scene_update_vertices
     // BVH build scratch and results
     DevBuf bvh_scratch;

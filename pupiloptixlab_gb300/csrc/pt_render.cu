@@ -289,7 +289,7 @@ PT_DI int2 *stage_smem(const DevScene &s, float4 *smem) {
 
 // ANY = false: closest hit of the extension rays; ANY = true: shadow rays.
 // Widths 2 and 4 are capped at 72 registers (7 blocks of 128 threads per SM).
-template <int K, bool ANY, bool COUNT, bool BATCH = false>
+template <int K, bool ANY, bool COUNT, bool BATCH = false, bool CURVES = false>
 __global__ void __maxnreg__(K == 8 ? 128 : 72) k_trace_queue(DevScene s, State st, Batch bt, uint32_t npix) {
     extern __shared__ float4 smem[];
     int2 *sstack = stage_smem<K>(s, smem);
@@ -299,11 +299,11 @@ __global__ void __maxnreg__(K == 8 ? 128 : 72) k_trace_queue(DevScene s, State s
             src.st = st;
             src.bt = bt;
             src.npix = npix;
-            trace_persistent<K, true, COUNT>(s, smem, sstack, src, st.counters + kWorkShadow, st.counters + kOverflow,
+            trace_persistent<K, true, COUNT, decltype(src), CURVES>(s, smem, sstack, src, st.counters + kWorkShadow, st.counters + kOverflow,
                                              st.stats + kStatShNodes, st.stats + kStatShPrims, st.stats + kStatShRays);
         } else {
             ShadowSrc src{st};
-            trace_persistent<K, true, COUNT>(s, smem, sstack, src, st.counters + kWorkShadow, st.counters + kOverflow,
+            trace_persistent<K, true, COUNT, decltype(src), CURVES>(s, smem, sstack, src, st.counters + kWorkShadow, st.counters + kOverflow,
                                              st.stats + kStatShNodes, st.stats + kStatShPrims, st.stats + kStatShRays);
         }
     } else {
@@ -312,11 +312,11 @@ __global__ void __maxnreg__(K == 8 ? 128 : 72) k_trace_queue(DevScene s, State s
             src.st = st;
             src.bt = bt;
             src.npix = npix;
-            trace_persistent<K, false, COUNT>(s, smem, sstack, src, st.counters + kWorkExtend, st.counters + kOverflow,
+            trace_persistent<K, false, COUNT, decltype(src), CURVES>(s, smem, sstack, src, st.counters + kWorkExtend, st.counters + kOverflow,
                                               st.stats + kStatExtNodes, st.stats + kStatExtPrims, st.stats + kStatExtRays);
         } else {
             ExtendSrc src{st};
-            trace_persistent<K, false, COUNT>(s, smem, sstack, src, st.counters + kWorkExtend, st.counters + kOverflow,
+            trace_persistent<K, false, COUNT, decltype(src), CURVES>(s, smem, sstack, src, st.counters + kWorkExtend, st.counters + kOverflow,
                                               st.stats + kStatExtNodes, st.stats + kStatExtPrims, st.stats + kStatExtRays);
         }
     }
@@ -327,11 +327,18 @@ struct HitGeo {
     float2 uv;
 };
 
-// Geometry::GetHitLocalGeometry (framework/render/geometry.h:60-100,176-180)
-// on world-space data.
+// Geometry::GetHitLocalGeometry (framework/render/geometry.h:60-180) on
+// world-space data; for a curve hit h.z is the curve parameter.
 PT_DI void hit_geometry(const DevScene &s, float4 h, float3 o, float3 d, const DevInstance &in, bool twosided, HitGeo &g) {
     int prim = __float_as_int(h.y);
-    if (!(in.flags & kInstSphere)) {
+    if (in.flags & kInstCurve) {  // geometry.h:101-172, in world space
+        g.pos = o + h.x * d;
+        const float4 *cp = s.curve_cp + 4 * (size_t)s.curve_seg[prim - (int)s.curve_prim0];
+        const float4 q[4] = {cp[0], cp[1], cp[2], cp[3]};
+        const CurveSeg seg = curve_segment((in.flags >> kInstCurveTypeShift) & 3u, q);
+        g.nrm = curve_normal(seg, h.z, g.pos);
+        g.uv = make_float2(0.f, 0.f);
+    } else if (!(in.flags & kInstSphere)) {
         uint32_t i0 = s.tri_vidx[3 * prim], i1 = s.tri_vidx[3 * prim + 1], i2 = s.tri_vidx[3 * prim + 2];
         float3 p0 = xyz(s.vpos[i0]), p1 = xyz(s.vpos[i1]), p2 = xyz(s.vpos[i2]);
         float u = h.z, v = h.w;
@@ -685,12 +692,12 @@ __global__ void k_accumulate(State st, Wave w, Outputs out0, Batch bt) {
 }
 
 // pt_trace_rays: rays (ox,oy,oz,tmin, dx,dy,dz,tmax) -> hits.
-template <int K, bool ANY>
+template <int K, bool ANY, bool CURVES>
 __global__ void k_trace_rays(DevScene s, const float4 *rays, float4 *hits, uint32_t n, uint32_t *work, uint32_t *ovf_flag) {
     extern __shared__ float4 smem[];
     int2 *sstack = stage_smem<K>(s, smem);
     UserSrc<ANY> src{rays, hits, n};
-    trace_persistent<K, ANY, false>(s, smem, sstack, src, work, ovf_flag, nullptr, nullptr, nullptr);
+    trace_persistent<K, ANY, false, UserSrc<ANY>, CURVES>(s, smem, sstack, src, work, ovf_flag, nullptr, nullptr, nullptr);
 }
 
 __global__ void k_bsdf_eval(const float *bsdf, const float *wo, const float *wi, float *f, float *pdf, uint32_t n) {
@@ -773,6 +780,7 @@ struct RunTarget {
     int num_sms;
     uint32_t tuned_block, tuned_wave_paths;
     pt_render_stats *rs;
+    bool curves;  // some scene has curve pieces: use the traversal with the curve test
 };
 
 static Outputs make_outputs(const pt_frame_buffers *fb, uint32_t flags) {
@@ -789,7 +797,8 @@ static Outputs make_outputs(const pt_frame_buffers *fb, uint32_t flags) {
 template <int K>
 struct Launcher {
     static int run(pt_scene *s, const pt_render_params *p, const pt_frame_buffers *fb, cudaStream_t st) {
-        RunTarget t{&s->ws, s->ev0, s->ev1, s->num_sms, s->tuned_block, s->tuned_wave_paths, &s->render_stats};
+        RunTarget t{&s->ws, s->ev0, s->ev1, s->num_sms, s->tuned_block, s->tuned_wave_paths, &s->render_stats,
+                    s->num_curve_pieces > 0};
         const uint32_t max_depth = p->max_depth ? p->max_depth : s->desc_shallow.max_depth;
         const uint32_t npix = s->dev.width_px * s->dev.height_px;
         return run_waves<false>(t, s->dev, Batch{}, npix, max_depth, max_depth, p, make_outputs(fb, p->flags), st);
@@ -839,8 +848,10 @@ struct Launcher {
 
         const int tb = p->block_size ? (int)p->block_size : (t.tuned_block ? (int)t.tuned_block : 128);
         const size_t smem = (size_t)d.smem_nodes * 32 * K + (size_t)kShortStack * 8 * tb;
-        auto k_ext = count ? k_trace_queue<K, false, true, BATCH> : k_trace_queue<K, false, false, BATCH>;
-        auto k_sh = count ? k_trace_queue<K, true, true, BATCH> : k_trace_queue<K, true, false, BATCH>;
+        auto k_ext = t.curves ? (count ? k_trace_queue<K, false, true, BATCH, true> : k_trace_queue<K, false, false, BATCH, true>)
+                              : (count ? k_trace_queue<K, false, true, BATCH> : k_trace_queue<K, false, false, BATCH>);
+        auto k_sh = t.curves ? (count ? k_trace_queue<K, true, true, BATCH, true> : k_trace_queue<K, true, false, BATCH, true>)
+                             : (count ? k_trace_queue<K, true, true, BATCH> : k_trace_queue<K, true, false, BATCH>);
         if ((e = set_smem(k_ext, smem)) != PT_OK || (e = set_smem(k_sh, smem)) != PT_OK) return e;
         int occ_t = 0, occ_s = 0;
         PT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_t, k_ext, tb, smem));
@@ -1012,7 +1023,9 @@ struct Launcher {
         if (e != PT_OK) return e;
         const int tb = 128;
         const size_t smem = (size_t)d.smem_nodes * 32 * K + (size_t)kShortStack * 8 * tb;
-        auto kern = anyhit ? k_trace_rays<K, true> : k_trace_rays<K, false>;
+        const bool curves = s->num_curve_pieces > 0;
+        auto kern = curves ? (anyhit ? k_trace_rays<K, true, true> : k_trace_rays<K, false, true>)
+                           : (anyhit ? k_trace_rays<K, true, false> : k_trace_rays<K, false, false>);
         if ((e = set_smem(kern, smem)) != PT_OK) return e;
         int occ = 0;
         PT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, tb, smem));
@@ -1162,7 +1175,9 @@ int render_batch(pt_context *ctx, pt_scene *const *scenes, const pt_render_param
     uint32_t bounces = max_depth;
     if (!bounces)
         for (uint32_t k = 0; k < n; k++) bounces = std::max(bounces, scenes[k]->dev.max_depth);
-    RunTarget t{&b.ws, b.ev0, b.ev1, ctx->num_sms, 0, 0, &b.stats};
+    bool curves = false;
+    for (uint32_t k = 0; k < n; k++) curves = curves || scenes[k]->num_curve_pieces > 0;
+    RunTarget t{&b.ws, b.ev0, b.ev1, ctx->num_sms, 0, 0, &b.stats, curves};
     Outputs none{};
     return Launcher<K>::template run_waves<true>(t, dt, bt, static_cast<uint32_t>(total_pix), max_depth, bounces, p,
                                                  none, st);
@@ -1375,8 +1390,9 @@ int render_noalloc(pt_scene *s, const pt_render_params *p, const pt_frame_buffer
 
     const int tb = p->block_size ? (int)p->block_size : 128;
     const size_t smem = (size_t)d.smem_nodes * 32 * K + (size_t)kShortStack * 8 * tb;
-    auto k_ext = k_trace_queue<K, false, false>;
-    auto k_sh = k_trace_queue<K, true, false>;
+    const bool curves = s->num_curve_pieces > 0;
+    auto k_ext = curves ? k_trace_queue<K, false, false, false, true> : k_trace_queue<K, false, false>;
+    auto k_sh = curves ? k_trace_queue<K, true, false, false, true> : k_trace_queue<K, true, false>;
     int e;
     if ((e = set_smem(k_ext, smem)) != PT_OK || (e = set_smem(k_sh, smem)) != PT_OK) return e;
     int occ_t = 0, occ_s = 0;

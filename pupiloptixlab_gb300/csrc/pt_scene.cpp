@@ -163,7 +163,7 @@ int upload(DevBuf &b, const std::vector<T> &v) {
 int validate(const pt_scene_desc *d) {
     if (!d) { pt_set_error("scene descriptor is NULL"); return PT_ERR_INVALID; }
     if ((d->num_meshes && !d->meshes) || (d->num_spheres && !d->spheres) || (d->num_materials && !d->materials) ||
-        (d->num_instances && !d->instances)) {
+        (d->num_instances && !d->instances) || (d->num_curves && !d->curves)) {
         pt_set_error("scene descriptor has a non-zero count with a NULL array");
         return PT_ERR_INVALID;
     }
@@ -204,6 +204,28 @@ int validate(const pt_scene_desc *d) {
                 return PT_ERR_INVALID;
             }
     }
+    for (uint32_t i = 0; i < d->num_curves; i++) {
+        const pt_curves_desc &c = d->curves[i];
+        if (c.type > PT_CURVE_CATMULL_ROM) { pt_set_error("curves %u: unknown curve type %u", i, c.type); return PT_ERR_INVALID; }
+        if ((c.num_points && (!c.positions || !c.radii)) || (c.num_segments && !c.segments)) {
+            pt_set_error("curves %u has NULL positions, radii or segments", i);
+            return PT_ERR_INVALID;
+        }
+        const uint32_t deg = ptd::curve_degree(c.type);
+        for (uint32_t k = 0; k < c.num_segments; k++)
+            if ((uint64_t)c.segments[k] + deg >= c.num_points) {
+                pt_set_error("curves %u segment %u: control points %u..%u out of range (%u points)", i, k, c.segments[k],
+                             c.segments[k] + deg, c.num_points);
+                return PT_ERR_OOB;
+            }
+        for (uint64_t v = 0; v < 3ull * c.num_points; v++)
+            if (!std::isfinite(c.positions[v])) { pt_set_error("curves %u has a non-finite position", i); return PT_ERR_INVALID; }
+        for (uint32_t v = 0; v < c.num_points; v++)
+            if (!(c.radii[v] >= 0.f) || !std::isfinite(c.radii[v])) {
+                pt_set_error("curves %u point %u: radius must be finite and >= 0", i, v);
+                return PT_ERR_INVALID;
+            }
+    }
     for (uint32_t i = 0; i < d->num_instances; i++) {
         const pt_instance_desc &in = d->instances[i];
         if (in.material >= d->num_materials) { pt_set_error("instance %u: material out of range", i); return PT_ERR_OOB; }
@@ -212,6 +234,9 @@ int validate(const pt_scene_desc *d) {
         } else if (in.shape_type == PT_SHAPE_SPHERE) {
             if (in.shape_index >= d->num_spheres) { pt_set_error("instance %u: sphere out of range", i); return PT_ERR_OOB; }
             if (!(d->spheres[in.shape_index].radius > 0.f)) { pt_set_error("instance %u: sphere radius must be > 0", i); return PT_ERR_INVALID; }
+        } else if (in.shape_type == PT_SHAPE_CURVES) {
+            if (in.shape_index >= d->num_curves) { pt_set_error("instance %u: curves out of range", i); return PT_ERR_OOB; }
+            if (in.is_emitter) { pt_set_error("instance %u: curves cannot be emitters", i); return PT_ERR_UNSUPPORTED; }
         } else {
             pt_set_error("instance %u: unknown shape type %u", i, in.shape_type);
             return PT_ERR_INVALID;
@@ -302,6 +327,7 @@ int build_scene(pt_scene *s, const pt_scene_desc *d) {
     s->desc_shallow.spheres = nullptr;
     s->desc_shallow.materials = nullptr;
     s->desc_shallow.instances = nullptr;
+    s->desc_shallow.curves = nullptr;
 
     std::vector<float4> vpos, vnrm, prims;
     std::vector<float2> vuv;
@@ -395,9 +421,68 @@ int build_scene(pt_scene *s, const pt_scene_desc *d) {
         mag = std::max({mag, fabsf(cw.x) + r, fabsf(cw.y) + r, fabsf(cw.z) + r});
         nsph++;
     }
+    // round-cone pieces of the curve segments after the spheres
+    uint32_t nseg = 0, npiece = 0;
+    std::vector<uint32_t> curve_seg;
+    std::vector<float4> curve_cp;
+    for (uint32_t ii = 0; ii < d->num_instances; ii++) {
+        const pt_instance_desc &id = d->instances[ii];
+        if (id.shape_type != PT_SHAPE_CURVES) continue;
+        DevInstance &in = insts[ii];
+        const pt_curves_desc &cv = d->curves[id.shape_index];
+        in.flags |= ptd::kInstCurve | (cv.type << ptd::kInstCurveTypeShift);
+        in.prim_offset = ntri + nsph + npiece;
+        const float *m = id.to_world;
+        const float scale = hlen(h3(m[0], m[4], m[8]));  // length of the transformed x axis
+        const uint32_t deg = ptd::curve_degree(cv.type);
+        for (uint32_t i = 0; i < cv.num_segments; i++, nseg++) {
+            const uint32_t first = cv.segments[i];
+            float4 q[4] = {};
+            float rmax = 0.f;
+            for (uint32_t j = 0; j <= deg; j++) {
+                const uint32_t v = first + j;
+                H3 p = xform_point(m, h3(cv.positions[3 * v], cv.positions[3 * v + 1], cv.positions[3 * v + 2]));
+                q[j] = make_float4(p.x, p.y, p.z, cv.radii[v] * scale);
+                rmax = std::max(rmax, q[j].w);
+            }
+            for (int j = 0; j < 4; j++) curve_cp.push_back(q[j]);
+            if (!(rmax > 0.f)) continue;  // an invisible segment gets no pieces
+            const bool strand_first = i == 0 || cv.segments[i - 1] + 1 != first;
+            const bool strand_last = i + 1 == cv.num_segments || cv.segments[i + 1] != first + 1;
+            const ptd::CurveSeg sg = ptd::curve_segment(cv.type, q);
+            const uint32_t np = ptd::curve_piece_count(sg, rmax);
+            for (uint32_t k = 0; k < np; k++) {
+                const float u0 = (float)k / (float)np, u1 = (float)(k + 1) / (float)np;
+                const float4 p0 = ptd::curve_pos(sg, u0), p1 = ptd::curve_pos(sg, u1);
+                int kind = ptd::kPieceCurve;
+                if (cv.type == PT_CURVE_LINEAR) {  // round caps at every vertex, one sphere per vertex
+                    kind |= ptd::kPieceSphere0;
+                    if (strand_last) kind |= ptd::kPieceSphere1;
+                } else {  // smooth joints; open ends at the strand's ends
+                    if (k > 0 || !strand_first) kind |= ptd::kPieceSphere0;
+                    kind |= ptd::kPieceClampU;
+                }
+                const float r0 = std::max(p0.w, 0.f), r1 = std::max(p1.w, 0.f);
+                const uint32_t bits = (ntri + nsph + npiece) | 0x80000000u;
+                float idf, kindf;
+                memcpy(&idf, &bits, 4);
+                memcpy(&kindf, &kind, 4);
+                prims.push_back(make_float4(p0.x, p0.y, p0.z, idf));
+                prims.push_back(make_float4(r0, r1, u0, kindf));
+                prims.push_back(make_float4(p1.x, p1.y, p1.z, u1));
+                prim_inst.push_back(ii);
+                curve_seg.push_back(nseg);
+                mag = std::max({mag, fabsf(p0.x) + r0, fabsf(p0.y) + r0, fabsf(p0.z) + r0, fabsf(p1.x) + r1,
+                                fabsf(p1.y) + r1, fabsf(p1.z) + r1});
+                npiece++;
+            }
+        }
+    }
     s->num_tris = ntri;
     s->num_spheres = nsph;
-    s->num_prims = ntri + nsph;
+    s->num_curve_segments = nseg;
+    s->num_curve_pieces = npiece;
+    s->num_prims = ntri + nsph + npiece;
     s->num_vertices = (uint32_t)vpos.size();
     s->scene_mag = std::max(mag, 1e-6f);
 
@@ -476,6 +561,8 @@ int build_scene(pt_scene *s, const pt_scene_desc *d) {
     if ((e = upload(s->vnrm, vnrm)) != PT_OK) return e;
     if ((e = upload(s->vuv, vuv)) != PT_OK) return e;
     if ((e = upload(s->prim_inst, prim_inst)) != PT_OK) return e;
+    if ((e = upload(s->curve_seg, curve_seg)) != PT_OK) return e;
+    if ((e = upload(s->curve_cp, curve_cp)) != PT_OK) return e;
     if ((e = upload(s->inst, insts)) != PT_OK) return e;
     if ((e = upload(s->mats, mats)) != PT_OK) return e;
     s->h_prims_world = std::move(prims);
@@ -486,6 +573,9 @@ int build_scene(pt_scene *s, const pt_scene_desc *d) {
     dv.vnrm = s->vnrm.as<float4>();
     dv.vuv = s->vuv.as<float2>();
     dv.prim_inst = s->prim_inst.as<uint32_t>();
+    dv.curve_seg = s->curve_seg.as<uint32_t>();
+    dv.curve_cp = s->curve_cp.as<float4>();
+    dv.curve_prim0 = ntri + nsph;
     dv.inst = s->inst.as<DevInstance>();
     dv.mats = s->mats.as<DevMaterial>();
     dv.num_tris = ntri;
@@ -630,7 +720,7 @@ void DevBuf::release() {
 }
 
 pt_scene::~pt_scene() {
-    DevBuf *all[] = {&prims_world, &prims_bvh, &nodes, &tri_vidx, &vpos, &vnrm, &vuv, &prim_inst, &inst, &mats,
+    DevBuf *all[] = {&prims_world, &prims_bvh, &nodes, &tri_vidx, &vpos, &vnrm, &vuv, &prim_inst, &inst, &mats, &curve_seg, &curve_cp,
                      &emitters, &emitter_cdf, &mesh_obj_pos, &bvh_scratch, &bvh_order, &sah_scratch, &xform_table, &all_obj_pos, &ws.ray_o, &ws.ray_d, &ws.hit, &ws.thr,
                      &ws.rad, &ws.rng, &ws.meta, &ws.q0, &ws.q1, &ws.sh_o, &ws.sh_d, &ws.sh_c, &ws.mat_key,
                      &ws.counters, &ws.sort_tmp};
@@ -725,6 +815,13 @@ int pt_scene_num_prims(const pt_scene *scene, uint32_t *nt, uint32_t *ns) {
     if (!scene) { pt_set_error("scene is NULL"); return PT_ERR_INVALID; }
     if (nt) *nt = scene->num_tris;
     if (ns) *ns = scene->num_spheres;
+    return PT_OK;
+}
+
+int pt_scene_num_curves(const pt_scene *scene, uint32_t *num_segments, uint32_t *num_pieces) {
+    if (!scene) { pt_set_error("scene is NULL"); return PT_ERR_INVALID; }
+    if (num_segments) *num_segments = scene->num_curve_segments;
+    if (num_pieces) *num_pieces = scene->num_curve_pieces;
     return PT_OK;
 }
 

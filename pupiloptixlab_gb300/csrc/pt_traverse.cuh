@@ -17,11 +17,15 @@
 //           [child, child + count); count == 0 and child >= 0: inner node;
 //           child < 0: empty slot.  Loaded as 2*K float4 (128-bit) loads.
 //   prim  = 3 float4 per slot: triangle (v0, id) (v1, 0) (v2, 0);
-//           sphere (centre, id | 1<<31) (radius, 0, 0, 0) (0).
+//           sphere (centre, id | 1<<31) (radius, 0, 0, 0) (0);
+//           curve piece (c0, id | 1<<31) (r0, r1, u0, kind bits) (c1, u1):
+//           a round cone from centre c0 / radius r0 to c1 / r1 covering the
+//           curve parameters [u0, u1] of its segment (pt_curve.h).
 // Nodes are in breadth-first order, so the first smem_nodes nodes are the
 // top levels; those are staged in shared memory once per (persistent) block.
 #pragma once
 
+#include "pt_curve.h"
 #include "pt_device.cuh"
 
 namespace ptd {
@@ -118,6 +122,91 @@ PT_DI bool intersect_sphere(float3 o, float3 d, float3 c, float r, float tmin, f
     return false;
 }
 
+// ---------------------------------------------------------------- curve pieces
+PT_DI float dot_rn(float3 a, float3 b) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)), __fmul_rn(a.z, b.z));
+}
+PT_DI float3 sub_rn(float3 a, float3 b) { return f3(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z)); }
+PT_DI float3 madd_rn(float3 a, float s, float3 b) {  // a + s*b, rounded per step
+    return f3(__fadd_rn(a.x, __fmul_rn(s, b.x)), __fadd_rn(a.y, __fmul_rn(s, b.y)), __fadd_rn(a.z, __fmul_rn(s, b.z)));
+}
+
+// Entry into a sphere, the ray origin first moved to the point of closest
+// approach (Haines et al., "Precision Improvements for Ray/Sphere
+// Intersection", Ray Tracing Gems 2019), which keeps hair-thin spheres exact
+// for distant origins.  Only the entering root counts.
+PT_DI bool curve_sphere_entry(float3 o, float3 d, float dd, float3 c, float r, float tmin, float tmax, float &t_out) {
+    const float3 f = sub_rn(o, c);
+    const float tc = __fdiv_rn(-dot_rn(f, d), dd);
+    const float3 l = madd_rn(f, tc, d);
+    const float h = __fsub_rn(__fmul_rn(r, r), dot_rn(l, l));
+    if (!(h >= 0.f)) return false;
+    const float t = __fsub_rn(tc, __fsqrt_rn(__fdiv_rn(h, dd)));
+    if (!(t > tmin && t < tmax)) return false;
+    t_out = t;
+    return true;
+}
+
+// Round-cone piece: the lateral surface of the cone frustum between the
+// planes through c0 and c1 normal to the axis (radius linear along the
+// axis), plus spheres at the ends that the kind bits ask for.  The frustum
+// quadratic is formed from the components normal to the axis, origin moved to
+// the closest approach to c0; its entering root is (-B - sqrt(B^2 - AC)) / A
+// whatever the sign of A.  Returns the smallest entering t in (tmin, tmax)
+// and the curve parameter there (projection onto the axis, mapped to [u0, u1]).
+PT_DI bool intersect_curve_piece(float3 o, float3 d, float4 a, float4 b, float4 c, float tmin, float tmax, float &t_out,
+                                 float &u_out) {
+    const int kind = __float_as_int(b.w);
+    const float3 c0 = xyz(a), c1 = xyz(c);
+    const float r0 = b.x, r1 = b.y, u0 = b.z, u1 = c.w;
+    const float dd = dot_rn(d, d);
+    bool hit = false;
+    float best = tmax, bu = 0.f, t;
+    if ((kind & kPieceSphere0) && curve_sphere_entry(o, d, dd, c0, r0, tmin, best, t)) {
+        hit = true;
+        best = t;
+        bu = u0;
+    }
+    if ((kind & kPieceSphere1) && curve_sphere_entry(o, d, dd, c1, r1, tmin, best, t)) {
+        hit = true;
+        best = t;
+        bu = u1;
+    }
+    const float3 e = sub_rn(c1, c0);
+    const float len = __fsqrt_rn(dot_rn(e, e));
+    if (len > 0.f) {
+        const float inv_len = __frcp_rn(len);
+        const float3 ax = f3(__fmul_rn(e.x, inv_len), __fmul_rn(e.y, inv_len), __fmul_rn(e.z, inv_len));
+        const float k = __fmul_rn(__fsub_rn(r1, r0), inv_len);  // dr / dz
+        const float3 f = sub_rn(o, c0);
+        const float tc = __fdiv_rn(-dot_rn(f, d), dd);
+        const float3 w = madd_rn(f, tc, d);
+        const float we = dot_rn(w, ax), de = dot_rn(d, ax);
+        const float3 wp = madd_rn(w, -we, ax), dp = madd_rn(d, -de, ax);
+        const float rz = __fadd_rn(r0, __fmul_rn(k, we));
+        const float kde = __fmul_rn(k, de);
+        const float A = __fsub_rn(dot_rn(dp, dp), __fmul_rn(kde, kde));
+        const float B = __fsub_rn(dot_rn(wp, dp), __fmul_rn(kde, rz));
+        const float C = __fsub_rn(dot_rn(wp, wp), __fmul_rn(rz, rz));
+        const float disc = __fsub_rn(__fmul_rn(B, B), __fmul_rn(A, C));
+        if (disc >= 0.f && A != 0.f) {
+            const float tp = __fdiv_rn(__fsub_rn(-B, __fsqrt_rn(disc)), A);
+            const float z = __fadd_rn(we, __fmul_rn(tp, de));
+            const float tt = __fadd_rn(tc, tp);
+            if (z >= 0.f && z <= len && tt > tmin && tt < best) {
+                hit = true;
+                best = tt;
+                bu = __fadd_rn(u0, __fmul_rn(__fmul_rn(z, inv_len), __fsub_rn(u1, u0)));
+            }
+        }
+    }
+    if (!hit) return false;
+    if (kind & kPieceClampU) bu = fminf(fmaxf(bu, kCurveUMin), kCurveUMax);
+    t_out = best;
+    u_out = bu;
+    return true;
+}
+
 PT_DI float3 safe_inv(float3 d) {
     return f3(d.x != 0.f ? __frcp_rn(d.x) : copysignf(1e30f, d.x), d.y != 0.f ? __frcp_rn(d.y) : copysignf(1e30f, d.y),
               d.z != 0.f ? __frcp_rn(d.z) : copysignf(1e30f, d.z));
@@ -209,7 +298,10 @@ constexpr int kRefillBusyMax = 20;
 //
 // Src provides: count(), load(i, o, d, tmin, tmax, tag), root(tag) (the node
 // the ray starts at), store(i, tag, result).
-template <int K, bool ANY, bool COUNT, class Src>
+// CURVES = false compiles the leaf test without the curve-piece branch (a
+// record with non-zero kind bits is then treated as a sphere), so that scenes
+// without curves run the smaller kernel.
+template <int K, bool ANY, bool COUNT, class Src, bool CURVES = false>
 PT_DI void trace_persistent(const DevScene &s, const float4 *snodes, int2 *sstack_base, Src &src, uint32_t *work,
                             uint32_t *ovf_flag, unsigned long long *stat_nodes, unsigned long long *stat_prims,
                             unsigned long long *stat_rays) {
@@ -370,9 +462,13 @@ PT_DI void trace_persistent(const DevScene &s, const float4 *snodes, int2 *sstac
                     if (pid >= 0) {
                         float4 cc = __ldg(pr + 2);
                         hit = intersect_triangle(o, w, xyz(a), xyz(b), xyz(cc), tmin, tlim, t, u, v);
-                    } else {
+                    } else if (!CURVES || __float_as_int(b.w) == 0) {
                         pid &= 0x7fffffff;
                         hit = intersect_sphere(o, d, xyz(a), b.x, tmin, tlim, t);
+                    } else {
+                        pid &= 0x7fffffff;
+                        float4 cc = __ldg(pr + 2);
+                        hit = intersect_curve_piece(o, d, a, b, cc, tmin, tlim, t, u);
                     }
                     if (!hit) continue;
                     if (ANY) {

@@ -473,6 +473,22 @@ struct Loader {
             s.spheres.push_back(sp);
             ins.shape_type = PT_SHAPE_SPHERE;
             ins.shape_index = (uint32_t)s.spheres.size() - 1;
+        } else if (type == "hair") {  // resource/shape.cpp:153-181
+            std::string file = get_string(n, "filename", "");
+            std::string path = (file.size() && file[0] == '/') ? file : m_root_join(file);
+            std::string sm = get_string(n, "spline_mode", "cubic");
+            uint32_t mode = PT_CURVE_CUBIC_BSPLINE;
+            if (sm == "linear") mode = PT_CURVE_LINEAR;
+            else if (sm == "quadratic") mode = PT_CURVE_QUADRATIC_BSPLINE;
+            else if (sm == "catrom") mode = PT_CURVE_CATMULL_ROM;
+            float radius = 0.f;
+            get_float(n, "radius", radius);
+            Curves cv;
+            std::string e;
+            if (!LoadCyHair(path, radius, get_bool(n, "tapered", false), mode, cv, e)) return fail(n, e);
+            s.curves.push_back(std::move(cv));
+            ins.shape_type = PT_SHAPE_CURVES;
+            ins.shape_index = (uint32_t)s.curves.size() - 1;
         } else {
             return fail(n, "shape type '" + type + "' is not supported");
         }
@@ -665,6 +681,19 @@ const pt_scene_desc &Scene::Desc() {
     m_desc.num_materials = (uint32_t)materials.size();
     m_desc.instances = m_inst_descs.data();
     m_desc.num_instances = (uint32_t)m_inst_descs.size();
+    m_curve_descs.clear();
+    for (auto &c : curves) {
+        pt_curves_desc d{};
+        d.positions = c.positions.data();
+        d.radii = c.radii.data();
+        d.segments = c.segments.data();
+        d.num_points = (uint32_t)c.radii.size();
+        d.num_segments = (uint32_t)c.segments.size();
+        d.type = c.type;
+        m_curve_descs.push_back(d);
+    }
+    m_desc.curves = m_curve_descs.data();
+    m_desc.num_curves = (uint32_t)m_curve_descs.size();
     m_desc.env.type = has_env ? PT_ENV_CONST : PT_ENV_NONE;
     memcpy(m_desc.env.radiance, env_radiance, sizeof(env_radiance));
     if (env_map.on) {

@@ -2,11 +2,11 @@
 //
 // The host-side counterpart of resource::Scene (framework/resource/scene.h:
 // 39-57): integrator, perspective sensor + film, shapes (obj, rectangle,
-// cube, sphere) with to_world transforms, the seven BSDFs plus `twosided`,
-// area emitters on shapes and the constant environment.  `$name` values are
+// cube, sphere, hair) with to_world transforms, the seven BSDFs plus
+// `twosided`, bitmap and checkerboard textures, area emitters on shapes, the
+// constant environment and the environment map.  `$name` values are
 // substituted from <default> entries and <ref id=...> resolves named BSDFs,
-// as in framework/resource/xml/visitor.h.  Bitmap textures and environment
-// maps are reported as unsupported.
+// as in framework/resource/xml/visitor.h.
 #pragma once
 
 #include <map>
@@ -20,6 +20,14 @@ namespace Pupil::resource {
 struct Mesh {
     std::vector<float> positions, normals, texcoords;
     std::vector<uint32_t> indices;
+};
+
+// Curve strands (resource::Shape _hair): control points, per-point radii,
+// first control point of every segment, PT_CURVE_* type.
+struct Curves {
+    std::vector<float> positions, radii;
+    std::vector<uint32_t> segments;
+    uint32_t type = PT_CURVE_CUBIC_BSPLINE;
 };
 
 struct ShapeInstance {
@@ -47,6 +55,7 @@ public:
     Sensor sensor;
     std::vector<Mesh> meshes;
     std::vector<pt_sphere_desc> spheres;
+    std::vector<Curves> curves;
     std::vector<pt_material_desc> materials;
     std::vector<ShapeInstance> shape_instances;
     bool has_env = false;
@@ -76,11 +85,17 @@ private:
     std::map<std::string, uint32_t> m_named_bsdf;
     std::vector<pt_mesh_desc> m_mesh_descs;
     std::vector<pt_instance_desc> m_inst_descs;
+    std::vector<pt_curves_desc> m_curve_descs;
     pt_scene_desc m_desc{};
     friend struct Loader;
 };
 
 // Wavefront OBJ (v / vt / vn / f, polygons fan-triangulated).
 bool LoadObj(const std::string &path, Mesh &out, std::string &error);
+
+// Cem Yuksel's HAIR file as curve strands (hair.cpp): radius 0 keeps the
+// file's thickness, tapered strands fall to zero radius at the tip, mode is
+// the PT_CURVE_* type.
+bool LoadCyHair(const std::string &path, float radius, bool tapered, uint32_t mode, Curves &out, std::string &error);
 
 }  // namespace Pupil::resource

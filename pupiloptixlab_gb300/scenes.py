@@ -212,6 +212,34 @@ class Mesh:
 
 
 @dataclass
+class Curves:
+    """Curve strands (pt_curves_desc): control points, per-point radii, the
+    first control point of every segment and the curve type (abi.CURVE_*)."""
+    positions: np.ndarray          # (P, 3) float32
+    radii: np.ndarray              # (P,) float32
+    segments: np.ndarray           # (S,) uint32
+    type: int = abi.CURVE_CUBIC_BSPLINE
+
+    def __post_init__(self):
+        self.positions = np.ascontiguousarray(self.positions, np.float32).reshape(-1, 3)
+        self.radii = np.ascontiguousarray(self.radii, np.float32).reshape(-1)
+        self.segments = np.ascontiguousarray(self.segments, np.uint32).reshape(-1)
+
+    @staticmethod
+    def from_strands(strands, radii, type=abi.CURVE_CUBIC_BSPLINE) -> "Curves":
+        """Strands given as point lists; segments as the reference's hair
+        loader forms them (framework/resource/shape.cpp:401-408): every start
+        index of a strand up to its point count minus the degree."""
+        deg = 3 if type > 2 else type + 1
+        pos = [np.asarray(p, np.float32).reshape(-1, 3) for p in strands]
+        counts = np.array([p.shape[0] for p in pos], np.int64)
+        rad = [np.broadcast_to(np.asarray(r, np.float32), (c,)) for r, c in zip(radii, counts)]
+        starts = np.concatenate([[0], np.cumsum(counts)[:-1]])
+        seg = np.concatenate([np.arange(a, a + max(0, c - deg)) for a, c in zip(starts, counts)])
+        return Curves(np.concatenate(pos), np.concatenate(rad), seg.astype(np.uint32), type)
+
+
+@dataclass
 class Scene:
     """Host-side scene: what resource::Scene holds for the path-tracing pass."""
     width: int
@@ -221,6 +249,7 @@ class Scene:
     spheres: list = field(default_factory=list)     # (center(3), radius)
     materials: list = field(default_factory=list)   # abi.MaterialDesc
     instances: list = field(default_factory=list)   # dicts
+    curves: list = field(default_factory=list)      # Curves
     env: tuple | EnvMap | None = None                # constant environment radiance or a map
     camera: abi.CameraDesc | None = None
     name: str = "scene"
@@ -232,6 +261,10 @@ class Scene:
     def add_sphere(self, center, radius) -> int:
         self.spheres.append((tuple(float(c) for c in center), float(radius)))
         return len(self.spheres) - 1
+
+    def add_curves(self, curves: Curves) -> int:
+        self.curves.append(curves)
+        return len(self.curves) - 1
 
     def add_material(self, m: abi.MaterialDesc) -> int:
         self.materials.append(m)
@@ -266,6 +299,16 @@ class Scene:
         for i, (c, r) in enumerate(self.spheres):
             spheres[i].center[:] = list(c)
             spheres[i].radius = r
+        curves = (abi.CurvesDesc * max(1, len(self.curves)))()
+        for i, cv in enumerate(self.curves):
+            d = curves[i]
+            d.positions = cv.positions.ctypes.data_as(abi.c_float_p)
+            d.radii = cv.radii.ctypes.data_as(abi.c_float_p)
+            d.segments = cv.segments.ctypes.data_as(abi.c_uint_p)
+            d.num_points = cv.positions.shape[0]
+            d.num_segments = cv.segments.shape[0]
+            d.type = cv.type
+            keep.append(cv)
         mats = (abi.MaterialDesc * max(1, len(self.materials)))(*self.materials)
         insts = (abi.InstanceDesc * max(1, len(self.instances)))()
         for i, inst in enumerate(self.instances):
@@ -287,6 +330,8 @@ class Scene:
         sd.num_materials = len(self.materials)
         sd.instances = C.cast(insts, C.POINTER(abi.InstanceDesc))
         sd.num_instances = len(self.instances)
+        sd.curves = C.cast(curves, C.POINTER(abi.CurvesDesc))
+        sd.num_curves = len(self.curves)
         if isinstance(self.env, EnvMap):
             px = np.ascontiguousarray(self.env.pixels, np.float32)
             keep.append(px)
@@ -302,7 +347,7 @@ class Scene:
         if self.camera is not None:
             sd.camera = self.camera
         sd.width, sd.height, sd.max_depth = self.width, self.height, self.max_depth
-        sd._keep = (keep, meshes, spheres, mats, insts)
+        sd._keep = (keep, meshes, spheres, mats, insts, curves)
         return sd
 
 
@@ -589,4 +634,54 @@ def material_spheres(width: int = 96, height: int = 64, max_depth: int = 6) -> S
                    radiance=(8.0, 8.0, 8.0))
     s.env = (0.3, 0.35, 0.4)
     s.camera = camera(35.0, width / height, look_at_to_world((0.0, 3.0, 12.0), (0.0, 1.0, 0.0)))
+    return s
+
+
+def hair_strands(num_strands: int, points: int = 10, length: float = 1.2, radius: float = 0.012, tapered: bool = False,
+                 seed: int = 0, curl: float = 0.25) -> tuple[list, list]:
+    """Strands grown from the upper half of a unit sphere: each root steps out
+    along its normal, bends down under a constant pull and wanders with a
+    seeded curl.  Returns (point lists, radius lists); radii taper to zero
+    along a strand as the reference's tapered hair does
+    (framework/resource/shape.cpp:385-393) when tapered is set."""
+    rng = np.random.default_rng(seed)
+    roots = rng.normal(size=(num_strands, 3))
+    roots[:, 1] = np.abs(roots[:, 1]) + 0.2
+    roots /= np.linalg.norm(roots, axis=1, keepdims=True)
+    step = length / (points - 1)
+    noise = rng.normal(size=(points - 1, num_strands, 3)) * curl
+    p, d = roots.copy(), roots.copy()
+    pts = [p]
+    for k in range(points - 1):  # all strands advance together
+        d = d + np.array([0.0, -0.35, 0.0]) + noise[k]
+        d /= np.linalg.norm(d, axis=1, keepdims=True)
+        p = p + d * step
+        pts.append(p)
+    strands = list(np.stack(pts, 1).astype(np.float32))
+    r = radius * (points - 1 - np.arange(points)) / (points - 1) if tapered else np.full(points, radius)
+    return strands, [r] * num_strands
+
+
+def hair_scene(width: int = 64, height: int = 48, curve_type: int = abi.CURVE_CUBIC_BSPLINE, num_strands: int = 300,
+               points: int = 10, radius: float = 0.012, tapered: bool = False, max_depth: int = 6, seed: int = 0,
+               env: bool = True, curl: float = 0.25) -> Scene:
+    """A sphere ("head", mesh) carrying curve strands of one curve type over a
+    floor, lit by a sphere light and a constant environment; the strands'
+    instance has a rotation, a uniform scale and a translation."""
+    s = Scene(width, height, max_depth, name=f"hair_t{curve_type}")
+    floor = s.add_material(diffuse(checkerboard((0.7, 0.7, 0.7), (0.3, 0.3, 0.3), 6.0)))
+    s.add_instance(abi.SHAPE_MESH, s.add_mesh(grid(4, 4, 6.0, 0.0)), floor)
+    head = s.add_material(plastic((0.6, 0.5, 0.4), 1.5, 1.0))
+    s.add_instance(abi.SHAPE_MESH, s.add_mesh(displaced_icosphere(1, 0.0, 3)), head,
+                   translate(0.0, 1.4, 0.0) @ scale(0.95))
+    strands, radii = hair_strands(num_strands, points, radius=radius, tapered=tapered, seed=seed, curl=curl)
+    hair = s.add_material(rough_conductor(0.25, eta=(0.2, 0.4, 1.4), k=(3.5, 2.5, 2.0)))
+    cv = s.add_curves(Curves.from_strands(strands, radii, curve_type))
+    s.add_instance(abi.SHAPE_CURVES, cv, hair, translate(0.0, 1.4, 0.0) @ rotate_y(25.0) @ scale(1.0))
+    lm = s.add_material(diffuse(0.0, twosided=True))
+    s.add_instance(abi.SHAPE_SPHERE, s.add_sphere((0.0, 0.0, 0.0), 0.6), lm, translate(2.0, 5.0, 3.0),
+                   radiance=(14.0, 13.0, 12.0))
+    if env:
+        s.env = (0.25, 0.3, 0.35)
+    s.camera = camera(35.0, width / height, look_at_to_world((0.0, 2.2, 5.5), (0.0, 1.3, 0.0)))
     return s

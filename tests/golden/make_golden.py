@@ -3,8 +3,8 @@ headers compiled for the host (oracle/_ref/libpupil_ref.so, built by
 `make -C oracle ref` from the PupilOptixLab tree).
 
 The reference has no tests and no fixtures of its own; these vectors are
-its material, Fresnel, GGX, sampling, random-stream and emitter code run on
-seeded inputs.  Run once in a container that holds the reference tree:
+its material, Fresnel, GGX, sampling, random-stream, emitter and curve code
+run on seeded inputs.  Run once in a container that holds the reference tree:
 
     make -C oracle ref && python tests/golden/make_golden.py
 
@@ -186,6 +186,28 @@ def main():
                    P(ev), m)
     g.update(envmap_pixels=emap, envmap_tw=tw, envmap_tl=tl, envmap_xi=xi, envmap_sample=es, envmap_eval_in=ev_in,
              envmap_eval=ev)
+
+    # curve interpolators and SurfaceNormal (render/curve.h) for the four
+    # curve types: random control points (radius in w), u with the end values
+    # 0 and 1 (cap normals, the cubic derivative's triple-knot nudge), hit
+    # points slightly off the swept circle at u
+    nc = 256
+    for ct in range(4):
+        ctrl = np.zeros((nc, 4, 4), np.float32)
+        ctrl[:, :, :3] = rng.uniform(-1, 1, (nc, 4, 3))
+        ctrl[:, :, 3] = rng.uniform(0.01, 0.2, (nc, 4))
+        u = rng.uniform(0, 1, nc).astype(np.float32)
+        u[:4] = [0.0, 1.0, 0.5, 1e-7]
+        probe = np.zeros((nc, 15), np.float32)
+        ref.ref_curve(ct, P(ctrl), P(u), P(np.zeros((nc, 3), np.float32)), P(probe), nc)
+        vel = probe[:, 4:7].astype(np.float64)
+        side = rng.normal(size=(nc, 3))
+        side -= (np.sum(side * vel, 1) / np.maximum(np.sum(vel * vel, 1), 1e-12))[:, None] * vel
+        side /= np.linalg.norm(side, axis=1, keepdims=True)
+        ps = (probe[:, 0:3] + side * (probe[:, 3:4] * rng.uniform(0.98, 1.02, (nc, 1)))).astype(np.float32)
+        out = np.zeros((nc, 15), np.float32)
+        ref.ref_curve(ct, P(ctrl), P(u), P(ps), P(out), nc)
+        g.update({f"curve{ct}_ctrl": ctrl, f"curve{ct}_u": u, f"curve{ct}_ps": ps, f"curve{ct}_out": out})
 
     np.savez_compressed(OUT, **g)
     print(f"wrote {OUT} ({OUT.stat().st_size} bytes, {len(g)} arrays)")

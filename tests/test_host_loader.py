@@ -310,3 +310,82 @@ def test_exr_writer_and_reader(host, tmp_path):
     assert (e.type, e.width, e.height) == (abi.ENV_MAP, 7, 5)
     px = np.ctypeslib.as_array(C.cast(e.pixels, C.POINTER(C.c_float)), shape=(5, 7, 4))
     assert np.array_equal(px, img)
+
+
+def _write_hair(path, strands, thickness=None, default_segments=None, default_thickness=0.01):
+    """Cem Yuksel's HAIR layout: 128-byte header, then (by flag bit) the
+    per-strand segment counts (u16), points (3 f32), thickness (f32)."""
+    import struct
+    seg = np.array([len(s) - 1 for s in strands], np.uint16)
+    pts = np.concatenate(strands).astype("<f4")
+    flags = 2 | (0 if default_segments is not None else 1) | (4 if thickness is not None else 0)
+    head = struct.pack("<4sIIIIff3f", b"HAIR", len(strands), pts.shape[0], flags,
+                       default_segments or 0, default_thickness, 1.0, 0.5, 0.5, 0.5)
+    head += b"test".ljust(88, b"\0")
+    body = b"" if default_segments is not None else seg.astype("<u2").tobytes()
+    body += pts.tobytes()
+    if thickness is not None:
+        body += np.asarray(thickness, "<f4").tobytes()
+    path.write_bytes(head + body)
+
+
+def test_hair_shape(host, tmp_path):
+    """<shape type="hair"> (resource/shape.cpp:153-181, 369-420): the HAIR file's
+    points become curve control points, the segments start at every point of a
+    strand up to its count minus the spline degree, radius overrides the file
+    thickness, tapered strands fall linearly to zero; the descriptor renders
+    through the oracle."""
+    import oracle
+    rng = np.random.default_rng(4)
+    strands = [np.cumsum(rng.normal(size=(n, 3)) * 0.2, 0) + [0, 1, 0] for n in (6, 9, 5)]
+    npts = sum(len(s) for s in strands)
+    thick = rng.uniform(0.01, 0.03, npts)
+    _write_hair(tmp_path / "a.hair", strands, thick)
+    _write_hair(tmp_path / "b.hair", [s[:5] for s in strands], None, default_segments=4, default_thickness=0.02)
+    modes = {"linear": (abi.CURVE_LINEAR, 1), "quadratic": (abi.CURVE_QUADRATIC_BSPLINE, 2),
+             "cubic": (abi.CURVE_CUBIC_BSPLINE, 3), "catrom": (abi.CURVE_CATMULL_ROM, 3)}
+    for mode, (ctype, deg) in modes.items():
+        xml = f"""<scene version="3.0.0">
+          <sensor type="perspective"><float name="fov" value="40"/>
+            <transform name="to_world"><lookat origin="0, 1, 6" target="0, 1, 0" up="0, 1, 0"/></transform>
+            <film type="hdrfilm"><integer name="width" value="24"/><integer name="height" value="16"/></film></sensor>
+          <shape type="hair"><string name="filename" value="a.hair"/><string name="spline_mode" value="{mode}"/>
+            <bsdf type="roughconductor"/></shape>
+          <shape type="hair"><string name="filename" value="a.hair"/><string name="spline_mode" value="{mode}"/>
+            <float name="radius" value="0.05"/><boolean name="tapered" value="true"/>
+            <transform name="to_world"><translate x="1"/></transform></shape>
+          <shape type="hair"><string name="filename" value="b.hair"/><float name="radius" value="0.04"/></shape>
+          <emitter type="constant"><rgb name="radiance" value="0.5"/></emitter>
+        </scene>"""
+        (tmp_path / "h.xml").write_text(xml)
+        s = host.XmlScene(str(tmp_path / "h.xml"))
+        d = s.desc()
+        assert d.num_curves == 3
+        c0, c1, c2 = d.curves[0], d.curves[1], d.curves[2]
+        assert (c0.type, c1.type, c2.type) == (ctype, ctype, abi.CURVE_CUBIC_BSPLINE)
+        assert c0.num_points == npts
+        pos = np.ctypeslib.as_array(c0.positions, (npts * 3,)).reshape(-1, 3)
+        assert np.array_equal(pos, np.concatenate(strands).astype(np.float32))
+        r0 = np.ctypeslib.as_array(c0.radii, (npts,))
+        assert np.array_equal(r0, thick.astype(np.float32))
+        segs = np.ctypeslib.as_array(c0.segments, (c0.num_segments,))
+        starts = np.cumsum([0] + [len(s) for s in strands])
+        expect = np.concatenate([np.arange(a, b - deg) for a, b in zip(starts[:-1], starts[1:])])
+        assert np.array_equal(segs, expect)
+        r1 = np.ctypeslib.as_array(c1.radii, (npts,))
+        taper = np.concatenate([0.05 * (len(s) - 1 - np.arange(len(s))) / (len(s) - 1) for s in strands])
+        assert np.allclose(r1, taper, rtol=1e-6, atol=0)
+        r2 = np.ctypeslib.as_array(c2.radii, (15,))
+        assert np.all(r2 == np.float32(0.04)) and c2.num_segments == 3 * (5 - 3)
+        insts = [d.instances[i] for i in range(d.num_instances)]
+        assert [i.shape_type for i in insts] == [abi.SHAPE_CURVES] * 3
+        assert insts[1].to_world[3] == 1.0
+        o = oracle.OracleScene(s)
+        assert o.num_curves()[0] == c0.num_segments + c1.num_segments + c2.num_segments
+        out = o.render(abi.RenderParams(spp=1, seed=0, accumulate=1, rng=abi.RNG_PCG32))
+        assert np.isfinite(out["accum"]).all()
+    (tmp_path / "bad.hair").write_bytes(b"HAIX" + bytes(124))
+    (tmp_path / "h2.xml").write_text("<scene><shape type='hair'><string name='filename' value='bad.hair'/></shape></scene>")
+    with pytest.raises(abi.PtError) as e:
+        host.XmlScene(str(tmp_path / "h2.xml"))
+    assert "not a HAIR file" in str(e.value)

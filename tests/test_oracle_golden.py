@@ -127,3 +127,16 @@ def test_envmap_matches_reference(golden):
     e, _ = oracle.envmap(1, px, 1.5, tw, tl, golden["envmap_eval_in"])
     assert np.allclose(e, golden["envmap_eval"], rtol=1e-4, atol=1e-6)
     assert (s[:, 6] > 0).mean() > 0.9
+
+
+@pytest.mark.parametrize("curve_type", [0, 1, 2, 3])
+def test_curve_interpolators_and_normal_match_reference(golden, curve_type):
+    """Curve interpolators (Position4, Velocity4, Acceleration3) and
+    SurfaceNormal of render/curve.h, compiled for the host from the reference
+    tree, against the oracle's restatement: bit for bit, including the cap
+    normals at u = 0 / 1 and the cubic derivative's triple-knot nudge."""
+    k = f"curve{curve_type}"
+    got = oracle.curve(curve_type, golden[k + "_ctrl"], golden[k + "_u"], golden[k + "_ps"])
+    ref = golden[k + "_out"]
+    assert np.isfinite(ref).all()
+    assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
