@@ -119,9 +119,10 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def committed_traffic():
-    """DRAM bytes per launch of the closest-hit kernel from the committed ncu summary."""
-    p = ROOT / "profiles" / "extend_traffic.json"
+def committed_traffic(workload: str = "headline"):
+    """DRAM bytes per launch of the closest-hit kernel from the committed ncu
+    summary of the same workload."""
+    p = ROOT / "profiles" / ("extend_traffic.json" if workload == "headline" else f"extend_traffic_{workload}.json")
     if p.exists():
         try:
             return json.loads(p.read_text())
@@ -641,7 +642,7 @@ def main():
     avg_launch_s = ext_ms / max(1, ext_launches) * 1e-3
     achieved = per_launch_bytes / avg_launch_s / 1e9 if ext_ms > 0 else None
     peak, peak_kind = measured_peaks()
-    traffic = committed_traffic()
+    traffic = committed_traffic(args.workload)
     cpu = None
     if not args.no_cpu_baseline:
         cpu = cpu_baseline(sc, 0, args.cpu_seconds, args.depth)
