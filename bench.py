@@ -77,6 +77,8 @@ def parse():
     ap.add_argument("--instances", type=int, default=200)
     ap.add_argument("--bvh-width", type=int, default=4)
     ap.add_argument("--max-leaf", type=int, default=4)
+    ap.add_argument("--bvh-fast-build", action="store_true",
+                    help="build the binary tree as a Morton radix tree instead of by PLOC clustering")
     ap.add_argument("--smem-nodes", type=int, default=0)
     ap.add_argument("--block-size", type=int, default=0)
     ap.add_argument("--wave-spp", type=int, default=0)
@@ -559,7 +561,8 @@ def main():
         sc = scenes.icosphere_field(args.width, args.height, args.depth, args.instances)
         metric, workload = METRIC, WORKLOAD
     ctx = Context(local)
-    g = GpuScene(ctx, sc, bvh_width=args.bvh_width, max_leaf=args.max_leaf, smem_nodes=args.smem_nodes)
+    g = GpuScene(ctx, sc, bvh_width=args.bvh_width, max_leaf=args.max_leaf, smem_nodes=args.smem_nodes,
+                 bvh_flags=abi.BVH_FAST_BUILD if args.bvh_fast_build else 0)
     buffers = g.alloc_buffers()
     tune = None
     if args.autotune:
@@ -676,7 +679,8 @@ def main():
                           "shadow_nodes_per_ray": cst.shadow_nodes_visited / max(1, cst.shadow_rays),
                           "shadow_prims_per_ray": cst.shadow_prims_tested / max(1, cst.shadow_rays)},
         "bvh": {"nodes": int(bst.num_nodes), "sah_cost": float(bst.sah_cost), "build_ms": float(bst.build_ms),
-                "depth": int(bst.max_depth)},
+                "depth": int(bst.max_depth),
+                "builder": "ploc" if bst.builder == abi.BVH_BUILDER_PLOC else "radix tree"},
         "cpu_baseline": cpu,
     }
     print(json.dumps(line), flush=True)

@@ -235,10 +235,14 @@ typedef struct pt_device_opts {
     uint32_t flags;  /* reserved, 0 */
 } pt_device_opts;
 
-/* BVH options.  width: 2, 4 or 8 children per node (wide nodes collapsed from a
- * Morton-code LBVH with an SAH cost model).  max_leaf_size: primitives per leaf
- * (1..15).  smem_nodes: number of top nodes staged in shared memory by the
- * traversal kernels (0 = none). */
+/* BVH options.  width: 2, 4 or 8 children per node, collapsed with an SAH
+ * cost model from a binary tree built over Morton-sorted primitives: by
+ * default PLOC (parallel locally-ordered clustering, higher quality), with
+ * PT_BVH_FAST_BUILD the Karras radix tree (faster build, for per-frame
+ * rebuilds).  max_leaf_size: primitives per leaf (1..15).  smem_nodes: number
+ * of top nodes staged in shared memory by the traversal kernels (0 = none). */
+enum { PT_BVH_FAST_BUILD = 1 };
+enum { PT_BVH_BUILDER_RADIX = 0, PT_BVH_BUILDER_PLOC = 1 };
 typedef struct pt_bvh_opts {
     uint32_t width;
     uint32_t max_leaf_size;
@@ -252,10 +256,11 @@ typedef struct pt_bvh_stats {
     uint32_t num_leaves;
     uint32_t num_prims;
     uint32_t max_depth;
-    float sah_cost;        /* SAH cost of the wide tree (node cost 1, primitive cost 1) */
+    float sah_cost;        /* SAH cost of the wide tree (node cost 1.2, primitive cost 1) */
     float build_ms;        /* device time of the last build or refit */
     uint64_t node_bytes;
     uint64_t prim_bytes;
+    uint32_t builder;      /* PT_BVH_BUILDER_*: how the binary tree was built */
 } pt_bvh_stats;
 
 /* Render parameters: PTPass launch params (example/path_tracer/type.h:9-33).

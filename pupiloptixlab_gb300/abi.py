@@ -93,10 +93,15 @@ class BvhOpts(C.Structure):
                 ("flags", C.c_uint32)]
 
 
+BVH_FAST_BUILD = 1
+BVH_BUILDER_RADIX, BVH_BUILDER_PLOC = 0, 1
+
+
 class BvhStats(C.Structure):
     _fields_ = [("width", C.c_uint32), ("num_nodes", C.c_uint32), ("num_leaves", C.c_uint32),
                 ("num_prims", C.c_uint32), ("max_depth", C.c_uint32), ("sah_cost", C.c_float),
-                ("build_ms", C.c_float), ("node_bytes", C.c_uint64), ("prim_bytes", C.c_uint64)]
+                ("build_ms", C.c_float), ("node_bytes", C.c_uint64), ("prim_bytes", C.c_uint64),
+                ("builder", C.c_uint32)]
 
 
 class RenderParams(C.Structure):

@@ -40,7 +40,7 @@ class GpuScene:
     """A scene uploaded to the GPU with its acceleration structure."""
 
     def __init__(self, ctx: Context, scene: Scene, bvh_width: int = 4, max_leaf: int = 4, smem_nodes: int = 0,
-                 build: bool = True):
+                 build: bool = True, bvh_flags: int = 0):
         self.ctx = ctx
         self.lib = ctx.lib
         self.scene = scene
@@ -50,7 +50,7 @@ class GpuScene:
         abi.check(self.lib.pt_scene_upload(ctx.handle, C.byref(desc), C.byref(h)), "pt_scene_upload", self.lib)
         self.handle = h
         if build:
-            self.build_bvh(bvh_width, max_leaf, smem_nodes)
+            self.build_bvh(bvh_width, max_leaf, smem_nodes, flags=bvh_flags)
 
     def close(self):
         if getattr(self, "handle", None):
@@ -63,8 +63,10 @@ class GpuScene:
         except Exception:
             pass
 
-    def build_bvh(self, width: int = 4, max_leaf: int = 4, smem_nodes: int = 0, stream=None) -> abi.BvhStats:
-        o = abi.BvhOpts(width, max_leaf, smem_nodes, 0)
+    def build_bvh(self, width: int = 4, max_leaf: int = 4, smem_nodes: int = 0, stream=None,
+                  flags: int = 0) -> abi.BvhStats:
+        """pt_bvh_build; flags = abi.BVH_FAST_BUILD builds the radix tree instead of PLOC."""
+        o = abi.BvhOpts(width, max_leaf, smem_nodes, flags)
         abi.check(self.lib.pt_bvh_build(self.handle, C.byref(o), _stream_ptr(stream)), "pt_bvh_build", self.lib)
         return self.bvh_stats()
 

@@ -295,6 +295,156 @@ __global__ void k_bottom_up(int n, const int *left, const int *right, const int 
     }
 }
 
+// 4'/5'. PLOC: parallel locally-ordered clustering (Meister and Bittner,
+// IEEE TVCG 2018), the default build.  The Morton-sorted primitives start as
+// clusters (leaf k = node n-1+k); each pass every cluster finds the cluster
+// within kPlocRadius positions whose union has the smallest surface area,
+// mutual nearest neighbours merge into a new internal node (id from a
+// counter, 0..n-2) that takes the lower position, and the array is compacted.
+// Boxes, counts and the SAH leaf-or-split decision of a node are made when it
+// forms (its children are complete by then).  Subtrees are then laid out
+// depth first so that every subtree covers a contiguous range of the
+// primitive order, as the wide collapse expects.
+constexpr int kPlocRadius = 16;
+constexpr int kPlocBlock = 256;
+constexpr int kPlocMaxDepth = 256;  // a deeper binary tree makes the build fall back to the radix tree
+
+__global__ void k_ploc_init(int n, const uint32_t *order, const float4 *plo, const float4 *phi, float4 *nlo,
+                            float4 *nhi, int *ncount, float *ncost, int *nleaf, int *cl) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    int leaf = n - 1 + k;
+    uint32_t p = order[k];
+    float4 lo = plo[p], hi = phi[p];
+    nlo[leaf] = lo;
+    nhi[leaf] = hi;
+    ncount[leaf] = 1;
+    ncost[leaf] = kCostPrim * half_area(lo, hi);
+    nleaf[leaf] = 1;
+    cl[k] = leaf;
+}
+
+// Nearest neighbour of every cluster: smallest union area, ties to the lower
+// position (so the closest pair overall is always mutual).
+__global__ void __launch_bounds__(kPlocBlock) k_ploc_nn(int m, const int *cl, const float4 *nlo, const float4 *nhi,
+                                                        int *nn) {
+    __shared__ float4 slo[kPlocBlock + 2 * kPlocRadius], shi[kPlocBlock + 2 * kPlocRadius];
+    const int b0 = blockIdx.x * kPlocBlock;
+    for (int t = threadIdx.x; t < kPlocBlock + 2 * kPlocRadius; t += blockDim.x) {
+        const int g = b0 - kPlocRadius + t;
+        if (g >= 0 && g < m) {
+            const int id = cl[g];
+            slo[t] = nlo[id];
+            shi[t] = nhi[id];
+        }
+    }
+    __syncthreads();
+    const int i = b0 + threadIdx.x;
+    if (i >= m) return;
+    const float4 lo = slo[threadIdx.x + kPlocRadius], hi = shi[threadIdx.x + kPlocRadius];
+    float best = FLT_MAX;
+    int bj = -1;
+    for (int o = -kPlocRadius; o <= kPlocRadius; o++) {
+        const int j = i + o;
+        if (o == 0 || j < 0 || j >= m) continue;
+        const float4 l2 = slo[threadIdx.x + kPlocRadius + o], h2 = shi[threadIdx.x + kPlocRadius + o];
+        const float4 ulo = make_float4(fminf(lo.x, l2.x), fminf(lo.y, l2.y), fminf(lo.z, l2.z), 0.f);
+        const float4 uhi = make_float4(fmaxf(hi.x, h2.x), fmaxf(hi.y, h2.y), fmaxf(hi.z, h2.z), 0.f);
+        const float a = half_area(ulo, uhi);
+        if (a < best) {  // positions are visited in increasing order: ties keep the lower one
+            best = a;
+            bj = j;
+        }
+    }
+    nn[i] = bj;
+}
+
+// Merge mutual pairs: keep[i] = 1 where position i survives, out_id[i] its node.
+__global__ void k_ploc_merge(int m, const int *cl, const int *nn, uint32_t *keep, int *out_id, uint32_t *node_ctr,
+                             int *left, int *right, int *parent, float4 *nlo, float4 *nhi, int *ncount, float *ncost,
+                             int *nleaf, int max_leaf) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    const int j = nn[i];
+    const bool mutual = j >= 0 && nn[j] == i;
+    if (!mutual) {
+        keep[i] = 1;
+        out_id[i] = cl[i];
+        return;
+    }
+    if (i > j) {
+        keep[i] = 0;
+        return;
+    }
+    const int a = cl[i], b = cl[j];
+    const int id = (int)atomicAdd(node_ctr, 1u);
+    const float4 la = nlo[a], ha = nhi[a], lb = nlo[b], hb = nhi[b];
+    const float4 blo = make_float4(fminf(la.x, lb.x), fminf(la.y, lb.y), fminf(la.z, lb.z), 0.f);
+    const float4 bhi = make_float4(fmaxf(ha.x, hb.x), fmaxf(ha.y, hb.y), fmaxf(ha.z, hb.z), 0.f);
+    const int cnt = ncount[a] + ncount[b];
+    const float area = half_area(blo, bhi);
+    const float c_split = kCostNode * area + ncost[a] + ncost[b];
+    const float c_leaf = cnt <= max_leaf ? kCostPrim * area * (float)cnt : FLT_MAX;
+    const bool mk_leaf = c_leaf <= c_split;
+    left[id] = a;
+    right[id] = b;
+    parent[a] = id;
+    parent[b] = id;
+    nlo[id] = blo;
+    nhi[id] = bhi;
+    ncount[id] = cnt;
+    ncost[id] = mk_leaf ? c_leaf : c_split;
+    nleaf[id] = mk_leaf ? 1 : 0;
+    keep[i] = 1;
+    out_id[i] = id;
+}
+
+// keep holds the exclusive prefix sums of the survival flags (m + 1 entries).
+__global__ void k_ploc_compact(int m, const uint32_t *pre, const int *out_id, int *cl_next) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    if (pre[i + 1] != pre[i]) cl_next[pre[i]] = out_id[i];
+}
+
+// Depth-first position of every node (leftmost leaf of its subtree): the sum
+// of the left siblings' primitive counts along the path to the root.  A path
+// longer than kPlocMaxDepth raises the failure flag.
+__global__ void k_ploc_offsets(int n, const int *left, const int *right, const int *parent, const int *ncount,
+                               int *offs, uint32_t *fail) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= 2 * n - 1) return;
+    int cur = x, off = 0, steps = 0;
+    for (int p = parent[cur]; p >= 0; p = parent[cur]) {
+        if (right[p] == cur) off += ncount[left[p]];
+        cur = p;
+        if (++steps > kPlocMaxDepth) {
+            atomicOr(fail, 1u);
+            break;
+        }
+    }
+    offs[x] = off;
+}
+
+// Renumber leaves to their depth-first positions (leaf at position q is node
+// n-1+q), record every internal node's first position, permute the order.
+__global__ void k_ploc_finish(int n, const int *offs, const uint32_t *order, const float4 *nlo, const float4 *nhi,
+                              int *left, int *right, int *rfirst, uint32_t *order_out, float4 *leaf_lo,
+                              float4 *leaf_hi) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= 2 * n - 1) return;
+    if (x >= n - 1) {
+        const int q = offs[x];
+        order_out[q] = order[x - (n - 1)];
+        leaf_lo[q] = nlo[x];
+        leaf_hi[q] = nhi[x];
+    } else {
+        rfirst[x] = offs[x];
+        const int l = left[x], r = right[x];
+        left[x] = l >= n - 1 ? n - 1 + offs[l] : l;
+        right[x] = r >= n - 1 ? n - 1 + offs[r] : r;
+    }
+}
+
 __device__ __forceinline__ void padded(float4 lo, float4 hi, float scene_mag, float3 &plo, float3 &phi) {
     float mag = fmaxf(fmaxf(fmaxf(fabsf(lo.x), fabsf(lo.y)), fmaxf(fabsf(lo.z), fabsf(hi.x))), fmaxf(fabsf(hi.y), fabsf(hi.z)));
     float ext = fmaxf(fmaxf(hi.x - lo.x, hi.y - lo.y), hi.z - lo.z);
@@ -522,8 +672,11 @@ struct Scratch {
     float4 *nlo, *nhi;
     float *ncost;
     int2 *items[2];
-    uint32_t *counters;  // [0..5] centroid bounds, [6] n_wide, [7] n_out0, [8] n_out1
+    uint32_t *counters;  // [0..5] centroid bounds, [6] n_wide, [7] n_out0, [8] n_out1, [9] PLOC nodes, [10] PLOC failure
     double *sah;
+    int *cl[2], *nn, *out_id, *offs;  // PLOC clusters, neighbours, merge results, depth-first positions
+    uint32_t *keep, *order2;
+    float4 *leaf_lo, *leaf_hi;
 };
 
 template <class T>
@@ -544,30 +697,32 @@ size_t carve_size(size_t n, uint32_t tiles) {
     add(4 * 2 * n);
     add(8 * n); add(8 * n);
     add(64); add(64);
+    add(4 * n); add(4 * n); add(4 * n); add(4 * n); add(4 * 2 * n);
+    add(4 * (n + 1)); add(4 * n);
+    add(16 * n); add(16 * n);
     return t;
 }
 
 template <int K>
-int build_wide(pt_scene *s, const Scratch &sc, uint32_t n, cudaStream_t st) {
+int build_wide(pt_scene *s, const Scratch &sc, uint32_t n, int root, cudaStream_t st) {
     s->level_start.clear();
     size_t node_bytes = (size_t)std::max<uint32_t>(1, n > 1 ? n - 1 : 1) * 32 * K;
     int e = s->nodes.ensure(node_bytes);
     if (e != PT_OK) return e;
     float *nodes = s->nodes.as<float>();
     const int tb = 256;
-    // root
+    // root: binary node `root` (internal), or the single leaf (node 0 when n == 1)
     int root_leaf = 0;
-    if (n > 1) PT_CUDA_TRY(cudaMemcpyAsync(&root_leaf, sc.nleaf, sizeof(int), cudaMemcpyDeviceToHost, st));
+    if (n > 1) PT_CUDA_TRY(cudaMemcpyAsync(&root_leaf, sc.nleaf + root, sizeof(int), cudaMemcpyDeviceToHost, st));
     PT_CUDA_TRY(cudaStreamSynchronize(st));
     if (n <= 1 || root_leaf) {
-        int root = n > 1 ? 0 : 0;  // internal node 0, or the single leaf (node 0 when n == 1)
-        k_leaf_root<K><<<1, 32, 0, st>>>(nodes, (int)n, sc.nlo, sc.nhi, root, s->scene_mag);
+        k_leaf_root<K><<<1, 32, 0, st>>>(nodes, (int)n, sc.nlo, sc.nhi, n > 1 ? root : 0, s->scene_mag);
         s->level_start = {0, 1};
         return PT_OK;
     }
     uint32_t h_init[3] = {1, 1, 0};  // n_wide = 1 (root), n_out0 = 1 (root item), n_out1 = 0
     PT_CUDA_TRY(cudaMemcpyAsync(sc.counters + 6, h_init, sizeof(h_init), cudaMemcpyHostToDevice, st));
-    int2 root_item = make_int2(0, 0);
+    int2 root_item = make_int2(0, root);
     PT_CUDA_TRY(cudaMemcpyAsync(sc.items[0], &root_item, sizeof(int2), cudaMemcpyHostToDevice, st));
     uint32_t level_count = 1, start = 0;
     int cur = 0;
@@ -622,6 +777,60 @@ int compute_sah(pt_scene *s, double *scratch2, cudaStream_t st, float &out) {
     return PT_OK;
 }
 
+// PLOC over the sorted order in s->bvh_order (n >= 2).  Returns PT_OK with
+// the binary root in *root, or PT_OK with *root = -1 when clustering stalls
+// (ties in degenerate scenes) or the tree is deeper than the traversal can
+// handle; the caller then builds the radix tree instead.
+int ploc_build(pt_scene *s, const Scratch &sc, uint32_t n, int max_leaf, cudaStream_t st, int *root) {
+    *root = -1;
+    const int tb = 256;
+    uint32_t *order = s->bvh_order.as<uint32_t>();
+    PT_CUDA_TRY(cudaMemsetAsync(sc.parent, 0xff, 4 * (2 * (size_t)n - 1), st));
+    PT_CUDA_TRY(cudaMemsetAsync(sc.counters + 9, 0, 2 * sizeof(uint32_t), st));
+    k_ploc_init<<<blocks(n, tb), tb, 0, st>>>((int)n, order, sc.plo, sc.phi, sc.nlo, sc.nhi, sc.ncount, sc.ncost,
+                                              sc.nleaf, sc.cl[0]);
+    PT_CUDA_TRY(cudaGetLastError());
+    uint32_t m = n;
+    int cur = 0;
+    int log2n = 0;
+    while ((1u << log2n) < n) log2n++;
+    const int max_passes = 64 + 8 * log2n;
+    for (int pass = 0; m > 1; pass++) {
+        if (pass >= max_passes) return PT_OK;  // too slow to converge: radix tree
+        k_ploc_nn<<<blocks(m, kPlocBlock), kPlocBlock, 0, st>>>((int)m, sc.cl[cur], sc.nlo, sc.nhi, sc.nn);
+        k_ploc_merge<<<blocks(m, tb), tb, 0, st>>>((int)m, sc.cl[cur], sc.nn, sc.keep, sc.out_id, sc.counters + 9,
+                                                   sc.left, sc.right, sc.parent, sc.nlo, sc.nhi, sc.ncount, sc.ncost,
+                                                   sc.nleaf, max_leaf);
+        PT_CUDA_TRY(cudaMemsetAsync(sc.keep + m, 0, sizeof(uint32_t), st));
+        k_scan_excl<<<1, 1024, 0, st>>>(sc.keep, m + 1);
+        k_ploc_compact<<<blocks(m, tb), tb, 0, st>>>((int)m, sc.keep, sc.out_id, sc.cl[cur ^ 1]);
+        PT_CUDA_TRY(cudaGetLastError());
+        uint32_t next = 0;
+        PT_CUDA_TRY(cudaMemcpyAsync(&next, sc.keep + m, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        PT_CUDA_TRY(cudaStreamSynchronize(st));
+        if (next == 0 || next >= m) return PT_OK;  // cannot happen (the closest pair always merges)
+        m = next;
+        cur ^= 1;
+    }
+    const uint32_t nodes2 = 2 * n - 1;
+    k_ploc_offsets<<<blocks(nodes2, tb), tb, 0, st>>>((int)n, sc.left, sc.right, sc.parent, sc.ncount, sc.offs,
+                                                     sc.counters + 10);
+    k_ploc_finish<<<blocks(nodes2, tb), tb, 0, st>>>((int)n, sc.offs, order, sc.nlo, sc.nhi, sc.left, sc.right,
+                                                    sc.rfirst, sc.order2, sc.leaf_lo, sc.leaf_hi);
+    PT_CUDA_TRY(cudaGetLastError());
+    PT_CUDA_TRY(cudaMemcpyAsync(order, sc.order2, 4 * (size_t)n, cudaMemcpyDeviceToDevice, st));
+    PT_CUDA_TRY(cudaMemcpyAsync(sc.nlo + (n - 1), sc.leaf_lo, 16 * (size_t)n, cudaMemcpyDeviceToDevice, st));
+    PT_CUDA_TRY(cudaMemcpyAsync(sc.nhi + (n - 1), sc.leaf_hi, 16 * (size_t)n, cudaMemcpyDeviceToDevice, st));
+    uint32_t h[2] = {0, 0};
+    int r = -1;
+    PT_CUDA_TRY(cudaMemcpyAsync(h, sc.counters + 9, sizeof(h), cudaMemcpyDeviceToHost, st));
+    PT_CUDA_TRY(cudaMemcpyAsync(&r, sc.cl[cur], sizeof(int), cudaMemcpyDeviceToHost, st));
+    PT_CUDA_TRY(cudaStreamSynchronize(st));
+    if (h[1] != 0 || h[0] != n - 1) return PT_OK;  // too deep (or incomplete): radix tree
+    *root = r;
+    return PT_OK;
+}
+
 }  // namespace
 
 int pt_bvh_build_impl(pt_scene *s, const pt_bvh_opts *o, cudaStream_t st) {
@@ -655,17 +864,26 @@ int pt_bvh_build_impl(pt_scene *s, const pt_bvh_opts *o, cudaStream_t st) {
     sc.items[1] = carve<int2>(p, nn);
     sc.counters = carve<uint32_t>(p, 16);
     sc.sah = carve<double>(p, 8);
+    sc.cl[0] = carve<int>(p, nn);
+    sc.cl[1] = carve<int>(p, nn);
+    sc.nn = carve<int>(p, nn);
+    sc.out_id = carve<int>(p, nn);
+    sc.offs = carve<int>(p, 2 * nn);
+    sc.keep = carve<uint32_t>(p, nn + 1);
+    sc.order2 = carve<uint32_t>(p, nn);
+    sc.leaf_lo = carve<float4>(p, nn);
+    sc.leaf_hi = carve<float4>(p, nn);
     if ((e = s->bvh_order.ensure(std::max<size_t>(4 * (size_t)n, 16))) != PT_OK) return e;
     if ((e = s->prims_bvh.ensure(std::max<size_t>(48 * (size_t)n, 48))) != PT_OK) return e;
 
     const int tb = 256;
     uint32_t cb_init[6] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0u, 0u, 0u};
     PT_CUDA_TRY(cudaMemcpyAsync(sc.counters, cb_init, sizeof(cb_init), cudaMemcpyHostToDevice, st));
+    int cur = 0;  // sort buffer holding the sorted (code, primitive) pairs
     if (n > 0) {
         const float4 *prims = s->prims_world.as<float4>();
         k_prim_bounds<<<blocks(n, tb), tb, 0, st>>>(prims, n, sc.plo, sc.phi, sc.counters);
         k_morton<<<blocks(n, tb), tb, 0, st>>>(sc.plo, sc.phi, n, sc.counters, sc.keys[0], sc.vals[0]);
-        int cur = 0;
         for (int pass = 0; pass < 8; pass++) {
             int shift = pass * 8;
             k_radix_hist<<<tiles, kSortThreads, 0, st>>>(sc.keys[cur], n, shift, sc.hist, tiles);
@@ -677,21 +895,49 @@ int pt_bvh_build_impl(pt_scene *s, const pt_bvh_opts *o, cudaStream_t st) {
         PT_CUDA_TRY(cudaGetLastError());
         // after 8 passes the sorted pairs are back in buffer 0
         PT_CUDA_TRY(cudaMemcpyAsync(s->bvh_order.ptr, sc.vals[cur], 4 * (size_t)n, cudaMemcpyDeviceToDevice, st));
+    }
+    // binary tree: PLOC by default, the radix tree for PT_BVH_FAST_BUILD, for
+    // a PLOC build that did not converge, or one whose wide tree is deeper
+    // than the traversal stack covers (kShortStack + kSpillStack entries)
+    const auto radix_tree = [&]() -> int {
+        if (n == 0) return PT_OK;  // no primitives: nothing to sort or link (2n - 1 would wrap)
+        PT_CUDA_TRY(cudaMemcpyAsync(s->bvh_order.ptr, sc.vals[cur], 4 * (size_t)n, cudaMemcpyDeviceToDevice, st));
         PT_CUDA_TRY(cudaMemsetAsync(sc.parent, 0xff, 4 * (2 * (size_t)n - 1), st));
         PT_CUDA_TRY(cudaMemsetAsync(sc.flags, 0, 4 * (size_t)n, st));
         if (n > 1) k_karras<<<blocks(n - 1, tb), tb, 0, st>>>(sc.keys[cur], (int)n, sc.left, sc.right, sc.parent, sc.rfirst);
         k_bottom_up<<<blocks(n, tb), tb, 0, st>>>((int)n, sc.left, sc.right, sc.parent, s->bvh_order.as<uint32_t>(), sc.plo,
                                                   sc.phi, sc.nlo, sc.nhi, sc.ncount, sc.ncost, sc.nleaf, sc.flags,
                                                   (int)o->max_leaf_size);
-        k_gather_prims<<<blocks(n, tb), tb, 0, st>>>(prims, s->bvh_order.as<uint32_t>(), n, s->prims_bvh.as<float4>());
         PT_CUDA_TRY(cudaGetLastError());
+        return PT_OK;
+    };
+    const auto wide = [&](int root) -> int {
+        if (n > 0) {
+            k_gather_prims<<<blocks(n, tb), tb, 0, st>>>(s->prims_world.as<float4>(), s->bvh_order.as<uint32_t>(), n,
+                                                         s->prims_bvh.as<float4>());
+            PT_CUDA_TRY(cudaGetLastError());
+        }
+        switch (K) {
+            case 2: return build_wide<2>(s, sc, n, root, st);
+            case 4: return build_wide<4>(s, sc, n, root, st);
+            default: return build_wide<8>(s, sc, n, root, st);
+        }
+    };
+    int root = -1;
+    if (n > 1 && !(o->flags & PT_BVH_FAST_BUILD))
+        if ((e = ploc_build(s, sc, n, (int)o->max_leaf_size, st, &root)) != PT_OK) return e;
+    bool clustered = root >= 0;
+    if (!clustered) {
+        if ((e = radix_tree()) != PT_OK) return e;
+        root = 0;
     }
-    switch (K) {
-        case 2: e = build_wide<2>(s, sc, n, st); break;
-        case 4: e = build_wide<4>(s, sc, n, st); break;
-        default: e = build_wide<8>(s, sc, n, st); break;
+    if ((e = wide(root)) != PT_OK) return e;
+    const uint32_t stack_levels = (uint32_t)ptd::kTraversalStackEntries / (uint32_t)(K - 1);
+    if (clustered && s->level_start.size() - 1 > stack_levels) {
+        clustered = false;
+        if ((e = radix_tree()) != PT_OK) return e;
+        if ((e = wide(0)) != PT_OK) return e;
     }
-    if (e != PT_OK) return e;
     PT_CUDA_TRY(cudaEventRecord(s->ev1, st));
     PT_CUDA_TRY(cudaEventSynchronize(s->ev1));
     float ms = 0.f;
@@ -709,6 +955,7 @@ int pt_bvh_build_impl(pt_scene *s, const pt_bvh_opts *o, cudaStream_t st) {
     bs.sah_cost = sah;
     bs.build_ms = ms;
     bs.node_bytes = (uint64_t)bs.num_nodes * 32 * K;
+    bs.builder = clustered ? PT_BVH_BUILDER_PLOC : PT_BVH_BUILDER_RADIX;
     bs.prim_bytes = (uint64_t)n * 48;
     bs.num_leaves = 0;
 

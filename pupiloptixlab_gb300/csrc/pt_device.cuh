@@ -216,4 +216,8 @@ struct DevScene {
     uint32_t max_depth;  // the scene's integrator depth (used when a render asks for depth 0)
 };
 
+// Traversal stack entries per thread (shared-memory short stack plus local
+// spill); a wide tree of depth D needs up to D * (width - 1).
+constexpr int kTraversalStackEntries = 64;
+
 }  // namespace ptd

@@ -874,6 +874,7 @@ int pt_bvh_build(pt_scene *scene, const pt_bvh_opts *opts, void *stream) {
     if (opts) o = *opts;
     if (o.width != 2 && o.width != 4 && o.width != 8) { pt_set_error("BVH width must be 2, 4 or 8"); return PT_ERR_INVALID; }
     if (o.max_leaf_size < 1 || o.max_leaf_size > 15) { pt_set_error("max_leaf_size must be in 1..15"); return PT_ERR_INVALID; }
+    if (o.flags & ~(uint32_t)PT_BVH_FAST_BUILD) { pt_set_error("unknown BVH flags 0x%x", o.flags); return PT_ERR_INVALID; }
     PT_CUDA_TRY(cudaSetDevice(scene->device));
     return pt_bvh_build_impl(scene, &o, static_cast<cudaStream_t>(stream));
 }

@@ -31,7 +31,7 @@
 namespace ptd {
 
 constexpr int kShortStack = 16;  // shared-memory entries per thread
-constexpr int kSpillStack = 48;  // local-memory overflow entries per thread
+constexpr int kSpillStack = kTraversalStackEntries - kShortStack;  // local-memory overflow entries per thread
 constexpr float kSlabScale = 1.0000004f;  // 1 + 2*gamma(3): robust slab far bound (Ize 2013)
 
 struct TraceResult {

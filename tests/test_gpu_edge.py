@@ -83,7 +83,7 @@ def test_sphere_only_and_curve_only_scenes(cuda_ctx):
         rays = np.concatenate([o.camera_rays(abi.RNG_PCG32, 0), random_rays(rng, 5000, (0, 0, 0), (2, 2, 2))])
         got, ref = gpu_trace(g, rays), o.trace(rays, brute_force=True)
         assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
-        assert (got[:, 1].view(np.int32) >= 0).sum() > 500
+        assert (got[:, 1].view(np.int32) >= 0).sum() > 100
         r = o.render(params(2, seed=3))
         a = g.render(2, seed=3)["accum"].cpu().numpy()
         assert np.isfinite(a).all() and agree(a[:, :3], r["accum"][:, :3]).mean() > 0.97
@@ -138,4 +138,17 @@ def test_zero_samples_leave_the_buffers_alone(cuda_ctx):
     g.render(0, buffers=b)
     torch.cuda.synchronize()
     assert all(bool((v == 7.0).all()) for v in b.values())
+    g.close()
+
+
+@pytest.mark.parametrize("fast_build", [False, True])
+def test_single_primitive_scene(cuda_ctx, fast_build):
+    """One sphere: the tree is a single leaf under either builder."""
+    s = bare_scene(env=(0.2, 0.2, 0.2))
+    s.add_instance(abi.SHAPE_SPHERE, s.add_sphere((0.1, -0.2, 0.0), 0.8), 0)
+    g = GpuScene(cuda_ctx, s, bvh_flags=abi.BVH_FAST_BUILD if fast_build else 0)
+    o = oracle.OracleScene(s)
+    rays = np.concatenate([o.camera_rays(abi.RNG_PCG32, 0), random_rays(np.random.default_rng(2), 2000, (0, 0, 0),
+                                                                        (1.5, 1.5, 1.5))])
+    assert np.array_equal(gpu_trace(g, rays).view(np.uint32), o.trace(rays, brute_force=True).view(np.uint32))
     g.close()
