@@ -248,7 +248,9 @@ def run_reference(args):
 def run_dynamic(args):
     """800 displaced icospheres (4.1 M triangles); every frame the object-space
     vertices are the rest positions plus seeded N(0, 0.002) noise (seed = frame),
-    then either a full rebuild or a refit, then 4 spp at 1920x1080, depth 6."""
+    then a full rebuild (PLOC clustering, or the radix tree with
+    PT_BVH_FAST_BUILD) or a refit of the initial PLOC tree, then 4 spp at
+    1920x1080, depth 6."""
     import numpy as np
     import torch
 
@@ -262,15 +264,16 @@ def run_dynamic(args):
     buffers = g.alloc_buffers()
     res = {}
     sah_by_frame = {}
-    for mode in ("rebuild", "refit"):
+    for mode in ("rebuild", "rebuild_fast", "refit"):
+        fl = abi.BVH_FAST_BUILD if mode == "rebuild_fast" else 0
         g.update_all_vertices(base)
-        g.build_bvh(args.bvh_width, args.max_leaf)
+        g.build_bvh(args.bvh_width, args.max_leaf, flags=fl)
         build_ms, rays, trace_ms, render_ms, sah = [], 0, 0.0, 0.0, []
         for f in range(args.frames):
             gen = torch.Generator(device="cuda").manual_seed(f)
             jit = base + 0.002 * torch.randn(base.shape, generator=gen, device="cuda")
             g.update_all_vertices(jit)
-            st = g.build_bvh(args.bvh_width, args.max_leaf) if mode == "rebuild" else g.refit()
+            st = g.build_bvh(args.bvh_width, args.max_leaf, flags=fl) if mode != "refit" else g.refit()
             build_ms.append(st.build_ms)
             sah.append(st.sah_cost)
             g.render(4, seed=f * 4, rng=abi.RNG_PCG32, max_depth=6, buffers=buffers,
@@ -286,7 +289,8 @@ def run_dynamic(args):
     line = {"metric": "dynamic geometry: build ms, traversal Mrays/s, SAH refit/rebuild", "unit": "mixed",
             "workload": f"800 displaced icospheres ({g.num_prims()[0]} triangles), per-frame N(0, 0.002) vertex jitter, "
                         f"{args.frames} frames, 4 spp {args.width}x{args.height} depth 6, BVH{args.bvh_width}",
-            "frames": args.frames, "rebuild": res["rebuild"], "refit": res["refit"],
+            "frames": args.frames, "rebuild": res["rebuild"], "rebuild_fast": res["rebuild_fast"],
+            "refit": res["refit"],
             "sah_ratio_refit_over_rebuild": float(np.mean(sah_by_frame["refit"] / sah_by_frame["rebuild"])),
             "dtype": "f32", "data": "synthetic (seeded procedural scene)"}
     print(json.dumps(line), flush=True)

@@ -239,7 +239,10 @@ typedef struct pt_device_opts {
  * cost model from a binary tree built over Morton-sorted primitives: by
  * default PLOC (parallel locally-ordered clustering, higher quality), with
  * PT_BVH_FAST_BUILD the Karras radix tree (faster build, for per-frame
- * rebuilds).  max_leaf_size: primitives per leaf (1..15).  smem_nodes: number
+ * rebuilds); scenes whose primitives are mostly curve pieces always get the
+ * radix tree, which traces them faster.  Leaves are chosen by SAH with curve
+ * pieces weighted as three triangle tests.  max_leaf_size: primitives per
+ * leaf (1..15).  smem_nodes: number
  * of top nodes staged in shared memory by the traversal kernels (0 = none). */
 enum { PT_BVH_FAST_BUILD = 1 };
 enum { PT_BVH_BUILDER_RADIX = 0, PT_BVH_BUILDER_PLOC = 1 };

@@ -34,6 +34,13 @@ constexpr int kSortItems = 16;
 constexpr int kSortTile = kSortThreads * kSortItems;
 constexpr float kCostNode = 1.2f;
 constexpr float kCostPrim = 1.0f;
+constexpr float kCostCurvePiece = 3.0f;  // a round-cone test costs about three triangle tests
+
+// SAH intersection cost of one primitive record (triangle and sphere 1).
+__device__ __forceinline__ float prim_cost(const float4 *prims, uint32_t p) {
+    const float4 a = prims[3 * (size_t)p], b = prims[3 * (size_t)p + 1];
+    return (__float_as_int(a.w) < 0 && __float_as_int(b.w) != 0) ? kCostCurvePiece : kCostPrim;
+}
 
 __device__ __forceinline__ uint32_t f2ord(float f) {
     uint32_t u = __float_as_uint(f);
@@ -260,17 +267,19 @@ __device__ __forceinline__ float half_area(float4 lo, float4 hi) {
 
 // 5. bottom-up boxes, counts and SAH costs (second arrival processes a node).
 __global__ void k_bottom_up(int n, const int *left, const int *right, const int *parent, const uint32_t *order,
-                            const float4 *plo, const float4 *phi, float4 *nlo, float4 *nhi, int *ncount, float *ncost,
-                            int *nleaf, int *flags, int max_leaf) {
+                            const float4 *prims, const float4 *plo, const float4 *phi, float4 *nlo, float4 *nhi,
+                            int *ncount, float *ncost, float *nwt, int *nleaf, int *flags, int max_leaf) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     int leaf = n - 1 + k;
     uint32_t p = order[k];
     float4 lo = plo[p], hi = phi[p];
+    const float w = prim_cost(prims, p);
     nlo[leaf] = lo;
     nhi[leaf] = hi;
     ncount[leaf] = 1;
-    ncost[leaf] = kCostPrim * half_area(lo, hi);
+    ncost[leaf] = w * half_area(lo, hi);
+    nwt[leaf] = w;
     nleaf[leaf] = 1;
     int cur = parent[leaf];
     while (cur >= 0) {
@@ -282,13 +291,15 @@ __global__ void k_bottom_up(int n, const int *left, const int *right, const int 
         float4 blo = make_float4(fminf(llo.x, rlo.x), fminf(llo.y, rlo.y), fminf(llo.z, rlo.z), 0.f);
         float4 bhi = make_float4(fmaxf(lhi.x, rhi.x), fmaxf(lhi.y, rhi.y), fmaxf(lhi.z, rhi.z), 0.f);
         int cnt = __ldcg(&ncount[l]) + __ldcg(&ncount[r]);
+        float wsum = __ldcg(&nwt[l]) + __ldcg(&nwt[r]);
         float a = half_area(blo, bhi);
         float c_split = kCostNode * a + __ldcg(&ncost[l]) + __ldcg(&ncost[r]);
-        float c_leaf = cnt <= max_leaf ? kCostPrim * a * (float)cnt : FLT_MAX;
+        float c_leaf = cnt <= max_leaf ? a * wsum : FLT_MAX;
         bool mk_leaf = c_leaf <= c_split;
         nlo[cur] = blo;
         nhi[cur] = bhi;
         ncount[cur] = cnt;
+        nwt[cur] = wsum;
         ncost[cur] = mk_leaf ? c_leaf : c_split;
         nleaf[cur] = mk_leaf ? 1 : 0;
         cur = parent[cur];
@@ -309,17 +320,19 @@ constexpr int kPlocRadius = 16;
 constexpr int kPlocBlock = 256;
 constexpr int kPlocMaxDepth = 256;  // a deeper binary tree makes the build fall back to the radix tree
 
-__global__ void k_ploc_init(int n, const uint32_t *order, const float4 *plo, const float4 *phi, float4 *nlo,
-                            float4 *nhi, int *ncount, float *ncost, int *nleaf, int *cl) {
+__global__ void k_ploc_init(int n, const uint32_t *order, const float4 *prims, const float4 *plo, const float4 *phi,
+                            float4 *nlo, float4 *nhi, int *ncount, float *ncost, float *nwt, int *nleaf, int *cl) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     int leaf = n - 1 + k;
     uint32_t p = order[k];
     float4 lo = plo[p], hi = phi[p];
+    const float w = prim_cost(prims, p);
     nlo[leaf] = lo;
     nhi[leaf] = hi;
     ncount[leaf] = 1;
-    ncost[leaf] = kCostPrim * half_area(lo, hi);
+    ncost[leaf] = w * half_area(lo, hi);
+    nwt[leaf] = w;
     nleaf[leaf] = 1;
     cl[k] = leaf;
 }
@@ -362,7 +375,7 @@ __global__ void __launch_bounds__(kPlocBlock) k_ploc_nn(int m, const int *cl, co
 // Merge mutual pairs: keep[i] = 1 where position i survives, out_id[i] its node.
 __global__ void k_ploc_merge(int m, const int *cl, const int *nn, uint32_t *keep, int *out_id, uint32_t *node_ctr,
                              int *left, int *right, int *parent, float4 *nlo, float4 *nhi, int *ncount, float *ncost,
-                             int *nleaf, int max_leaf) {
+                             float *nwt, int *nleaf, int max_leaf) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m) return;
     const int j = nn[i];
@@ -382,9 +395,10 @@ __global__ void k_ploc_merge(int m, const int *cl, const int *nn, uint32_t *keep
     const float4 blo = make_float4(fminf(la.x, lb.x), fminf(la.y, lb.y), fminf(la.z, lb.z), 0.f);
     const float4 bhi = make_float4(fmaxf(ha.x, hb.x), fmaxf(ha.y, hb.y), fmaxf(ha.z, hb.z), 0.f);
     const int cnt = ncount[a] + ncount[b];
+    const float wsum = nwt[a] + nwt[b];
     const float area = half_area(blo, bhi);
     const float c_split = kCostNode * area + ncost[a] + ncost[b];
-    const float c_leaf = cnt <= max_leaf ? kCostPrim * area * (float)cnt : FLT_MAX;
+    const float c_leaf = cnt <= max_leaf ? area * wsum : FLT_MAX;
     const bool mk_leaf = c_leaf <= c_split;
     left[id] = a;
     right[id] = b;
@@ -393,6 +407,7 @@ __global__ void k_ploc_merge(int m, const int *cl, const int *nn, uint32_t *keep
     nlo[id] = blo;
     nhi[id] = bhi;
     ncount[id] = cnt;
+    nwt[id] = wsum;
     ncost[id] = mk_leaf ? c_leaf : c_split;
     nleaf[id] = mk_leaf ? 1 : 0;
     keep[i] = 1;
@@ -670,7 +685,7 @@ struct Scratch {
     float4 *plo, *phi;
     int *left, *right, *parent, *rfirst, *ncount, *nleaf, *flags;
     float4 *nlo, *nhi;
-    float *ncost;
+    float *ncost, *nwt;  // SAH cost and summed primitive cost weight of each binary node
     int2 *items[2];
     uint32_t *counters;  // [0..5] centroid bounds, [6] n_wide, [7] n_out0, [8] n_out1, [9] PLOC nodes, [10] PLOC failure
     double *sah;
@@ -700,6 +715,7 @@ size_t carve_size(size_t n, uint32_t tiles) {
     add(4 * n); add(4 * n); add(4 * n); add(4 * n); add(4 * 2 * n);
     add(4 * (n + 1)); add(4 * n);
     add(16 * n); add(16 * n);
+    add(4 * 2 * n);
     return t;
 }
 
@@ -787,8 +803,8 @@ int ploc_build(pt_scene *s, const Scratch &sc, uint32_t n, int max_leaf, cudaStr
     uint32_t *order = s->bvh_order.as<uint32_t>();
     PT_CUDA_TRY(cudaMemsetAsync(sc.parent, 0xff, 4 * (2 * (size_t)n - 1), st));
     PT_CUDA_TRY(cudaMemsetAsync(sc.counters + 9, 0, 2 * sizeof(uint32_t), st));
-    k_ploc_init<<<blocks(n, tb), tb, 0, st>>>((int)n, order, sc.plo, sc.phi, sc.nlo, sc.nhi, sc.ncount, sc.ncost,
-                                              sc.nleaf, sc.cl[0]);
+    k_ploc_init<<<blocks(n, tb), tb, 0, st>>>((int)n, order, s->prims_world.as<float4>(), sc.plo, sc.phi, sc.nlo,
+                                              sc.nhi, sc.ncount, sc.ncost, sc.nwt, sc.nleaf, sc.cl[0]);
     PT_CUDA_TRY(cudaGetLastError());
     uint32_t m = n;
     int cur = 0;
@@ -800,7 +816,7 @@ int ploc_build(pt_scene *s, const Scratch &sc, uint32_t n, int max_leaf, cudaStr
         k_ploc_nn<<<blocks(m, kPlocBlock), kPlocBlock, 0, st>>>((int)m, sc.cl[cur], sc.nlo, sc.nhi, sc.nn);
         k_ploc_merge<<<blocks(m, tb), tb, 0, st>>>((int)m, sc.cl[cur], sc.nn, sc.keep, sc.out_id, sc.counters + 9,
                                                    sc.left, sc.right, sc.parent, sc.nlo, sc.nhi, sc.ncount, sc.ncost,
-                                                   sc.nleaf, max_leaf);
+                                                   sc.nwt, sc.nleaf, max_leaf);
         PT_CUDA_TRY(cudaMemsetAsync(sc.keep + m, 0, sizeof(uint32_t), st));
         k_scan_excl<<<1, 1024, 0, st>>>(sc.keep, m + 1);
         k_ploc_compact<<<blocks(m, tb), tb, 0, st>>>((int)m, sc.keep, sc.out_id, sc.cl[cur ^ 1]);
@@ -873,6 +889,7 @@ int pt_bvh_build_impl(pt_scene *s, const pt_bvh_opts *o, cudaStream_t st) {
     sc.order2 = carve<uint32_t>(p, nn);
     sc.leaf_lo = carve<float4>(p, nn);
     sc.leaf_hi = carve<float4>(p, nn);
+    sc.nwt = carve<float>(p, 2 * nn);
     if ((e = s->bvh_order.ensure(std::max<size_t>(4 * (size_t)n, 16))) != PT_OK) return e;
     if ((e = s->prims_bvh.ensure(std::max<size_t>(48 * (size_t)n, 48))) != PT_OK) return e;
 
@@ -905,9 +922,9 @@ int pt_bvh_build_impl(pt_scene *s, const pt_bvh_opts *o, cudaStream_t st) {
         PT_CUDA_TRY(cudaMemsetAsync(sc.parent, 0xff, 4 * (2 * (size_t)n - 1), st));
         PT_CUDA_TRY(cudaMemsetAsync(sc.flags, 0, 4 * (size_t)n, st));
         if (n > 1) k_karras<<<blocks(n - 1, tb), tb, 0, st>>>(sc.keys[cur], (int)n, sc.left, sc.right, sc.parent, sc.rfirst);
-        k_bottom_up<<<blocks(n, tb), tb, 0, st>>>((int)n, sc.left, sc.right, sc.parent, s->bvh_order.as<uint32_t>(), sc.plo,
-                                                  sc.phi, sc.nlo, sc.nhi, sc.ncount, sc.ncost, sc.nleaf, sc.flags,
-                                                  (int)o->max_leaf_size);
+        k_bottom_up<<<blocks(n, tb), tb, 0, st>>>((int)n, sc.left, sc.right, sc.parent, s->bvh_order.as<uint32_t>(),
+                                                  s->prims_world.as<float4>(), sc.plo, sc.phi, sc.nlo, sc.nhi, sc.ncount,
+                                                  sc.ncost, sc.nwt, sc.nleaf, sc.flags, (int)o->max_leaf_size);
         PT_CUDA_TRY(cudaGetLastError());
         return PT_OK;
     };
@@ -923,8 +940,12 @@ int pt_bvh_build_impl(pt_scene *s, const pt_bvh_opts *o, cudaStream_t st) {
             default: return build_wide<8>(s, sc, n, root, st);
         }
     };
+    // curve pieces (long, thin, often diagonal) trace faster under the radix
+    // tree although PLOC gives them a lower SAH cost (50 k-strand hair at
+    // 1080p: 341 vs 320 Msamples/s), so curve-dominated scenes use it
+    const bool curve_heavy = 2ull * s->num_curve_pieces > n;
     int root = -1;
-    if (n > 1 && !(o->flags & PT_BVH_FAST_BUILD))
+    if (n > 1 && !(o->flags & PT_BVH_FAST_BUILD) && !curve_heavy)
         if ((e = ploc_build(s, sc, n, (int)o->max_leaf_size, st, &root)) != PT_OK) return e;
     bool clustered = root >= 0;
     if (!clustered) {
