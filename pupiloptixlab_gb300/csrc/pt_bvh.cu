@@ -414,11 +414,45 @@ __global__ void k_ploc_merge(int m, const int *cl, const int *nn, uint32_t *keep
     out_id[i] = id;
 }
 
-// keep holds the exclusive prefix sums of the survival flags (m + 1 entries).
-__global__ void k_ploc_compact(int m, const uint32_t *pre, const int *out_id, int *cl_next) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= m) return;
-    if (pre[i + 1] != pre[i]) cl_next[pre[i]] = out_id[i];
+// Order-preserving compaction of the surviving positions in blocks of
+// kCompactBlock: survivors per block (warp ballots), an exclusive scan of the
+// block counts, then each survivor's rank = block offset + warp offset + its
+// rank among the warp's survivors.
+constexpr int kCompactBlock = 1024;
+
+__global__ void __launch_bounds__(kCompactBlock) k_ploc_block_counts(int m, const uint32_t *keep, uint32_t *bsum) {
+    __shared__ uint32_t wc[kCompactBlock / 32];
+    const int i = blockIdx.x * kCompactBlock + threadIdx.x;
+    const unsigned b = __ballot_sync(0xffffffffu, i < m && keep[i] != 0);
+    if ((threadIdx.x & 31) == 0) wc[threadIdx.x >> 5] = __popc(b);
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        uint32_t v = wc[threadIdx.x];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (threadIdx.x == 0) bsum[blockIdx.x] = v;
+    }
+}
+
+__global__ void __launch_bounds__(kCompactBlock) k_ploc_compact(int m, const uint32_t *keep, const uint32_t *boff,
+                                                                const int *out_id, int *cl_next) {
+    __shared__ uint32_t woff[kCompactBlock / 32];
+    const int i = blockIdx.x * kCompactBlock + threadIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const bool k = i < m && keep[i] != 0;
+    const unsigned b = __ballot_sync(0xffffffffu, k);
+    if (lane == 0) woff[warp] = __popc(b);
+    __syncthreads();
+    if (warp == 0) {  // exclusive scan of the per-warp counts
+        const uint32_t v = woff[lane];
+        uint32_t x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        woff[lane] = x - v;
+    }
+    __syncthreads();
+    if (k) cl_next[boff[blockIdx.x] + woff[warp] + __popc(b & ((1u << lane) - 1u))] = out_id[i];
 }
 
 // Depth-first position of every node (leftmost leaf of its subtree): the sum
@@ -690,7 +724,7 @@ struct Scratch {
     uint32_t *counters;  // [0..5] centroid bounds, [6] n_wide, [7] n_out0, [8] n_out1, [9] PLOC nodes, [10] PLOC failure
     double *sah;
     int *cl[2], *nn, *out_id, *offs;  // PLOC clusters, neighbours, merge results, depth-first positions
-    uint32_t *keep, *order2;
+    uint32_t *keep, *order2, *bsum;  // survival flags, permuted order, per-block survivor counts
     float4 *leaf_lo, *leaf_hi;
 };
 
@@ -716,6 +750,7 @@ size_t carve_size(size_t n, uint32_t tiles) {
     add(4 * (n + 1)); add(4 * n);
     add(16 * n); add(16 * n);
     add(4 * 2 * n);
+    add(4 * (n / 1024 + 2));
     return t;
 }
 
@@ -817,12 +852,14 @@ int ploc_build(pt_scene *s, const Scratch &sc, uint32_t n, int max_leaf, cudaStr
         k_ploc_merge<<<blocks(m, tb), tb, 0, st>>>((int)m, sc.cl[cur], sc.nn, sc.keep, sc.out_id, sc.counters + 9,
                                                    sc.left, sc.right, sc.parent, sc.nlo, sc.nhi, sc.ncount, sc.ncost,
                                                    sc.nwt, sc.nleaf, max_leaf);
-        PT_CUDA_TRY(cudaMemsetAsync(sc.keep + m, 0, sizeof(uint32_t), st));
-        k_scan_excl<<<1, 1024, 0, st>>>(sc.keep, m + 1);
-        k_ploc_compact<<<blocks(m, tb), tb, 0, st>>>((int)m, sc.keep, sc.out_id, sc.cl[cur ^ 1]);
+        const uint32_t nb = (m + kCompactBlock - 1) / kCompactBlock;
+        k_ploc_block_counts<<<nb, kCompactBlock, 0, st>>>((int)m, sc.keep, sc.bsum);
+        PT_CUDA_TRY(cudaMemsetAsync(sc.bsum + nb, 0, sizeof(uint32_t), st));
+        k_scan_excl<<<1, 1024, 0, st>>>(sc.bsum, nb + 1);
+        k_ploc_compact<<<nb, kCompactBlock, 0, st>>>((int)m, sc.keep, sc.bsum, sc.out_id, sc.cl[cur ^ 1]);
         PT_CUDA_TRY(cudaGetLastError());
         uint32_t next = 0;
-        PT_CUDA_TRY(cudaMemcpyAsync(&next, sc.keep + m, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        PT_CUDA_TRY(cudaMemcpyAsync(&next, sc.bsum + nb, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
         PT_CUDA_TRY(cudaStreamSynchronize(st));
         if (next == 0 || next >= m) return PT_OK;  // cannot happen (the closest pair always merges)
         m = next;
@@ -890,6 +927,7 @@ int pt_bvh_build_impl(pt_scene *s, const pt_bvh_opts *o, cudaStream_t st) {
     sc.leaf_lo = carve<float4>(p, nn);
     sc.leaf_hi = carve<float4>(p, nn);
     sc.nwt = carve<float>(p, 2 * nn);
+    sc.bsum = carve<uint32_t>(p, nn / 1024 + 2);
     if ((e = s->bvh_order.ensure(std::max<size_t>(4 * (size_t)n, 16))) != PT_OK) return e;
     if ((e = s->prims_bvh.ensure(std::max<size_t>(48 * (size_t)n, 48))) != PT_OK) return e;
 
