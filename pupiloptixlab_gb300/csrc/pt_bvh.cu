@@ -8,13 +8,14 @@
 //   3. stable LSD radix sort of (code, primitive) pairs, 8 passes of 8 bits:
 //      tile histogram -> one-block exclusive scan -> warp-multisplit scatter
 //      (__match_any_sync ranks, per-warp digit counts in shared memory)
-//   4. Karras (HPG 2012) binary radix tree, equal codes split by index
+//   4. binary tree: PLOC clustering (default) or the Karras (HPG 2012)
+//      binary radix tree, equal codes split by index
 //   5. bottom-up boxes with an SAH cost per node (leaf vs split decision,
 //      leaves of at most max_leaf_size primitives)
-//   6. top-down, level-synchronous collapse into 2/4/8-wide nodes: each wide
-//      node repeatedly opens its child with the largest surface area until it
-//      has `width` children (SAH-driven collapse); children that the cost model
-//      made leaves become leaf slots.  Nodes come out in breadth-first order.
+//   6. SAH-optimal assignment of the binary subtrees to the slots of 2/4/8-wide
+//      nodes (dynamic programming, bottom up), then a top-down,
+//      level-synchronous collapse that follows it; nodes come out in
+//      breadth-first order.
 //   7. primitive records gathered into leaf order
 // Child boxes are padded outward (relative to the box and scene magnitude) so
 // that the conservative slab test never rejects a primitive the exact test
@@ -477,8 +478,8 @@ __global__ void k_ploc_offsets(int n, const int *left, const int *right, const i
 // Renumber leaves to their depth-first positions (leaf at position q is node
 // n-1+q), record every internal node's first position, permute the order.
 __global__ void k_ploc_finish(int n, const int *offs, const uint32_t *order, const float4 *nlo, const float4 *nhi,
-                              int *left, int *right, int *rfirst, uint32_t *order_out, float4 *leaf_lo,
-                              float4 *leaf_hi) {
+                              const int *parent, int *left, int *right, int *rfirst, uint32_t *order_out,
+                              float4 *leaf_lo, float4 *leaf_hi, int *parent_out) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     if (x >= 2 * n - 1) return;
     if (x >= n - 1) {
@@ -486,7 +487,9 @@ __global__ void k_ploc_finish(int n, const int *offs, const uint32_t *order, con
         order_out[q] = order[x - (n - 1)];
         leaf_lo[q] = nlo[x];
         leaf_hi[q] = nhi[x];
+        parent_out[n - 1 + q] = parent[x];
     } else {
+        parent_out[x] = parent[x];
         rfirst[x] = offs[x];
         const int l = left[x], r = right[x];
         left[x] = l >= n - 1 ? n - 1 + offs[l] : l;
@@ -518,53 +521,135 @@ __device__ __forceinline__ void write_empty(float *node, int c) {
     write_slot<K>(node, c, f3(1e30f, 1e30f, 1e30f), f3(1e30f, 1e30f, 1e30f), -1, 0);
 }
 
-// 6. one level of the wide collapse.  item = (wide node index, binary node).
+// 6. SAH-optimal wide collapse (Ylitie, Karras and Laine, HPG 2017): for
+// every binary node x and i = 1..K, S(x, i) is the cheapest way to represent
+// its subtree with at most i slots of a wide parent:
+//   S(x, 1) = min(leaf: area * primitive weight (if count <= max_leaf),
+//                 wide node: 1.2 * area + min_j S(l, j) + S(r, K - j))
+//   S(x, i) = min(S(x, i - 1), min_j S(l, j) + S(r, i - j))
+// computed bottom up (second arrival processes a node).  dsel[8x] keeps the
+// wide node's split j, dsel[8x + i - 1] the split for i = 2..K slots (0: use
+// i - 1 slots), and nleaf[x] the leaf-or-wide choice; the collapse below
+// follows them.
 template <int K>
-__global__ void k_collapse(int n, const int2 *items_in, const uint32_t *n_in_ptr, int2 *items_out, uint32_t *n_out,
-                           uint32_t *n_wide, float *nodes, const int *left, const int *right, const int *rfirst,
-                           const float4 *nlo, const float4 *nhi, const int *ncount, const int *nleaf, float scene_mag) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= *n_in_ptr) return;
-    int2 it = items_in[i];
-    int ch[K];
-    int cnt = 2;
-    ch[0] = left[it.y];
-    ch[1] = right[it.y];
-    for (int c = 2; c < K; c++) ch[c] = -1;
-    while (cnt < K) {
-        int best = -1;
-        float best_a = -1.f;
-        for (int c = 0; c < cnt; c++) {
-            int b = ch[c];
-            if (b >= n - 1 || nleaf[b]) continue;  // binary leaf or leaf by cost
-            float a = half_area(nlo[b], nhi[b]);
-            if (a > best_a) {
-                best_a = a;
+__global__ void k_wide_dp(int n, const int *left, const int *right, const int *parent, const float4 *nlo,
+                          const float4 *nhi, const int *ncount, const float *nwt, float *dval, uint8_t *dsel,
+                          int *nleaf, int *flags, int max_leaf) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int leaf = n - 1 + k;
+    const float v = half_area(nlo[leaf], nhi[leaf]) * nwt[leaf];
+#pragma unroll
+    for (int i = 0; i < K; i++) dval[(size_t)leaf * 8 + i] = v;
+    int cur = parent[leaf];
+    while (cur >= 0) {
+        __threadfence();
+        if (atomicAdd(&flags[cur], 1) == 0) return;
+        __threadfence();
+        const int l = left[cur], r = right[cur];
+        float sl[K + 1], sr[K + 1], sx[K + 1];
+#pragma unroll
+        for (int i = 1; i <= K; i++) {
+            sl[i] = __ldcg(&dval[(size_t)l * 8 + i - 1]);
+            sr[i] = __ldcg(&dval[(size_t)r * 8 + i - 1]);
+        }
+        const float area = half_area(nlo[cur], nhi[cur]);
+        float best = FLT_MAX;
+        int jw = 1;
+#pragma unroll
+        for (int j = 1; j < K; j++) {
+            const float c = sl[j] + sr[K - j];
+            if (c < best) {
                 best = c;
+                jw = j;
             }
         }
-        if (best < 0) break;
-        int b = ch[best];
-        ch[best] = left[b];
-        ch[cnt++] = right[b];
+        const float c_wide = kCostNode * area + best;
+        const float c_leaf = ncount[cur] <= max_leaf ? area * nwt[cur] : FLT_MAX;
+        const bool mk_leaf = c_leaf <= c_wide;
+        sx[1] = mk_leaf ? c_leaf : c_wide;
+        dsel[(size_t)cur * 8] = (uint8_t)jw;
+#pragma unroll
+        for (int i = 2; i <= K; i++) {
+            float vi = sx[i - 1];
+            int sel = 0;
+#pragma unroll
+            for (int j = 1; j < i; j++) {
+                const float c = sl[j] + sr[i - j];
+                if (c < vi) {
+                    vi = c;
+                    sel = j;
+                }
+            }
+            sx[i] = vi;
+            dsel[(size_t)cur * 8 + i - 1] = (uint8_t)sel;
+        }
+#pragma unroll
+        for (int i = 1; i <= K; i++) dval[(size_t)cur * 8 + i - 1] = sx[i];
+        nleaf[cur] = mk_leaf ? 1 : 0;
+        cur = parent[cur];
+    }
+}
+
+// 6'. one level of the collapse, following the choices of k_wide_dp: the
+// wide node of binary node b gets the slots of left(b) (dsel[8b] of them) and
+// right(b) (the rest), each expanded while its choice splits it further.
+template <int K>
+__global__ void k_collapse_dp(int n, const int2 *items_in, const uint32_t *n_in_ptr, int2 *items_out, uint32_t *n_out,
+                              uint32_t *n_wide, float *nodes, const int *left, const int *right, const int *rfirst,
+                              const float4 *nlo, const float4 *nhi, const int *ncount, const int *nleaf,
+                              const uint8_t *dsel, float scene_mag) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= *n_in_ptr) return;
+    const int2 it = items_in[t];
+    const int b = it.y;
+    int slot[K];
+    int ns = 0;
+    int stn[K], sti[K];  // pending (node, slots); their slots sum to at most K
+    int sp = 0;
+    const int jw = dsel[(size_t)b * 8];
+    stn[sp] = right[b];
+    sti[sp++] = K - jw;
+    stn[sp] = left[b];
+    sti[sp++] = jw;
+    while (sp > 0) {
+        --sp;
+        const int x = stn[sp];
+        int si = sti[sp];
+        if (x < n - 1) {
+            while (si > 1 && dsel[(size_t)x * 8 + si - 1] == 0) si--;
+        }
+        if (x >= n - 1 || si <= 1) {
+            if (ns < K) slot[ns++] = x;
+            continue;
+        }
+        const int sel = dsel[(size_t)x * 8 + si - 1];
+        if (sp + 2 > K) {  // cannot happen (slots on the stack sum to at most K)
+            if (ns < K) slot[ns++] = x;
+            continue;
+        }
+        stn[sp] = right[x];
+        sti[sp++] = si - sel;
+        stn[sp] = left[x];
+        sti[sp++] = sel;
     }
     float *node = nodes + (size_t)it.x * 8 * K;
     for (int c = 0; c < K; c++) {
-        if (c >= cnt) {
+        if (c >= ns) {
             write_empty<K>(node, c);
             continue;
         }
-        int b = ch[c];
+        const int x = slot[c];
         float3 lo, hi;
-        padded(nlo[b], nhi[b], scene_mag, lo, hi);
-        if (b >= n - 1) {
-            write_slot<K>(node, c, lo, hi, b - (n - 1), 1);
-        } else if (nleaf[b]) {
-            write_slot<K>(node, c, lo, hi, rfirst[b], ncount[b]);
+        padded(nlo[x], nhi[x], scene_mag, lo, hi);
+        if (x >= n - 1) {
+            write_slot<K>(node, c, lo, hi, x - (n - 1), 1);
+        } else if (nleaf[x]) {
+            write_slot<K>(node, c, lo, hi, rfirst[x], ncount[x]);
         } else {
-            uint32_t w = atomicAdd(n_wide, 1u);
-            uint32_t q = atomicAdd(n_out, 1u);
-            items_out[q] = make_int2((int)w, b);
+            const uint32_t w = atomicAdd(n_wide, 1u);
+            const uint32_t q = atomicAdd(n_out, 1u);
+            items_out[q] = make_int2((int)w, x);
             write_slot<K>(node, c, lo, hi, (int)w, 0);
         }
     }
@@ -725,6 +810,9 @@ struct Scratch {
     double *sah;
     int *cl[2], *nn, *out_id, *offs;  // PLOC clusters, neighbours, merge results, depth-first positions
     uint32_t *keep, *order2, *bsum;  // survival flags, permuted order, per-block survivor counts
+    int *par2;                       // parents renumbered with the leaves
+    float *dval;                     // wide-collapse costs S(x, 1..8)
+    uint8_t *dsel;                   // wide-collapse choices
     float4 *leaf_lo, *leaf_hi;
 };
 
@@ -751,17 +839,24 @@ size_t carve_size(size_t n, uint32_t tiles) {
     add(16 * n); add(16 * n);
     add(4 * 2 * n);
     add(4 * (n / 1024 + 2));
+    add(4 * 2 * n); add(4 * 8 * 2 * n); add(8 * 2 * n);
     return t;
 }
 
 template <int K>
-int build_wide(pt_scene *s, const Scratch &sc, uint32_t n, int root, cudaStream_t st) {
+int build_wide(pt_scene *s, const Scratch &sc, uint32_t n, int root, int max_leaf, cudaStream_t st) {
     s->level_start.clear();
     size_t node_bytes = (size_t)std::max<uint32_t>(1, n > 1 ? n - 1 : 1) * 32 * K;
     int e = s->nodes.ensure(node_bytes);
     if (e != PT_OK) return e;
     float *nodes = s->nodes.as<float>();
     const int tb = 256;
+    if (n > 1) {  // SAH-optimal slot assignment for this width (also the final leaf decisions)
+        PT_CUDA_TRY(cudaMemsetAsync(sc.flags, 0, 4 * (size_t)n, st));
+        k_wide_dp<K><<<blocks(n, tb), tb, 0, st>>>((int)n, sc.left, sc.right, sc.parent, sc.nlo, sc.nhi, sc.ncount,
+                                                   sc.nwt, sc.dval, sc.dsel, sc.nleaf, sc.flags, max_leaf);
+        PT_CUDA_TRY(cudaGetLastError());
+    }
     // root: binary node `root` (internal), or the single leaf (node 0 when n == 1)
     int root_leaf = 0;
     if (n > 1) PT_CUDA_TRY(cudaMemcpyAsync(&root_leaf, sc.nleaf + root, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -781,9 +876,10 @@ int build_wide(pt_scene *s, const Scratch &sc, uint32_t n, int root, cudaStream_
         s->level_start.push_back(start);
         uint32_t *n_in = sc.counters + 7 + cur, *n_out = sc.counters + 7 + (cur ^ 1);
         PT_CUDA_TRY(cudaMemsetAsync(n_out, 0, sizeof(uint32_t), st));
-        k_collapse<K><<<blocks(level_count, tb), tb, 0, st>>>((int)n, sc.items[cur], n_in, sc.items[cur ^ 1], n_out,
-                                                             sc.counters + 6, nodes, sc.left, sc.right, sc.rfirst,
-                                                             sc.nlo, sc.nhi, sc.ncount, sc.nleaf, s->scene_mag);
+        k_collapse_dp<K><<<blocks(level_count, tb), tb, 0, st>>>((int)n, sc.items[cur], n_in, sc.items[cur ^ 1], n_out,
+                                                                sc.counters + 6, nodes, sc.left, sc.right, sc.rfirst,
+                                                                sc.nlo, sc.nhi, sc.ncount, sc.nleaf, sc.dsel,
+                                                                s->scene_mag);
         PT_CUDA_TRY(cudaGetLastError());
         uint32_t nxt = 0;
         PT_CUDA_TRY(cudaMemcpyAsync(&nxt, n_out, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
@@ -868,9 +964,10 @@ int ploc_build(pt_scene *s, const Scratch &sc, uint32_t n, int max_leaf, cudaStr
     const uint32_t nodes2 = 2 * n - 1;
     k_ploc_offsets<<<blocks(nodes2, tb), tb, 0, st>>>((int)n, sc.left, sc.right, sc.parent, sc.ncount, sc.offs,
                                                      sc.counters + 10);
-    k_ploc_finish<<<blocks(nodes2, tb), tb, 0, st>>>((int)n, sc.offs, order, sc.nlo, sc.nhi, sc.left, sc.right,
-                                                    sc.rfirst, sc.order2, sc.leaf_lo, sc.leaf_hi);
+    k_ploc_finish<<<blocks(nodes2, tb), tb, 0, st>>>((int)n, sc.offs, order, sc.nlo, sc.nhi, sc.parent, sc.left,
+                                                    sc.right, sc.rfirst, sc.order2, sc.leaf_lo, sc.leaf_hi, sc.par2);
     PT_CUDA_TRY(cudaGetLastError());
+    PT_CUDA_TRY(cudaMemcpyAsync(sc.parent, sc.par2, 4 * (size_t)nodes2, cudaMemcpyDeviceToDevice, st));
     PT_CUDA_TRY(cudaMemcpyAsync(order, sc.order2, 4 * (size_t)n, cudaMemcpyDeviceToDevice, st));
     PT_CUDA_TRY(cudaMemcpyAsync(sc.nlo + (n - 1), sc.leaf_lo, 16 * (size_t)n, cudaMemcpyDeviceToDevice, st));
     PT_CUDA_TRY(cudaMemcpyAsync(sc.nhi + (n - 1), sc.leaf_hi, 16 * (size_t)n, cudaMemcpyDeviceToDevice, st));
@@ -928,6 +1025,9 @@ int pt_bvh_build_impl(pt_scene *s, const pt_bvh_opts *o, cudaStream_t st) {
     sc.leaf_hi = carve<float4>(p, nn);
     sc.nwt = carve<float>(p, 2 * nn);
     sc.bsum = carve<uint32_t>(p, nn / 1024 + 2);
+    sc.par2 = carve<int>(p, 2 * nn);
+    sc.dval = carve<float>(p, 8 * 2 * nn);
+    sc.dsel = carve<uint8_t>(p, 8 * 2 * nn);
     if ((e = s->bvh_order.ensure(std::max<size_t>(4 * (size_t)n, 16))) != PT_OK) return e;
     if ((e = s->prims_bvh.ensure(std::max<size_t>(48 * (size_t)n, 48))) != PT_OK) return e;
 
@@ -973,9 +1073,9 @@ int pt_bvh_build_impl(pt_scene *s, const pt_bvh_opts *o, cudaStream_t st) {
             PT_CUDA_TRY(cudaGetLastError());
         }
         switch (K) {
-            case 2: return build_wide<2>(s, sc, n, root, st);
-            case 4: return build_wide<4>(s, sc, n, root, st);
-            default: return build_wide<8>(s, sc, n, root, st);
+            case 2: return build_wide<2>(s, sc, n, root, (int)o->max_leaf_size, st);
+            case 4: return build_wide<4>(s, sc, n, root, (int)o->max_leaf_size, st);
+            default: return build_wide<8>(s, sc, n, root, (int)o->max_leaf_size, st);
         }
     };
     // curve pieces (long, thin, often diagonal) trace faster under the radix
