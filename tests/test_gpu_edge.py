@@ -152,3 +152,24 @@ def test_single_primitive_scene(cuda_ctx, fast_build):
                                                                         (1.5, 1.5, 1.5))])
     assert np.array_equal(gpu_trace(g, rays).view(np.uint32), o.trace(rays, brute_force=True).view(np.uint32))
     g.close()
+
+
+def test_coincident_primitives(cuda_ctx):
+    """3,000 copies of one triangle next to a few ordinary ones: clustering
+    finds one mutual pair per pass among equal boxes, so the build must fall
+    back to the radix tree within its pass limit; hits stay exact (equal t
+    breaks to the lowest primitive id on both sides)."""
+    rng = np.random.default_rng(12)
+    tri = np.array([[-0.5, -0.5, 0.0], [0.5, -0.5, 0.0], [0.0, 0.5, 0.0]], np.float32)
+    extra = rng.uniform(-1.5, 1.5, (30, 3)).astype(np.float32)
+    pos = np.concatenate([np.tile(tri, (3000, 1)), extra])
+    idx = np.concatenate([np.arange(9000).reshape(-1, 3), 9000 + rng.integers(0, 30, (10, 3))])
+    s = bare_scene(env=(0.5, 0.5, 0.5))
+    s.add_instance(abi.SHAPE_MESH, s.add_mesh(scenes.Mesh(pos, idx.astype(np.uint32))), 0)
+    g, o = GpuScene(cuda_ctx, s), oracle.OracleScene(s)
+    assert g.bvh_stats().builder == abi.BVH_BUILDER_RADIX
+    rays = np.concatenate([o.camera_rays(abi.RNG_PCG32, 0), random_rays(rng, 3000, (0, 0, 0), (1.0, 1.0, 1.0))])
+    got, ref = gpu_trace(g, rays), o.trace(rays, brute_force=True)
+    assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
+    assert (got[:, 1].view(np.int32) == 0).sum() > 50  # the lowest id of the stack of copies
+    g.close()
