@@ -241,11 +241,15 @@ __device__ __forceinline__ void fwd_epilogue(const FwdArgs &a, uint32_t tmem, in
 // byte offset = plane size between the two 8-channel groups, stride byte
 // offset = 128 B between 8-row groups), so the input is read from L2 once per
 // chunk instead of once per tap.  B holds the chunk's weights for all nine
-// taps (32-byte swizzle, one TMA box per tap).
+// taps (32-byte swizzle, one TMA box per tap).  When one channel tile covers
+// every output channel and all (chunk, tap) weight boxes fit in
+// kMaxResidentWeights bytes, they are loaded once per CTA ahead of the ring
+// (on their own barrier) and the stages carry only the two A planes.
 constexpr int kHaloW = 130, kHaloRows = 3;
 constexpr int kHaloBoxBytes = kHaloW * kHaloRows * 16;       // one 8-channel plane as TMA writes it
 constexpr int kHaloPlaneBytes = (kHaloBoxBytes + 1023) / 1024 * 1024;  // plane stride: TMA destinations 1 KiB-aligned
 __host__ __device__ constexpr int halo_b_tap_bytes(int n_tile) { return (n_tile * 32 + 1023) / 1024 * 1024; }
+constexpr int kMaxResidentWeights = 64 * 1024;
 
 // ---------------------------------------------------------------------------
 // persistent forward / data-gradient kernel
@@ -265,12 +269,14 @@ __global__ void __launch_bounds__(192, 1)
     constexpr int R = KC * 2;
     constexpr uint32_t SWZ = swz_mode<KC>();
     extern __shared__ uint8_t smem_raw[];
-    __shared__ __align__(8) uint64_t bars[2 * kMaxStages + 4];
+    __shared__ __align__(8) uint64_t bars[2 * kMaxStages + 5];
     __shared__ uint32_t tmem_slot;
     __shared__ int s_fail;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
+    const bool wres = HALO && a.wres_bytes > 0;  // weights resident ahead of the ring
+    const uint32_t wbase = (smem_u32(smem_raw) + 1023u) & ~1023u;
+    const uint32_t base = wbase + (wres ? static_cast<uint32_t>(a.wres_bytes) : 0u);
     const int S = a.stages;
     const int tiles_img = a.tiles_x * a.tiles_y;
     const int n_n = a.n_tiles_n;
@@ -278,13 +284,14 @@ __global__ void __launch_bounds__(192, 1)
     const int nk = HALO ? a.nchunks : 9 * a.nchunks;  // stages per tile
     const int a_bytes = HALO ? a.halo_a_bytes : 128 * R;
     const int b_tap = HALO ? halo_b_tap_bytes(a.n_tile) : 0;
-    const uint32_t tx_bytes = HALO ? static_cast<uint32_t>(2 * kHaloBoxBytes + 9 * a.n_tile * R)
+    const uint32_t tx_bytes = HALO ? static_cast<uint32_t>(2 * kHaloBoxBytes + (wres ? 0 : 9 * a.n_tile * R))
                                    : static_cast<uint32_t>(a.tile_w * a.tile_rows * R + a.n_tile * R);
     const uint32_t bar0 = smem_u32(bars);
     auto full = [&](int s) { return bar0 + 8u * s; };
     auto empty = [&](int s) { return bar0 + 8u * (kMaxStages + s); };
     auto acc_full = [&](int b) { return bar0 + 8u * (2 * kMaxStages + b); };
     auto acc_empty = [&](int b) { return bar0 + 8u * (2 * kMaxStages + 2 + b); };
+    const uint32_t wbar = bar0 + 8u * (2 * kMaxStages + 4);  // resident weights landed
     auto tile_of = [&](int t, int &img, int &x0, int &y0, int &n0) {
         const int pt = t / n_n;
         n0 = (t - pt * n_n) * a.n_tile;
@@ -304,6 +311,7 @@ __global__ void __launch_bounds__(192, 1)
             mbar_init(acc_full(b), 1);
             mbar_init(acc_empty(b), 128);
         }
+        mbar_init(wbar, 1);
         mbar_fence_init();
         s_fail = 0;
     }
@@ -315,6 +323,13 @@ __global__ void __launch_bounds__(192, 1)
 
     if (warp == 0) {
         if (lane == 0) {  // producer
+            if (wres) {  // every (chunk, tap) weight box once: b_tap apart, chunk-major
+                mbar_expect_tx(wbar, static_cast<uint32_t>(a.nchunks * 9 * a.n_tile * R));
+                for (int k = 0; k < a.nchunks; k++)
+                    for (int tap = 0; tap < 9; tap++)
+                        tma_load_2d(wbase + static_cast<uint32_t>((k * 9 + tap) * b_tap), &wgt, wbar,
+                                    tap * a.cin + k * 16, 0);
+            }
             int kg = 0;  // stages issued so far (ring position and phase)
             for (int t = blockIdx.x; t < total && !*fail; t += gridDim.x) {
                 int img, x0, y0, n0;
@@ -331,8 +346,9 @@ __global__ void __launch_bounds__(192, 1)
                     if (HALO) {
                         tma_load_4d(sa, &act, full(s), k * 16, x0 - 1, y0 - 1, img);
                         tma_load_4d(sa + kHaloPlaneBytes, &act, full(s), k * 16 + 8, x0 - 1, y0 - 1, img);
-                        for (int tap = 0; tap < 9; tap++)
-                            tma_load_2d(sb + tap * b_tap, &wgt, full(s), tap * a.cin + k * 16, n0);
+                        if (!wres)
+                            for (int tap = 0; tap < 9; tap++)
+                                tma_load_2d(sb + tap * b_tap, &wgt, full(s), tap * a.cin + k * 16, n0);
                     } else {
                         const int tap = k / a.nchunks, ch = k - tap * a.nchunks;
                         const int dy = tap / 3, dx = tap - dy * 3;
@@ -341,13 +357,19 @@ __global__ void __launch_bounds__(192, 1)
                     }
                 }
             }
-            // drain: wait until every issued stage has been consumed
+            // drain: wait until every issued stage has been consumed and the
+            // resident weights (if any) have landed
             for (int k = kg - S; k < kg; k++)
                 if (k >= 0) (void)mbar_wait(empty(k % S), (k / S) & 1, true);
+            if (wres) (void)mbar_wait(wbar, 0, true);
         }
     } else if (warp == 1) {
         if (lane == 0) {  // MMA issuer
             const uint32_t idesc = idesc_bf16(128, a.n_tile, false, false);
+            if (wres && !mbar_wait(wbar, 0)) {
+                record_error(a.err, 2u);
+                *fail = 1;
+            }
             int kg = 0, j = 0;
             for (int t = blockIdx.x; t < total && !*fail; t += gridDim.x, j++) {
                 const int buf = j & 1;
@@ -366,7 +388,8 @@ __global__ void __launch_bounds__(192, 1)
                         break;
                     }
                     tc_fence_after();
-                    const uint32_t sa = base + s * a.stage_bytes, sb = sa + a_bytes;
+                    const uint32_t sa = base + s * a.stage_bytes;
+                    const uint32_t sb = wres ? wbase + static_cast<uint32_t>(k * 9 * b_tap) : sa + a_bytes;
                     if (HALO) {
 #pragma unroll
                         for (int tap = 0; tap < 9; tap++) {
@@ -773,10 +796,13 @@ int fwd_prepare(FwdOp *op, const Act &in, const void *w, int w_rows, int cout, c
     a.n_tiles_n = ntiles;
     a.tmem_cols = pow2_cols(2 * n_tile);  // two accumulators
     a.halo_a_bytes = 2 * kHaloPlaneBytes;
-    a.stage_bytes = halo ? a.halo_a_bytes + 9 * halo_b_tap_bytes(n_tile)
+    const int wres_bytes = a.nchunks * 9 * halo_b_tap_bytes(n_tile);
+    a.wres_bytes = (halo && ntiles == 1 && wres_bytes <= kMaxResidentWeights && !getenv_flag("PT_CONV_NO_RESIDENT"))
+                       ? wres_bytes : 0;
+    a.stage_bytes = halo ? a.halo_a_bytes + (a.wres_bytes ? 0 : 9 * halo_b_tap_bytes(n_tile))
                          : (128 * 2 * kc + n_tile * 2 * kc + 1023) / 1024 * 1024;
     const int target_ctas = std::min(512 / a.tmem_cols, 2);
-    const int budget = (225 * 1024) / target_ctas - 2048;
+    const int budget = (225 * 1024) / target_ctas - 2048 - a.wres_bytes;
     a.stages = std::max(2, std::min(kMaxStages, budget / a.stage_bytes));
     if (halo) {
         a.tile_w = 128;
@@ -798,7 +824,7 @@ int fwd_prepare(FwdOp *op, const Act &in, const void *w, int w_rows, int cout, c
     a.err = err;
     op->kc = kc;
     op->halo = halo;
-    op->smem = smem_request(a.stages, a.stage_bytes, a.tmem_cols);
+    op->smem = smem_request(a.stages, a.stage_bytes, a.tmem_cols) + a.wres_bytes;
     const long long total = (long long)in.n * a.tiles_x * a.tiles_y * ntiles;
     const int per_sm = std::max(1, std::min((228 * 1024) / (op->smem + 1024), 512 / a.tmem_cols));
     op->grid = dim3(static_cast<unsigned>(std::min<long long>(total, (long long)per_sm * sm_count())), 1, 1);

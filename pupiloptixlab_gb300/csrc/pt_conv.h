@@ -40,6 +40,7 @@ struct FwdArgs {
     int n_tile, cout;     // N per CTA; valid output channels
     int tmem_cols, stages, stage_bytes;
     int halo_a_bytes;     // halo kernel: bytes of the A planes at the start of a stage
+    int wres_bytes;       // halo kernel: > 0 = all weights resident in shared memory (loaded once per CTA)
     int n_tiles_n;        // output-channel tiles (persistent kernel: tile = pixel tile x channel tile)
     int epi, relu;
     const float *bias;
