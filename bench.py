@@ -68,6 +68,8 @@ def parse():
     ap.add_argument("--dn-crop", type=int, default=256)
     ap.add_argument("--dn-lr", type=float, default=1e-3)
     ap.add_argument("--dn-ref-spp", type=int, default=4096, help="spp of the 1080p reference image")
+    ap.add_argument("--dn-single-pass", action="store_true",
+                    help="denoise with one network pass instead of the frame + mirror-image ensemble")
     ap.add_argument("--dn-train-only", action="store_true",
                     help="time denoiser training steps on a seeded random batch (no rendering, no evaluation)")
     ap.add_argument("--width", type=int, default=1920)
@@ -473,10 +475,11 @@ def run_denoise(args):
         b, t = timed_render(spp, 0)
         plain.append({"spp": spp, "s": t, "rmse": rmse(b["accum"])})
     den = []
-    for spp in (1, 2, 4, 8, 16, 32, 48, 64, 96, 128):
+    ensemble = not args.dn_single_pass
+    for spp in (1, 2, 4, 8, 16, 32, 48, 64, 80, 96, 112, 128):
         b, t = timed_render(spp, 0)
-        dn.denoise(b, W, H)  # warm
-        out, st, _ = dn.denoise(b, W, H)
+        dn.denoise(b, W, H, ensemble=ensemble)  # warm
+        out, st, _ = dn.denoise(b, W, H, ensemble=ensemble)
         den.append({"spp": spp, "s": t + st.last_ms * 1e-3, "render_s": t, "denoise_ms": st.last_ms,
                     "rmse": rmse(out), "rmse_input": rmse(b["accum"]), "fallback_tiles": st.fallback_tiles,
                     "tiles": st.tiles})
@@ -521,7 +524,8 @@ def run_denoise(args):
                                  "pooling, up-sampling, loss, Adam) over its algorithmic convolution FLOPs; "
                                  "peak = sustained cuBLAS bf16"},
             "workload": f"U-Net 5 levels 32-256 ch, {dn.num_params} params, batch {B} x {args.dn_crop}^2; "
-                        f"eval on the {W}x{H} icosphere field",
+                        f"eval on the {W}x{H} icosphere field, "
+                        f"{'frame + mirror-image ensemble' if ensemble else 'one network pass'} per denoise",
             "dtype": "bf16 (fp32 accumulate)", "data": "synthetic (rendered by the tracer from seeded scenes)"}
     print(json.dumps(line), flush=True)
 

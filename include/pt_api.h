@@ -475,7 +475,12 @@ typedef struct pt_denoise_io {
     float fallback_rel;   /* fall back to the raw colour where a tile's mean luminance moved by more */
     float fallback_sigma; /* than max(fallback_rel * mean, fallback_sigma * standard error); <= 0: no fallback */
     uint8_t *tile_fallback; /* device, optional: one byte per tile, 1 = raw colour kept */
+    uint32_t flags;       /* PT_DENOISE_* */
 } pt_denoise_io;
+/* PT_DENOISE_FLIP_ENSEMBLE: run the network on the frame and on its
+ * left-right mirror image and average the two outputs (mirrored back) before
+ * the output step: one more network pass per frame for a lower error. */
+enum { PT_DENOISE_FLIP_ENSEMBLE = 1 };
 
 typedef struct pt_denoise_stats {
     uint32_t tiles;          /* tiles of the last pt_denoise */

@@ -138,7 +138,10 @@ class DenoiserOpts(C.Structure):
 class DenoiseIO(C.Structure):
     _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("color", C.c_void_p), ("albedo", C.c_void_p),
                 ("normal", C.c_void_p), ("output", C.c_void_p), ("tile", C.c_uint32), ("fallback_rel", C.c_float),
-                ("fallback_sigma", C.c_float), ("tile_fallback", C.c_void_p)]
+                ("fallback_sigma", C.c_float), ("tile_fallback", C.c_void_p), ("flags", C.c_uint32)]
+
+
+DENOISE_FLIP_ENSEMBLE = 1
 
 
 class DenoiseStats(C.Structure):

@@ -302,6 +302,32 @@ __device__ __forceinline__ float3 denoised(const float *o, const uint16_t *x0, l
                        fmaxf(expm1f(o[q * 3 + 2] + bf2f(x0[q * 16 + 2])), 0.f));
 }
 
+// Left-right mirror of every row of the 16-channel network input, in place
+// (pixel x <-> wp - 1 - x, 32 bytes each).
+__global__ void k_mirror_x0(uint16_t *x0, int wp, int hp) {
+    const long long half = (long long)(wp / 2) * hp;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < half; i += (long long)gridDim.x * blockDim.x) {
+        const long long y = i / (wp / 2), x = i - y * (wp / 2);
+        uint4 *a = reinterpret_cast<uint4 *>(x0 + (y * wp + x) * 16);
+        uint4 *b = reinterpret_cast<uint4 *>(x0 + (y * wp + (wp - 1 - x)) * 16);
+        const uint4 a0 = a[0], a1 = a[1], b0 = b[0], b1 = b[1];
+        a[0] = b0;
+        a[1] = b1;
+        b[0] = a0;
+        b[1] = a1;
+    }
+}
+
+// acc = (acc + mirror(o)) / 2 for the 3-channel network output.
+__global__ void k_mirror_average(float *acc, const float *o, int wp, long long npix) {
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < npix; q += (long long)gridDim.x * blockDim.x) {
+        const long long y = q / wp, x = q - y * wp;
+        const long long m = y * wp + (wp - 1 - x);
+#pragma unroll
+        for (int c = 0; c < 3; c++) acc[q * 3 + c] = 0.5f * (acc[q * 3 + c] + o[m * 3 + c]);
+    }
+}
+
 // One block per tile: mean luminance of the raw and the denoised colour and
 // the raw colour's standard error; write the tile's pixels, falling back to
 // the raw colour where the denoised mean moved by more than the threshold.
@@ -377,6 +403,7 @@ struct Plan {
     DevBuf g_out, g_d0, g_cat0, g_d1, g_cat1, g_d2, g_cat2, g_d3, g_cat3, g_b4, g_p3, g_e3b, g_a3, g_p2, g_e2b, g_a2,
         g_p1, g_e1b, g_a1, g_p0, g_e0b, g_a0;
     DevBuf in_stage, tgt_stage;
+    DevBuf out_acc;  // inference: network output averaged over the frame and its mirror image
     ptconv::FwdOp fwd[kLayers], bwd[kLayers];
     ptconv::WgradOp wg[kLayers];
     Act x_of[kLayers], g_of[kLayers];
@@ -387,7 +414,7 @@ struct Plan {
                          &a3,    &cat3,  &p3,     &b4,    &d3,    &d2,     &d1,    &d0,    &out,   &g_out,
                          &g_d0,  &g_cat0, &g_d1,  &g_cat1, &g_d2, &g_cat2, &g_d3,  &g_cat3, &g_b4, &g_p3,
                          &g_e3b, &g_a3,  &g_p2,   &g_e2b, &g_a2,  &g_p1,   &g_e1b, &g_a1,  &g_p0,  &g_e0b,
-                         &g_a0,  &in_stage, &tgt_stage};
+                         &g_a0,  &in_stage, &tgt_stage, &out_acc};
         for (DevBuf *b : all) b->release();
         if (graph) cudaGraphExecDestroy(graph);
         graph = nullptr;
@@ -975,6 +1002,10 @@ int pt_denoise(pt_denoiser *dn, const pt_denoise_io *io, void *stream) {
         pt_set_error("pt_denoise: NULL argument or empty frame");
         return PT_ERR_INVALID;
     }
+    if (io->flags & ~(uint32_t)PT_DENOISE_FLIP_ENSEMBLE) {
+        pt_set_error("pt_denoise: unknown flags 0x%x", io->flags);
+        return PT_ERR_INVALID;
+    }
     cudaStream_t caller = static_cast<cudaStream_t>(stream);
     PT_TRY(enter(dn, caller));
     const int w = io->width, h = io->height;
@@ -986,10 +1017,22 @@ int pt_denoise(pt_denoiser *dn, const pt_denoise_io *io, void *stream) {
     const int tiles = ((w + tile - 1) / tile) * ((h + tile - 1) / tile);
     PT_CUDA_TRY(cudaMemsetAsync(dn->fallback.ptr, 0, 4, s));
     PT_CUDA_TRY(cudaEventRecord(dn->t0, s));
+    const bool ensemble = (io->flags & PT_DENOISE_FLIP_ENSEMBLE) != 0;
+    const long long npix = (long long)wp * hp;
+    if (ensemble) PT_TRY(P.out_acc.ensure(npix * 3 * sizeof(float)));
     k_pack_frame<<<grid_for((long long)wp * hp), 256, 0, s>>>(reinterpret_cast<const float4 *>(io->color), io->albedo,
                                                                io->normal, w, h, wp, hp, P.x0.as<uint16_t>());
     PT_TRY(run_forward(dn, P, s));
-    k_denoise_out<<<tiles, 256, 0, s>>>(reinterpret_cast<const float4 *>(io->color), P.out.as<float>(),
+    const float *o = P.out.as<float>();
+    if (ensemble) {  // second pass on the mirror image, averaged in the network's output (log residual) space
+        PT_CUDA_TRY(cudaMemcpyAsync(P.out_acc.ptr, P.out.ptr, npix * 3 * sizeof(float), cudaMemcpyDeviceToDevice, s));
+        k_mirror_x0<<<grid_for(npix / 2), 256, 0, s>>>(P.x0.as<uint16_t>(), wp, hp);
+        PT_TRY(run_forward(dn, P, s));
+        k_mirror_average<<<grid_for(npix), 256, 0, s>>>(P.out_acc.as<float>(), P.out.as<float>(), wp, npix);
+        k_mirror_x0<<<grid_for(npix / 2), 256, 0, s>>>(P.x0.as<uint16_t>(), wp, hp);
+        o = P.out_acc.as<float>();
+    }
+    k_denoise_out<<<tiles, 256, 0, s>>>(reinterpret_cast<const float4 *>(io->color), o,
                                         P.x0.as<uint16_t>(), w, h, wp, tile,
                                         io->fallback_rel, io->fallback_sigma, reinterpret_cast<float4 *>(io->output),
                                         io->tile_fallback, dn->fallback.as<unsigned>());

@@ -154,15 +154,17 @@ class Denoiser:
         return out
 
     def denoise(self, buffers: dict, width: int, height: int, tile: int = 16, fallback_rel: float = 0.25,
-                fallback_sigma: float = 4.0, want_tiles: bool = False):
-        """Denoise a rendered frame; returns (output (h*w, 4) f32, stats, tile flags or None)."""
+                fallback_sigma: float = 4.0, want_tiles: bool = False, ensemble: bool = False):
+        """Denoise a rendered frame; returns (output (h*w, 4) f32, stats, tile flags or None).
+        ensemble = True averages the network over the frame and its mirror image."""
         dev = buffers["accum"].device
         out = torch.empty(width * height, 4, device=dev, dtype=torch.float32)
         tiles = ((width + tile - 1) // tile) * ((height + tile - 1) // tile)
         flags = torch.zeros(tiles, dtype=torch.uint8, device=dev) if want_tiles else None
         io = abi.DenoiseIO(width, height, buffers["accum"].data_ptr(), buffers["albedo"].data_ptr(),
                            buffers["normal"].data_ptr(), out.data_ptr(), tile, fallback_rel, fallback_sigma,
-                           flags.data_ptr() if flags is not None else None)
+                           flags.data_ptr() if flags is not None else None,
+                           abi.DENOISE_FLIP_ENSEMBLE if ensemble else 0)
         abi.check(self.lib.pt_denoise(self.handle, C.byref(io), _stream_ptr()), "pt_denoise", self.lib)
         st = abi.DenoiseStats()
         abi.check(self.lib.pt_denoise_get_stats(self.handle, C.byref(st)), "pt_denoise_get_stats", self.lib)

@@ -146,3 +146,23 @@ def test_denoise_frame_and_fallback(cuda_ctx, dn):
     fb = flags2.view(3, 5).repeat_interleave(16, 0).repeat_interleave(16, 1)[:40, :72].reshape(-1).bool()
     assert torch.equal(out2[fb, :3], buf["accum"][fb, :3])
     g.close()
+
+
+def test_flip_ensemble_is_mirror_consistent(cuda_ctx, dn):
+    """PT_DENOISE_FLIP_ENSEMBLE averages the network over the frame and its
+    mirror image, so denoising the mirrored frame gives exactly the mirrored
+    result (width and height multiples of 16, no tile fallback); the result
+    differs from a single pass and stays finite."""
+    from pupiloptixlab_gb300 import scenes
+    from pupiloptixlab_gb300.api import GpuScene
+    w, h = 64, 32
+    g = GpuScene(cuda_ctx, scenes.cornell_box(w, h))
+    buf = g.render(spp=4)
+    mir = {k: v.view(h, w, -1).flip(1).reshape(h * w, -1).contiguous() for k, v in buf.items() if v.dim() == 2}
+    e1, _, _ = dn.denoise(buf, w, h, fallback_sigma=0.0, ensemble=True)
+    e2, _, _ = dn.denoise(mir, w, h, fallback_sigma=0.0, ensemble=True)
+    single, _, _ = dn.denoise(buf, w, h, fallback_sigma=0.0)
+    assert torch.isfinite(e1).all()
+    assert torch.equal(e1, e2.view(h, w, 4).flip(1).reshape(h * w, 4))
+    assert not torch.equal(e1, single)
+    g.close()
