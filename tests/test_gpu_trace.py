@@ -82,6 +82,27 @@ def test_leaf_sizes(cuda_ctx, max_leaf):
     assert_hits_equal(gpu_trace(g, rays), o.trace(rays, brute_force=True))
 
 
+@pytest.mark.parametrize("width", [2, 4, 8])
+@pytest.mark.parametrize("fast_build", [False, True])
+def test_both_tree_builders(cuda_ctx, width, fast_build):
+    """PLOC clustering and the radix tree (PT_BVH_FAST_BUILD) give the same
+    hits for every width; the stats name the builder that ran."""
+    sc = scenes.icosphere_field(48, 32, num_instances=20, subdivisions=3, seed=5)
+    o = oracle.OracleScene(sc, bvh=False)
+    g = GpuScene(cuda_ctx, sc, bvh_width=width, bvh_flags=abi.BVH_FAST_BUILD if fast_build else 0)
+    st = g.bvh_stats()
+    if fast_build:
+        assert st.builder == abi.BVH_BUILDER_RADIX
+    elif width < 8:  # a PLOC BVH8 deeper than the stack covers falls back to the radix tree
+        assert st.builder == abi.BVH_BUILDER_PLOC
+    rng = np.random.default_rng(width + 10 * fast_build)
+    rays = np.concatenate([o.camera_rays(abi.RNG_PCG32, 0), rays_inside(rng, 10000, (0, 1, 0), (8, 2, 5))])
+    assert_hits_equal(gpu_trace(g, rays), o.trace(rays, brute_force=True))
+    rays[:, 7] = rng.uniform(0.05, 6.0, rays.shape[0])
+    assert np.array_equal(gpu_trace(g, rays, anyhit=True)[:, 0], o.trace(rays, anyhit=True, brute_force=True)[:, 0])
+    g.close()
+
+
 def test_full_size_scene_primary_rays(cuda_ctx):
     """Icosphere-field geometry (1,032,192 triangles + 4 spheres) at 1920x1080:
     every 16th primary ray against the oracle's BVH2 (itself equal to brute
