@@ -678,6 +678,9 @@ def main():
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else
                      "fallback 6.8 TB/s",
                      "algorithmic_bytes_per_ray": ext_bytes / max(1, cst.extension_rays),
+                     "dram_bytes_per_ray": (traffic["dram_bytes_per_launch"] * launches_per_step
+                                            / max(1, cst.extension_rays)) if traffic else None,
+                     "l2_hit_rate_pct": traffic.get("lts_sector_hit_rate_pct") if traffic else None,
                      "nodes_per_ray": cst.nodes_visited / max(1, cst.extension_rays),
                      "prims_per_ray": cst.prims_tested / max(1, cst.extension_rays),
                      "extend_ms_per_step": ext_ms / args.steps, "shadow_ms_per_step": sh_ms / args.steps,
