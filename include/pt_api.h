@@ -417,8 +417,8 @@ int pt_render_batch_get_stats(const pt_context *ctx, pt_render_stats *out);
 /* No reference counterpart (the reference has a single OptiX configuration).
  * Times `params` renders on this scene (coordinate search): every
  * combination of BVH width {2, 4, 8} (the BVH is rebuilt) and traversal block
- * size {64, 128, 256} at the default wave size, then wave sizes {4Mi, 16Mi,
- * 64Mi paths} with the best pair.  The BVH is rebuilt with the winning width
+ * size {64, 128, 256} at the default wave size (128 Mi paths), then wave
+ * sizes {16Mi, 32Mi, 64Mi paths} with the best pair.  The BVH is rebuilt with the winning width
  * and its block size and wave size become the scene's defaults (used when
  * pt_render_params.block_size / wave_spp are 0).  fb receives the tuning
  * renders.  Use the spp of the renders to be tuned for: the best wave size

@@ -30,8 +30,9 @@
 namespace {
 using namespace ptd;
 
-// Paths in flight per wave unless autotuned: 32 Mi slots (about 4.6 GiB of path state).
-constexpr uint32_t kDefaultWavePaths = 32u << 20;
+// Paths in flight per wave unless autotuned: 128 Mi slots (about 20 GB of path
+// state; 64 frames of 1080p in one wave: fewer, fuller launches per bounce).
+constexpr uint32_t kDefaultWavePaths = 128u << 20;
 
 enum Counter : int {
     kNIn = 0,
@@ -1242,7 +1243,7 @@ int pt_autotune_impl(pt_scene *s, const pt_render_params *params, const pt_frame
     r.baseline_msamples_per_s = base_ms > 0.f ? (float)((double)npix * spp / (base_ms * 1e-3) / 1e6) : 0.f;
     float best_ms = 1e30f;
     uint32_t best_w = opts.width, best_b = 128, best_wave = default_wave;
-    const uint32_t widths[3] = {2, 4, 8}, blocks[3] = {64, 128, 256}, waves[3] = {4u << 20, 16u << 20, 64u << 20};
+    const uint32_t widths[3] = {2, 4, 8}, blocks[3] = {64, 128, 256}, waves[3] = {16u << 20, 32u << 20, 64u << 20};
     for (uint32_t wd : widths) {
         opts.width = wd;
         if ((e = pt_bvh_build_impl(s, &opts, st)) != PT_OK) return e;

@@ -137,7 +137,7 @@ def test_autotune_picks_a_configuration_and_keeps_the_image(cuda_ctx):
     before = gpu_render(g, 4, seed=1)["accum"]
     r = g.autotune(spp=2)
     assert r.bvh_width in (2, 4, 8) and r.block_size in (64, 128, 256)
-    assert r.wave_paths in (4 << 20, 16 << 20, 32 << 20, 64 << 20)
+    assert r.wave_paths in (16 << 20, 32 << 20, 64 << 20, 128 << 20)
     assert r.trials >= 10 and r.msamples_per_s > 0
     assert g.bvh_stats().width == r.bvh_width
     after = gpu_render(g, 4, seed=1)["accum"]
