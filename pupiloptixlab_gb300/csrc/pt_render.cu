@@ -213,8 +213,8 @@ struct ExtendSrc {  // closest hit of the active queue (entries are path slots)
     PT_DI int root(uint32_t) const { return 0; }
     PT_DI uint32_t count() const { return st.counters[kNIn]; }
     PT_DI void load(uint32_t i, float3 &o, float3 &d, float &tmin, float &tmax, uint32_t &tag) const {
-        uint32_t slot = st.q_in[i];
-        float4 o4 = st.ray_o[slot], d4 = st.ray_d[slot];
+        uint32_t slot = ld_stream(st.q_in + i);
+        float4 o4 = ld_stream(st.ray_o + slot), d4 = ld_stream(st.ray_d + slot);
         o = xyz(o4);
         d = xyz(d4);
         tmin = o4.w;
@@ -222,7 +222,7 @@ struct ExtendSrc {  // closest hit of the active queue (entries are path slots)
         tag = slot;
     }
     PT_DI void store(uint32_t, uint32_t slot, const TraceResult &r) const {
-        st.hit[slot] = make_float4(r.t, __int_as_float(r.prim), r.u, r.v);
+        st_stream(st.hit + slot, make_float4(r.t, __int_as_float(r.prim), r.u, r.v));
     }
 };
 struct ShadowSrc {  // any hit of the shadow queue; unoccluded rays add their NEE radiance
@@ -230,7 +230,7 @@ struct ShadowSrc {  // any hit of the shadow queue; unoccluded rays add their NE
     PT_DI int root(uint32_t) const { return 0; }
     PT_DI uint32_t count() const { return st.counters[kNShadow]; }
     PT_DI void load(uint32_t i, float3 &o, float3 &d, float &tmin, float &tmax, uint32_t &tag) const {
-        float4 o4 = st.sh_o[i], d4 = st.sh_d[i];
+        float4 o4 = ld_stream(st.sh_o + i), d4 = ld_stream(st.sh_d + i);
         o = xyz(o4);
         d = xyz(d4);
         tmin = o4.w;
@@ -239,7 +239,7 @@ struct ShadowSrc {  // any hit of the shadow queue; unoccluded rays add their NE
     }
     PT_DI void store(uint32_t i, uint32_t, const TraceResult &r) const {
         if (r.prim >= 0) return;
-        float4 c = st.sh_c[i];
+        float4 c = ld_stream(st.sh_c + i);
         uint32_t ps = __float_as_uint(c.w);
         float4 rr = st.rad[ps];
         st.rad[ps] = make_float4(rr.x + c.x, rr.y + c.y, rr.z + c.z, rr.w);
