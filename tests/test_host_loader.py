@@ -389,3 +389,27 @@ def test_hair_shape(host, tmp_path):
     with pytest.raises(abi.PtError) as e:
         host.XmlScene(str(tmp_path / "h2.xml"))
     assert "not a HAIR file" in str(e.value)
+
+
+def _hair_header(strands, points, flags, default_segments=0):
+    import struct
+    return struct.pack("<4sIIIIff3f", b"HAIR", strands, points, flags, default_segments, 0.01, 1.0, 0.5, 0.5,
+                       0.5) + bytes(88)
+
+
+@pytest.mark.parametrize("body, needle", [
+    (b"HAIR" + bytes(60), "truncated HAIR header"),
+    (_hair_header(3, 12, 3) + bytes(4), "truncated segment array"),
+    (_hair_header(2, 8, 1) + np.array([3, 3], "<u2").tobytes(), "has no points"),
+    (_hair_header(2, 6, 3) + np.array([3, 3], "<u2").tobytes() + bytes(72), "need more points"),
+    (_hair_header(2, 8, 3) + np.array([3, 3], "<u2").tobytes() + bytes(40), "truncated point array"),
+    (_hair_header(1, 4, 6, default_segments=3) + bytes(48) + bytes(8), "truncated thickness array"),
+])
+def test_malformed_hair_files_are_reported(host, tmp_path, body, needle):
+    """A HAIR file cut short anywhere, or with strands that need more points
+    than it holds, is refused with a message naming the part that is wrong."""
+    (tmp_path / "x.hair").write_bytes(body)
+    (tmp_path / "x.xml").write_text("<scene><shape type='hair'><string name='filename' value='x.hair'/></shape></scene>")
+    with pytest.raises(abi.PtError) as e:
+        host.XmlScene(str(tmp_path / "x.xml"))
+    assert needle in str(e.value)
