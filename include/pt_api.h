@@ -345,7 +345,11 @@ int pt_last_error(char *buf, size_t buf_size);
 int pt_api_version(void);
 
 /* ---- scene ------------------------------------------------------------ */
-/* The library copies everything it needs; the descriptor can be freed after. */
+/* The library copies everything it needs; the descriptor can be freed after.
+ * A scene holds at most PT_MAX_PRIMITIVES primitives after instancing
+ * (triangles + spheres + the round-cone pieces of its curves); a larger one
+ * is refused with PT_ERR_UNSUPPORTED before any device memory is allocated. */
+#define PT_MAX_PRIMITIVES 134217727u /* 2^27 - 1 */
 int pt_scene_upload(pt_context *ctx, const pt_scene_desc *desc, pt_scene **out);
 int pt_scene_destroy(pt_scene *scene);
 int pt_scene_set_camera(pt_scene *scene, const pt_camera_desc *camera);

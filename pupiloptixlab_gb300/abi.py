@@ -14,6 +14,8 @@ c_float_p = C.POINTER(C.c_float)
 c_uint_p = C.POINTER(C.c_uint32)
 
 PT_OK = 0
+PT_ERR_UNSUPPORTED = 6
+MAX_PRIMITIVES = (1 << 27) - 1  # PT_MAX_PRIMITIVES: per scene after instancing, and per multi-scene launch
 STATUS_NAMES = {0: "PT_OK", 1: "PT_ERR_INVALID", 2: "PT_ERR_CUDA", 3: "PT_ERR_OOM", 4: "PT_ERR_TIMEOUT",
                 5: "PT_ERR_NAN", 6: "PT_ERR_UNSUPPORTED", 7: "PT_ERR_OOB", 8: "PT_ERR_STATE"}
 

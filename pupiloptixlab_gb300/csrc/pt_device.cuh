@@ -220,4 +220,9 @@ struct DevScene {
 // spill); a wide tree of depth D needs up to D * (width - 1).
 constexpr int kTraversalStackEntries = 64;
 
+// Primitives per BVH (one scene, or the merged scenes of a batch): a leaf on
+// the traversal stack packs its first primitive slot into 27 bits.
+constexpr uint32_t kMaxPrimitives = PT_MAX_PRIMITIVES;
+static_assert(kMaxPrimitives == (1u << 27) - 1, "leaf items hold 27-bit primitive slots");
+
 }  // namespace ptd

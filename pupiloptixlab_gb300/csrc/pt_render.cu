@@ -1124,7 +1124,7 @@ int render_batch(pt_context *ctx, pt_scene *const *scenes, const pt_render_param
         pt_set_error("pt_render_batch: at most %d scenes per call", 1024 / kNumBins);
         return PT_ERR_INVALID;
     }
-    if (total_prims >= (1u << 27) || total_nodes >= (1u << 31) || total_pix >= (1ull << 31)) {
+    if (total_prims > ptd::kMaxPrimitives || total_nodes >= (1u << 31) || total_pix >= (1ull << 31)) {
         pt_set_error("pt_render_batch: batch too large (%llu primitives, %llu pixels)",
                      (unsigned long long)total_prims, (unsigned long long)total_pix);
         return PT_ERR_INVALID;

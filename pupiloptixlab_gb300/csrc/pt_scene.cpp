@@ -245,6 +245,20 @@ int validate(const pt_scene_desc *d) {
         for (int k = 0; k < 16; k++)
             if (!std::isfinite(in.to_world[k])) { pt_set_error("instance %u: non-finite transform", i); return PT_ERR_INVALID; }
     }
+    // primitives after instancing; curve segments count once here (each gets
+    // at least one piece when visible), their pieces are counted as they are made
+    uint64_t nprim = 0;
+    for (uint32_t i = 0; i < d->num_instances; i++) {
+        const pt_instance_desc &in = d->instances[i];
+        nprim += in.shape_type == PT_SHAPE_MESH     ? d->meshes[in.shape_index].num_triangles
+                 : in.shape_type == PT_SHAPE_SPHERE ? 1u
+                                                    : 0u;
+    }
+    if (nprim > ptd::kMaxPrimitives) {
+        pt_set_error("scene has %llu primitives after instancing; at most %u are supported", (unsigned long long)nprim,
+                     ptd::kMaxPrimitives);
+        return PT_ERR_UNSUPPORTED;
+    }
     if (d->env.type != PT_ENV_NONE && d->env.type != PT_ENV_CONST && d->env.type != PT_ENV_MAP) {
         pt_set_error("environment type %u not supported", d->env.type);
         return PT_ERR_UNSUPPORTED;
@@ -451,6 +465,10 @@ int build_scene(pt_scene *s, const pt_scene_desc *d) {
             const bool strand_last = i + 1 == cv.num_segments || cv.segments[i + 1] != first + 1;
             const ptd::CurveSeg sg = ptd::curve_segment(cv.type, q);
             const uint32_t np = ptd::curve_piece_count(sg, rmax);
+            if ((uint64_t)ntri + nsph + npiece + np > ptd::kMaxPrimitives) {
+                pt_set_error("scene has more than %u primitives (curve pieces included)", ptd::kMaxPrimitives);
+                return PT_ERR_UNSUPPORTED;
+            }
             for (uint32_t k = 0; k < np; k++) {
                 const float u0 = (float)k / (float)np, u1 = (float)(k + 1) / (float)np;
                 const float4 p0 = ptd::curve_pos(sg, u0), p1 = ptd::curve_pos(sg, u1);

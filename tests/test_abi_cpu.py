@@ -60,6 +60,17 @@ def test_ctypes_layouts_match_header(tmp_path):
         assert C.sizeof(MIRROR[s]) == sizes[s], s
 
 
+def test_header_constants_match_the_mirror(tmp_path):
+    src = tmp_path / "consts.c"
+    src.write_text('#include <stdio.h>\n#include "pt_api.h"\n'
+                   'int main(void) { printf("%u %d\\n", PT_MAX_PRIMITIVES, PT_ERR_UNSUPPORTED); return 0; }\n')
+    exe = tmp_path / "consts"
+    subprocess.run(["gcc", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
+    assert int(out[0]) == abi.MAX_PRIMITIVES == (1 << 27) - 1
+    assert int(out[1]) == abi.PT_ERR_UNSUPPORTED
+
+
 def test_camera_make_matches_oracle(ptlib):
     import oracle
     from pupiloptixlab_gb300 import scenes

@@ -173,3 +173,24 @@ def test_coincident_primitives(cuda_ctx):
     assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
     assert (got[:, 1].view(np.int32) == 0).sum() > 50  # the lowest id of the stack of copies
     g.close()
+
+
+def test_too_many_primitives_are_refused(cuda_ctx):
+    """Instances that add up to more than 2^27 - 1 primitives (the leaf items
+    on the traversal stack hold 27-bit primitive slots) are refused with
+    PT_ERR_UNSUPPORTED before anything is allocated on the device; the same
+    mesh under fewer instances uploads."""
+    n = 1 << 20
+    rng = np.random.default_rng(3)
+    tris = rng.uniform(-1, 1, (n, 1, 3)) + rng.uniform(-0.01, 0.01, (n, 3, 3))
+    s = bare_scene()
+    m = s.add_mesh(scenes.Mesh(tris.reshape(-1, 3).astype(np.float32), np.arange(3 * n, dtype=np.uint32).reshape(n, 3)))
+    for _ in range(abi.MAX_PRIMITIVES // n + 1):
+        s.add_instance(abi.SHAPE_MESH, m, 0)
+    with pytest.raises(abi.PtError) as e:
+        GpuScene(cuda_ctx, s)
+    assert e.value.status == abi.PT_ERR_UNSUPPORTED and str(abi.MAX_PRIMITIVES) in str(e.value)
+    s.instances = s.instances[:2]
+    g = GpuScene(cuda_ctx, s)
+    assert g.bvh_stats().num_nodes > 0
+    g.close()
