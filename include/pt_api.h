@@ -220,7 +220,7 @@ typedef struct pt_scene_desc {
     uint32_t num_instances;
     pt_env_desc env;
     pt_camera_desc camera;
-    uint32_t width;     /* film size (resource::Film) */
+    uint32_t width;     /* film size (resource::Film); width x height < 2^31 */
     uint32_t height;
     uint32_t max_depth; /* integrator max_depth (resource::Integrator) */
     const pt_curves_desc *curves;
@@ -277,7 +277,7 @@ typedef struct pt_render_params {
     uint32_t sample_cnt;  /* sample_cnt of the first frame */
     uint32_t accumulate;  /* accumulated_flag */
     uint32_t rng;         /* pt_rng_mode */
-    uint32_t wave_spp;    /* frames per wavefront wave (0 = auto) */
+    uint32_t wave_spp;    /* frames per wavefront wave (0 = auto; frames x pixels < 2^31) */
     uint32_t block_size;  /* threads per block of the wavefront kernels (0 = auto) */
     uint32_t flags;       /* PT_RENDER_* */
 } pt_render_params;

@@ -822,6 +822,11 @@ struct Launcher {
         if (frames_per_wave == 0) frames_per_wave = std::max<uint32_t>(1, (uint32_t)(wave_paths / std::max<uint32_t>(npix, 1)));
         frames_per_wave = std::max<uint32_t>(1, std::min(frames_per_wave, std::max<uint32_t>(p->spp, 1)));
         const size_t cap = (size_t)frames_per_wave * npix;
+        if (cap > 0x7fffffffu) {  // path slots are 32-bit indices
+            pt_set_error("a wave of %u frames x %u pixels exceeds 2^31 - 1 path slots; lower wave_spp",
+                         frames_per_wave, npix);
+            return PT_ERR_INVALID;
+        }
         if (ws.capacity < cap) {
             int e;
             if ((e = ws.ray_o.ensure(16 * cap)) || (e = ws.ray_d.ensure(16 * cap)) || (e = ws.hit.ensure(16 * cap)) ||

@@ -168,6 +168,10 @@ int validate(const pt_scene_desc *d) {
         return PT_ERR_INVALID;
     }
     if (d->width == 0 || d->height == 0) { pt_set_error("film size must be non-zero"); return PT_ERR_INVALID; }
+    if ((uint64_t)d->width * d->height > 0x7fffffffu) {  // path slots and pixel indices are 32-bit
+        pt_set_error("film of %u x %u pixels: at most 2^31 - 1 pixels are supported", d->width, d->height);
+        return PT_ERR_UNSUPPORTED;
+    }
     for (uint32_t i = 0; i < d->num_materials; i++) {
         const pt_material_desc &m = d->materials[i];
         if (m.type < PT_MAT_DIFFUSE || m.type > PT_MAT_ROUGH_PLASTIC) {

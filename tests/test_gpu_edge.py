@@ -194,3 +194,22 @@ def test_too_many_primitives_are_refused(cuda_ctx):
     g = GpuScene(cuda_ctx, s)
     assert g.bvh_stats().num_nodes > 0
     g.close()
+
+
+def test_oversized_films_and_waves_are_refused(cuda_ctx):
+    """Path slots and pixel indices are 32-bit: a film of 2^31 pixels or more
+    is refused at upload, a wave of 2^31 path slots or more (frames x pixels)
+    at render time, both before any device allocation."""
+    s = bare_scene(env=(0.5, 0.5, 0.5))
+    s.width, s.height = 65536, 32768
+    with pytest.raises(abi.PtError) as e:
+        GpuScene(cuda_ctx, s)
+    assert e.value.status == abi.PT_ERR_UNSUPPORTED and "2^31" in str(e.value)
+    g = GpuScene(cuda_ctx, bare_scene(64, 64, env=(0.5, 0.5, 0.5)))
+    frames = (1 << 31) // (64 * 64)
+    with pytest.raises(abi.PtError) as e:
+        g.render(frames, wave_spp=frames)
+    assert "2^31 - 1 path slots" in str(e.value)
+    out = g.render(4, wave_spp=2)["accum"].cpu().numpy()
+    assert np.allclose(out[:, :3], 0.5)
+    g.close()
