@@ -39,12 +39,21 @@ from pathlib import Path
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-WORKLOAD = "1M-triangle displaced-icosphere field (200 x 5120 tris + 8192 ground tris + 4 sphere lights), " \
-           "1920x1080, 64 spp, max depth 8, NEE+MIS, 7 materials"
+WORKLOAD = "{m:.0f}M-triangle displaced-icosphere field ({n} x 5120 tris + 8192 ground tris + 4 sphere lights), " \
+           "{w}x{h}, {spp} spp, max depth {d}, NEE+MIS, 7 materials"
 METRIC = "Msamples/s at 1080p depth 8 (1 GB300)"
 HAIR_WORKLOAD = "{n} strands x 16 points (curve type {t}, radius 0.003) on a head sphere + floor + sphere light, " \
-                "1920x1080, 64 spp, max depth 8, NEE+MIS"
+                "{w}x{h}, {spp} spp, max depth {d}, NEE+MIS"
+# Options that shape the closest-hit launches: the committed DRAM-traffic
+# capture of a workload applies only when these keep their defaults.
+CAPTURE_KEYS = ("width", "height", "spp", "depth", "instances", "hair_strands", "hair_type", "bvh_width", "max_leaf",
+                "bvh_fast_build", "smem_nodes", "block_size", "wave_spp", "no_material_sort", "autotune")
 HAIR_METRIC = "Msamples/s at 1080p depth 8, hair (1 GB300)"
+
+
+def headline_workload(args) -> str:
+    return WORKLOAD.format(m=(args.instances * 5120 + 8192) / 1e6, n=args.instances, w=args.width, h=args.height,
+                           spp=args.spp, d=args.depth)
 
 
 def parse():
@@ -90,7 +99,9 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    return ap.parse_args()
+    args = ap.parse_args()
+    args.at_capture_config = all(getattr(args, k) == ap.get_default(k) for k in CAPTURE_KEYS)
+    return args
 
 
 def replica_throughput(local_ms: float, units_per_rank: float, ws: int, device: str = "cuda"):
@@ -239,7 +250,7 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Msamples/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_t / len(times) * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "implementation": "CPU restatement of the reference integrator "
+            "config": {"workload": headline_workload(args), "implementation": "CPU restatement of the reference integrator "
                        "(oracle/pt_oracle.cpp: reference BSDF/emitter/RNG math, host binned-SAH BVH2); the "
                        "reference's OptiX 7.5 / DX12 build is unavailable on this box"},
             "cpu_baseline": {"value": value, "unit": "Msamples/s", "cores": threads, "kind": "port", "sample": sample},
@@ -564,10 +575,11 @@ def main():
     if args.workload == "hair":
         sc = scenes.hair_scene(args.width, args.height, curve_type=args.hair_type, num_strands=args.hair_strands,
                                points=16, radius=0.003, max_depth=args.depth, curl=0.08)
-        metric, workload = HAIR_METRIC, HAIR_WORKLOAD.format(n=args.hair_strands, t=args.hair_type)
+        metric, workload = HAIR_METRIC, HAIR_WORKLOAD.format(n=args.hair_strands, t=args.hair_type, w=args.width,
+                                                             h=args.height, spp=args.spp, d=args.depth)
     else:
         sc = scenes.icosphere_field(args.width, args.height, args.depth, args.instances)
-        metric, workload = METRIC, WORKLOAD
+        metric, workload = METRIC, headline_workload(args)
     ctx = Context(local)
     g = GpuScene(ctx, sc, bvh_width=args.bvh_width, max_leaf=args.max_leaf, smem_nodes=args.smem_nodes,
                  bvh_flags=abi.BVH_FAST_BUILD if args.bvh_fast_build else 0)
@@ -653,7 +665,7 @@ def main():
     avg_launch_s = ext_ms / max(1, ext_launches) * 1e-3
     achieved = per_launch_bytes / avg_launch_s / 1e9 if ext_ms > 0 else None
     peak, peak_kind = measured_peaks()
-    traffic = committed_traffic(args.workload)
+    traffic = committed_traffic(args.workload) if args.at_capture_config else None
     cpu = None
     if not args.no_cpu_baseline:
         cpu = cpu_baseline(sc, 0, args.cpu_seconds, args.depth)
