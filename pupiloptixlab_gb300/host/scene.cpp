@@ -612,6 +612,12 @@ struct Loader {
                     for (auto &t : n->children)
                         if (t->name == "transform" && !transform(t.get(), s.env_map.to_world)) return false;
                     s.has_env = true;
+                } else if (et == "point") {
+                    // Parsed by the reference (resource/scene.cpp:194-202) but never
+                    // placed in its emitter tables (world/emitter.cpp:314-315 leaves
+                    // the Point case as a TODO), so it lights nothing there: accepted
+                    // and dropped here the same way.
+                    continue;
                 } else {
                     return fail(n, "emitter '" + et + "' is not supported");
                 }

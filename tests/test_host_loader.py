@@ -122,7 +122,7 @@ def test_obj_mesh(host):
     ("<scene><bsdf type='velvet' id='a'/></scene>", "unknown bsdf"),
     ("<scene><shape type='cube'><ref id='nope'/></shape></scene>", "unknown bsdf id"),
     ("<scene><emitter type='envmap'/></scene>", "without a filename"),
-    ("<scene><emitter type='point'/></scene>", "not supported"),
+    ("<scene><emitter type='spot'/></scene>", "not supported"),
     ("<scene><shape type='rectangle'><bsdf type='diffuse'><texture type='bitmap' name='reflectance'/>"
      "</bsdf></shape></scene>", "without a filename"),
     ("<scene><shape type='rectangle'><bsdf type='diffuse'><texture type='bitmap' name='reflectance'>"
@@ -413,3 +413,21 @@ def test_malformed_hair_files_are_reported(host, tmp_path, body, needle):
     with pytest.raises(abi.PtError) as e:
         host.XmlScene(str(tmp_path / "x.xml"))
     assert needle in str(e.value)
+
+
+def test_point_emitters_are_dropped_as_the_reference_does(host):
+    """<emitter type="point"> is parsed by the reference (resource/scene.cpp:194-202)
+    but never enters its emitter tables (world/emitter.cpp:314-315), so it
+    lights nothing: the scene loads and equals the same scene without it."""
+    base = """<scene version="3.0.0"><sensor type="perspective"><film type="hdrfilm">
+      <integer name="width" value="8"/><integer name="height" value="8"/></film></sensor>
+      <shape type="rectangle"><bsdf type="diffuse"/></shape>{extra}
+      <emitter type="constant"><rgb name="radiance" value="0.5"/></emitter></scene>"""
+    point = """<emitter type="point"><point name="position" x="0" y="2" z="0"/>
+      <rgb name="intensity" value="10"/></emitter>"""
+    a = host.XmlScene(base.format(extra=point), is_text=True).desc()
+    b = host.XmlScene(base.format(extra=""), is_text=True).desc()
+    assert (a.num_instances, a.num_materials, a.num_meshes, a.env.type) == \
+           (b.num_instances, b.num_materials, b.num_meshes, b.env.type)
+    assert [a.instances[i].is_emitter for i in range(a.num_instances)] == \
+           [b.instances[i].is_emitter for i in range(b.num_instances)]
