@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -14,13 +15,26 @@
 extern "C" int pupil_write_pfm(const char *path, const float *rgba, uint32_t w, uint32_t h);
 extern "C" int pupil_write_exr(const char *path, const float *rgba, uint32_t w, uint32_t h);
 
+static int usage(const char *prog) {
+    fprintf(stderr, "usage: %s <scene.xml> <out.pfm|out.exr> [frames >= 1] [lcg|pcg32]\n", prog);
+    return 2;
+}
+
 int main(int argc, char **argv) {
-    if (argc < 3) {
-        fprintf(stderr, "usage: %s <scene.xml> <out.pfm|out.exr> [frames] [lcg|pcg32]\n", argv[0]);
-        return 2;
+    if (argc < 3 || argc > 5) return usage(argv[0]);
+    uint32_t frames = 64;
+    if (argc > 3) {
+        char *end = nullptr;
+        const unsigned long v = strtoul(argv[3], &end, 10);
+        if (end == argv[3] || *end != '\0' || argv[3][0] == '-' || v == 0 || v > 0xffffffffUL) return usage(argv[0]);
+        frames = (uint32_t)v;
     }
-    uint32_t frames = argc > 3 ? (uint32_t)std::stoul(argv[3]) : 64;
-    uint32_t rng = (argc > 4 && std::string(argv[4]) == "pcg32") ? PT_RNG_PCG32 : PT_RNG_REF_LCG;
+    uint32_t rng = PT_RNG_REF_LCG;
+    if (argc > 4) {
+        const std::string r = argv[4];
+        if (r == "pcg32") rng = PT_RNG_PCG32;
+        else if (r != "lcg") return usage(argv[0]);
+    }
     Pupil::System *sys = Pupil::System::Instance();
     if (!sys->Init(0)) {
         fprintf(stderr, "%s\n", sys->error().c_str());
@@ -40,7 +54,11 @@ int main(int argc, char **argv) {
     }
     uint32_t w = sys->scene()->sensor.width, h = sys->scene()->sensor.height;
     std::vector<float> img((size_t)w * h * 4);
-    cudaMemcpy(img.data(), sys->buffers().GetBuffer("final result")->device, img.size() * 4, cudaMemcpyDeviceToHost);
+    if (cudaMemcpy(img.data(), sys->buffers().GetBuffer("final result")->device, img.size() * 4,
+                   cudaMemcpyDeviceToHost) != cudaSuccess) {
+        fprintf(stderr, "cannot read the frame back from the device\n");
+        return 1;
+    }
     const std::string out = argv[2];
     int st;
     if (out.size() > 4 && out.compare(out.size() - 4, 4, ".exr") == 0) {

@@ -431,3 +431,25 @@ def test_point_emitters_are_dropped_as_the_reference_does(host):
            (b.num_instances, b.num_materials, b.num_meshes, b.env.type)
     assert [a.instances[i].is_emitter for i in range(a.num_instances)] == \
            [b.instances[i].is_emitter for i in range(b.num_instances)]
+
+
+@pytest.mark.parametrize("args", [[], ["a.xml"], ["a.xml", "o.pfm", "x"], ["a.xml", "o.pfm", "0"],
+                                  ["a.xml", "o.pfm", "-3"], ["a.xml", "o.pfm", "4", "xorshift"],
+                                  ["a.xml", "o.pfm", "4", "pcg32", "extra"]])
+def test_cli_rejects_bad_arguments(host, args):
+    """pupil_pt checks its arguments before touching the device: a missing
+    output, a frame count that is not a positive integer or an unknown random
+    stream prints the usage line and exits with status 2."""
+    import subprocess
+    r = subprocess.run([str(build.HOST_CLI), *args], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 2 and "usage:" in r.stderr
+
+
+def test_cli_reports_an_unloadable_scene(host, tmp_path):
+    """Well-formed arguments naming a missing scene end with status 1 and a
+    message (on a machine without a GPU the device set-up reports first)."""
+    import subprocess
+    r = subprocess.run([str(build.HOST_CLI), str(tmp_path / "missing.xml"), str(tmp_path / "o.pfm"), "2", "lcg"],
+                       capture_output=True, text=True, timeout=120)
+    assert r.returncode == 1 and r.stderr.strip()
+    assert not (tmp_path / "o.pfm").exists()
