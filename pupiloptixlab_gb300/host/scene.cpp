@@ -14,6 +14,7 @@
 #include <fstream>
 #include <memory>
 #include <sstream>
+#include <stdexcept>
 
 #include "xml.h"
 
@@ -639,7 +640,18 @@ bool Scene::LoadFromString(const std::string &text, const std::string &root_dir)
         return false;
     }
     Loader l{*this, m_error};
-    return l.load(root.get());
+    // malformed or out-of-range numbers surface as std::stof / std::stod
+    // exceptions; they end the load with an error instead of leaving the library
+    try {
+        return l.load(root.get());
+    } catch (const std::invalid_argument &) {
+        m_error = "malformed number in the scene description";
+    } catch (const std::out_of_range &) {
+        m_error = "number out of range in the scene description";
+    } catch (const std::exception &e) {
+        m_error = std::string("scene load failed: ") + e.what();
+    }
+    return false;
 }
 
 bool Scene::LoadFromXML(const std::string &path) {
@@ -761,12 +773,17 @@ bool LoadObj(const std::string &path, Mesh &out, std::string &error) {
             while (is >> tok) {
                 long vi = 0, ti = 0, ni = 0;
                 size_t a = tok.find('/');
-                vi = std::stol(tok.substr(0, a));
-                if (a != std::string::npos) {
-                    size_t b = tok.find('/', a + 1);
-                    std::string ts = tok.substr(a + 1, b == std::string::npos ? std::string::npos : b - a - 1);
-                    if (!ts.empty()) ti = std::stol(ts);
-                    if (b != std::string::npos && b + 1 < tok.size()) ni = std::stol(tok.substr(b + 1));
+                try {
+                    vi = std::stol(tok.substr(0, a));
+                    if (a != std::string::npos) {
+                        size_t b = tok.find('/', a + 1);
+                        std::string ts = tok.substr(a + 1, b == std::string::npos ? std::string::npos : b - a - 1);
+                        if (!ts.empty()) ti = std::stol(ts);
+                        if (b != std::string::npos && b + 1 < tok.size()) ni = std::stol(tok.substr(b + 1));
+                    }
+                } catch (const std::exception &) {
+                    error = path + ":" + std::to_string(lineno) + ": malformed face index '" + tok + "'";
+                    return false;
                 }
                 long rv = resolve(vi, P.size() / 3), rt = ti ? resolve(ti, T.size() / 2) : -1,
                      rn = ni ? resolve(ni, N.size() / 3) : -1;

@@ -128,6 +128,10 @@ def test_obj_mesh(host):
     ("<scene><shape type='rectangle'><bsdf type='diffuse'><texture type='bitmap' name='reflectance'>"
      "<string name='filename' value='a.png'/></texture></bsdf></shape></scene>", "uncompressed .exr images can be read"),
     ("<scene><sensor type='thinlens'/></scene>", "perspective"),
+    ("<scene><shape type='cube'><transform name='to_world'><translate x='abc'/></transform></shape></scene>",
+     "malformed number"),
+    ("<scene><shape type='cube'><transform name='to_world'><rotate y='1' angle='1e999'/></transform></shape></scene>",
+     "out of range"),
     ("<notascene/>", "<scene>"),
     ("<scene><a></b></scene>", "mismatched"),
 ])
@@ -453,3 +457,13 @@ def test_cli_reports_an_unloadable_scene(host, tmp_path):
                        capture_output=True, text=True, timeout=120)
     assert r.returncode == 1 and r.stderr.strip()
     assert not (tmp_path / "o.pfm").exists()
+
+
+def test_malformed_obj_face_is_reported(host, tmp_path):
+    """A face token that is not an index ends the load with the file, the line
+    and the token in the message, not with an exception through the C API."""
+    (tmp_path / "m.obj").write_text("v 0 0 0\nv 1 0 0\nv 0 1 0\nf 1 2 x3\n")
+    (tmp_path / "m.xml").write_text("<scene><shape type='obj'><string name='filename' value='m.obj'/></shape></scene>")
+    with pytest.raises(abi.PtError) as e:
+        host.XmlScene(str(tmp_path / "m.xml"))
+    assert "m.obj:4: malformed face index 'x3'" in str(e.value)
