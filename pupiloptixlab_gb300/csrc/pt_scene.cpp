@@ -14,6 +14,8 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <new>
+#include <stdexcept>
 
 namespace {
 thread_local std::string g_last_error;
@@ -762,6 +764,24 @@ pt_scene::~pt_scene() {
     if (ev1) cudaEventDestroy(ev1);
 }
 
+// C++ exceptions (a host allocation that fails while a large scene's tables
+// are built, for instance) must not cross the C ABI: they become statuses.
+template <class F>
+static int no_throw(const char *where, F &&f) noexcept {
+    try {
+        return f();
+    } catch (const std::bad_alloc &) {
+        pt_set_error("%s: out of host memory", where);
+        return PT_ERR_OOM;
+    } catch (const std::exception &e) {
+        pt_set_error("%s: %s", where, e.what());
+        return PT_ERR_INVALID;
+    } catch (...) {
+        pt_set_error("%s: unexpected C++ exception", where);
+        return PT_ERR_INVALID;
+    }
+}
+
 extern "C" {
 
 int pt_api_version(void) { return PT_API_VERSION; }
@@ -810,7 +830,7 @@ int pt_scene_upload(pt_context *ctx, const pt_scene_desc *desc, pt_scene **out) 
     s->device = ctx->device;
     s->num_sms = ctx->num_sms;
     s->max_smem_per_block = ctx->max_smem_per_block;
-    int st = build_scene(s.get(), desc);
+    int st = no_throw("pt_scene_upload", [&] { return build_scene(s.get(), desc); });
     if (st != PT_OK) return st;
     PT_CUDA_TRY(cudaEventCreate(&s->ev0));
     PT_CUDA_TRY(cudaEventCreate(&s->ev1));
@@ -863,7 +883,7 @@ int pt_scene_update_vertices(pt_scene *scene, uint32_t mesh, const float *positi
     st = pt_update_world_vertices(scene, mesh, scene->mesh_obj_pos.as<float>(), num_vertices, 0);
     if (st != PT_OK || !scene->has_emissive_mesh) return st;
     PT_CUDA_TRY(cudaDeviceSynchronize());
-    return pt_rebuild_emitters(scene, nullptr);
+    return no_throw("pt_scene_update_vertices", [&] { return pt_rebuild_emitters(scene, nullptr); });
 }
 
 int pt_scene_update_all_vertices(pt_scene *scene, const float *positions, int on_device, void *stream) {
@@ -886,7 +906,7 @@ int pt_scene_update_all_vertices(pt_scene *scene, const float *positions, int on
     // Light triangles moved: the emitter table is rebuilt from the new world
     // vertices once the update kernels on `stream` have finished.
     PT_CUDA_TRY(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)));
-    return pt_rebuild_emitters(scene, nullptr);
+    return no_throw("pt_scene_update_all_vertices", [&] { return pt_rebuild_emitters(scene, nullptr); });
 }
 
 int pt_bvh_build(pt_scene *scene, const pt_bvh_opts *opts, void *stream) {
@@ -898,7 +918,7 @@ int pt_bvh_build(pt_scene *scene, const pt_bvh_opts *opts, void *stream) {
     if (o.max_leaf_size < 1 || o.max_leaf_size > 15) { pt_set_error("max_leaf_size must be in 1..15"); return PT_ERR_INVALID; }
     if (o.flags & ~(uint32_t)PT_BVH_FAST_BUILD) { pt_set_error("unknown BVH flags 0x%x", o.flags); return PT_ERR_INVALID; }
     PT_CUDA_TRY(cudaSetDevice(scene->device));
-    return pt_bvh_build_impl(scene, &o, static_cast<cudaStream_t>(stream));
+    return no_throw("pt_bvh_build", [&] { return pt_bvh_build_impl(scene, &o, static_cast<cudaStream_t>(stream)); });
 }
 
 int pt_bvh_refit(pt_scene *scene, void *stream) {
@@ -921,7 +941,7 @@ int pt_render(pt_scene *scene, const pt_render_params *params, const pt_frame_bu
     if (!scene->bvh_built) { pt_set_error("pt_render before pt_bvh_build"); return PT_ERR_STATE; }
     if (params->rng != PT_RNG_REF_LCG && params->rng != PT_RNG_PCG32) { pt_set_error("unknown rng mode"); return PT_ERR_INVALID; }
     PT_CUDA_TRY(cudaSetDevice(scene->device));
-    return pt_render_impl(scene, params, fb, static_cast<cudaStream_t>(stream));
+    return no_throw("pt_render", [&] { return pt_render_impl(scene, params, fb, static_cast<cudaStream_t>(stream)); });
 }
 
 int pt_render_batch(pt_context *ctx, pt_scene *const *scenes, const pt_render_params *params,
@@ -940,7 +960,8 @@ int pt_render_batch(pt_context *ctx, pt_scene *const *scenes, const pt_render_pa
         }
     }
     PT_CUDA_TRY(cudaSetDevice(ctx->device));
-    return pt_render_batch_impl(ctx, scenes, params, fbs, n, static_cast<cudaStream_t>(stream));
+    return no_throw("pt_render_batch",
+                    [&] { return pt_render_batch_impl(ctx, scenes, params, fbs, n, static_cast<cudaStream_t>(stream)); });
 }
 
 int pt_render_batch_get_stats(const pt_context *ctx, pt_render_stats *out) {
@@ -955,7 +976,7 @@ int pt_autotune(pt_scene *scene, const pt_render_params *params, const pt_frame_
     if (!scene->bvh_built) { pt_set_error("pt_autotune before pt_bvh_build"); return PT_ERR_STATE; }
     if (params->rng != PT_RNG_REF_LCG && params->rng != PT_RNG_PCG32) { pt_set_error("unknown rng mode"); return PT_ERR_INVALID; }
     PT_CUDA_TRY(cudaSetDevice(scene->device));
-    return pt_autotune_impl(scene, params, fb, out, static_cast<cudaStream_t>(stream));
+    return no_throw("pt_autotune", [&] { return pt_autotune_impl(scene, params, fb, out, static_cast<cudaStream_t>(stream)); });
 }
 
 int pt_render_get_stats(const pt_scene *scene, pt_render_stats *out) {
@@ -969,7 +990,8 @@ int pt_trace_rays(pt_scene *scene, const float *rays, float *hits, uint32_t n, i
     if (!scene || (n && (!rays || !hits))) { pt_set_error("scene, rays or hits is NULL"); return PT_ERR_INVALID; }
     if (!scene->bvh_built) { pt_set_error("pt_trace_rays before pt_bvh_build"); return PT_ERR_STATE; }
     PT_CUDA_TRY(cudaSetDevice(scene->device));
-    return pt_trace_rays_impl(scene, rays, hits, n, anyhit, static_cast<cudaStream_t>(stream));
+    return no_throw("pt_trace_rays",
+                    [&] { return pt_trace_rays_impl(scene, rays, hits, n, anyhit, static_cast<cudaStream_t>(stream)); });
 }
 
 int pt_bsdf_eval_batch(const float *bsdf, const float *wo, const float *wi, float *f, float *pdf, uint32_t n, void *stream) {
