@@ -19,6 +19,7 @@ std::string pt_error() {
 Pass::Pass(std::string_view n, EPassTag t) noexcept : name(n), tag(t) {}
 
 void Pass::Run() noexcept {
+    if (!m_enable) return;
     auto t0 = std::chrono::steady_clock::now();
     OnRun();
     last_exec_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();

@@ -30,11 +30,19 @@ public:
     virtual ~Pass() noexcept = default;
     virtual void OnRun() noexcept = 0;
     virtual void Inspector() noexcept {}
-    void Run() noexcept;  // OnRun, timed (pass.cpp:6-13)
+    void Run() noexcept;  // OnRun, timed, skipped while disabled (pass.cpp:6-13)
+
+    // enable switch (pass.h:37-39; the reference's spelling of SetEnablility kept)
+    void Toggle() noexcept { m_enable = !m_enable; }
+    void SetEnablility(bool enable) noexcept { m_enable = enable; }
+    bool IsEnabled() const noexcept { return m_enable; }
 
     const std::string name;
     const EPassTag tag;
     double last_exec_ms = 0.0;
+
+protected:
+    bool m_enable = true;
 };
 
 class BufferManager {

@@ -467,3 +467,39 @@ def test_malformed_obj_face_is_reported(host, tmp_path):
     with pytest.raises(abi.PtError) as e:
         host.XmlScene(str(tmp_path / "m.xml"))
     assert "m.obj:4: malformed face index 'x3'" in str(e.value)
+
+
+def test_pass_enable_switch(host, tmp_path):
+    """Pupil::Pass keeps the reference's enable switch (system/pass.h:37-39,
+    pass.cpp:6-13): Run() skips OnRun while the pass is disabled; Toggle and
+    SetEnablility flip it.  Compiled against the host headers, no GPU needed."""
+    import subprocess
+    src = tmp_path / "pass_switch.cpp"
+    src.write_text(r'''
+#include <cstdio>
+#include "pass.h"
+struct Count : Pupil::Pass {
+    int runs = 0;
+    Count() noexcept : Pupil::Pass("count") {}
+    void OnRun() noexcept override { runs++; }
+};
+int main() {
+    Count p;
+    p.Run();
+    p.SetEnablility(false);
+    p.Run();
+    const bool off = !p.IsEnabled();
+    p.Toggle();
+    p.Run();
+    std::printf("%d %d %d\n", p.runs, off ? 1 : 0, p.IsEnabled() ? 1 : 0);
+    return 0;
+}
+''')
+    exe = tmp_path / "pass_switch"
+    cuda_inc = build._cuda_include()
+    subprocess.run(["g++", "-std=c++17", "-I", str(build.ROOT / "include"), "-I", str(build.HOST), "-I", cuda_inc,
+                    str(src), "-o", str(exe), "-L", str(build.BUILD), "-lpupil_host", "-lpt_gb300",
+                    "-L", build._cuda_lib_dir(), "-lcudart", f"-Wl,-rpath,{build.BUILD}",
+                    f"-Wl,-rpath,{build._cuda_lib_dir()}"], check=True, capture_output=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True, timeout=60).stdout.split()
+    assert out == ["2", "1", "1"]
