@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cstring>
 
@@ -31,17 +32,25 @@ BufferManager::Buffer *BufferManager::AllocBuffer(const std::string &name, size_
         cudaMemset(slot->device, 0, slot->bytes);
         return slot.get();
     }
+    const bool is_new = !slot;
     if (slot && slot->device) cudaFree(slot->device);
     slot = std::make_unique<Buffer>();
     slot->name = name;
     if (cudaMalloc(&slot->device, bytes) != cudaSuccess) {
         slot.reset();
         m_buffers.erase(name);
+        if (!is_new) m_names.erase(std::find(m_names.begin(), m_names.end(), name));
         return nullptr;
     }
+    if (is_new) m_names.push_back(name);
     slot->bytes = bytes;
     cudaMemset(slot->device, 0, bytes);
     return slot.get();
+}
+
+BufferManager::Buffer *BufferManager::AllocBuffer(const BufferDesc &desc) {
+    if (!desc.name) return nullptr;
+    return AllocBuffer(std::string(desc.name), (size_t)desc.width * desc.height * desc.stride_in_byte);
 }
 
 BufferManager::Buffer *BufferManager::GetBuffer(const std::string &name) {
@@ -53,6 +62,7 @@ void BufferManager::Destroy() {
     for (auto &kv : m_buffers)
         if (kv.second && kv.second->device) cudaFree(kv.second->device);
     m_buffers.clear();
+    m_names.clear();
 }
 
 System *System::Instance() {

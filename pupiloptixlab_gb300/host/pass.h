@@ -52,13 +52,27 @@ public:
         void *device = nullptr;
         size_t bytes = 0;
     };
+    // BufferDesc (buffer.h:25-31): width * height * stride_in_byte bytes; the
+    // flag (DX12 sharing) has no meaning without a display and is ignored
+    struct BufferDesc {
+        const char *name = nullptr;
+        uint32_t flag = 0;
+        uint32_t width = 1;
+        uint32_t height = 1;
+        uint32_t stride_in_byte = 1;
+    };
+    static constexpr std::string_view DEFAULT_FINAL_RESULT_BUFFER_NAME = "final result";
+
     Buffer *AllocBuffer(const std::string &name, size_t bytes);  // zero-filled; reused if big enough
+    Buffer *AllocBuffer(const BufferDesc &desc);
     Buffer *GetBuffer(const std::string &name);
+    const std::vector<std::string> &GetBufferNameList() const { return m_names; }  // in allocation order
     void Destroy();
     ~BufferManager() { Destroy(); }
 
 private:
     std::map<std::string, std::unique_ptr<Buffer>> m_buffers;
+    std::vector<std::string> m_names;
 };
 
 class System {

@@ -469,10 +469,13 @@ def test_malformed_obj_face_is_reported(host, tmp_path):
     assert "m.obj:4: malformed face index 'x3'" in str(e.value)
 
 
-def test_pass_enable_switch(host, tmp_path):
+def test_pass_enable_switch_and_buffer_desc(host, tmp_path):
     """Pupil::Pass keeps the reference's enable switch (system/pass.h:37-39,
     pass.cpp:6-13): Run() skips OnRun while the pass is disabled; Toggle and
-    SetEnablility flip it.  Compiled against the host headers, no GPU needed."""
+    SetEnablility flip it.  BufferManager takes the reference's BufferDesc
+    (buffer.h:25-31) and lists buffer names in allocation order; without a
+    device an allocation fails cleanly and lists nothing.  Compiled against
+    the host headers, no GPU needed."""
     import subprocess
     src = tmp_path / "pass_switch.cpp"
     src.write_text(r'''
@@ -491,7 +494,14 @@ int main() {
     const bool off = !p.IsEnabled();
     p.Toggle();
     p.Run();
-    std::printf("%d %d %d\n", p.runs, off ? 1 : 0, p.IsEnabled() ? 1 : 0);
+    Pupil::BufferManager bm;
+    Pupil::BufferManager::BufferDesc none{};
+    Pupil::BufferManager::BufferDesc d{"pt accum buffer", 0, 4, 2, 16};
+    auto *b = bm.AllocBuffer(d);  // fails cleanly where no device is present
+    const bool consistent = (b != nullptr) == (bm.GetBufferNameList().size() == 1) &&
+                            (!b || (b->bytes == 128 && bm.GetBufferNameList()[0] == "pt accum buffer"));
+    std::printf("%d %d %d %d %d %d\n", p.runs, off ? 1 : 0, p.IsEnabled() ? 1 : 0, bm.AllocBuffer(none) == nullptr,
+                consistent ? 1 : 0, Pupil::BufferManager::DEFAULT_FINAL_RESULT_BUFFER_NAME == "final result");
     return 0;
 }
 ''')
@@ -502,4 +512,4 @@ int main() {
                     "-L", build._cuda_lib_dir(), "-lcudart", f"-Wl,-rpath,{build.BUILD}",
                     f"-Wl,-rpath,{build._cuda_lib_dir()}"], check=True, capture_output=True)
     out = subprocess.run([str(exe)], capture_output=True, text=True, check=True, timeout=60).stdout.split()
-    assert out == ["2", "1", "1"]
+    assert out == ["2", "1", "1", "1", "1", "1"]
