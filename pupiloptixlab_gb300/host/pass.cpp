@@ -117,6 +117,7 @@ bool System::SetScene(std::unique_ptr<resource::Scene> scene) {
 }
 
 void System::Run(uint32_t frames) {
+    if (!render_flag) return;
     for (uint32_t f = 0; f < frames; f++)
         for (Pass *p : m_passes) p->Run();
 }

@@ -77,6 +77,11 @@ private:
 
 class System {
 public:
+    // system.h:26-27: the render loop runs the passes only while render_flag
+    // is set (the GUI's pause); quit_flag is kept for callers that poll it
+    bool render_flag = true;
+    bool quit_flag = false;
+
     static System *Instance();
     bool Init(int device = 0);
     void AddPass(Pass *pass);

@@ -474,8 +474,9 @@ def test_pass_enable_switch_and_buffer_desc(host, tmp_path):
     pass.cpp:6-13): Run() skips OnRun while the pass is disabled; Toggle and
     SetEnablility flip it.  BufferManager takes the reference's BufferDesc
     (buffer.h:25-31) and lists buffer names in allocation order; without a
-    device an allocation fails cleanly and lists nothing.  Compiled against
-    the host headers, no GPU needed."""
+    device an allocation fails cleanly and lists nothing.  System::Run runs
+    no pass while render_flag is clear (system.h:26).  Compiled against the
+    host headers, no GPU needed."""
     import subprocess
     src = tmp_path / "pass_switch.cpp"
     src.write_text(r'''
@@ -494,14 +495,23 @@ int main() {
     const bool off = !p.IsEnabled();
     p.Toggle();
     p.Run();
+    Pupil::System sys;
+    Count q;
+    sys.AddPass(&q);
+    sys.render_flag = false;
+    sys.Run(3);
+    const int paused_runs = q.runs;
+    sys.render_flag = true;
+    sys.Run(3);
     Pupil::BufferManager bm;
     Pupil::BufferManager::BufferDesc none{};
     Pupil::BufferManager::BufferDesc d{"pt accum buffer", 0, 4, 2, 16};
     auto *b = bm.AllocBuffer(d);  // fails cleanly where no device is present
     const bool consistent = (b != nullptr) == (bm.GetBufferNameList().size() == 1) &&
                             (!b || (b->bytes == 128 && bm.GetBufferNameList()[0] == "pt accum buffer"));
-    std::printf("%d %d %d %d %d %d\n", p.runs, off ? 1 : 0, p.IsEnabled() ? 1 : 0, bm.AllocBuffer(none) == nullptr,
-                consistent ? 1 : 0, Pupil::BufferManager::DEFAULT_FINAL_RESULT_BUFFER_NAME == "final result");
+    std::printf("%d %d %d %d %d %d %d %d\n", p.runs, off ? 1 : 0, p.IsEnabled() ? 1 : 0, bm.AllocBuffer(none) == nullptr,
+                consistent ? 1 : 0, Pupil::BufferManager::DEFAULT_FINAL_RESULT_BUFFER_NAME == "final result",
+                paused_runs, q.runs);
     return 0;
 }
 ''')
@@ -512,4 +522,4 @@ int main() {
                     "-L", build._cuda_lib_dir(), "-lcudart", f"-Wl,-rpath,{build.BUILD}",
                     f"-Wl,-rpath,{build._cuda_lib_dir()}"], check=True, capture_output=True)
     out = subprocess.run([str(exe)], capture_output=True, text=True, check=True, timeout=60).stdout.split()
-    assert out == ["2", "1", "1", "1", "1", "1"]
+    assert out == ["2", "1", "1", "1", "1", "1", "0", "3"]
