@@ -103,3 +103,22 @@ def test_accumulation_equals_frame_by_frame(ptlib):
         acc = o.render(abi.RenderParams(spp=1, seed=10 + f, sample_cnt=f, accumulate=1, rng=abi.RNG_REF_LCG),
                        accum=acc)["accum"]
     assert np.array_equal(one, acc)
+
+
+def test_render_does_not_depend_on_threads_or_pixel_subsets(ptlib):
+    """The CPU baseline renders strided pixel subsets on all host cores: every
+    pixel's result is the same whatever the thread count, and a subset render
+    writes exactly the full render's values at its pixels (and nothing else)."""
+    import oracle
+    from pupiloptixlab_gb300 import abi, scenes
+    o = oracle.OracleScene(scenes.cornell_box(24, 16))
+    p = abi.RenderParams(spp=2, max_depth=4, seed=3, sample_cnt=0, accumulate=1, rng=abi.RNG_PCG32)
+    one = o.render(p, threads=1)
+    many = o.render(p, threads=4)
+    for k in one:
+        assert np.array_equal(one[k].view(np.uint32), many[k].view(np.uint32)), k
+    px = np.arange(5, 24 * 16, 7, dtype=np.uint32)
+    sub = o.render(p, pixels=px, threads=3)
+    assert np.array_equal(sub["accum"][px].view(np.uint32), one["accum"][px].view(np.uint32))
+    rest = np.setdiff1d(np.arange(24 * 16), px)
+    assert not sub["accum"][rest].any()
