@@ -228,7 +228,10 @@ def run_reference(args):
 
     import oracle
     from pupiloptixlab_gb300 import abi, scenes
-    sc = scenes.icosphere_field(args.width, args.height, args.depth, args.instances)
+    # the scene's camera from the oracle's own camera arithmetic: this arm never
+    # loads the library under test
+    with scenes.camera_maker(oracle.camera_make):
+        sc = scenes.icosphere_field(args.width, args.height, args.depth, args.instances)
     o = oracle.OracleScene(sc, bvh=True)
     threads = os.cpu_count() or 1
     npix = sc.width * sc.height

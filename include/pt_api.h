@@ -391,7 +391,9 @@ int pt_render_get_stats(const pt_scene *scene, pt_render_stats *out);
  * with PT_ERR_INVALID.  The first call on a device looks up the array's device
  * address (cudaGetSymbolAddress), so make that first call before any stream
  * capture.  All calls share the array: calls that overlap on the GPU (on
- * different streams or threads) race.  No statistics are recorded. */
+ * different streams or threads) race.  No statistics are recorded; the
+ * traversal block size is the caller's, else the one pt_autotune chose, as in
+ * pt_render, and PT_RENDER_CHECK_FINITE returns PT_ERR_NAN as there. */
 int pt_render_noalloc(pt_scene *scene, const pt_render_params *params, const pt_frame_buffers *fb, void *stream);
 
 /* Autotuner result: the configuration pt_autotune found fastest. */
@@ -443,6 +445,13 @@ int pt_bsdf_eval_batch(const float *bsdf, const float *wo, const float *wi,
 int pt_bsdf_sample_batch(const float *bsdf, const float *wo, uint32_t *rng_state,
                          float *out_wi, float *out_f, float *out_pdf, uint32_t *out_type,
                          uint32_t n, void *stream);
+/* The library's own trigonometry on the device (no counterpart in the
+ * reference, which calls the platform's sinf/cosf/atan2f/acosf): fn 0 sin(x),
+ * 1 cos(x), 2 atan2(y, x), 3 acos(x).  out: the functions every kernel uses;
+ * out_platform (may be NULL): CUDA's own function of the same name, for
+ * accuracy checks.  DEVICE pointers, n floats each (y only for atan2). */
+int pt_trig_eval(uint32_t fn, const float *x, const float *y, float *out, float *out_platform,
+                 uint32_t n, void *stream);
 
 /* ---- learned denoiser ------------------------------------------------- */
 /* Replaces the OptiX HDR denoiser of the reference's DenoisePass

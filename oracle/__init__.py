@@ -71,6 +71,7 @@ def load() -> C.CDLL:
                                       C.c_uint32, _VP]
         lib.oracle_camera_make.argtypes = [C.c_float, C.c_float, C.c_float, C.c_float, _VP,
                                            C.POINTER(abi.CameraDesc)]
+        lib.oracle_trig.argtypes = [C.c_uint32, _VP, _VP, _VP, C.c_uint32]
         _lib = lib
     return _lib
 
@@ -276,3 +277,16 @@ def camera_make(fov_y, aspect, near, far, to_world):
     if st != 0:
         raise RuntimeError("oracle_camera_make failed")
     return cam
+
+
+TRIG_SIN, TRIG_COS, TRIG_ATAN2, TRIG_ACOS = 0, 1, 2, 3
+
+
+def trig(fn: int, x, y=None) -> np.ndarray:
+    """The shared trigonometry of pt_trig.h evaluated on the host."""
+    x = np.ascontiguousarray(x, np.float32)
+    y = np.ascontiguousarray(x if y is None else y, np.float32)
+    out = np.empty_like(x)
+    if load().oracle_trig(fn, _ptr(x), _ptr(y), _ptr(out), x.size) != 0:
+        raise RuntimeError("oracle_trig failed")
+    return out

@@ -12,6 +12,10 @@
 // compiler or to uninitialised memory (the product follows the same rules):
 //  * Next2() draws x first, then y (the reference's make_float2(Next(), Next())
 //    has unspecified argument order in C++).
+//  * sin, cos, atan2 and acos are the library's own deterministic functions
+//    (pupiloptixlab_gb300/csrc/pt_trig.h, within 3 ulp of the exact values),
+//    where the reference calls the platform's (CUDA's device math, or the C
+//    library's on a host build), whose last bits differ between platforms.
 //  * EmitterSampleRecord::is_delta is false for area/sphere emitters
 //    (framework/render/emitter/types.h:25 leaves it uninitialised).
 //  * EmitEvalRecord::pdf is 0 when the emitter faces away
@@ -26,6 +30,7 @@
 //    the smaller primitive id.
 
 #include "pt_oracle.h"
+#include "pt_trig.h"
 #include "tex_fetch.h"
 
 #include <algorithm>
@@ -143,19 +148,19 @@ static inline V3 uniform_sample_sphere(float u1, float u2) {  // util.h:38-43
     float z = 1.f - 2.f * u1;
     float sin_theta = sqrtf(std::max(0.f, 1.f - z * z));
     float phi = 2.f * kPi * u2;
-    return {sin_theta * cosf(phi), sin_theta * sinf(phi), z};
+    return {sin_theta * pt_cosf(phi), sin_theta * pt_sinf(phi), z};
 }
 static inline V3 cosine_sample_hemisphere(float u1, float u2) {  // util.h:45-54
     float sin_theta = sqrtf(u1);
     float phi = 2.0f * kPi * u2;
-    return {sin_theta * cosf(phi), sin_theta * sinf(phi), sqrtf(fmaxf(0.f, 1.f - sin_theta * sin_theta))};
+    return {sin_theta * pt_cosf(phi), sin_theta * pt_sinf(phi), sqrtf(fmaxf(0.f, 1.f - sin_theta * sin_theta))};
 }
 static inline float cosine_hemisphere_pdf(V3 v) { return v.z > 0.f ? kInvPi * v.z : 0.f; }  // util.h:55-57
 static inline V3 uniform_sample_hemisphere(float u1, float u2) {  // util.h:59-69
     float z = 1.f - 2.f * u1;
     float sin_theta = sqrtf(fmaxf(0.f, 1.f - z * z));
     float phi = 2.0f * kPi * u2;
-    return {sin_theta * cosf(phi), sin_theta * sinf(phi), fabsf(z)};
+    return {sin_theta * pt_cosf(phi), sin_theta * pt_sinf(phi), fabsf(z)};
 }
 static inline float uniform_hemisphere_pdf(V3 v) { return v.z > 0.f ? kInvPi * 0.5f : 0.f; }  // util.h:70-72
 static inline V3 reflect_local(V3 v) { return {-v.x, -v.y, v.z}; }                         // util.h:74-78
@@ -186,9 +191,9 @@ static inline V3 to_world(V3 v, V3 n) {  // util.h:110-115
     return b1 * v.x + b2 * v.y + n * v.z;
 }
 static inline V2 sphere_texcoord(V3 p) {  // util.h:117-128
-    float phi = atan2f(p.y, p.x);
+    float phi = pt_atan2f(p.y, p.x);
     phi = phi < 0.f ? phi + kPi * 2.f : phi;
-    float theta = acosf(p.z);
+    float theta = pt_acosf(p.z);
     return {phi * kInvPi * 0.5f, theta * kInvPi};
 }
 static inline float luminance(V3 c) { return 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z; }  // util.h:161-163
@@ -267,8 +272,8 @@ static inline V3 ggx_sample(V3 wo, float alpha, V2 xi) {
     V3 t2v = cross(vh, t1v);
     float r = sqrtf(xi.x);
     float phi = 2.f * kPi * xi.y;
-    float t1 = r * cosf(phi);
-    float t2 = r * sinf(phi);
+    float t1 = r * pt_cosf(phi);
+    float t2 = r * pt_sinf(phi);
     float s = 0.5f * (1.f + vh.z);
     t2 = (1.f - s) * sqrtf(1.f - t1 * t1) + s * t2;
     V3 nh = t1 * t1v + t2 * t2v + sqrtf(fmaxf(0.f, 1.f - t1 * t1 - t2 * t2)) * vh;
@@ -776,8 +781,8 @@ struct EnvMapData {
         const uint32_t col = scan(col_cdf.data() + (size_t)crow * (map.w + 1), map.w - 1, xi.y);
         const float phi = static_cast<float>(col) * kPi * 2.f / static_cast<float>(map.w);
         const float theta = static_cast<float>(row) * kPi / static_cast<float>(map.h);
-        const float st = std::sin(theta);
-        const V3 local{st * std::sin(kPi - phi), std::cos(theta), st * std::cos(kPi - phi)};
+        const float st = pt_sinf(theta);
+        const V3 local{st * pt_sinf(kPi - phi), pt_cosf(theta), st * pt_cosf(kPi - phi)};
         wi = {dot(to_world[0], local), dot(to_world[1], local), dot(to_world[2], local)};
         rad = lookup(phi * 0.5f * kInvPi, theta * kInvPi);
         pdf = luminance(rad) * row_weight[crow] * normalization / std::max(1e-4f, std::fabs(st));
@@ -787,15 +792,15 @@ struct EnvMapData {
     void eval(V3 scatter_pos, V3 emit_pos, V3 &rad, float &pdf) const {
         V3 dir = normalize(emit_pos - scatter_pos);
         dir = {dot(to_local[0], dir), dot(to_local[1], dir), dot(to_local[2], dir)};
-        const float phi = kPi - std::atan2(dir.x, dir.z);
-        const float theta = std::acos(dir.y);
+        const float phi = kPi - pt_atan2f(dir.x, dir.z);
+        const float theta = pt_acosf(dir.y);
         const float tu = phi * 0.5f * kInvPi, tv = theta * kInvPi;
         uint32_t row = static_cast<uint32_t>(tv * static_cast<float>(map.h));
         row = std::min(row, map.h - 2u);
         rad = lookup(tu, tv);
         const float t = tv * static_cast<float>(map.h) - 1.f * static_cast<float>(row);
         pdf = luminance(rad) * (row_weight[row] + t * (row_weight[row + 1] - row_weight[row])) * normalization /
-              std::max(1e-4f, std::fabs(std::sin(theta)));
+              std::max(1e-4f, std::fabs(pt_sinf(theta)));
     }
 };
 
@@ -2314,6 +2319,21 @@ int oracle_select_emitter(const float *probs, uint32_t num, int has_env, const f
             if (p[i] <= cdf[k]) { r = (int32_t)k; break; }
         if (r == -2) r = has_env ? -1 : (num ? (int32_t)num - 1 : -2);
         out[i] = r;
+    }
+    return PT_OK;
+}
+
+// The shared trigonometry (pt_trig.h) on the host: fn 0 sin(x), 1 cos(x),
+// 2 atan2(y, x), 3 acos(x).
+int oracle_trig(uint32_t fn, const float *x, const float *y, float *out, uint32_t n) {
+    if (fn > 3) return PT_ERR_INVALID;
+    for (uint32_t i = 0; i < n; i++) {
+        switch (fn) {
+            case 0: out[i] = pt_sinf(x[i]); break;
+            case 1: out[i] = pt_cosf(x[i]); break;
+            case 2: out[i] = pt_atan2f(y[i], x[i]); break;
+            default: out[i] = pt_acosf(x[i]); break;
+        }
     }
     return PT_OK;
 }

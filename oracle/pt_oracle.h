@@ -90,6 +90,9 @@ int oracle_select_emitter(const float *probs, uint32_t num, int has_env, const f
 int oracle_camera_make(float fov_y_deg, float aspect, float near_clip, float far_clip,
                        const float to_world[16], pt_camera_desc *out);
 
+/* the shared trigonometry: fn 0 sin(x), 1 cos(x), 2 atan2(y, x), 3 acos(x) */
+int oracle_trig(uint32_t fn, const float *x, const float *y, float *out, uint32_t n);
+
 #ifdef __cplusplus
 }
 #endif

@@ -7,7 +7,11 @@ Layers:
   abi.py                   ctypes mirror of the ABI and the library loader
   scenes.py                scene builder, materials, procedural scenes
   api.py                   Python host wrapper (device buffers via torch)
-  passes.py                Pass / System mirror of the reference's pass API
+  host_api.py              ctypes access to the C++ host layer (host/: mitsuba
+                           XML/OBJ/HAIR loader, Pass / System / BufferManager
+                           mirror of the reference's pass API, WavefrontPTPass)
+  denoiser.py              learned U-Net denoiser (training and inference)
+  denoise_data.py          training pairs rendered by the tracer
 """
 from . import abi  # noqa: F401
 

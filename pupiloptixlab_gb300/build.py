@@ -24,7 +24,10 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = BUILD / "libpt_gb300.so"
 ORACLE = ROOT / "oracle"
-REFERENCE_TREE = Path("/root/reference")
+# The PupilOptixLab source tree (only for the oracle's reference-compiled
+# known-answer library): $PUPIL_REFERENCE_DIR if set, else a `reference`
+# directory beside this repository; absent on machines that only run the tests.
+REFERENCE_TREE = Path(os.environ.get("PUPIL_REFERENCE_DIR") or (ROOT.parent / "reference"))
 
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_COMMON = GENCODE + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",

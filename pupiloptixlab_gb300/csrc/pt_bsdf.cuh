@@ -3,12 +3,14 @@
 //
 // Semantics follow PupilOptixLab's render layer; each function names the
 // reference file:line it implements (paths relative to the PupilOptixLab
-// tree).  Expressions keep the reference's operation order so that, compiled
-// with -fmad=false, results differ from the host-compiled reference only where
-// CUDA's sinf/cosf/acosf/atan2f round differently.
+// tree).  Expressions keep the reference's operation order, and the
+// trigonometric functions are the library's own (pt_trig.h), so that, compiled
+// with -fmad=false, results equal a host build of the same arithmetic bit for
+// bit.
 #pragma once
 
 #include "pt_device.cuh"
+#include "pt_trig.h"
 
 namespace ptd {
 
@@ -22,19 +24,19 @@ PT_DI float3 uniform_sample_sphere(float u1, float u2) {  // util.h:38-43
     float z = 1.f - 2.f * u1;
     float sin_theta = sqrtf(fmaxf(0.f, 1.f - z * z));
     float phi = 2.f * kPi * u2;
-    return f3(sin_theta * cosf(phi), sin_theta * sinf(phi), z);
+    return f3(sin_theta * pt_cosf(phi), sin_theta * pt_sinf(phi), z);
 }
 PT_DI float3 cosine_sample_hemisphere(float u1, float u2) {  // util.h:45-54
     float sin_theta = sqrtf(u1);
     float phi = 2.0f * kPi * u2;
-    return f3(sin_theta * cosf(phi), sin_theta * sinf(phi), sqrtf(fmaxf(0.f, 1.f - sin_theta * sin_theta)));
+    return f3(sin_theta * pt_cosf(phi), sin_theta * pt_sinf(phi), sqrtf(fmaxf(0.f, 1.f - sin_theta * sin_theta)));
 }
 PT_DI float cosine_hemisphere_pdf(float3 v) { return v.z > 0.f ? kInvPi * v.z : 0.f; }  // util.h:55-57
 PT_DI float3 uniform_sample_hemisphere(float u1, float u2) {                         // util.h:59-69
     float z = 1.f - 2.f * u1;
     float sin_theta = sqrtf(fmaxf(0.f, 1.f - z * z));
     float phi = 2.0f * kPi * u2;
-    return f3(sin_theta * cosf(phi), sin_theta * sinf(phi), fabsf(z));
+    return f3(sin_theta * pt_cosf(phi), sin_theta * pt_sinf(phi), fabsf(z));
 }
 PT_DI float uniform_hemisphere_pdf(float3 v) { return v.z > 0.f ? kInvPi * 0.5f : 0.f; }  // util.h:70-72
 PT_DI float3 reflect_local(float3 v) { return f3(-v.x, -v.y, v.z); }                     // util.h:74-78
@@ -65,9 +67,9 @@ PT_DI float3 to_world(float3 v, float3 n) {  // util.h:110-115
     return b1 * v.x + b2 * v.y + n * v.z;
 }
 PT_DI float2 sphere_texcoord(float3 p) {  // util.h:117-128
-    float phi = atan2f(p.y, p.x);
+    float phi = pt_atan2f(p.y, p.x);
     phi = phi < 0.f ? phi + kPi * 2.f : phi;
-    float theta = acosf(p.z);
+    float theta = pt_acosf(p.z);
     return make_float2(phi * kInvPi * 0.5f, theta * kInvPi);
 }
 PT_DI float luminance(float3 c) { return 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z; }
@@ -140,8 +142,8 @@ PT_DI float3 ggx_sample(float3 wo, float alpha, float2 xi) {
     float3 t2v = cross(vh, t1v);
     float r = sqrtf(xi.x);
     float phi = 2.f * kPi * xi.y;
-    float t1 = r * cosf(phi);
-    float t2 = r * sinf(phi);
+    float t1 = r * pt_cosf(phi);
+    float t2 = r * pt_sinf(phi);
     float s = 0.5f * (1.f + vh.z);
     t2 = (1.f - s) * sqrtf(1.f - t1 * t1) + s * t2;
     float3 nh = t1 * t1v + t2 * t2v + sqrtf(fmaxf(0.f, 1.f - t1 * t1 - t2 * t2)) * vh;
@@ -555,8 +557,8 @@ PT_DI void envmap_sample_direct(const DevEnvMap &m, float2 xi, EmitterSample &r)
     const uint32_t col = cdf_first_geq(m.col_cdf + (size_t)crow * (m.w + 1), m.w - 1, xi.y);
     const float phi = static_cast<float>(col) * kPi * 2.f / static_cast<float>(m.w);
     const float theta = static_cast<float>(row) * kPi / static_cast<float>(m.h);
-    const float st = sinf(theta);
-    const float3 local = f3(st * sinf(kPi - phi), cosf(theta), st * cosf(kPi - phi));
+    const float st = pt_sinf(theta);
+    const float3 local = f3(st * pt_sinf(kPi - phi), pt_cosf(theta), st * pt_cosf(kPi - phi));
     r.wi = f3(dot(xyz(m.to_world[0]), local), dot(xyz(m.to_world[1]), local), dot(xyz(m.to_world[2]), local));
     r.distance = kMaxDistance;
     r.radiance = envmap_lookup(m, make_float2(phi * 0.5f * kInvPi, theta * kInvPi));
@@ -571,15 +573,15 @@ PT_DI void envmap_eval(const DevEnvMap &m, float3 scatter_pos, float3 d, float3 
     const float3 pos = scatter_pos + d;
     float3 dir = normalize(pos - scatter_pos);
     dir = f3(dot(xyz(m.to_local[0]), dir), dot(xyz(m.to_local[1]), dir), dot(xyz(m.to_local[2]), dir));
-    const float phi = kPi - atan2f(dir.x, dir.z);
-    const float theta = acosf(dir.y);
+    const float phi = kPi - pt_atan2f(dir.x, dir.z);
+    const float theta = pt_acosf(dir.y);
     const float2 tex = make_float2(phi * 0.5f * kInvPi, theta * kInvPi);
     uint32_t row = static_cast<uint32_t>(tex.y * static_cast<float>(m.h));
     row = min(row, m.h - 2u);
     radiance = envmap_lookup(m, tex);
     const float w0 = __ldg(m.row_weight + row), w1 = __ldg(m.row_weight + row + 1);
     const float t = tex.y * static_cast<float>(m.h) - 1.f * static_cast<float>(row);
-    pdf = luminance(radiance) * (w0 + t * (w1 - w0)) * m.normalization / fmaxf(1e-4f, fabsf(sinf(theta)));
+    pdf = luminance(radiance) * (w0 + t * (w1 - w0)) * m.normalization / fmaxf(1e-4f, fabsf(pt_sinf(theta)));
 }
 
 // Emitter::Eval at an emitter hit (area.h:37-45, sphere.h:34-42): pdf 0 if it faces away.

@@ -151,6 +151,8 @@ int pt_bsdf_eval_impl(const float *bsdf, const float *wo, const float *wi, float
                       cudaStream_t stream);
 int pt_bsdf_sample_impl(const float *bsdf, const float *wo, uint32_t *rng, float *wi, float *f, float *pdf,
                         uint32_t *type, uint32_t n, cudaStream_t stream);
+int pt_trig_eval_impl(uint32_t fn, const float *x, const float *y, float *out, float *out_platform, uint32_t n,
+                      cudaStream_t st);
 // Re-transforms the world vertices / primitive records of mesh instances on the device.
 int pt_update_world_vertices(pt_scene *s, uint32_t mesh, const float *d_obj_pos, uint32_t num_vertices,
                              cudaStream_t stream);

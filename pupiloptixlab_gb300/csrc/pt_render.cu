@@ -1297,6 +1297,31 @@ int pt_trace_rays_impl(pt_scene *s, const float *rays, float *hits, uint32_t n, 
     }
 }
 
+// pt_trig_eval: the library's trigonometry next to CUDA's, for the accuracy
+// and host-equality checks of pt_trig.h.
+__global__ void k_trig_eval(uint32_t fn, const float *x, const float *y, float *out, float *out_platform, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float a = x[i];
+    float ours, theirs;
+    switch (fn) {
+        case 0: ours = pt_sinf(a); theirs = sinf(a); break;
+        case 1: ours = pt_cosf(a); theirs = cosf(a); break;
+        case 2: ours = pt_atan2f(y[i], a); theirs = atan2f(y[i], a); break;
+        default: ours = pt_acosf(a); theirs = acosf(a); break;
+    }
+    out[i] = ours;
+    if (out_platform) out_platform[i] = theirs;
+}
+
+int pt_trig_eval_impl(uint32_t fn, const float *x, const float *y, float *out, float *out_platform, uint32_t n,
+                      cudaStream_t st) {
+    if (n) k_trig_eval<<<nblocks(n, 256), 256, 0, st>>>(fn, x, y, out, out_platform, n);
+    PT_CUDA_TRY(cudaGetLastError());
+    PT_CUDA_TRY(cudaStreamSynchronize(st));
+    return PT_OK;
+}
+
 int pt_bsdf_eval_impl(const float *bsdf, const float *wo, const float *wi, float *f, float *pdf, uint32_t n, cudaStream_t st) {
     if (n) k_bsdf_eval<<<nblocks(n, 128), 128, 0, st>>>(bsdf, wo, wi, f, pdf, n);
     PT_CUDA_TRY(cudaGetLastError());
@@ -1394,7 +1419,8 @@ int render_noalloc(pt_scene *s, const pt_render_params *p, const pt_frame_buffer
     out.test = fb->test;
     out.drop_nonfinite = (p->flags & PT_RENDER_DROP_NONFINITE) ? 1u : 0u;
 
-    const int tb = p->block_size ? (int)p->block_size : 128;
+    // the traversal block size pt_render would use: the caller's, else the autotuned one, else 128
+    const int tb = p->block_size ? (int)p->block_size : (s->tuned_block ? (int)s->tuned_block : 128);
     const size_t smem = (size_t)d.smem_nodes * 32 * K + (size_t)kShortStack * 8 * tb;
     const bool curves = s->num_curve_pieces > 0;
     auto k_ext = curves ? k_trace_queue<K, false, false, false, true> : k_trace_queue<K, false, false>;
@@ -1433,20 +1459,46 @@ int render_noalloc(pt_scene *s, const pt_render_params *p, const pt_frame_buffer
         k_accumulate<false><<<nblocks(npix, 256), 256, 0, st>>>(stt, w, out, Batch{});
     }
     PT_CUDA_TRY(cudaGetLastError());
-    uint32_t ovf = 0;
-    PT_CUDA_TRY(cudaMemcpyAsync(&ovf, stt.counters + kOverflow, sizeof(ovf), cudaMemcpyDeviceToHost, st));
+    // the overflow and non-finite counters are adjacent: one small read-back
+    static_assert(kNonFinite == kOverflow + 1, "counter layout");
+    uint32_t hc[2] = {0, 0};
+    PT_CUDA_TRY(cudaMemcpyAsync(hc, stt.counters + kOverflow, sizeof(hc), cudaMemcpyDeviceToHost, st));
     PT_CUDA_TRY(cudaStreamSynchronize(st));
-    if (ovf) {
+    if (hc[0]) {
         pt_set_error("traversal stack overflow");
         return PT_ERR_OOB;
     }
+    if (hc[1] && (p->flags & PT_RENDER_CHECK_FINITE)) {
+        pt_set_error("%u samples had NaN or infinite radiance", hc[1]);
+        return PT_ERR_NAN;
+    }
     return PT_OK;
 }
+
+int render_noalloc_checked(pt_scene *scene, const pt_render_params *params, const pt_frame_buffers *fb, void *stream);
 
 }  // namespace
 
 extern "C" int pt_render_noalloc(pt_scene *scene, const pt_render_params *params, const pt_frame_buffers *fb,
                                  void *stream) {
+    // as every entry point: an error left behind by another call in the process
+    // is not reported here, and no C++ exception (std::mutex::lock may throw)
+    // crosses the C ABI
+    (void)cudaGetLastError();
+    try {
+        return render_noalloc_checked(scene, params, fb, stream);
+    } catch (const std::exception &e) {
+        pt_set_error("pt_render_noalloc: %s", e.what());
+        return PT_ERR_INVALID;
+    } catch (...) {
+        pt_set_error("pt_render_noalloc: unexpected C++ exception");
+        return PT_ERR_INVALID;
+    }
+}
+
+namespace {
+
+int render_noalloc_checked(pt_scene *scene, const pt_render_params *params, const pt_frame_buffers *fb, void *stream) {
     if (!scene || !params || !fb || !fb->accum) {
         pt_set_error("scene, params, buffers or accum is NULL");
         return PT_ERR_INVALID;
@@ -1478,3 +1530,5 @@ extern "C" int pt_render_noalloc(pt_scene *scene, const pt_render_params *params
         default: return render_noalloc<8>(scene, params, fb, scratch, st);
     }
 }
+
+}  // namespace

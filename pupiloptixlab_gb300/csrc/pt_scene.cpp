@@ -1007,6 +1007,13 @@ int pt_bsdf_sample_batch(const float *bsdf, const float *wo, uint32_t *rng, floa
     return pt_bsdf_sample_impl(bsdf, wo, rng, wi, f, pdf, type, n, static_cast<cudaStream_t>(stream));
 }
 
+int pt_trig_eval(uint32_t fn, const float *x, const float *y, float *out, float *out_platform, uint32_t n, void *stream) {
+    clear_stale_cuda_error();
+    if (fn > 3) { pt_set_error("unknown function %u", fn); return PT_ERR_INVALID; }
+    if (n && (!x || !out || (fn == 2 && !y))) { pt_set_error("NULL buffer"); return PT_ERR_INVALID; }
+    return pt_trig_eval_impl(fn, x, y, out, out_platform, n, static_cast<cudaStream_t>(stream));
+}
+
 // util::Camera::GetSampleToCameraMatrix (framework/util/camera.cpp:7-20):
 // sample_to_camera = transpose(inverse(P * T(1,1,0) * S(0.5,0.5,1))) where P is
 // DirectXMath's row-vector XMMatrixPerspectiveFovRH; computed in double here.

@@ -19,6 +19,7 @@ Procedural scenes (seeded, synthetic; no external assets):
 """
 from __future__ import annotations
 
+import contextlib
 import ctypes as C
 import math
 from dataclasses import dataclass, field
@@ -184,8 +185,29 @@ def look_at_to_world(eye, target, up=(0.0, 1.0, 0.0)):
     return m
 
 
+_camera_maker = None
+
+
+@contextlib.contextmanager
+def camera_maker(fn):
+    """Within the block, scene cameras are made by `fn(fov_y, aspect, near,
+    far, to_world) -> CameraDesc` instead of the library's pt_camera_make, so
+    that a CPU-only caller (the timed CPU restatement of the integrator) can
+    build the procedural scenes without loading libpt_gb300.so."""
+    global _camera_maker
+    prev, _camera_maker = _camera_maker, fn
+    try:
+        yield
+    finally:
+        _camera_maker = prev
+
+
 def camera(fov_y_deg: float, aspect: float, to_world, near_clip=0.01, far_clip=10000.0) -> abi.CameraDesc:
-    """sample_to_camera / camera_to_world through the library's pt_camera_make."""
+    """sample_to_camera / camera_to_world through the library's pt_camera_make
+    (or the maker installed by camera_maker)."""
+    if _camera_maker is not None:
+        return _camera_maker(fov_y_deg, aspect, near_clip, far_clip,
+                             np.asarray(to_world, np.float64).reshape(-1).astype(np.float32))
     lib = abi.load()
     cam = abi.CameraDesc()
     tw = (C.c_float * 16)(*[float(v) for v in np.asarray(to_world, np.float64).reshape(-1)])

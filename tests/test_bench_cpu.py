@@ -39,3 +39,23 @@ def test_timing_options_keep_the_captured_configuration(monkeypatch):
     assert a.at_capture_config
     a = _parse(monkeypatch, "--workload", "hair")
     assert a.at_capture_config
+
+
+def test_reference_arm_never_loads_the_library_under_test():
+    """`bench.py --impl reference` times the CPU restatement alone: the
+    process maps the oracle library and not libpt_gb300.so (its camera comes
+    from the oracle's own camera arithmetic)."""
+    import json
+    import subprocess
+    code = (
+        "import sys, json; sys.argv = ['bench.py', '--impl', 'reference', '--instances', '2', '--width', '48', "
+        "'--height', '27', '--steps', '1', '--warmup', '0']\n"
+        "import bench; bench.main()\n"
+        "maps = open('/proc/self/maps').read()\n"
+        "print(json.dumps({'pt': 'libpt_gb300' in maps, 'oracle': 'liboracle' in maps}))\n")
+    r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [json.loads(x) for x in r.stdout.strip().splitlines() if x.startswith("{")]
+    line, maps = lines[0], lines[-1]
+    assert line["impl"] == "reference" and line["value"] > 0
+    assert maps == {"pt": False, "oracle": True}

@@ -18,12 +18,15 @@ from pupiloptixlab_gb300.api import GpuScene
 pytestmark = pytest.mark.gpu
 
 
+def noalloc_call(g, bufs, spp, seed, rng, accumulate=True, flags=0):
+    p = abi.RenderParams(spp, 0, seed, 0, 1 if accumulate else 0, rng, 0, 0, flags)
+    fb = abi.FrameBuffers(*[bufs[k].data_ptr() for k in ("accum", "frame", "albedo", "normal", "test")])
+    return g.lib.pt_render_noalloc(g.handle, C.byref(p), C.byref(fb), C.c_void_p(torch.cuda.current_stream().cuda_stream))
+
+
 def noalloc_render(g, spp, seed, rng, accumulate=True):
     bufs = g.alloc_buffers()
-    p = abi.RenderParams(spp, 0, seed, 0, 1 if accumulate else 0, rng, 0, 0, 0)
-    fb = abi.FrameBuffers(*[bufs[k].data_ptr() for k in ("accum", "frame", "albedo", "normal", "test")])
-    st = g.lib.pt_render_noalloc(g.handle, C.byref(p), C.byref(fb), C.c_void_p(torch.cuda.current_stream().cuda_stream))
-    abi.check(st, "pt_render_noalloc", g.lib)
+    abi.check(noalloc_call(g, bufs, spp, seed, rng, accumulate), "pt_render_noalloc", g.lib)
     torch.cuda.synchronize()
     return {k: v.cpu().numpy() for k, v in bufs.items()}
 
@@ -66,3 +69,40 @@ def test_noalloc_rejects_images_over_the_limit(cuda_ctx):
     assert st == 1  # PT_ERR_INVALID
     msg = abi.last_error(g.lib)
     assert "76800 pixels exceed the limit of 65536" in msg
+
+
+def test_noalloc_allocates_no_device_memory(cuda_ctx):
+    """The defining claim: after one warm-up call (which loads the kernels and
+    looks up the array's address), further calls leave the device's free
+    memory unchanged.  The scene's own pt_render workspace is never created,
+    because pt_render is not called on this scene."""
+    g = GpuScene(cuda_ctx, scenes.material_spheres(96, 64))
+    bufs = g.alloc_buffers()
+    abi.check(noalloc_call(g, bufs, 2, 0, abi.RNG_PCG32), "pt_render_noalloc", g.lib)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for seed in range(1, 4):
+        abi.check(noalloc_call(g, bufs, 5, seed, abi.RNG_PCG32 if seed % 2 else abi.RNG_REF_LCG), "pt_render_noalloc",
+                  g.lib)
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+    assert np.isfinite(bufs["accum"].cpu().numpy()).all()
+
+
+def test_noalloc_reports_nonfinite_samples_like_pt_render(cuda_ctx):
+    """PT_RENDER_CHECK_FINITE: a material whose reflectance is NaN poisons
+    paths; pt_render_noalloc returns PT_ERR_NAN as pt_render does, and a clean
+    scene afterwards returns PT_OK (the counter is cleared per call)."""
+    sc = scenes.cornell_box(24, 24)
+    sc.materials[0].tex[0].color0[:] = [float("nan")] * 3
+    g = GpuScene(cuda_ctx, sc)
+    bufs = g.alloc_buffers()
+    assert noalloc_call(g, bufs, 2, 1, abi.RNG_PCG32) == 0  # counted, not reported
+    st = noalloc_call(g, bufs, 2, 1, abi.RNG_PCG32, flags=abi.RENDER_CHECK_FINITE)
+    assert st == 5 and "NaN or infinite" in abi.last_error(g.lib)
+    with pytest.raises(abi.PtError) as e:
+        g.render(2, seed=1, flags=abi.RENDER_CHECK_FINITE)
+    assert e.value.status == 5
+    clean = GpuScene(cuda_ctx, scenes.cornell_box(24, 24))
+    cb = clean.alloc_buffers()
+    assert noalloc_call(clean, cb, 2, 1, abi.RNG_PCG32, flags=abi.RENDER_CHECK_FINITE) == 0
