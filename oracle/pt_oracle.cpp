@@ -1014,16 +1014,24 @@ static inline bool intersect_triangle(const Ray &ray, const RayWT &w, V3 p0, V3 
     return true;
 }
 
+// OptiX's built-in sphere intersector is closed; this is the library's own:
+// the precise formulation of Haines, Guenther and Akenine-Moeller (Ray Tracing
+// Gems 2019, ch. 7): discriminant r^2 - |f + (b'/a) d|^2 from the closest
+// approach, roots c/q and q/a with q = b' + sign(b') sqrt(a disc), so that
+// hits are accurate to a few ulp of t and never fall outside the sphere's box.
 static inline bool intersect_sphere(const Ray &ray, V3 c, float r, float tmax, float &t_out) {
-    V3 oc = ray.o - c;
+    V3 f = ray.o - c;
     float a = dot(ray.d, ray.d);
-    float b = dot(oc, ray.d);
-    float cc = dot(oc, oc) - r * r;
-    float disc = b * b - a * cc;
+    float bp = -dot(f, ray.d);
+    float s = bp / a;
+    V3 l = {f.x + s * ray.d.x, f.y + s * ray.d.y, f.z + s * ray.d.z};
+    float rr = r * r;
+    float disc = rr - dot(l, l);
     if (!(disc >= 0.f)) return false;
-    float sq = sqrtf(disc);
-    float t0 = (-b - sq) / a;
-    float t1 = (-b + sq) / a;
+    float cc = dot(f, f) - rr;
+    float q = bp + copysignf(sqrtf(a * disc), bp);
+    float t0 = cc / q, t1 = q / a;
+    if (t0 > t1) std::swap(t0, t1);
     if (t0 > ray.tmin && t0 < tmax) { t_out = t0; return true; }
     if (t1 > ray.tmin && t1 < tmax) { t_out = t1; return true; }
     return false;

@@ -100,17 +100,34 @@ PT_DI bool intersect_triangle(float3 o, const RayWT &w, float3 p0, float3 p1, fl
     return true;
 }
 
+// Ray/sphere with the two precision improvements of Haines, Guenther and
+// Akenine-Moeller ("Precision Improvements for Ray/Sphere Intersection", Ray
+// Tracing Gems, 2019): the discriminant from the distance of the closest
+// approach to the centre, r^2 - |f + (b'/a) d|^2, instead of b^2 - ac (which
+// cancels for distant or small spheres), and the two roots as c/q and q/a with
+// q = b' + sign(b') sqrt(a * disc) (no subtraction of nearly equal values).
+// The roots are then accurate to a few ulp of t, so a hit always lies inside
+// the sphere's (padded) bounding box and the result cannot depend on which
+// BVH nodes the traversal culls.  Every step is rounded separately, as in
+// the oracle's host build of the same formula.
 PT_DI bool intersect_sphere(float3 o, float3 d, float3 c, float r, float tmin, float tmax, float &t_out) {
-    float3 oc = f3(__fsub_rn(o.x, c.x), __fsub_rn(o.y, c.y), __fsub_rn(o.z, c.z));
-    float a = __fadd_rn(__fadd_rn(__fmul_rn(d.x, d.x), __fmul_rn(d.y, d.y)), __fmul_rn(d.z, d.z));
-    float b = __fadd_rn(__fadd_rn(__fmul_rn(oc.x, d.x), __fmul_rn(oc.y, d.y)), __fmul_rn(oc.z, d.z));
-    float cc = __fsub_rn(__fadd_rn(__fadd_rn(__fmul_rn(oc.x, oc.x), __fmul_rn(oc.y, oc.y)), __fmul_rn(oc.z, oc.z)),
-                         __fmul_rn(r, r));
-    float disc = __fsub_rn(__fmul_rn(b, b), __fmul_rn(a, cc));
+    const float3 f = f3(__fsub_rn(o.x, c.x), __fsub_rn(o.y, c.y), __fsub_rn(o.z, c.z));
+    const float a = __fadd_rn(__fadd_rn(__fmul_rn(d.x, d.x), __fmul_rn(d.y, d.y)), __fmul_rn(d.z, d.z));
+    const float bp = -__fadd_rn(__fadd_rn(__fmul_rn(f.x, d.x), __fmul_rn(f.y, d.y)), __fmul_rn(f.z, d.z));
+    const float s = __fdiv_rn(bp, a);
+    const float3 l = f3(__fadd_rn(f.x, __fmul_rn(s, d.x)), __fadd_rn(f.y, __fmul_rn(s, d.y)),
+                        __fadd_rn(f.z, __fmul_rn(s, d.z)));
+    const float rr = __fmul_rn(r, r);
+    const float disc = __fsub_rn(rr, __fadd_rn(__fadd_rn(__fmul_rn(l.x, l.x), __fmul_rn(l.y, l.y)), __fmul_rn(l.z, l.z)));
     if (!(disc >= 0.f)) return false;
-    float sq = __fsqrt_rn(disc);
-    float t0 = __fdiv_rn(__fsub_rn(-b, sq), a);
-    float t1 = __fdiv_rn(__fadd_rn(-b, sq), a);
+    const float cc = __fsub_rn(__fadd_rn(__fadd_rn(__fmul_rn(f.x, f.x), __fmul_rn(f.y, f.y)), __fmul_rn(f.z, f.z)), rr);
+    const float q = __fadd_rn(bp, copysignf(__fsqrt_rn(__fmul_rn(a, disc)), bp));
+    float t0 = __fdiv_rn(cc, q), t1 = __fdiv_rn(q, a);
+    if (t0 > t1) {
+        const float tt = t0;
+        t0 = t1;
+        t1 = tt;
+    }
     if (t0 > tmin && t0 < tmax) {
         t_out = t0;
         return true;

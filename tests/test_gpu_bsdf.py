@@ -40,25 +40,16 @@ def test_sample_matches_reference(cuda_ctx, golden):
     wi, f, pdf, typ, rng = api.bsdf_sample(T(golden["sample_bsdf"]), T(golden["sample_wo"]), T(seeds))
     wi, f, pdf = wi.cpu().numpy(), f.cpu().numpy(), pdf.cpu().numpy()
     typ, rng = typ.cpu().numpy().view(np.uint32), rng.cpu().numpy().view(np.uint32)
-    same_path = (typ == golden["sample_type"]) & (rng == golden["sample_seed_out"])
-    # a lobe choice can only flip when a random number sits within an ulp of a threshold
-    assert same_path.mean() > 0.998
-    assert close(wi[same_path], golden["sample_wi"][same_path])
-    delta = same_path & ((typ & 0x60) != 0)
-    # delta lobes: reflect / refract / Fresnel use no transcendental function -> identical
-    assert np.array_equal(f[delta], golden["sample_f"][delta], equal_nan=True)
-    assert np.array_equal(pdf[delta], golden["sample_pdf"][delta], equal_nan=True)
-    # sampled non-delta lobes: value and pdf are the reference's evaluation at the
-    # direction the GPU drew (which may differ from the host's by an ulp of sin/cos)
-    smooth = same_path & ((typ & 0x60) == 0) & (typ != 0)
-    # early returns after the lobe was chosen (e.g. a refraction that stays on
-    # the same side, rough_dielectric.h:149-150) leave f = pdf = 0 on both sides
-    rejected = smooth & (golden["sample_pdf"] == 0)
-    assert np.all(pdf[rejected] == 0) and np.all(f[rejected] == 0)
-    smooth &= golden["sample_pdf"] != 0
+    # the shared trigonometry makes every sample identical to the reference's
+    # headers compiled for the host: same lobe, random stream and bits
+    assert np.array_equal(typ, golden["sample_type"]) and np.array_equal(rng, golden["sample_seed_out"])
+    assert close(wi, golden["sample_wi"])
+    assert np.array_equal(wi, golden["sample_wi"], equal_nan=True)
+    assert np.array_equal(f, golden["sample_f"], equal_nan=True)
+    assert np.array_equal(pdf, golden["sample_pdf"], equal_nan=True)
+    # sampled non-delta lobes: value and pdf also equal the reference's
+    # evaluation at the drawn direction (within the eval tolerance)
+    smooth = ((typ & 0x60) == 0) & (typ != 0) & (golden["sample_pdf"] != 0)
     ref_f, ref_pdf = oracle.bsdf_eval(golden["sample_bsdf"][smooth], golden["sample_wo"][smooth], wi[smooth])
     assert close(f[smooth], ref_f)
     assert close(pdf[smooth], ref_pdf)
-    for k in range(1, 8):
-        m = (golden["sample_bsdf"][:, 0] == k) & same_path & ~delta & ~smooth
-        assert close(f[m], golden["sample_f"][m]) and close(pdf[m], golden["sample_pdf"][m]), f"material {k}"

@@ -10,6 +10,7 @@ import torch
 import oracle
 from pupiloptixlab_gb300 import abi, build
 from pupiloptixlab_gb300.api import GpuScene
+from _parity import assert_bit_identical
 
 pytestmark = pytest.mark.gpu
 HERE = Path(__file__).resolve().parent / "scenes"
@@ -38,11 +39,10 @@ def test_pass_equals_c_abi_render(cuda_ctx, host, name):
 @pytest.mark.parametrize("name", ["box.xml", "materials.xml"])
 def test_pass_matches_oracle(cuda_ctx, host, name):
     path = str(HERE / name)
-    img = host.run_scene(path, 4, rng=abi.RNG_PCG32)[:, :3]
+    img = host.run_scene(path, 4, rng=abi.RNG_PCG32)
     o = oracle.OracleScene(host.XmlScene(path))
-    ref = o.render(abi.RenderParams(spp=4, seed=0, accumulate=1, rng=abi.RNG_PCG32))["accum"][:, :3]
-    ok = np.all(np.abs(img - ref) <= 1e-4 * np.maximum(1.0, np.abs(ref)), axis=1)
-    assert ok.mean() > 0.97
+    ref = o.render(abi.RenderParams(spp=4, seed=0, accumulate=1, rng=abi.RNG_PCG32))["frame"]
+    assert_bit_identical(f"WavefrontPTPass {name}", img, ref)
 
 
 def test_cli_writes_pfm(host, tmp_path):

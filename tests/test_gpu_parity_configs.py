@@ -28,6 +28,7 @@ import torch
 import oracle
 from pupiloptixlab_gb300 import abi, build, scenes
 from pupiloptixlab_gb300.api import GpuScene
+from _parity import compare
 
 pytestmark = pytest.mark.gpu
 REF_SCENES = Path(__file__).resolve().parent / "golden" / "ref_scenes"
@@ -35,19 +36,6 @@ REF_SCENES = Path(__file__).resolve().parent / "golden" / "ref_scenes"
 
 def params(spp, seed=0, rng=abi.RNG_PCG32):
     return abi.RenderParams(spp=spp, max_depth=0, seed=seed, sample_cnt=0, accumulate=1, rng=rng)
-
-
-def compare(name, got, ref):
-    """Bit equality of RGBA pixels, with a report of how far off the rest are."""
-    g = got.reshape(-1, got.shape[-1])
-    r = ref.reshape(-1, ref.shape[-1])
-    same = np.all(g.view(np.uint32) == r.view(np.uint32), axis=1)
-    close = np.all(np.abs(g - r) <= 1e-4 * np.maximum(1.0, np.abs(r)), axis=1)
-    err = np.abs(g.astype(np.float64) - r.astype(np.float64)).max(axis=1)
-    worst = float(err[~same].max()) if (~same).any() else 0.0
-    print(f"{name}: {same.mean() * 100:.4f}% of {g.shape[0]} pixels bit-identical, {close.mean() * 100:.4f}% within "
-          f"1e-4, largest error elsewhere {worst:.3g}")
-    return same, close
 
 
 def rmse(a, b):
@@ -70,7 +58,7 @@ def test_cornell_config0_as_stated(cuda_ctx, rng):
     assert np.array_equal(got["albedo"].view(np.uint32), ref["albedo"].view(np.uint32))
     assert np.array_equal(got["normal"].view(np.uint32), ref["normal"].view(np.uint32))
     assert np.array_equal(got["test"].view(np.uint32), ref["test"].view(np.uint32))
-    assert got["accum"][:, :3].mean() > 0.05
+    assert got["accum"][:, :3].mean() > 0.02
 
 
 def test_config1_window_converged(cuda_ctx):
