@@ -19,6 +19,20 @@ MIS, FP32, PCG32 streams.  One step = one full 64-spp frame (132.7 M samples).
   cpu_baseline  the CPU oracle (C++ restatement of the reference integrator)
              on all host cores, on a bounded pixel subset of the same frame
 
+The default run also carries the method's other configurations, each
+measured on the same GPU after the headline (keys of the same JSON line;
+`--headline-only` skips them):
+  config0_cornell  Cornell box 256x256, 16 spp, depth 4: Msamples/s and the
+             CPU oracle on the same frame
+  batch      64 seeded scenes (10k-2M triangles, 256^2-1280x720), 16 spp,
+             depth 8: one multi-scene launch per bounce vs 64 serial renders
+  dynamic    4.1M triangles jittered per frame, 120 frames: rebuild vs refit
+             build ms, traversal Mrays/s, SAH ratio
+  denoise    the learned denoiser trained on tracer-rendered pairs (4-spp
+             inputs, 4096-spp targets, batch 16; crop and step counts cut to
+             fit, as stated in the result), then time-to-RMSE 0.01 at 1080p,
+             render + denoise vs plain accumulation, both measured directly
+
 `--impl reference` times the reference's CPU implementation of the path
 (the oracle port; the reference's OptiX/DX12 build cannot run here) on the
 same workload and metric.
@@ -70,9 +84,15 @@ def parse():
     ap.add_argument("--frames", type=int, default=120, help="frames of the dynamic workload")
     ap.add_argument("--batch-scenes", type=int, default=64, help="scenes of the multi-scene workload")
     ap.add_argument("--batch-spp", type=int, default=16)
-    ap.add_argument("--dn-pairs", type=int, default=512, help="denoiser training pairs rendered by the tracer")
-    ap.add_argument("--dn-target-spp", type=int, default=1024, help="spp of the denoiser training targets")
-    ap.add_argument("--dn-steps", type=int, default=20000, help="denoiser training steps")
+    ap.add_argument("--dn-pairs", type=int, default=256, help="denoiser training pairs rendered by the tracer "
+                    "(the learned-denoiser configuration names 4000; cut to fit the run)")
+    ap.add_argument("--dn-target-spp", type=int, default=4096, help="spp of the denoiser training targets")
+    ap.add_argument("--dn-noisy-spp", default="4", help="spp of the denoiser training inputs: one value or a "
+                    "comma-separated list drawn from per pair")
+    ap.add_argument("--dn-steps", type=int, default=6000, help="denoiser training steps (20k in the stated "
+                    "configuration; cut to fit the run)")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="default workload: skip the Cornell, multi-scene, dynamic and denoiser results")
     ap.add_argument("--dn-batch", type=int, default=16)
     ap.add_argument("--dn-crop", type=int, default=256)
     ap.add_argument("--dn-lr", type=float, default=1e-3)
@@ -261,20 +281,18 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def run_dynamic(args):
-    """800 displaced icospheres (4.1 M triangles); every frame the object-space
-    vertices are the rest positions plus seeded N(0, 0.002) noise (seed = frame),
-    then a full rebuild (PLOC clustering, or the radix tree with
-    PT_BVH_FAST_BUILD) or a refit of the initial PLOC tree, then 4 spp at
-    1920x1080, depth 6."""
+def dynamic_result(args, ctx) -> dict:
+    """Dynamic geometry: 800 displaced icospheres (4.1 M triangles); every
+    frame the object-space vertices are the rest positions plus seeded
+    N(0, 0.002) noise (seed = frame), then a full rebuild (PLOC clustering, or
+    the radix tree with PT_BVH_FAST_BUILD) or a refit of the initial PLOC
+    tree, then 4 spp at 1920x1080, depth 6."""
     import numpy as np
     import torch
 
     from pupiloptixlab_gb300 import abi, scenes
-    from pupiloptixlab_gb300.api import Context, GpuScene
-    torch.cuda.set_device(0)
+    from pupiloptixlab_gb300.api import GpuScene
     sc = scenes.icosphere_field(args.width, args.height, 6, num_instances=800, seed=1)
-    ctx = Context(0)
     g = GpuScene(ctx, sc, bvh_width=args.bvh_width, max_leaf=args.max_leaf)
     base = torch.from_numpy(np.concatenate([m.positions for m in sc.meshes]).astype(np.float32)).cuda()
     buffers = g.alloc_buffers()
@@ -302,17 +320,20 @@ def run_dynamic(args):
                      "traversal_mrays_per_s": rays / (trace_ms * 1e-3) / 1e6,
                      "render_ms_per_frame": render_ms / args.frames, "sah_cost_mean": float(np.mean(sah))}
         sah_by_frame[mode] = np.array(sah)
-    line = {"metric": "dynamic geometry: build ms, traversal Mrays/s, SAH refit/rebuild", "unit": "mixed",
-            "workload": f"800 displaced icospheres ({g.num_prims()[0]} triangles), per-frame N(0, 0.002) vertex jitter, "
+    n_tris = g.num_prims()[0]
+    g.close()
+    return {"metric": "dynamic geometry: build ms, traversal Mrays/s, SAH refit/rebuild", "unit": "mixed",
+            "workload": f"800 displaced icospheres ({n_tris} triangles), per-frame N(0, 0.002) vertex jitter, "
                         f"{args.frames} frames, 4 spp {args.width}x{args.height} depth 6, BVH{args.bvh_width}",
             "frames": args.frames, "rebuild": res["rebuild"], "rebuild_fast": res["rebuild_fast"],
             "refit": res["refit"],
             "sah_ratio_refit_over_rebuild": float(np.mean(sah_by_frame["refit"] / sah_by_frame["rebuild"])),
+            "timing": "build: CUDA events inside pt_bvh_build / pt_bvh_refit; traversal: CUDA events around every "
+                      "closest-hit and any-hit launch (PT_RENDER_KERNEL_TIMING)",
             "dtype": "f32", "data": "synthetic (seeded procedural scene)"}
-    print(json.dumps(line), flush=True)
 
 
-def run_batch(args):
+def batch_result(args, ctx) -> dict:
     """Multi-scene launches: `--batch-scenes` seeded icosphere fields with
     triangle counts log-uniform in [10k, 2M] and resolutions drawn from
     {256^2, 512^2, 1024^2, 1280x720}, `--batch-spp` spp at depth 8, rendered
@@ -321,10 +342,8 @@ def run_batch(args):
     import numpy as np
     import torch
 
-    from pupiloptixlab_gb300 import abi, scenes
-    from pupiloptixlab_gb300.api import Context, GpuScene, render_batch, render_batch_stats
-    torch.cuda.set_device(0)
-    ctx = Context(0)
+    from pupiloptixlab_gb300 import scenes
+    from pupiloptixlab_gb300.api import GpuScene, render_batch, render_batch_stats
     pool = scenes.mesh_pool(32)
     rng = np.random.default_rng(2)
     res = [(256, 256), (512, 512), (1024, 1024), (1280, 720)]
@@ -363,20 +382,69 @@ def run_batch(args):
     for i in range(max(1, args.warmup)):
         serial(i)
         batched(i)
-    t_serial = [serial(100 + i) for i in range(args.steps)]
-    t_batch = [batched(100 + i) for i in range(args.steps)]
+    steps = max(1, min(args.steps, 5))
+    t_serial = [serial(100 + i) for i in range(steps)]
+    t_batch = [batched(100 + i) for i in range(steps)]
     same = all(torch.equal(a["accum"], b["accum"]) for a, b in zip(bufs_serial, bufs_batch))
     st = render_batch_stats(ctx)
     ms_s, ms_b = statistics.median(t_serial), statistics.median(t_batch)
-    line = {"metric": "multi-scene aggregate Msamples/s (one launch per bounce vs serial renders)", "unit": "Msamples/s",
-            "value": samples / (ms_b * 1e-3) / 1e6, "serial_value": samples / (ms_s * 1e-3) / 1e6,
-            "speedup_vs_serial": ms_s / ms_b, "ms_batch": ms_b, "ms_serial": ms_s, "steps": args.steps,
-            "warmup": args.warmup, "images_identical_to_serial": bool(same), "batch_waves": st.waves,
+    for g in gs:
+        g.close()
+    return {"metric": "multi-scene aggregate Msamples/s (one launch per bounce vs serial renders)",
+            "unit": "Msamples/s", "value": samples / (ms_b * 1e-3) / 1e6,
+            "serial_value": samples / (ms_s * 1e-3) / 1e6, "speedup_vs_serial": ms_s / ms_b, "ms_batch": ms_b,
+            "ms_serial": ms_s, "steps": steps, "images_identical_to_serial": bool(same), "batch_waves": st.waves,
             "batch_kernel_launches": st.kernel_launches, "higher_is_better": True,
             "workload": f"{len(gs)} icosphere fields, {min(tris)}-{max(tris)} triangles (total {sum(tris)}), "
                         f"{pixels} pixels, {args.batch_spp} spp, depth {args.depth}, BVH{args.bvh_width}",
             "dtype": "f32", "data": "synthetic (seeded procedural scenes)"}
-    print(json.dumps(line), flush=True)
+
+
+def cornell_result(args, ctx) -> dict:
+    """The small plain configuration: procedural Cornell box, 256x256, 16 spp,
+    max depth 4, PCG32, seed 0 per step; device-timed Msamples/s (CUDA events
+    around each pt_render on the launching stream; the whole scene fits in L2,
+    which is the configuration as stated), plus the CPU oracle on all host
+    cores over the same frame."""
+    import torch
+
+    import oracle
+    from pupiloptixlab_gb300 import abi, scenes
+    from pupiloptixlab_gb300.api import GpuScene
+    W = H = 256
+    spp, depth = 16, 4
+    sc = scenes.cornell_box(W, H, max_depth=depth)
+    g = GpuScene(ctx, sc)
+    buffers = g.alloc_buffers()
+    stream = torch.cuda.current_stream()
+    for w in range(max(3, args.warmup)):
+        g.render(spp, seed=1000 + w * spp, rng=abi.RNG_PCG32, buffers=buffers)
+    torch.cuda.synchronize()
+    times = []
+    steps = max(5, args.steps)
+    for step in range(steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        g.render(spp, seed=step * spp, rng=abi.RNG_PCG32, buffers=buffers)
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    g.close()
+    samples = W * H * spp
+    out = {"metric": "Msamples/s, Cornell box 256x256 16 spp depth 4", "unit": "Msamples/s",
+           "value": samples * steps / (sum(times) * 1e-3) / 1e6, "ms_per_step": sum(times) / steps, "steps": steps,
+           "l2": "not flushed: the 34-triangle scene and its 2 MiB of frame buffers stay in L2, as the configuration "
+                 "is stated"}
+    if not args.no_cpu_baseline:
+        o = oracle.OracleScene(sc, bvh=False)
+        threads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        o.render(abi.RenderParams(spp=spp, max_depth=depth, seed=0, sample_cnt=0, accumulate=1, rng=abi.RNG_PCG32),
+                 threads=threads)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": samples / dt / 1e6, "unit": "Msamples/s", "cores": threads, "kind": "port",
+                               "sample": f"the whole 256x256 16-spp frame ({samples} samples) in {dt:.1f} s"}
+    return out
 
 
 def unet_flops(layers, n: int, h: int, w: int) -> float:
@@ -392,18 +460,201 @@ def unet_flops(layers, n: int, h: int, w: int) -> float:
     return tot
 
 
-def run_denoise(args):
+def denoise_result(args, ctx, log) -> dict:
     """Learned denoiser: training pairs rendered by the tracer (seeded
-    icosphere-field scenes, random 256^2 views, 4-spp inputs, high-spp
-    targets), Adam training with the library's tcgen05 kernels, then on the
-    1080p headline frame the time to reach RMSE 0.01 against a high-spp
-    reference, plain accumulation vs render + denoise."""
+    icosphere-field scenes, random 256^2 views, `--dn-noisy-spp` inputs,
+    `--dn-target-spp` targets), Adam training with the library's tcgen05
+    kernels (crops flipped / transposed at random each step), then on the
+    1080p headline frame the time to reach RMSE 0.01 against a 4,096-spp
+    reference, plain accumulation vs render + denoise, each measured
+    directly: plain accumulation is rendered at the smallest spp that reaches
+    the threshold (found by bisection over renders) and that render is timed;
+    render + denoise is timed at each spp of a ladder, with one network pass
+    and with the mirror-image ensemble."""
     import numpy as np
     import torch
 
     from pupiloptixlab_gb300 import abi, scenes
-    from pupiloptixlab_gb300.api import Context, GpuScene
+    from pupiloptixlab_gb300.api import GpuScene
     from pupiloptixlab_gb300.denoise_data import render_pairs
+    from pupiloptixlab_gb300.denoiser import Denoiser
+    noisy = [int(v) for v in str(args.dn_noisy_spp).split(",")]
+    inputs, targets, data_info = render_pairs(ctx, args.dn_pairs, crop=args.dn_crop, target_spp=args.dn_target_spp,
+                                              noisy_spp=noisy if len(noisy) > 1 else noisy[0], log=log)
+    dn = Denoiser(ctx, lr=args.dn_lr, seed=1)
+    B, P = args.dn_batch, args.dn_pairs
+    inp_buf = torch.empty((B,) + tuple(inputs.shape[1:]), device=inputs.device, dtype=inputs.dtype)
+    tgt_buf = torch.empty((B,) + tuple(targets.shape[1:]), device=targets.device, dtype=targets.dtype)
+    gen = torch.Generator(device="cpu").manual_seed(5)
+
+    def stage(k):
+        """Batch k: B random pairs, each flipped / transposed at random (8 variants)."""
+        idx = torch.randint(0, P, (B,), generator=gen)
+        mode = int(torch.randint(0, 8, (1,), generator=gen))
+        x, y = inputs[idx.to(inputs.device)], targets[idx.to(targets.device)]
+        if mode & 1:
+            x, y = x.flip(2), y.flip(2)
+        if mode & 2:
+            x, y = x.flip(1), y.flip(1)
+        if mode & 4:
+            x, y = x.transpose(1, 2), y.transpose(1, 2)
+        inp_buf.copy_(x)
+        tgt_buf.copy_(y)
+
+    for i in range(3):  # warm-up (graph capture)
+        stage(i)
+        dn.train_step(inp_buf, tgt_buf)
+    first_loss = dn.read_loss()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    losses, step_ms_sum = [], 0.0
+    for k in range(args.dn_steps):
+        if k % 250 == 0:  # cosine decay of the Adam step size to 5 % over the run
+            dn.set_lr(args.dn_lr * (0.05 + 0.95 * 0.5 * (1.0 + math.cos(math.pi * k / max(args.dn_steps, 1)))))
+        stage(k)
+        if k % 100 == 0:
+            e0.record()
+            dn.train_step(inp_buf, tgt_buf)
+            e1.record()
+            e1.synchronize()
+            step_ms_sum += e0.elapsed_time(e1)
+        else:
+            dn.train_step(inp_buf, tgt_buf)
+        if (k + 1) % 500 == 0:
+            losses.append((k + 1, dn.read_loss()))
+    torch.cuda.synchronize()
+    step_ms = step_ms_sum / max(1, (args.dn_steps + 99) // 100)
+    flops = unet_flops(dn.layers, B, args.dn_crop, args.dn_crop)
+    pk_file = ROOT / "MEASURED_PEAKS.json"
+    bf16_peak, bf16_src = (float(json.loads(pk_file.read_text())["bf16_tflops_sustained"]), "measured") \
+        if pk_file.exists() else (1700.0, "fallback")
+    tf = flops / (step_ms * 1e-3) / 1e12
+    log(f"denoiser trained: {args.dn_steps} steps, {step_ms:.3f} ms/step, {tf:.1f} TFLOP/s, losses {losses[-3:]}")
+    del inputs, targets
+
+    # evaluation on the 1080p headline frame
+    W, H = args.width, args.height
+    sc = scenes.icosphere_field(W, H, args.depth)
+    g = GpuScene(ctx, sc, bvh_width=args.bvh_width, max_leaf=args.max_leaf)
+    flags = abi.RENDER_DROP_NONFINITE
+    buf = g.alloc_buffers()
+
+    def timed_render(spp, seed):
+        torch.cuda.synchronize()
+        a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        g.render(spp=spp, seed=seed, flags=flags, buffers=buf)
+        z.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(z) * 1e-3
+
+    g.render(spp=8, seed=0, flags=flags, buffers=buf)  # warm-up (graph capture)
+    ref_s = timed_render(args.dn_ref_spp, 1 << 22)
+    R = buf["accum"][:, :3].clone()
+    thr = 0.01
+
+    def rmse(x):
+        x = x[:, :3]
+        lin = float((x.clamp(0, 1) - R.clamp(0, 1)).pow(2).mean().sqrt())
+        lg = float((torch.log1p(x.clamp(min=0)) - torch.log1p(R.clamp(min=0))).pow(2).mean().sqrt())
+        return lin, lg
+
+    plain_cache = {}
+
+    def plain(spp):
+        if spp not in plain_cache:
+            t = timed_render(spp, 0)
+            plain_cache[spp] = {"spp": spp, "s": t, "rmse": rmse(buf["accum"])}
+        return plain_cache[spp]
+
+    def plain_time_to(k):
+        """Smallest spp whose plain render reaches thr in space k, found by
+        doubling and then bisection over renders; its measured render time."""
+        hi = 1
+        while plain(hi)["rmse"][k] > thr:
+            if hi >= args.dn_ref_spp // 2:
+                return None
+            hi *= 2
+        lo = hi // 2
+        while hi - lo > 1:
+            mid = (lo + hi) // 2
+            if plain(mid)["rmse"][k] <= thr:
+                hi = mid
+            else:
+                lo = mid
+        return plain(hi)
+
+    out = {}
+    plain_best = {0: plain_time_to(0), 1: plain_time_to(1)}
+    den = []
+    ladder = (1, 2, 4, 8, 12, 16, 24, 32, 48, 64, 80, 96, 128, 160, 192, 256)
+    for spp in ladder:
+        t = timed_render(spp, 0)
+        row = {"spp": spp, "render_s": t, "rmse_input": rmse(buf["accum"])}
+        for ens, key in ((False, "single"), (True, "ensemble")):
+            dn.denoise(buf, W, H, ensemble=ens)  # warm
+            o, st, _ = dn.denoise(buf, W, H, ensemble=ens)
+            row[key] = {"s": t + st.last_ms * 1e-3, "denoise_ms": st.last_ms, "rmse": rmse(o),
+                        "fallback_tiles": st.fallback_tiles, "tiles": st.tiles}
+        den.append(row)
+        if row["single"]["rmse"][0] <= thr and row["single"]["rmse"][1] <= thr and \
+                row["ensemble"]["rmse"][0] <= thr and row["ensemble"]["rmse"][1] <= thr:
+            break
+    for k, name in ((0, "display_clamped"), (1, "log1p")):
+        pb = plain_best[k]
+        entry = {"plain_s": pb["s"] if pb else None, "plain_spp": pb["spp"] if pb else None}
+        for key in ("single", "ensemble"):
+            hits = [(r[key]["s"], r["spp"]) for r in den if r[key]["rmse"][k] <= thr]
+            td, sd = min(hits) if hits else (None, None)
+            entry[f"{key}_s"] = td
+            entry[f"{key}_spp"] = sd
+            entry[f"{key}_speedup"] = (pb["s"] / td) if (pb and td) else None
+        out[name] = entry
+    g.close()
+    best = out["display_clamped"]
+    return {"metric": "denoiser: time-to-RMSE 0.01 at 1080p, render+denoise vs plain accumulation", "unit": "s",
+            "value": best["ensemble_s"], "higher_is_better": False,
+            "speedup_single_pass": best["single_speedup"], "speedup_ensemble": best["ensemble_speedup"],
+            "time_to_rmse_0.01": out, "rmse_spaces": {"display_clamped": "RGB clamped to [0,1], linear",
+                                                      "log1p": "log(1 + RGB)"},
+            "reference_image": {"spp": args.dn_ref_spp, "render_s": ref_s},
+            "plain_curve": sorted(plain_cache.values(), key=lambda c: c["spp"]), "denoised_curve": den,
+            "training": {"data": data_info, "steps": args.dn_steps, "batch": B, "crop": args.dn_crop,
+                         "augmentation": "each batch: random pairs, one of 8 flips/transposes",
+                         "step_ms": step_ms, "flops_per_step": flops, "tflops": tf,
+                         "first_loss": first_loss, "losses": losses,
+                         "cut_from_stated": f"{args.dn_pairs} of 4000 crops, {args.dn_steps} of 20000 steps"},
+            "roofline": {"bound": "tensor", "achieved": tf, "peak": bf16_peak, "peak_source": bf16_src,
+                         "unit": "TFLOP/s", "frac": tf / bf16_peak, "traffic": None,
+                         "note": "whole training step (14 convolutions x forward, data and weight gradients, "
+                                 "pooling, up-sampling, loss, Adam) over its algorithmic convolution FLOPs; "
+                                 "peak = sustained cuBLAS bf16"},
+            "workload": f"U-Net 5 levels 32-256 ch, {dn.num_params} params, batch {B} x {args.dn_crop}^2, inputs "
+                        f"{args.dn_noisy_spp} spp, targets {args.dn_target_spp} spp; eval on the {W}x{H} icosphere "
+                        f"field vs a {args.dn_ref_spp}-spp reference",
+            "dtype": "bf16 (fp32 accumulate)", "data": "synthetic (rendered by the tracer from seeded scenes)"}
+
+
+def run_dynamic(args):
+    import torch
+
+    from pupiloptixlab_gb300.api import Context
+    torch.cuda.set_device(0)
+    print(json.dumps(dynamic_result(args, Context(0))), flush=True)
+
+
+def run_batch(args):
+    import torch
+
+    from pupiloptixlab_gb300.api import Context
+    torch.cuda.set_device(0)
+    print(json.dumps(batch_result(args, Context(0))), flush=True)
+
+
+def run_denoise(args):
+    import torch
+
+    from pupiloptixlab_gb300.api import Context
     from pupiloptixlab_gb300.denoiser import Denoiser
     torch.cuda.set_device(0)
     ctx = Context(0)
@@ -429,119 +680,7 @@ def run_denoise(args):
                           "tflops": flops / (step_ms * 1e-3) / 1e12, "steps": args.dn_steps,
                           "batch": args.dn_batch, "crop": args.dn_crop, "loss": dn.read_loss()}), flush=True)
         return
-    inputs, targets, data_info = render_pairs(ctx, args.dn_pairs, crop=args.dn_crop, target_spp=args.dn_target_spp,
-                                              noisy_spp=(1, 2, 4, 4, 8, 16, 32, 64, 128, 256), log=log)
-    dn = Denoiser(ctx, lr=args.dn_lr, seed=1)
-    B, P = args.dn_batch, args.dn_pairs
-    nb = P // B
-    batches = [(inputs[i * B:(i + 1) * B], targets[i * B:(i + 1) * B]) for i in range(nb)]
-    for i in range(3):  # warm-up (graph capture)
-        dn.train_step(*batches[i % nb])
-    first_loss = dn.read_loss()
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    losses = []
-    e0.record()
-    for k in range(args.dn_steps):
-        if k % 250 == 0:  # cosine decay of the Adam step size to 5 % over the run
-            dn.set_lr(args.dn_lr * (0.05 + 0.95 * 0.5 * (1.0 + math.cos(math.pi * k / max(args.dn_steps, 1)))))
-        dn.train_step(*batches[k % nb])
-        if (k + 1) % 500 == 0:
-            losses.append((k + 1, dn.read_loss()))
-    e1.record()
-    torch.cuda.synchronize()
-    train_ms = e0.elapsed_time(e1)
-    step_ms = train_ms / max(args.dn_steps, 1)
-    flops = unet_flops(dn.layers, B, args.dn_crop, args.dn_crop)
-    pk_file = ROOT / "MEASURED_PEAKS.json"
-    bf16_peak, bf16_src = (float(json.loads(pk_file.read_text())["bf16_tflops_sustained"]), "measured") \
-        if pk_file.exists() else (1700.0, "fallback")
-    tf = flops / (step_ms * 1e-3) / 1e12
-    log(f"denoiser trained: {args.dn_steps} steps, {step_ms:.3f} ms/step, {tf:.1f} TFLOP/s, losses {losses[-3:]}")
-
-    # evaluation on the 1080p headline frame
-    W, H = args.width, args.height
-    sc = scenes.icosphere_field(W, H, args.depth)
-    g = GpuScene(ctx, sc, bvh_width=args.bvh_width, max_leaf=args.max_leaf)
-    flags = abi.RENDER_DROP_NONFINITE
-
-    def timed_render(spp, seed):
-        b = g.alloc_buffers()
-        torch.cuda.synchronize()
-        a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record()
-        g.render(spp=spp, seed=seed, flags=flags, buffers=b)
-        z.record()
-        torch.cuda.synchronize()
-        return b, a.elapsed_time(z) * 1e-3
-
-    ref, ref_s = timed_render(args.dn_ref_spp, 1 << 22)
-    R = ref["accum"][:, :3].clone()
-
-    def rmse(x):
-        x = x[:, :3]
-        lin = float((x.clamp(0, 1) - R.clamp(0, 1)).pow(2).mean().sqrt())
-        lg = float((torch.log1p(x.clamp(min=0)) - torch.log1p(R.clamp(min=0))).pow(2).mean().sqrt())
-        return lin, lg
-
-    plain = []
-    for spp in (1, 4, 16, 64, 256, 1024):
-        b, t = timed_render(spp, 0)
-        plain.append({"spp": spp, "s": t, "rmse": rmse(b["accum"])})
-    den = []
-    ensemble = not args.dn_single_pass
-    for spp in (1, 2, 4, 8, 16, 32, 48, 64, 80, 96, 112, 128):
-        b, t = timed_render(spp, 0)
-        dn.denoise(b, W, H, ensemble=ensemble)  # warm
-        out, st, _ = dn.denoise(b, W, H, ensemble=ensemble)
-        den.append({"spp": spp, "s": t + st.last_ms * 1e-3, "render_s": t, "denoise_ms": st.last_ms,
-                    "rmse": rmse(out), "rmse_input": rmse(b["accum"]), "fallback_tiles": st.fallback_tiles,
-                    "tiles": st.tiles})
-
-    def time_to(curve, k, thr=0.01, model=False):
-        """Denoised: the fastest measured point at or below thr.  Plain
-        accumulation (model=True): its MSE against the reference is
-        a / spp + a / ref_spp; a is fitted at the last point above thr (or the
-        last point), the spp that reaches thr is solved for and timed at the
-        per-spp rate of the nearest measured point above it."""
-        if not model:
-            hits = [c["s"] for c in curve if c["rmse"][k] <= thr]
-            return (min(hits), None) if hits else (None, None)
-        above = [c for c in curve if c["rmse"][k] > thr] or [curve[-1]]
-        fit = above[-1]
-        s, m = fit["spp"], fit["rmse"][k] ** 2
-        a = m * s * args.dn_ref_spp / (args.dn_ref_spp + s)
-        if thr * thr <= a / args.dn_ref_spp:
-            return None, None
-        need = a / (thr * thr - a / args.dn_ref_spp)
-        rate = [c for c in curve if c["spp"] >= need] or [curve[-1]]
-        return rate[0]["s"] / rate[0]["spp"] * need, need
-
-    out = {}
-    for k, name in ((0, "display_clamped"), (1, "log1p")):
-        tp, need = time_to(plain, k, model=True)
-        td, _ = time_to(den, k)
-        out[name] = {"plain_s": tp, "plain_spp_needed": need, "denoised_s": td,
-                     "speedup": (tp / td) if (tp and td) else None}
-    line = {"metric": "denoiser: time-to-RMSE 0.01 at 1080p, render+denoise vs plain accumulation", "unit": "s",
-            "value": out["display_clamped"]["denoised_s"], "higher_is_better": False,
-            "time_to_rmse_0.01": out, "rmse_spaces": {"display_clamped": "RGB clamped to [0,1], linear",
-                                                      "log1p": "log(1 + RGB)"},
-            "reference_image": {"spp": args.dn_ref_spp, "render_s": ref_s},
-            "plain_curve": plain, "denoised_curve": den,
-            "training": {"data": data_info, "steps": args.dn_steps, "batch": B, "crop": args.dn_crop,
-                         "step_ms": step_ms, "flops_per_step": flops, "tflops": tf,
-                         "first_loss": first_loss, "losses": losses},
-            "roofline": {"bound": "tensor", "achieved": tf, "peak": bf16_peak, "peak_source": bf16_src,
-                         "unit": "TFLOP/s", "frac": tf / bf16_peak, "traffic": None,
-                         "note": "whole training step (14 convolutions x forward, data and weight gradients, "
-                                 "pooling, up-sampling, loss, Adam) over its algorithmic convolution FLOPs; "
-                                 "peak = sustained cuBLAS bf16"},
-            "workload": f"U-Net 5 levels 32-256 ch, {dn.num_params} params, batch {B} x {args.dn_crop}^2; "
-                        f"eval on the {W}x{H} icosphere field, "
-                        f"{'frame + mirror-image ensemble' if ensemble else 'one network pass'} per denoise",
-            "dtype": "bf16 (fp32 accumulate)", "data": "synthetic (rendered by the tracer from seeded scenes)"}
-    print(json.dumps(line), flush=True)
+    print(json.dumps(denoise_result(args, ctx, log)), flush=True)
 
 
 def main():
@@ -709,6 +848,26 @@ def main():
                 "builder": "ploc" if bst.builder == abi.BVH_BUILDER_PLOC else "radix tree"},
         "cpu_baseline": cpu,
     }
+    if ws == 1 and args.workload == "headline" and not args.headline_only:
+        # the other configurations of the same method, on the same GPU, after
+        # the headline measurement: the small plain case, multi-scene
+        # launches, dynamic geometry and the learned denoiser
+        g.close()
+        del buffers, flush
+        torch.cuda.empty_cache()
+        log = lambda m: print(m, file=sys.stderr, flush=True)  # noqa: E731
+        for key, fn in (("config0_cornell", lambda: cornell_result(args, ctx)),
+                        ("batch", lambda: batch_result(args, ctx)),
+                        ("dynamic", lambda: dynamic_result(args, ctx)),
+                        ("denoise", lambda: denoise_result(args, ctx, log))):
+            t0 = time.perf_counter()
+            try:
+                line[key] = fn()
+            except Exception as e:  # one failing part must not lose the headline line
+                line[key] = {"error": repr(e)}
+            line[key]["wall_s"] = time.perf_counter() - t0
+            log(f"{key}: done in {line[key]['wall_s']:.1f} s")
+            torch.cuda.empty_cache()
     print(json.dumps(line), flush=True)
 
 
