@@ -28,9 +28,9 @@ measured on the same GPU after the headline (keys of the same JSON line;
              depth 8: one multi-scene launch per bounce vs 64 serial renders
   dynamic    4.1M triangles jittered per frame, 120 frames: rebuild vs refit
              build ms, traversal Mrays/s, SAH ratio
-  denoise    the learned denoiser trained on tracer-rendered pairs (4-spp
-             inputs, 4096-spp targets, batch 16; crop and step counts cut to
-             fit, as stated in the result), then time-to-RMSE 0.01 at 1080p,
+  denoise    the learned denoiser trained on tracer-rendered pairs (inputs of
+             1-128 spp, 4096-spp targets, batch 16; crop and step counts cut
+             to fit, as stated in the result), then time-to-RMSE 0.01 at 1080p,
              render + denoise vs plain accumulation, both measured directly
 
 `--impl reference` times the reference's CPU implementation of the path
@@ -87,8 +87,10 @@ def parse():
     ap.add_argument("--dn-pairs", type=int, default=256, help="denoiser training pairs rendered by the tracer "
                     "(the learned-denoiser configuration names 4000; cut to fit the run)")
     ap.add_argument("--dn-target-spp", type=int, default=4096, help="spp of the denoiser training targets")
-    ap.add_argument("--dn-noisy-spp", default="4", help="spp of the denoiser training inputs: one value or a "
-                    "comma-separated list drawn from per pair")
+    ap.add_argument("--dn-noisy-spp", default="1,2,4,8,16,32,64,128",
+                    help="spp of the denoiser training inputs: one value or a comma-separated list drawn from per "
+                         "pair (inputs of 4 spp alone leave the network at RMSE 0.016 on higher-spp frames: it "
+                         "never reaches 0.01)")
     ap.add_argument("--dn-steps", type=int, default=6000, help="denoiser training steps (20k in the stated "
                     "configuration; cut to fit the run)")
     ap.add_argument("--headline-only", action="store_true",
@@ -155,8 +157,9 @@ def measured_peaks():
 
 
 def committed_traffic(workload: str = "headline"):
-    """DRAM bytes per launch of the closest-hit kernel from the committed ncu
-    summary of the same workload."""
+    """DRAM bytes per closest-hit ray, cache hit rates and throughputs of the
+    closest-hit kernel from the committed ncu summary of a small case of the
+    same workload (profiles/extend_traffic*.json)."""
     p = ROOT / "profiles" / ("extend_traffic.json" if workload == "headline" else f"extend_traffic_{workload}.json")
     if p.exists():
         try:
@@ -808,6 +811,9 @@ def main():
     achieved = per_launch_bytes / avg_launch_s / 1e9 if ext_ms > 0 else None
     peak, peak_kind = measured_peaks()
     traffic = committed_traffic(args.workload) if args.at_capture_config else None
+    # DRAM traffic per launch: the small case's DRAM bytes per ray times this
+    # workload's closest-hit rays per launch
+    traffic_per_launch = (traffic["dram_bytes_per_ray"] * cst.extension_rays / launches_per_step) if traffic else None
     cpu = None
     if not args.no_cpu_baseline:
         cpu = cpu_baseline(sc, 0, args.cpu_seconds, args.depth)
@@ -827,14 +833,20 @@ def main():
         "clocks": clk,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None,
-                     "traffic": traffic.get("dram_bytes_per_launch") if traffic else None,
+                     "traffic": traffic_per_launch,
+                     "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum per closest-hit ray on the "
+                                        "2-spp case of this workload (profiles/extend_traffic.json), times this "
+                                        "launch's rays") if traffic else None,
                      "kernel": "k_trace_queue closest hit (extend)",
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else
                      "fallback 6.8 TB/s",
                      "algorithmic_bytes_per_ray": ext_bytes / max(1, cst.extension_rays),
-                     "dram_bytes_per_ray": (traffic["dram_bytes_per_launch"] * launches_per_step
-                                            / max(1, cst.extension_rays)) if traffic else None,
+                     "dram_bytes_per_ray": traffic["dram_bytes_per_ray"] if traffic else None,
                      "l2_hit_rate_pct": traffic.get("lts_sector_hit_rate_pct") if traffic else None,
+                     "l1_hit_rate_pct": traffic.get("l1tex_sector_hit_rate_pct") if traffic else None,
+                     "l1_throughput_pct_of_peak": traffic.get("l1tex_throughput_pct_of_peak") if traffic else None,
+                     "l2_throughput_pct_of_peak": traffic.get("lts_throughput_pct_of_peak") if traffic else None,
+                     "active_lanes_of_32": traffic.get("active_lanes_per_warp_instruction") if traffic else None,
                      "nodes_per_ray": cst.nodes_visited / max(1, cst.extension_rays),
                      "prims_per_ray": cst.prims_tested / max(1, cst.extension_rays),
                      "extend_ms_per_step": ext_ms / args.steps, "shadow_ms_per_step": sh_ms / args.steps,

@@ -21,8 +21,7 @@ def test_default_run_is_the_captured_configuration(monkeypatch):
     w = bench.headline_workload(a)
     assert w.startswith("1M-triangle") and "200 x 5120" in w and "1920x1080, 64 spp, max depth 8" in w
     t = bench.committed_traffic("headline")
-    assert t and t["dram_bytes_per_launch"] > 0 and t["passes"] == 1
-    assert bench.committed_traffic("hair")["dram_bytes_per_launch"] > 0
+    assert t and t["dram_bytes_per_ray"] > 0 and "--spp 2" in t["command"]
 
 
 def test_other_configurations_get_no_committed_traffic(monkeypatch):
