@@ -418,26 +418,34 @@ struct Loader {
         return m;
     }
     static Mesh cube() {
+        // Faces in the reference's order (-X, -Z, +X, +Z, +Y, -Y), each with
+        // its four corners counter-clockwise seen from outside, uv (0,0) (1,0)
+        // (1,1) (0,1) and triangles (0,1,2) (0,2,3): the vertex order, and so
+        // the quad diagonals, primitive ids, barycentrics and uvs, are the
+        // reference's built-in cube's.
+        struct Face {
+            float n[3];
+            float c[4][3];
+        };
+        static const Face faces[6] = {
+            {{-1, 0, 0}, {{-1, -1, -1}, {-1, -1, 1}, {-1, 1, 1}, {-1, 1, -1}}},
+            {{0, 0, -1}, {{1, -1, -1}, {-1, -1, -1}, {-1, 1, -1}, {1, 1, -1}}},
+            {{1, 0, 0}, {{1, -1, 1}, {1, -1, -1}, {1, 1, -1}, {1, 1, 1}}},
+            {{0, 0, 1}, {{-1, -1, 1}, {1, -1, 1}, {1, 1, 1}, {-1, 1, 1}}},
+            {{0, 1, 0}, {{-1, 1, 1}, {1, 1, 1}, {1, 1, -1}, {-1, 1, -1}}},
+            {{0, -1, 0}, {{-1, -1, -1}, {1, -1, -1}, {1, -1, 1}, {-1, -1, 1}}},
+        };
+        static const float uv[4][2] = {{0, 0}, {1, 0}, {1, 1}, {0, 1}};
         Mesh m;
-        for (int axis = 0; axis < 3; axis++)
-            for (int sgn = -1; sgn <= 1; sgn += 2) {
-                float n[3] = {0, 0, 0}, u[3] = {0, 0, 0}, v[3];
-                n[axis] = (float)sgn;
-                u[(axis + 1) % 3] = 1.f;
-                v[0] = n[1] * u[2] - n[2] * u[1];
-                v[1] = n[2] * u[0] - n[0] * u[2];
-                v[2] = n[0] * u[1] - n[1] * u[0];
-                uint32_t base = (uint32_t)m.positions.size() / 3;
-                const float su[4] = {-1, 1, 1, -1}, sv[4] = {-1, -1, 1, 1};
-                for (int k = 0; k < 4; k++) {
-                    for (int i = 0; i < 3; i++) m.positions.push_back(n[i] + su[k] * u[i] + sv[k] * v[i]);
-                    for (int i = 0; i < 3; i++) m.normals.push_back(n[i]);
-                    m.texcoords.push_back(su[k] * 0.5f + 0.5f);
-                    m.texcoords.push_back(sv[k] * 0.5f + 0.5f);
-                }
-                const uint32_t idx[6] = {0, 1, 2, 0, 2, 3};
-                for (uint32_t i : idx) m.indices.push_back(base + i);
+        for (const Face &f : faces) {
+            const uint32_t base = (uint32_t)m.positions.size() / 3;
+            for (int k = 0; k < 4; k++) {
+                m.positions.insert(m.positions.end(), f.c[k], f.c[k] + 3);
+                m.normals.insert(m.normals.end(), f.n, f.n + 3);
+                m.texcoords.insert(m.texcoords.end(), uv[k], uv[k] + 2);
             }
+            for (uint32_t i : {0u, 1u, 2u, 0u, 2u, 3u}) m.indices.push_back(base + i);
+        }
         return m;
     }
 
