@@ -552,6 +552,17 @@ int pt_conv3x3_backward_data(const void *dy, uint32_t n, uint32_t h, uint32_t w,
                              uint32_t cin, const void *mask, void *dx, void *stream);
 int pt_conv3x3_backward_weights(const void *x, uint32_t n, uint32_t h, uint32_t w, uint32_t cin, const void *dy,
                                 uint32_t cout, float *dweight, float *dbias, void *stream);
+/* Bounded waits of the convolution kernels (no counterpart in the reference,
+ * whose closed OptiX denoiser has none): every mbarrier wait gives up after
+ * wait_ns of GPU time (0 restores the default, 2 s); the kernel then records
+ * an error, lets the copies and MMAs it issued finish, frees its tensor memory
+ * and returns, and the call reports PT_ERR_TIMEOUT.  stall_next = 1 makes the
+ * next forward convolution that is prepared first wait on a barrier that
+ * nothing arrives at, so that this path can be tested without a fault.
+ * Process-wide; applies to convolutions prepared after the call (the
+ * denoiser's training and inference graphs keep the limit they were built
+ * with). */
+int pt_conv_set_wait_limit(uint64_t wait_ns, uint32_t stall_next);
 
 /* ---- host helpers (no GPU needed) ------------------------------------- */
 /* Camera matrices from a mitsuba-style sensor: fov_y in degrees,

@@ -177,6 +177,7 @@ PROTOTYPES = [
     ("pt_bsdf_eval_batch", C.c_int, [C.c_void_p] * 5 + [C.c_uint32, C.c_void_p]),
     ("pt_bsdf_sample_batch", C.c_int, [C.c_void_p] * 7 + [C.c_uint32, C.c_void_p]),
     ("pt_trig_eval", C.c_int, [C.c_uint32] + [C.c_void_p] * 4 + [C.c_uint32, C.c_void_p]),
+    ("pt_conv_set_wait_limit", C.c_int, [C.c_uint64, C.c_uint32]),
     ("pt_denoiser_create", C.c_int, [C.c_void_p, C.POINTER(DenoiserOpts), C.POINTER(C.c_void_p)]),
     ("pt_denoiser_destroy", None, [C.c_void_p]),
     ("pt_denoiser_num_params", C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),

@@ -35,6 +35,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -83,13 +84,17 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-// Bounded wait for the phase with the given parity to complete.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, bool backoff = false) {
+// Bounded wait for the phase with the given parity to complete: false after
+// limit_ns of %globaltimer, or as soon as *abort is set (another warp of the
+// CTA gave up), so that a failing CTA leaves within one limit.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, bool backoff = false,
+                                          uint64_t limit_ns = kWaitNs, const volatile int *abort = nullptr) {
     if (mbar_try(bar, parity)) return true;
     const uint64_t t0 = gtimer();
     while (!mbar_try(bar, parity)) {
         if (backoff) __nanosleep(128);
-        if (gtimer() - t0 > kWaitNs) return false;
+        if (gtimer() - t0 > limit_ns) return false;
+        if (abort && *abort) return false;
     }
     return true;
 }
@@ -269,7 +274,7 @@ __global__ void __launch_bounds__(192, 1)
     constexpr int R = KC * 2;
     constexpr uint32_t SWZ = swz_mode<KC>();
     extern __shared__ uint8_t smem_raw[];
-    __shared__ __align__(8) uint64_t bars[2 * kMaxStages + 5];
+    __shared__ __align__(8) uint64_t bars[2 * kMaxStages + 7];
     __shared__ uint32_t tmem_slot;
     __shared__ int s_fail;
 
@@ -292,6 +297,9 @@ __global__ void __launch_bounds__(192, 1)
     auto acc_full = [&](int b) { return bar0 + 8u * (2 * kMaxStages + b); };
     auto acc_empty = [&](int b) { return bar0 + 8u * (2 * kMaxStages + 2 + b); };
     const uint32_t wbar = bar0 + 8u * (2 * kMaxStages + 4);  // resident weights landed
+    const uint32_t sbar = bar0 + 8u * (2 * kMaxStages + 5);  // never arrived at: the stall test waits on it
+    const uint32_t mdone = bar0 + 8u * (2 * kMaxStages + 6);  // MMAs of a failing CTA completed
+    const uint64_t lim = a.wait_ns;
     auto tile_of = [&](int t, int &img, int &x0, int &y0, int &n0) {
         const int pt = t / n_n;
         n0 = (t - pt * n_n) * a.n_tile;
@@ -312,6 +320,8 @@ __global__ void __launch_bounds__(192, 1)
             mbar_init(acc_empty(b), 128);
         }
         mbar_init(wbar, 1);
+        mbar_init(sbar, 1);
+        mbar_init(mdone, 1);
         mbar_fence_init();
         s_fail = 0;
     }
@@ -336,7 +346,7 @@ __global__ void __launch_bounds__(192, 1)
                 tile_of(t, img, x0, y0, n0);
                 for (int k = 0; k < nk; k++, kg++) {
                     const int s = kg % S;
-                    if (kg >= S && !mbar_wait(empty(s), ((kg / S) - 1) & 1)) {
+                    if (kg >= S && !mbar_wait(empty(s), ((kg / S) - 1) & 1, false, lim, fail)) {
                         record_error(a.err, 1u);
                         *fail = 1;
                         break;
@@ -357,23 +367,28 @@ __global__ void __launch_bounds__(192, 1)
                     }
                 }
             }
-            // drain: wait until every issued stage has been consumed and the
-            // resident weights (if any) have landed
+            // drain: every copy this thread issued has landed before the CTA
+            // leaves (the last issue on each ring slot, and the resident
+            // weights), also when another warp gave up; within the normal limit
             for (int k = kg - S; k < kg; k++)
-                if (k >= 0) (void)mbar_wait(empty(k % S), (k / S) & 1, true);
+                if (k >= 0) (void)mbar_wait(full(k % S), (k / S) & 1, true);
             if (wres) (void)mbar_wait(wbar, 0, true);
         }
     } else if (warp == 1) {
         if (lane == 0) {  // MMA issuer
             const uint32_t idesc = idesc_bf16(128, a.n_tile, false, false);
-            if (wres && !mbar_wait(wbar, 0)) {
+            if (a.stall && !mbar_wait(sbar, 0, true, lim)) {  // the stall test: this wait always runs out
+                record_error(a.err, 2u);
+                *fail = 1;
+            }
+            if (wres && !*fail && !mbar_wait(wbar, 0, false, lim, fail)) {
                 record_error(a.err, 2u);
                 *fail = 1;
             }
             int kg = 0, j = 0;
             for (int t = blockIdx.x; t < total && !*fail; t += gridDim.x, j++) {
                 const int buf = j & 1;
-                if (!mbar_wait(acc_empty(buf), ((j >> 1) & 1) ^ 1)) {  // epilogue of tile j - 2 done
+                if (!mbar_wait(acc_empty(buf), ((j >> 1) & 1) ^ 1, false, lim, fail)) {  // epilogue of tile j - 2 done
                     record_error(a.err, 2u);
                     *fail = 1;
                     break;
@@ -382,7 +397,7 @@ __global__ void __launch_bounds__(192, 1)
                 const uint32_t d = tmem + static_cast<uint32_t>(buf * a.n_tile);
                 for (int k = 0; k < nk; k++, kg++) {
                     const int s = kg % S;
-                    if (!mbar_wait(full(s), (kg / S) & 1)) {
+                    if (!mbar_wait(full(s), (kg / S) & 1, false, lim, fail)) {
                         record_error(a.err, 2u);
                         *fail = 1;
                         break;
@@ -411,6 +426,10 @@ __global__ void __launch_bounds__(192, 1)
                 if (*fail) break;
                 umma_commit(acc_full(buf));
             }
+            if (*fail && kg > 0) {  // let the MMAs already issued finish before tensor memory is freed
+                umma_commit(mdone);
+                (void)mbar_wait(mdone, 0, true);
+            }
         }
     } else {  // epilogue warps 2-5
         const int quad = warp & 3;
@@ -418,7 +437,7 @@ __global__ void __launch_bounds__(192, 1)
         int j = 0;
         for (int t = blockIdx.x; t < total; t += gridDim.x, j++) {
             const int buf = j & 1;
-            const bool ok = mbar_wait(acc_full(buf), (j >> 1) & 1, true);
+            const bool ok = mbar_wait(acc_full(buf), (j >> 1) & 1, true, lim, fail);
             if (!ok) {
                 if (row == 0) record_error(a.err, 4u);
                 break;
@@ -496,7 +515,7 @@ __global__ void __launch_bounds__(128, 1)
         int k = 0;
         for (; k < nk; k++) {
             const int s = k % S;
-            if (k >= S && !mbar_wait(empty(s), ((k / S) - 1) & 1)) {
+            if (k >= S && !mbar_wait(empty(s), ((k / S) - 1) & 1, false, a.wait_ns)) {
                 record_error(a.err, 1u);
                 s_fail = 1;
                 break;
@@ -521,7 +540,7 @@ __global__ void __launch_bounds__(128, 1)
         int k = 0;
         for (; k < nk; k++) {
             const int s = k % S;
-            if (!mbar_wait(full(s), (k / S) & 1)) {
+            if (!mbar_wait(full(s), (k / S) & 1, false, a.wait_ns)) {
                 record_error(a.err, 2u);
                 s_fail = 1;
                 break;
@@ -540,7 +559,7 @@ __global__ void __launch_bounds__(128, 1)
         umma_commit(done);
     }
     __syncwarp();
-    const bool ok = nk > 0 && mbar_wait(done, 0, true);
+    const bool ok = nk > 0 && mbar_wait(done, 0, true, a.wait_ns);
     if (!ok && nk > 0 && tid == 0) record_error(a.err, 4u);
     tc_fence_after();
 
@@ -752,6 +771,20 @@ int pick_kc(int c) {
     return 16;
 }
 
+// Limit of the kernels' bounded waits (pt_conv_set_wait_limit; 0 = kWaitNs)
+// and the one-shot request to stall the next forward convolution.
+static std::atomic<unsigned long long> g_wait_ns{0};
+static std::atomic<int> g_stall_next{0};
+unsigned long long wait_limit_ns() {
+    const unsigned long long v = g_wait_ns.load();
+    return v ? v : kWaitNs;
+}
+bool take_stall_request() { return g_stall_next.exchange(0) != 0; }
+void set_wait_limit(unsigned long long ns, bool stall_next) {
+    g_wait_ns.store(ns);
+    g_stall_next.store(stall_next ? 1 : 0);
+}
+
 int fwd_prepare(FwdOp *op, const Act &in, const void *w, int w_rows, int cout, const float *bias, int epi, int relu,
                 void *out, int out_ctot, int out_coff, const Act *mask, unsigned *err) {
     if (in.c <= 0 || in.c % 16 || cout <= 0 || in.n <= 0 || in.h <= 0 || in.w <= 0) {
@@ -822,6 +855,8 @@ int fwd_prepare(FwdOp *op, const Act &in, const void *w, int w_rows, int cout, c
         a.mask_coff = mask->coff;
     }
     a.err = err;
+    a.wait_ns = wait_limit_ns();
+    a.stall = take_stall_request() ? 1 : 0;
     op->kc = kc;
     op->halo = halo;
     op->smem = smem_request(a.stages, a.stage_bytes, a.tmem_cols) + a.wres_bytes;
@@ -896,6 +931,7 @@ int wgrad_prepare(WgradOp *op, const Act &x, const Act &gy, float *dw, int num_s
     splits = (a.total_tiles + a.tiles_per_split - 1) / a.tiles_per_split;
     a.dw = dw;
     a.err = err;
+    a.wait_ns = wait_limit_ns();
     op->kca = kca;
     op->kcb = kcb;
     op->grid = dim3(static_cast<unsigned>(m_tiles), static_cast<unsigned>(ntiles), static_cast<unsigned>(splits));

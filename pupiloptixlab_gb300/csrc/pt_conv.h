@@ -49,6 +49,8 @@ struct FwdArgs {
     const uint16_t *mask;
     int mask_ctot, mask_coff;
     unsigned *err;
+    unsigned long long wait_ns;  // limit of every bounded wait (kWaitNs unless pt_conv_set_wait_limit changed it)
+    int stall;                   // test of the timeout path: the MMA warp first waits on a barrier nothing arrives at
 };
 
 struct WgradArgs {
@@ -61,6 +63,7 @@ struct WgradArgs {
     int zero_fill;        // pixel tiles smaller than 128: clear the stages once
     float *dw;            // [cout][9][cin] FP32, accumulated
     unsigned *err;
+    unsigned long long wait_ns;
 };
 
 struct FwdOp {
@@ -88,6 +91,14 @@ int pick_kc(int c);
 // in bf16 (rows beyond w_rows read as zero); `cout` output channels are
 // written to channels [out_coff, out_coff + cout) of `out` (out_ctot channels,
 // same n/h/w as `in`).  `mask` (EPI_BF16_MASK) is a tensor of the output's shape.
+// Limit of every bounded wait of the convolution kernels prepared from now on
+// (0 = the default of 2 s), and a one-shot request that the next prepared
+// forward convolution first waits on a barrier nothing arrives at, so that the
+// wait runs out and the kernel takes its error path (test of that path).
+void set_wait_limit(unsigned long long ns, bool stall_next);
+unsigned long long wait_limit_ns();
+bool take_stall_request();
+
 int fwd_prepare(FwdOp *op, const Act &in, const void *w, int w_rows, int cout, const float *bias, int epi,
                 int relu, void *out, int out_ctot, int out_coff, const Act *mask, unsigned *err);
 int fwd_launch(const FwdOp &op, cudaStream_t stream);

@@ -1091,6 +1091,11 @@ static int conv_check(DevBuf &e, cudaStream_t s) {
     return PT_OK;
 }
 
+int pt_conv_set_wait_limit(uint64_t wait_ns, uint32_t stall_next) {
+    ptconv::set_wait_limit(wait_ns, stall_next != 0);
+    return PT_OK;
+}
+
 int pt_conv3x3_forward(const void *x, uint32_t n, uint32_t h, uint32_t w, uint32_t cin, const void *weight,
                        const float *bias, uint32_t cout, int relu, int out_f32, void *y, void *stream) {
     (void)cudaGetLastError();

@@ -106,3 +106,37 @@ def test_conv_backward_weights(cuda_ctx, shape):
     ref = wr.grad.permute(0, 2, 3, 1).reshape(cout, 9, cin)
     assert _rel_l2(dw, ref) <= 1e-4
     assert _rel_l2(db, br.grad) <= 1e-4
+
+
+@pytest.mark.parametrize("shape", [(2, 16, 16, 16, 32), (1, 8, 256, 128, 256)], ids=["ring", "halo_resident"])
+def test_bounded_wait_runs_out_and_the_next_convolution_is_right(cuda_ctx, shape):
+    """The timeout path of the forward kernel, without a fault: with a 1 ms
+    limit and the stall request, the MMA warp waits on a barrier that nothing
+    arrives at; the wait runs out, the CTA records the error, lets the copies
+    it issued land (and the other warps stop waiting), frees its tensor memory
+    and returns.  The call reports PT_ERR_TIMEOUT well inside the normal 2 s
+    limit, and the next convolution, with the default limit, is correct."""
+    import time
+
+    from pupiloptixlab_gb300 import abi
+    from pupiloptixlab_gb300 import denoiser as dnm
+    n, h, w, cin, cout = shape
+    g = torch.Generator().manual_seed(7)
+    x = _bf16((n, h, w, cin), g).cuda()
+    wt = _bf16((cout, 9, cin), g, 0.1).cuda()
+    lib = cuda_ctx.lib
+    assert lib.pt_conv_set_wait_limit(1_000_000, 1) == 0
+    try:
+        t0 = time.perf_counter()
+        with pytest.raises(abi.PtError) as e:
+            dnm.conv3x3_forward(x, wt, None, cout, relu=False, out_f32=True)
+        elapsed = time.perf_counter() - t0
+    finally:
+        assert lib.pt_conv_set_wait_limit(0, 0) == 0
+    assert e.value.status == 4 and "bounded wait ran out" in str(e.value)
+    assert elapsed < 1.5, elapsed
+    # the context is healthy: the same convolution with the default limit
+    y = dnm.conv3x3_forward(x, wt, None, cout, relu=False, out_f32=True).cpu()
+    ref = _ref_conv(x.cpu(), wt.cpu(), None)
+    assert float((y - ref).abs().max()) <= 2e-3 * float(ref.abs().max())
+    assert _rel_l2(y, ref) <= 1e-4
