@@ -37,7 +37,7 @@
 extern "C" {
 #endif
 
-#define PT_API_VERSION 1
+#define PT_API_VERSION 2
 
 typedef enum pt_status {
     PT_OK = 0,
@@ -177,15 +177,23 @@ enum { PT_INST_FLIP_NORMALS = 1, PT_INST_FLIP_TEXCOORDS = 2 };
  * the translation in the last column (util::Transform).  Spheres accept
  * similarity transforms only (rotation, uniform scale, translation); curve
  * radii scale by the length of the transformed x axis.  Curves cannot be
- * emitters. */
+ * emitters.  An emissive instance is an area emitter (AreaEmitter,
+ * framework/resource/emitter.h:17-19): its radiance is radiance[3], or, with
+ * radiance_textured = 1, the texture radiance_tex (RGB, checkerboard or
+ * bitmap, sampled at the surface's texture coordinates as
+ * framework/render/emitter/area.h:17-45 and sphere.h:14-42 do; its selection
+ * weight is the texture's mean maximum channel times the area,
+ * framework/world/emitter.cpp:77-101). */
 typedef struct pt_instance_desc {
     uint32_t shape_type;  /* PT_SHAPE_* */
     uint32_t shape_index; /* into meshes[], spheres[] or curves[] */
     uint32_t material;    /* into materials[] */
     uint32_t flags;       /* PT_INST_* */
     float to_world[16];
-    uint32_t is_emitter;  /* area emitter with constant RGB radiance */
-    float radiance[3];
+    uint32_t is_emitter;  /* area emitter */
+    float radiance[3];    /* its constant RGB radiance (radiance_textured = 0) */
+    uint32_t radiance_textured;
+    pt_texture_desc radiance_tex;
 } pt_instance_desc;
 
 /* optix::Camera (framework/render/camera.h:7-10): two row-major 4x4 matrices. */

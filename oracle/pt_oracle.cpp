@@ -620,9 +620,22 @@ struct Texture {  // cuda::Texture::Sample, framework/cuda/texture.h:33-57
         return c0;
     }
     float max_weight() const {  // GetWeight, world/emitter.cpp:77-101
-        auto m3 = [](V3 v) { return std::max(std::max(v.x, v.y), v.z); };
-        if (type == PT_TEX_CHECKERBOARD) return (m3(c0) + m3(c1)) * 0.5f;
-        return m3(c0);
+        auto mx = [](float r, float g, float b) { return r > g ? (r > b ? r : b) : (g > b ? g : b); };
+        if (type == PT_TEX_CHECKERBOARD) return (mx(c0.x, c0.y, c0.z) + mx(c1.x, c1.y, c1.z)) * 0.5f;
+        if (type == PT_TEX_BITMAP && bitmap) {
+            // the reference's loop: i over the width, j over the height, pixel
+            // i * w + j (past the last pixel for w > h, where the reference reads
+            // beyond its array: the last pixel here)
+            const size_t w = bitmap->w, h = bitmap->h, last = w * h - 1;
+            float sum = 0.f;
+            for (size_t i = 0; i < w; i++)
+                for (size_t j = 0; j < h; j++) {
+                    const size_t q = std::min(i * w + j, last);
+                    sum += mx(bitmap->px[q * 4], bitmap->px[q * 4 + 1], bitmap->px[q * 4 + 2]);
+                }
+            return sum / (1.f * w * h);
+        }
+        return mx(c0.x, c0.y, c0.z);
     }
     static Texture from_desc(const pt_texture_desc &d) {
         Texture t;
@@ -814,6 +827,10 @@ struct Emitter {  // optix::Emitter, framework/render/emitter.h:13-29
     V3 n[3]{};   // triangle: world normals (normalised)
     V2 uv[3]{};
     float radius = 0.f;
+    bool textured = false;  // radiance from `tex` (AreaEmitter radiance texture) instead of `radiance`
+    Texture tex;
+
+    V3 radiance_at(V2 texcoord) const { return textured ? tex.sample(texcoord) : radiance; }  // radiance.Sample
 
     struct SampleRecord {  // EmitterSampleRecord, emitter/types.h:17-26
         V3 radiance{0, 0, 0}, wi{0, 0, 0}, pos{0, 0, 0}, normal{0, 0, 0};
@@ -829,7 +846,8 @@ struct Emitter {  // optix::Emitter, framework/render/emitter.h:13-29
                 V3 t = uniform_sample_triangle(xi.x, xi.y);
                 V3 position = p[0] * t.x + p[1] * t.y + p[2] * t.z;
                 V3 normal = normalize(n[0] * t.x + n[1] * t.y + n[2] * t.z);
-                ret.radiance = radiance;
+                V2 texcoord = uv[0] * t.x + uv[1] * t.y + uv[2] * t.z;  // area.h:21
+                ret.radiance = radiance_at(texcoord);
                 ret.wi = normalize(position - hit.position);
                 float NoL = dot(hit.normal, ret.wi);
                 float LNoL = dot(normal, -ret.wi);
@@ -846,7 +864,7 @@ struct Emitter {  // optix::Emitter, framework/render/emitter.h:13-29
                 V3 t = uniform_sample_sphere(xi.x, xi.y);
                 V3 position = t * radius + p[0];
                 V3 normal = normalize(t);
-                ret.radiance = radiance;
+                ret.radiance = radiance_at(sphere_texcoord(t));  // sphere.h:19-20
                 ret.wi = normalize(position - hit.position);
                 float NoL = dot(hit.normal, ret.wi);
                 float LNoL = dot(normal, -ret.wi);
@@ -891,7 +909,7 @@ struct Emitter {  // optix::Emitter, framework/render/emitter.h:13-29
             if (LNoL > 0.f) {
                 float d = length(scatter_pos - g.position);
                 out_pdf = d * d / (LNoL * area);
-                out_radiance = radiance;
+                out_radiance = radiance_at(g.texcoord);
             }
         } else if (type == kEmitConstEnv) {
             out_pdf = 0.25f * kInvPi;
@@ -1647,7 +1665,12 @@ static int build_scene(const pt_scene_desc *d, Scene &s) {
         Instance &in = s.instances[ii];
         in.emitter_offset = (int32_t)s.areas.size();
         V3 rad{id.radiance[0], id.radiance[1], id.radiance[2]};
-        float w = std::max(std::max(rad.x, rad.y), rad.z);
+        Texture rtex = Texture::from_desc(id.radiance_tex);
+        if (!id.radiance_textured) {
+            rtex = Texture();
+            rtex.c0 = rad;
+        }
+        const float w = rtex.max_weight();  // GetWeight (world/emitter.cpp:77-101)
         if (id.shape_type == PT_SHAPE_MESH) {
             const pt_mesh_desc &m = d->meshes[id.shape_index];
             double invd[16];
@@ -1658,6 +1681,8 @@ static int build_scene(const pt_scene_desc *d, Scene &s) {
                 Emitter e;
                 e.type = kEmitTri;
                 e.radiance = rad;
+                e.textured = id.radiance_textured != 0;
+                e.tex = rtex;
                 for (int k = 0; k < 3; k++) {
                     uint32_t vi = m.indices[3 * t + k];
                     e.p[k] = s.vpos[in.vertex_offset + vi];
@@ -1676,6 +1701,8 @@ static int build_scene(const pt_scene_desc *d, Scene &s) {
             Emitter e;
             e.type = kEmitSphere;
             e.radiance = rad;
+            e.textured = id.radiance_textured != 0;
+            e.tex = rtex;
             e.p[0] = in.center;
             e.radius = in.radius;
             e.area = 4 * 3.14159265358979323846f * e.radius * e.radius;
@@ -1784,7 +1811,7 @@ static SampleOut trace_path(const Scene &s, uint32_t pixel, uint32_t seed, uint3
     };
     if (!done) {
         load_hit(h, ray);
-        if (emitter_index >= 0) radiance = radiance + s.areas[emitter_index].radiance;  // GetRadiance (RGB)
+        if (emitter_index >= 0) radiance = radiance + s.areas[emitter_index].radiance_at(geo.texcoord);  // GetRadiance
         out.albedo = bsdf.albedo();
         out.normal = geo.normal;
     } else {

@@ -59,7 +59,7 @@ class SphereDesc(C.Structure):
 class InstanceDesc(C.Structure):
     _fields_ = [("shape_type", C.c_uint32), ("shape_index", C.c_uint32), ("material", C.c_uint32),
                 ("flags", C.c_uint32), ("to_world", C.c_float * 16), ("is_emitter", C.c_uint32),
-                ("radiance", C.c_float * 3)]
+                ("radiance", C.c_float * 3), ("radiance_textured", C.c_uint32), ("radiance_tex", TextureDesc)]
 
 
 class CameraDesc(C.Structure):

@@ -494,24 +494,37 @@ struct EmitterSample {  // EmitterSampleRecord (framework/render/emitter/types.h
 
 PT_DI uint32_t emitter_type(const DevEmitter &e) { return __float_as_uint(e.a.x); }
 
+// An area emitter's radiance at texture coordinate uv: its constant RGB
+// value, or its radiance texture (AreaEmitter radiance.Sample, area.h:22,43;
+// sphere.h:20,40; Emitter::GetRadiance at a primary hit, main.cu:90-95).
+PT_DI float3 emitter_radiance(const DevEmitter &e, const DevTexture *emit_tex, float2 uv) {
+    const uint32_t t = __float_as_uint(e.rad.w);
+    return t ? texture_sample(emit_tex[t - 1u], uv) : xyz(e.rad);
+}
+
 // Emitter::SampleDirect (emitter.h:124-139; area.h:17-35, sphere.h:14-32, env.h:69-80).
 // pdf stays 0 when the sample is unusable; is_delta is always false here.
-PT_DI void emitter_sample_direct(const DevEmitter &e, float3 pos, float3 nrm, float2 xi, EmitterSample &r) {
+PT_DI void emitter_sample_direct(const DevEmitter &e, const DevTexture *emit_tex, float3 pos, float3 nrm, float2 xi,
+                                 EmitterSample &r) {
     r.pdf = 0.f;
     r.distance = 0.f;
     uint32_t type = emitter_type(e);
     if (type == kEmitTri || type == kEmitSphere) {
         float3 position, normal;
+        float2 tex;
         if (type == kEmitTri) {
             float3 t = uniform_sample_triangle(xi.x, xi.y);
             position = xyz(e.p0) * t.x + xyz(e.p1) * t.y + xyz(e.p2) * t.z;
             normal = normalize(xyz(e.n0) * t.x + xyz(e.n1) * t.y + xyz(e.n2) * t.z);
+            // vertex texture coordinates (u in p*.w, v in n*.w), area.h:21
+            tex = make_float2(e.p0.w * t.x + e.p1.w * t.y + e.p2.w * t.z, e.n0.w * t.x + e.n1.w * t.y + e.n2.w * t.z);
         } else {
             float3 t = uniform_sample_sphere(xi.x, xi.y);
             position = t * e.a.w + xyz(e.p0);
             normal = normalize(t);
+            tex = sphere_texcoord(t);  // of the world-space sample direction, sphere.h:19
         }
-        r.radiance = xyz(e.rad);
+        r.radiance = emitter_radiance(e, emit_tex, tex);
         r.wi = normalize(position - pos);
         float NoL = dot(nrm, r.wi);
         float LNoL = dot(normal, -r.wi);

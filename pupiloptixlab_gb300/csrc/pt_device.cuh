@@ -163,9 +163,9 @@ struct DevEnvMap {
 // Emitter (optix::Emitter, framework/render/emitter.h:13-29): 8 float4.
 struct DevEmitter {
     float4 a;   // type (bits), select_probability, area, radius
-    float4 rad; // radiance xyz
-    float4 p0, p1, p2;  // triangle vertices / sphere centre (p0)
-    float4 n0, n1, n2;  // triangle vertex normals (normalised)
+    float4 rad; // radiance xyz; w: bits of (1 + index into DevScene::emit_tex) for a textured radiance, else 0
+    float4 p0, p1, p2;  // triangle vertices / sphere centre (p0); w: vertex texture coordinate u
+    float4 n0, n1, n2;  // triangle vertex normals (normalised); w: vertex texture coordinate v
 };
 
 // Per-instance data used when shading a hit.
@@ -203,6 +203,7 @@ struct DevScene {
     const DevInstance *inst;
     const DevMaterial *mats;
     const DevEmitter *emitters; // area emitters
+    const DevTexture *emit_tex; // textures of textured emitter radiance
     const float *emitter_cdf;   // running sums of select probabilities
     uint32_t num_emitters;
     uint32_t num_tris;

@@ -56,7 +56,10 @@ struct MeshInstanceRef {  // where the world vertices of one mesh instance live
 // vertex updates (instance order = emitter order).
 struct EmitterSource {
     bool sphere = false;
-    float radiance[3] = {0, 0, 0};
+    float radiance[3] = {0, 0, 0};  // constant radiance (tex < 0)
+    int32_t tex = -1;               // textured radiance: index into the scene's emitter textures
+    float weight = 0.f;             // GetWeight of the radiance (world/emitter.cpp:77-101)
+    std::vector<float> uvs;         // mesh: object texture coordinates, 2 per vertex (empty: none)
     uint32_t vertex_offset = 0;     // mesh: first world vertex of the instance
     std::vector<uint32_t> indices;  // mesh: object-space triangle indices
     std::vector<float> normals;     // mesh: object-space vertex normals (empty: geometric)
@@ -98,6 +101,7 @@ struct pt_scene {
     DevBuf prims_bvh;    // 3 float4 per prim (leaf order)
     DevBuf nodes;
     DevBuf tri_vidx, vpos, vnrm, vuv, prim_inst, inst, mats, emitters, emitter_cdf;
+    DevBuf emitter_tex;  // textures of textured area-emitter radiance (DevTexture each)
     DevBuf curve_seg, curve_cp;  // piece -> segment; 4 world control points per segment
     DevBuf mesh_obj_pos;  // scratch for pt_scene_update_vertices
     // BVH build scratch and results

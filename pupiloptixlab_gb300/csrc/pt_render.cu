@@ -416,7 +416,7 @@ PT_DI void shade_one(const DevScene &s, const Outputs &out, const State &st, con
         bsdf = material_local(m, g.uv);
         int ei = in.emitter_offset >= 0 ? in.emitter_offset + (prim - (int)in.prim_offset) : -1;
         if (depth == 0) {  // main.cu:90-98
-            if (ei >= 0) rad = rad + xyz(s.emitters[ei].rad);
+            if (ei >= 0) rad = rad + emitter_radiance(s.emitters[ei], s.emit_tex, g.uv);
             if (last) {
                 float3 al = bsdf.albedo();
                 if (out.albedo) { out.albedo[3 * p] = al.x; out.albedo[3 * p + 1] = al.y; out.albedo[3 * p + 2] = al.z; }
@@ -427,7 +427,7 @@ PT_DI void shade_one(const DevScene &s, const Outputs &out, const State &st, con
             float epdf = emitter_eval_pdf(e, g.pos, g.nrm, ro);
             if (!is_zero(epdf)) {
                 float mis = prev_delta ? 1.f : mis_weight(prev_pdf, epdf * e.a.y);
-                rad = rad + thr * xyz(e.rad) * mis;
+                rad = rad + thr * emitter_radiance(e, s.emit_tex, g.uv) * mis;
             }
         }
     }
@@ -452,7 +452,7 @@ PT_DI void shade_one(const DevScene &s, const Outputs &out, const State &st, con
             const DevEmitter &e = ei >= 0 ? s.emitters[ei] : s.env;
             EmitterSample es;
             if (ei < 0 && emitter_type(e) == kEmitEnvMap) envmap_sample_direct(s.envmap, xi, es);
-            else emitter_sample_direct(e, g.pos, g.nrm, xi, es);
+            else emitter_sample_direct(e, s.emit_tex, g.pos, g.nrm, xi, es);
             if (es.pdf != 0.f) {
                 BsdfRecord er;
                 er.wi = to_local(es.wi, g.nrm);

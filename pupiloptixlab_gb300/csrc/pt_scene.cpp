@@ -103,6 +103,34 @@ H3 tex_average(const pt_texture_desc &t) {  // GetPixelAverage (optix_material.c
     return {t.color0[0], t.color0[1], t.color0[2]};
 }
 
+// GetWeight (world/emitter.cpp:77-101): the selection weight of an area
+// emitter's radiance texture per unit area -- the largest channel of an RGB
+// value, the mean of the two patches' largest channels of a checkerboard, and
+// for a bitmap the mean largest channel over its pixels, summed in the
+// reference's loop order (i over the width, j over the height, pixel
+// i * width + j).  For a bitmap wider than high that index runs past the last
+// pixel, where the reference reads beyond its array; here it reads the last
+// pixel instead.
+float emitter_weight(const pt_texture_desc &t) {
+    auto max3 = [](float r, float g, float b) { return r > g ? (r > b ? r : b) : (g > b ? g : b); };
+    if (t.type == PT_TEX_CHECKERBOARD) {
+        float w1 = max3(t.color0[0], t.color0[1], t.color0[2]);
+        float w2 = max3(t.color1[0], t.color1[1], t.color1[2]);
+        return (w1 + w2) * 0.5f;
+    }
+    if (t.type == PT_TEX_BITMAP) {
+        const size_t w = t.width, h = t.height, last = w * h - 1;
+        float sum = 0.f;
+        for (size_t i = 0; i < w; i++)
+            for (size_t j = 0; j < h; j++) {
+                const size_t px = std::min(i * w + j, last);
+                sum += max3(t.pixels[px * 4 + 0], t.pixels[px * 4 + 1], t.pixels[px * 4 + 2]);
+            }
+        return sum / (1.f * w * h);
+    }
+    return max3(t.color0[0], t.color0[1], t.color0[2]);
+}
+
 // A float4 CUDA texture object over an RGBA float bitmap, made as the
 // reference makes it (framework/cuda/texture.cpp:60-102): normalized
 // coordinates, element reads, the given address and filter modes.
@@ -246,6 +274,18 @@ int validate(const pt_scene_desc *d) {
         } else {
             pt_set_error("instance %u: unknown shape type %u", i, in.shape_type);
             return PT_ERR_INVALID;
+        }
+        if (in.is_emitter && in.radiance_textured) {
+            const pt_texture_desc &t = in.radiance_tex;
+            if (t.type != PT_TEX_RGB && t.type != PT_TEX_CHECKERBOARD && t.type != PT_TEX_BITMAP) {
+                pt_set_error("instance %u: unknown emitter radiance texture type %u", i, t.type);
+                return PT_ERR_INVALID;
+            }
+            if (t.type == PT_TEX_BITMAP &&
+                (!t.pixels || !t.width || !t.height || t.address_mode > PT_TEX_ADDRESS_MIRROR || t.filter > PT_TEX_FILTER_LINEAR)) {
+                pt_set_error("instance %u: emitter radiance bitmap without pixels, of zero size or with unknown modes", i);
+                return PT_ERR_INVALID;
+            }
         }
         if (!affine(in.to_world)) { pt_set_error("instance %u: to_world must be affine", i); return PT_ERR_INVALID; }
         for (int k = 0; k < 16; k++)
@@ -539,6 +579,7 @@ int build_scene(pt_scene *s, const pt_scene_desc *d) {
     }
 
     // emissive instances in instance order (world/emitter.cpp:169-263)
+    std::vector<DevTexture> emit_tex;
     s->emitter_sources.clear();
     s->has_emissive_mesh = false;
     uint32_t n_area = 0;
@@ -549,8 +590,24 @@ int build_scene(pt_scene *s, const pt_scene_desc *d) {
         in.emitter_offset = (int32_t)n_area;
         EmitterSource src;
         memcpy(src.radiance, id.radiance, sizeof(src.radiance));
+        if (id.radiance_textured) {
+            const pt_texture_desc &t = id.radiance_tex;
+            DevTexture dt = to_dev(t);
+            if (t.type == PT_TEX_BITMAP) {
+                cudaTextureObject_t obj = 0;
+                int st = bitmap_texture(s, t.pixels, t.width, t.height, t.address_mode, t.filter, &obj);
+                if (st != PT_OK) return st;
+                dt.obj = static_cast<unsigned long long>(obj);
+            }
+            src.tex = (int32_t)emit_tex.size();
+            emit_tex.push_back(dt);
+            src.weight = emitter_weight(t);
+        } else {
+            src.weight = std::max(std::max(id.radiance[0], id.radiance[1]), id.radiance[2]);
+        }
         if (id.shape_type == PT_SHAPE_MESH) {
             const pt_mesh_desc &m = d->meshes[id.shape_index];
+            if (m.texcoords) src.uvs.assign(m.texcoords, m.texcoords + 2ull * m.num_vertices);
             double inv[16];
             inverse4f(id.to_world, inv);
             normal_matrix(inv, src.nm);
@@ -589,6 +646,7 @@ int build_scene(pt_scene *s, const pt_scene_desc *d) {
     if ((e = upload(s->curve_cp, curve_cp)) != PT_OK) return e;
     if ((e = upload(s->inst, insts)) != PT_OK) return e;
     if ((e = upload(s->mats, mats)) != PT_OK) return e;
+    if ((e = upload(s->emitter_tex, emit_tex)) != PT_OK) return e;
     s->h_prims_world = std::move(prims);
 
     ptd::DevScene &dv = s->dev;
@@ -602,6 +660,7 @@ int build_scene(pt_scene *s, const pt_scene_desc *d) {
     dv.curve_prim0 = ntri + nsph;
     dv.inst = s->inst.as<DevInstance>();
     dv.mats = s->mats.as<DevMaterial>();
+    dv.emit_tex = s->emitter_tex.as<DevTexture>();
     dv.num_tris = ntri;
     if ((e = pt_rebuild_emitters(s, vpos.data())) != PT_OK) return e;
     dv.width_px = d->width;
@@ -623,7 +682,14 @@ int pt_rebuild_emitters(pt_scene *s, const float4 *host_vpos) {
     std::vector<float4> fetched;
     for (const EmitterSource &src : s->emitter_sources) {
         H3 rad = h3(src.radiance[0], src.radiance[1], src.radiance[2]);
-        float w = std::max(std::max(rad.x, rad.y), rad.z);  // GetWeight (emitter.cpp:77-101)
+        const float w = src.weight;  // GetWeight (emitter.cpp:77-101)
+        // textured radiance: 1 + texture index in rad.w (rad.xyz unused)
+        float texw = 0.f;
+        if (src.tex >= 0) {
+            const uint32_t bits = (uint32_t)src.tex + 1u;
+            memcpy(&texw, &bits, 4);
+            rad = h3(0.f, 0.f, 0.f);
+        }
         if (!src.sphere) {
             const float4 *vp;
             if (host_vpos) {
@@ -657,13 +723,22 @@ int pt_rebuild_emitters(pt_scene *s, const float4 *host_vpos) {
                 memcpy(&tf, &type, 4);
                 e.a = make_float4(tf, 0.f, area, 0.f);  // type, select probability, area, radius
                 weights.push_back(w * area);
-                e.rad = make_float4(rad.x, rad.y, rad.z, 0.f);
-                e.p0 = make_float4(P[0].x, P[0].y, P[0].z, 0.f);
-                e.p1 = make_float4(P[1].x, P[1].y, P[1].z, 0.f);
-                e.p2 = make_float4(P[2].x, P[2].y, P[2].z, 0.f);
-                e.n0 = make_float4(N[0].x, N[0].y, N[0].z, 0.f);
-                e.n1 = make_float4(N[1].x, N[1].y, N[1].z, 0.f);
-                e.n2 = make_float4(N[2].x, N[2].y, N[2].z, 0.f);
+                e.rad = make_float4(rad.x, rad.y, rad.z, texw);
+                // vertex texture coordinates, as the reference reads them
+                // (mesh.texcoords, without flip_tex_coords; world/emitter.cpp:169-217)
+                float U[3] = {0.f, 0.f, 0.f}, V[3] = {0.f, 0.f, 0.f};
+                if (!src.uvs.empty())
+                    for (int k = 0; k < 3; k++) {
+                        const uint32_t vi = src.indices[3 * t + k];
+                        U[k] = src.uvs[2 * vi];
+                        V[k] = src.uvs[2 * vi + 1];
+                    }
+                e.p0 = make_float4(P[0].x, P[0].y, P[0].z, U[0]);
+                e.p1 = make_float4(P[1].x, P[1].y, P[1].z, U[1]);
+                e.p2 = make_float4(P[2].x, P[2].y, P[2].z, U[2]);
+                e.n0 = make_float4(N[0].x, N[0].y, N[0].z, V[0]);
+                e.n1 = make_float4(N[1].x, N[1].y, N[1].z, V[1]);
+                e.n2 = make_float4(N[2].x, N[2].y, N[2].z, V[2]);
                 ems.push_back(e);
             }
         } else {
@@ -675,7 +750,7 @@ int pt_rebuild_emitters(pt_scene *s, const float4 *host_vpos) {
             memcpy(&tf, &type, 4);
             e.a = make_float4(tf, 0.f, area, r);
             weights.push_back(w * area);
-            e.rad = make_float4(rad.x, rad.y, rad.z, 0.f);
+            e.rad = make_float4(rad.x, rad.y, rad.z, texw);
             e.p0 = make_float4(src.center[0], src.center[1], src.center[2], 0.f);
             ems.push_back(e);
         }
@@ -745,7 +820,7 @@ void DevBuf::release() {
 
 pt_scene::~pt_scene() {
     DevBuf *all[] = {&prims_world, &prims_bvh, &nodes, &tri_vidx, &vpos, &vnrm, &vuv, &prim_inst, &inst, &mats, &curve_seg, &curve_cp,
-                     &emitters, &emitter_cdf, &mesh_obj_pos, &bvh_scratch, &bvh_order, &sah_scratch, &xform_table, &all_obj_pos, &ws.ray_o, &ws.ray_d, &ws.hit, &ws.thr,
+                     &emitters, &emitter_cdf, &emitter_tex, &mesh_obj_pos, &bvh_scratch, &bvh_order, &sah_scratch, &xform_table, &all_obj_pos, &ws.ray_o, &ws.ray_d, &ws.hit, &ws.thr,
                      &ws.rad, &ws.rng, &ws.meta, &ws.q0, &ws.q1, &ws.sh_o, &ws.sh_d, &ws.sh_c, &ws.mat_key,
                      &ws.counters, &ws.sort_tmp};
     for (DevBuf *b : all) b->release();

@@ -175,13 +175,13 @@ bool ToPtSceneDesc(const resource::Scene &scene, const pt_camera_desc &camera, P
         std::memcpy(d.to_world, ins.transform.matrix.e, sizeof(d.to_world));
         if (ins.is_emitter && ins.emitter.type == resource::EEmitterType::Area) {
             const util::Texture &r = ins.emitter.area.radiance;
-            if (r.type != util::ETextureType::RGB) {
-                set_error(error, "shape instance " + std::to_string(i) + " (" + ins.name +
-                                     "): area emitter radiance must be a constant RGB value");
-                return false;
-            }
             d.is_emitter = 1;
-            for (int k = 0; k < 3; k++) d.radiance[k] = r.rgb.color.e[k];
+            if (r.type == util::ETextureType::RGB) {
+                for (int k = 0; k < 3; k++) d.radiance[k] = r.rgb.color.e[k];
+            } else {  // checkerboard or bitmap radiance
+                d.radiance_textured = 1;
+                d.radiance_tex = ToPtTexture(r);
+            }
         }
         out.instances.push_back(d);
     }

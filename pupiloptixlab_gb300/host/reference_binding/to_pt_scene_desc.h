@@ -35,9 +35,10 @@ struct PtSceneDesc {
 // helper (its device copy, world->camera->GetCudaMemory(), read back with
 // cudaMemcpy), which already holds the sensor's fov, aspect and transform.
 // Shapes shared by several instances (the built-in cube, rectangle and unit
-// sphere, OBJ files loaded once) become one mesh / sphere each.  Returns false
-// with a message in *error for what the tracer does not take: an emitter
-// radiance that is not a constant RGB value.  Point and directional emitters
+// sphere, OBJ files loaded once) become one mesh / sphere each; an area
+// emitter's radiance is its RGB value or its texture.  Returns false with a
+// message in *error for a shape instance without a usable shape.  Point and
+// directional emitters
 // are skipped, as the reference's emitter tables skip them
 // (framework/world/emitter.cpp:314-315).
 bool ToPtSceneDesc(const resource::Scene &scene, const pt_camera_desc &camera, PtSceneDesc &out,

@@ -519,9 +519,13 @@ struct Loader {
                 if (et != "area") return fail(c.get(), "shape emitter '" + et + "' is not supported");
                 pt_texture_desc rad;
                 if (!get_texture(c.get(), "radiance", rad, rgb(1, 1, 1))) return false;
-                if (rad.type != PT_TEX_RGB) return fail(c.get(), "area emitter radiance must be rgb");
                 ins.is_emitter = true;
-                memcpy(ins.radiance, rad.color0, sizeof(ins.radiance));
+                if (rad.type == PT_TEX_RGB) {
+                    memcpy(ins.radiance, rad.color0, sizeof(ins.radiance));
+                } else {  // checkerboard or bitmap radiance (AreaEmitter, resource/emitter.h:17-19)
+                    ins.radiance_textured = true;
+                    ins.radiance_tex = rad;
+                }
             }
         }
         if (!has_bsdf) {  // the reference's default material: diffuse 0.5
@@ -696,6 +700,8 @@ const pt_scene_desc &Scene::Desc() {
         memcpy(d.to_world, s.to_world, sizeof(d.to_world));
         d.is_emitter = s.is_emitter ? 1 : 0;
         memcpy(d.radiance, s.radiance, sizeof(d.radiance));
+        d.radiance_textured = s.radiance_textured ? 1u : 0u;
+        d.radiance_tex = s.radiance_tex;
         m_inst_descs.push_back(d);
     }
     m_desc = pt_scene_desc{};

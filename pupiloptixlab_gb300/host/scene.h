@@ -39,6 +39,8 @@ struct ShapeInstance {
     float to_world[16];
     bool is_emitter = false;
     float radiance[3] = {0, 0, 0};
+    bool radiance_textured = false;  // radiance from radiance_tex (checkerboard or bitmap)
+    pt_texture_desc radiance_tex{};
 };
 
 struct Sensor {

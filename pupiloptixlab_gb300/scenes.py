@@ -342,7 +342,11 @@ class Scene:
             d.to_world[:] = [float(v) for v in np.asarray(inst["to_world"], np.float32).reshape(-1)]
             if inst["radiance"] is not None:
                 d.is_emitter = 1
-                d.radiance[:] = [float(v) for v in inst["radiance"]]
+                if isinstance(inst["radiance"], abi.TextureDesc):  # a textured area emitter
+                    d.radiance_textured = 1
+                    d.radiance_tex = inst["radiance"]
+                else:
+                    d.radiance[:] = [float(v) for v in inst["radiance"]]
         sd = abi.SceneDesc()
         sd.meshes = C.cast(meshes, C.POINTER(abi.MeshDesc))
         sd.num_meshes = len(self.meshes)

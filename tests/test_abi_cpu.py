@@ -94,7 +94,7 @@ def test_camera_make_rejects_bad_input(ptlib):
 
 
 def test_entry_points_validate_without_a_device(ptlib):
-    assert ptlib.pt_api_version() == 1
+    assert ptlib.pt_api_version() == 2
     # NULL arguments are rejected before any device work
     assert ptlib.pt_render(None, None, None, None) == 1
     assert ptlib.pt_trace_rays(None, None, None, 4, 0, None) == 1

@@ -524,3 +524,28 @@ int main() {
                     f"-Wl,-rpath,{build._cuda_lib_dir()}"], check=True, capture_output=True)
     out = subprocess.run([str(exe)], capture_output=True, text=True, check=True, timeout=60).stdout.split()
     assert out == ["2", "1", "1", "1", "1", "1", "0", "3"]
+
+
+def test_textured_area_emitter_radiance(host):
+    """<emitter type="area"> with a checkerboard radiance texture (as
+    resource/emitter.h:17-19 allows) becomes a textured emitter instance."""
+    text = """<scene>
+      <sensor type='perspective'><film type='hdrfilm'><integer name='width' value='8'/>
+        <integer name='height' value='8'/></film></sensor>
+      <shape type='rectangle'>
+        <emitter type='area'>
+          <texture name='radiance' type='checkerboard'>
+            <rgb name='color0' value='5, 4, 3'/><rgb name='color1' value='1, 2, 3'/>
+            <transform name='to_uv'><scale x='4' y='2'/></transform>
+          </texture>
+        </emitter>
+      </shape>
+      <shape type='sphere'><emitter type='area'><rgb name='radiance' value='2, 3, 4'/></emitter></shape>
+    </scene>"""
+    s = host.XmlScene(text, is_text=True)
+    d = s.desc()
+    a, b = d.instances[0], d.instances[1]
+    assert a.is_emitter and a.radiance_textured and a.radiance_tex.type == abi.TEX_CHECKERBOARD
+    assert list(a.radiance_tex.color0) == [5.0, 4.0, 3.0] and list(a.radiance_tex.color1) == [1.0, 2.0, 3.0]
+    assert a.radiance_tex.uv_transform[0] == 4.0 and a.radiance_tex.uv_transform[5] == 2.0
+    assert b.is_emitter and not b.radiance_textured and list(b.radiance) == [2.0, 3.0, 4.0]
