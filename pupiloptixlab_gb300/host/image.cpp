@@ -1,6 +1,7 @@
-// image.cpp -- Radiance RGBE, PFM and uncompressed OpenEXR readers, OpenEXR
-// writer (see image.h).
+// image.cpp -- Radiance RGBE, PFM, PNG and OpenEXR (uncompressed, RLE, ZIP)
+// readers, OpenEXR writer (see image.h).
 #include "image.h"
+#include "inflate.h"
 
 #include <algorithm>
 #include <cstdint>
@@ -170,7 +171,214 @@ bool load_pfm(const std::vector<uint8_t> &d, std::vector<float> &rgba, uint32_t 
     return true;
 }
 
-// ---- OpenEXR (scanline, NO_COMPRESSION) ----------------------------------
+// ---- PNG -------------------------------------------------------------------
+// Per the PNG specification (ISO/IEC 15948): 8-byte signature, chunks of
+// (big-endian length, type, data, CRC-32); IHDR, PLTE, tRNS, IDAT (one zlib
+// stream over all IDAT chunks), IEND.  Scanlines carry a filter byte (None,
+// Sub, Up, Average, Paeth); interlaced images come as the seven Adam7 passes.
+
+uint32_t be32(const uint8_t *p) { return (uint32_t)p[0] << 24 | (uint32_t)p[1] << 16 | (uint32_t)p[2] << 8 | p[3]; }
+
+uint32_t crc32(const uint8_t *p, size_t n) {  // the CRC of the PNG specification (polynomial 0xEDB88320)
+    static uint32_t table[256];
+    static bool init = false;
+    if (!init) {
+        for (uint32_t i = 0; i < 256; i++) {
+            uint32_t c = i;
+            for (int k = 0; k < 8; k++) c = (c & 1) ? 0xEDB88320u ^ (c >> 1) : c >> 1;
+            table[i] = c;
+        }
+        init = true;
+    }
+    uint32_t c = 0xffffffffu;
+    for (size_t i = 0; i < n; i++) c = table[(c ^ p[i]) & 0xff] ^ (c >> 8);
+    return c ^ 0xffffffffu;
+}
+
+uint8_t paeth(uint8_t a, uint8_t b, uint8_t c) {
+    const int p = (int)a + b - c, pa = std::abs(p - a), pb = std::abs(p - b), pc = std::abs(p - c);
+    return (pa <= pb && pa <= pc) ? a : (pb <= pc ? b : c);
+}
+
+// Reverses the filters of `rows` scanlines of `line` bytes (each preceded by
+// its filter type byte) in place; bpp = bytes per complete pixel (>= 1).
+bool unfilter(uint8_t *data, size_t rows, size_t line, size_t bpp, std::string &error) {
+    std::vector<uint8_t> prev(line, 0);
+    for (size_t r = 0; r < rows; r++) {
+        uint8_t *row = data + r * (line + 1);
+        const uint8_t f = row[0];
+        uint8_t *x = row + 1;
+        for (size_t i = 0; i < line; i++) {
+            const uint8_t a = i >= bpp ? x[i - bpp] : 0, b = prev[i], c = i >= bpp ? prev[i - bpp] : 0;
+            switch (f) {
+                case 0: break;
+                case 1: x[i] = static_cast<uint8_t>(x[i] + a); break;
+                case 2: x[i] = static_cast<uint8_t>(x[i] + b); break;
+                case 3: x[i] = static_cast<uint8_t>(x[i] + ((a + b) >> 1)); break;
+                case 4: x[i] = static_cast<uint8_t>(x[i] + paeth(a, b, c)); break;
+                default: error = "PNG: unknown filter type"; return false;
+            }
+        }
+        std::copy(x, x + line, prev.begin());
+    }
+    return true;
+}
+
+// PNG -> 8-bit samples with `comp` channels per pixel, as an 8-bit image load
+// delivers them: grey 1, grey + alpha 2, RGB 3, RGBA 4, palette 3 (4 with a
+// tRNS chunk); 16-bit samples keep their high byte, grey samples of 1, 2 or 4
+// bits are scaled to 0..255.
+bool decode_png(const std::vector<uint8_t> &d, std::vector<uint8_t> &img, uint32_t &w, uint32_t &h, int &comp,
+                std::string &error) {
+    static const uint8_t sig[8] = {137, 80, 78, 71, 13, 10, 26, 10};
+    if (d.size() < 8 || std::memcmp(d.data(), sig, 8) != 0) {
+        error = "not a PNG file";
+        return false;
+    }
+    uint32_t depth = 0, ctype = 0, interlace = 0;
+    std::vector<uint8_t> idat, plte, trns;
+    bool have_ihdr = false, have_iend = false;
+    size_t p = 8;
+    while (p + 12 <= d.size() && !have_iend) {
+        const uint32_t len = be32(&d[p]);
+        if (len > d.size() - p - 12) {
+            error = "PNG: chunk runs past the end of the file";
+            return false;
+        }
+        const uint8_t *type = &d[p + 4], *body = &d[p + 8];
+        if (crc32(type, 4 + (size_t)len) != be32(body + len)) {
+            error = "PNG: chunk CRC mismatch";
+            return false;
+        }
+        const std::string t(reinterpret_cast<const char *>(type), 4);
+        if (t == "IHDR") {
+            if (len != 13) {
+                error = "PNG: bad IHDR";
+                return false;
+            }
+            w = be32(body);
+            h = be32(body + 4);
+            depth = body[8];
+            ctype = body[9];
+            interlace = body[12];
+            if (body[10] != 0 || body[11] != 0 || interlace > 1) {
+                error = "PNG: unknown compression, filter or interlace method";
+                return false;
+            }
+            have_ihdr = true;
+        } else if (t == "PLTE") {
+            plte.assign(body, body + len);
+        } else if (t == "tRNS") {
+            trns.assign(body, body + len);
+        } else if (t == "IDAT") {
+            idat.insert(idat.end(), body, body + len);
+        } else if (t == "IEND") {
+            have_iend = true;
+        } else if (!(type[0] & 0x20)) {
+            error = "PNG: unknown critical chunk " + t;
+            return false;
+        }
+        p += 12 + (size_t)len;
+    }
+    if (!have_ihdr || idat.empty()) {
+        error = "PNG: IHDR or image data missing";
+        return false;
+    }
+    const int chans = ctype == 0 ? 1 : ctype == 2 ? 3 : ctype == 3 ? 1 : ctype == 4 ? 2 : ctype == 6 ? 4 : 0;
+    const bool depth_ok = ctype == 0   ? (depth == 1 || depth == 2 || depth == 4 || depth == 8 || depth == 16)
+                          : ctype == 3 ? (depth == 1 || depth == 2 || depth == 4 || depth == 8)
+                                       : (depth == 8 || depth == 16);
+    if (!chans || !depth_ok || w == 0 || h == 0 || (uint64_t)w * h > (1ull << 28)) {
+        error = "PNG: unsupported colour type, bit depth or size";
+        return false;
+    }
+    if (ctype == 3 && (plte.empty() || plte.size() % 3)) {
+        error = "PNG: palette missing";
+        return false;
+    }
+    comp = ctype == 3 ? (trns.empty() ? 3 : 4) : chans;
+    const size_t bits_px = (size_t)chans * depth, bpp = std::max<size_t>(1, bits_px / 8);
+    struct Pass { uint32_t x0, y0, dx, dy; };
+    const Pass adam7[7] = {{0, 0, 8, 8}, {4, 0, 8, 8}, {0, 4, 4, 8}, {2, 0, 4, 4}, {0, 2, 2, 4}, {1, 0, 2, 2}, {0, 1, 1, 2}};
+    const Pass whole = {0, 0, 1, 1};
+    const int npass = interlace ? 7 : 1;
+    size_t total = 0;
+    for (int k = 0; k < npass; k++) {
+        const Pass &ps = interlace ? adam7[k] : whole;
+        const size_t pw = w > ps.x0 ? (w - ps.x0 + ps.dx - 1) / ps.dx : 0, ph = h > ps.y0 ? (h - ps.y0 + ps.dy - 1) / ps.dy : 0;
+        if (pw && ph) total += ph * ((pw * bits_px + 7) / 8 + 1);
+    }
+    std::vector<uint8_t> raw;
+    if (!ZlibInflate(idat.data(), idat.size(), raw, total, error)) {
+        error = "PNG: " + error;
+        return false;
+    }
+    if (raw.size() != total) {
+        error = "PNG: image data of the wrong size";
+        return false;
+    }
+    img.assign((size_t)w * h * comp, 0);
+    size_t off = 0;
+    for (int k = 0; k < npass; k++) {
+        const Pass &ps = interlace ? adam7[k] : whole;
+        const size_t pw = w > ps.x0 ? (w - ps.x0 + ps.dx - 1) / ps.dx : 0, ph = h > ps.y0 ? (h - ps.y0 + ps.dy - 1) / ps.dy : 0;
+        if (!pw || !ph) continue;
+        const size_t line = (pw * bits_px + 7) / 8;
+        if (!unfilter(raw.data() + off, ph, line, bpp, error)) return false;
+        for (size_t y = 0; y < ph; y++) {
+            const uint8_t *row = raw.data() + off + y * (line + 1) + 1;
+            for (size_t x = 0; x < pw; x++) {
+                uint8_t *dst = img.data() + ((size_t)(ps.y0 + y * ps.dy) * w + ps.x0 + x * ps.dx) * comp;
+                if (depth < 8) {  // one sample per pixel (grey or palette index), packed high bits first
+                    const size_t bit = x * depth;
+                    const uint32_t v = (row[bit / 8] >> (8 - depth - bit % 8)) & ((1u << depth) - 1);
+                    if (ctype == 3) {
+                        if (3 * v + 2 >= plte.size()) { error = "PNG: palette index out of range"; return false; }
+                        for (int c = 0; c < 3; c++) dst[c] = plte[3 * v + c];
+                        if (comp == 4) dst[3] = v < trns.size() ? trns[v] : 255;
+                    } else {
+                        dst[0] = static_cast<uint8_t>(v * (255u / ((1u << depth) - 1)));
+                    }
+                } else if (ctype == 3) {
+                    const uint32_t v = row[x];
+                    if (3 * v + 2 >= plte.size()) { error = "PNG: palette index out of range"; return false; }
+                    for (int c = 0; c < 3; c++) dst[c] = plte[3 * v + c];
+                    if (comp == 4) dst[3] = v < trns.size() ? trns[v] : 255;
+                } else {
+                    const size_t step = depth / 8;  // 16-bit samples: the high (first) byte
+                    for (int c = 0; c < chans; c++) dst[c] = row[(x * chans + c) * step];
+                }
+            }
+        }
+        off += ph * (line + 1);
+    }
+    return true;
+}
+
+// util::BitmapTexture from an 8-bit image as the reference fills it
+// (framework/util/texture.cpp:106-118): for every `comp` samples, R, G, B =
+// (sample / 255)^2.2 of the first three bytes from there and A = the fourth
+// byte / 255 for 4-channel images, else 1.  With fewer than 3 channels the
+// reference reads the bytes that follow (the next samples; past the last one
+// its buffer ends, read here as 0).
+bool load_png(const std::vector<uint8_t> &d, std::vector<float> &rgba, uint32_t &w, uint32_t &h, std::string &error) {
+    std::vector<uint8_t> img;
+    int c = 0;
+    if (!decode_png(d, img, w, h, c, error)) return false;
+    const size_t size = img.size();
+    auto at = [&](size_t i) -> float { return i < size ? static_cast<float>(img[i]) : 0.f; };
+    rgba.assign(4ull * w * h, 0.f);
+    size_t j = 0;
+    for (size_t i = 0; i < size; i += (size_t)c) {
+        rgba[j++] = std::pow(at(i) * 1.f / 255.f, 2.2f);
+        rgba[j++] = std::pow(at(i + 1) * 1.f / 255.f, 2.2f);
+        rgba[j++] = std::pow(at(i + 2) * 1.f / 255.f, 2.2f);
+        rgba[j++] = c == 4 ? at(i + 3) * 1.f / 255.f : 1.f;
+    }
+    return true;
+}
+
+// ---- OpenEXR (scanline; NO, RLE, ZIPS, ZIP compression) --------------------
 // Layout per the OpenEXR file format description: magic 20000630, version 2,
 // header = attributes (name\0 type\0 int32 size, value) ending with \0, a
 // table of uint64 offsets (one per scanline block), then blocks of
@@ -276,8 +484,10 @@ bool load_exr(const std::vector<uint8_t> &d, std::vector<float> &rgba, uint32_t 
         }
         p = end;
     }
-    if (compression != 0) {
-        error = "compressed OpenEXR files are not supported (only NO_COMPRESSION)";
+    // 0 NO_COMPRESSION, 1 RLE, 2 ZIPS (one scanline per block), 3 ZIP (16)
+    if (compression < 0 || compression > 3) {
+        error = "OpenEXR compression " + std::to_string(compression) +
+                " is not supported (PIZ, PXR24, B44 and DWA are not; NO, RLE, ZIPS and ZIP are)";
         return false;
     }
     if (xmax < xmin || ymax < ymin) {
@@ -297,35 +507,79 @@ bool load_exr(const std::vector<uint8_t> &d, std::vector<float> &rgba, uint32_t 
     rgba.assign(4ull * w * h, 0.f);
     for (size_t i = 0; i < (size_t)w * h; i++) rgba[4 * i + 3] = 1.f;
     const size_t table = p;
-    if (table + 8ull * h > d.size()) {
+    const uint32_t lines_per_block = compression == 3 ? 16u : 1u;
+    const size_t nblocks = (h + lines_per_block - 1) / lines_per_block;
+    if (table + 8ull * nblocks > d.size()) {
         error = "OpenEXR offset table truncated";
         return false;
     }
-    for (uint32_t line = 0; line < h; line++) {
-        const uint64_t off = get_u64(d, table + 8ull * line);
-        if (off + 8 + line_bytes > d.size()) {
-            error = "OpenEXR scanline out of range";
+    std::vector<uint8_t> tmp, unpacked;
+    for (size_t blk = 0; blk < nblocks; blk++) {
+        const uint64_t off = get_u64(d, table + 8ull * blk);
+        if (off + 8 > d.size()) {
+            error = "OpenEXR block out of range";
             return false;
         }
-        const int32_t y = static_cast<int32_t>(get_u32(d, off)) - ymin;
-        if (y < 0 || y >= static_cast<int32_t>(h) || get_u32(d, off + 4) != line_bytes) {
-            error = "OpenEXR scanline block malformed";
+        const int32_t y0 = static_cast<int32_t>(get_u32(d, off)) - ymin;
+        const uint32_t packed = get_u32(d, off + 4);
+        if (y0 < 0 || y0 >= static_cast<int32_t>(h) || y0 % (int32_t)lines_per_block || off + 8 + packed > d.size()) {
+            error = "OpenEXR block malformed";
             return false;
         }
-        size_t q = off + 8;
-        for (auto &c : chans) {
-            const int ch = c.name == "R" ? 0 : c.name == "G" ? 1 : c.name == "B" ? 2 : c.name == "A" ? 3 : -1;
-            for (uint32_t x = 0; x < w; x++) {
-                float v;
-                if (c.type == 1) {
-                    v = half_to_float(static_cast<uint16_t>(d[q] | (d[q + 1] << 8)));
-                    q += 2;
-                } else {
-                    const uint32_t u = get_u32(d, q);
-                    std::memcpy(&v, &u, 4);
-                    q += 4;
+        const uint32_t nlines = std::min<uint32_t>(lines_per_block, h - (uint32_t)y0);
+        const size_t expect = (size_t)nlines * line_bytes;
+        const uint8_t *src = &d[off + 8];
+        if (packed != expect) {  // compressed block (a block that would not shrink is stored as is)
+            if (compression == 0 || packed > expect) {
+                error = "OpenEXR block of the wrong size";
+                return false;
+            }
+            tmp.clear();
+            if (compression == 1) {  // run-length: count < 0 -> -count literal bytes, else count + 1 copies
+                size_t q = 0;
+                while (q < packed && tmp.size() < expect) {
+                    const int cnt = static_cast<int8_t>(src[q++]);
+                    if (cnt < 0) {
+                        if (q + (size_t)(-cnt) > packed) break;
+                        tmp.insert(tmp.end(), src + q, src + q + (-cnt));
+                        q += (size_t)(-cnt);
+                    } else {
+                        if (q >= packed) break;
+                        tmp.insert(tmp.end(), (size_t)cnt + 1, src[q++]);
+                    }
                 }
-                if (ch >= 0) rgba[4 * ((size_t)y * w + x) + ch] = v;
+            } else if (!ZlibInflate(src, packed, tmp, expect, error)) {
+                error = "OpenEXR: " + error;
+                return false;
+            }
+            if (tmp.size() != expect) {
+                error = "OpenEXR: a compressed block unpacks to the wrong size";
+                return false;
+            }
+            // undo the byte predictor, then the split into even / odd bytes
+            for (size_t i = 1; i < tmp.size(); i++) tmp[i] = static_cast<uint8_t>(tmp[i - 1] + tmp[i] - 128);
+            unpacked.resize(expect);
+            const size_t half = (expect + 1) / 2;
+            for (size_t i = 0; i < expect; i++) unpacked[i] = (i & 1) ? tmp[half + i / 2] : tmp[i / 2];
+            src = unpacked.data();
+        }
+        for (uint32_t l = 0; l < nlines; l++) {
+            const uint32_t y = (uint32_t)y0 + l;
+            const uint8_t *q = src + (size_t)l * line_bytes;
+            for (auto &c : chans) {
+                const int ch = c.name == "R" ? 0 : c.name == "G" ? 1 : c.name == "B" ? 2 : c.name == "A" ? 3 : -1;
+                for (uint32_t x = 0; x < w; x++) {
+                    float v;
+                    if (c.type == 1) {
+                        v = half_to_float(static_cast<uint16_t>(q[0] | (q[1] << 8)));
+                        q += 2;
+                    } else {
+                        uint32_t u = (uint32_t)q[0] | (uint32_t)q[1] << 8 | (uint32_t)q[2] << 16 | (uint32_t)q[3] << 24;
+                        std::memcpy(&v, &u, 4);
+                        q += 4;
+                    }
+                    if (ch >= 0) rgba[4 * ((size_t)y * w + x) + ch] = v;
+                }
             }
         }
     }
@@ -388,14 +642,16 @@ bool SaveExrRGBA(const std::string &path, const float *rgba, uint32_t width, uin
 bool LoadImageRGBA(const std::string &path, std::vector<float> &rgba, uint32_t &width, uint32_t &height,
                    std::string &error) {
     const std::string ext = lower_ext(path);
-    if (ext != "hdr" && ext != "pfm" && ext != "exr") {
-        error = "image '" + path + "': only .hdr (RGBE), .pfm and uncompressed .exr images can be read";
+    if (ext != "hdr" && ext != "pfm" && ext != "exr" && ext != "png") {
+        error = "image '" + path + "': only .hdr (RGBE), .pfm, .png and .exr (uncompressed, RLE, ZIP) images can be "
+                "read; JPEG and the other 8-bit formats are not supported";
         return false;
     }
     std::vector<uint8_t> data;
     if (!read_all(path, data, error)) return false;
     const bool ok = ext == "hdr"   ? load_hdr(data, rgba, width, height, error)
                     : ext == "exr" ? load_exr(data, rgba, width, height, error)
+                    : ext == "png" ? load_png(data, rgba, width, height, error)
                                    : load_pfm(data, rgba, width, height, error);
     if (!ok) error = "image '" + path + "': " + error;
     return ok;

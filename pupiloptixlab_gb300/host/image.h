@@ -7,10 +7,15 @@
 //         mantissa * 2^(exponent - 136), 0 when the exponent byte is 0;
 //   .pfm  portable float map (PF colour / Pf grey, either byte order, rows
 //         stored bottom-up in the file);
-//   .exr  OpenEXR scanline images without compression (HALF or FLOAT R, G, B
-//         and optional A channels; compressed files are reported as such);
+//   .png  PNG of every colour type and bit depth, interlaced or not (8-bit
+//         samples as an 8-bit load gives them, converted as the reference
+//         converts them: (v / 255)^2.2 for colour, v / 255 for alpha);
+//   .exr  OpenEXR scanline images, uncompressed or RLE / ZIPS / ZIP
+//         compressed (HALF or FLOAT R, G, B and optional A channels; PIZ,
+//         PXR24, B44 and DWA are reported as unsupported);
 // all returned as RGBA floats, alpha 1, first row = top of the image, as
-// util::BitmapTexture holds them.  Other formats are reported as unsupported.
+// util::BitmapTexture holds them.  JPEG and other formats are reported as
+// unsupported.
 #pragma once
 
 #include <cstdint>

@@ -126,7 +126,7 @@ def test_obj_mesh(host):
     ("<scene><shape type='rectangle'><bsdf type='diffuse'><texture type='bitmap' name='reflectance'/>"
      "</bsdf></shape></scene>", "without a filename"),
     ("<scene><shape type='rectangle'><bsdf type='diffuse'><texture type='bitmap' name='reflectance'>"
-     "<string name='filename' value='a.png'/></texture></bsdf></shape></scene>", "uncompressed .exr images can be read"),
+     "<string name='filename' value='a.jpg'/></texture></bsdf></shape></scene>", "JPEG and the other 8-bit formats"),
     ("<scene><sensor type='thinlens'/></scene>", "perspective"),
     ("<scene><shape type='cube'><transform name='to_world'><translate x='abc'/></transform></shape></scene>",
      "malformed number"),
@@ -549,3 +549,218 @@ def test_textured_area_emitter_radiance(host):
     assert list(a.radiance_tex.color0) == [5.0, 4.0, 3.0] and list(a.radiance_tex.color1) == [1.0, 2.0, 3.0]
     assert a.radiance_tex.uv_transform[0] == 4.0 and a.radiance_tex.uv_transform[5] == 2.0
     assert b.is_emitter and not b.radiance_textured and list(b.radiance) == [2.0, 3.0, 4.0]
+
+
+
+# ---- PNG and compressed OpenEXR, written here by independent encoders ------
+
+def _png_bytes(samples, ctype, depth, interlace=False, palette=None, trns=None):
+    """A PNG file per the specification: samples (h, w, channels) integers,
+    rows filtered with filter types cycling through 0..4, Adam7 passes when
+    interlaced, one zlib stream split over two IDAT chunks."""
+    import struct
+    import zlib
+    h, w = samples.shape[:2]
+    ch = samples.shape[2]
+
+    def pack_row(row):
+        if depth >= 8:
+            return row.astype(">u2" if depth == 16 else "u1").tobytes()
+        bits = "".join(format(int(v), f"0{depth}b") for v in row.reshape(-1))
+        bits += "0" * (-len(bits) % 8)
+        return bytes(int(bits[i:i + 8], 2) for i in range(0, len(bits), 8))
+
+    bpp = max(1, ch * depth // 8)
+
+    def filt(lines):
+        out, prev = b"", bytes(len(lines[0])) if lines else b""
+        for k, cur in enumerate(lines):
+            f = k % 5
+            enc = bytearray()
+            for i, x in enumerate(cur):
+                a = cur[i - bpp] if i >= bpp else 0
+                b = prev[i]
+                c = prev[i - bpp] if i >= bpp else 0
+                if f == 0:
+                    pred = 0
+                elif f == 1:
+                    pred = a
+                elif f == 2:
+                    pred = b
+                elif f == 3:
+                    pred = (a + b) >> 1
+                else:
+                    pp = a + b - c
+                    pa, pb, pc = abs(pp - a), abs(pp - b), abs(pp - c)
+                    pred = a if (pa <= pb and pa <= pc) else (b if pb <= pc else c)
+                enc.append((x - pred) & 0xFF)
+            out += bytes([f]) + bytes(enc)
+            prev = cur
+        return out
+
+    passes = [(0, 0, 8, 8), (4, 0, 8, 8), (0, 4, 4, 8), (2, 0, 4, 4), (0, 2, 2, 4), (1, 0, 2, 2), (0, 1, 1, 2)] \
+        if interlace else [(0, 0, 1, 1)]
+    raw = b""
+    for x0, y0, dx, dy in passes:
+        sub = samples[y0::dy, x0::dx]
+        if sub.shape[0] == 0 or sub.shape[1] == 0:
+            continue
+        raw += filt([pack_row(r) for r in sub])
+    comp = zlib.compress(raw, 9)
+
+    def chunk(t, body):
+        return struct.pack(">I", len(body)) + t + body + struct.pack(">I", zlib.crc32(t + body) & 0xFFFFFFFF)
+
+    out = b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, depth, ctype, 0, 0, int(interlace)))
+    if palette is not None:
+        out += chunk(b"PLTE", bytes(np.asarray(palette, np.uint8).reshape(-1)))
+    if trns is not None:
+        out += chunk(b"tRNS", bytes(np.asarray(trns, np.uint8)))
+    out += chunk(b"tEXt", b"Comment\x00written by the test")
+    half = len(comp) // 2
+    return out + chunk(b"IDAT", comp[:half]) + chunk(b"IDAT", comp[half:]) + chunk(b"IEND", b"")
+
+
+def _load_env(host, path):
+    xml = f"""<scene version="3.0.0"><sensor type="perspective"><film type="hdrfilm"><integer name="width" value="8"/>
+      <integer name="height" value="8"/></film></sensor><shape type="rectangle"><bsdf type="diffuse"/></shape>
+      <emitter type="envmap"><string name="filename" value="{path}"/></emitter></scene>"""
+    s = host.XmlScene(xml, is_text=True)
+    e = s.desc().env
+    return np.ctypeslib.as_array(C.cast(e.pixels, C.POINTER(C.c_float)), shape=(e.height, e.width, 4)).copy()
+
+
+def _expect_rgba(img8, c):
+    """The reference's 8-bit conversion (framework/util/texture.cpp:106-118) of
+    samples with c channels: (v / 255)^2.2 of three consecutive bytes, alpha
+    byte / 255 for 4 channels; bytes past the end read as 0."""
+    flat = img8.reshape(-1).astype(np.float32)
+    n = flat.shape[0] // c
+    pad = np.concatenate([flat, np.zeros(4, np.float32)])
+    out = np.empty((n, 4), np.float32)
+    for k in range(3):
+        out[:, k] = np.power(pad[np.arange(n) * c + k] / np.float32(255.0), np.float32(2.2))
+    out[:, 3] = pad[np.arange(n) * c + 3] / np.float32(255.0) if c == 4 else 1.0
+    return out
+
+
+@pytest.mark.parametrize("ctype,depth,interlace", [(2, 8, False), (6, 8, True), (6, 16, False), (2, 16, True),
+                                                   (0, 8, False), (4, 8, True), (0, 4, True), (0, 1, False),
+                                                   (3, 8, False), (3, 2, True)])
+def test_png_reader(host, tmp_path, ctype, depth, interlace):
+    rng = np.random.default_rng(ctype * 100 + depth + interlace)
+    h, w = 11, 13
+    chans = {0: 1, 2: 3, 3: 1, 4: 2, 6: 4}[ctype]
+    palette = trns = None
+    if ctype == 3:
+        n = 1 << depth
+        palette = rng.integers(0, 256, (n, 3))
+        trns = rng.integers(0, 256, n // 2) if depth == 8 else None
+        samples = rng.integers(0, n, (h, w, 1))
+    else:
+        samples = rng.integers(0, 1 << depth, (h, w, chans))
+    path = tmp_path / "t.png"
+    path.write_bytes(_png_bytes(samples, ctype, depth, interlace, palette, trns))
+    got = _load_env(host, path)
+    # what an 8-bit load delivers
+    if ctype == 3:
+        rgb = np.asarray(palette, np.uint8)[samples[..., 0]]
+        if trns is not None:
+            a = np.array([trns[i] if i < len(trns) else 255 for i in samples.reshape(-1)], np.uint8).reshape(h, w, 1)
+            img8, c = np.concatenate([rgb, a], 2), 4
+        else:
+            img8, c = rgb, 3
+    elif depth == 16:
+        img8, c = (samples >> 8).astype(np.uint8), chans
+    elif depth < 8:
+        img8, c = (samples * (255 // ((1 << depth) - 1))).astype(np.uint8), chans
+    else:
+        img8, c = samples.astype(np.uint8), chans
+    expect = _expect_rgba(img8, c).reshape(h, w, 4)
+    assert np.allclose(got, expect, rtol=2e-7, atol=0), np.abs(got - expect).max()
+    if c == 4:
+        assert np.array_equal(got[..., 3], expect[..., 3])
+
+
+def _exr_bytes(img, compression, half):
+    """A scanline OpenEXR file with channels A B G R (HALF or FLOAT), RLE
+    (1), ZIPS (2) or ZIP (3) compressed blocks per the file-format
+    description: bytes split into even / odd halves, delta-predicted (+128),
+    then run-length or zlib coded."""
+    import struct
+    import zlib
+    h, w = img.shape[:2]
+    lpb = 16 if compression == 3 else 1
+    typ = 1 if half else 2
+
+    def attr(name, t, value):
+        return name.encode() + b"\0" + t.encode() + b"\0" + struct.pack("<i", len(value)) + value
+
+    chl = b"".join(c + b"\0" + struct.pack("<iB3xii", typ, 0, 1, 1) for c in (b"A", b"B", b"G", b"R")) + b"\0"
+    head = struct.pack("<ii", 20000630, 2)
+    head += attr("channels", "chlist", chl) + attr("compression", "compression", bytes([compression]))
+    head += attr("dataWindow", "box2i", struct.pack("<4i", 0, 0, w - 1, h - 1))
+    head += attr("displayWindow", "box2i", struct.pack("<4i", 0, 0, w - 1, h - 1))
+    head += attr("lineOrder", "lineOrder", b"\0") + attr("pixelAspectRatio", "float", struct.pack("<f", 1.0))
+    head += attr("screenWindowCenter", "v2f", struct.pack("<ff", 0, 0)) + attr("screenWindowWidth", "float",
+                                                                                struct.pack("<f", 1.0)) + b"\0"
+    dt = "<f2" if half else "<f4"
+    blocks = []
+    for y0 in range(0, h, lpb):
+        raw = b"".join(img[y, :, ci].astype(dt).tobytes() for y in range(y0, min(h, y0 + lpb)) for ci in (3, 2, 1, 0))
+        t = bytearray(raw[0::2] + raw[1::2])
+        for i in range(len(t) - 1, 0, -1):
+            t[i] = (t[i] - t[i - 1] + 128) & 0xFF
+        if compression == 1:
+            enc, i = bytearray(), 0
+            while i < len(t):
+                run = 1
+                while i + run < len(t) and t[i + run] == t[i] and run < 128:
+                    run += 1
+                if run >= 3:
+                    enc += bytes([run - 1, t[i]])
+                    i += run
+                else:
+                    j = i
+                    while j < len(t) and j - i < 127 and not (j + 2 < len(t) and t[j] == t[j + 1] == t[j + 2]):
+                        j += 1
+                    enc += bytes([(256 - (j - i)) & 0xFF]) + bytes(t[i:j])
+                    i = j
+            data = bytes(enc)
+        else:
+            data = zlib.compress(bytes(t), 6)
+        if len(data) >= len(raw):
+            data = raw
+        blocks.append(struct.pack("<ii", y0, len(data)) + data)
+    table_at = len(head)
+    offsets, pos = [], table_at + 8 * len(blocks)
+    for b in blocks:
+        offsets.append(pos)
+        pos += len(b)
+    return head + b"".join(struct.pack("<Q", o) for o in offsets) + b"".join(blocks)
+
+
+@pytest.mark.parametrize("compression,half", [(1, True), (2, False), (3, True), (3, False)])
+def test_compressed_exr_reader(host, tmp_path, compression, half):
+    rng = np.random.default_rng(compression * 10 + half)
+    h, w = 37, 21
+    img = rng.uniform(0, 4, (h, w, 4)).astype(np.float32)
+    img[5:20, 3:9, :3] = 1.5  # runs for the run-length coder
+    img[..., 3] = rng.uniform(0.5, 1.0, (h, w)).astype(np.float32)
+    if half:
+        img = img.astype(np.float16).astype(np.float32)
+    path = tmp_path / "t.exr"
+    path.write_bytes(_exr_bytes(img, compression, half))
+    got = _load_env(host, path)
+    assert np.array_equal(got, img)
+
+
+def test_compression_the_reader_does_not_take_is_reported(host, tmp_path):
+    data = bytearray(_exr_bytes(np.ones((4, 4, 4), np.float32), 3, False))
+    i = data.index(b"compression\0compression\0") + len(b"compression\0compression\0") + 4
+    data[i] = 4  # PIZ
+    path = tmp_path / "piz.exr"
+    path.write_bytes(bytes(data))
+    with pytest.raises(abi.PtError) as e:
+        _load_env(host, path)
+    assert "PIZ" in str(e.value)
