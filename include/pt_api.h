@@ -521,6 +521,13 @@ int pt_denoiser_layer(const pt_denoiser *dn, uint32_t index, uint32_t *cin, uint
 /* HOST pointers: copy the FP32 master parameters out / in (in: also resets Adam). */
 int pt_denoiser_get_params(const pt_denoiser *dn, float *params);
 int pt_denoiser_set_params(pt_denoiser *dn, const float *params);
+/* Optimizer state, so that training can stop and resume (no counterpart in
+ * the reference, whose OptiX denoiser is not trained): HOST pointers to
+ * 2 * num_params + 4 floats -- Adam's first moments, second moments, then the
+ * step count, the two bias corrections and the step size.  set_state after
+ * set_params continues the saved run (set_params resets the state). */
+int pt_denoiser_get_state(const pt_denoiser *dn, float *state);
+int pt_denoiser_set_state(pt_denoiser *dn, const float *state);
 /* Forward + backward of the L1 log loss on a batch; gradients stay on the
  * device (pt_denoiser_get_grads, HOST pointer), *loss (HOST) the batch mean. */
 int pt_denoiser_compute_grads(pt_denoiser *dn, const void *input_f16, const float *target, uint32_t n,

@@ -184,6 +184,8 @@ PROTOTYPES = [
     ("pt_denoiser_layer", C.c_int, [C.c_void_p, C.c_uint32, c_uint_p, c_uint_p, C.POINTER(C.c_uint64)]),
     ("pt_denoiser_get_params", C.c_int, [C.c_void_p, C.c_void_p]),
     ("pt_denoiser_set_params", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("pt_denoiser_get_state", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("pt_denoiser_set_state", C.c_int, [C.c_void_p, C.c_void_p]),
     ("pt_denoiser_compute_grads", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32,
                                             C.POINTER(C.c_float), C.c_void_p]),
     ("pt_denoiser_get_grads", C.c_int, [C.c_void_p, C.c_void_p]),

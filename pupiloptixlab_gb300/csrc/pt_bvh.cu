@@ -21,6 +21,7 @@
 // that the conservative slab test never rejects a primitive the exact test
 // would hit.
 
+#include "pt_nvtx.h"
 #include "pt_internal.h"
 
 #include <algorithm>
@@ -984,6 +985,7 @@ int ploc_build(pt_scene *s, const Scratch &sc, uint32_t n, int max_leaf, cudaStr
 }  // namespace
 
 int pt_bvh_build_impl(pt_scene *s, const pt_bvh_opts *o, cudaStream_t st) {
+    pt_nvtx::Range nv("pt_bvh_build");
     const uint32_t n = s->num_prims;
     const uint32_t tiles = std::max<uint32_t>(1, (n + kSortTile - 1) / kSortTile);
     const int K = (int)o->width;
@@ -1131,6 +1133,7 @@ int pt_bvh_build_impl(pt_scene *s, const pt_bvh_opts *o, cudaStream_t st) {
 }
 
 int pt_bvh_refit_impl(pt_scene *s, cudaStream_t st) {
+    pt_nvtx::Range nv("pt_bvh_refit");
     const uint32_t n = s->num_prims;
     PT_CUDA_TRY(cudaEventRecord(s->ev0, st));
     if (n > 0)

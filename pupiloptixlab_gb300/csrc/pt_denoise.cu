@@ -21,6 +21,7 @@
 // Input channels: log(1 + max(rgb, 0)), albedo, normal, 7 zero channels.
 // Output: a log-domain correction; the denoised colour is
 // expm1(output + log(1 + max(rgb, 0))).
+#include "pt_nvtx.h"
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -860,6 +861,40 @@ int pt_denoiser_set_params(pt_denoiser *dn, const float *params) {
     return upload_params(dn, params);
 }
 
+int pt_denoiser_get_state(const pt_denoiser *dn, float *state) {
+    (void)cudaGetLastError();
+    if (!dn || !state) {
+        pt_set_error("pt_denoiser_get_state: NULL argument");
+        return PT_ERR_INVALID;
+    }
+    PT_CUDA_TRY(cudaSetDevice(dn->device));
+    PT_CUDA_TRY(cudaStreamSynchronize(dn->stream));
+    const size_t n = dn->nparams;
+    PT_CUDA_TRY(cudaMemcpy(state, dn->adam_m.ptr, n * sizeof(float), cudaMemcpyDeviceToHost));
+    PT_CUDA_TRY(cudaMemcpy(state + n, dn->adam_v.ptr, n * sizeof(float), cudaMemcpyDeviceToHost));
+    PT_CUDA_TRY(cudaMemcpy(state + 2 * n, dn->adam_state.ptr, 4 * sizeof(float), cudaMemcpyDeviceToHost));
+    return PT_OK;
+}
+
+int pt_denoiser_set_state(pt_denoiser *dn, const float *state) {
+    (void)cudaGetLastError();
+    if (!dn || !state) {
+        pt_set_error("pt_denoiser_set_state: NULL argument");
+        return PT_ERR_INVALID;
+    }
+    const size_t n = dn->nparams;
+    if (!(state[2 * n] >= 0.f) || !(state[2 * n + 3] >= 0.f)) {
+        pt_set_error("pt_denoiser_set_state: bad step count or step size");
+        return PT_ERR_INVALID;
+    }
+    PT_CUDA_TRY(cudaSetDevice(dn->device));
+    PT_CUDA_TRY(cudaStreamSynchronize(dn->stream));
+    PT_CUDA_TRY(cudaMemcpy(dn->adam_m.ptr, state, n * sizeof(float), cudaMemcpyHostToDevice));
+    PT_CUDA_TRY(cudaMemcpy(dn->adam_v.ptr, state + n, n * sizeof(float), cudaMemcpyHostToDevice));
+    PT_CUDA_TRY(cudaMemcpy(dn->adam_state.ptr, state + 2 * n, 4 * sizeof(float), cudaMemcpyHostToDevice));
+    return PT_OK;
+}
+
 int pt_denoiser_set_lr(pt_denoiser *dn, float lr) {
     (void)cudaGetLastError();
     if (!dn || !(lr >= 0.f)) {
@@ -914,6 +949,7 @@ int pt_denoiser_compute_grads(pt_denoiser *dn, const void *input_f16, const floa
 
 int pt_denoiser_train_step(pt_denoiser *dn, const void *input_f16, const float *target, uint32_t n, uint32_t crop,
                            void *stream) {
+    pt_nvtx::Range nv("pt_denoiser_train_step");
     (void)cudaGetLastError();
     if (!dn || !input_f16 || !target) {
         pt_set_error("pt_denoiser_train_step: NULL argument");
@@ -997,6 +1033,7 @@ int pt_denoiser_forward(pt_denoiser *dn, const void *input_f16, uint32_t n, uint
 }
 
 int pt_denoise(pt_denoiser *dn, const pt_denoise_io *io, void *stream) {
+    pt_nvtx::Range nv("pt_denoise");
     (void)cudaGetLastError();
     if (!dn || !io || !io->color || !io->albedo || !io->normal || !io->output || !io->width || !io->height) {
         pt_set_error("pt_denoise: NULL argument or empty frame");

@@ -22,6 +22,7 @@
 
 #include "pt_internal.h"
 #include "pt_bsdf.cuh"
+#include "pt_nvtx.h"
 #include "pt_traverse.cuh"
 
 #include <algorithm>
@@ -892,6 +893,7 @@ struct Launcher {
         Timer tm;
         uint32_t launches = 0;
         uint32_t waves = 0;
+        pt_nvtx::Range nv_render(graph ? "pt_render: capture" : "pt_render: launches");
         if (!graph) PT_CUDA_TRY(cudaEventRecord(t.ev0, st));
         cudaError_t enq = cudaMemsetAsync(ws.counters.ptr, 0, 256, ls);
         for (uint32_t f0 = 0; f0 < p->spp && enq == cudaSuccess; f0 += frames_per_wave) {
@@ -908,11 +910,19 @@ struct Launcher {
             stt.q_in = ws.q0.as<uint32_t>();
             stt.q_out = ws.q1.as<uint32_t>();
             const size_t slots = (size_t)w.frames * npix;
-            k_raygen<BATCH><<<nblocks(slots, 256), 256, 0, ls>>>(d, bt, stt, w);
+            pt_nvtx::Range nv_wave("wave");
+            {
+                pt_nvtx::Range r("raygen");
+                k_raygen<BATCH><<<nblocks(slots, 256), 256, 0, ls>>>(d, bt, stt, w);
+            }
             launches++;
             for (uint32_t b = 0; b < bounces; b++) {
+                pt_nvtx::Range nv_bounce("bounce");
                 if (timing) tm.mark(0, ls);
-                k_ext<<<grid_trace, tb, smem, ls>>>(d, stt, bt, npix);
+                {
+                    pt_nvtx::Range r("extend (closest hit)");
+                    k_ext<<<grid_trace, tb, smem, ls>>>(d, stt, bt, npix);
+                }
                 if (timing) tm.mark(0, ls);
                 State shade_st = stt;
                 if (sort && BATCH) {
@@ -930,15 +940,24 @@ struct Launcher {
                     launches += 3;
                 }
                 if (timing) tm.mark(2, ls);
-                k_shade<BATCH><<<grid_shade, 256, 0, ls>>>(d, bt, shade_st, w, out);
+                {
+                    pt_nvtx::Range r("shade (MIS, NEE, BSDF sample)");
+                    k_shade<BATCH><<<grid_shade, 256, 0, ls>>>(d, bt, shade_st, w, out);
+                }
                 if (timing) { tm.mark(2, ls); tm.mark(1, ls); }
-                k_sh<<<grid_trace, tb, smem, ls>>>(d, stt, bt, npix);
+                {
+                    pt_nvtx::Range r("shadow (any hit)");
+                    k_sh<<<grid_trace, tb, smem, ls>>>(d, stt, bt, npix);
+                }
                 if (timing) tm.mark(1, ls);
                 k_advance<<<1, 1, 0, ls>>>(stt.counters);
                 launches += 4;
                 std::swap(stt.q_in, stt.q_out);
             }
-            k_accumulate<BATCH><<<nblocks(npix, 256), 256, 0, ls>>>(stt, w, out, bt);
+            {
+                pt_nvtx::Range r("accumulate");
+                k_accumulate<BATCH><<<nblocks(npix, 256), 256, 0, ls>>>(stt, w, out, bt);
+            }
             launches++;
             waves++;
             enq = cudaGetLastError();
@@ -971,6 +990,7 @@ struct Launcher {
                 }
             }
             cudaGraphDestroy(g);
+            pt_nvtx::Range r("pt_render: graph launch");
             PT_CUDA_TRY(cudaEventRecord(t.ev0, ws.stream));
             PT_CUDA_TRY(cudaGraphLaunch(ws.exec, ws.stream));
             PT_CUDA_TRY(cudaEventRecord(t.ev1, ws.stream));

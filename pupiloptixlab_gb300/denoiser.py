@@ -111,6 +111,28 @@ class Denoiser:
         assert p.size == self.num_params
         abi.check(self.lib.pt_denoiser_set_params(self.handle, p.ctypes.data_as(C.c_void_p)), "set_params", self.lib)
 
+    def get_state(self) -> np.ndarray:
+        """Adam's moments and counters (2 * num_params + 4 floats)."""
+        out = np.empty(2 * self.num_params + 4, np.float32)
+        abi.check(self.lib.pt_denoiser_get_state(self.handle, out.ctypes.data_as(C.c_void_p)), "pt_denoiser_get_state",
+                  self.lib)
+        return out
+
+    def set_state(self, state: np.ndarray) -> None:
+        st = np.ascontiguousarray(state, np.float32)
+        assert st.shape == (2 * self.num_params + 4,)
+        abi.check(self.lib.pt_denoiser_set_state(self.handle, st.ctypes.data_as(C.c_void_p)), "pt_denoiser_set_state",
+                  self.lib)
+
+    def save(self, path) -> None:
+        """Weights and optimizer state to one .npz file."""
+        np.savez(path, params=self.get_params(), state=self.get_state())
+
+    def load(self, path) -> None:
+        d = np.load(path)
+        self.set_params(d["params"])
+        self.set_state(d["state"])
+
     def get_grads(self) -> np.ndarray:
         g = np.empty(self.num_params, dtype=np.float32)
         abi.check(self.lib.pt_denoiser_get_grads(self.handle, g.ctypes.data_as(C.c_void_p)), "get_grads", self.lib)

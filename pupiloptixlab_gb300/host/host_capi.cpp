@@ -83,6 +83,52 @@ int pupil_run_scene(const char *xml, int is_text, uint32_t frames, uint32_t rng,
     return PT_OK;
 }
 
+// The same with the world changing in between, through the events the pass
+// subscribes to: after `change_after` frames, `positions` (host, every mesh's
+// object-space vertices in mesh order; may be NULL) arrive as
+// EWorldEvent::RenderInstanceUpdate (refit) and `camera` (may be NULL) as
+// EWorldEvent::CameraChange; both restart accumulation.  `resume_from` (may
+// be NULL) loads a progress file right after the scene, `save_to` (may be
+// NULL) saves one after the last frame.
+int pupil_run_scene_ex(const char *xml, int is_text, uint32_t frames, uint32_t rng, const char *resume_from,
+                       const char *save_to, uint32_t change_after, const float *positions,
+                       const pt_camera_desc *camera, float *out_rgba, uint32_t *out_w, uint32_t *out_h) {
+    using namespace Pupil;
+    auto scene = std::make_unique<resource::Scene>();
+    if (!(is_text ? scene->LoadFromString(xml, "") : scene->LoadFromXML(xml))) return fail(scene->error());
+    uint32_t w = scene->sensor.width, h = scene->sensor.height;
+    System sys;
+    if (!sys.Init(0)) return fail(sys.error(), PT_ERR_UNSUPPORTED);
+    pt::WavefrontPTPass pass;
+    pass.SetRng(rng);
+    sys.AddPass(&pass);
+    auto bail = [&](const std::string &e, int st) {
+        sys.Destroy();
+        return fail(e, st);
+    };
+    if (!sys.SetScene(std::move(scene))) return bail(sys.error(), PT_ERR_CUDA);
+    if (resume_from && !pass.LoadProgress(resume_from)) return bail(pass.last_error(), PT_ERR_INVALID);
+    const bool change = positions || camera;
+    for (uint32_t f = 0; f < frames; f++) {
+        if (change && f == change_after) {
+            if (positions) sys.UpdateInstances(positions, false);
+            if (camera) sys.SetCamera(*camera);
+        }
+        sys.Run(1);
+        if (pass.last_status() != PT_OK) return bail(pass.last_error(), pass.last_status());
+    }
+    if (pass.last_status() != PT_OK) return bail(pass.last_error(), pass.last_status());
+    if (save_to && !pass.SaveProgress(save_to)) return bail(pass.last_error(), PT_ERR_INVALID);
+    if (out_rgba) {
+        auto *fr = sys.buffers().GetBuffer("final result");
+        cudaMemcpy(out_rgba, fr->device, (size_t)w * h * 16, cudaMemcpyDeviceToHost);
+    }
+    if (out_w) *out_w = w;
+    if (out_h) *out_h = h;
+    sys.Destroy();
+    return PT_OK;
+}
+
 // Portable float map (little endian, bottom row first: row 0 of the frame
 // buffer is the bottom of the image, as in the reference's display path).
 int pupil_write_pfm(const char *path, const float *rgba, uint32_t w, uint32_t h) {

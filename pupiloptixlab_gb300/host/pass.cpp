@@ -5,7 +5,9 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cstdio>
 #include <cstring>
+#include <vector>
 
 namespace Pupil {
 
@@ -105,15 +107,24 @@ bool System::SetScene(std::unique_ptr<resource::Scene> scene) {
         return false;
     }
     for (Pass *p : m_pre_passes) p->Run();
-    for (Pass *p : m_passes) {
-        if (auto *pt = dynamic_cast<pt::WavefrontPTPass *>(p)) {
-            if (!pt->SetScene(m_scene.get(), m_ctx, m_buffers)) {
-                m_error = pt->last_error();
-                return false;
-            }
+    SceneLoadEvent ev{m_scene.get(), m_ctx, &m_buffers};
+    EventDispatcher<ESystemEvent::SceneLoad>(&ev);
+    for (Pass *p : m_passes)
+        if (auto *pt = dynamic_cast<pt::WavefrontPTPass *>(p); pt && pt->last_status() != PT_OK) {
+            m_error = pt->last_error();
+            return false;
         }
-    }
     return true;
+}
+
+void System::SetCamera(const pt_camera_desc &camera) {
+    pt_camera_desc c = camera;
+    EventDispatcher<EWorldEvent::CameraChange>(&c);
+}
+
+void System::UpdateInstances(const float *positions, bool on_device, bool rebuild) {
+    InstanceUpdateEvent ev{positions, on_device ? 1 : 0, rebuild};
+    EventDispatcher<EWorldEvent::RenderInstanceUpdate>(&ev);
 }
 
 void System::Run(uint32_t frames) {
@@ -135,13 +146,31 @@ void System::Destroy() {
 
 namespace pt {
 
+// The events PTPass subscribes to (pt_pass.cpp:242-254).
 WavefrontPTPass::WavefrontPTPass(std::string_view n) noexcept : Pass(n) {
     m_params.spp = 1;
     m_params.accumulate = 1;
     m_params.rng = PT_RNG_REF_LCG;
+    m_ev_scene = EventBinder<ESystemEvent::SceneLoad>([this](void *p) {
+        auto *e = static_cast<SceneLoadEvent *>(p);
+        SetScene(e->scene, e->ctx, *e->buffers);
+    });
+    m_ev_camera = EventBinder<EWorldEvent::CameraChange>([this](void *p) {
+        if (p) SetCamera(*static_cast<const pt_camera_desc *>(p));
+        else m_dirty = true;
+    });
+    m_ev_update = EventBinder<EWorldEvent::RenderInstanceUpdate>([this](void *p) {
+        if (p) UpdateInstances(*static_cast<const InstanceUpdateEvent *>(p));
+        else m_dirty = true;
+    });
 }
 
-WavefrontPTPass::~WavefrontPTPass() noexcept { ReleaseScene(); }
+WavefrontPTPass::~WavefrontPTPass() noexcept {
+    EventUnbind<ESystemEvent::SceneLoad>(m_ev_scene);
+    EventUnbind<EWorldEvent::CameraChange>(m_ev_camera);
+    EventUnbind<EWorldEvent::RenderInstanceUpdate>(m_ev_update);
+    ReleaseScene();
+}
 
 void WavefrontPTPass::ReleaseScene() noexcept {
     if (m_scene) pt_scene_destroy(m_scene);
@@ -152,6 +181,7 @@ void WavefrontPTPass::ReleaseScene() noexcept {
 bool WavefrontPTPass::SetScene(resource::Scene *scene, pt_context *ctx, BufferManager &buffers) noexcept {
     if (m_scene) pt_scene_destroy(m_scene);
     m_scene = nullptr;
+    m_status = PT_OK;
     const pt_scene_desc &d = scene->Desc();
     if ((m_status = pt_scene_upload(ctx, &d, &m_scene)) != PT_OK ||
         (m_status = pt_bvh_build(m_scene, &m_bvh, nullptr)) != PT_OK) {
@@ -176,7 +206,113 @@ bool WavefrontPTPass::SetScene(resource::Scene *scene, pt_context *ctx, BufferMa
     m_fb.test = static_cast<float *>(test->device);
     m_params.max_depth = d.max_depth;
     m_camera = d.camera;
+    m_width = d.width;
+    m_height = d.height;
     m_dirty = true;
+    return true;
+}
+
+bool WavefrontPTPass::UpdateInstances(const InstanceUpdateEvent &e) noexcept {
+    if (!m_scene) return false;
+    m_status = pt_scene_update_all_vertices(m_scene, e.positions, e.on_device, nullptr);
+    if (m_status == PT_OK) {
+        if (e.rebuild) {
+            pt_bvh_opts o = m_bvh;
+            o.flags |= 1u;  // PT_BVH_FAST_BUILD: the per-frame rebuild
+            m_status = pt_bvh_build(m_scene, &o, nullptr);
+        } else {
+            m_status = pt_bvh_refit(m_scene, nullptr);
+        }
+    }
+    if (m_status != PT_OK) {
+        m_error = pt_error();
+        return false;
+    }
+    m_dirty = true;
+    return true;
+}
+
+namespace {
+constexpr char kProgressMagic[8] = {'P', 'T', 'P', 'R', 'O', 'G', '1', 0};
+struct ProgressHeader {
+    char magic[8];
+    uint32_t width, height, sample_cnt, seed, max_depth, rng, accumulate, reserved;
+    pt_camera_desc camera;
+};
+}  // namespace
+
+bool WavefrontPTPass::SaveProgress(const std::string &path) noexcept {
+    if (!m_scene || !m_fb.accum) {
+        m_error = "SaveProgress: no scene";
+        return false;
+    }
+    ProgressHeader h{};
+    std::memcpy(h.magic, kProgressMagic, 8);
+    h.width = m_width;
+    h.height = m_height;
+    h.sample_cnt = m_dirty ? 0 : m_params.sample_cnt;
+    h.seed = m_dirty ? 0 : m_params.seed;
+    h.max_depth = m_params.max_depth;
+    h.rng = m_params.rng;
+    h.accumulate = m_accumulate ? 1 : 0;
+    h.camera = m_camera;
+    std::vector<float> accum(4ull * m_width * m_height);
+    if (cudaMemcpy(accum.data(), m_fb.accum, accum.size() * 4, cudaMemcpyDeviceToHost) != cudaSuccess) {
+        m_error = "SaveProgress: reading the accumulation buffer failed";
+        return false;
+    }
+    FILE *f = fopen(path.c_str(), "wb");
+    if (!f) {
+        m_error = "SaveProgress: cannot write " + path;
+        return false;
+    }
+    const bool ok = fwrite(&h, sizeof(h), 1, f) == 1 && fwrite(accum.data(), 4, accum.size(), f) == accum.size();
+    fclose(f);
+    if (!ok) m_error = "SaveProgress: write failed";
+    return ok;
+}
+
+bool WavefrontPTPass::LoadProgress(const std::string &path) noexcept {
+    if (!m_scene || !m_fb.accum) {
+        m_error = "LoadProgress: no scene";
+        return false;
+    }
+    FILE *f = fopen(path.c_str(), "rb");
+    if (!f) {
+        m_error = "LoadProgress: cannot read " + path;
+        return false;
+    }
+    ProgressHeader h{};
+    std::vector<float> accum;
+    bool ok = fread(&h, sizeof(h), 1, f) == 1 && std::memcmp(h.magic, kProgressMagic, 8) == 0;
+    if (ok && (h.width != m_width || h.height != m_height)) {
+        fclose(f);
+        m_error = "LoadProgress: the saved image is " + std::to_string(h.width) + "x" + std::to_string(h.height) +
+                  ", the scene's film " + std::to_string(m_width) + "x" + std::to_string(m_height);
+        return false;
+    }
+    if (ok) {
+        accum.resize(4ull * h.width * h.height);
+        ok = fread(accum.data(), 4, accum.size(), f) == accum.size();
+    }
+    fclose(f);
+    if (!ok) {
+        m_error = "LoadProgress: " + path + " is not a progress file of this pass";
+        return false;
+    }
+    if (cudaMemcpy(m_fb.accum, accum.data(), accum.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess) {
+        m_error = "LoadProgress: writing the accumulation buffer failed";
+        return false;
+    }
+    m_camera = h.camera;
+    pt_scene_set_camera(m_scene, &m_camera);
+    m_params.sample_cnt = h.sample_cnt;
+    m_params.seed = h.seed;
+    m_params.max_depth = h.max_depth;
+    m_params.rng = h.rng;
+    m_accumulate = h.accumulate != 0;
+    m_params.accumulate = h.accumulate;
+    m_dirty = false;  // continue the saved sequence
     return true;
 }
 

@@ -17,6 +17,7 @@
 #include <string_view>
 #include <vector>
 
+#include "event.h"
 #include "pt_api.h"
 #include "scene.h"
 
@@ -75,6 +76,18 @@ private:
     std::vector<std::string> m_names;
 };
 
+// Payloads of the events System dispatches.
+struct SceneLoadEvent {  // ESystemEvent::SceneLoad (the reference passes its world::World *)
+    resource::Scene *scene;
+    pt_context *ctx;
+    BufferManager *buffers;
+};
+struct InstanceUpdateEvent {  // EWorldEvent::RenderInstanceUpdate
+    const float *positions;    // every mesh's object-space vertices, in mesh order (pt_scene_update_all_vertices)
+    int on_device;             // positions in device memory
+    bool rebuild;              // rebuild the BVH (PT_BVH_FAST_BUILD) instead of refitting it
+};
+
 class System {
 public:
     // system.h:26-27: the render loop runs the passes only while render_flag
@@ -86,7 +99,13 @@ public:
     bool Init(int device = 0);
     void AddPass(Pass *pass);
     bool SetScene(const std::string &xml_path);
+    // System::SetScene (system.cpp:136-173): the "final result" buffer, then
+    // ESystemEvent::SceneLoad to every pass that subscribed
     bool SetScene(std::unique_ptr<resource::Scene> scene);
+    // the world's camera moved (EWorldEvent::CameraChange, payload pt_camera_desc *)
+    void SetCamera(const pt_camera_desc &camera);
+    // instances changed (EWorldEvent::RenderInstanceUpdate; world.cpp:45-59)
+    void UpdateInstances(const float *positions, bool on_device, bool rebuild = false);
     void Run(uint32_t frames);
     void Destroy();
 
@@ -114,6 +133,14 @@ public:
 
     // SceneLoad event: upload the scene, build the BVH, allocate the pass buffers.
     bool SetScene(resource::Scene *scene, pt_context *ctx, BufferManager &buffers) noexcept;
+    // RenderInstanceUpdate event: new vertices, refit or rebuild, restart accumulation.
+    bool UpdateInstances(const InstanceUpdateEvent &e) noexcept;
+    // Progressive resume (the reference keeps its accumulation only in device
+    // memory): the accumulation buffer, sample count, seed, camera and render
+    // settings to a file, and back into a pass whose scene has the same size;
+    // the frames rendered after LoadProgress continue the saved sequence exactly.
+    bool SaveProgress(const std::string &path) noexcept;
+    bool LoadProgress(const std::string &path) noexcept;
     // CameraChange event: restart accumulation with the new camera.
     void SetCamera(const pt_camera_desc &camera) noexcept;
     void SetMaxDepth(uint32_t depth) noexcept;
@@ -138,6 +165,8 @@ private:
     bool m_accumulate = true;
     int m_status = PT_OK;
     std::string m_error;
+    uint32_t m_width = 0, m_height = 0;
+    uint64_t m_ev_scene = 0, m_ev_camera = 0, m_ev_update = 0;  // event subscriptions
 };
 
 }  // namespace pt

@@ -28,6 +28,9 @@ def load() -> C.CDLL:
         lib.pupil_run_scene.argtypes = [C.c_char_p, C.c_int, C.c_uint32, C.c_uint32, C.c_void_p,
                                         C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
         lib.pupil_write_pfm.argtypes = [C.c_char_p, C.c_void_p, C.c_uint32, C.c_uint32]
+        lib.pupil_run_scene_ex.argtypes = [C.c_char_p, C.c_int, C.c_uint32, C.c_uint32, C.c_char_p, C.c_char_p,
+                                           C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p,
+                                           C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
         lib.pupil_write_exr.argtypes = [C.c_char_p, C.c_void_p, C.c_uint32, C.c_uint32]
         _lib = lib
     return _lib
@@ -74,6 +77,26 @@ def run_scene(path_or_text: str, frames: int, rng: int = abi.RNG_REF_LCG, is_tex
                              out.ctypes.data_as(C.c_void_p), C.byref(w), C.byref(h))
     if st != 0:
         raise abi.PtError(st, "pupil_run_scene", last_error())
+    return out
+
+
+def run_scene_ex(path_or_text: str, frames: int, rng: int = abi.RNG_REF_LCG, is_text: bool = False,
+                 resume_from: str | None = None, save_to: str | None = None, change_after: int = 0,
+                 positions: np.ndarray | None = None, camera=None) -> np.ndarray:
+    """System + WavefrontPTPass with the world changing through its events
+    (pupil_run_scene_ex); returns the final frame (h*w, 4)."""
+    lib = load()
+    xs = XmlScene(path_or_text, is_text=is_text)
+    out = np.zeros((xs.width * xs.height, 4), np.float32)
+    pos = None if positions is None else np.ascontiguousarray(positions, np.float32)
+    w, h = C.c_uint32(), C.c_uint32()
+    st = lib.pupil_run_scene_ex(path_or_text.encode(), 1 if is_text else 0, frames, rng,
+                                resume_from.encode() if resume_from else None, save_to.encode() if save_to else None,
+                                change_after, pos.ctypes.data_as(C.c_void_p) if pos is not None else None,
+                                C.byref(camera) if camera is not None else None, out.ctypes.data_as(C.c_void_p),
+                                C.byref(w), C.byref(h))
+    if st != 0:
+        raise abi.PtError(st, "pupil_run_scene_ex", last_error())
     return out
 
 

@@ -194,3 +194,44 @@ def test_trained_network_beats_raw_accumulation(cuda_ctx):
     trained = log_rmse(d.forward(xt), yt)
     d.close()
     assert np.isfinite(trained) and trained < 0.8 * raw, (trained, raw)
+
+
+def test_training_resumes_from_saved_weights_and_optimizer_state(cuda_ctx, tmp_path):
+    """Checkpoint / resume of training: 8 Adam steps, save weights and optimizer
+    state (Denoiser.save: pt_denoiser_get_params + pt_denoiser_get_state),
+    8 more steps; a fresh denoiser that loads the file and takes the same 8
+    steps ends at the same weights (within the run-to-run spread of the FP32
+    atomic weight-gradient sums), while one that loads only the weights
+    (optimizer reset) ends elsewhere."""
+    from pupiloptixlab_gb300.denoiser import Denoiser
+    g = torch.Generator().manual_seed(11)
+    tgt = torch.rand(4, 64, 64, 3, generator=g) * 2.0
+    inp = torch.cat([tgt * torch.exp(0.5 * torch.randn(4, 64, 64, 3, generator=g)),
+                     torch.rand(4, 64, 64, 6, generator=g)], dim=-1).to(torch.float16).cuda()
+    tgt = tgt.cuda()
+    a = Denoiser(cuda_ctx, seed=4, lr=2e-3)
+    for _ in range(8):
+        a.train_step(inp, tgt)
+    path = tmp_path / "dn.npz"
+    a.save(path)
+    saved = np.load(path)
+    assert saved["state"][2 * a.num_params] == 8.0  # step count
+    for _ in range(8):
+        a.train_step(inp, tgt)
+    ref = a.get_params()
+    b = Denoiser(cuda_ctx, seed=9, lr=2e-3)
+    b.load(path)
+    for _ in range(8):
+        b.train_step(inp, tgt)
+    resumed = b.get_params()
+    c = Denoiser(cuda_ctx, seed=9, lr=2e-3)
+    c.set_params(saved["params"])
+    for _ in range(8):
+        c.train_step(inp, tgt)
+    reset = c.get_params()
+    step = np.linalg.norm(ref - saved["params"])
+    d_resumed, d_reset = np.linalg.norm(resumed - ref), np.linalg.norm(reset - ref)
+    assert d_resumed <= 1e-3 * step, (d_resumed, step)
+    assert d_reset > 20 * d_resumed + 1e-6, (d_reset, d_resumed)
+    for x in (a, b, c):
+        x.close()

@@ -107,7 +107,7 @@ def test_textured_area_emitters(cuda_ctx):
 
     import test_oracle_emitters_cpu as te
     s, _ = te.emitter_scene(48, 32)
-    s.instances[3]["radiance"] = scenes.checkerboard((6.0, 1.0, 1.0), (1.0, 1.0, 6.0), uv_scale=3.0)
+    s.instances[2]["radiance"] = scenes.checkerboard((6.0, 1.0, 1.0), (1.0, 1.0, 6.0), uv_scale=3.0)  # the bitmap light
     p = abi.RenderParams(spp=4, max_depth=0, seed=3, sample_cnt=0, accumulate=1, rng=abi.RNG_PCG32)
     for rng in (abi.RNG_PCG32, abi.RNG_REF_LCG):
         p.rng = rng

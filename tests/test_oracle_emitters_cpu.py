@@ -72,10 +72,9 @@ def test_textured_lights_render(ptlib):
     out = o.render(abi.RenderParams(spp=8, max_depth=0, seed=1, sample_cnt=0, accumulate=1, rng=abi.RNG_PCG32))
     img = out["accum"][:, :3]
     assert np.isfinite(img).all() and img.mean() > 0.01
-    # the same scene with the checkerboard light's patches swapped in brightness
-    # changes the image
+    # a dimmer checkerboard on the quad light darkens the image
     s2, _ = emitter_scene()
-    s2.instances[2]["radiance"] = scenes.checkerboard((0.1, 0.1, 0.1), (0.1, 0.1, 0.1), uv_scale=4.0)
+    s2.instances[1]["radiance"] = scenes.checkerboard((0.1, 0.1, 0.1), (0.1, 0.1, 0.1), uv_scale=4.0)
     img2 = oracle.OracleScene(s2, bvh=False).render(
         abi.RenderParams(spp=8, max_depth=0, seed=1, sample_cnt=0, accumulate=1, rng=abi.RNG_PCG32))["accum"][:, :3]
     assert img2.mean() < img.mean()
