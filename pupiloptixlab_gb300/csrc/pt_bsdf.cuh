@@ -511,18 +511,22 @@ PT_DI void emitter_sample_direct(const DevEmitter &e, const DevTexture *emit_tex
     uint32_t type = emitter_type(e);
     if (type == kEmitTri || type == kEmitSphere) {
         float3 position, normal;
-        float2 tex;
+        // the texture coordinates matter only for a textured radiance (and
+        // cost two inverse trigonometric functions on a sphere)
+        const bool textured = __float_as_uint(e.rad.w) != 0u;
+        float2 tex = make_float2(0.f, 0.f);
         if (type == kEmitTri) {
             float3 t = uniform_sample_triangle(xi.x, xi.y);
             position = xyz(e.p0) * t.x + xyz(e.p1) * t.y + xyz(e.p2) * t.z;
             normal = normalize(xyz(e.n0) * t.x + xyz(e.n1) * t.y + xyz(e.n2) * t.z);
             // vertex texture coordinates (u in p*.w, v in n*.w), area.h:21
-            tex = make_float2(e.p0.w * t.x + e.p1.w * t.y + e.p2.w * t.z, e.n0.w * t.x + e.n1.w * t.y + e.n2.w * t.z);
+            if (textured)
+                tex = make_float2(e.p0.w * t.x + e.p1.w * t.y + e.p2.w * t.z, e.n0.w * t.x + e.n1.w * t.y + e.n2.w * t.z);
         } else {
             float3 t = uniform_sample_sphere(xi.x, xi.y);
             position = t * e.a.w + xyz(e.p0);
             normal = normalize(t);
-            tex = sphere_texcoord(t);  // of the world-space sample direction, sphere.h:19
+            if (textured) tex = sphere_texcoord(t);  // of the world-space sample direction, sphere.h:19
         }
         r.radiance = emitter_radiance(e, emit_tex, tex);
         r.wi = normalize(position - pos);
