@@ -44,7 +44,7 @@ CPP_SOURCES = ["pt_scene.cpp"]
 # C++ host layer above the C-ABI (Pass / System / scene loader): its own
 # library, linked against libpt_gb300.so, plus the pupil_pt command-line tool.
 HOST = PKG / "host"
-HOST_SOURCES = ["xml.cpp", "image.cpp", "inflate.cpp", "hair.cpp", "scene.cpp", "pass.cpp", "host_capi.cpp"]
+HOST_SOURCES = ["xml.cpp", "image.cpp", "inflate.cpp", "jpeg.cpp", "hair.cpp", "scene.cpp", "pass.cpp", "host_capi.cpp"]
 HOST_LIB = BUILD / "libpupil_host.so"
 HOST_CLI = BUILD / "pupil_pt"
 

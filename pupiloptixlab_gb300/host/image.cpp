@@ -2,6 +2,7 @@
 // readers, OpenEXR writer (see image.h).
 #include "image.h"
 #include "inflate.h"
+#include "jpeg.h"
 
 #include <algorithm>
 #include <cstdint>
@@ -356,15 +357,12 @@ bool decode_png(const std::vector<uint8_t> &d, std::vector<uint8_t> &img, uint32
 }
 
 // util::BitmapTexture from an 8-bit image as the reference fills it
-// (framework/util/texture.cpp:106-118): for every `comp` samples, R, G, B =
+// (framework/util/texture.cpp:106-118): for every `c` samples, R, G, B =
 // (sample / 255)^2.2 of the first three bytes from there and A = the fourth
 // byte / 255 for 4-channel images, else 1.  With fewer than 3 channels the
 // reference reads the bytes that follow (the next samples; past the last one
 // its buffer ends, read here as 0).
-bool load_png(const std::vector<uint8_t> &d, std::vector<float> &rgba, uint32_t &w, uint32_t &h, std::string &error) {
-    std::vector<uint8_t> img;
-    int c = 0;
-    if (!decode_png(d, img, w, h, c, error)) return false;
+void rgba_from_8bit(const std::vector<uint8_t> &img, int c, uint32_t w, uint32_t h, std::vector<float> &rgba) {
     const size_t size = img.size();
     auto at = [&](size_t i) -> float { return i < size ? static_cast<float>(img[i]) : 0.f; };
     rgba.assign(4ull * w * h, 0.f);
@@ -375,6 +373,21 @@ bool load_png(const std::vector<uint8_t> &d, std::vector<float> &rgba, uint32_t 
         rgba[j++] = std::pow(at(i + 2) * 1.f / 255.f, 2.2f);
         rgba[j++] = c == 4 ? at(i + 3) * 1.f / 255.f : 1.f;
     }
+}
+
+bool load_png(const std::vector<uint8_t> &d, std::vector<float> &rgba, uint32_t &w, uint32_t &h, std::string &error) {
+    std::vector<uint8_t> img;
+    int c = 0;
+    if (!decode_png(d, img, w, h, c, error)) return false;
+    rgba_from_8bit(img, c, w, h, rgba);
+    return true;
+}
+
+bool load_jpeg(const std::vector<uint8_t> &d, std::vector<float> &rgba, uint32_t &w, uint32_t &h, std::string &error) {
+    std::vector<uint8_t> img;
+    int c = 0;
+    if (!DecodeJpeg(d, img, w, h, c, error)) return false;
+    rgba_from_8bit(img, c, w, h, rgba);
     return true;
 }
 
@@ -642,9 +655,10 @@ bool SaveExrRGBA(const std::string &path, const float *rgba, uint32_t width, uin
 bool LoadImageRGBA(const std::string &path, std::vector<float> &rgba, uint32_t &width, uint32_t &height,
                    std::string &error) {
     const std::string ext = lower_ext(path);
-    if (ext != "hdr" && ext != "pfm" && ext != "exr" && ext != "png") {
-        error = "image '" + path + "': only .hdr (RGBE), .pfm, .png and .exr (uncompressed, RLE, ZIP) images can be "
-                "read; JPEG and the other 8-bit formats are not supported";
+    const bool jpeg = ext == "jpg" || ext == "jpeg";
+    if (ext != "hdr" && ext != "pfm" && ext != "exr" && ext != "png" && !jpeg) {
+        error = "image '" + path + "': only .hdr (RGBE), .pfm, .png, sequential .jpg and .exr (uncompressed, RLE, "
+                "ZIP) images can be read";
         return false;
     }
     std::vector<uint8_t> data;
@@ -652,6 +666,7 @@ bool LoadImageRGBA(const std::string &path, std::vector<float> &rgba, uint32_t &
     const bool ok = ext == "hdr"   ? load_hdr(data, rgba, width, height, error)
                     : ext == "exr" ? load_exr(data, rgba, width, height, error)
                     : ext == "png" ? load_png(data, rgba, width, height, error)
+                    : jpeg         ? load_jpeg(data, rgba, width, height, error)
                                    : load_pfm(data, rgba, width, height, error);
     if (!ok) error = "image '" + path + "': " + error;
     return ok;

@@ -13,9 +13,11 @@
 //   .exr  OpenEXR scanline images, uncompressed or RLE / ZIPS / ZIP
 //         compressed (HALF or FLOAT R, G, B and optional A channels; PIZ,
 //         PXR24, B44 and DWA are reported as unsupported);
+//   .jpg  sequential Huffman-coded JPEG (baseline or extended, grey or YCbCr,
+//         any sampling factors, restart intervals), converted like .png;
+//         progressive and arithmetic-coded files are reported as unsupported;
 // all returned as RGBA floats, alpha 1, first row = top of the image, as
-// util::BitmapTexture holds them.  JPEG and other formats are reported as
-// unsupported.
+// util::BitmapTexture holds them.  Other formats are reported as unsupported.
 #pragma once
 
 #include <cstdint>

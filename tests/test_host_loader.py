@@ -126,7 +126,7 @@ def test_obj_mesh(host):
     ("<scene><shape type='rectangle'><bsdf type='diffuse'><texture type='bitmap' name='reflectance'/>"
      "</bsdf></shape></scene>", "without a filename"),
     ("<scene><shape type='rectangle'><bsdf type='diffuse'><texture type='bitmap' name='reflectance'>"
-     "<string name='filename' value='a.jpg'/></texture></bsdf></shape></scene>", "JPEG and the other 8-bit formats"),
+     "<string name='filename' value='a.gif'/></texture></bsdf></shape></scene>", "images can be read"),
     ("<scene><sensor type='thinlens'/></scene>", "perspective"),
     ("<scene><shape type='cube'><transform name='to_world'><translate x='abc'/></transform></shape></scene>",
      "malformed number"),
@@ -764,3 +764,225 @@ def test_compression_the_reader_does_not_take_is_reported(host, tmp_path):
     with pytest.raises(abi.PtError) as e:
         _load_env(host, path)
     assert "PIZ" in str(e.value)
+
+
+# ---- JPEG: an independent baseline encoder (ITU-T T.81) and the expected decode
+
+def _jpeg_bytes(rgb, subsample, quality_q, restart=0, grey=False):
+    """A baseline JPEG of an (h, w, 3) uint8 image (or (h, w) grey): JFIF
+    YCbCr, 4:2:0 (subsample) or 4:4:4, one quantisation table value, forward
+    DCT from its definition, every Huffman code 8 bits long (a valid table for
+    up to 255 symbols), byte stuffing, optional restart markers.  Returns the
+    file and the quantised coefficients per component."""
+    import struct
+    h, w = rgb.shape[:2]
+    x = rgb.astype(np.float64)
+    if grey:
+        planes = [x]
+        samp = [(1, 1)]
+    else:
+        r, g, b = x[..., 0], x[..., 1], x[..., 2]
+        Y = 0.299 * r + 0.587 * g + 0.114 * b
+        Cb = -0.168736 * r - 0.331264 * g + 0.5 * b + 128
+        Cr = 0.5 * r - 0.418688 * g - 0.081312 * b + 128
+        planes = [Y, Cb, Cr]
+        samp = [(2, 2), (1, 1), (1, 1)] if subsample else [(1, 1), (1, 1), (1, 1)]
+    hmax = max(s[0] for s in samp)
+    vmax = max(s[1] for s in samp)
+    if grey:
+        hmax = vmax = 1
+    mw, mh = 8 * hmax, 8 * vmax
+    W, H = -(-w // mw) * mw, -(-h // mh) * mh
+    cu = np.array([np.sqrt(0.5)] + [1.0] * 7)
+    cosm = np.array([[cu[u] * np.cos((2 * xx + 1) * u * np.pi / 16) for u in range(8)] for xx in range(8)])
+    zz = [0, 1, 8, 16, 9, 2, 3, 10, 17, 24, 32, 25, 18, 11, 4, 5, 12, 19, 26, 33, 40, 48, 41, 34, 27, 20, 13, 6, 7, 14,
+          21, 28, 35, 42, 49, 56, 57, 50, 43, 36, 29, 22, 15, 23, 30, 37, 44, 51, 58, 59, 52, 45, 38, 31, 39, 46, 53, 60,
+          61, 54, 47, 55, 62, 63]
+    comps = []
+    for pl, (sh, sv) in zip(planes, samp):
+        padded = np.pad(pl, ((0, H - h), (0, W - w)), mode="edge")
+        fx, fy = hmax // sh, vmax // sv
+        sub = padded.reshape(H // fy, fy, W // fx, fx).mean(axis=(1, 3)) if (fx > 1 or fy > 1) else padded
+        bh, bw = sub.shape[0] // 8, sub.shape[1] // 8
+        q = np.zeros((bh, bw, 64), np.int64)
+        for by in range(bh):
+            for bx in range(bw):
+                blk = sub[by * 8:by * 8 + 8, bx * 8:bx * 8 + 8] - 128.0
+                S = 0.25 * cosm.T @ blk @ cosm  # S[v, u]
+                nat = S.reshape(-1)
+                q[by, bx] = np.round(np.array([nat[zz[k]] for k in range(64)]) / quality_q).astype(np.int64)
+        comps.append(q)
+    # entropy coding
+    def cat(v):
+        return 0 if v == 0 else int(abs(v)).bit_length()
+
+    def bits_of(v, s):
+        return v if v >= 0 else v + (1 << s) - 1
+
+    mcux, mcuy = W // mw, H // mh
+    units = []  # (comp index, block) in coding order
+    for my in range(mcuy):
+        for mx in range(mcux):
+            for ci, (sh, sv) in enumerate(samp):
+                ch, cv = (1, 1) if grey else (sh, sv)
+                for by in range(cv):
+                    for bx in range(ch):
+                        units.append((my * mcux + mx, ci, comps[ci][my * cv + by, mx * ch + bx]))
+    dc_syms = [set(), set()]
+    ac_syms = [set(), set()]
+    pred = [0] * len(comps)
+    seq = []
+    last_mcu = -1
+    for mcu, ci, blk in units:
+        if restart and mcu != last_mcu and mcu > 0 and mcu % restart == 0:
+            pred = [0] * len(comps)
+            seq.append(("RST", mcu // restart - 1))
+        last_mcu = mcu
+        t = 0 if ci == 0 else 1
+        diff = int(blk[0]) - pred[ci]
+        pred[ci] = int(blk[0])
+        s = cat(diff)
+        dc_syms[t].add(s)
+        seq.append(("DC", t, s, bits_of(diff, s)))
+        run = 0
+        last_nz = max([k for k in range(1, 64) if blk[k] != 0], default=0)
+        for k in range(1, last_nz + 1):
+            v = int(blk[k])
+            if v == 0:
+                run += 1
+                continue
+            while run > 15:
+                ac_syms[t].add(0xF0)
+                seq.append(("AC", t, 0xF0, 0, 0))
+                run -= 16
+            s = cat(v)
+            ac_syms[t].add((run << 4) | s)
+            seq.append(("AC", t, (run << 4) | s, s, bits_of(v, s)))
+            run = 0
+        if last_nz < 63:
+            ac_syms[t].add(0x00)
+            seq.append(("AC", t, 0x00, 0, 0))
+    tables = {}
+    for cls, syms in ((0, dc_syms), (1, ac_syms)):
+        for t in (0, 1):
+            ss = sorted(syms[t]) or [0]
+            tables[(cls, t)] = {s: i for i, s in enumerate(ss)}
+    out, acc, nacc = bytearray(), 0, 0
+
+    def put(v, n):
+        nonlocal acc, nacc
+        for i in range(n - 1, -1, -1):
+            acc = (acc << 1) | ((v >> i) & 1)
+            nacc += 1
+            if nacc == 8:
+                out.append(acc)
+                if acc == 0xFF:
+                    out.append(0)
+                acc, nacc = 0, 0
+
+    def flush():
+        nonlocal acc, nacc
+        if nacc:
+            put((1 << (8 - nacc)) - 1, 8 - nacc)
+
+    for e in seq:
+        if e[0] == "RST":
+            flush()
+            out += bytes([0xFF, 0xD0 + (e[1] % 8)])
+        elif e[0] == "DC":
+            put(tables[(0, e[1])][e[2]], 8)
+            put(e[3], e[2])
+        else:
+            put(tables[(1, e[1])][e[2]], 8)
+            put(e[4], e[3])
+    flush()
+    ncomp = len(comps)
+    f = bytearray(b"\xFF\xD8")
+    f += b"\xFF\xE0" + struct.pack(">H", 16) + b"JFIF\x00\x01\x01\x00\x00\x01\x00\x01\x00\x00"
+    f += b"\xFF\xDB" + struct.pack(">H", 67) + bytes([0]) + bytes([quality_q] * 64)
+    f += b"\xFF\xC0" + struct.pack(">HBHHB", 8 + 3 * ncomp, 8, h, w, ncomp)
+    for ci, (sh, sv) in enumerate(samp):
+        f += bytes([ci + 1, (sh << 4) | sv, 0])
+    for (cls, t), mp in tables.items():
+        syms = sorted(mp, key=lambda s: mp[s])
+        counts = [0] * 16
+        counts[7] = len(syms)
+        f += b"\xFF\xC4" + struct.pack(">H", 2 + 17 + len(syms)) + bytes([(cls << 4) | t] + counts + syms)
+    if restart:
+        f += b"\xFF\xDD" + struct.pack(">HH", 4, restart)
+    f += b"\xFF\xDA" + struct.pack(">HB", 6 + 2 * ncomp, ncomp)
+    for ci in range(ncomp):
+        t = 0 if ci == 0 else 1
+        f += bytes([ci + 1, (t << 4) | t])
+    f += bytes([0, 63, 0]) + out + b"\xFF\xD9"
+    return bytes(f), comps, samp, (mcux, mcuy, hmax, vmax)
+
+
+def _jpeg_expected(comps, samp, layout, h, w, q, grey):
+    """The decoder's arithmetic restated: dequantise, IDCT from the definition,
+    round half away from zero, clamp; replicate chroma; JFIF YCbCr -> RGB."""
+    mcux, mcuy, hmax, vmax = layout
+    cu = np.array([np.sqrt(0.5)] + [1.0] * 7)
+    cosm = np.array([[cu[u] * np.cos((2 * xx + 1) * u * np.pi / 16) for u in range(8)] for xx in range(8)])
+    zz = [0, 1, 8, 16, 9, 2, 3, 10, 17, 24, 32, 25, 18, 11, 4, 5, 12, 19, 26, 33, 40, 48, 41, 34, 27, 20, 13, 6, 7, 14,
+          21, 28, 35, 42, 49, 56, 57, 50, 43, 36, 29, 22, 15, 23, 30, 37, 44, 51, 58, 59, 52, 45, 38, 31, 39, 46, 53, 60,
+          61, 54, 47, 55, 62, 63]
+    rnd = lambda v: np.sign(v) * np.floor(np.abs(v) + 0.5)  # noqa: E731
+    planes = []
+    for blocks in comps:
+        bh, bw = blocks.shape[:2]
+        pl = np.zeros((bh * 8, bw * 8))
+        for by in range(bh):
+            for bx in range(bw):
+                nat = np.zeros(64)
+                for k in range(64):
+                    nat[zz[k]] = blocks[by, bx, k] * q
+                S = nat.reshape(8, 8)
+                pl[by * 8:by * 8 + 8, bx * 8:bx * 8 + 8] = np.clip(rnd(cosm @ S @ cosm.T / 4.0 + 128.0), 0, 255)
+        planes.append(pl)
+    if grey:
+        return planes[0][:h, :w].astype(np.uint8)[..., None]
+    ys, xs = np.arange(h), np.arange(w)
+    up = [p[(ys * s[1] // vmax)[:, None], (xs * s[0] // hmax)[None, :]] for p, s in zip(planes, samp)]
+    Y, cb, cr = up[0], up[1] - 128.0, up[2] - 128.0
+    rgb = np.stack([Y + 1.402 * cr, Y - 0.344136 * cb - 0.714136 * cr, Y + 1.772 * cb], -1)
+    return np.clip(rnd(rgb), 0, 255).astype(np.uint8)
+
+
+@pytest.mark.parametrize("subsample,restart,grey,size", [(True, 0, False, (37, 29)), (False, 3, False, (16, 24)),
+                                                          (True, 2, False, (40, 41)), (False, 0, True, (21, 18))])
+def test_jpeg_reader(host, tmp_path, subsample, restart, grey, size):
+    rng = np.random.default_rng(size[0] * 7 + size[1])
+    h, w = size
+    yy, xx = np.mgrid[0:h, 0:w]
+    img = np.stack([128 + 90 * np.sin(xx / 5.0), 128 + 80 * np.cos(yy / 4.0), (xx * 3 + yy * 2) % 256], -1)
+    img = np.clip(img + rng.normal(0, 12, img.shape), 0, 255).astype(np.uint8)
+    src = img[..., 1] if grey else img
+    q = 3
+    data, comps, samp, layout = _jpeg_bytes(src, subsample, q, restart, grey)
+    path = tmp_path / "t.jpg"
+    path.write_bytes(data)
+    got = _load_env(host, path)
+    img8 = _jpeg_expected(comps, samp, layout, h, w, q, grey)
+    c = img8.shape[-1]
+    expect = _expect_rgba(img8, c).reshape(h, w, 4)
+    # every sample within one level of the restated arithmetic (rounding of
+    # exact halves may differ with the summation order), almost all exact
+    lvl = np.round(np.power(got[..., :3], 1 / 2.2) * 255).astype(int)
+    ref = np.round(np.power(expect[..., :3], 1 / 2.2) * 255).astype(int)
+    assert np.abs(lvl - ref).max() <= 1 and (lvl == ref).mean() > 0.999
+    # and close to the source image (a sanity check of the whole round trip)
+    srcf = (src[..., None] if grey else src).astype(float)
+    dec = np.round(np.power(got[..., :3], 1 / 2.2) * 255)[..., :c] if not grey else lvl[..., :1]
+    assert np.abs(dec - srcf).mean() < (10.0 if subsample else 4.0)  # 4:2:0 averages noisy chroma
+
+
+def test_progressive_jpeg_is_reported(host, tmp_path):
+    data = bytearray(_jpeg_bytes(np.zeros((8, 8, 3), np.uint8), False, 2)[0])
+    i = data.index(b"\xFF\xC0")
+    data[i + 1] = 0xC2
+    path = tmp_path / "p.jpg"
+    path.write_bytes(bytes(data))
+    with pytest.raises(abi.PtError) as e:
+        _load_env(host, path)
+    assert "progressive" in str(e.value)
