@@ -250,9 +250,13 @@ __device__ __forceinline__ void fwd_epilogue(const FwdArgs &a, uint32_t tmem, in
 // every output channel and all (chunk, tap) weight boxes fit in
 // kMaxResidentWeights bytes, they are loaded once per CTA ahead of the ring
 // (on their own barrier) and the stages carry only the two A planes.
-constexpr int kHaloW = 130, kHaloRows = 3;
-constexpr int kHaloBoxBytes = kHaloW * kHaloRows * 16;       // one 8-channel plane as TMA writes it
-constexpr int kHaloPlaneBytes = (kHaloBoxBytes + 1023) / 1024 * 1024;  // plane stride: TMA destinations 1 KiB-aligned
+// A tile may cover two output rows (halo_rows = 2: a 4-row box, two M = 128
+// accumulators sharing each B operand), so that every input row crosses L2
+// twice per pass instead of three times; the second row's A operand is the
+// same planes read one box row (130 pixels) further on.
+constexpr int kHaloW = 130;
+__host__ __device__ constexpr int halo_box_bytes(int rows) { return kHaloW * (rows + 2) * 16; }
+__host__ __device__ constexpr int halo_plane_bytes(int rows) { return (halo_box_bytes(rows) + 1023) / 1024 * 1024; }
 __host__ __device__ constexpr int halo_b_tap_bytes(int n_tile) { return (n_tile * 32 + 1023) / 1024 * 1024; }
 constexpr int kMaxResidentWeights = 64 * 1024;
 
@@ -289,7 +293,8 @@ __global__ void __launch_bounds__(192, 1)
     const int nk = HALO ? a.nchunks : 9 * a.nchunks;  // stages per tile
     const int a_bytes = HALO ? a.halo_a_bytes : 128 * R;
     const int b_tap = HALO ? halo_b_tap_bytes(a.n_tile) : 0;
-    const uint32_t tx_bytes = HALO ? static_cast<uint32_t>(2 * kHaloBoxBytes + (wres ? 0 : 9 * a.n_tile * R))
+    const int hrows = HALO ? a.halo_rows : 1;  // output rows (accumulators) per tile
+    const uint32_t tx_bytes = HALO ? static_cast<uint32_t>(2 * a.halo_box_bytes + (wres ? 0 : 9 * a.n_tile * R))
                                    : static_cast<uint32_t>(a.tile_w * a.tile_rows * R + a.n_tile * R);
     const uint32_t bar0 = smem_u32(bars);
     auto full = [&](int s) { return bar0 + 8u * s; };
@@ -355,7 +360,7 @@ __global__ void __launch_bounds__(192, 1)
                     mbar_expect_tx(full(s), tx_bytes);
                     if (HALO) {
                         tma_load_4d(sa, &act, full(s), k * 16, x0 - 1, y0 - 1, img);
-                        tma_load_4d(sa + kHaloPlaneBytes, &act, full(s), k * 16 + 8, x0 - 1, y0 - 1, img);
+                        tma_load_4d(sa + a.halo_plane_bytes, &act, full(s), k * 16 + 8, x0 - 1, y0 - 1, img);
                         if (!wres)
                             for (int tap = 0; tap < 9; tap++)
                                 tma_load_2d(sb + tap * b_tap, &wgt, full(s), tap * a.cin + k * 16, n0);
@@ -394,7 +399,7 @@ __global__ void __launch_bounds__(192, 1)
                     break;
                 }
                 tc_fence_after();
-                const uint32_t d = tmem + static_cast<uint32_t>(buf * a.n_tile);
+                const uint32_t d = tmem + static_cast<uint32_t>(buf * hrows * a.n_tile);
                 for (int k = 0; k < nk; k++, kg++) {
                     const int s = kg % S;
                     if (!mbar_wait(full(s), (kg / S) & 1, false, lim, fail)) {
@@ -409,9 +414,13 @@ __global__ void __launch_bounds__(192, 1)
 #pragma unroll
                         for (int tap = 0; tap < 9; tap++) {
                             const int dy = tap / 3, dx = tap - 3 * (tap / 3);
-                            const uint64_t da = sdesc(sa + 16u * (dy * kHaloW + dx), kHaloPlaneBytes, 128u, 0u);
                             const uint64_t db = sdesc(sb + tap * b_tap, 16u, 8u * R, SWZ);
-                            umma_bf16(d, da, db, idesc, (k | tap) != 0 ? 1u : 0u);
+                            for (int r = 0; r < hrows; r++) {
+                                const uint64_t da = sdesc(sa + 16u * ((dy + r) * kHaloW + dx),
+                                                          static_cast<uint32_t>(a.halo_plane_bytes), 128u, 0u);
+                                umma_bf16(d + static_cast<uint32_t>(r * a.n_tile), da, db, idesc,
+                                          (k | tap) != 0 ? 1u : 0u);
+                            }
                         }
                     } else {
 #pragma unroll
@@ -445,7 +454,9 @@ __global__ void __launch_bounds__(192, 1)
             tc_fence_after();
             int img, x0, y0, n0;
             tile_of(t, img, x0, y0, n0);
-            fwd_epilogue(a, tmem + static_cast<uint32_t>(buf * a.n_tile), row, quad, img, x0, y0, n0, true);
+            for (int r = 0; r < hrows; r++)
+                fwd_epilogue(a, tmem + static_cast<uint32_t>((buf * hrows + r) * a.n_tile), row, quad, img, x0, y0 + r,
+                             n0, true);
             tc_fence_before();
             mbar_arrive(acc_empty(buf));
         }
@@ -806,9 +817,15 @@ int fwd_prepare(FwdOp *op, const Act &in, const void *w, int w_rows, int cout, c
     int ntiles = (cout_pad + 255) / 256;
     int n_tile = ((cout_pad / ntiles) + 15) / 16 * 16;
     ntiles = (cout_pad + n_tile - 1) / n_tile;
+    // two output rows per halo tile while both rows' double-buffered
+    // accumulators still leave room for two CTAs per SM (PT_CONV_HALO_ROWS=1..4
+    // overrides, within the 512 tensor-memory columns)
+    int halo_rows = pow2_cols(4 * n_tile) <= 256 ? 2 : 1;
+    if (const char *e = getenv("PT_CONV_HALO_ROWS")) halo_rows = std::min(std::max(atoi(e), 1), 4);
+    while (halo_rows > 1 && pow2_cols(2 * halo_rows * n_tile) > 512) halo_rows--;
     int st;
     if (halo) {
-        if ((st = act_map_box(&op->act, in, 8, kHaloW, kHaloRows, CU_TENSOR_MAP_SWIZZLE_NONE, 8)) != PT_OK) return st;
+        if ((st = act_map_box(&op->act, in, 8, kHaloW, halo_rows + 2, CU_TENSOR_MAP_SWIZZLE_NONE, 8)) != PT_OK) return st;
     } else if ((st = act_map(&op->act, in, kc, t)) != PT_OK) {
         return st;
     }
@@ -827,8 +844,11 @@ int fwd_prepare(FwdOp *op, const Act &in, const void *w, int w_rows, int cout, c
     a.n_tile = n_tile;
     a.cout = cout;
     a.n_tiles_n = ntiles;
-    a.tmem_cols = pow2_cols(2 * n_tile);  // two accumulators
-    a.halo_a_bytes = 2 * kHaloPlaneBytes;
+    a.tmem_cols = pow2_cols(2 * (halo ? halo_rows : 1) * n_tile);  // double-buffered accumulators
+    a.halo_rows = halo_rows;
+    a.halo_box_bytes = halo_box_bytes(halo_rows);
+    a.halo_plane_bytes = halo_plane_bytes(halo_rows);
+    a.halo_a_bytes = 2 * a.halo_plane_bytes;
     const int wres_bytes = a.nchunks * 9 * halo_b_tap_bytes(n_tile);
     a.wres_bytes = (halo && ntiles == 1 && wres_bytes <= kMaxResidentWeights && !getenv_flag("PT_CONV_NO_RESIDENT"))
                        ? wres_bytes : 0;
@@ -839,9 +859,9 @@ int fwd_prepare(FwdOp *op, const Act &in, const void *w, int w_rows, int cout, c
     a.stages = std::max(2, std::min(kMaxStages, budget / a.stage_bytes));
     if (halo) {
         a.tile_w = 128;
-        a.tile_rows = 1;
+        a.tile_rows = halo_rows;
         a.tiles_x = (in.w + 127) / 128;
-        a.tiles_y = in.h;
+        a.tiles_y = (in.h + halo_rows - 1) / halo_rows;
     }
     a.epi = epi;
     a.relu = relu;
@@ -859,6 +879,7 @@ int fwd_prepare(FwdOp *op, const Act &in, const void *w, int w_rows, int cout, c
     a.stall = take_stall_request() ? 1 : 0;
     op->kc = kc;
     op->halo = halo;
+    while (a.stages > 2 && smem_request(a.stages, a.stage_bytes, a.tmem_cols) + a.wres_bytes > 220 * 1024) a.stages--;
     op->smem = smem_request(a.stages, a.stage_bytes, a.tmem_cols) + a.wres_bytes;
     const long long total = (long long)in.n * a.tiles_x * a.tiles_y * ntiles;
     const int per_sm = std::max(1, std::min((228 * 1024) / (op->smem + 1024), 512 / a.tmem_cols));

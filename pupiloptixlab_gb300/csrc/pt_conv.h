@@ -51,6 +51,9 @@ struct FwdArgs {
     unsigned *err;
     unsigned long long wait_ns;  // limit of every bounded wait (kWaitNs unless pt_conv_set_wait_limit changed it)
     int stall;                   // test of the timeout path: the MMA warp first waits on a barrier nothing arrives at
+    int halo_rows;               // halo kernel: output rows per tile (1 or 2); the box holds halo_rows + 2 rows
+    int halo_box_bytes;          // halo kernel: bytes of one 8-channel plane as TMA writes it
+    int halo_plane_bytes;        // halo kernel: plane stride (1 KiB-aligned TMA destinations)
 };
 
 struct WgradArgs {

@@ -37,7 +37,27 @@ SHAPES = [
     (1, 8, 64, 384, 128),     # K = 9 * 384
     (1, 16, 32, 80, 384),     # N tiled (2 x 192)
     (3, 4, 4, 48, 16),        # tiny images
+    (2, 7, 130, 16, 32),      # two-row halo tiles, odd height (the last tile's second row is outside)
 ]
+
+
+@pytest.mark.parametrize("shape", [(2, 7, 130, 16, 32), (1, 9, 256, 32, 64), (2, 6, 128, 48, 48)])
+def test_conv_forward_halo_rows_agree(cuda_ctx, shape, monkeypatch):
+    """Halo tiles of one to four output rows issue the same MMAs per output
+    row in the same order: the FP32 results are identical."""
+    from pupiloptixlab_gb300 import denoiser as dnm
+    n, h, w, cin, cout = shape
+    g = torch.Generator().manual_seed(5 + h)
+    x = _bf16((n, h, w, cin), g).cuda()
+    wt = _bf16((cout, 9, cin), g, 0.1).cuda()
+    b = torch.randn(cout, generator=g).cuda()
+    ys = []
+    for rows in ("1", "2", "3", "4"):
+        monkeypatch.setenv("PT_CONV_HALO_ROWS", rows)
+        ys.append(dnm.conv3x3_forward(x, wt, b, cout, relu=False, out_f32=True).cpu())
+    for y in ys[1:]:
+        assert torch.equal(ys[0], y)
+    assert _rel_l2(ys[0], _ref_conv(x.cpu(), wt.cpu(), b.cpu())) <= 1e-4
 
 
 @pytest.mark.parametrize("shape", SHAPES)
