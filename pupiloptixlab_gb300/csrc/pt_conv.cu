@@ -499,10 +499,20 @@ __global__ void __launch_bounds__(128, 1)
     auto empty = [&](int s) { return bar0 + 8u * (kMaxStages + s); };
     const uint32_t done = bar0 + 8u * (2 * kMaxStages);
 
-    if (a.zero_fill) {  // rows that no box covers must read as zero pixels
-        uint4 z = make_uint4(0, 0, 0, 0);
+    // The last M tile's spare A chunk holds BF16 ones in every stage (no box
+    // writes it), so its D rows are the sums of gy over the pixels: the bias
+    // gradient from the same MMAs.
+    const bool ones = a.db != nullptr && a.ones_row >= 0 && blockIdx.x == gridDim.x - 1;
+    if (a.zero_fill || ones) {  // zero fill: rows that no box covers must read as zero pixels
+        const int ob = ones ? (a.ones_row / KCA) * 128 * RA : a.stage_bytes;  // ones chunk offset in a stage
         uint8_t *p = smem_raw + (base - smem_u32(smem_raw));
-        for (int i = tid; i < S * a.stage_bytes / 16; i += blockDim.x) reinterpret_cast<uint4 *>(p)[i] = z;
+        for (int i = tid; i < S * a.stage_bytes / 16; i += blockDim.x) {
+            const int off = (i * 16) % a.stage_bytes;
+            if (off >= ob && off < ob + 128 * RA)
+                reinterpret_cast<uint4 *>(p)[i] = make_uint4(0x3f803f80u, 0x3f803f80u, 0x3f803f80u, 0x3f803f80u);
+            else if (a.zero_fill)
+                reinterpret_cast<uint4 *>(p)[i] = make_uint4(0, 0, 0, 0);
+        }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
     if (warp == 0) tmem_alloc(smem_u32(&tmem_slot), a.tmem_cols);
@@ -577,15 +587,18 @@ __global__ void __launch_bounds__(128, 1)
     // epilogue: row tid = A row (tap, ci) index g; dw[co][g] += D[tid][co - n0]
     const int g = blk0 * KCA + tid;
     const bool valid = ok && tid < nblk * KCA;
+    const bool bias_row = ok && ones && tid == a.ones_row;  // db[co] += D[ones_row][co - n0]
     const uint32_t trow = tmem + (static_cast<uint32_t>(warp * 32) << 16);
     const size_t kdim = 9 * static_cast<size_t>(a.cin);
     for (int c = 0; c < a.n_tile; c += 16) {
         float v[16];
         tmem_ld16(trow + c, v);
-        if (!valid) continue;
+        if (!valid && !bias_row) continue;
+        float *dst = valid ? a.dw + g : a.db;
+        const size_t stride = valid ? kdim : 1;
         for (int i = 0; i < 16; i++) {
             const int co = n0 + c + i;
-            if (co < a.cout) atomicAdd(a.dw + co * kdim + g, v[i]);
+            if (co < a.cout) atomicAdd(dst + co * stride, v[i]);
         }
     }
 
@@ -907,7 +920,7 @@ int fwd_launch(const FwdOp &op, cudaStream_t stream) {
     return fwd_persistent_go<16, false>(op, stream);
 }
 
-int wgrad_prepare(WgradOp *op, const Act &x, const Act &gy, float *dw, int num_sms, unsigned *err) {
+int wgrad_prepare(WgradOp *op, const Act &x, const Act &gy, float *dw, float *db, int num_sms, unsigned *err) {
     if (x.n != gy.n || x.h != gy.h || x.w != gy.w || x.c % 16 || gy.c % 16 || x.c <= 0 || gy.c <= 0) {
         pt_set_error("conv weight gradient: shapes differ or channels not multiples of 16");
         return PT_ERR_INVALID;
@@ -946,6 +959,10 @@ int wgrad_prepare(WgradOp *op, const Act &x, const Act &gy, float *dw, int num_s
     a.zero_fill = t.tile_w * t.tile_rows < 128 ? 1 : 0;
     const int m_tiles = (9 * a.nchunks_a * kca + 127) / 128;
     const int base_ctas = m_tiles * ntiles;
+    const int last_blocks = 9 * a.nchunks_a - (m_tiles - 1) * (128 / kca);  // chunks in the last M tile
+    a.ones_row = last_blocks < 128 / kca ? last_blocks * kca : -1;
+    a.db = a.ones_row >= 0 && !getenv_flag("PT_CONV_NO_FUSED_BIAS") ? db : nullptr;
+    op->bias_fused = a.db != nullptr;
     op->smem = smem_request(a.stages, a.stage_bytes, a.tmem_cols);
     // split the pixel tiles so that the grid is one full wave of resident CTAs
     const int per_sm = std::max(1, std::min((228 * 1024) / (op->smem + 1024), 512 / a.tmem_cols));

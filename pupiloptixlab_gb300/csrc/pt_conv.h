@@ -51,7 +51,7 @@ struct FwdArgs {
     unsigned *err;
     unsigned long long wait_ns;  // limit of every bounded wait (kWaitNs unless pt_conv_set_wait_limit changed it)
     int stall;                   // test of the timeout path: the MMA warp first waits on a barrier nothing arrives at
-    int halo_rows;               // halo kernel: output rows per tile (1 or 2); the box holds halo_rows + 2 rows
+    int halo_rows;               // halo kernel: output rows per tile (1-4); the box holds halo_rows + 2 rows
     int halo_box_bytes;          // halo kernel: bytes of one 8-channel plane as TMA writes it
     int halo_plane_bytes;        // halo kernel: plane stride (1 KiB-aligned TMA destinations)
 };
@@ -65,6 +65,8 @@ struct WgradArgs {
     int total_tiles, tiles_per_split;
     int zero_fill;        // pixel tiles smaller than 128: clear the stages once
     float *dw;            // [cout][9][cin] FP32, accumulated
+    float *db;            // [cout] FP32, accumulated through the ones row (null: not fused)
+    int ones_row;         // row of the last M tile whose A block holds ones (its D row = sum of gy)
     unsigned *err;
     unsigned long long wait_ns;
 };
@@ -82,18 +84,12 @@ struct WgradOp {
     WgradArgs args;
     dim3 grid;
     int smem = 0, kca = 0, kcb = 0;
+    bool bias_fused = false;  // the kernel also accumulates db (else bias_grad_launch does)
 };
 
 // Largest chunk in {64, 32, 16} channels dividing c (c a multiple of 16).
 int pick_kc(int c);
 
-// Forward (or data-gradient) launch over `in`.  Images at least 128 pixels
-// wide use the halo kernel (one input load per 16-channel chunk for all nine
-// taps); the environment variable PT_CONV_NO_HALO=1 selects the per-tap kernel
-// for every width, for comparison runs.  `w` holds rows [w_rows][9][in.c]
-// in bf16 (rows beyond w_rows read as zero); `cout` output channels are
-// written to channels [out_coff, out_coff + cout) of `out` (out_ctot channels,
-// same n/h/w as `in`).  `mask` (EPI_BF16_MASK) is a tensor of the output's shape.
 // Limit of every bounded wait of the convolution kernels prepared from now on
 // (0 = the default of 2 s), and a one-shot request that the next prepared
 // forward convolution first waits on a barrier nothing arrives at, so that the
@@ -102,12 +98,24 @@ void set_wait_limit(unsigned long long ns, bool stall_next);
 unsigned long long wait_limit_ns();
 bool take_stall_request();
 
+// Forward (or data-gradient) launch over `in`.  Images at least 128 pixels
+// wide use the halo kernel (one input load per 16-channel chunk for all nine
+// taps, two output rows per tile); the environment variable PT_CONV_NO_HALO=1
+// selects the per-tap kernel for every width, for comparison runs.  `w` holds
+// rows [w_rows][9][in.c] in bf16 (rows beyond w_rows read as zero); `cout`
+// output channels are written to channels [out_coff, out_coff + cout) of `out`
+// (out_ctot channels, same n/h/w as `in`).  `mask` (EPI_BF16_MASK) is a tensor
+// of the output's shape.
 int fwd_prepare(FwdOp *op, const Act &in, const void *w, int w_rows, int cout, const float *bias, int epi,
                 int relu, void *out, int out_ctot, int out_coff, const Act *mask, unsigned *err);
 int fwd_launch(const FwdOp &op, cudaStream_t stream);
 
 // dw[co][tap][ci] += sum over pixels of x[p + off(tap), ci] * gy[p, co].
-int wgrad_prepare(WgradOp *op, const Act &x, const Act &gy, float *dw, int num_sms, unsigned *err);
+// When db is given and the last 128-row block of (tap, channel) rows has a
+// spare chunk, that chunk of A is filled with ones and the same MMAs also give
+// db[co] += sum over pixels of gy[p, co] (op->bias_fused); otherwise the
+// caller runs bias_grad_launch.
+int wgrad_prepare(WgradOp *op, const Act &x, const Act &gy, float *dw, float *db, int num_sms, unsigned *err);
 int wgrad_launch(const WgradOp &op, cudaStream_t stream);
 
 // db[c] += sum over pixels of g[p, c].

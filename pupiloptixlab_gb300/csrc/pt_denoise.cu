@@ -536,7 +536,7 @@ int plan_prepare(pt_denoiser *dn, Plan &P, int n, int h, int w, bool train) {
             const LayerSpec &L = kSpec[l];
             P.g_of[l] = g[l];
             if ((st = ptconv::wgrad_prepare(&P.wg[l], P.x_of[l], g[l], dn->grads.as<float>() + dn->w_off[l],
-                                            dn->num_sms, err)) != PT_OK)
+                                            dn->grads.as<float>() + dn->b_off[l], dn->num_sms, err)) != PT_OK)
                 return st;
             if (!back[l].dst) continue;
             const int lvl = io[l].lvl;
@@ -609,7 +609,7 @@ int run_backward(pt_denoiser *dn, Plan &P, const float *target, cudaStream_t s) 
                                           P.g_out.as<uint16_t>(), dn->loss.as<float>());
     auto layer = [&](int l) -> int {
         PT_TRY(ptconv::wgrad_launch(P.wg[l], s));
-        PT_TRY(ptconv::bias_grad_launch(P.g_of[l], dn->grads.as<float>() + dn->b_off[l], s));
+        if (!P.wg[l].bias_fused) PT_TRY(ptconv::bias_grad_launch(P.g_of[l], dn->grads.as<float>() + dn->b_off[l], s));
         if (l != E0A) PT_TRY(ptconv::fwd_launch(P.bwd[l], s));
         return PT_OK;
     };
@@ -1222,9 +1222,9 @@ int pt_conv3x3_backward_weights(const void *x, uint32_t n, uint32_t h, uint32_t 
     ga.ctot = cout;
     ga.c = cout;
     ptconv::WgradOp op;
-    if (st == PT_OK) st = ptconv::wgrad_prepare(&op, xa, ga, dweight, sms, e.as<unsigned>());
+    if (st == PT_OK) st = ptconv::wgrad_prepare(&op, xa, ga, dweight, dbias, sms, e.as<unsigned>());
     if (st == PT_OK) st = ptconv::wgrad_launch(op, s);
-    if (st == PT_OK && dbias) st = ptconv::bias_grad_launch(ga, dbias, s);
+    if (st == PT_OK && dbias && !op.bias_fused) st = ptconv::bias_grad_launch(ga, dbias, s);
     if (st == PT_OK) st = conv_check(e, s);
     e.release();
     return st;
