@@ -802,7 +802,7 @@ def main():
     if rank != 0:
         return
     # algorithmic bytes of the closest-hit kernel (per-ray counters of the identical counting render)
-    node_bytes = 32 * args.bvh_width
+    node_bytes = 96 if args.bvh_width == 8 else 32 * args.bvh_width  # 8-wide nodes are read compressed
     ext_bytes = cst.nodes_visited * node_bytes + cst.prims_tested * 48 + cst.extension_rays * (32 + 16)
     # per launch: one step's algorithmic bytes over that step's closest-hit launches
     launches_per_step = max(1, ext_launches // args.steps)

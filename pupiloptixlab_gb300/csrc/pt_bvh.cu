@@ -23,6 +23,7 @@
 
 #include "pt_nvtx.h"
 #include "pt_internal.h"
+#include "pt_traverse.cuh"
 
 #include <algorithm>
 #include <cfloat>
@@ -798,6 +799,111 @@ __global__ void k_root_area(const float *nodes, double *out) {
 
 inline uint32_t blocks(size_t n, int b) { return (uint32_t)((n + b - 1) / b); }
 
+// Compressed copies of 8-wide float nodes (layout in pt_traverse.cuh, same
+// node indices).  The grid origin is the low corner of the union of the
+// children's boxes; each axis's cell size is the smallest power of two for
+// which 255 cells span the union; each child's cells are rounded outwards and
+// then checked with the same fused multiply-add the traversal evaluates, so
+// the decoded box always encloses the child's padded float box.  Children go
+// to slots by a greedy matching on dot(child centroid - node centroid,
+// direction of the slot's octant), smallest first (Ylitie, Karras and Laine,
+// HPG 2017): slot s holds the child met first by rays of octant s.
+__global__ void k_compress8(const float *nodes, uint32_t n, float4 *out) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float *f = nodes + (size_t)i * 64;
+        float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+        uint32_t occupied = 0;
+        for (int c = 0; c < 8; c++) {
+            if (__float_as_int(f[48 + c]) < 0) continue;
+            occupied |= 1u << c;
+            for (int a = 0; a < 3; a++) {
+                lo[a] = fminf(lo[a], f[16 * a + c]);
+                hi[a] = fmaxf(hi[a], f[16 * a + 8 + c]);
+            }
+        }
+        float4 *q = out + (size_t)i * ptd::kCwFloat4;
+        if (!occupied) {
+            q[0] = make_float4(0.f, 0.f, 0.f, __uint_as_float(127u | 127u << 8 | 127u << 16));
+            q[1] = q[2] = q[3] = make_float4(0.f, 0.f, 0.f, 0.f);
+            q[4] = q[5] = make_float4(__int_as_float(ptd::kNoItem), __int_as_float(ptd::kNoItem),
+                                      __int_as_float(ptd::kNoItem), __int_as_float(ptd::kNoItem));
+            continue;
+        }
+        uint32_t eb[3];
+        float cell[3];
+        for (int a = 0; a < 3; a++) {
+            const float r = __fdiv_ru(__fsub_ru(hi[a], lo[a]), 255.f);
+            uint32_t e = 1;
+            if (r > 0.f) {
+                const uint32_t bits = __float_as_uint(r);
+                e = (bits >> 23) + ((bits & 0x7fffffu) ? 1u : 0u);
+                e = e < 1u ? 1u : e;
+            }
+            while (e < 254u && __fmaf_rn(255.f, __uint_as_float(e << 23), lo[a]) < hi[a]) e++;
+            eb[a] = e;
+            cell[a] = __uint_as_float(e << 23);
+        }
+        // slot assignment
+        float cen[8][3];
+        for (int c = 0; c < 8; c++)
+            for (int a = 0; a < 3; a++)
+                cen[c][a] = (occupied >> c) & 1u ? 0.5f * (f[16 * a + c] + f[16 * a + 8 + c]) - 0.5f * (lo[a] + hi[a])
+                                                 : 0.f;
+        int slot_of[8];
+        for (int c = 0; c < 8; c++) slot_of[c] = -1;
+        uint32_t used = 0, todo = occupied;
+        while (todo) {
+            float best = FLT_MAX;
+            int bc = -1, bs = -1;
+            for (int c = 0; c < 8; c++) {
+                if (!((todo >> c) & 1u)) continue;
+                for (int sl = 0; sl < 8; sl++) {
+                    if ((used >> sl) & 1u) continue;
+                    const float cost = (sl & 1 ? -cen[c][0] : cen[c][0]) + (sl & 2 ? -cen[c][1] : cen[c][1]) +
+                                       (sl & 4 ? -cen[c][2] : cen[c][2]);
+                    if (bc < 0 || cost < best) {
+                        best = cost;
+                        bc = c;
+                        bs = sl;
+                    }
+                }
+            }
+            slot_of[bc] = bs;
+            used |= 1u << bs;
+            todo &= ~(1u << bc);
+        }
+        uint32_t cl[3][2] = {{0, 0}, {0, 0}, {0, 0}}, ch[3][2] = {{0, 0}, {0, 0}, {0, 0}};
+        int items[8];
+        for (int sl = 0; sl < 8; sl++) items[sl] = ptd::kNoItem;
+        for (int c = 0; c < 8; c++) {
+            const int sl = slot_of[c];
+            if (sl < 0) continue;
+            for (int a = 0; a < 3; a++) {
+                const float clo = f[16 * a + c], chi = f[16 * a + 8 + c];
+                const float inv_cell = __frcp_rn(cell[a]);
+                int ql = (int)floorf(__fmul_rd(__fsub_rd(clo, lo[a]), inv_cell));
+                ql = min(max(ql, 0), 255);
+                while (ql > 0 && __fmaf_rn((float)ql, cell[a], lo[a]) > clo) ql--;
+                int qh = (int)ceilf(__fmul_ru(__fsub_ru(chi, lo[a]), inv_cell));
+                qh = min(max(qh, 0), 255);
+                while (qh < 255 && __fmaf_rn((float)qh, cell[a], lo[a]) < chi) qh++;
+                cl[a][sl >> 2] |= (uint32_t)ql << (8 * (sl & 3));
+                ch[a][sl >> 2] |= (uint32_t)qh << (8 * (sl & 3));
+            }
+            const int child = __float_as_int(f[48 + c]), count = __float_as_int(f[56 + c]);
+            items[sl] = count > 0 ? ptd::make_leaf(child, count) : child;
+        }
+        q[0] = make_float4(lo[0], lo[1], lo[2], __uint_as_float(eb[0] | eb[1] << 8 | eb[2] << 16 | used << 24));
+        for (int a = 0; a < 3; a++)
+            q[1 + a] = make_float4(__uint_as_float(cl[a][0]), __uint_as_float(cl[a][1]), __uint_as_float(ch[a][0]),
+                                   __uint_as_float(ch[a][1]));
+        q[4] = make_float4(__int_as_float(items[0]), __int_as_float(items[1]), __int_as_float(items[2]),
+                           __int_as_float(items[3]));
+        q[5] = make_float4(__int_as_float(items[4]), __int_as_float(items[5]), __int_as_float(items[6]),
+                           __int_as_float(items[7]));
+    }
+}
+
 struct Scratch {
     uint64_t *keys[2];
     uint32_t *vals[2];
@@ -1099,6 +1205,11 @@ int pt_bvh_build_impl(pt_scene *s, const pt_bvh_opts *o, cudaStream_t st) {
         if ((e = radix_tree()) != PT_OK) return e;
         if ((e = wide(0)) != PT_OK) return e;
     }
+    if (o->width == 8) {  // the traversal reads compressed copies of the 8-wide nodes
+        const uint32_t nn = s->level_start.back();
+        if ((e = s->cnodes.ensure((size_t)std::max<uint32_t>(nn, 1) * 16 * ptd::kCwFloat4)) != PT_OK) return e;
+        if ((e = pt_compress_wide8(s->nodes.as<float>(), nn, s->cnodes.as<float4>(), st)) != PT_OK) return e;
+    }
     PT_CUDA_TRY(cudaEventRecord(s->ev1, st));
     PT_CUDA_TRY(cudaEventSynchronize(s->ev1));
     float ms = 0.f;
@@ -1115,20 +1226,27 @@ int pt_bvh_build_impl(pt_scene *s, const pt_bvh_opts *o, cudaStream_t st) {
     bs.max_depth = (uint32_t)s->level_start.size() - 1;
     bs.sah_cost = sah;
     bs.build_ms = ms;
-    bs.node_bytes = (uint64_t)bs.num_nodes * 32 * K;
+    bs.node_bytes = (uint64_t)bs.num_nodes * (K == 8 ? 16 * ptd::kCwFloat4 : 32 * K);  // the bytes the traversal reads
     bs.builder = clustered ? PT_BVH_BUILDER_PLOC : PT_BVH_BUILDER_RADIX;
     bs.prim_bytes = (uint64_t)n * 48;
     bs.num_leaves = 0;
 
     ptd::DevScene &d = s->dev;
     d.nodes = s->nodes.as<float4>();
+    d.cnodes = o->width == 8 ? s->cnodes.as<float4>() : nullptr;
     d.prims = s->prims_bvh.as<float4>();
     d.width = o->width;
     d.num_nodes = bs.num_nodes;
     uint32_t max_smem = (uint32_t)std::max(0, s->max_smem_per_block - 64 * 1024) / (32 * K);
-    d.smem_nodes = std::min<uint32_t>(std::min(o->smem_nodes, bs.num_nodes), max_smem);
+    d.smem_nodes = o->width == 8 ? 0 : std::min<uint32_t>(std::min(o->smem_nodes, bs.num_nodes), max_smem);
     d.pad_mag = s->scene_mag;
     s->bvh_built = true;
+    return PT_OK;
+}
+
+int pt_compress_wide8(const float *nodes, uint32_t n, float4 *out, cudaStream_t st) {
+    if (n) k_compress8<<<blocks(n, 128), 128, 0, st>>>(nodes, n, out);
+    PT_CUDA_TRY(cudaGetLastError());
     return PT_OK;
 }
 
@@ -1145,6 +1263,10 @@ int pt_bvh_refit_impl(pt_scene *s, cudaStream_t st) {
         default: refit_levels<8>(s, st); break;
     }
     PT_CUDA_TRY(cudaGetLastError());
+    if (s->bvh_opts.width == 8) {
+        const int e = pt_compress_wide8(s->nodes.as<float>(), s->bvh_stats.num_nodes, s->cnodes.as<float4>(), st);
+        if (e != PT_OK) return e;
+    }
     PT_CUDA_TRY(cudaEventRecord(s->ev1, st));
     PT_CUDA_TRY(cudaEventSynchronize(s->ev1));
     float ms = 0.f;

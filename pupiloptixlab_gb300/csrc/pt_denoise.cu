@@ -251,27 +251,39 @@ __global__ void k_adam_begin(float *state, float beta1, float beta2) {
     state[2] = 1.f / (1.f - powf(beta2, t));
 }
 
-// One layer: weights [cout][9][cin] then bias[cout].  Also writes the BF16
-// weights and their flipped transpose [cin][9][cout] for the data gradient.
-__global__ void k_adam(float *p, float *m, float *v, const float *g, long long nw, int nb, int cout, int cin,
-                       const float *state, float beta1, float beta2, float eps, uint16_t *wbf, uint16_t *wtbf) {
+// Adam over every layer in one launch.  Layer l's parameters are its weights
+// [cout][9][cin] at w_off[l] followed by its bias[cout]; the kernel also
+// writes the BF16 weights and their flipped transpose [cin][9][cout] (for the
+// data gradient) at wbf_off[l].
+struct AdamLayers {
+    long long w_off[kLayers], nw[kLayers], wbf_off[kLayers];
+    int cin[kLayers], cout[kLayers];
+};
+
+__global__ void k_adam(float *p, float *m, float *v, const float *g, const AdamLayers L, const float *state,
+                       float beta1, float beta2, float eps, uint16_t *wbf, uint16_t *wtbf) {
     const float c1 = state[1], c2 = state[2], lr = state[3];
-    const long long n = nw + nb;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const float gi = g[i];
-        const float mi = beta1 * m[i] + (1.f - beta1) * gi;
-        const float vi = beta2 * v[i] + (1.f - beta2) * gi * gi;
-        m[i] = mi;
-        v[i] = vi;
-        const float pi = p[i] - lr * (mi * c1) / (sqrtf(vi * c2) + eps);
-        p[i] = pi;
-        if (i < nw) {
-            const uint16_t b = f2bf(pi);
-            wbf[i] = b;
-            const int ci = static_cast<int>(i % cin);
-            const int tap = static_cast<int>((i / cin) % 9);
-            const int co = static_cast<int>(i / (9ll * cin));
-            wtbf[(static_cast<long long>(ci) * 9 + (8 - tap)) * cout + co] = b;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (int l = 0; l < kLayers; l++) {
+        const long long nw = L.nw[l], n = nw + L.cout[l], o = L.w_off[l];
+        const int cin = L.cin[l], cout = L.cout[l];
+        uint16_t *wb = wbf + L.wbf_off[l], *wt = wtbf + L.wbf_off[l];
+        for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride) {
+            const float gi = g[o + i];
+            const float mi = beta1 * m[o + i] + (1.f - beta1) * gi;
+            const float vi = beta2 * v[o + i] + (1.f - beta2) * gi * gi;
+            m[o + i] = mi;
+            v[o + i] = vi;
+            const float pi = p[o + i] - lr * (mi * c1) / (sqrtf(vi * c2) + eps);
+            p[o + i] = pi;
+            if (i < nw) {
+                const uint16_t b = f2bf(pi);
+                wb[i] = b;
+                const int ci = static_cast<int>(i % cin);
+                const int tap = static_cast<int>((i / cin) % 9);
+                const int co = static_cast<int>(i / (9ll * cin));
+                wt[(static_cast<long long>(ci) * 9 + (8 - tap)) * cout + co] = b;
+            }
         }
     }
 }
@@ -655,15 +667,19 @@ int run_backward(pt_denoiser *dn, Plan &P, const float *target, cudaStream_t s) 
 int run_adam(pt_denoiser *dn, cudaStream_t s) {
     const pt_denoiser_opts &o = dn->opts;
     k_adam_begin<<<1, 1, 0, s>>>(dn->adam_state.as<float>(), o.beta1, o.beta2);
+    AdamLayers L;
+    long long largest = 0;
     for (int l = 0; l < kLayers; l++) {
-        const LayerSpec &L = kSpec[l];
-        const long long nw = 9ll * L.cin * L.cout;
-        const uint64_t off = dn->w_off[l];
-        k_adam<<<grid_for(nw + L.cout), 256, 0, s>>>(
-            dn->params.as<float>() + off, dn->adam_m.as<float>() + off, dn->adam_v.as<float>() + off,
-            dn->grads.as<float>() + off, nw, L.cout, L.cout, L.cin, dn->adam_state.as<float>(), o.beta1, o.beta2, o.eps,
-            dn->wbf.as<uint16_t>() + dn->wbf_off[l], dn->wtbf.as<uint16_t>() + dn->wbf_off[l]);
+        L.w_off[l] = static_cast<long long>(dn->w_off[l]);
+        L.nw[l] = 9ll * kSpec[l].cin * kSpec[l].cout;
+        L.wbf_off[l] = static_cast<long long>(dn->wbf_off[l]);
+        L.cin[l] = kSpec[l].cin;
+        L.cout[l] = kSpec[l].cout;
+        largest = std::max(largest, L.nw[l] + L.cout[l]);
     }
+    k_adam<<<grid_for(largest), 256, 0, s>>>(dn->params.as<float>(), dn->adam_m.as<float>(), dn->adam_v.as<float>(),
+                                             dn->grads.as<float>(), L, dn->adam_state.as<float>(), o.beta1, o.beta2,
+                                             o.eps, dn->wbf.as<uint16_t>(), dn->wtbf.as<uint16_t>());
     PT_CUDA_TRY(cudaGetLastError());
     return PT_OK;
 }

@@ -185,6 +185,7 @@ constexpr uint32_t kInstCurveTypeShift = 12;  // 2 bits: PT_CURVE_*
 struct DevScene {
     // acceleration structure
     const float4 *nodes;    // wide nodes, 8*width floats each
+    const float4 *cnodes;   // width 8: the same nodes compressed (6 float4 each), which the traversal reads
     const float4 *prims;    // 3 float4 per primitive slot in leaf order
     uint32_t width;         // 2, 4 or 8
     uint32_t num_nodes;
@@ -219,7 +220,7 @@ struct DevScene {
 
 // Traversal stack entries per thread (shared-memory short stack plus local
 // spill); a wide tree of depth D needs up to D * (width - 1).
-constexpr int kTraversalStackEntries = 64;
+constexpr int kTraversalStackEntries = 96;
 
 // Primitives per BVH (one scene, or the merged scenes of a batch): a leaf on
 // the traversal stack packs its first primitive slot into 27 bits.

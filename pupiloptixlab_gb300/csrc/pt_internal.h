@@ -100,6 +100,7 @@ struct pt_scene {
     DevBuf prims_world;  // 3 float4 per prim (world order)
     DevBuf prims_bvh;    // 3 float4 per prim (leaf order)
     DevBuf nodes;
+    DevBuf cnodes;       // width 8: compressed copies of the nodes (the traversal reads these)
     DevBuf tri_vidx, vpos, vnrm, vuv, prim_inst, inst, mats, emitters, emitter_cdf;
     DevBuf emitter_tex;  // textures of textured area-emitter radiance (DevTexture each)
     DevBuf curve_seg, curve_cp;  // piece -> segment; 4 world control points per segment
@@ -143,6 +144,8 @@ struct pt_scene {
 // pt_bvh.cu
 int pt_bvh_build_impl(pt_scene *s, const pt_bvh_opts *opts, cudaStream_t stream);
 int pt_bvh_refit_impl(pt_scene *s, cudaStream_t stream);
+// Compressed copies of n 8-wide float nodes (6 float4 each, same indices).
+int pt_compress_wide8(const float *nodes, uint32_t n, float4 *out, cudaStream_t stream);
 // pt_render.cu
 int pt_render_impl(pt_scene *s, const pt_render_params *p, const pt_frame_buffers *fb, cudaStream_t stream);
 int pt_render_batch_impl(pt_context *ctx, pt_scene *const *scenes, const pt_render_params *p,

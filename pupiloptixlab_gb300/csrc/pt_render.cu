@@ -292,7 +292,7 @@ PT_DI int2 *stage_smem(const DevScene &s, float4 *smem) {
 // ANY = false: closest hit of the extension rays; ANY = true: shadow rays.
 // Widths 2 and 4 are capped at 72 registers (7 blocks of 128 threads per SM).
 template <int K, bool ANY, bool COUNT, bool BATCH = false, bool CURVES = false>
-__global__ void __maxnreg__(K == 8 ? 128 : 72) k_trace_queue(DevScene s, State st, Batch bt, uint32_t npix) {
+__global__ void __maxnreg__(K == 8 ? 96 : 72) k_trace_queue(DevScene s, State st, Batch bt, uint32_t npix) {
     extern __shared__ float4 smem[];
     int2 *sstack = stage_smem<K>(s, smem);
     if (ANY) {
@@ -1094,14 +1094,14 @@ __global__ void k_rebase_nodes(float4 *nodes, uint32_t num_nodes, int node_off, 
 // the wave workspace (with its CUDA graph) and the last call's statistics.
 struct BatchWorkspace {
     RenderWorkspace ws;
-    DevBuf nodes, prims, scenes, outs, pix_off, roots, bins;
+    DevBuf nodes, cnodes, prims, scenes, outs, pix_off, roots, bins;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     pt_render_stats stats{};
 };
 
 void pt_batch_release(BatchWorkspace *b) {
     if (!b) return;
-    DevBuf *bufs[] = {&b->nodes, &b->prims, &b->scenes, &b->outs, &b->pix_off, &b->roots, &b->bins};
+    DevBuf *bufs[] = {&b->nodes, &b->cnodes, &b->prims, &b->scenes, &b->outs, &b->pix_off, &b->roots, &b->bins};
     for (DevBuf *d : bufs) d->release();
     RenderWorkspace &w = b->ws;
     DevBuf *wb[] = {&w.ray_o, &w.ray_d, &w.hit, &w.thr, &w.rad, &w.rng, &w.meta, &w.q0,
@@ -1176,6 +1176,12 @@ int render_batch(pt_context *ctx, pt_scene *const *scenes, const pt_render_param
         node_off += s->dev.num_nodes;
         prim_off += s->num_prims;
     }
+    if (K == 8) {  // the traversal reads compressed copies of the merged 8-wide nodes
+        if ((e = b.cnodes.ensure(std::max<uint64_t>(total_nodes, 1) * 16 * ptd::kCwFloat4)) != PT_OK) return e;
+        if ((e = pt_compress_wide8(b.nodes.as<float>(), static_cast<uint32_t>(total_nodes), b.cnodes.as<float4>(),
+                                   st)) != PT_OK)
+            return e;
+    }
     PT_CUDA_TRY(cudaMemcpyAsync(b.scenes.ptr, hs.data(), n * sizeof(DevScene), cudaMemcpyHostToDevice, st));
     PT_CUDA_TRY(cudaMemcpyAsync(b.outs.ptr, ho.data(), n * sizeof(Outputs), cudaMemcpyHostToDevice, st));
     PT_CUDA_TRY(cudaMemcpyAsync(b.pix_off.ptr, pix_off.data(), (n + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
@@ -1185,6 +1191,7 @@ int render_batch(pt_context *ctx, pt_scene *const *scenes, const pt_render_param
 
     DevScene dt = scenes[0]->dev;  // traversal view: merged arrays, no shared-memory top levels
     dt.nodes = b.nodes.as<float4>();
+    dt.cnodes = K == 8 ? b.cnodes.as<float4>() : nullptr;
     dt.prims = b.prims.as<float4>();
     dt.num_nodes = static_cast<uint32_t>(total_nodes);
     dt.smem_nodes = 0;

@@ -819,7 +819,7 @@ void DevBuf::release() {
 }
 
 pt_scene::~pt_scene() {
-    DevBuf *all[] = {&prims_world, &prims_bvh, &nodes, &tri_vidx, &vpos, &vnrm, &vuv, &prim_inst, &inst, &mats, &curve_seg, &curve_cp,
+    DevBuf *all[] = {&prims_world, &prims_bvh, &nodes, &cnodes, &tri_vidx, &vpos, &vnrm, &vuv, &prim_inst, &inst, &mats, &curve_seg, &curve_cp,
                      &emitters, &emitter_cdf, &emitter_tex, &mesh_obj_pos, &bvh_scratch, &bvh_order, &sah_scratch, &xform_table, &all_obj_pos, &ws.ray_o, &ws.ray_d, &ws.hit, &ws.thr,
                      &ws.rad, &ws.rng, &ws.meta, &ws.q0, &ws.q1, &ws.sh_o, &ws.sh_d, &ws.sh_c, &ws.mat_key,
                      &ws.counters, &ws.sort_tmp};

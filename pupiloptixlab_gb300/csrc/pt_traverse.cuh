@@ -23,6 +23,7 @@
 //           curve parameters [u0, u1] of its segment (pt_curve.h).
 // Nodes are in breadth-first order, so the first smem_nodes nodes are the
 // top levels; those are staged in shared memory once per (persistent) block.
+// Width 8 traverses compressed copies of the nodes instead (CwNode below).
 #pragma once
 
 #include "pt_curve.h"
@@ -287,6 +288,105 @@ PT_DI void load_node_smem(const float4 *p, WideNode<K> &n) {
     }
 }
 
+// Traversal items: a node index (>= 0), a leaf (bit 31 | first << 4 | count)
+// or kNoItem.  Leaves must start below 2^27 - 1 (checked at scene upload).
+constexpr int kNoItem = -1;
+PT_DI int make_leaf(int first, int count) { return (int)(0x80000000u | ((uint32_t)first << 4) | (uint32_t)count); }
+PT_DI bool is_leaf(int item) { return item < 0 && item != kNoItem; }
+PT_DI int leaf_first(int item) { return (int)(((uint32_t)item >> 4) & 0x7ffffffu); }
+PT_DI int leaf_count(int item) { return item & 15; }
+
+// Compressed 8-wide nodes: 96 bytes (6 float4) per node, after the quantised
+// wide nodes of Ylitie, Karras and Laine ("Efficient Incoherent Ray Traversal
+// on GPUs Through Compressed Wide BVHs", HPG 2017), with 32-bit child items:
+//   q0      xyz: grid origin p; w bits: biased exponents of the per-axis cell
+//           sizes 2^e (bytes 0-2), mask of the occupied slots (byte 3)
+//   q1..q3  axis x, y, z: low cells of slots 0-7 (8 bytes), high cells (8 bytes)
+//   q4, q5  child items of slots 0-7 (inner node index, leaf item or kNoItem)
+// Slot c's box is [fma(lo, 2^e, p), fma(hi, 2^e, p)] per axis; the builder
+// picks the cells so that these bounds enclose the child's padded float box.
+// Slot s holds the child that rays of direction octant s (bit 0: d.x < 0,
+// bit 1: d.y < 0, bit 2: d.z < 0) should visit first, and a ray takes the hit
+// children in the order slot ^ octant: no sorting of the children.
+constexpr int kCwFloat4 = 6;
+
+PT_DI int4 ld_bvh_i4(const float4 *p) {
+    int4 v;
+    asm("ld.global.nc.L1::evict_last.v4.s32 {%0, %1, %2, %3}, [%4];"
+        : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+        : "l"(p));
+    return v;
+}
+
+// Cell `c` (0-7) of the 8 bytes held by the words (w0, w1): the byte is
+// placed in the mantissa of 2^23 with one byte permute, and 2^23 is taken
+// off again (exact), which avoids the slower integer-to-float conversion.
+PT_DI float cw_cell(uint32_t w0, uint32_t w1, int c) {
+    const uint32_t v = __byte_perm(c & 4 ? w1 : w0, 0x4b000000u, 0x7650u | static_cast<uint32_t>(c & 3));
+    return __fsub_rn(__uint_as_float(v), 8388608.f);
+}
+PT_DI int cw_pick(int4 i0, int4 i1, int c) {
+    const int4 h = c & 4 ? i1 : i0;
+    return c & 2 ? (c & 1 ? h.w : h.z) : (c & 1 ? h.y : h.x);
+}
+
+// Slab test of the 8 children of compressed node `p`, in visiting order:
+// entry k is slot k ^ oct.  ci[k] = child item (kNoItem: missed or empty),
+// ct[k] = entry distance.  fast: origin within the magnitude the boxes were
+// padded for, so t = fma(cell, 2^e * inv, (p - o) * inv) is conservative
+// (its error, at most about 2 ulp of |p - o|, stays inside the padding);
+// otherwise each bound is formed as in the build and tested as a float box.
+PT_DI void cw_children(const float4 *p, float3 o, float3 inv, bool fast, float tmin, float tlimit, int oct, int *ci,
+                       float *ct) {
+    const float4 q0 = ld_bvh(p), q1 = ld_bvh(p + 1), q2 = ld_bvh(p + 2), q3 = ld_bvh(p + 3);
+    const int4 i0 = ld_bvh_i4(p + 4), i1 = ld_bvh_i4(p + 5);
+    const uint32_t meta = __float_as_uint(q0.w);
+    const float sx = __uint_as_float((meta & 0xffu) << 23), sy = __uint_as_float(((meta >> 8) & 0xffu) << 23),
+                sz = __uint_as_float(((meta >> 16) & 0xffu) << 23);
+    const uint32_t occupied = meta >> 24;
+    const float ax = __fmul_rn(sx, inv.x), ay = __fmul_rn(sy, inv.y), az = __fmul_rn(sz, inv.z);
+    const float bx = __fmul_rn(__fsub_rn(q0.x, o.x), inv.x), by = __fmul_rn(__fsub_rn(q0.y, o.y), inv.y),
+                bz = __fmul_rn(__fsub_rn(q0.z, o.z), inv.z);
+    const uint32_t lx0 = __float_as_uint(q1.x), lx1 = __float_as_uint(q1.y), hx0 = __float_as_uint(q1.z),
+                   hx1 = __float_as_uint(q1.w);
+    const uint32_t ly0 = __float_as_uint(q2.x), ly1 = __float_as_uint(q2.y), hy0 = __float_as_uint(q2.z),
+                   hy1 = __float_as_uint(q2.w);
+    const uint32_t lz0 = __float_as_uint(q3.x), lz1 = __float_as_uint(q3.y), hz0 = __float_as_uint(q3.z),
+                   hz1 = __float_as_uint(q3.w);
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const int c = k ^ oct;
+        ci[k] = kNoItem;
+        ct[k] = __int_as_float(0x7f800000);
+        if (!((occupied >> c) & 1u)) continue;
+        const float clx = cw_cell(lx0, lx1, c), chx = cw_cell(hx0, hx1, c);
+        const float cly = cw_cell(ly0, ly1, c), chy = cw_cell(hy0, hy1, c);
+        const float clz = cw_cell(lz0, lz1, c), chz = cw_cell(hz0, hz1, c);
+        float tx0, tx1, ty0, ty1, tz0, tz1;
+        if (fast) {
+            tx0 = __fmaf_rn(clx, ax, bx);
+            tx1 = __fmaf_rn(chx, ax, bx);
+            ty0 = __fmaf_rn(cly, ay, by);
+            ty1 = __fmaf_rn(chy, ay, by);
+            tz0 = __fmaf_rn(clz, az, bz);
+            tz1 = __fmaf_rn(chz, az, bz);
+        } else {
+            tx0 = __fmul_rn(__fsub_rn(__fmaf_rn(clx, sx, q0.x), o.x), inv.x);
+            tx1 = __fmul_rn(__fsub_rn(__fmaf_rn(chx, sx, q0.x), o.x), inv.x);
+            ty0 = __fmul_rn(__fsub_rn(__fmaf_rn(cly, sy, q0.y), o.y), inv.y);
+            ty1 = __fmul_rn(__fsub_rn(__fmaf_rn(chy, sy, q0.y), o.y), inv.y);
+            tz0 = __fmul_rn(__fsub_rn(__fmaf_rn(clz, sz, q0.z), o.z), inv.z);
+            tz1 = __fmul_rn(__fsub_rn(__fmaf_rn(chz, sz, q0.z), o.z), inv.z);
+        }
+        const float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
+        float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
+        tf = fminf(__fmul_rn(tf, kSlabScale), tlimit);
+        if (!(tn <= tf)) continue;
+        ci[k] = cw_pick(i0, i1, c);
+        ct[k] = tn;
+    }
+}
+
 // Per-thread traversal stack of (item, entry distance): kShortStack entries
 // in shared memory (strided by the block size to avoid bank conflicts), the
 // rest in local memory.
@@ -311,13 +411,6 @@ struct ShortStack {
     }
 };
 
-// Traversal items: a node index (>= 0), a leaf (bit 31 | first << 4 | count)
-// or kNoItem.  Leaves must start below 2^27 - 1 (checked at scene upload).
-constexpr int kNoItem = -1;
-PT_DI int make_leaf(int first, int count) { return (int)(0x80000000u | ((uint32_t)first << 4) | (uint32_t)count); }
-PT_DI bool is_leaf(int item) { return item < 0 && item != kNoItem; }
-PT_DI int leaf_first(int item) { return (int)(((uint32_t)item >> 4) & 0x7ffffffu); }
-PT_DI int leaf_count(int item) { return item & 15; }
 
 // Lanes refill their ray when at most this many lanes of the warp are busy.
 constexpr int kRefillBusyMax = 20;
@@ -356,6 +449,7 @@ PT_DI void trace_persistent(const DevScene &s, const float4 *snodes, int2 *sstac
     uint32_t idx = 0, tag = 0;
     float3 o = f3s(0.f), d = f3s(0.f), inv = f3s(0.f), oi = f3s(0.f);
     bool fma_slab = false;
+    int oct = 0;  // direction octant (compressed 8-wide nodes)
     RayWT w{0, 1, 2, 0.f, 0.f, 1.f};
     float tmin = 0.f, tmax = 0.f;
     TraceResult best{0.f, -1, 0.f, 0.f};
@@ -389,6 +483,7 @@ PT_DI void trace_persistent(const DevScene &s, const float4 *snodes, int2 *sstac
                     // the FMA slab form is conservative for origins inside the
                     // magnitude the boxes were padded for
                     fma_slab = fmaxf(fmaxf(fabsf(o.x), fabsf(o.y)), fabsf(o.z)) <= s.pad_mag;
+                    oct = (d.x < 0.f ? 1 : 0) | (d.y < 0.f ? 2 : 0) | (d.z < 0.f ? 4 : 0);
                     best.t = tmax;
                     best.prim = -1;
                     best.u = best.v = 0.f;
@@ -414,71 +509,90 @@ PT_DI void trace_persistent(const DevScene &s, const float4 *snodes, int2 *sstac
             if (__all_sync(FULL, satisfied)) break;
             if (!__any_sync(FULL, can_step)) break;
             if (!can_step) continue;
-            WideNode<K> nd;
-            if (item < static_cast<int>(s.smem_nodes)) load_node_smem<K>(snodes + (size_t)item * 2 * K, nd);
-            else load_node<K>(s.nodes + (size_t)item * 2 * K, nd);
-            if (COUNT) nodes++;
-            int ci[K];
-            float ct[K];
-            const float tlimit = best.t * kSlabScale;
+            if constexpr (K == 8) {  // compressed node: children come in the octant's visiting order
+                if (COUNT) nodes++;
+                int ci[8];
+                float ct[8];
+                cw_children(s.cnodes + (size_t)item * kCwFloat4, o, inv, fma_slab, tmin, best.t * kSlabScale, oct, ci,
+                            ct);
+                // the first hit child is descended, the later ones pushed (popped in visiting order)
+                int next = kNoItem;
+                float next_t = 0.f;
 #pragma unroll
-            for (int c = 0; c < K; c++) {
-                ci[c] = kNoItem;
-                ct[c] = __int_as_float(0x7f800000);
-                int ch = nd.child(c);
-                if (ch < 0) continue;
-                float tx0, tx1, ty0, ty1, tz0, tz1;
-                if (fma_slab) {  // t = lo * inv - o * inv: one rounding, conservative within pad_mag
-                    tx0 = __fmaf_rn(nd.lox(c), inv.x, -oi.x);
-                    tx1 = __fmaf_rn(nd.hix(c), inv.x, -oi.x);
-                    ty0 = __fmaf_rn(nd.loy(c), inv.y, -oi.y);
-                    ty1 = __fmaf_rn(nd.hiy(c), inv.y, -oi.y);
-                    tz0 = __fmaf_rn(nd.loz(c), inv.z, -oi.z);
-                    tz1 = __fmaf_rn(nd.hiz(c), inv.z, -oi.z);
-                } else {
-                    tx0 = (nd.lox(c) - o.x) * inv.x;
-                    tx1 = (nd.hix(c) - o.x) * inv.x;
-                    ty0 = (nd.loy(c) - o.y) * inv.y;
-                    ty1 = (nd.hiy(c) - o.y) * inv.y;
-                    tz0 = (nd.loz(c) - o.z) * inv.z;
-                    tz1 = (nd.hiz(c) - o.z) * inv.z;
+                for (int i = 7; i >= 0; i--) {
+                    if (ci[i] == kNoItem) continue;
+                    if (next != kNoItem) st.push(next, next_t, ovf);
+                    next = ci[i];
+                    next_t = ct[i];
                 }
-                float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
-                float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
-                tf = fminf(tf * kSlabScale, tlimit);
-                if (!(tn <= tf)) continue;
-                int cnt = nd.count(c);
-                ci[c] = cnt > 0 ? make_leaf(ch, cnt) : ch;
-                ct[c] = tn;
-            }
-            // closest hit: nearest child first (sorting network); any hit: order
-            // does not matter, the children are taken as they come
+                item = next != kNoItem ? next : pop_valid();
+            } else {
+                WideNode<K> nd;
+                if (item < static_cast<int>(s.smem_nodes)) load_node_smem<K>(snodes + (size_t)item * 2 * K, nd);
+                else load_node<K>(s.nodes + (size_t)item * 2 * K, nd);
+                if (COUNT) nodes++;
+                int ci[K];
+                float ct[K];
+                const float tlimit = best.t * kSlabScale;
 #pragma unroll
-            for (int i = 1; i < (ANY ? 1 : K); i++) {
+                for (int c = 0; c < K; c++) {
+                    ci[c] = kNoItem;
+                    ct[c] = __int_as_float(0x7f800000);
+                    int ch = nd.child(c);
+                    if (ch < 0) continue;
+                    float tx0, tx1, ty0, ty1, tz0, tz1;
+                    if (fma_slab) {  // t = lo * inv - o * inv: one rounding, conservative within pad_mag
+                        tx0 = __fmaf_rn(nd.lox(c), inv.x, -oi.x);
+                        tx1 = __fmaf_rn(nd.hix(c), inv.x, -oi.x);
+                        ty0 = __fmaf_rn(nd.loy(c), inv.y, -oi.y);
+                        ty1 = __fmaf_rn(nd.hiy(c), inv.y, -oi.y);
+                        tz0 = __fmaf_rn(nd.loz(c), inv.z, -oi.z);
+                        tz1 = __fmaf_rn(nd.hiz(c), inv.z, -oi.z);
+                    } else {
+                        tx0 = (nd.lox(c) - o.x) * inv.x;
+                        tx1 = (nd.hix(c) - o.x) * inv.x;
+                        ty0 = (nd.loy(c) - o.y) * inv.y;
+                        ty1 = (nd.hiy(c) - o.y) * inv.y;
+                        tz0 = (nd.loz(c) - o.z) * inv.z;
+                        tz1 = (nd.hiz(c) - o.z) * inv.z;
+                    }
+                    float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
+                    float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
+                    tf = fminf(tf * kSlabScale, tlimit);
+                    if (!(tn <= tf)) continue;
+                    int cnt = nd.count(c);
+                    ci[c] = cnt > 0 ? make_leaf(ch, cnt) : ch;
+                    ct[c] = tn;
+                }
+                // closest hit: nearest child first (sorting network); any hit: order
+                // does not matter, the children are taken as they come
 #pragma unroll
-                for (int j = i; j > 0; j--) {
-                    if (ct[j] < ct[j - 1]) {
-                        float tt = ct[j];
-                        ct[j] = ct[j - 1];
-                        ct[j - 1] = tt;
-                        int ti = ci[j];
-                        ci[j] = ci[j - 1];
-                        ci[j - 1] = ti;
+                for (int i = 1; i < (ANY ? 1 : K); i++) {
+#pragma unroll
+                    for (int j = i; j > 0; j--) {
+                        if (ct[j] < ct[j - 1]) {
+                            float tt = ct[j];
+                            ct[j] = ct[j - 1];
+                            ct[j - 1] = tt;
+                            int ti = ci[j];
+                            ci[j] = ci[j - 1];
+                            ci[j - 1] = ti;
+                        }
                     }
                 }
-            }
-            if (ANY) {  // unsorted: the first hit child is descended, the others pushed
+                if (ANY) {  // unsorted: the first hit child is descended, the others pushed
 #pragma unroll
-                for (int i = 1; i < K; i++)
-                    if (ci[0] == kNoItem && ci[i] != kNoItem) {
-                        ci[0] = ci[i];
-                        ci[i] = kNoItem;
-                    }
-            }
+                    for (int i = 1; i < K; i++)
+                        if (ci[0] == kNoItem && ci[i] != kNoItem) {
+                            ci[0] = ci[i];
+                            ci[i] = kNoItem;
+                        }
+                }
 #pragma unroll
-            for (int i = K - 1; i >= 1; i--)
-                if (ci[i] != kNoItem) st.push(ci[i], ct[i], ovf);
-            item = ci[0] != kNoItem ? ci[0] : pop_valid();
+                for (int i = K - 1; i >= 1; i--)
+                    if (ci[i] != kNoItem) st.push(ci[i], ct[i], ovf);
+                item = ci[0] != kNoItem ? ci[0] : pop_valid();
+            }
             if (is_leaf(item) && leaf == kNoItem) {  // postpone the first leaf
                 leaf = item;
                 item = pop_valid();

@@ -1,5 +1,6 @@
-"""Traversal parity: pt_trace_rays (closest and any hit, BVH widths 2/4/8,
-with and without top levels in shared memory) against the oracle's
+"""Traversal parity: pt_trace_rays (closest and any hit, BVH widths 2/4/8 --
+8 as compressed nodes -- with and without top levels in shared memory,
+origins inside and far outside the scene) against the oracle's
 brute-force intersector.  Hit primitive ids, distances and barycentrics must
 be bit-identical: both sides run the same watertight triangle test with
 explicitly rounded FP32 operations and the (t, id) tie-break."""
@@ -103,13 +104,34 @@ def test_both_tree_builders(cuda_ctx, width, fast_build):
     g.close()
 
 
-def test_full_size_scene_primary_rays(cuda_ctx):
+@pytest.mark.parametrize("width", [2, 4, 8])
+def test_far_origins(cuda_ctx, width):
+    """Origins far outside the scene's magnitude, where the traversal leaves
+    the padded fused-multiply-add slab form for the rounded-difference one
+    (for compressed 8-wide nodes: each bound decoded as in the build)."""
+    sc = scenes.cornell_box(16, 16)
+    o = oracle.OracleScene(sc, bvh=False)
+    g = GpuScene(cuda_ctx, sc, bvh_width=width)
+    rng = np.random.default_rng(40 + width)
+    target = rays_inside(rng, 20000, (0, 1, 0), (0.9, 0.9, 0.9))
+    d = rng.normal(size=(target.shape[0], 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    dist = rng.uniform(50.0, 5e3, (target.shape[0], 1))
+    rays = target.copy()
+    rays[:, 0:3] = target[:, 0:3] - d * dist
+    rays[:, 4:7] = d
+    assert_hits_equal(gpu_trace(g, rays), o.trace(rays, brute_force=True))
+    assert (gpu_trace(g, rays)[:, 1].view(np.int32) >= 0).mean() > 0.5
+
+
+@pytest.mark.parametrize("width", [4, 8])
+def test_full_size_scene_primary_rays(cuda_ctx, width):
     """Icosphere-field geometry (1,032,192 triangles + 4 spheres) at 1920x1080:
     every 16th primary ray against the oracle's BVH2 (itself equal to brute
     force, tests/test_oracle_host.py) and 192 rays against brute force."""
     sc = scenes.icosphere_field()
     o = oracle.OracleScene(sc, bvh=True)
-    g = GpuScene(cuda_ctx, sc, bvh_width=4)
+    g = GpuScene(cuda_ctx, sc, bvh_width=width)
     st = g.bvh_stats()
     assert st.num_prims == 1032196 and st.num_nodes > 1000
     rays = o.camera_rays(abi.RNG_PCG32, 0)[::16]
