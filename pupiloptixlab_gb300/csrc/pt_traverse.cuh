@@ -399,7 +399,7 @@ struct ShortStack {
         int2 e = make_int2(item, __float_as_int(t));
         if (sp < kShortStack) smem[sp * stride] = e;
         else if (sp < kShortStack + kSpillStack) spill[sp - kShortStack] = e;
-        else {  // cannot happen for trees of depth <= 21 (width 4); reported, entry dropped
+        else {  // cannot happen for trees of depth <= 32 (width 4), 13 (width 8); reported, entry dropped
             overflow = 1;
             return;
         }
