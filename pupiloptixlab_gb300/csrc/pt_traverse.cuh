@@ -256,6 +256,14 @@ PT_DI float4 ld_bvh(const float4 *p) {
         : "l"(p));
     return v;
 }
+// 32 bytes per load (256-bit global loads, sm_100 and later): a node is
+// 32 * K bytes at a 32-byte-aligned offset of a cudaMalloc'd array.
+PT_DI void ld_bvh8(const float4 *p, float *f) {
+    asm("ld.global.nc.L1::evict_last.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(f[0]), "=f"(f[1]), "=f"(f[2]), "=f"(f[3]), "=f"(f[4]), "=f"(f[5]), "=f"(f[6]), "=f"(f[7])
+        : "l"(p));
+}
+
 template <typename T>
 PT_DI T ld_stream(const T *p) {
     return __ldcs(p);
@@ -268,13 +276,7 @@ PT_DI void st_stream(T *p, T v) {
 template <int K>
 PT_DI void load_node(const float4 *__restrict__ p, WideNode<K> &n) {
 #pragma unroll
-    for (int i = 0; i < 2 * K; i++) {
-        float4 v = ld_bvh(p + i);
-        n.f[4 * i + 0] = v.x;
-        n.f[4 * i + 1] = v.y;
-        n.f[4 * i + 2] = v.z;
-        n.f[4 * i + 3] = v.w;
-    }
+    for (int i = 0; i < K; i++) ld_bvh8(p + 2 * i, n.f + 8 * i);
 }
 template <int K>
 PT_DI void load_node_smem(const float4 *p, WideNode<K> &n) {
@@ -310,14 +312,6 @@ PT_DI int leaf_count(int item) { return item & 15; }
 // children in the order slot ^ octant: no sorting of the children.
 constexpr int kCwFloat4 = 6;
 
-PT_DI int4 ld_bvh_i4(const float4 *p) {
-    int4 v;
-    asm("ld.global.nc.L1::evict_last.v4.s32 {%0, %1, %2, %3}, [%4];"
-        : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
-        : "l"(p));
-    return v;
-}
-
 // Cell `c` (0-7) of the 8 bytes held by the words (w0, w1): the byte is
 // placed in the mantissa of 2^23 with one byte permute, and 2^23 is taken
 // off again (exact), which avoids the slower integer-to-float conversion.
@@ -338,8 +332,14 @@ PT_DI int cw_pick(int4 i0, int4 i1, int c) {
 // otherwise each bound is formed as in the build and tested as a float box.
 PT_DI void cw_children(const float4 *p, float3 o, float3 inv, bool fast, float tmin, float tlimit, int oct, int *ci,
                        float *ct) {
-    const float4 q0 = ld_bvh(p), q1 = ld_bvh(p + 1), q2 = ld_bvh(p + 2), q3 = ld_bvh(p + 3);
-    const int4 i0 = ld_bvh_i4(p + 4), i1 = ld_bvh_i4(p + 5);
+    float f[24];  // 96 bytes at a 32-byte-aligned offset: three 256-bit loads
+    ld_bvh8(p, f);
+    ld_bvh8(p + 2, f + 8);
+    ld_bvh8(p + 4, f + 16);
+    const float4 q0 = make_float4(f[0], f[1], f[2], f[3]), q1 = make_float4(f[4], f[5], f[6], f[7]),
+                 q2 = make_float4(f[8], f[9], f[10], f[11]), q3 = make_float4(f[12], f[13], f[14], f[15]);
+    const int4 i0 = make_int4(__float_as_int(f[16]), __float_as_int(f[17]), __float_as_int(f[18]), __float_as_int(f[19])),
+               i1 = make_int4(__float_as_int(f[20]), __float_as_int(f[21]), __float_as_int(f[22]), __float_as_int(f[23]));
     const uint32_t meta = __float_as_uint(q0.w);
     const float sx = __uint_as_float((meta & 0xffu) << 23), sy = __uint_as_float(((meta >> 8) & 0xffu) << 23),
                 sz = __uint_as_float(((meta >> 16) & 0xffu) << 23);
