@@ -176,6 +176,19 @@ __device__ __forceinline__ uint16_t f2bf(float f) {
     return *reinterpret_cast<uint16_t *>(&h);
 }
 
+// 32-byte global accesses (256-bit loads and stores, sm_100 and later): the
+// 16 BF16 channels a thread handles per step are one full sector.
+__device__ __forceinline__ void ld_global_v8(const uint16_t *p, uint4 &a, uint4 &b) {
+    asm volatile("ld.global.v8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                 : "=r"(a.x), "=r"(a.y), "=r"(a.z), "=r"(a.w), "=r"(b.x), "=r"(b.y), "=r"(b.z), "=r"(b.w)
+                 : "l"(p));
+}
+__device__ __forceinline__ void st_global_v8(uint16_t *p, uint4 a, uint4 b) {
+    asm volatile("st.global.v8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(p), "r"(a.x), "r"(a.y), "r"(a.z),
+                 "r"(a.w), "r"(b.x), "r"(b.y), "r"(b.z), "r"(b.w)
+                 : "memory");
+}
+
 // Forward epilogue: accumulator row `tid` = pixel (x0 + tid % tile_w,
 // y0 + tid / tile_w); warp w reads TMEM lanes 32w..32w+31, 16 columns at a time.
 __device__ __forceinline__ void fwd_epilogue(const FwdArgs &a, uint32_t tmem, int tid, int warp, int img, int x0, int y0,
@@ -205,7 +218,13 @@ __device__ __forceinline__ void fwd_epilogue(const FwdArgs &a, uint32_t tmem, in
         } else {
             const uint16_t *m = a.mask + pix * a.mask_ctot + a.mask_coff + ch0;
             if (nvalid == 16) {
-                uint4 q0 = *reinterpret_cast<const uint4 *>(m), q1 = *reinterpret_cast<const uint4 *>(m + 8);
+                uint4 q0, q1;
+                if (a.wide_io) {
+                    ld_global_v8(m, q0, q1);
+                } else {
+                    q0 = *reinterpret_cast<const uint4 *>(m);
+                    q1 = *reinterpret_cast<const uint4 *>(m + 8);
+                }
                 const uint16_t *h0 = reinterpret_cast<const uint16_t *>(&q0), *h1 = reinterpret_cast<const uint16_t *>(&q1);
 #pragma unroll
                 for (int i = 0; i < 8; i++) {
@@ -226,8 +245,12 @@ __device__ __forceinline__ void fwd_epilogue(const FwdArgs &a, uint32_t tmem, in
                 w0[i] = f2bf(v[2 * i]) | (static_cast<uint32_t>(f2bf(v[2 * i + 1])) << 16);
                 w1[i] = f2bf(v[8 + 2 * i]) | (static_cast<uint32_t>(f2bf(v[8 + 2 * i + 1])) << 16);
             }
-            reinterpret_cast<uint4 *>(o)[0] = q0;
-            reinterpret_cast<uint4 *>(o)[1] = q1;
+            if (a.wide_io) {
+                st_global_v8(o, q0, q1);
+            } else {
+                reinterpret_cast<uint4 *>(o)[0] = q0;
+                reinterpret_cast<uint4 *>(o)[1] = q1;
+            }
         } else {
             for (int i = 0; i < nvalid; i++) o[i] = f2bf(v[i]);
         }
@@ -887,6 +910,13 @@ int fwd_prepare(FwdOp *op, const Act &in, const void *w, int w_rows, int cout, c
         a.mask_ctot = mask->ctot;
         a.mask_coff = mask->coff;
     }
+    // 32-byte accesses when every 16-channel group of the output (and mask)
+    // starts on a 32-byte boundary
+    auto al32 = [](const void *ptr, int ctot, int coff) {
+        return (reinterpret_cast<uintptr_t>(ptr) % 32) == 0 && ctot % 16 == 0 && coff % 16 == 0;
+    };
+    a.wide_io = epi != EPI_F32 && al32(out, out_ctot, out_coff) &&
+                (!mask || al32(mask->ptr, mask->ctot, mask->coff)) && !getenv_flag("PT_CONV_NO_WIDE_IO");
     a.err = err;
     a.wait_ns = wait_limit_ns();
     a.stall = take_stall_request() ? 1 : 0;

@@ -54,6 +54,7 @@ struct FwdArgs {
     int halo_rows;               // halo kernel: output rows per tile (1-4); the box holds halo_rows + 2 rows
     int halo_box_bytes;          // halo kernel: bytes of one 8-channel plane as TMA writes it
     int halo_plane_bytes;        // halo kernel: plane stride (1 KiB-aligned TMA destinations)
+    int wide_io;                 // BF16 output / mask rows 32-byte aligned: 256-bit accesses in the epilogue
 };
 
 struct WgradArgs {
