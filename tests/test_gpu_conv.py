@@ -128,6 +128,27 @@ def test_conv_backward_weights(cuda_ctx, shape):
     assert _rel_l2(db, br.grad) <= 1e-4
 
 
+@pytest.mark.parametrize("shape", [(4, 64, 64, 16, 32), (2, 8, 256, 32, 48), (2, 16, 64, 80, 32)])
+def test_conv_backward_weights_repeatable(cuda_ctx, shape):
+    """Repeated weight gradients (and the bias gradient taken from the same
+    MMAs) differ only by the order of the FP32 atomic sums: no stage is read
+    before its copies landed or after the next tile's copies overwrote it."""
+    from pupiloptixlab_gb300 import denoiser as dnm
+    n, h, w, cin, cout = shape
+    g = torch.Generator().manual_seed(31 + cin)
+    x = _bf16((n, h, w, cin), g).cuda()
+    dy = _bf16((n, h, w, cout), g).cuda()
+    outs = []
+    for _ in range(6):
+        dw, db = dnm.conv3x3_backward_weights(x, dy)
+        outs.append((dw.cpu(), db.cpu()))
+    scale_w = float(outs[0][0].abs().max())
+    scale_b = float(outs[0][1].abs().max())
+    for dw, db in outs[1:]:
+        assert float((dw - outs[0][0]).abs().max()) <= 1e-5 * scale_w
+        assert float((db - outs[0][1]).abs().max()) <= 1e-5 * scale_b
+
+
 @pytest.mark.parametrize("shape", [(2, 16, 16, 16, 32), (1, 8, 256, 128, 256)], ids=["ring", "halo_resident"])
 def test_bounded_wait_runs_out_and_the_next_convolution_is_right(cuda_ctx, shape):
     """The timeout path of the forward kernel, without a fault: with a 1 ms
