@@ -210,9 +210,23 @@ __device__ __forceinline__ void fwd_epilogue(const FwdArgs &a, uint32_t tmem, in
             continue;
         }
         if (a.epi == EPI_BF16) {
+            float b[16];
+            if (a.bias && nvalid == 16 && a.bias16) {  // 16 biases in four 16-byte loads
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    const float4 q = __ldg(reinterpret_cast<const float4 *>(a.bias + ch0) + i);
+                    b[4 * i] = q.x;
+                    b[4 * i + 1] = q.y;
+                    b[4 * i + 2] = q.z;
+                    b[4 * i + 3] = q.w;
+                }
+            } else {
+#pragma unroll
+                for (int i = 0; i < 16; i++) b[i] = (a.bias && i < nvalid) ? a.bias[ch0 + i] : 0.f;
+            }
 #pragma unroll
             for (int i = 0; i < 16; i++) {
-                float f = v[i] + ((a.bias && i < nvalid) ? a.bias[ch0 + i] : 0.f);
+                const float f = v[i] + b[i];
                 v[i] = a.relu ? fmaxf(f, 0.f) : f;
             }
         } else {
@@ -263,20 +277,23 @@ __device__ __forceinline__ void fwd_epilogue(const FwdArgs &a, uint32_t tmem, in
 // ---------------------------------------------------------------------------
 // The pixel tile is a 128-pixel row segment.  Per 16-channel chunk one TMA box
 // brings its 3 x 130-pixel neighbourhood (the segment and a one-pixel border,
-// zero outside the image) into the non-swizzled K-major layout: two planes of
-// 8 channels, 16 bytes per pixel, pixels in row-major order.  The A operand of
-// tap (dy, dx) is the same planes read from row dy * 130 + dx on (leading
-// byte offset = plane size between the two 8-channel groups, stride byte
-// offset = 128 B between 8-row groups), so the input is read from L2 once per
-// chunk instead of once per tap.  B holds the chunk's weights for all nine
+// zero outside the image) as 32-byte pixel rows in the 32-byte-swizzled
+// K-major layout, pixels in row-major order.  The A operand of tap (dy, dx) is
+// the same box read from pixel row dy * 130 + dx on (stride byte offset =
+// 256 B between 8-row groups): the tensor cores apply the swizzle to the
+// absolute shared-memory address, as the TMA wrote it, so a start at any
+// 32-byte row reads the right data.  The input is thus read from L2 once per
+// chunk instead of once per tap.  (PT_CONV_HALO_PLANES=1 selects the earlier
+// layout: two TMA boxes per chunk into non-swizzled planes of 8 channels,
+// 16 bytes per pixel, leading byte offset = plane size.)  B holds the chunk's weights for all nine
 // taps (32-byte swizzle, one TMA box per tap).  When one channel tile covers
 // every output channel and all (chunk, tap) weight boxes fit in
 // kMaxResidentWeights bytes, they are loaded once per CTA ahead of the ring
-// (on their own barrier) and the stages carry only the two A planes.
+// (on their own barrier) and the stages carry only the A box.
 // A tile may cover two output rows (halo_rows = 2: a 4-row box, two M = 128
 // accumulators sharing each B operand), so that every input row crosses L2
 // twice per pass instead of three times; the second row's A operand is the
-// same planes read one box row (130 pixels) further on.
+// same box read one box row (130 pixels) further on.
 constexpr int kHaloW = 130;
 __host__ __device__ constexpr int halo_box_bytes(int rows) { return kHaloW * (rows + 2) * 16; }
 __host__ __device__ constexpr int halo_plane_bytes(int rows) { return (halo_box_bytes(rows) + 1023) / 1024 * 1024; }
@@ -317,7 +334,7 @@ __global__ void __launch_bounds__(192, 1)
     const int a_bytes = HALO ? a.halo_a_bytes : 128 * R;
     const int b_tap = HALO ? halo_b_tap_bytes(a.n_tile) : 0;
     const int hrows = HALO ? a.halo_rows : 1;  // output rows (accumulators) per tile
-    const uint32_t tx_bytes = HALO ? static_cast<uint32_t>(2 * a.halo_box_bytes + (wres ? 0 : 9 * a.n_tile * R))
+    const uint32_t tx_bytes = HALO ? static_cast<uint32_t>(a.halo_a_tx + (wres ? 0 : 9 * a.n_tile * R))
                                    : static_cast<uint32_t>(a.tile_w * a.tile_rows * R + a.n_tile * R);
     const uint32_t bar0 = smem_u32(bars);
     auto full = [&](int s) { return bar0 + 8u * s; };
@@ -382,8 +399,12 @@ __global__ void __launch_bounds__(192, 1)
                     const uint32_t sa = base + s * a.stage_bytes, sb = sa + a_bytes;
                     mbar_expect_tx(full(s), tx_bytes);
                     if (HALO) {
-                        tma_load_4d(sa, &act, full(s), k * 16, x0 - 1, y0 - 1, img);
-                        tma_load_4d(sa + a.halo_plane_bytes, &act, full(s), k * 16 + 8, x0 - 1, y0 - 1, img);
+                        if (a.halo_sw32) {
+                            tma_load_4d(sa, &act, full(s), k * 16, x0 - 1, y0 - 1, img);
+                        } else {
+                            tma_load_4d(sa, &act, full(s), k * 16, x0 - 1, y0 - 1, img);
+                            tma_load_4d(sa + a.halo_plane_bytes, &act, full(s), k * 16 + 8, x0 - 1, y0 - 1, img);
+                        }
                         if (!wres)
                             for (int tap = 0; tap < 9; tap++)
                                 tma_load_2d(sb + tap * b_tap, &wgt, full(s), tap * a.cin + k * 16, n0);
@@ -439,8 +460,13 @@ __global__ void __launch_bounds__(192, 1)
                             const int dy = tap / 3, dx = tap - 3 * (tap / 3);
                             const uint64_t db = sdesc(sb + tap * b_tap, 16u, 8u * R, SWZ);
                             for (int r = 0; r < hrows; r++) {
-                                const uint64_t da = sdesc(sa + 16u * ((dy + r) * kHaloW + dx),
-                                                          static_cast<uint32_t>(a.halo_plane_bytes), 128u, 0u);
+                                uint64_t da;
+                                if (a.halo_sw32) {  // 32-byte rows, 32-byte swizzle, 8-row groups 256 B apart
+                                    da = sdesc(sa + 32u * ((dy + r) * kHaloW + dx), 16u, 256u, 6u);
+                                } else {
+                                    da = sdesc(sa + 16u * ((dy + r) * kHaloW + dx),
+                                               static_cast<uint32_t>(a.halo_plane_bytes), 128u, 0u);
+                                }
                                 umma_bf16(d + static_cast<uint32_t>(r * a.n_tile), da, db, idesc,
                                           (k | tap) != 0 ? 1u : 0u);
                             }
@@ -861,7 +887,12 @@ int fwd_prepare(FwdOp *op, const Act &in, const void *w, int w_rows, int cout, c
     while (halo_rows > 1 && pow2_cols(2 * halo_rows * n_tile) > 512) halo_rows--;
     int st;
     if (halo) {
-        if ((st = act_map_box(&op->act, in, 8, kHaloW, halo_rows + 2, CU_TENSOR_MAP_SWIZZLE_NONE, 8)) != PT_OK) return st;
+        if (!getenv_flag("PT_CONV_HALO_PLANES")) {
+            if ((st = act_map_box(&op->act, in, 16, kHaloW, halo_rows + 2, CU_TENSOR_MAP_SWIZZLE_32B, 16)) != PT_OK)
+                return st;
+        } else if ((st = act_map_box(&op->act, in, 8, kHaloW, halo_rows + 2, CU_TENSOR_MAP_SWIZZLE_NONE, 8)) != PT_OK) {
+            return st;
+        }
     } else if ((st = act_map(&op->act, in, kc, t)) != PT_OK) {
         return st;
     }
@@ -884,7 +915,9 @@ int fwd_prepare(FwdOp *op, const Act &in, const void *w, int w_rows, int cout, c
     a.halo_rows = halo_rows;
     a.halo_box_bytes = halo_box_bytes(halo_rows);
     a.halo_plane_bytes = halo_plane_bytes(halo_rows);
-    a.halo_a_bytes = 2 * a.halo_plane_bytes;
+    a.halo_sw32 = halo && !getenv_flag("PT_CONV_HALO_PLANES");
+    a.halo_a_tx = a.halo_sw32 ? 2 * halo_box_bytes(halo_rows) : 2 * a.halo_box_bytes;
+    a.halo_a_bytes = a.halo_sw32 ? (a.halo_a_tx + 1023) / 1024 * 1024 : 2 * a.halo_plane_bytes;
     const int wres_bytes = a.nchunks * 9 * halo_b_tap_bytes(n_tile);
     a.wres_bytes = (halo && ntiles == 1 && wres_bytes <= kMaxResidentWeights && !getenv_flag("PT_CONV_NO_RESIDENT"))
                        ? wres_bytes : 0;
@@ -915,6 +948,7 @@ int fwd_prepare(FwdOp *op, const Act &in, const void *w, int w_rows, int cout, c
     auto al32 = [](const void *ptr, int ctot, int coff) {
         return (reinterpret_cast<uintptr_t>(ptr) % 32) == 0 && ctot % 16 == 0 && coff % 16 == 0;
     };
+    a.bias16 = bias && (reinterpret_cast<uintptr_t>(bias) % 16) == 0 ? 1 : 0;
     a.wide_io = epi != EPI_F32 && al32(out, out_ctot, out_coff) &&
                 (!mask || al32(mask->ptr, mask->ctot, mask->coff)) && !getenv_flag("PT_CONV_NO_WIDE_IO");
     a.err = err;

@@ -55,6 +55,9 @@ struct FwdArgs {
     int halo_box_bytes;          // halo kernel: bytes of one 8-channel plane as TMA writes it
     int halo_plane_bytes;        // halo kernel: plane stride (1 KiB-aligned TMA destinations)
     int wide_io;                 // BF16 output / mask rows 32-byte aligned: 256-bit accesses in the epilogue
+    int halo_sw32;               // halo kernel: one 16-channel box per chunk, 32-byte swizzle (else two planes)
+    int halo_a_tx;               // halo kernel: bytes of A the TMA delivers per stage
+    int bias16;                  // bias 16-byte aligned: the epilogue reads it in 16-byte loads
 };
 
 struct WgradArgs {
