@@ -28,6 +28,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -447,6 +448,11 @@ struct pt_denoiser {
     Plan train_plan, infer_plan;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev_in = nullptr, ev_out = nullptr, t0 = nullptr, t1 = nullptr;
+    // weight gradients on side streams, taken in turn (forked per layer once
+    // its output gradient exists, joined before Adam), beside the
+    // data-gradient chain
+    cudaStream_t side[2] = {};
+    cudaEvent_t ev_fork[kLayers] = {}, ev_join[2] = {};
     pt_denoise_stats stats{};
 };
 
@@ -619,9 +625,19 @@ int run_backward(pt_denoiser *dn, Plan &P, const float *target, cudaStream_t s) 
     PT_CUDA_TRY(cudaMemsetAsync(dn->grads.ptr, 0, dn->nparams * sizeof(float), s));
     k_loss<<<grid_for(npix), 256, 0, s>>>(P.out.as<float>(), P.x0.as<uint16_t>(), target, npix, 1.f / (3.f * npix),
                                           P.g_out.as<uint16_t>(), dn->loss.as<float>());
+    // layer l: its weight (and bias) gradient and its data gradient both read
+    // only the layer's output gradient, so the weight gradient runs on the
+    // side stream while the data gradients continue on s
+    const int nside = dn->side[1] ? 2 : dn->side[0] ? 1 : 0;
+    int turn = 0;
     auto layer = [&](int l) -> int {
-        PT_TRY(ptconv::wgrad_launch(P.wg[l], s));
-        if (!P.wg[l].bias_fused) PT_TRY(ptconv::bias_grad_launch(P.g_of[l], dn->grads.as<float>() + dn->b_off[l], s));
+        cudaStream_t ws = nside ? dn->side[turn++ % nside] : s;
+        if (nside) {
+            PT_CUDA_TRY(cudaEventRecord(dn->ev_fork[l], s));
+            PT_CUDA_TRY(cudaStreamWaitEvent(ws, dn->ev_fork[l], 0));
+        }
+        PT_TRY(ptconv::wgrad_launch(P.wg[l], ws));
+        if (!P.wg[l].bias_fused) PT_TRY(ptconv::bias_grad_launch(P.g_of[l], dn->grads.as<float>() + dn->b_off[l], ws));
         if (l != E0A) PT_TRY(ptconv::fwd_launch(P.bwd[l], s));
         return PT_OK;
     };
@@ -660,6 +676,10 @@ int run_backward(pt_denoiser *dn, Plan &P, const float *target, cudaStream_t s) 
     skip_back(P.cat0, P.g_cat0, 80, 48, P.g_p0, 32, 0, P.g_e0b);
     PT_TRY(layer(E0B));
     PT_TRY(layer(E0A));
+    for (int i = 0; i < nside; i++) {
+        PT_CUDA_TRY(cudaEventRecord(dn->ev_join[i], dn->side[i]));
+        PT_CUDA_TRY(cudaStreamWaitEvent(s, dn->ev_join[i], 0));
+    }
     PT_CUDA_TRY(cudaGetLastError());
     return PT_OK;
 }
@@ -810,6 +830,19 @@ int pt_denoiser_create(pt_context *ctx, const pt_denoiser_opts *opts, pt_denoise
         pt_set_error("pt_denoiser_create: CUDA set-up failed");
         return fail(PT_ERR_CUDA);
     }
+    if (!getenv("PT_DENOISER_ONE_STREAM")) {  // the side stream for weight gradients
+        const int nside = 1;  // a second side stream measured no faster (2.333 vs 2.332 ms per step)
+        bool ok = true;
+        for (int i = 0; ok && i < nside; i++)
+            ok = cudaStreamCreateWithFlags(&dn->side[i], cudaStreamNonBlocking) == cudaSuccess &&
+                 cudaEventCreateWithFlags(&dn->ev_join[i], cudaEventDisableTiming) == cudaSuccess;
+        for (int l = 0; ok && l < kLayers; l++)
+            ok = cudaEventCreateWithFlags(&dn->ev_fork[l], cudaEventDisableTiming) == cudaSuccess;
+        if (!ok) {
+            pt_set_error("pt_denoiser_create: CUDA set-up failed");
+            return fail(PT_ERR_CUDA);
+        }
+    }
     std::vector<float> p;
     init_params(dn, p);
     if ((st = upload_params(dn, p.data())) != PT_OK) return fail(st);
@@ -830,6 +863,15 @@ void pt_denoiser_destroy(pt_denoiser *dn) {
     if (dn->ev_out) cudaEventDestroy(dn->ev_out);
     if (dn->t0) cudaEventDestroy(dn->t0);
     if (dn->t1) cudaEventDestroy(dn->t1);
+    for (cudaEvent_t e : dn->ev_fork)
+        if (e) cudaEventDestroy(e);
+    for (int i = 0; i < 2; i++) {
+        if (dn->ev_join[i]) cudaEventDestroy(dn->ev_join[i]);
+        if (dn->side[i]) {
+            cudaStreamSynchronize(dn->side[i]);
+            cudaStreamDestroy(dn->side[i]);
+        }
+    }
     if (dn->stream) cudaStreamDestroy(dn->stream);
     delete dn;
 }
