@@ -251,6 +251,9 @@ __device__ __forceinline__ void fwd_epilogue(const FwdArgs &a, uint32_t tmem, in
             }
         }
         uint16_t *o = static_cast<uint16_t *>(a.out) + pix * a.out_ctot + a.out_coff + ch0;
+        // the four up-sampled copies (pixel (2y + i, 2x + j) of the 2H x 2W tensor)
+        uint16_t *u = a.up ? a.up + (((size_t)img * 2 * a.H + 2 * y) * 2 * a.W + 2 * x) * a.up_ctot + ch0 : nullptr;
+        const size_t urow = static_cast<size_t>(2 * a.W) * a.up_ctot;
         if (nvalid == 16) {
             uint4 q0, q1;
             uint32_t *w0 = reinterpret_cast<uint32_t *>(&q0), *w1 = reinterpret_cast<uint32_t *>(&q1);
@@ -261,15 +264,102 @@ __device__ __forceinline__ void fwd_epilogue(const FwdArgs &a, uint32_t tmem, in
             }
             if (a.wide_io) {
                 st_global_v8(o, q0, q1);
+                if (u) {
+                    st_global_v8(u, q0, q1);
+                    st_global_v8(u + a.up_ctot, q0, q1);
+                    st_global_v8(u + urow, q0, q1);
+                    st_global_v8(u + urow + a.up_ctot, q0, q1);
+                }
             } else {
                 reinterpret_cast<uint4 *>(o)[0] = q0;
                 reinterpret_cast<uint4 *>(o)[1] = q1;
+                for (int k = 0; u && k < 4; k++) {
+                    uint16_t *uk = u + (k >> 1) * urow + (k & 1) * a.up_ctot;
+                    reinterpret_cast<uint4 *>(uk)[0] = q0;
+                    reinterpret_cast<uint4 *>(uk)[1] = q1;
+                }
             }
         } else {
-            for (int i = 0; i < nvalid; i++) o[i] = f2bf(v[i]);
+            for (int i = 0; i < nvalid; i++) {
+                const uint16_t b = f2bf(v[i]);
+                o[i] = b;
+                for (int k = 0; u && k < 4; k++) u[(k >> 1) * urow + (k & 1) * a.up_ctot + i] = b;
+            }
         }
     }
 
+}
+
+// Two-row halo tile with the pooled output (EPI_BF16, cout a multiple of 16,
+// 32-byte aligned rows): thread `tid` holds pixel x = x0 + tid of rows y0 and
+// y0 + 1 (accumulators tmem and tmem + n_tile), its neighbour lane x ^ 1.
+// Each row is written as fwd_epilogue writes it; the even lane of each pair
+// writes the average of the four BF16 outputs, summed in the order
+// (y0, x), (y0, x + 1), (y0 + 1, x), (y0 + 1, x + 1).
+__device__ __forceinline__ void fwd_epilogue_pool2(const FwdArgs &a, uint32_t tmem, int tid, int warp, int img, int x0,
+                                                   int y0, int n0) {
+    const int x = x0 + tid;
+    const bool valid = x < a.W && y0 < a.H;
+    const size_t pix0 = ((size_t)img * a.H + (valid ? y0 : 0)) * a.W + (valid ? x : 0);
+    const size_t ppix = ((size_t)img * (a.H / 2) + (valid ? y0 / 2 : 0)) * (a.W / 2) + (valid ? x / 2 : 0);
+    const uint32_t trow = tmem + (static_cast<uint32_t>(warp * 32) << 16);
+    for (int c = 0; c < a.n_tile; c += 16) {
+        float v[2][16];
+        tmem_ld16(trow + c, v[0]);
+        tmem_ld16(trow + a.n_tile + c, v[1]);
+        const int ch0 = n0 + c;
+        if (ch0 >= a.cout) continue;  // uniform across the warp
+        float b[16];
+        if (a.bias && a.bias16) {
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const float4 q = __ldg(reinterpret_cast<const float4 *>(a.bias + ch0) + i);
+                b[4 * i] = q.x;
+                b[4 * i + 1] = q.y;
+                b[4 * i + 2] = q.z;
+                b[4 * i + 3] = q.w;
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < 16; i++) b[i] = a.bias ? a.bias[ch0 + i] : 0.f;
+        }
+        uint32_t w[2][8];
+#pragma unroll
+        for (int r = 0; r < 2; r++)
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                float f0 = v[r][2 * i] + b[2 * i], f1 = v[r][2 * i + 1] + b[2 * i + 1];
+                if (a.relu) {
+                    f0 = fmaxf(f0, 0.f);
+                    f1 = fmaxf(f1, 0.f);
+                }
+                w[r][i] = f2bf(f0) | (static_cast<uint32_t>(f2bf(f1)) << 16);
+            }
+        uint32_t pw[8];
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            float acc[2];
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const float own0 = __uint_as_float((w[0][i] >> (16 * h)) << 16);
+                const float own1 = __uint_as_float((w[1][i] >> (16 * h)) << 16);
+                const float nb0 = __shfl_xor_sync(0xffffffffu, own0, 1);
+                const float nb1 = __shfl_xor_sync(0xffffffffu, own1, 1);
+                acc[h] = 0.25f * ((((0.f + own0) + nb0) + own1) + nb1);  // k_pool's order, from 0
+            }
+            pw[i] = f2bf(acc[0]) | (static_cast<uint32_t>(f2bf(acc[1])) << 16);
+        }
+        if (!valid) continue;
+#pragma unroll
+        for (int r = 0; r < 2; r++) {
+            uint16_t *o = static_cast<uint16_t *>(a.out) + (pix0 + (size_t)r * a.W) * a.out_ctot + a.out_coff + ch0;
+            st_global_v8(o, make_uint4(w[r][0], w[r][1], w[r][2], w[r][3]), make_uint4(w[r][4], w[r][5], w[r][6], w[r][7]));
+        }
+        if ((tid & 1) == 0) {
+            uint16_t *o = a.pool + ppix * a.pool_ctot + a.pool_coff + ch0;
+            st_global_v8(o, make_uint4(pw[0], pw[1], pw[2], pw[3]), make_uint4(pw[4], pw[5], pw[6], pw[7]));
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -503,9 +593,12 @@ __global__ void __launch_bounds__(192, 1)
             tc_fence_after();
             int img, x0, y0, n0;
             tile_of(t, img, x0, y0, n0);
-            for (int r = 0; r < hrows; r++)
-                fwd_epilogue(a, tmem + static_cast<uint32_t>((buf * hrows + r) * a.n_tile), row, quad, img, x0, y0 + r,
-                             n0, true);
+            if (HALO && a.pool)
+                fwd_epilogue_pool2(a, tmem + static_cast<uint32_t>(buf * 2 * a.n_tile), row, quad, img, x0, y0, n0);
+            else
+                for (int r = 0; r < hrows; r++)
+                    fwd_epilogue(a, tmem + static_cast<uint32_t>((buf * hrows + r) * a.n_tile), row, quad, img, x0,
+                                 y0 + r, n0, true);
             tc_fence_before();
             mbar_arrive(acc_empty(buf));
         }
@@ -859,7 +952,8 @@ void set_wait_limit(unsigned long long ns, bool stall_next) {
 }
 
 int fwd_prepare(FwdOp *op, const Act &in, const void *w, int w_rows, int cout, const float *bias, int epi, int relu,
-                void *out, int out_ctot, int out_coff, const Act *mask, unsigned *err) {
+                void *out, int out_ctot, int out_coff, const Act *mask, unsigned *err, void *up, int up_ctot,
+                void *pool, int pool_ctot, int pool_coff) {
     if (in.c <= 0 || in.c % 16 || cout <= 0 || in.n <= 0 || in.h <= 0 || in.w <= 0) {
         pt_set_error("conv forward: channel counts must be positive multiples of 16 (cin %d, cout %d)", in.c, cout);
         return PT_ERR_INVALID;
@@ -949,8 +1043,26 @@ int fwd_prepare(FwdOp *op, const Act &in, const void *w, int w_rows, int cout, c
         return (reinterpret_cast<uintptr_t>(ptr) % 32) == 0 && ctot % 16 == 0 && coff % 16 == 0;
     };
     a.bias16 = bias && (reinterpret_cast<uintptr_t>(bias) % 16) == 0 ? 1 : 0;
+    if (up && epi == EPI_BF16) {
+        if (up_ctot < cout || up_ctot % 8) {
+            pt_set_error("conv forward: up-sampled output needs at least cout channels, a multiple of 8");
+            return PT_ERR_INVALID;
+        }
+        a.up = static_cast<uint16_t *>(up);
+        a.up_ctot = up_ctot;
+    }
+    // the 2x2 average pooling of the output, in the epilogue of two-row halo
+    // tiles (both rows of a pixel pair are in one thread, the pair in
+    // neighbouring lanes); otherwise the caller pools
+    if (pool && halo && halo_rows == 2 && epi == EPI_BF16 && cout % 16 == 0 && in.w % 128 == 0 && in.h % 2 == 0 &&
+        ntiles == 1 && al32(pool, pool_ctot, pool_coff) && !getenv_flag("PT_CONV_NO_FUSED_POOL")) {
+        a.pool = static_cast<uint16_t *>(pool);
+        a.pool_ctot = pool_ctot;
+        a.pool_coff = pool_coff;
+    }
     a.wide_io = epi != EPI_F32 && al32(out, out_ctot, out_coff) &&
-                (!mask || al32(mask->ptr, mask->ctot, mask->coff)) && !getenv_flag("PT_CONV_NO_WIDE_IO");
+                (!mask || al32(mask->ptr, mask->ctot, mask->coff)) && (!a.up || al32(a.up, a.up_ctot, 0)) &&
+                !getenv_flag("PT_CONV_NO_WIDE_IO");
     a.err = err;
     a.wait_ns = wait_limit_ns();
     a.stall = take_stall_request() ? 1 : 0;

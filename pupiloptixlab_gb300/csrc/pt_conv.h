@@ -58,6 +58,10 @@ struct FwdArgs {
     int halo_sw32;               // halo kernel: one 16-channel box per chunk, 32-byte swizzle (else two planes)
     int halo_a_tx;               // halo kernel: bytes of A the TMA delivers per stage
     int bias16;                  // bias 16-byte aligned: the epilogue reads it in 16-byte loads
+    uint16_t *up;                // EPI_BF16: also written, 2x nearest up-sampled, to channels [0, cout) of
+    int up_ctot;                 // this (n, 2H, 2W, up_ctot) tensor (the decoder's concatenation)
+    uint16_t *pool;              // halo kernel, two-row tiles, EPI_BF16: the 2x2 average of the BF16 outputs
+    int pool_ctot, pool_coff;    // also goes to this (n, H/2, W/2, pool_ctot) tensor at channel pool_coff
 };
 
 struct WgradArgs {
@@ -111,7 +115,10 @@ bool take_stall_request();
 // (out_ctot channels, same n/h/w as `in`).  `mask` (EPI_BF16_MASK) is a tensor
 // of the output's shape.
 int fwd_prepare(FwdOp *op, const Act &in, const void *w, int w_rows, int cout, const float *bias, int epi,
-                int relu, void *out, int out_ctot, int out_coff, const Act *mask, unsigned *err);
+                int relu, void *out, int out_ctot, int out_coff, const Act *mask, unsigned *err, void *up = nullptr,
+                int up_ctot = 0, void *pool = nullptr, int pool_ctot = 0, int pool_coff = 0);
+// Whether the forward launch prepared in op also wrote the 2x2-pooled output.
+inline bool fwd_pooled(const FwdOp &op) { return op.args.pool != nullptr; }
 int fwd_launch(const FwdOp &op, cudaStream_t stream);
 
 // dw[co][tap][ci] += sum over pixels of x[p + off(tap), ci] * gy[p, co].

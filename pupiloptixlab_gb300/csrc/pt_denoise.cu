@@ -146,7 +146,8 @@ __global__ void k_pool(const uint16_t *src, int sctot, int scoff, int c, int n, 
     }
 }
 
-// cat[n, y, x, 0:c] = lo[n, y/2, x/2, 0:c]
+// cat[n, y, x, 0:c] = lo[n, y/2, x/2, 0:c] (when the producing convolution's
+// epilogue does not write the up-sampled copy itself)
 __global__ void k_upcat(const uint16_t *lo, int c, int n, int h, int w, uint16_t *cat, int cat_ctot) {
     const int groups = c / 8;
     const long long total = (long long)n * h * w * groups;
@@ -422,6 +423,7 @@ struct Plan {
     ptconv::WgradOp wg[kLayers];
     Act x_of[kLayers], g_of[kLayers];
     cudaGraphExec_t graph = nullptr;
+    bool fused_up = true;  // the decoder convolutions write the up-sampled copies themselves
 
     void release() {
         DevBuf *all[] = {&x0,    &a0,    &cat0,   &p0,    &a1,    &cat1,   &p1,    &a2,    &cat2,  &p2,
@@ -509,23 +511,34 @@ int plan_prepare(pt_denoiser *dn, Plan &P, int n, int h, int w, bool train) {
         Act in;
         const DevBuf *out;
         int lvl, octot, ocoff;
+        DevBuf *up = nullptr;  // decoder: the 2x up-sampled copy goes to channels [0, cout) of this concatenation
+        int up_ctot = 0;
+        DevBuf *pool = nullptr;  // encoder: the 2x2 average (the next level's input), when the kernel can fuse it
     };
     const Io io[kLayers] = {
-        {A(P.x0, 0, 16, 0, 16), &P.a0, 0, 32, 0},         {A(P.a0, 0, 32, 0, 32), &P.cat0, 0, 80, 48},
-        {A(P.p0, 1, 32, 0, 32), &P.a1, 1, 48, 0},         {A(P.a1, 1, 48, 0, 48), &P.cat1, 1, 112, 64},
+        {A(P.x0, 0, 16, 0, 16), &P.a0, 0, 32, 0},
+        {A(P.a0, 0, 32, 0, 32), &P.cat0, 0, 80, 48, nullptr, 0, &P.p0},
+        {A(P.p0, 1, 32, 0, 32), &P.a1, 1, 48, 0},
+        {A(P.a1, 1, 48, 0, 48), &P.cat1, 1, 112, 64, nullptr, 0, &P.p1},
         {A(P.p1, 2, 48, 0, 48), &P.a2, 2, 64, 0},         {A(P.a2, 2, 64, 0, 64), &P.cat2, 2, 192, 128},
         {A(P.p2, 3, 64, 0, 64), &P.a3, 3, 128, 0},        {A(P.a3, 3, 128, 0, 128), &P.cat3, 3, 384, 256},
-        {A(P.p3, 4, 128, 0, 128), &P.b4, 4, 256, 0},      {A(P.cat3, 3, 384, 0, 384), &P.d3, 3, 128, 0},
-        {A(P.cat2, 2, 192, 0, 192), &P.d2, 2, 64, 0},     {A(P.cat1, 1, 112, 0, 112), &P.d1, 1, 48, 0},
+        {A(P.p3, 4, 128, 0, 128), &P.b4, 4, 256, 0, &P.cat3, 384},
+        {A(P.cat3, 3, 384, 0, 384), &P.d3, 3, 128, 0, &P.cat2, 192},
+        {A(P.cat2, 2, 192, 0, 192), &P.d2, 2, 64, 0, &P.cat1, 112},
+        {A(P.cat1, 1, 112, 0, 112), &P.d1, 1, 48, 0, &P.cat0, 80},
         {A(P.cat0, 0, 80, 0, 80), &P.d0, 0, 32, 0},       {A(P.d0, 0, 32, 0, 32), &P.out, 0, 3, 0},
     };
     unsigned *err = dn->err.as<unsigned>();
+    const bool separate_up = getenv("PT_DENOISER_SEPARATE_UPSAMPLE") != nullptr;
+    P.fused_up = !separate_up;
     for (int l = 0; l < kLayers; l++) {
         const LayerSpec &L = kSpec[l];
         const bool last = l == OUT;
         if ((st = ptconv::fwd_prepare(&P.fwd[l], io[l].in, wbf_ptr(dn, l), L.cout, last ? kOutChannels : L.cout,
                                       bias_ptr(dn, l), last ? ptconv::EPI_F32 : ptconv::EPI_BF16, L.relu,
-                                      io[l].out->ptr, io[l].octot, io[l].ocoff, nullptr, err)) != PT_OK)
+                                      io[l].out->ptr, io[l].octot, io[l].ocoff, nullptr, err,
+                                      io[l].up && !separate_up ? io[l].up->ptr : nullptr, io[l].up_ctot,
+                                      io[l].pool ? io[l].pool->ptr : nullptr, L.cout, 0)) != PT_OK)
             return st;
         P.x_of[l] = io[l].in;
     }
@@ -587,23 +600,24 @@ int run_forward(pt_denoiser *dn, Plan &P, cudaStream_t s) {
         const long long tot = (long long)n * h2 * w2 * (c / 8);
         k_pool<<<grid_for(tot), 256, 0, s>>>(src.as<uint16_t>(), sctot, scoff, c, n, h2, w2, dst.as<uint16_t>());
     };
-    auto up = [&](const DevBuf &lo, int c, int lvl, DevBuf &cat, int cat_ctot) {
-        const int hh = h >> lvl, ww = w >> lvl;
-        const long long tot = (long long)n * hh * ww * (c / 8);
-        k_upcat<<<grid_for(tot), 256, 0, s>>>(lo.as<uint16_t>(), c, n, hh, ww, cat.as<uint16_t>(), cat_ctot);
-    };
     PT_TRY(ptconv::fwd_launch(P.fwd[E0A], s));
     PT_TRY(ptconv::fwd_launch(P.fwd[E0B], s));
-    pool(P.cat0, 80, 48, 32, 0, P.p0);
+    if (!ptconv::fwd_pooled(P.fwd[E0B])) pool(P.cat0, 80, 48, 32, 0, P.p0);
     PT_TRY(ptconv::fwd_launch(P.fwd[E1A], s));
     PT_TRY(ptconv::fwd_launch(P.fwd[E1B], s));
-    pool(P.cat1, 112, 64, 48, 1, P.p1);
+    if (!ptconv::fwd_pooled(P.fwd[E1B])) pool(P.cat1, 112, 64, 48, 1, P.p1);
     PT_TRY(ptconv::fwd_launch(P.fwd[E2A], s));
     PT_TRY(ptconv::fwd_launch(P.fwd[E2B], s));
     pool(P.cat2, 192, 128, 64, 2, P.p2);
     PT_TRY(ptconv::fwd_launch(P.fwd[E3A], s));
     PT_TRY(ptconv::fwd_launch(P.fwd[E3B], s));
     pool(P.cat3, 384, 256, 128, 3, P.p3);
+    auto up = [&](const DevBuf &lo, int c, int lvl, DevBuf &cat, int cat_ctot) {
+        if (P.fused_up) return;
+        const int hh = h >> lvl, ww = w >> lvl;
+        const long long tot = (long long)n * hh * ww * (c / 8);
+        k_upcat<<<grid_for(tot), 256, 0, s>>>(lo.as<uint16_t>(), c, n, hh, ww, cat.as<uint16_t>(), cat_ctot);
+    };
     PT_TRY(ptconv::fwd_launch(P.fwd[BOT], s));
     up(P.b4, 256, 3, P.cat3, 384);
     PT_TRY(ptconv::fwd_launch(P.fwd[D3], s));

@@ -63,6 +63,27 @@ def test_forward_matches_cpu(dn):
     assert _rel(out, ref) <= 2e-2
 
 
+def test_wide_frame_with_fused_pooling_and_upsampling(cuda_ctx, dn, monkeypatch):
+    """Frames at least 256 wide: the first two encoder levels pool in the
+    convolution epilogue (two-row halo tiles) and every decoder level writes
+    its up-sampled copy there too.  The output equals the one with separate
+    pooling and up-sampling kernels bit for bit, and matches the CPU
+    restatement."""
+    from oracle import denoiser_ref
+    from pupiloptixlab_gb300.denoiser import Denoiser
+    inp, _ = _batch(1, 48, 256, 5)
+    fused = dn.forward(inp.cuda()).cpu()
+    monkeypatch.setenv("PT_CONV_NO_FUSED_POOL", "1")
+    monkeypatch.setenv("PT_DENOISER_SEPARATE_UPSAMPLE", "1")
+    d2 = Denoiser(cuda_ctx, seed=3)
+    d2.set_params(dn.get_params())
+    separate = d2.forward(inp.cuda()).cpu()
+    d2.close()
+    assert torch.equal(fused, separate)
+    ref = denoiser_ref.denoise(dn.get_params(), inp.float().numpy())
+    assert _rel(fused.numpy(), ref) <= 2e-2
+
+
 def test_gradients_match_cpu(dn):
     from oracle import denoiser_ref
     inp, tgt = _batch(2, 32, 32, 2)
