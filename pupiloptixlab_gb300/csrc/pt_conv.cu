@@ -1017,7 +1017,11 @@ int fwd_prepare(FwdOp *op, const Act &in, const void *w, int w_rows, int cout, c
                        ? wres_bytes : 0;
     a.stage_bytes = halo ? a.halo_a_bytes + (a.wres_bytes ? 0 : 9 * halo_b_tap_bytes(n_tile))
                          : (128 * 2 * kc + n_tile * 2 * kc + 1023) / 1024 * 1024;
-    const int target_ctas = std::min(512 / a.tmem_cols, 2);
+    // CTAs per SM the ring is sized for (PT_CONV_FWD_CTAS=1..4 overrides):
+    // training step at batch 16 x 256^2 2.308 / 2.251 / 2.298 ms for 2 / 3 / 4
+    int max_ctas = 3;
+    if (const char *e = getenv("PT_CONV_FWD_CTAS")) max_ctas = std::min(std::max(atoi(e), 1), 4);
+    const int target_ctas = std::min(512 / a.tmem_cols, max_ctas);
     const int budget = (225 * 1024) / target_ctas - 2048 - a.wres_bytes;
     a.stages = std::max(2, std::min(kMaxStages, budget / a.stage_bytes));
     if (halo) {
