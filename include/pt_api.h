@@ -251,7 +251,9 @@ typedef struct pt_device_opts {
  * radix tree, which traces them faster.  Leaves are chosen by SAH with curve
  * pieces weighted as three triangle tests.  max_leaf_size: primitives per
  * leaf (1..15).  smem_nodes: number
- * of top nodes staged in shared memory by the traversal kernels (0 = none). */
+ * of top nodes staged in shared memory by the traversal kernels (0 = none;
+ * width 8 ignores it).  Width-8 trees are traversed as compressed 96-byte
+ * nodes (per-node grid, 8-bit child boxes, children in octant order). */
 enum { PT_BVH_FAST_BUILD = 1 };
 enum { PT_BVH_BUILDER_RADIX = 0, PT_BVH_BUILDER_PLOC = 1 };
 typedef struct pt_bvh_opts {
@@ -269,7 +271,7 @@ typedef struct pt_bvh_stats {
     uint32_t max_depth;
     float sah_cost;        /* SAH cost of the wide tree (node cost 1.2, primitive cost 1) */
     float build_ms;        /* device time of the last build or refit */
-    uint64_t node_bytes;
+    uint64_t node_bytes;   /* bytes of the nodes the traversal reads (32 * width; 96 per node for width 8) */
     uint64_t prim_bytes;
     uint32_t builder;      /* PT_BVH_BUILDER_*: how the binary tree was built */
 } pt_bvh_stats;
