@@ -51,6 +51,30 @@ enum { E0A, E0B, E1A, E1B, E2A, E2B, E3A, E3B, BOT, D3, D2, D1, D0, OUT };
 constexpr int kOutChannels = 3;
 
 __device__ __forceinline__ float bf2f(uint16_t h) { return __uint_as_float(static_cast<uint32_t>(h) << 16); }
+
+// 16 BF16 channels = 32 bytes = one sector, moved with one 256-bit access
+// (sm_100 and later; every tensor here has channel counts and offsets that
+// are multiples of 16 on 256-byte-aligned buffers).
+struct C16 {
+    uint32_t w[8];
+    __device__ __forceinline__ uint16_t operator[](int k) const { return (w[k >> 1] >> (16 * (k & 1))) & 0xffffu; }
+    __device__ __forceinline__ void set(int k, uint16_t h) {
+        w[k >> 1] = (w[k >> 1] & (0xffff0000u >> (16 * (k & 1)))) | (static_cast<uint32_t>(h) << (16 * (k & 1)));
+    }
+};
+__device__ __forceinline__ C16 ld_c16(const uint16_t *p) {
+    C16 v;
+    asm volatile("ld.global.v8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                 : "=r"(v.w[0]), "=r"(v.w[1]), "=r"(v.w[2]), "=r"(v.w[3]), "=r"(v.w[4]), "=r"(v.w[5]), "=r"(v.w[6]),
+                   "=r"(v.w[7])
+                 : "l"(p));
+    return v;
+}
+__device__ __forceinline__ void st_c16(uint16_t *p, const C16 &v) {
+    asm volatile("st.global.v8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(p), "r"(v.w[0]), "r"(v.w[1]),
+                 "r"(v.w[2]), "r"(v.w[3]), "r"(v.w[4]), "r"(v.w[5]), "r"(v.w[6]), "r"(v.w[7])
+                 : "memory");
+}
 __device__ __forceinline__ uint16_t f2bf(float f) {
     __nv_bfloat16 h = __float2bfloat16_rn(f);
     return *reinterpret_cast<uint16_t *>(&h);
@@ -166,7 +190,7 @@ __global__ void k_upcat(const uint16_t *lo, int c, int n, int h, int w, uint16_t
 // g_lo[n, y, x, c] = (lo > 0) * sum over the 2x2 children of g_cat[.., 0:c]
 __global__ void k_up_back(const uint16_t *gcat, int cat_ctot, const uint16_t *lo, int c, int n, int h2, int w2,
                           uint16_t *glo) {
-    const int groups = c / 8;
+    const int groups = c / 16;
     const long long total = (long long)n * h2 * w2 * groups;
     const int w = 2 * w2;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
@@ -175,21 +199,21 @@ __global__ void k_up_back(const uint16_t *gcat, int cat_ctot, const uint16_t *lo
         const int x = static_cast<int>(p % w2);
         const int y = static_cast<int>((p / w2) % h2);
         const int b = static_cast<int>(p / ((long long)w2 * h2));
-        float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        float acc[16];
+#pragma unroll
+        for (int k = 0; k < 16; k++) acc[k] = 0.f;
         for (int dy = 0; dy < 2; dy++)
             for (int dx = 0; dx < 2; dx++) {
                 const long long q = ((long long)b * 2 * h2 + 2 * y + dy) * w + 2 * x + dx;
-                uint4 v = *reinterpret_cast<const uint4 *>(gcat + q * cat_ctot + gq * 8);
-                const uint16_t *hv = reinterpret_cast<const uint16_t *>(&v);
+                const C16 v = ld_c16(gcat + q * cat_ctot + gq * 16);
 #pragma unroll
-                for (int k = 0; k < 8; k++) acc[k] += bf2f(hv[k]);
+                for (int k = 0; k < 16; k++) acc[k] += bf2f(v[k]);
             }
-        uint4 m = *reinterpret_cast<const uint4 *>(lo + p * c + gq * 8);
-        const uint16_t *hm = reinterpret_cast<const uint16_t *>(&m);
-        uint16_t o[8];
+        const C16 m = ld_c16(lo + p * c + gq * 16);
+        C16 o{};
 #pragma unroll
-        for (int k = 0; k < 8; k++) o[k] = pos(hm[k]) ? f2bf(acc[k]) : 0;
-        *reinterpret_cast<uint4 *>(glo + p * c + gq * 8) = *reinterpret_cast<uint4 *>(o);
+        for (int k = 0; k < 16; k++) o.set(k, pos(m[k]) ? f2bf(acc[k]) : 0);
+        st_c16(glo + p * c + gq * 16, o);
     }
 }
 
@@ -198,7 +222,7 @@ __global__ void k_up_back(const uint16_t *gcat, int cat_ctot, const uint16_t *lo
 //   g[n, y, x, k] = (y > 0) * (g_cat[.., coff + k] + 0.25 * g_pool[n, y/2, x/2, k])
 __global__ void k_skip_back(const uint16_t *cat, const uint16_t *gcat, int cat_ctot, int coff, const uint16_t *gpool,
                             int c, int n, int h, int w, uint16_t *g) {
-    const int groups = c / 8;
+    const int groups = c / 16;
     const long long total = (long long)n * h * w * groups;
     const int h2 = h / 2, w2 = w / 2;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
@@ -208,15 +232,13 @@ __global__ void k_skip_back(const uint16_t *cat, const uint16_t *gcat, int cat_c
         const int y = static_cast<int>((p / w) % h);
         const int b = static_cast<int>(p / ((long long)w * h));
         const long long q = ((long long)b * h2 + y / 2) * w2 + x / 2;
-        uint4 yv = *reinterpret_cast<const uint4 *>(cat + p * cat_ctot + coff + gq * 8);
-        uint4 gv = *reinterpret_cast<const uint4 *>(gcat + p * cat_ctot + coff + gq * 8);
-        uint4 pv = *reinterpret_cast<const uint4 *>(gpool + q * c + gq * 8);
-        const uint16_t *hy = reinterpret_cast<const uint16_t *>(&yv), *hg = reinterpret_cast<const uint16_t *>(&gv),
-                       *hp = reinterpret_cast<const uint16_t *>(&pv);
-        uint16_t o[8];
+        const C16 yv = ld_c16(cat + p * cat_ctot + coff + gq * 16);
+        const C16 gv = ld_c16(gcat + p * cat_ctot + coff + gq * 16);
+        const C16 pv = ld_c16(gpool + q * c + gq * 16);
+        C16 o{};
 #pragma unroll
-        for (int k = 0; k < 8; k++) o[k] = pos(hy[k]) ? f2bf(bf2f(hg[k]) + 0.25f * bf2f(hp[k])) : 0;
-        *reinterpret_cast<uint4 *>(g + p * c + gq * 8) = *reinterpret_cast<uint4 *>(o);
+        for (int k = 0; k < 16; k++) o.set(k, pos(yv[k]) ? f2bf(__fmaf_rn(0.25f, bf2f(pv[k]), bf2f(gv[k]))) : 0);
+        st_c16(g + p * c + gq * 16, o);
     }
 }
 
@@ -657,14 +679,14 @@ int run_backward(pt_denoiser *dn, Plan &P, const float *target, cudaStream_t s) 
     };
     auto up_back = [&](const DevBuf &gcat, int cat_ctot, const DevBuf &lo, int c, int lvl, DevBuf &glo) {
         const int h2 = h >> (lvl + 1), w2 = w >> (lvl + 1);
-        const long long tot = (long long)n * h2 * w2 * (c / 8);
+        const long long tot = (long long)n * h2 * w2 * (c / 16);
         k_up_back<<<grid_for(tot), 256, 0, s>>>(gcat.as<uint16_t>(), cat_ctot, lo.as<uint16_t>(), c, n, h2, w2,
                                                  glo.as<uint16_t>());
     };
     auto skip_back = [&](const DevBuf &cat, const DevBuf &gcat, int cat_ctot, int coff, const DevBuf &gpool, int c,
                          int lvl, DevBuf &g) {
         const int hh = h >> lvl, ww = w >> lvl;
-        const long long tot = (long long)n * hh * ww * (c / 8);
+        const long long tot = (long long)n * hh * ww * (c / 16);
         k_skip_back<<<grid_for(tot), 256, 0, s>>>(cat.as<uint16_t>(), gcat.as<uint16_t>(), cat_ctot, coff,
                                                    gpool.as<uint16_t>(), c, n, hh, ww, g.as<uint16_t>());
     };
