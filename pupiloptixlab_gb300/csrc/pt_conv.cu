@@ -487,6 +487,11 @@ __global__ void __launch_bounds__(192, 1)
                         break;
                     }
                     const uint32_t sa = base + s * a.stage_bytes, sb = sa + a_bytes;
+                    if ((sa | sb) & 1023u) {  // never with a layout fwd_prepare accepted: give up, bounded
+                        record_error(a.err, 8u);
+                        *fail = 1;
+                        break;
+                    }
                     mbar_expect_tx(full(s), tx_bytes);
                     if (HALO) {
                         if (a.halo_sw32) {
@@ -1024,6 +1029,13 @@ int fwd_prepare(FwdOp *op, const Act &in, const void *w, int w_rows, int cout, c
     const int target_ctas = std::min(512 / a.tmem_cols, max_ctas);
     const int budget = (225 * 1024) / target_ctas - 2048 - a.wres_bytes;
     a.stages = std::max(2, std::min(kMaxStages, budget / a.stage_bytes));
+    // every TMA destination (stage, A box or plane, weight tap region) on a
+    // 1 KiB boundary of the 1 KiB-aligned ring; the producer checks it again
+    if (a.stage_bytes % 1024 || a.wres_bytes % 1024 ||
+        (halo && (a.halo_a_bytes % 1024 || a.halo_plane_bytes % 1024 || halo_b_tap_bytes(n_tile) % 1024))) {
+        pt_set_error("conv forward: shared-memory layout off 1 KiB boundaries");
+        return PT_ERR_INVALID;
+    }
     if (halo) {
         a.tile_w = 128;
         a.tile_rows = halo_rows;
