@@ -38,10 +38,12 @@ SHAPES = [
     (1, 16, 32, 80, 384),     # N tiled (2 x 192)
     (3, 4, 4, 48, 16),        # tiny images
     (2, 7, 130, 16, 32),      # two-row halo tiles, odd height (the last tile's second row is outside)
+    (1, 6, 128, 32, 112),     # two-row halo tiles with 448 of the 512 TMEM columns (one CTA per SM)
 ]
 
 
-@pytest.mark.parametrize("shape", [(2, 7, 130, 16, 32), (1, 9, 256, 32, 64), (2, 6, 128, 48, 48)])
+@pytest.mark.parametrize("shape", [(2, 7, 130, 16, 32), (1, 9, 256, 32, 64), (2, 6, 128, 48, 48),
+                                   (1, 4, 256, 16, 80)])
 def test_conv_forward_halo_rows_agree(cuda_ctx, shape, monkeypatch):
     """Halo tiles of one to four output rows issue the same MMAs per output
     row in the same order: the FP32 results are identical."""
