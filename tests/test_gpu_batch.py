@@ -17,12 +17,13 @@ def _scenes():
             scenes.cornell_box(16, 16, max_depth=5)]
 
 
-@pytest.mark.parametrize("flags", [0, "nosort", "nograph"])
-def test_batch_equals_serial_renders(cuda_ctx, flags):
+@pytest.mark.parametrize("flags,width", [(0, 4), ("nosort", 4), ("nograph", 4), (0, 8)])
+def test_batch_equals_serial_renders(cuda_ctx, flags, width):
+    """Width 8: the merged BVH is compressed after rebasing, as each scene's own."""
     from pupiloptixlab_gb300 import abi
     from pupiloptixlab_gb300.api import GpuScene, render_batch, render_batch_stats
     fl = {0: 0, "nosort": abi.RENDER_NO_MATERIAL_SORT, "nograph": abi.RENDER_NO_GRAPH}[flags]
-    gs = [GpuScene(cuda_ctx, sc) for sc in _scenes()]
+    gs = [GpuScene(cuda_ctx, sc, bvh_width=width) for sc in _scenes()]
     serial = [g.render(spp=3, seed=11, max_depth=5, flags=fl) for g in gs]
     batched = render_batch(cuda_ctx, gs, spp=3, seed=11, max_depth=5, flags=fl)
     torch.cuda.synchronize()

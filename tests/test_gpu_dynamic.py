@@ -26,10 +26,11 @@ def all_positions(sc):
     return np.concatenate([m.positions for m in sc.meshes]).astype(np.float32)
 
 
-@pytest.mark.parametrize("on_device", [True, False])
-def test_update_refit_rebuild_match_brute_force(cuda_ctx, on_device):
+@pytest.mark.parametrize("on_device,width", [(True, 4), (False, 4), (True, 8)])
+def test_update_refit_rebuild_match_brute_force(cuda_ctx, on_device, width):
+    """Width 8: the refit recompresses the 8-wide nodes the traversal reads."""
     sc = scenes.icosphere_field(64, 36, num_instances=10, subdivisions=3)
-    g = GpuScene(cuda_ctx, sc)
+    g = GpuScene(cuda_ctx, sc, bvh_width=width)
     sah0 = g.bvh_stats().sah_cost
     moved = jittered(sc, 0.02, 5)
     pos = all_positions(moved)
@@ -41,7 +42,7 @@ def test_update_refit_rebuild_match_brute_force(cuda_ctx, on_device):
     got = g.trace(torch.from_numpy(rays).cuda()).cpu().numpy()
     assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
     assert refit.sah_cost > 0 and refit.build_ms > 0
-    rebuilt = g.build_bvh()
+    rebuilt = g.build_bvh(width=width)
     got2 = g.trace(torch.from_numpy(rays).cuda()).cpu().numpy()
     assert np.array_equal(got2.view(np.uint32), ref.view(np.uint32))
     # refitting a small jitter keeps the tree close to a rebuild
