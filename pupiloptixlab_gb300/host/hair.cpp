@@ -62,6 +62,33 @@ bool LoadCyHair(const std::string &path, float radius, bool tapered, uint32_t mo
         error = "unknown spline mode";
         return false;
     }
+    // every array the flags announce must fit in the file before anything is
+    // allocated for it, so that a corrupt count cannot ask for gigabytes
+    in.seekg(0, std::ios::end);
+    const uint64_t file_bytes = static_cast<uint64_t>(in.tellg());
+    in.seekg(128, std::ios::beg);
+    const uint64_t body = file_bytes > 128 ? file_bytes - 128 : 0;
+    const uint64_t seg_bytes = (flags & 1u) ? 2ull * strands : 0;
+    if (seg_bytes > body) {
+        error = path + ": truncated segment array";
+        return false;
+    }
+    if (!(flags & 2u)) {
+        error = path + ": HAIR file has no points";
+        return false;
+    }
+    if (12ull * points > body - seg_bytes) {
+        error = path + ": truncated point array";
+        return false;
+    }
+    if ((flags & 4u) && 4ull * points > body - seg_bytes - 12ull * points) {
+        error = path + ": truncated thickness array";
+        return false;
+    }
+    if (strands > points) {  // every strand holds at least one point
+        error = path + ": strands need more points than the file holds";
+        return false;
+    }
     std::vector<uint32_t> segs(strands, def_segments);
     if (flags & 1u) {
         std::vector<unsigned char> raw(2ull * strands);
@@ -70,10 +97,6 @@ bool LoadCyHair(const std::string &path, float radius, bool tapered, uint32_t mo
             return false;
         }
         for (uint32_t i = 0; i < strands; i++) segs[i] = (uint32_t)raw[2 * i] | ((uint32_t)raw[2 * i + 1] << 8);
-    }
-    if (!(flags & 2u)) {
-        error = path + ": HAIR file has no points";
-        return false;
     }
     // strand i holds points [first[i], first[i + 1])
     std::vector<uint64_t> first(strands + 1, 0);

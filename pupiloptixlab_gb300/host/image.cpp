@@ -11,6 +11,7 @@
 #include <cstring>
 #include <fstream>
 #include <sstream>
+#include <stdexcept>
 
 namespace Pupil::util {
 
@@ -45,6 +46,17 @@ void rgbe(const uint8_t *p, float *out) {
     out[2] = p[2] * f;
 }
 
+// Image sizes a reader accepts before it allocates: at most 65,536 pixels on
+// a side and 2^28 pixels (4 GiB of RGBA floats), so that a corrupt or hostile
+// header cannot ask for more.
+bool size_ok(uint64_t w, uint64_t h, std::string &error) {
+    if (w == 0 || h == 0 || w > 65536 || h > 65536 || w * h > (1ull << 28)) {
+        error = "image size " + std::to_string(w) + " x " + std::to_string(h) + " out of range";
+        return false;
+    }
+    return true;
+}
+
 bool load_hdr(const std::vector<uint8_t> &d, std::vector<float> &rgba, uint32_t &w, uint32_t &h, std::string &error) {
     size_t pos = 0;
     auto line = [&](std::string &s) {
@@ -74,6 +86,7 @@ bool load_hdr(const std::vector<uint8_t> &d, std::vector<float> &rgba, uint32_t 
         error = "HDR file: only the '-Y h +X w' orientation is supported";
         return false;
     }
+    if (!size_ok((uint64_t)ww, (uint64_t)hh, error)) return false;
     w = static_cast<uint32_t>(ww);
     h = static_cast<uint32_t>(hh);
     rgba.assign(4ull * w * h, 1.f);
@@ -145,6 +158,7 @@ bool load_pfm(const std::vector<uint8_t> &d, std::vector<float> &rgba, uint32_t 
         error = "PFM header invalid";
         return false;
     }
+    if (!size_ok((uint64_t)ww, (uint64_t)hh, error)) return false;
     w = static_cast<uint32_t>(ww);
     h = static_cast<uint32_t>(hh);
     const size_t n = (size_t)w * h * channels;
@@ -289,10 +303,11 @@ bool decode_png(const std::vector<uint8_t> &d, std::vector<uint8_t> &img, uint32
     const bool depth_ok = ctype == 0   ? (depth == 1 || depth == 2 || depth == 4 || depth == 8 || depth == 16)
                           : ctype == 3 ? (depth == 1 || depth == 2 || depth == 4 || depth == 8)
                                        : (depth == 8 || depth == 16);
-    if (!chans || !depth_ok || w == 0 || h == 0 || (uint64_t)w * h > (1ull << 28)) {
-        error = "PNG: unsupported colour type, bit depth or size";
+    if (!chans || !depth_ok) {
+        error = "PNG: unsupported colour type or bit depth";
         return false;
     }
+    if (!size_ok(w, h, error)) return false;
     if (ctype == 3 && (plte.empty() || plte.size() % 3)) {
         error = "PNG: palette missing";
         return false;
@@ -483,13 +498,17 @@ bool load_exr(const std::vector<uint8_t> &d, std::vector<float> &rgba, uint32_t 
             while (p < end && d[p]) {
                 Chan c;
                 cstr(c.name);
+                if (p + 16 > end) {
+                    error = "OpenEXR channel list truncated";
+                    return false;
+                }
                 c.type = get_u32(d, p);
                 p += 16;  // type, pLinear + 3 reserved, xSampling, ySampling
                 chans.push_back(c);
             }
-        } else if (name == "compression") {
+        } else if (name == "compression" && size >= 1) {
             compression = d[p];
-        } else if (name == "dataWindow") {
+        } else if (name == "dataWindow" && size >= 16) {
             xmin = static_cast<int32_t>(get_u32(d, p));
             ymin = static_cast<int32_t>(get_u32(d, p + 4));
             xmax = static_cast<int32_t>(get_u32(d, p + 8));
@@ -507,8 +526,9 @@ bool load_exr(const std::vector<uint8_t> &d, std::vector<float> &rgba, uint32_t 
         error = "OpenEXR data window empty";
         return false;
     }
-    w = static_cast<uint32_t>(xmax - xmin + 1);
-    h = static_cast<uint32_t>(ymax - ymin + 1);
+    if (!size_ok((uint64_t)((int64_t)xmax - xmin + 1), (uint64_t)((int64_t)ymax - ymin + 1), error)) return false;
+    w = static_cast<uint32_t>((int64_t)xmax - xmin + 1);
+    h = static_cast<uint32_t>((int64_t)ymax - ymin + 1);
     size_t line_bytes = 0;
     for (auto &c : chans) {
         if (c.type != 1 && c.type != 2) {
@@ -517,8 +537,6 @@ bool load_exr(const std::vector<uint8_t> &d, std::vector<float> &rgba, uint32_t 
         }
         line_bytes += (c.type == 1 ? 2 : 4) * (size_t)w;
     }
-    rgba.assign(4ull * w * h, 0.f);
-    for (size_t i = 0; i < (size_t)w * h; i++) rgba[4 * i + 3] = 1.f;
     const size_t table = p;
     const uint32_t lines_per_block = compression == 3 ? 16u : 1u;
     const size_t nblocks = (h + lines_per_block - 1) / lines_per_block;
@@ -526,6 +544,8 @@ bool load_exr(const std::vector<uint8_t> &d, std::vector<float> &rgba, uint32_t 
         error = "OpenEXR offset table truncated";
         return false;
     }
+    rgba.assign(4ull * w * h, 0.f);
+    for (size_t i = 0; i < (size_t)w * h; i++) rgba[4 * i + 3] = 1.f;
     std::vector<uint8_t> tmp, unpacked;
     for (size_t blk = 0; blk < nblocks; blk++) {
         const uint64_t off = get_u64(d, table + 8ull * blk);
@@ -533,9 +553,9 @@ bool load_exr(const std::vector<uint8_t> &d, std::vector<float> &rgba, uint32_t 
             error = "OpenEXR block out of range";
             return false;
         }
-        const int32_t y0 = static_cast<int32_t>(get_u32(d, off)) - ymin;
+        const int64_t y0 = (int64_t)static_cast<int32_t>(get_u32(d, off)) - ymin;
         const uint32_t packed = get_u32(d, off + 4);
-        if (y0 < 0 || y0 >= static_cast<int32_t>(h) || y0 % (int32_t)lines_per_block || off + 8 + packed > d.size()) {
+        if (y0 < 0 || y0 >= (int64_t)h || y0 % (int64_t)lines_per_block || off + 8 + packed > d.size()) {
             error = "OpenEXR block malformed";
             return false;
         }
@@ -661,14 +681,23 @@ bool LoadImageRGBA(const std::string &path, std::vector<float> &rgba, uint32_t &
                 "ZIP) images can be read";
         return false;
     }
-    std::vector<uint8_t> data;
-    if (!read_all(path, data, error)) return false;
-    const bool ok = ext == "hdr"   ? load_hdr(data, rgba, width, height, error)
-                    : ext == "exr" ? load_exr(data, rgba, width, height, error)
-                    : ext == "png" ? load_png(data, rgba, width, height, error)
-                    : jpeg         ? load_jpeg(data, rgba, width, height, error)
-                                   : load_pfm(data, rgba, width, height, error);
-    if (!ok) error = "image '" + path + "': " + error;
+    bool ok = false;
+    try {  // a reader that cannot allocate reports it instead of throwing through the C interface
+        std::vector<uint8_t> data;
+        if (!read_all(path, data, error)) return false;
+        ok = ext == "hdr"   ? load_hdr(data, rgba, width, height, error)
+             : ext == "exr" ? load_exr(data, rgba, width, height, error)
+             : ext == "png" ? load_png(data, rgba, width, height, error)
+             : jpeg         ? load_jpeg(data, rgba, width, height, error)
+                            : load_pfm(data, rgba, width, height, error);
+    } catch (const std::exception &e) {
+        error = std::string("out of memory (") + e.what() + ")";
+        ok = false;
+    }
+    if (!ok) {
+        rgba.clear();
+        error = "image '" + path + "': " + error;
+    }
     return ok;
 }
 

@@ -420,6 +420,16 @@ def test_malformed_hair_files_are_reported(host, tmp_path, body, needle):
     assert needle in str(e.value)
 
 
+def test_hair_counts_beyond_the_file_are_refused_before_allocation(host, tmp_path):
+    """A HAIR header announcing billions of strands or points in a file of a
+    few bytes is refused from the file size, without allocating for it."""
+    for strands, points, flags in ((0xffffffff, 0xffffffff, 3), (0xfffffff0, 4, 2), (4, 0x40000000, 6)):
+        (tmp_path / "x.hair").write_bytes(_hair_header(strands, points, flags, default_segments=3) + bytes(64))
+        (tmp_path / "x.xml").write_text("<scene><shape type='hair'><string name='filename' value='x.hair'/></shape></scene>")
+        with pytest.raises(abi.PtError):
+            host.XmlScene(str(tmp_path / "x.xml"))
+
+
 def test_point_emitters_are_dropped_as_the_reference_does(host):
     """<emitter type="point"> is parsed by the reference (resource/scene.cpp:194-202)
     but never enters its emitter tables (world/emitter.cpp:314-315), so it
@@ -680,6 +690,33 @@ def test_png_reader(host, tmp_path, ctype, depth, interlace):
     assert np.allclose(got, expect, rtol=2e-7, atol=0), np.abs(got - expect).max()
     if c == 4:
         assert np.array_equal(got[..., 3], expect[..., 3])
+
+
+@pytest.mark.parametrize("kind", ["exr_window", "hdr", "pfm", "png"])
+def test_image_sizes_beyond_the_limit_are_refused(host, tmp_path, kind):
+    """Headers asking for more than 65,536 pixels on a side (or 2^28 pixels)
+    are refused before anything is allocated for them."""
+    import struct
+    import zlib
+    if kind == "exr_window":
+        good = _exr_bytes(np.zeros((2, 3, 4), np.float32), 1, True)
+        i = good.index(b"dataWindow\0box2i\0") + len(b"dataWindow\0box2i\0") + 4
+        data = good[:i] + struct.pack("<iiii", -2000000000, 0, 2000000000, 1) + good[i + 16:]
+        name = "t.exr"
+    elif kind == "hdr":
+        data, name = b"#?RADIANCE\nFORMAT=32-bit_rle_rgbe\n\n-Y 100000 +X 100000\n" + bytes(64), "t.hdr"
+    elif kind == "pfm":
+        data, name = b"PF\n300000 300000\n-1.0\n" + bytes(64), "t.pfm"
+    else:
+        ihdr = struct.pack(">IIBBBBB", 1 << 20, 1 << 20, 8, 2, 0, 0, 0)
+        chunk = lambda t, b: struct.pack(">I", len(b)) + t + b + struct.pack(">I", zlib.crc32(t + b) & 0xffffffff)
+        data = b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", ihdr) + chunk(b"IDAT", zlib.compress(b"\0" * 16)) + chunk(b"IEND", b"")
+        name = "t.png"
+    path = tmp_path / name
+    path.write_bytes(data)
+    with pytest.raises(abi.PtError) as e:
+        _load_env(host, path)
+    assert "out of range" in str(e.value)
 
 
 def _exr_bytes(img, compression, half):
