@@ -577,20 +577,31 @@ __global__ void k_bin_scan(uint32_t *counters) {
     }
 }
 
+// Each block reserves one range per bin with a single global atomic: the
+// warps first count their entries per bin in shared memory (one shared
+// atomic per warp and key), then the block adds its counts to the cursors.
 __global__ void k_bin_scatter(State st, const uint8_t *keys, uint32_t *q_sorted) {
+    __shared__ uint32_t cnt[kNumBins], start[kNumBins];
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const uint32_t n = st.counters[kNIn];
-    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
-        uint32_t i = base + threadIdx.x;
-        bool valid = i < n;
-        uint32_t key = valid ? keys[i] : 0xffu;
-        unsigned peers = __match_any_sync(FULL, key);
-        int leader = __ffs(peers) - 1;
+    for (uint32_t blk = blockIdx.x * blockDim.x; blk < n; blk += gridDim.x * blockDim.x) {  // uniform per block
+        if (threadIdx.x < kNumBins) cnt[threadIdx.x] = 0;
+        __syncthreads();
+        const uint32_t i = blk + threadIdx.x;
+        const bool valid = i < n;
+        const uint32_t key = valid ? keys[i] : 0xffu;
+        const unsigned peers = __match_any_sync(FULL, key);
+        const int leader = __ffs(peers) - 1;
         uint32_t pos = 0;
-        if (valid && lane == leader) pos = atomicAdd(st.counters + kBinCursor + key, (uint32_t)__popc(peers));
+        if (valid && lane == leader) pos = atomicAdd(&cnt[key], (uint32_t)__popc(peers));
         pos = __shfl_sync(FULL, pos, leader);
-        if (valid) q_sorted[pos + __popc(peers & ((1u << lane) - 1u))] = st.q_in[i];
+        __syncthreads();
+        if (threadIdx.x < kNumBins && cnt[threadIdx.x])
+            start[threadIdx.x] = atomicAdd(st.counters + kBinCursor + threadIdx.x, cnt[threadIdx.x]);
+        __syncthreads();
+        if (valid) q_sorted[start[key] + pos + __popc(peers & ((1u << lane) - 1u))] = st.q_in[i];
+        __syncthreads();  // the counts are reset for the next stretch
     }
 }
 
