@@ -655,21 +655,32 @@ __global__ void __launch_bounds__(1024) k_bin_scan_batch(Batch bt) {
     }
 }
 
+// As k_bin_scatter, with the scene-and-material bins (counts and starts in
+// 2 x nbins words of dynamic shared memory).
 __global__ void k_bin_scatter_batch(Batch bt, State st, const uint16_t *keys, uint32_t *q_sorted) {
+    extern __shared__ uint32_t sbins[];
+    uint32_t *cnt = sbins, *start = sbins + bt.nbins;
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const uint32_t n = st.counters[kNIn];
     uint32_t *cursor = bt.bins + bt.nbins;
-    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
-        const uint32_t i = base + threadIdx.x;
+    for (uint32_t blk = blockIdx.x * blockDim.x; blk < n; blk += gridDim.x * blockDim.x) {  // uniform per block
+        for (uint32_t k = threadIdx.x; k < bt.nbins; k += blockDim.x) cnt[k] = 0;
+        __syncthreads();
+        const uint32_t i = blk + threadIdx.x;
         const bool valid = i < n;
         const uint32_t key = valid ? keys[i] : 0xffffffffu;
         const unsigned peers = __match_any_sync(FULL, key);
         const int leader = __ffs(peers) - 1;
         uint32_t pos = 0;
-        if (valid && lane == leader) pos = atomicAdd(cursor + key, (uint32_t)__popc(peers));
+        if (valid && lane == leader) pos = atomicAdd(&cnt[key], (uint32_t)__popc(peers));
         pos = __shfl_sync(FULL, pos, leader);
-        if (valid) q_sorted[pos + __popc(peers & ((1u << lane) - 1u))] = st.q_in[i];
+        __syncthreads();
+        for (uint32_t k = threadIdx.x; k < bt.nbins; k += blockDim.x)
+            if (cnt[k]) start[k] = atomicAdd(cursor + k, cnt[k]);
+        __syncthreads();
+        if (valid) q_sorted[start[key] + pos + __popc(peers & ((1u << lane) - 1u))] = st.q_in[i];
+        __syncthreads();  // the counts are reset for the next stretch
     }
 }
 
@@ -939,7 +950,7 @@ struct Launcher {
                 if (sort && BATCH) {
                     k_bin_count_batch<<<grid_bin, 256, bt.nbins * 4, ls>>>(bt, npix, stt, ws.mat_key.as<uint16_t>());
                     k_bin_scan_batch<<<1, 1024, 0, ls>>>(bt);
-                    k_bin_scatter_batch<<<grid_bin, 256, 0, ls>>>(bt, stt, ws.mat_key.as<uint16_t>(),
+                    k_bin_scatter_batch<<<grid_bin, 256, 2 * bt.nbins * 4, ls>>>(bt, stt, ws.mat_key.as<uint16_t>(),
                                                                   ws.sort_tmp.as<uint32_t>());
                     shade_st.q_in = ws.sort_tmp.as<uint32_t>();
                     launches += 3;
