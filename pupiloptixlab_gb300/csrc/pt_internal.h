@@ -71,6 +71,7 @@ struct EmitterSource {
 struct RenderWorkspace {
     size_t capacity = 0;  // path slots
     DevBuf ray_o, ray_d, hit, thr, rad, rng, meta, q0, q1, sh_o, sh_d, sh_c, mat_key, counters, sort_tmp;
+    DevBuf bin_blocks;  // material binning: each block's count, then start, per bin
     size_t sort_capacity = 0;
     // CUDA-graph replay: an internal stream (the caller's may be the legacy
     // default stream, which cannot be captured), events that order it after

@@ -550,13 +550,27 @@ PT_DI uint32_t material_bin(const DevScene &s, int prim) {
     return prim >= 0 ? (s.mats[s.inst[s.prim_inst[prim]].material].type & (kNumBins - 1)) : 0u;
 }
 
+// Material binning is a stable counting sort over the bins: block b takes
+// the contiguous stretch [b * chunk, (b + 1) * chunk) of the queue, so that
+// each bin keeps the queue's order (neighbouring path slots, i.e.
+// neighbouring pixels, stay neighbours inside a bin).  k_bin_count writes
+// every block's per-bin counts, k_bin_scan turns them into each block's first
+// position in every bin, k_bin_scatter places the entries.
+__device__ __forceinline__ void bin_stretch(uint32_t n, uint32_t &lo, uint32_t &hi) {
+    const uint32_t per = (n + gridDim.x - 1) / gridDim.x;
+    const uint32_t chunk = (per + blockDim.x - 1) / blockDim.x * blockDim.x;
+    lo = min(n, blockIdx.x * chunk);
+    hi = min(n, lo + chunk);
+}
+
 template <bool BATCH>
-__global__ void k_bin_count(DevScene s, Batch bt, uint32_t npix, State st, uint8_t *keys) {
+__global__ void k_bin_count(DevScene s, Batch bt, uint32_t npix, State st, uint8_t *keys, uint32_t *block_bins) {
     __shared__ uint32_t h[kNumBins];
     if (threadIdx.x < kNumBins) h[threadIdx.x] = 0;
     __syncthreads();
-    const uint32_t n = st.counters[kNIn];
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    uint32_t lo, hi;
+    bin_stretch(st.counters[kNIn], lo, hi);
+    for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
         uint32_t slot = st.q_in[i];
         int prim = __float_as_int(st.hit[slot].y);
         const uint32_t key = BATCH ? material_bin(bt.scenes[batch_scene(bt, slot % npix)], prim) : material_bin(s, prim);
@@ -564,44 +578,71 @@ __global__ void k_bin_count(DevScene s, Batch bt, uint32_t npix, State st, uint8
         atomicAdd(&h[key], 1u);
     }
     __syncthreads();
-    if (threadIdx.x < kNumBins && h[threadIdx.x]) atomicAdd(st.counters + kBinCount + threadIdx.x, h[threadIdx.x]);
+    if (threadIdx.x < kNumBins) block_bins[blockIdx.x * kNumBins + threadIdx.x] = h[threadIdx.x];
 }
 
-__global__ void k_bin_scan(uint32_t *counters) {
-    uint32_t run = 0;
-    for (int k = 0; k < kNumBins; k++) {
-        uint32_t c = counters[kBinCount + k];
-        counters[kBinCursor + k] = run;
-        counters[kBinCount + k] = 0;  // ready for the next bounce
-        run += c;
+// One warp per bin (blockDim = 32 * kNumBins): the bin's total over the
+// blocks, the bins' starts, then each block's start in the bin (in place).
+__global__ void k_bin_scan(uint32_t *block_bins, uint32_t nblocks) {
+    __shared__ uint32_t total[kNumBins];
+    const unsigned FULL = 0xffffffffu;
+    const uint32_t bin = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    uint32_t t = 0;
+    for (uint32_t b = lane; b < nblocks; b += 32) t += block_bins[b * kNumBins + bin];
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(FULL, t, o);
+    if (lane == 0) total[bin] = t;
+    __syncthreads();
+    uint32_t carry = 0;
+    for (uint32_t k = 0; k < bin; k++) carry += total[k];
+    for (uint32_t b0 = 0; b0 < nblocks; b0 += 32) {
+        const uint32_t b = b0 + lane;
+        const uint32_t v = b < nblocks ? block_bins[b * kNumBins + bin] : 0u;
+        uint32_t x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(FULL, x, o);
+            if (lane >= (uint32_t)o) x += y;
+        }
+        if (b < nblocks) block_bins[b * kNumBins + bin] = carry + x - v;
+        carry += __shfl_sync(FULL, x, 31);
     }
 }
 
-// Each block reserves one range per bin with a single global atomic: the
-// warps first count their entries per bin in shared memory (one shared
-// atomic per warp and key), then the block adds its counts to the cursors.
-__global__ void k_bin_scatter(State st, const uint8_t *keys, uint32_t *q_sorted) {
-    __shared__ uint32_t cnt[kNumBins], start[kNumBins];
+// Per stretch of blockDim entries: each warp's count per key, a prefix over
+// the warps per key, then every entry at its block's running position in
+// its bin plus its rank among the warp's entries of the same key.
+__global__ void k_bin_scatter(State st, const uint8_t *keys, const uint32_t *block_bins, uint32_t *q_sorted) {
+    constexpr int kWarps = 256 / 32;
+    __shared__ uint32_t wc[kWarps][kNumBins];
+    __shared__ uint32_t run[kNumBins];
     const unsigned FULL = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
-    const uint32_t n = st.counters[kNIn];
-    for (uint32_t blk = blockIdx.x * blockDim.x; blk < n; blk += gridDim.x * blockDim.x) {  // uniform per block
-        if (threadIdx.x < kNumBins) cnt[threadIdx.x] = 0;
-        __syncthreads();
-        const uint32_t i = blk + threadIdx.x;
-        const bool valid = i < n;
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x < kNumBins) run[threadIdx.x] = block_bins[blockIdx.x * kNumBins + threadIdx.x];
+    if (threadIdx.x < kWarps * kNumBins) wc[threadIdx.x / kNumBins][threadIdx.x % kNumBins] = 0;
+    __syncthreads();
+    uint32_t lo, hi;
+    bin_stretch(st.counters[kNIn], lo, hi);
+    for (uint32_t base = lo; base < hi; base += blockDim.x) {  // uniform per block
+        const uint32_t i = base + threadIdx.x;
+        const bool valid = i < hi;
         const uint32_t key = valid ? keys[i] : 0xffu;
         const unsigned peers = __match_any_sync(FULL, key);
-        const int leader = __ffs(peers) - 1;
-        uint32_t pos = 0;
-        if (valid && lane == leader) pos = atomicAdd(&cnt[key], (uint32_t)__popc(peers));
-        pos = __shfl_sync(FULL, pos, leader);
+        const uint32_t rank = __popc(peers & ((1u << lane) - 1u));
+        if (valid && lane == (uint32_t)(__ffs(peers) - 1)) wc[warp][key] = __popc(peers);
         __syncthreads();
-        if (threadIdx.x < kNumBins && cnt[threadIdx.x])
-            start[threadIdx.x] = atomicAdd(st.counters + kBinCursor + threadIdx.x, cnt[threadIdx.x]);
+        if (threadIdx.x < kNumBins) {
+            uint32_t r = run[threadIdx.x];
+            for (int w = 0; w < kWarps; w++) {
+                const uint32_t c = wc[w][threadIdx.x];
+                wc[w][threadIdx.x] = r;
+                r += c;
+            }
+            run[threadIdx.x] = r;
+        }
         __syncthreads();
-        if (valid) q_sorted[start[key] + pos + __popc(peers & ((1u << lane) - 1u))] = st.q_in[i];
-        __syncthreads();  // the counts are reset for the next stretch
+        if (valid) q_sorted[wc[warp][key] + rank] = st.q_in[i];
+        __syncthreads();
+        if (threadIdx.x < kWarps * kNumBins) wc[threadIdx.x / kNumBins][threadIdx.x % kNumBins] = 0;
+        __syncthreads();
     }
 }
 
@@ -896,6 +937,7 @@ struct Launcher {
         int occ_b = 0;
         PT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_b, k_bin_scatter, 256, 0));
         const uint32_t grid_bin = (uint32_t)std::max(1, occ_b) * t.num_sms;
+        if (sort && (e = ws.bin_blocks.ensure((size_t)grid_bin * kNumBins * 4)) != PT_OK) return e;
 
         // The whole render is captured into a CUDA graph on the scene's own
         // stream (ordered after and before the caller's stream by events) and
@@ -955,9 +997,11 @@ struct Launcher {
                     shade_st.q_in = ws.sort_tmp.as<uint32_t>();
                     launches += 3;
                 } else if (sort) {
-                    k_bin_count<BATCH><<<grid_bin, 256, 0, ls>>>(d, bt, npix, stt, ws.mat_key.as<uint8_t>());
-                    k_bin_scan<<<1, 1, 0, ls>>>(stt.counters);
-                    k_bin_scatter<<<grid_bin, 256, 0, ls>>>(stt, ws.mat_key.as<uint8_t>(), ws.sort_tmp.as<uint32_t>());
+                    k_bin_count<BATCH><<<grid_bin, 256, 0, ls>>>(d, bt, npix, stt, ws.mat_key.as<uint8_t>(),
+                                                                 ws.bin_blocks.as<uint32_t>());
+                    k_bin_scan<<<1, 32 * kNumBins, 0, ls>>>(ws.bin_blocks.as<uint32_t>(), grid_bin);
+                    k_bin_scatter<<<grid_bin, 256, 0, ls>>>(stt, ws.mat_key.as<uint8_t>(), ws.bin_blocks.as<uint32_t>(),
+                                                            ws.sort_tmp.as<uint32_t>());
                     shade_st.q_in = ws.sort_tmp.as<uint32_t>();
                     launches += 3;
                 }
@@ -1127,7 +1171,7 @@ void pt_batch_release(BatchWorkspace *b) {
     for (DevBuf *d : bufs) d->release();
     RenderWorkspace &w = b->ws;
     DevBuf *wb[] = {&w.ray_o, &w.ray_d, &w.hit, &w.thr, &w.rad, &w.rng, &w.meta, &w.q0,
-                    &w.q1, &w.sh_o, &w.sh_d, &w.sh_c, &w.mat_key, &w.counters, &w.sort_tmp};
+                    &w.q1, &w.sh_o, &w.sh_d, &w.sh_c, &w.mat_key, &w.counters, &w.sort_tmp, &w.bin_blocks};
     for (DevBuf *d : wb) d->release();
     if (w.exec) cudaGraphExecDestroy(w.exec);
     if (w.ev_in) cudaEventDestroy(w.ev_in);

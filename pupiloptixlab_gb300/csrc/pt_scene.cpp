@@ -822,7 +822,7 @@ pt_scene::~pt_scene() {
     DevBuf *all[] = {&prims_world, &prims_bvh, &nodes, &cnodes, &tri_vidx, &vpos, &vnrm, &vuv, &prim_inst, &inst, &mats, &curve_seg, &curve_cp,
                      &emitters, &emitter_cdf, &emitter_tex, &mesh_obj_pos, &bvh_scratch, &bvh_order, &sah_scratch, &xform_table, &all_obj_pos, &ws.ray_o, &ws.ray_d, &ws.hit, &ws.thr,
                      &ws.rad, &ws.rng, &ws.meta, &ws.q0, &ws.q1, &ws.sh_o, &ws.sh_d, &ws.sh_c, &ws.mat_key,
-                     &ws.counters, &ws.sort_tmp};
+                     &ws.counters, &ws.sort_tmp, &ws.bin_blocks};
     for (DevBuf *b : all) b->release();
     env_row_cdf.release();
     env_col_cdf.release();
