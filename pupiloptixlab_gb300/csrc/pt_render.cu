@@ -540,11 +540,8 @@ __global__ void __launch_bounds__(256, 3) k_shade(DevScene s, Batch bt, State st
 
 // Material-sorted shading (default; PT_RENDER_NO_MATERIAL_SORT turns it off): the active queue is
 // binned by the material type of each hit (0 = miss) before k_shade, so that
-// warps run one BSDF at a time.  Counting pass (block histogram in shared
-// memory, one atomic per bin and block), a one-thread scan, and a scatter pass
-// with warp-aggregated atomics (__match_any_sync groups lanes with equal keys).
+// warps run one BSDF at a time (a stable counting sort: see k_bin_count).
 constexpr int kNumBins = 8;
-enum : int { kBinCount = 24, kBinCursor = 40 };  // word offsets in the counters block
 
 PT_DI uint32_t material_bin(const DevScene &s, int prim) {
     return prim >= 0 ? (s.mats[s.inst[s.prim_inst[prim]].material].type & (kNumBins - 1)) : 0u;
