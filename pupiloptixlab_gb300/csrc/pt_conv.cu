@@ -1072,7 +1072,8 @@ int fwd_prepare(FwdOp *op, const Act &in, const void *w, int w_rows, int cout, c
     // tiles (both rows of a pixel pair are in one thread, the pair in
     // neighbouring lanes); otherwise the caller pools
     if (pool && halo && halo_rows == 2 && epi == EPI_BF16 && cout % 16 == 0 && in.w % 128 == 0 && in.h % 2 == 0 &&
-        ntiles == 1 && al32(pool, pool_ctot, pool_coff) && !getenv_flag("PT_CONV_NO_FUSED_POOL")) {
+        ntiles == 1 && al32(pool, pool_ctot, pool_coff) && al32(out, out_ctot, out_coff) &&
+        !getenv_flag("PT_CONV_NO_FUSED_POOL")) {  // (the pooled epilogue writes both outputs with 32-byte stores)
         a.pool = static_cast<uint16_t *>(pool);
         a.pool_ctot = pool_ctot;
         a.pool_coff = pool_coff;
