@@ -290,7 +290,8 @@ PT_DI int2 *stage_smem(const DevScene &s, float4 *smem) {
 }
 
 // ANY = false: closest hit of the extension rays; ANY = true: shadow rays.
-// Widths 2 and 4 are capped at 72 registers (7 blocks of 128 threads per SM).
+// Widths 2 and 4 are capped at 72 registers (7 blocks of 128 threads per SM),
+// width 8 (compressed nodes) at 96.
 template <int K, bool ANY, bool COUNT, bool BATCH = false, bool CURVES = false>
 __global__ void __maxnreg__(K == 8 ? 96 : 72) k_trace_queue(DevScene s, State st, Batch bt, uint32_t npix) {
     extern __shared__ float4 smem[];
