@@ -22,7 +22,8 @@ MIS, FP32, PCG32 streams.  One step = one full 64-spp frame (132.7 M samples).
 The default run also carries the method's other configurations, each
 measured on the same GPU after the headline (keys of the same JSON line;
 `--headline-only` skips them):
-  config0_cornell  Cornell box 256x256, 16 spp, depth 4: Msamples/s and the
+  cornell_256x256_16spp
+             Cornell box 256x256, 16 spp, depth 4: Msamples/s and the
              CPU oracle on the same frame
   batch      64 seeded scenes (10k-2M triangles, 256^2-1280x720), 16 spp,
              depth 8: one multi-scene launch per bounce vs 64 serial renders
@@ -868,7 +869,7 @@ def main():
         del buffers, flush
         torch.cuda.empty_cache()
         log = lambda m: print(m, file=sys.stderr, flush=True)  # noqa: E731
-        for key, fn in (("config0_cornell", lambda: cornell_result(args, ctx)),
+        for key, fn in (("cornell_256x256_16spp", lambda: cornell_result(args, ctx)),
                         ("batch", lambda: batch_result(args, ctx)),
                         ("dynamic", lambda: dynamic_result(args, ctx)),
                         ("denoise", lambda: denoise_result(args, ctx, log))):

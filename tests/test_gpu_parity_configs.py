@@ -10,9 +10,9 @@ equality of every pixel of the accumulated image and of the AOVs.  Each test
 prints the fraction of bit-identical pixels, the fraction within 1e-4 and the
 largest error of the rest, so that a failure says how far off it is.
 
-* configs[0] as stated: Cornell box, 256x256, 16 spp, max depth 4, seed 0, in
-  both random-stream modes (reference LCG and PCG32), full image;
-* configs[1] window, converged: the 1M-triangle icosphere field's 1080p
+* the Cornell box as the benchmark states it: 256x256, 16 spp, max depth 4,
+  seed 0, in both random-stream modes (reference LCG and PCG32), full image;
+* a window of the headline scene, converged: the 1M-triangle icosphere field's 1080p
   camera at 4,096 spp, depth 8, all seven materials; the oracle renders a
   160x90 window (every 4th pixel of it) and RMSE <= 1e-3 is required on top
   of bit equality;
@@ -43,7 +43,7 @@ def rmse(a, b):
 
 
 @pytest.mark.parametrize("rng", [abi.RNG_REF_LCG, abi.RNG_PCG32], ids=["ref_lcg", "pcg32"])
-def test_cornell_config0_as_stated(cuda_ctx, rng):
+def test_cornell_256_16spp_depth4_as_stated(cuda_ctx, rng):
     sc = scenes.cornell_box(256, 256, max_depth=4)
     o = oracle.OracleScene(sc)
     g = GpuScene(cuda_ctx, sc)
@@ -61,7 +61,7 @@ def test_cornell_config0_as_stated(cuda_ctx, rng):
     assert got["accum"][:, :3].mean() > 0.02
 
 
-def test_config1_window_converged(cuda_ctx):
+def test_icosphere_field_window_converged(cuda_ctx):
     """4,096 spp of the 1080p headline camera; a 160x90 window near the image
     centre (every 4th pixel in x and y: 40x23 pixels) rendered by the oracle
     on the same streams."""
