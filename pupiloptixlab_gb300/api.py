@@ -63,11 +63,16 @@ class GpuScene:
         except Exception:
             pass
 
-    def build_bvh(self, width: int = 4, max_leaf: int = 4, smem_nodes: int = 0, stream=None,
-                  flags: int = 0) -> abi.BvhStats:
-        """pt_bvh_build; flags = abi.BVH_FAST_BUILD builds the radix tree instead of PLOC."""
-        o = abi.BvhOpts(width, max_leaf, smem_nodes, flags)
+    def build_bvh(self, width: int | None = None, max_leaf: int | None = None, smem_nodes: int | None = None,
+                  stream=None, flags: int | None = None) -> abi.BvhStats:
+        """pt_bvh_build; flags = abi.BVH_FAST_BUILD builds the radix tree instead of PLOC.
+        An option left out keeps the value of the previous build (at the first
+        build: width 4, leaves of up to 4 primitives, no shared-memory nodes, PLOC)."""
+        prev = getattr(self, "_bvh_args", (4, 4, 0, 0))
+        args = tuple(p if v is None else v for v, p in zip((width, max_leaf, smem_nodes, flags), prev))
+        o = abi.BvhOpts(*args)
         abi.check(self.lib.pt_bvh_build(self.handle, C.byref(o), _stream_ptr(stream)), "pt_bvh_build", self.lib)
+        self._bvh_args = args
         return self.bvh_stats()
 
     def refit(self, stream=None) -> abi.BvhStats:
